@@ -1,0 +1,209 @@
+"""The circuit the engine runs: a flat list of operations with matrices already resolved.
+
+Field names and ``kind`` tags match Orrery's IR (``src/lucivant_sim/circuit.py:21-81``), so the
+engine also accepts circuits built by Orrery itself: everything below dispatches on ``op.kind``.
+:meth:`Circuit.digest` hashes the same canonical JSON as ``circuit.py:165-199`` (matrices rounded
+to 12 decimals), so a fingerprint names the same circuit in both projects.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+from dataclasses import dataclass, field
+from typing import Any, Literal
+
+import numpy as np
+
+from lucivant_sim_gb300.gates import Matrix
+
+
+@dataclass(frozen=True, eq=False)
+class Gate:
+    """A unitary on ``qubits``; the first qubit is the matrix's most significant bit."""
+
+    name: str
+    qubits: tuple[int, ...]
+    matrix: Matrix
+    params: tuple[float, ...] = ()
+    kind: Literal["gate"] = "gate"
+
+
+@dataclass(frozen=True)
+class Measure:
+    qubit: int
+    clbit: int | None  # None: the outcome is discarded
+    kind: Literal["measure"] = "measure"
+
+
+@dataclass(frozen=True)
+class Reset:
+    qubit: int
+    kind: Literal["reset"] = "reset"
+
+
+@dataclass(frozen=True)
+class Barrier:
+    qubits: tuple[int, ...]
+    kind: Literal["barrier"] = "barrier"
+
+
+@dataclass(frozen=True)
+class GlobalPhase:
+    angle: float
+    kind: Literal["gphase"] = "gphase"
+
+
+@dataclass(frozen=True)
+class Condition:
+    """Holds when classical bits ``clbits`` (least significant first) read ``value``."""
+
+    clbits: tuple[int, ...]
+    value: int
+    negate: bool = False
+
+    def holds(self, bits: list[int]) -> bool:
+        reading = 0
+        for i, c in enumerate(self.clbits):
+            reading |= bits[c] << i
+        return (reading == self.value) != self.negate
+
+
+@dataclass(frozen=True)
+class IfElse:
+    condition: Condition
+    then: tuple[Any, ...]
+    otherwise: tuple[Any, ...] = ()
+    kind: Literal["if"] = "if"
+
+
+Operation = Gate | Measure | Reset | Barrier | GlobalPhase | IfElse
+
+
+@dataclass(frozen=True)
+class Register:
+    name: str
+    offset: int
+    size: int
+
+
+_JSON_CACHE: dict[bytes, list[list[list[float]]]] = {}
+
+
+def _matrix_entries(matrix: np.ndarray) -> list[list[list[float]]]:
+    key = np.ascontiguousarray(matrix).tobytes()
+    hit = _JSON_CACHE.get(key)
+    if hit is None:
+        rounded = np.round(np.asarray(matrix, dtype=np.complex128), 12) + 0.0  # folds -0.0 into 0.0
+        hit = [[[float(v.real), float(v.imag)] for v in row] for row in rounded]
+        if len(_JSON_CACHE) < 8192:
+            _JSON_CACHE[key] = hit
+    return hit
+
+
+def _op_record(op: Any) -> object:
+    kind = op.kind
+    if kind == "gate":
+        return ["g", list(op.qubits), _matrix_entries(op.matrix)]
+    if kind == "measure":
+        return ["m", op.qubit, op.clbit]
+    if kind == "reset":
+        return ["r", op.qubit]
+    if kind == "barrier":
+        return ["b"]
+    if kind == "gphase":
+        return ["p", round(op.angle, 12)]
+    cond = op.condition
+    return [
+        "if",
+        [list(cond.clbits), cond.value, cond.negate],
+        [_op_record(o) for o in op.then],
+        [_op_record(o) for o in op.otherwise],
+    ]
+
+
+def is_dynamic(circuit: Any) -> bool:
+    """True when outcomes feed conditions, or a qubit is used after being measured or reset
+    mid-circuit (``circuit.py:121-138``): such circuits run one shot at a time."""
+    touched: set[int] = set()
+    finished: set[int] = set()
+    for op in circuit.operations:
+        kind = op.kind
+        if kind == "if":
+            return True
+        if kind == "gate":
+            if finished.intersection(op.qubits):
+                return True
+            touched.update(op.qubits)
+        elif kind == "reset":
+            if op.qubit in touched or op.qubit in finished:
+                return True
+        elif kind == "measure":
+            finished.add(op.qubit)
+    return False
+
+
+def final_measurements(circuit: Any) -> list[tuple[int, int]]:
+    """(qubit, clbit) pairs in program order of each clbit's first write; a later write to a
+    clbit replaces the qubit (``circuit.py:140-146``)."""
+    last: dict[int, int] = {}
+    for op in circuit.operations:
+        if op.kind == "measure" and op.clbit is not None:
+            last[op.clbit] = op.qubit
+    return [(q, c) for c, q in last.items()]
+
+
+def format_bits(circuit: Any, bits: int) -> str:
+    """Registers last-declared first, space separated, bit 0 of each on the right
+    (``circuit.py:202-211``)."""
+    if not circuit.cregs:
+        return format(bits, f"0{circuit.num_clbits}b") if circuit.num_clbits else ""
+    return " ".join(
+        format((bits >> reg.offset) & ((1 << reg.size) - 1), f"0{reg.size}b") for reg in reversed(circuit.cregs)
+    )
+
+
+@dataclass(frozen=True)
+class Circuit:
+    num_qubits: int
+    num_clbits: int
+    operations: tuple[Any, ...]
+    qregs: tuple[Register, ...] = ()
+    cregs: tuple[Register, ...] = ()
+    inputs: dict[str, float] = field(default_factory=dict)
+
+    def is_dynamic(self) -> bool:
+        return is_dynamic(self)
+
+    def final_measurements(self) -> list[tuple[int, int]]:
+        return final_measurements(self)
+
+    def count_ops(self) -> dict[str, int]:
+        tally: dict[str, int] = {}
+
+        def walk(ops: tuple[Any, ...]) -> None:
+            for op in ops:
+                if op.kind == "if":
+                    walk(op.then)
+                    walk(op.otherwise)
+                    continue
+                key = op.name if op.kind == "gate" else op.kind
+                tally[key] = tally.get(key, 0) + 1
+
+        walk(self.operations)
+        return dict(sorted(tally.items()))
+
+    def canonical(self) -> dict[str, object]:
+        return {
+            "qubits": self.num_qubits,
+            "clbits": self.num_clbits,
+            "cregs": [[r.name, r.offset, r.size] for r in self.cregs],
+            "ops": [_op_record(o) for o in self.operations],
+        }
+
+    def digest(self) -> str:
+        text = json.dumps(self.canonical(), separators=(",", ":"), sort_keys=True).encode()
+        return "sha256:" + hashlib.sha256(text).hexdigest()
+
+    def format_bits(self, bits: int) -> str:
+        return format_bits(self, bits)

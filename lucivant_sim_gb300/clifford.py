@@ -1,0 +1,178 @@
+"""Host-side Clifford tables for the stabilizer engine.
+
+A gate matrix is classified once into its Pauli-conjugation table (how U P U† maps each local
+Pauli), and a noise channel into Pauli branches; these small tables are what the tableau and
+frame kernels consume. The index convention — Pauli bits (x0, z0, x1, z1, ...) with the first
+qubit most significant, Y as x = z = 1 — and the refusal messages follow
+``src/lucivant_sim/stabilizer.py:48-187`` and ``:457-471``.
+"""
+
+from __future__ import annotations
+
+import itertools
+from dataclasses import dataclass
+from functools import lru_cache
+from typing import Any
+
+import numpy as np
+from numpy.typing import NDArray
+
+MAX_STABILIZER_QUBITS = 2048
+MAX_CLIFFORD_GATE_QUBITS = 3
+
+_ONE_QUBIT = {
+    (0, 0): np.eye(2, dtype=np.complex128),
+    (1, 0): np.array([[0, 1], [1, 0]], dtype=np.complex128),
+    (1, 1): np.array([[0, -1j], [1j, 0]], dtype=np.complex128),
+    (0, 1): np.array([[1, 0], [0, -1]], dtype=np.complex128),
+}
+
+
+@dataclass(frozen=True)
+class CliffordMap:
+    """``bits[i]`` is the image of Pauli i as (x0, z0, x1, z1, ...); ``sign[i]`` = 1 for a minus."""
+
+    k: int
+    bits: NDArray[np.uint8]
+    sign: NDArray[np.uint8]
+
+
+@lru_cache(maxsize=4)
+def _basis(k: int) -> tuple[NDArray[np.uint8], NDArray[np.complex128]]:
+    labels = np.array(list(itertools.product((0, 1), repeat=2 * k)), dtype=np.uint8)
+    mats = []
+    for row in labels:
+        m = np.ones((1, 1), dtype=np.complex128)
+        for q in range(k):
+            m = np.kron(m, _ONE_QUBIT[(int(row[2 * q]), int(row[2 * q + 1]))])
+        mats.append(m)
+    return labels, np.stack(mats)
+
+
+@lru_cache(maxsize=1024)
+def _map_of(raw: bytes, k: int) -> CliffordMap | None:
+    u = np.frombuffer(raw, dtype=np.complex128).reshape(1 << k, 1 << k)
+    labels, mats = _basis(k)
+    d = 1 << k
+    bits = np.zeros((len(labels), 2 * k), dtype=np.uint8)
+    sign = np.zeros(len(labels), dtype=np.uint8)
+    for i, p in enumerate(mats):
+        image = u @ p @ u.conj().T
+        # overlap with every Pauli: tr(Q† image) / d
+        overlaps = np.einsum("qji,ji->q", mats.conj(), image) / d
+        j = int(np.argmax(np.abs(overlaps)))
+        c = overlaps[j]
+        if abs(abs(c) - 1) > 1e-8 or abs(c.imag) > 1e-8:
+            return None
+        bits[i] = labels[j]
+        sign[i] = 1 if c.real < 0 else 0
+    return CliffordMap(k, bits, sign)
+
+
+_SEEN: dict[bytes, CliffordMap | None] = {}
+
+
+def clifford_map(matrix: NDArray[np.complex128]) -> CliffordMap | None:
+    """The conjugation table of a gate matrix, or None when it isn't Clifford (or too wide)."""
+    key = np.ascontiguousarray(matrix).tobytes()
+    if key in _SEEN:
+        return _SEEN[key]
+    k = matrix.shape[0].bit_length() - 1
+    found = None
+    if 0 < k <= MAX_CLIFFORD_GATE_QUBITS:
+        rounded = np.round(np.ascontiguousarray(matrix, dtype=np.complex128), 12) + 0.0
+        found = _map_of(rounded.tobytes(), k)
+    if len(_SEEN) < 4096:
+        _SEEN[key] = found
+    return found
+
+
+def _named_kinds() -> dict[tuple[int, bytes, bytes], str]:
+    r = 1 / np.sqrt(2)
+    named = {
+        "h": np.array([[r, r], [r, -r]]),
+        "s": np.diag([1, 1j]),
+        "sdg": np.diag([1, -1j]),
+        "x": np.array([[0, 1], [1, 0]]),
+        "y": np.array([[0, -1j], [1j, 0]]),
+        "z": np.diag([1, -1]),
+        "id": np.eye(2),
+        "cx": np.eye(4)[[0, 1, 3, 2]],
+        "cz": np.diag([1, 1, 1, -1]),
+    }
+    table = {}
+    for label, m in named.items():
+        k = m.shape[0].bit_length() - 1
+        cmap = _map_of((np.round(np.asarray(m, dtype=np.complex128), 12) + 0.0).tobytes(), k)
+        assert cmap is not None
+        table[(k, cmap.bits.tobytes(), cmap.sign.tobytes())] = label
+    return table
+
+
+_KINDS = _named_kinds()
+
+
+def kind_of(cmap: CliffordMap) -> str | None:
+    """The standard gate a table is (h, s, sdg, x, y, z, id, cx, cz), or None for the generic path."""
+    return _KINDS.get((cmap.k, cmap.bits.tobytes(), cmap.sign.tobytes()))
+
+
+def pauli_label(matrix: NDArray[np.complex128]) -> list[tuple[int, int]] | None:
+    """(x, z) bits per qubit of a Pauli-string matrix (first qubit first), or None."""
+    k = matrix.shape[0].bit_length() - 1
+    labels, mats = _basis(k)
+    overlaps = np.einsum("qji,ij->q", mats.conj(), matrix) / (1 << k)
+    j = int(np.argmax(np.abs(overlaps)))
+    if abs(abs(overlaps[j]) - 1) > 1e-8:
+        return None
+    return [(int(labels[j][2 * i]), int(labels[j][2 * i + 1])) for i in range(k)]
+
+
+@dataclass(frozen=True)
+class PauliNoise:
+    """Branches of a Pauli channel: cumulative probabilities (normalised) and per-branch bits."""
+
+    cumulative: NDArray[np.float64]
+    branches: tuple[tuple[tuple[int, int], ...], ...]
+
+
+@lru_cache(maxsize=256)
+def pauli_noise(channel: Any) -> PauliNoise | None:
+    if channel.mixture is None:
+        return None
+    probs, branches = [], []
+    for p, m in channel.mixture:
+        label = pauli_label(m)
+        if label is None:
+            return None
+        probs.append(p)
+        branches.append(tuple(label))
+    return PauliNoise(np.cumsum(probs) / sum(probs), tuple(branches))
+
+
+def all_gates(ops: Any) -> list[Any]:
+    found: list[Any] = []
+    for op in ops:
+        if op.kind == "gate":
+            found.append(op)
+        elif op.kind == "if":
+            found += all_gates(op.then)
+            found += all_gates(op.otherwise)
+    return found
+
+
+def clifford_problem(circuit: Any, noise: Any = None) -> str | None:
+    """Why the stabilizer engine can't run ``circuit`` exactly, or None."""
+    if circuit.num_qubits > MAX_STABILIZER_QUBITS:
+        return f"it has {circuit.num_qubits} qubits; the stabilizer engine allows up to {MAX_STABILIZER_QUBITS}"
+    for g in all_gates(circuit.operations):
+        if clifford_map(g.matrix) is None:
+            return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
+        ch = noise.gate_error(g.name, g.qubits) if noise else None
+        if ch is not None and pauli_noise(ch) is None:
+            return f"the {ch.name} noise after {g.name} isn't a Pauli channel"
+    return None
+
+
+def is_clifford(circuit: Any) -> bool:
+    return clifford_problem(circuit) is None

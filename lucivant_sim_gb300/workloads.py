@@ -1,0 +1,154 @@
+"""Seeded synthetic circuits for the five benchmark workloads.
+
+Every builder returns OpenQASM 3 text (angles written with ``repr(float)``, so parsing round-trips
+exactly) and, for the very wide Clifford workload, can also build the Circuit directly, because
+its text is tens of megabytes.
+
+* brickwork(n, layers, seed): each layer applies u3(θ, φ, λ) to every qubit, θ, φ, λ i.i.d.
+  uniform on [0, 2π) from ``default_rng(seed)`` drawn as one (layers, n, 3) array; then cx on
+  (2i, 2i+1) in even layers and (2i+1, 2i+2) in odd layers.
+* midcircuit(n, rounds, seed): each round is u3 on all qubits, brickwork cx, measure q[0..3]
+  into c, ``if (c[k] == 1) x q[k+4]``, reset q[0..3]; finally q[4..7] are measured into f.
+* clifford_layers(n, layers, seed): per qubit one of h/s/sdg/x/z uniformly, then a random
+  perfect matching (``rng.permutation``) with cx then cz on each pair (a, b).
+* hea(n, layers, seed): ry and rz layers with a linear cx chain (hardware-efficient ansatz).
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from lucivant_sim_gb300.circuit import Circuit, Gate, Measure, Register
+from lucivant_sim_gb300.gates import GATES
+from lucivant_sim_gb300.noise import NoiseModel, ReadoutError, depolarizing, thermal_relaxation
+
+TWO_PI = 2 * math.pi
+
+
+def _header(n: int) -> list[str]:
+    return ["OPENQASM 3.0;", 'include "stdgates.inc";', f"qubit[{n}] q;"]
+
+
+def brickwork(n: int, layers: int, seed: int = 7, measure: bool = True) -> str:
+    rng = np.random.default_rng(seed)
+    angles = rng.uniform(0.0, TWO_PI, size=(layers, n, 3))
+    lines = _header(n)
+    if measure:
+        lines.append(f"bit[{n}] c;")
+    for layer in range(layers):
+        for q in range(n):
+            t, p, lam = (repr(float(v)) for v in angles[layer, q])
+            lines.append(f"u3({t}, {p}, {lam}) q[{q}];")
+        for a in range(layer % 2, n - 1, 2):
+            lines.append(f"cx q[{a}], q[{a + 1}];")
+    if measure:
+        lines.append("c = measure q;")
+    return "\n".join(lines) + "\n"
+
+
+def midcircuit(n: int, rounds: int, seed: int = 7) -> str:
+    if n < 8:
+        raise ValueError("the mid-circuit workload needs at least 8 qubits")
+    rng = np.random.default_rng(seed)
+    angles = rng.uniform(0.0, TWO_PI, size=(rounds, n, 3))
+    lines = _header(n) + ["bit[4] c;", "bit[4] f;"]
+    for r in range(rounds):
+        for q in range(n):
+            t, p, lam = (repr(float(v)) for v in angles[r, q])
+            lines.append(f"u3({t}, {p}, {lam}) q[{q}];")
+        for a in range(r % 2, n - 1, 2):
+            lines.append(f"cx q[{a}], q[{a + 1}];")
+        for k in range(4):
+            lines.append(f"c[{k}] = measure q[{k}];")
+        for k in range(4):
+            lines.append(f"if (c[{k}] == 1) x q[{k + 4}];")
+        for k in range(4):
+            lines.append(f"reset q[{k}];")
+    lines.append("f = measure q[4:7];")
+    return "\n".join(lines) + "\n"
+
+
+_CLIFFORD_1Q = ("h", "s", "sdg", "x", "z")
+
+
+def _clifford_plan(n: int, layers: int, seed: int) -> list[tuple[np.ndarray, np.ndarray]]:
+    rng = np.random.default_rng(seed)
+    plan = []
+    for _ in range(layers):
+        picks = rng.integers(0, len(_CLIFFORD_1Q), size=n)
+        perm = rng.permutation(n)
+        plan.append((picks, perm))
+    return plan
+
+
+def clifford_layers(n: int, layers: int, seed: int = 11) -> str:
+    lines = _header(n) + [f"bit[{n}] c;"]
+    for picks, perm in _clifford_plan(n, layers, seed):
+        lines += [f"{_CLIFFORD_1Q[int(g)]} q[{q}];" for q, g in enumerate(picks)]
+        for i in range(0, n - 1, 2):
+            a, b = int(perm[i]), int(perm[i + 1])
+            lines.append(f"cx q[{a}], q[{b}];")
+            lines.append(f"cz q[{a}], q[{b}];")
+    lines.append("c = measure q;")
+    return "\n".join(lines) + "\n"
+
+
+def clifford_layers_circuit(n: int, layers: int, seed: int = 11) -> Circuit:
+    """The same circuit as :func:`clifford_layers` without writing and parsing its text."""
+    mats = {name: GATES[name].build() for name in (*_CLIFFORD_1Q, "cx", "cz")}
+    ops: list = []
+    for picks, perm in _clifford_plan(n, layers, seed):
+        ops += [Gate(_CLIFFORD_1Q[int(g)], (q,), mats[_CLIFFORD_1Q[int(g)]]) for q, g in enumerate(picks)]
+        for i in range(0, n - 1, 2):
+            a, b = int(perm[i]), int(perm[i + 1])
+            ops.append(Gate("cx", (a, b), mats["cx"]))
+            ops.append(Gate("cz", (a, b), mats["cz"]))
+    ops += [Measure(q, q) for q in range(n)]
+    return Circuit(n, n, tuple(ops), (Register("q", 0, n),), (Register("c", 0, n),))
+
+
+def hea(n: int, layers: int, seed: int, measure: bool = False) -> str:
+    rng = np.random.default_rng(seed)
+    angles = rng.uniform(0.0, TWO_PI, size=(layers, n, 2))
+    lines = _header(n)
+    if measure:
+        lines.append(f"bit[{n}] c;")
+    for layer in range(layers):
+        for q in range(n):
+            lines.append(f"ry({float(angles[layer, q, 0])!r}) q[{q}];")
+            lines.append(f"rz({float(angles[layer, q, 1])!r}) q[{q}];")
+        for a in range(n - 1):
+            lines.append(f"cx q[{a}], q[{a + 1}];")
+    if measure:
+        lines.append("c = measure q;")
+    return "\n".join(lines) + "\n"
+
+
+def random_pauli_sum(n: int, terms: int, seed: int) -> dict[str, float]:
+    """``terms`` random Pauli strings (qubit 0 rightmost) with N(0, 1) coefficients."""
+    rng = np.random.default_rng(seed)
+    out: dict[str, float] = {}
+    while len(out) < terms:
+        label = "".join("IXYZ"[int(v)] for v in rng.integers(0, 4, size=n))
+        out[label] = out.get(label, 0.0) + float(rng.normal())
+    return out
+
+
+def dm_noise(single: float = 1e-3, two: float = 1e-2, readout: float = 2e-2) -> NoiseModel:
+    """Uniform gate and readout noise, with thermal relaxation (T1 = 120, T2 = 90, t = 0.05)
+    on u3. By the rule-specificity order, thermal relaxation replaces the uniform one-qubit
+    error on u3 (a gate-named rule outranks a gate-agnostic one)."""
+    return NoiseModel.uniform(single=single, two=two, readout=readout).add_gate_error(
+        thermal_relaxation(t1=120, t2=90, time=0.05), gates="u3"
+    )
+
+
+def stabilizer_noise(p: float = 1e-3) -> NoiseModel:
+    """Depolarising p on every one- and two-qubit gate, readout p01 = 0.01, p10 = 0.03."""
+    model = NoiseModel()
+    model.add_gate_error(depolarizing(p, 1))
+    model.add_gate_error(depolarizing(p, 2))
+    model.add_readout_error(ReadoutError(0.01, 0.03))
+    return model
