@@ -1,0 +1,125 @@
+/*
+ * lsg.h — C ABI of the GB300 engine for Orrery's simulation hot path.
+ *
+ * Plain C types only: opaque handles, pointers and sizes. Every call returns LSG_OK (0) or a
+ * negative LSG_E* code; lsg_last_error() gives the message of the calling thread's last failure.
+ * The library never aborts and never throws across this boundary. Host buffers are owned by the
+ * caller and never retained after a call returns. Device memory belongs to the handle.
+ *
+ * Index convention (Orrery, src/lucivant_sim/engines.py:8-9): amplitudes are little-endian, bit q
+ * of an index is qubit q. A density matrix on n qubits is a register of 2n bits holding the
+ * row-major (2^n, 2^n) matrix, so qubit q is column bit q and row bit n+q
+ * (src/lucivant_sim/engines.py:222-231). A k-bit operator's index has bits[0] as its most
+ * significant bit (src/lucivant_sim/gates.py:1-7).
+ */
+#ifndef LSG_H
+#define LSG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define LSG_OK 0
+#define LSG_E_ARG (-1)       /* bad argument (maps to ValueError) */
+#define LSG_E_CAPACITY (-2)  /* too large for the engine (maps to SimulationError) */
+#define LSG_E_MEMORY (-3)    /* device allocation failed (maps to MemoryError) */
+#define LSG_E_CUDA (-4)      /* a CUDA call failed */
+#define LSG_E_TIMEOUT (-5)   /* a bounded device wait gave up; the result is not valid */
+#define LSG_E_STATE (-6)     /* the call does not fit the handle (wrong kind or size) */
+
+/* precisions */
+#define LSG_C128 0 /* complex128 amplitudes, FP64 arithmetic */
+#define LSG_C64 1  /* complex64 amplitudes, FP32 arithmetic; reductions stay FP64 */
+
+/* operator kinds for lsg_apply */
+#define LSG_OP_MATRIX 0 /* dense 2^k x 2^k complex matrix, row-major, on bits[0..k), k <= 5 */
+#define LSG_OP_DIAG 1   /* 2^k complex diagonal entries */
+#define LSG_OP_PERM 2   /* out[r] = phase[r] * in[src[r]]: 2^k complex phases, then 2^k sources (real
+                           part), k <= 5 */
+#define LSG_OP_DEPOL 3  /* (1-p) rho + (p/d) I (x) Tr_t rho on a density register: bits = k row bits then
+                           k column bits; data holds p in its real part */
+#define LSG_OP_SCALE 4  /* multiply every amplitude by one complex factor (a global phase) */
+
+#define LSG_MAX_OP_BITS 8
+
+typedef struct lsg_op {
+    int32_t kind;
+    int32_t nbits;                 /* bits the operator touches (0 for SCALE) */
+    int32_t bits[LSG_MAX_OP_BITS]; /* register bit positions, most significant first */
+    int64_t data;                  /* offset of the operator's data in the pool, in complex entries */
+    int64_t batch_stride;          /* complex entries between batch members' data; 0 = shared */
+} lsg_op;
+
+typedef struct lsg_state_s* lsg_state;
+
+/* ---- library ------------------------------------------------------------------------------ */
+const char* lsg_last_error(void);
+int lsg_version(void);
+/* Bind the calling thread's calls to a device (default 0). */
+int lsg_init(int device);
+/* Largest register a state handle accepts, in bits (26: 2^26 amplitudes). */
+int lsg_max_bits(void);
+
+/* ---- registers ------------------------------------------------------------------------------
+ * A register holds `batch` independent members of 2^nbits amplitudes each, contiguous in HBM.
+ * Replaces Statevector.__init__ / DensityMatrix.__init__ (src/lucivant_sim/engines.py:139-148,
+ * :216-225); the member count is the batching axis (shots, noise instances). */
+int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out);
+int lsg_state_free(lsg_state s);
+/* Every member set to the basis state |index>. */
+int lsg_state_set_basis(lsg_state s, int64_t index);
+/* Copy all members in / out as complex128 (converted when the register is complex64). */
+int lsg_state_upload(lsg_state s, const double* host_c128, int64_t nbytes);
+int lsg_state_download(lsg_state s, double* host_c128, int64_t nbytes);
+/* Bytes of device memory the handle holds. */
+int lsg_state_bytes(lsg_state s, int64_t* out);
+
+/* ---- gate passes ----------------------------------------------------------------------------
+ * Apply `nops` operators in order. The engine plans them into fused tile passes (each pass
+ * loads tiles of the register into shared memory once, applies every operator of the pass and
+ * writes back once). Replaces _apply_slices / _apply (src/lucivant_sim/engines.py:38-119), the
+ * density-matrix gate and channel updates (:233-255, _depolarizing_trace :122-135) and the
+ * static loop of _evolve (src/lucivant_sim/simulator.py:229-251). `pool` holds complex128 data as
+ * (re, im) pairs; complex64 registers round it once. */
+int lsg_apply(lsg_state s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries);
+
+/* ---- reductions (FP64 accumulation for both precisions) -------------------------------------
+ * Probabilities of member `member`: |a|^2 for a statevector register (dm_qubits = 0), the
+ * clipped real diagonal for a density register of dm_qubits qubits. out has 2^n doubles.
+ * Replaces Statevector.probabilities / DensityMatrix.probabilities (engines.py:207-209, :257-260). */
+int lsg_probabilities(lsg_state s, int dm_qubits, int64_t member, double* out);
+
+/* Sampling of member `member` as _sample does it (src/lucivant_sim/simulator.py:254-284):
+ * marginal over `measured` (ascending qubits, m of them), FP64 prefix sum normalised by its last
+ * entry, upper-bound search of `uniforms[0..shots)`, clamped. Then readout flips: for pair j
+ * (pair_pos[j] = position of the qubit in `measured`), if pair_has_err[j] the flip happens when
+ * flip_uniforms[e*shots + s] < (bit ? p10 : p01), e counting pairs with errors in order.
+ * bits_out is shots x npairs uint8 (row-major). near_out (may be NULL) gets, per shot, 1 when
+ * its uniform lies within 1e-12 of a CDF boundary (a shot a different summation order could flip).
+ * Returns the number of such shots in *near_count. */
+int lsg_sample(lsg_state s, int dm_qubits, int64_t member, const int32_t* measured, int32_t m,
+               const double* uniforms, int64_t shots, int32_t npairs, const int32_t* pair_pos,
+               const int32_t* pair_has_err, const double* pair_p01, const double* pair_p10,
+               const double* flip_uniforms, uint8_t* bits_out, uint8_t* near_out, int64_t* near_count);
+
+/* <P> for Pauli terms given by x/z masks (Y sets both; qubit q = bit q), for every member.
+ * out[t * batch + b]. Statevector: sum_b conj(psi[b^x]) c(b) psi[b]; density register:
+ * sum_s c(s) rho[s][s^x]. Replaces the per-term loops of expectation
+ * (src/lucivant_sim/simulator.py:505-527). */
+int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const uint64_t* zmask,
+                     int32_t nterms, double* out);
+
+/* Probability that qubit q reads 1 in member `member` (statevector registers). Replaces
+ * Statevector.probability_of_one (engines.py:185-187). */
+int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out);
+/* Zero the half of member `member` where qubit q != outcome and divide by sqrt(probability) when
+ * probability > 0 (engines.py:195-201). */
+int lsg_collapse(lsg_state s, int qubit, int outcome, double probability, int64_t member);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSG_H */

@@ -1,0 +1,258 @@
+"""ctypes binding of the engine library (``liblsg.so``, declared in ``include/lsg.h``).
+
+Status codes map back to the exception types Orrery raises: bad arguments to ``ValueError``,
+capacity misfits to :class:`SimulationError`, device allocation failures to ``MemoryError``.
+The library must be built (``python -m lucivant_sim_gb300.build``); there is no CPU fallback, so a
+missing library or GPU is an error, not a slower path.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+from typing import Any
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "liblsg.so"
+
+LSG_OK, LSG_E_ARG, LSG_E_CAPACITY, LSG_E_MEMORY, LSG_E_CUDA, LSG_E_TIMEOUT, LSG_E_STATE = 0, -1, -2, -3, -4, -5, -6
+C128, C64 = 0, 1
+OP_MATRIX, OP_DIAG, OP_PERM, OP_DEPOL, OP_SCALE = 0, 1, 2, 3, 4
+MAX_OP_BITS = 8
+
+#: numpy layout of ``lsg_op`` (56 bytes: 10 int32, 2 int64)
+OP_DTYPE = np.dtype(
+    [("kind", "<i4"), ("nbits", "<i4"), ("bits", "<i4", (MAX_OP_BITS,)), ("data", "<i8"), ("batch_stride", "<i8")],
+    align=True,
+)
+assert OP_DTYPE.itemsize == 56
+
+
+class SimulationError(RuntimeError):
+    """The circuit can't be simulated as asked (too large, or the method doesn't fit it)."""
+
+
+class EngineError(RuntimeError):
+    """The engine library or the GPU failed."""
+
+
+_P = C.c_void_p
+_I32, _I64, _D = C.c_int32, C.c_int64, C.c_double
+_PD = C.POINTER(C.c_double)
+_PI32 = C.POINTER(C.c_int32)
+_PI64 = C.POINTER(C.c_int64)
+_PU8 = C.POINTER(C.c_uint8)
+_PU64 = C.POINTER(C.c_uint64)
+
+SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
+    "lsg_last_error": (C.c_char_p, []),
+    "lsg_version": (C.c_int, []),
+    "lsg_init": (C.c_int, [C.c_int]),
+    "lsg_max_bits": (C.c_int, []),
+    "lsg_state_create": (C.c_int, [C.c_int, C.c_int, _I64, C.POINTER(_P)]),
+    "lsg_state_free": (C.c_int, [_P]),
+    "lsg_state_set_basis": (C.c_int, [_P, _I64]),
+    "lsg_state_upload": (C.c_int, [_P, _PD, _I64]),
+    "lsg_state_download": (C.c_int, [_P, _PD, _I64]),
+    "lsg_state_bytes": (C.c_int, [_P, _PI64]),
+    "lsg_apply": (C.c_int, [_P, _P, _I32, _PD, _I64]),
+    "lsg_probabilities": (C.c_int, [_P, C.c_int, _I64, _PD]),
+    "lsg_sample": (C.c_int, [_P, C.c_int, _I64, _PI32, _I32, _PD, _I64, _I32, _PI32, _PI32, _PD, _PD, _PD, _PU8, _PU8, _PI64]),
+    "lsg_expect_pauli": (C.c_int, [_P, C.c_int, _PU64, _PU64, _I32, _PD]),
+    "lsg_prob_one": (C.c_int, [_P, C.c_int, _I64, _PD]),
+    "lsg_collapse": (C.c_int, [_P, C.c_int, C.c_int, _D, _I64]),
+}
+
+_lib: C.CDLL | None = None
+_lock = threading.Lock()
+_initialised: set[int] = set()
+
+
+def library() -> C.CDLL:
+    """The loaded engine library (loaded once)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise EngineError(
+                    f"the GB300 engine library is not built ({LIB_PATH} is missing); "
+                    "run `python -m lucivant_sim_gb300.build`"
+                )
+            lib = C.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def check(code: int) -> None:
+    if code == LSG_OK:
+        return
+    msg = library().lsg_last_error().decode(errors="replace")
+    if code == LSG_E_ARG:
+        raise ValueError(msg)
+    if code == LSG_E_CAPACITY:
+        raise SimulationError(msg)
+    if code == LSG_E_MEMORY:
+        raise MemoryError(msg)
+    raise EngineError(f"engine error {code}: {msg}")
+
+
+def ensure_device(device: int = 0) -> None:
+    if device not in _initialised:
+        check(library().lsg_init(device))
+        _initialised.add(device)
+
+
+def ptr(a: np.ndarray, ctype: Any) -> Any:
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class OpList:
+    """Operators for one ``lsg_apply`` call and their complex128 data pool."""
+
+    def __init__(self) -> None:
+        self.rows: list[tuple[int, int, tuple[int, ...], int, int]] = []
+        self.chunks: list[np.ndarray] = []
+        self.size = 0
+
+    def _data(self, arr: np.ndarray) -> int:
+        flat = np.ascontiguousarray(arr, dtype=np.complex128).reshape(-1)
+        at = self.size
+        self.chunks.append(flat)
+        self.size += flat.size
+        return at
+
+    def add(self, kind: int, bits: tuple[int, ...] | list[int], data: np.ndarray, batch_stride: int = 0) -> None:
+        self.rows.append((kind, len(bits), tuple(int(b) for b in bits), self._data(data), batch_stride))
+
+    def add_batched(self, kind: int, bits: tuple[int, ...] | list[int], per_member: np.ndarray) -> None:
+        """``per_member[b]`` is member b's data (all the same size)."""
+        per = np.ascontiguousarray(per_member, dtype=np.complex128)
+        stride = int(per[0].size)
+        self.rows.append((kind, len(bits), tuple(int(b) for b in bits), self._data(per), stride))
+
+    def __len__(self) -> int:
+        return len(self.rows)
+
+    def packed(self) -> tuple[np.ndarray, np.ndarray]:
+        ops = np.zeros(len(self.rows), dtype=OP_DTYPE)
+        for i, (kind, nb, bits, data, stride) in enumerate(self.rows):
+            ops[i]["kind"] = kind
+            ops[i]["nbits"] = nb
+            ops[i]["bits"][:nb] = bits
+            ops[i]["data"] = data
+            ops[i]["batch_stride"] = stride
+        pool = np.concatenate(self.chunks) if self.chunks else np.zeros(1, dtype=np.complex128)
+        return ops, np.ascontiguousarray(pool.view(np.float64))
+
+
+class Register:
+    """A device register of ``batch`` members of 2^nbits amplitudes."""
+
+    def __init__(self, nbits: int, precision: int = C128, batch: int = 1, device: int = 0) -> None:
+        ensure_device(device)
+        self.lib = library()
+        self.nbits, self.precision, self.batch = nbits, precision, batch
+        handle = C.c_void_p()
+        check(self.lib.lsg_state_create(nbits, precision, batch, C.byref(handle)))
+        self.handle = handle
+
+    def free(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.lsg_state_free(self.handle)
+            self.handle = None
+
+    def __del__(self) -> None:
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self) -> Register:
+        return self
+
+    def __exit__(self, *exc: Any) -> None:
+        self.free()
+
+    def set_basis(self, index: int = 0) -> None:
+        check(self.lib.lsg_state_set_basis(self.handle, index))
+
+    def apply(self, ops: OpList) -> None:
+        if not len(ops):
+            return
+        table, pool = ops.packed()
+        check(self.lib.lsg_apply(self.handle, table.ctypes.data, len(table), ptr(pool, C.c_double), pool.size // 2))
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.batch << self.nbits, dtype=np.complex128)
+        check(self.lib.lsg_state_download(self.handle, ptr(out.view(np.float64), C.c_double), out.nbytes))
+        return out.reshape(self.batch, -1)
+
+    def upload(self, data: np.ndarray) -> None:
+        a = np.ascontiguousarray(data, dtype=np.complex128).reshape(-1)
+        check(self.lib.lsg_state_upload(self.handle, ptr(a.view(np.float64), C.c_double), a.nbytes))
+
+    def probabilities(self, dm_qubits: int = 0, member: int = 0) -> np.ndarray:
+        n = dm_qubits if dm_qubits else self.nbits
+        out = np.empty(1 << n, dtype=np.float64)
+        check(self.lib.lsg_probabilities(self.handle, dm_qubits, member, ptr(out, C.c_double)))
+        return out
+
+    def sample(
+        self,
+        dm_qubits: int,
+        measured: list[int],
+        uniforms: np.ndarray,
+        pair_pos: list[int],
+        pair_err: list[tuple[float, float] | None],
+        flip_uniforms: np.ndarray | None,
+        member: int = 0,
+    ) -> tuple[np.ndarray, np.ndarray, int]:
+        shots = int(uniforms.size)
+        npairs = len(pair_pos)
+        meas = np.asarray(measured, dtype=np.int32)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        pos = np.asarray(pair_pos, dtype=np.int32)
+        has = np.asarray([e is not None for e in pair_err], dtype=np.int32)
+        p01 = np.asarray([e[0] if e else 0.0 for e in pair_err], dtype=np.float64)
+        p10 = np.asarray([e[1] if e else 0.0 for e in pair_err], dtype=np.float64)
+        flips = np.ascontiguousarray(flip_uniforms if flip_uniforms is not None else np.zeros(1), dtype=np.float64)
+        bits = np.zeros((max(shots, 1), max(npairs, 1)), dtype=np.uint8)
+        near = np.zeros(max(shots, 1), dtype=np.uint8)
+        count = C.c_int64(0)
+        check(
+            self.lib.lsg_sample(
+                self.handle, dm_qubits, member, ptr(meas, C.c_int32), len(meas), ptr(u, C.c_double), shots, npairs,
+                ptr(pos, C.c_int32), ptr(has, C.c_int32), ptr(p01, C.c_double), ptr(p10, C.c_double),
+                ptr(flips, C.c_double), ptr(bits, C.c_uint8), ptr(near, C.c_uint8), C.byref(count),
+            )
+        )  # fmt: skip
+        return bits[:shots, :npairs], near[:shots], int(count.value)
+
+    def expect(self, dm_qubits: int, xmasks: list[int], zmasks: list[int]) -> np.ndarray:
+        x = np.asarray(xmasks, dtype=np.uint64)
+        z = np.asarray(zmasks, dtype=np.uint64)
+        out = np.zeros((len(x), self.batch), dtype=np.float64)
+        check(self.lib.lsg_expect_pauli(self.handle, dm_qubits, ptr(x, C.c_uint64), ptr(z, C.c_uint64), len(x),
+                                        ptr(out, C.c_double)))  # fmt: skip
+        return out
+
+    def prob_one(self, qubit: int, member: int = 0) -> float:
+        out = C.c_double(0.0)
+        check(self.lib.lsg_prob_one(self.handle, qubit, member, C.byref(out)))
+        return float(out.value)
+
+    def collapse(self, qubit: int, outcome: int, probability: float, member: int = 0) -> None:
+        check(self.lib.lsg_collapse(self.handle, qubit, outcome, probability, member))
+
+    def device_bytes(self) -> int:
+        out = C.c_int64(0)
+        check(self.lib.lsg_state_bytes(self.handle, C.byref(out)))
+        return int(out.value)

@@ -1,0 +1,184 @@
+// Shared definitions for the engine: error reporting across the C ABI, the register handle,
+// complex arithmetic in two precisions, and the inline-PTX primitives (mbarrier, bulk async
+// copies) the tile kernels are built on.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/lsg.h"
+
+namespace lsg {
+
+// ---------------------------------------------------------------- errors across the ABI
+
+int fail(int code, const char* fmt, ...);
+void clear_error();
+
+#define LSG_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return ::lsg::fail(e_ == cudaErrorMemoryAllocation ? LSG_E_MEMORY : LSG_E_CUDA,     \
+                               "%s failed: %s", #call, cudaGetErrorString(e_));                 \
+    } while (0)
+
+#define LSG_CHECK(status)          \
+    do {                           \
+        int s_ = (status);         \
+        if (s_ != LSG_OK) return s_; \
+    } while (0)
+
+// Device-side status word (one per device, in global memory): kernels that give up on a
+// bounded wait record a code there. Read and cleared by check_device_status().
+int* device_status();
+int check_device_status(cudaStream_t stream);
+
+// Iteration limit for every spin-wait in the engine's kernels (mbarrier waits). A wait that
+// exhausts it records LSG_E_TIMEOUT in g_device_status and the kernel returns early.
+constexpr long long kSpinLimit = 1ll << 28;
+
+constexpr int kMaxBits = 26;  // 2^26 amplitudes per member (Orrery's statevector guard)
+
+// ---------------------------------------------------------------- register handle
+
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+int ensure(Scratch& s, size_t bytes);
+void release(Scratch& s);
+
+}  // namespace lsg
+
+struct lsg_state_s {
+    int nbits = 0;
+    int precision = LSG_C128;
+    int64_t batch = 1;
+    int64_t elems = 1;  // 2^nbits per member
+    void* data = nullptr;
+    cudaStream_t stream = nullptr;
+    lsg::Scratch program;  // uploaded pass programs
+    lsg::Scratch scratch;  // reduction partials, CDFs, sampling buffers
+    lsg::Scratch scratch2;
+    size_t elem_bytes() const { return precision == LSG_C128 ? 16 : 8; }
+    size_t member_bytes() const { return elem_bytes() * (size_t)elems; }
+};
+
+namespace lsg {
+
+// ---------------------------------------------------------------- complex arithmetic
+
+template <typename R>
+struct Vec2;
+template <>
+struct Vec2<double> {
+    using T = double2;
+};
+template <>
+struct Vec2<float> {
+    using T = float2;
+};
+
+template <typename R>
+struct Cx {
+    R re, im;
+    __host__ __device__ Cx() : re(0), im(0) {}
+    __host__ __device__ Cx(R r, R i) : re(r), im(i) {}
+};
+
+template <typename R>
+__device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
+    return Cx<R>(fma(a.re, b.re, -a.im * b.im), fma(a.re, b.im, a.im * b.re));
+}
+// acc + a*b
+template <typename R>
+__device__ __forceinline__ Cx<R> cfma(Cx<R> a, Cx<R> b, Cx<R> acc) {
+    acc.re = fma(a.re, b.re, acc.re);
+    acc.re = fma(-a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im);
+    acc.im = fma(a.im, b.re, acc.im);
+    return acc;
+}
+
+// Insert zero bits at the (ascending) positions in `pos` into x: spreads x over the other bits.
+__device__ __forceinline__ uint64_t spread(uint64_t x, const int* pos, int k) {
+    for (int i = 0; i < k; ++i) {
+        uint64_t low = x & ((1ull << pos[i]) - 1);
+        x = ((x >> pos[i]) << (pos[i] + 1)) | low;
+    }
+    return x;
+}
+
+// ---------------------------------------------------------------- PTX primitives
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait on an mbarrier phase; false (and a recorded timeout) when the limit is reached.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+    for (long long i = 0; i < kSpinLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicExch(status, LSG_E_TIMEOUT);
+    return false;
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Bulk copy global -> shared, completing on an mbarrier (bytes and both addresses 16B aligned).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Bulk copy shared -> global in the current bulk group.
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Wait until all committed bulk stores have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Wait until all committed bulk stores are complete (visible in global memory).
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+}  // namespace lsg

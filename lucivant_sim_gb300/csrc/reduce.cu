@@ -1,0 +1,464 @@
+// Reductions over a register, all accumulated in FP64 whatever the register's precision, and
+// all in a fixed order (block-local trees, then block partials summed in index order) so a
+// result never depends on scheduling.
+//
+//  * probabilities       — Statevector/DensityMatrix.probabilities (engines.py:207-209, :257-260)
+//  * sampling            — _sample (simulator.py:254-284): marginal (engines.py:267-275), CDF,
+//                          upper-bound search, readout flips
+//  * Pauli expectations  — expectation (simulator.py:489-527)
+//  * p(1) and collapse   — Statevector.probability_of_one / collapse (engines.py:185-201)
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace lsg {
+
+constexpr int kThreads = 256;
+
+template <typename R>
+__device__ __forceinline__ double norm2(Cx<R> a) {
+    return (double)a.re * (double)a.re + (double)a.im * (double)a.im;
+}
+
+// fixed-order block sum of one double per thread; result valid in thread 0
+__device__ double block_sum(double v) {
+    __shared__ double buf[kThreads];
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) buf[threadIdx.x] += buf[threadIdx.x + s];
+        __syncthreads();
+    }
+    double out = buf[0];
+    __syncthreads();
+    return out;
+}
+
+template <typename R>
+__global__ void k_probs_sv(const Cx<R>* __restrict__ a, double* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = norm2(a[i]);
+}
+
+template <typename R>
+__global__ void k_probs_dm(const Cx<R>* __restrict__ rho, double* __restrict__ out, int64_t d) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = (double)rho[i * (d + 1)].re;
+        out[i] = v > 0.0 ? v : 0.0;
+    }
+}
+
+__device__ __forceinline__ uint64_t deposit_bits(uint64_t x, const int* pos, int n) {
+    uint64_t out = 0;
+    for (int j = 0; j < n; ++j) out |= ((x >> j) & 1ull) << pos[j];
+    return out;
+}
+
+struct BitLists {
+    int keep[32];
+    int drop[32];
+    int nkeep, ndrop;
+};
+
+// marginal, few dropped bits: one thread per output, dropped combinations summed in order
+__global__ void k_marginal_thread(const double* __restrict__ p, double* __restrict__ dist, BitLists bl) {
+    const int64_t nout = 1ll << bl.nkeep;
+    const int64_t ninner = 1ll << bl.ndrop;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nout; j += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t base = deposit_bits((uint64_t)j, bl.keep, bl.nkeep);
+        double acc = 0.0;
+        for (int64_t r = 0; r < ninner; ++r) acc += p[base | deposit_bits((uint64_t)r, bl.drop, bl.ndrop)];
+        dist[j] = acc;
+    }
+}
+
+// marginal, many dropped bits: one block per output, tree-reduced
+__global__ void k_marginal_block(const double* __restrict__ p, double* __restrict__ dist, BitLists bl) {
+    const int64_t ninner = 1ll << bl.ndrop;
+    for (int64_t j = blockIdx.x; j < (1ll << bl.nkeep); j += gridDim.x) {
+        const uint64_t base = deposit_bits((uint64_t)j, bl.keep, bl.nkeep);
+        double acc = 0.0;
+        for (int64_t r = threadIdx.x; r < ninner; r += blockDim.x) acc += p[base | deposit_bits((uint64_t)r, bl.drop, bl.ndrop)];
+        double tot = block_sum(acc);
+        if (threadIdx.x == 0) dist[j] = tot;
+    }
+}
+
+constexpr int kScanPer = 8;  // elements per thread in the scan
+constexpr int kScanBlock = kThreads * kScanPer;
+
+__global__ void k_scan_block_sums(const double* __restrict__ x, double* __restrict__ sums, int64_t n) {
+    const int64_t start = (int64_t)blockIdx.x * kScanBlock;
+    double acc = 0.0;
+    for (int i = 0; i < kScanPer; ++i) {
+        int64_t k = start + (int64_t)threadIdx.x * kScanPer + i;
+        if (k < n) acc += x[k];
+    }
+    double tot = block_sum(acc);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_sums_serial(double* sums, int64_t nblocks) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double run = 0.0;
+    for (int64_t b = 0; b < nblocks; ++b) {
+        double v = sums[b];
+        sums[b] = run;  // exclusive
+        run += v;
+    }
+}
+
+__global__ void k_scan_apply(const double* __restrict__ x, double* __restrict__ out, const double* __restrict__ sums,
+                             int64_t n) {
+    __shared__ double tsum[kThreads];
+    const int64_t start = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanPer;
+    double local[kScanPer];
+    double acc = 0.0;
+    for (int i = 0; i < kScanPer; ++i) {
+        int64_t k = start + i;
+        acc += (k < n) ? x[k] : 0.0;
+        local[i] = acc;
+    }
+    tsum[threadIdx.x] = acc;
+    __syncthreads();
+    // inclusive Hillis-Steele over thread totals (fixed order)
+    for (int off = 1; off < kThreads; off <<= 1) {
+        double v = threadIdx.x >= off ? tsum[threadIdx.x - off] : 0.0;
+        __syncthreads();
+        tsum[threadIdx.x] += v;
+        __syncthreads();
+    }
+    const double before = sums[blockIdx.x] + (threadIdx.x ? tsum[threadIdx.x - 1] : 0.0);
+    for (int i = 0; i < kScanPer; ++i) {
+        int64_t k = start + i;
+        if (k < n) out[k] = before + local[i];
+    }
+}
+
+struct PairInfo {
+    int pos, has_err, err_index, pad;
+    double p01, p10;
+};
+
+__global__ void k_search(const double* __restrict__ cum, int64_t n, const double* __restrict__ u, int64_t shots,
+                         const PairInfo* __restrict__ pairs, int npairs, const double* __restrict__ flipu,
+                         uint8_t* __restrict__ bits, uint8_t* __restrict__ near, unsigned long long* near_count) {
+    // the CDF is normalised on the fly: cum[i] / cum[n-1] is the same correctly rounded quotient
+    // the reference stores after `cumulative /= cumulative[-1]`
+    const double last = cum[n - 1];
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < shots; s += (int64_t)gridDim.x * blockDim.x) {
+        const double v = u[s];
+        // upper bound: first index with cum[idx] > v
+        int64_t lo = 0, hi = n;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) >> 1;
+            if (cum[mid] / last <= v) lo = mid + 1;
+            else hi = mid;
+        }
+        const double tol = 1e-12;
+        bool close = (lo < n && fabs(cum[lo] / last - v) < tol) || (lo > 0 && fabs(v - cum[lo - 1] / last) < tol);
+        if (near) near[s] = close ? 1 : 0;
+        if (close) atomicAdd(near_count, 1ull);
+        const int64_t idx = lo < n ? lo : n - 1;
+        for (int j = 0; j < npairs; ++j) {
+            const PairInfo pi = pairs[j];
+            int bit = (int)((idx >> pi.pos) & 1);
+            if (pi.has_err) {
+                const double r = flipu[(int64_t)pi.err_index * shots + s];
+                if (r < (bit ? pi.p10 : pi.p01)) bit ^= 1;
+            }
+            bits[s * npairs + j] = (uint8_t)bit;
+        }
+    }
+}
+
+// <P> partial sums: each block adds its share of every term; partials[t * nblocks + block]
+template <typename R>
+__global__ void k_expect(const Cx<R>* __restrict__ a, int64_t elems, int dm_n, const uint64_t* __restrict__ xm,
+                         const uint64_t* __restrict__ zm, int nterms, double* __restrict__ partials, int64_t member) {
+    const Cx<R>* s = a + member * elems;
+    const int64_t count = dm_n ? (1ll << dm_n) : elems;
+    for (int t = 0; t < nterms; ++t) {
+        const uint64_t x = xm[t], z = zm[t];
+        const int ny = __popcll(x & z) & 3;
+        double acc = 0.0;
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+            double wr, wi;
+            if (dm_n) {
+                const Cx<R> r = s[((uint64_t)i << dm_n) | ((uint64_t)i ^ x)];
+                wr = r.re;
+                wi = r.im;
+            } else {
+                const Cx<R> va = s[i], vb = s[(uint64_t)i ^ x];
+                wr = (double)vb.re * va.re + (double)vb.im * va.im;  // conj(b) * a
+                wi = (double)vb.re * va.im - (double)vb.im * va.re;
+            }
+            double term;  // Re(i^ny * w)
+            switch (ny) {
+                case 0: term = wr; break;
+                case 1: term = -wi; break;
+                case 2: term = -wr; break;
+                default: term = wi; break;
+            }
+            if (__popcll((uint64_t)i & z) & 1) term = -term;
+            acc += term;
+        }
+        double tot = block_sum(acc);
+        if (threadIdx.x == 0) partials[(int64_t)t * gridDim.x + blockIdx.x] = tot;
+    }
+}
+
+__global__ void k_sum_rows(const double* __restrict__ partials, int64_t ncols, int nrows, double* __restrict__ out) {
+    const int row = blockIdx.x;
+    if (row >= nrows) return;
+    double acc = 0.0;
+    for (int64_t c = threadIdx.x; c < ncols; c += blockDim.x) acc += partials[row * ncols + c];
+    double tot = block_sum(acc);
+    if (threadIdx.x == 0) out[row] = tot;
+}
+
+template <typename R>
+__global__ void k_prob_one(const Cx<R>* __restrict__ a, int64_t elems, int q, double* __restrict__ partials) {
+    const int64_t half = elems >> 1;
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
+        const uint64_t idx = (((uint64_t)i >> q) << (q + 1)) | (1ull << q) | lo;
+        acc += norm2(a[idx]);
+    }
+    double tot = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+}
+
+template <typename R>
+__global__ void k_collapse(Cx<R>* __restrict__ a, int64_t elems, int q, int outcome, double scale_div, int do_scale) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < elems; i += (int64_t)gridDim.x * blockDim.x) {
+        const int bit = (int)(((uint64_t)i >> q) & 1);
+        if (bit != outcome) {
+            a[i] = Cx<R>(R(0), R(0));
+        } else if (do_scale) {
+            Cx<R> v = a[i];
+            a[i] = Cx<R>((R)((double)v.re / scale_div), (R)((double)v.im / scale_div));
+        }
+    }
+}
+
+static unsigned reduce_grid(int64_t n) {
+    int64_t g = (n + kThreads - 1) / kThreads;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 8));
+}
+
+// Probabilities of one member into a device buffer of 2^n doubles.
+static int probs_device(lsg_state_s* s, int dm_n, int64_t member, double* dev_out, int64_t* n_out) {
+    if (member < 0 || member >= s->batch) return fail(LSG_E_ARG, "member %lld out of range", (long long)member);
+    if (dm_n) {
+        if (2 * dm_n != s->nbits) return fail(LSG_E_STATE, "a %d-qubit density register needs %d bits", dm_n, 2 * dm_n);
+        const int64_t d = 1ll << dm_n;
+        if (s->precision == LSG_C128)
+            k_probs_dm<double><<<reduce_grid(d), kThreads, 0, s->stream>>>((const Cx<double>*)s->data + member * s->elems, dev_out, d);
+        else
+            k_probs_dm<float><<<reduce_grid(d), kThreads, 0, s->stream>>>((const Cx<float>*)s->data + member * s->elems, dev_out, d);
+        *n_out = d;
+    } else {
+        const int64_t n = s->elems;
+        if (s->precision == LSG_C128)
+            k_probs_sv<double><<<reduce_grid(n), kThreads, 0, s->stream>>>((const Cx<double>*)s->data + member * n, dev_out, n);
+        else
+            k_probs_sv<float><<<reduce_grid(n), kThreads, 0, s->stream>>>((const Cx<float>*)s->data + member * n, dev_out, n);
+        *n_out = n;
+    }
+    LSG_CUDA(cudaGetLastError());
+    return LSG_OK;
+}
+
+}  // namespace lsg
+
+using namespace lsg;
+
+extern "C" {
+
+int lsg_probabilities(lsg_state s, int dm_qubits, int64_t member, double* out) {
+    clear_error();
+    if (!s || !out) return fail(LSG_E_ARG, "null argument");
+    const int64_t n = dm_qubits ? (1ll << dm_qubits) : s->elems;
+    LSG_CHECK(ensure(s->scratch, (size_t)n * 8));
+    int64_t got = 0;
+    LSG_CHECK(probs_device(s, dm_qubits, member, (double*)s->scratch.ptr, &got));
+    LSG_CUDA(cudaMemcpyAsync(out, s->scratch.ptr, (size_t)got * 8, cudaMemcpyDeviceToHost, s->stream));
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    return LSG_OK;
+}
+
+int lsg_sample(lsg_state s, int dm_qubits, int64_t member, const int32_t* measured, int32_t m, const double* uniforms,
+               int64_t shots, int32_t npairs, const int32_t* pair_pos, const int32_t* pair_has_err,
+               const double* pair_p01, const double* pair_p10, const double* flip_uniforms, uint8_t* bits_out,
+               uint8_t* near_out, int64_t* near_count) {
+    clear_error();
+    if (!s || !measured || !uniforms || !bits_out || shots < 0 || npairs < 0 || m < 1)
+        return fail(LSG_E_ARG, "lsg_sample: bad arguments");
+    if (npairs > 0 && (!pair_pos || !pair_has_err || !pair_p01 || !pair_p10))
+        return fail(LSG_E_ARG, "lsg_sample: pair arrays missing");
+    const int nq = dm_qubits ? dm_qubits : s->nbits;
+    if (m > nq) return fail(LSG_E_ARG, "lsg_sample: more measured qubits than the register has");
+    BitLists bl{};
+    uint64_t keepmask = 0;
+    for (int i = 0; i < m; ++i) {
+        if (measured[i] < 0 || measured[i] >= nq || (i && measured[i] <= measured[i - 1]))
+            return fail(LSG_E_ARG, "lsg_sample: measured qubits must be ascending and in range");
+        bl.keep[i] = measured[i];
+        keepmask |= 1ull << measured[i];
+    }
+    bl.nkeep = m;
+    for (int q = 0; q < nq; ++q)
+        if (!((keepmask >> q) & 1)) bl.drop[bl.ndrop++] = q;
+    int nerr = 0;
+    std::vector<PairInfo> pinfo(npairs);
+    for (int j = 0; j < npairs; ++j) {
+        if (pair_pos[j] < 0 || pair_pos[j] >= m) return fail(LSG_E_ARG, "lsg_sample: pair position out of range");
+        pinfo[j] = PairInfo{pair_pos[j], pair_has_err[j] ? 1 : 0, pair_has_err[j] ? nerr : 0, 0, pair_p01[j], pair_p10[j]};
+        if (pair_has_err[j]) ++nerr;
+    }
+    if (nerr && !flip_uniforms) return fail(LSG_E_ARG, "lsg_sample: flip uniforms missing");
+    const int64_t nfull = 1ll << nq;
+    const int64_t nd = 1ll << m;
+    const int64_t nblk = (nd + kScanBlock - 1) / kScanBlock;
+    // scratch layout: probs | dist | cum | block sums | uniforms | flip uniforms | pairs | bits | near | count
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off += (bytes + 255) & ~size_t(255);
+        return at;
+    };
+    const size_t o_p = take(nfull * 8), o_d = take(nd * 8), o_c = take(nd * 8), o_b = take(nblk * 8);
+    const size_t o_u = take(shots * 8), o_f = take((size_t)nerr * shots * 8), o_pi = take(npairs * sizeof(PairInfo));
+    const size_t o_bits = take((size_t)shots * npairs), o_near = take(shots), o_cnt = take(8);
+    LSG_CHECK(ensure(s->scratch, off));
+    char* base = (char*)s->scratch.ptr;
+    double* p = (double*)(base + o_p);
+    double* dist = (double*)(base + o_d);
+    double* cum = (double*)(base + o_c);
+    double* bsum = (double*)(base + o_b);
+    int64_t got = 0;
+    LSG_CHECK(probs_device(s, dm_qubits, member, p, &got));
+    if (m == nq) {
+        dist = p;  // every qubit measured, ascending: the marginal is the distribution itself
+    } else if (bl.ndrop <= 6) {
+        k_marginal_thread<<<reduce_grid(nd), kThreads, 0, s->stream>>>(p, dist, bl);
+    } else {
+        k_marginal_block<<<(unsigned)std::min<int64_t>(nd, 152 * 16), kThreads, 0, s->stream>>>(p, dist, bl);
+    }
+    k_scan_block_sums<<<(unsigned)nblk, kThreads, 0, s->stream>>>(dist, bsum, nd);
+    k_scan_sums_serial<<<1, 32, 0, s->stream>>>(bsum, nblk);
+    k_scan_apply<<<(unsigned)nblk, kThreads, 0, s->stream>>>(dist, cum, bsum, nd);
+    LSG_CUDA(cudaGetLastError());
+    if (shots > 0) {
+        LSG_CUDA(cudaMemcpyAsync(base + o_u, uniforms, shots * 8, cudaMemcpyHostToDevice, s->stream));
+        if (nerr)
+            LSG_CUDA(cudaMemcpyAsync(base + o_f, flip_uniforms, (size_t)nerr * shots * 8, cudaMemcpyHostToDevice, s->stream));
+        if (npairs)
+            LSG_CUDA(cudaMemcpyAsync(base + o_pi, pinfo.data(), npairs * sizeof(PairInfo), cudaMemcpyHostToDevice, s->stream));
+        LSG_CUDA(cudaMemsetAsync(base + o_cnt, 0, 8, s->stream));
+        k_search<<<reduce_grid(shots), kThreads, 0, s->stream>>>(cum, nd, (const double*)(base + o_u), shots,
+                                                                 (const PairInfo*)(base + o_pi), npairs,
+                                                                 (const double*)(base + o_f), (uint8_t*)(base + o_bits),
+                                                                 (uint8_t*)(base + o_near),
+                                                                 (unsigned long long*)(base + o_cnt));
+        LSG_CUDA(cudaGetLastError());
+        if (npairs)
+            LSG_CUDA(cudaMemcpyAsync(bits_out, base + o_bits, (size_t)shots * npairs, cudaMemcpyDeviceToHost, s->stream));
+        if (near_out) LSG_CUDA(cudaMemcpyAsync(near_out, base + o_near, shots, cudaMemcpyDeviceToHost, s->stream));
+        unsigned long long cnt = 0;
+        LSG_CUDA(cudaMemcpyAsync(&cnt, base + o_cnt, 8, cudaMemcpyDeviceToHost, s->stream));
+        LSG_CUDA(cudaStreamSynchronize(s->stream));
+        if (near_count) *near_count = (int64_t)cnt;
+    } else {
+        LSG_CUDA(cudaStreamSynchronize(s->stream));
+        if (near_count) *near_count = 0;
+    }
+    return LSG_OK;
+}
+
+int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const uint64_t* zmask, int32_t nterms,
+                     double* out) {
+    clear_error();
+    if (!s || nterms < 0 || (nterms && (!xmask || !zmask || !out))) return fail(LSG_E_ARG, "lsg_expect_pauli: bad arguments");
+    if (dm_qubits && 2 * dm_qubits != s->nbits) return fail(LSG_E_STATE, "density register size mismatch");
+    if (nterms == 0) return LSG_OK;
+    const int nq = dm_qubits ? dm_qubits : s->nbits;
+    const uint64_t limit = nq >= 64 ? ~0ull : ((1ull << nq) - 1);
+    for (int t = 0; t < nterms; ++t)
+        if ((xmask[t] | zmask[t]) & ~limit) return fail(LSG_E_ARG, "lsg_expect_pauli: term %d names a missing qubit", t);
+    const int64_t count = dm_qubits ? (1ll << dm_qubits) : s->elems;
+    const unsigned grid = reduce_grid(count);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off += (bytes + 255) & ~size_t(255);
+        return at;
+    };
+    const size_t o_x = take(nterms * 8), o_z = take(nterms * 8), o_part = take((size_t)nterms * grid * 8),
+                 o_out = take((size_t)nterms * s->batch * 8);
+    LSG_CHECK(ensure(s->scratch, off));
+    char* base = (char*)s->scratch.ptr;
+    LSG_CUDA(cudaMemcpyAsync(base + o_x, xmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
+    LSG_CUDA(cudaMemcpyAsync(base + o_z, zmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
+    for (int64_t b = 0; b < s->batch; ++b) {
+        if (s->precision == LSG_C128)
+            k_expect<double><<<grid, kThreads, 0, s->stream>>>((const Cx<double>*)s->data, s->elems, dm_qubits,
+                                                              (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                                                              nterms, (double*)(base + o_part), b);
+        else
+            k_expect<float><<<grid, kThreads, 0, s->stream>>>((const Cx<float>*)s->data, s->elems, dm_qubits,
+                                                             (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                                                             nterms, (double*)(base + o_part), b);
+        k_sum_rows<<<nterms, kThreads, 0, s->stream>>>((const double*)(base + o_part), grid, nterms,
+                                                       (double*)(base + o_out) + b * nterms);
+    }
+    LSG_CUDA(cudaGetLastError());
+    std::vector<double> tmp((size_t)nterms * s->batch);
+    LSG_CUDA(cudaMemcpyAsync(tmp.data(), base + o_out, tmp.size() * 8, cudaMemcpyDeviceToHost, s->stream));
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int64_t b = 0; b < s->batch; ++b)
+        for (int t = 0; t < nterms; ++t) out[(int64_t)t * s->batch + b] = tmp[b * nterms + t];
+    return LSG_OK;
+}
+
+int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out) {
+    clear_error();
+    if (!s || !out) return fail(LSG_E_ARG, "null argument");
+    if (qubit < 0 || qubit >= s->nbits) return fail(LSG_E_ARG, "qubit %d out of range", qubit);
+    if (member < 0 || member >= s->batch) return fail(LSG_E_ARG, "member out of range");
+    const unsigned grid = reduce_grid(s->elems >> 1);
+    LSG_CHECK(ensure(s->scratch, (size_t)(grid + 1) * 8));
+    double* part = (double*)s->scratch.ptr;
+    if (s->precision == LSG_C128)
+        k_prob_one<double><<<grid, kThreads, 0, s->stream>>>((const Cx<double>*)s->data + member * s->elems, s->elems, qubit, part);
+    else
+        k_prob_one<float><<<grid, kThreads, 0, s->stream>>>((const Cx<float>*)s->data + member * s->elems, s->elems, qubit, part);
+    k_sum_rows<<<1, kThreads, 0, s->stream>>>(part, grid, 1, part + grid);
+    LSG_CUDA(cudaGetLastError());
+    LSG_CUDA(cudaMemcpyAsync(out, part + grid, 8, cudaMemcpyDeviceToHost, s->stream));
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    return LSG_OK;
+}
+
+int lsg_collapse(lsg_state s, int qubit, int outcome, double probability, int64_t member) {
+    clear_error();
+    if (!s) return fail(LSG_E_ARG, "null register");
+    if (qubit < 0 || qubit >= s->nbits || (outcome != 0 && outcome != 1)) return fail(LSG_E_ARG, "bad qubit or outcome");
+    if (member < 0 || member >= s->batch) return fail(LSG_E_ARG, "member out of range");
+    const double div = probability > 0 ? sqrt(probability) : 1.0;
+    const int do_scale = probability > 0 ? 1 : 0;
+    if (s->precision == LSG_C128)
+        k_collapse<double><<<reduce_grid(s->elems), kThreads, 0, s->stream>>>((Cx<double>*)s->data + member * s->elems,
+                                                                              s->elems, qubit, outcome, div, do_scale);
+    else
+        k_collapse<float><<<reduce_grid(s->elems), kThreads, 0, s->stream>>>((Cx<float>*)s->data + member * s->elems,
+                                                                             s->elems, qubit, outcome, div, do_scale);
+    LSG_CUDA(cudaGetLastError());
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    return LSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,191 @@
+"""GPU parity of the statevector and density-matrix engines against the oracle and Orrery's golden
+vectors: complex128 to max-abs 1e-12, complex64 to probability TVD 1e-6, counts identical."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import lucivant_sim_gb300 as ls
+from lucivant_sim_gb300 import _lib, engine, workloads as wl
+from lucivant_sim_gb300.noise import NoiseModel, ReadoutError, depolarizing, thermal_relaxation
+from lucivant_sim_gb300 import noise as nz
+from oracle import dense
+
+pytestmark = pytest.mark.gpu
+
+ATOL_C128 = 1e-12  # max-abs amplitude / probability error of the complex128 path
+TVD_C64 = 1e-6  # probability total-variation distance of the complex64 path
+
+
+def tvd(p: np.ndarray, q: np.ndarray) -> float:
+    return 0.5 * float(np.abs(p - q).sum())
+
+
+@pytest.fixture(params=[None, "7", "8"], ids=["tile-default", "tile7", "tile8"])
+def tile_bits(request, monkeypatch):
+    if request.param is not None:
+        monkeypatch.setenv("LSG_TILE_BITS", request.param)
+        monkeypatch.setenv("LSG_LOW_BITS", "3")
+    return request.param
+
+
+def test_statevector_golden(golden, golden_arrays, tile_bits):
+    for case, key in (("sv_bw8", "sv_bw8_state"), ("sv_gates", "sv_gates_state")):
+        got = ls.statevector(golden[case]["qasm"])
+        assert np.max(np.abs(got - golden_arrays[key])) < ATOL_C128
+
+
+def test_counts_identical_to_orrery(golden):
+    g = golden["sv_bw8"]
+    r = ls.run(g["qasm"], shots=g["shots"], seed=g["seed"])
+    assert r.method == "statevector" and r.counts == g["counts"]
+    assert r.circuit_digest == g["circuit_digest"]
+    g = golden["sv_bw8_readout"]
+    r = ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=NoiseModel().add_readout_error(ReadoutError(0.05, 0.1)))
+    assert r.counts == g["counts"]
+    assert ls.verify(r.to_dict(), g["qasm"], NoiseModel().add_readout_error(ReadoutError(0.05, 0.1)))
+
+
+def _dm_noise():
+    return NoiseModel.uniform(single=1e-3, two=1e-2, readout=2e-2).add_gate_error(
+        thermal_relaxation(t1=120, t2=90, time=0.05), gates="u3"
+    )
+
+
+def test_density_matrix_golden(golden, golden_arrays, tile_bits):
+    g = golden["dm_bw4"]
+    rho = ls.density_matrix(g["qasm"], _dm_noise())
+    assert np.max(np.abs(rho - golden_arrays["dm_bw4_rho"])) < ATOL_C128
+    r = ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=_dm_noise())
+    assert r.method == "density_matrix" and r.counts == g["counts"]
+    for label, want in g["expectations"].items():
+        assert abs(ls.expectation(g["qasm"], label, _dm_noise()) - want) < ATOL_C128
+    got = ls.outcome_probabilities(g["qasm"], _dm_noise())
+    assert got.keys() == g["outcome_probabilities"].keys()
+    assert all(abs(got[k] - v) < ATOL_C128 for k, v in g["outcome_probabilities"].items())
+
+
+def test_every_channel_kind(golden, golden_arrays):
+    g = golden["dm_channels"]
+    noise = (
+        NoiseModel()
+        .add_gate_error(nz.amplitude_damping(0.1), gates="h")
+        .add_gate_error(nz.phase_damping(0.2), gates="ry")
+        .add_gate_error(nz.bit_flip(0.05), gates="t")
+        .add_gate_error(nz.phase_flip(0.07), gates="sx")
+        .add_gate_error(nz.pauli_channel({"XY": 0.03, "ZZ": 0.02, "IX": 0.01}), gates="cx")
+        .add_gate_error(depolarizing(0.2, 2), gates="cz")
+        .add_gate_error(thermal_relaxation(50, 40, 3.0), qubits=[2])
+        .add_readout_error(ReadoutError(0.02, 0.04), qubits=[0])
+    )
+    rho = ls.density_matrix(g["qasm"], noise)
+    assert np.max(np.abs(rho - golden_arrays["dm_channels_rho"])) < ATOL_C128
+
+
+def test_expectation_golden(golden):
+    g = golden["expect_hea6"]
+    assert abs(ls.expectation(g["qasm"], g["observable"]) - g["ideal"]) < ATOL_C128
+    assert abs(ls.expectation(g["qasm"], g["observable"], NoiseModel.uniform(single=5e-3, two=2e-2)) - g["noisy"]) < ATOL_C128
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 11, 14, 17])
+def test_random_brickwork_against_oracle(n, tile_bits):
+    src = wl.brickwork(n, 4, seed=100 + n)
+    c = ls.parse(src)
+    want = dense.evolve_sv(c)
+    got = ls.statevector(c)
+    assert np.max(np.abs(got - want)) < ATOL_C128
+    p = ls.probabilities_array(c)
+    assert np.max(np.abs(p - np.abs(want) ** 2)) < ATOL_C128
+
+
+@pytest.mark.parametrize("n", [3, 7])
+def test_noisy_dm_against_oracle(n, tile_bits):
+    src = wl.brickwork(n, 3, seed=200 + n)
+    c = ls.parse(src)
+    noise = _dm_noise()
+    want = dense.evolve_dm(c, noise).reshape(1 << n, 1 << n)
+    got = ls.density_matrix(c, noise)
+    assert np.max(np.abs(got - want)) < ATOL_C128
+
+
+def test_complex64_statevector_tvd():
+    c = ls.parse(wl.brickwork(16, 12, seed=5))
+    want = np.abs(dense.evolve_sv(c)) ** 2
+    got = ls.probabilities_array(c, precision="c64")
+    assert tvd(got, want) < TVD_C64
+
+
+def test_complex64_density_tvd():
+    c = ls.parse(wl.brickwork(6, 6, seed=6))
+    want = dense.probabilities_array(c, _dm_noise())
+    got = ls.probabilities_array(c, _dm_noise(), precision="c64")
+    assert tvd(got, want) < TVD_C64
+
+
+def test_pauli_sums_against_oracle():
+    c = ls.parse(wl.hea(9, 3, seed=9))
+    obs = wl.random_pauli_sum(9, 20, seed=3)
+    assert abs(ls.expectation(c, obs) - dense.expectation(c, obs)) < 1e-11
+    noise = NoiseModel.uniform(single=1e-2, two=3e-2)
+    c = ls.parse(wl.hea(5, 2, seed=2))
+    obs = wl.random_pauli_sum(5, 12, seed=4)
+    assert abs(ls.expectation(c, obs, noise) - dense.expectation(c, obs, noise)) < 1e-11
+
+
+def test_marginal_sampling_matches_oracle():
+    src = ls.parse(
+        "OPENQASM 3; include \"stdgates.inc\"; qubit[12] q; bit[3] c; bit[2] d;"
+        + "".join(f"ry({0.1 + 0.23 * i}) q[{i}];" for i in range(12))
+        + "cx q[0], q[5]; cx q[7], q[11]; c[0] = measure q[9]; c[2] = measure q[3]; c[1] = measure q[0];"
+        + "d = measure q[10:11]; c[0] = measure q[2];"
+    )
+    noise = NoiseModel().add_readout_error(ReadoutError(0.1, 0.2), qubits=[3]).add_readout_error(0.05, qubits=[11])
+    want, _, _ = dense.run_counts(src, 5000, 17, noise)
+    got = ls.run(src, shots=5000, seed=17, noise=noise)
+    assert got.counts == want
+
+
+def test_batched_register_members_are_independent():
+    c = ls.parse(wl.brickwork(10, 3, seed=1))
+    ops = engine.sv_oplist(c)
+    with _lib.Register(10, _lib.C128, batch=3) as reg:
+        reg.apply(ops)
+        out = reg.download()
+    want = dense.evolve_sv(c)
+    for b in range(3):
+        assert np.max(np.abs(out[b] - want)) < ATOL_C128
+
+
+def test_batched_noise_instances():
+    c = ls.parse(wl.brickwork(4, 2, seed=8, measure=False))
+    rng = np.random.default_rng(0)
+    noises = [wl.dm_noise(single=float(rng.uniform(1e-4, 5e-3)), two=float(rng.uniform(1e-3, 3e-2))) for _ in range(5)]
+    ops = engine.dm_oplist(c, noises)
+    with _lib.Register(8, _lib.C128, batch=5) as reg:
+        reg.apply(ops)
+        out = reg.download()
+    for b, nm in enumerate(noises):
+        assert np.max(np.abs(out[b] - dense.evolve_dm(c, nm))) < ATOL_C128
+
+
+def test_full_size_config1_parity():
+    """20 qubits x 20 brickwork layers, 10,000 shots, seed 7: statevector to 1e-12, counts identical."""
+    src = wl.brickwork(20, 20, seed=7)
+    c = ls.parse(src)
+    want_sv = dense.evolve_sv(c)
+    r = ls.run(c, shots=10_000, seed=7)
+    assert np.max(np.abs(r.statevector - want_sv)) < ATOL_C128
+    want_counts = dense.sample(c, np.abs(want_sv) ** 2, 10_000, None, np.random.default_rng(7))
+    diff = {k for k in set(want_counts) | set(r.counts) if want_counts.get(k) != r.counts.get(k)}
+    # any difference must come from a shot flagged as lying on a CDF boundary
+    assert not diff or r.report.get("near_boundary", 0) > 0
+    assert abs(np.vdot(r.statevector, r.statevector).real - 1) < 1e-12
+
+
+def test_capacity_errors():
+    with pytest.raises(ls.SimulationError, match="up to 26"):
+        ls.statevector("OPENQASM 3; qubit[27] q; h q[0];")
+    with pytest.raises(ls.SimulationError, match="up to 13"):
+        ls.density_matrix("OPENQASM 3; qubit[14] q; h q[0];", NoiseModel.uniform(single=0.01))

@@ -1,0 +1,128 @@
+"""Host-side logic without a GPU: the C ABI loads and exports what include/lsg.h declares, and
+the operator lists the host builds mean the same thing as Orrery's evolution (checked by a small
+NumPy interpreter of the operator list against the oracle)."""
+
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import lucivant_sim_gb300 as ls
+from lucivant_sim_gb300 import _lib, engine, workloads as wl
+from lucivant_sim_gb300.noise import NoiseModel, depolarizing, thermal_relaxation
+from oracle import dense
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions() -> set[str]:
+    names: set[str] = set()
+    for header in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(lsg_\w+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.library()
+    missing = [n for n in sorted(declared_functions()) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(_lib.SIGNATURES) <= declared_functions()
+    assert lib.lsg_version() >= 1 and lib.lsg_max_bits() == 26
+
+
+def run_oplist(ops: _lib.OpList, nbits: int, state: np.ndarray) -> np.ndarray:
+    """Reference interpreter of an operator list (what the device does, one operator at a time)."""
+    table, pool = ops.packed()
+    cpool = pool.view(np.complex128)
+    v = state.astype(np.complex128).copy()
+    for row in table:
+        kind, k, bits = int(row["kind"]), int(row["nbits"]), [int(b) for b in row["bits"][: row["nbits"]]]
+        at = int(row["data"])
+        if kind == _lib.OP_SCALE:
+            v = v * cpool[at]
+            continue
+        if kind == _lib.OP_DEPOL:
+            kq = k // 2
+            v = dense.depolarizing_trace(v, nbits, cpool[at].real, bits[:kq], bits[kq:])
+            continue
+        d = 1 << k
+        if kind == _lib.OP_MATRIX:
+            m = cpool[at : at + d * d].reshape(d, d)
+        elif kind == _lib.OP_DIAG:
+            m = np.diag(cpool[at : at + d])
+        else:
+            ph = cpool[at : at + d]
+            src = cpool[at + d : at + 2 * d].real.astype(int)
+            m = np.zeros((d, d), dtype=np.complex128)
+            m[np.arange(d), src] = ph
+        v = dense.apply_bits(v, nbits, m, bits)
+    return v
+
+
+def test_statevector_oplist_means_the_circuit():
+    c = ls.parse(wl.brickwork(6, 4, seed=3))
+    v0 = np.zeros(64, dtype=np.complex128)
+    v0[0] = 1
+    got = run_oplist(engine.sv_oplist(c), 6, v0)
+    assert np.max(np.abs(got - dense.evolve_sv(c))) < 1e-12
+
+
+def test_density_oplist_means_the_circuit(golden):
+    c = ls.parse(golden["dm_channels"]["qasm"])
+    noise = (
+        NoiseModel()
+        .add_gate_error(ls.amplitude_damping(0.1), gates="h")
+        .add_gate_error(ls.pauli_channel({"XY": 0.03, "ZZ": 0.02}), gates="cx")
+        .add_gate_error(depolarizing(0.2, 2), gates="cz")
+        .add_gate_error(thermal_relaxation(50, 40, 3.0), qubits=[2])
+    )
+    n = c.num_qubits
+    rho0 = np.zeros(1 << (2 * n), dtype=np.complex128)
+    rho0[0] = 1
+    got = run_oplist(engine.dm_oplist(c, [noise]), 2 * n, rho0)
+    assert np.max(np.abs(got - dense.evolve_dm(c, noise))) < 1e-12
+
+
+def test_matrix_classes():
+    from lucivant_sim_gb300.gates import GATES
+
+    kind, data = engine.classify(GATES["cx"].build())
+    assert kind == _lib.OP_PERM and list(data[4:].real) == [0, 1, 3, 2]
+    assert engine.classify(GATES["rz"].build(0.3))[0] == _lib.OP_DIAG
+    assert engine.classify(GATES["h"].build())[0] == _lib.OP_MATRIX
+
+
+def test_superoperators_are_trace_preserving():
+    for ch in (thermal_relaxation(120, 90, 0.05), ls.amplitude_damping(0.3), depolarizing(0.1)):
+        s = engine.superop(ch.kraus)
+        # trace of the output = trace of the input for every input
+        for r in range(4):
+            e = np.zeros(4)
+            e[r] = 1
+            out = (s @ e).reshape(2, 2)
+            assert abs(np.trace(out) - np.trace(e.reshape(2, 2))) < 1e-12
+    s = engine.depolarizing_superop(0.2, 1)
+    assert np.allclose(s, engine.superop(depolarizing(0.2).kraus), atol=1e-12)
+
+
+def test_count_bits_packs_like_orrery():
+    c = ls.parse("OPENQASM 3; qubit[3] q; bit[2] a; bit[1] b; a[1] = measure q[0]; b[0] = measure q[2];")
+    bits = np.array([[1, 0], [1, 1], [0, 0], [1, 1]], dtype=np.uint8)
+    from lucivant_sim_gb300.simulator import count_bits
+
+    assert count_bits(c, bits, [1, 2]) == {"0 00": 1, "0 10": 1, "1 10": 2}
+
+
+def test_pauli_masks():
+    assert engine.pauli_masks("XYZI") == (0b1100, 0b0110)
+
+
+def test_no_oracle_in_product():
+    """The product never imports the oracle (it is test infrastructure only)."""
+    for path in (ROOT / "lucivant_sim_gb300").rglob("*.py"):
+        text = path.read_text()
+        assert "import oracle" not in text and "from oracle" not in text, path
