@@ -1,0 +1,474 @@
+#!/usr/bin/env python3
+"""Benchmark: the batched noisy density-matrix hot path on one GB300 (per rank).
+
+Workload (one step): 256 noise instances of a 12-qubit, 12-layer u3+cx brickwork circuit (angles
+U[0, 2π) from seed 7), each with thermal relaxation (T1 = 120, T2 = 90, t = 0.05) composed with a
+depolarising one-qubit error ~ U[1e-4, 5e-3] on every u3, depolarising two-qubit error
+~ U[1e-3, 3e-2] on every cx, evolved as one 256-member register of vectorised density matrices
+(24-bit registers, 32 GiB in complex64), then the exact probabilities and the 23 observables
+<Z_i>, <Z_i Z_i+1> of every instance. Inputs are larger than L2 (no flush needed).
+
+metric: statevector HBM GB/s — algorithmic HBM bytes of the step (2 x register bytes per fused
+pass, one register write to reset, the reduction reads) per second, whole job. Beside it: the
+instances (circuits) per second, and the same circuit as a plain complex128 single-instance run on
+the same GPU ("plain_c128"), with the complex64 path's error against it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun each rank runs its own 256 instances on its own GPU (weak scaling, no data-path
+collective). ``--impl reference`` times the CPU port of Orrery's algorithm (the oracle) on the
+host cores instead, on rank 0 only.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+QUBITS, LAYERS, SEED, INSTANCES = 12, 12, 7, 256
+FALLBACK_HBM_GBS = 6800.0
+CPU_SAMPLE_U3, CPU_SAMPLE_CX = 4, 2  # oracle ops timed for the CPU baseline (about 10-15 s)
+REF_SAMPLE_U3, REF_SAMPLE_CX = 2, 1  # per worker per step in the reference arm
+
+
+def parse_args() -> argparse.Namespace:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--precision", choices=("c64", "c128"), default="c64")
+    ap.add_argument("--instances", type=int, default=INSTANCES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info() -> tuple[int, int, int]:
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max-over-ranks on the host (gloo) when launched by torchrun."""
+
+    def __init__(self, world: int) -> None:
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self) -> None:
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, value: float) -> float:
+        if self.world == 1:
+            return value
+        import torch
+
+        t = torch.tensor([value], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while running (SM clock, throttle reasons)."""
+
+    QUERY = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+        "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+        "clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu: int) -> None:
+        self.gpu = gpu
+        self.proc: subprocess.Popen | None = None
+
+    def start(self) -> None:
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)  # fmt: skip
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9], strict=True):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def measured_peak() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(precision: str) -> float | None:
+    """DRAM bytes per launch of the tile pass, from the committed ncu summary (scaled there to a
+    full-size launch), or None."""
+    path = ROOT / "profiles" / f"tile_pass_dm12_{precision}.md"
+    if not path.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", path.read_text())
+    return float(m.group(1)) if m else None
+
+
+def workload():
+    from lucivant_sim_gb300 import qasm, workloads as wl
+
+    circuit = qasm.parse(wl.brickwork(QUBITS, LAYERS, seed=SEED, measure=False))
+    return circuit, wl.z_observables(QUBITS)
+
+
+def bytes_per_instance(circuit, noises, precision: str) -> tuple[int, int]:
+    """(algorithmic HBM bytes per instance, fused passes) for one evolution plus reductions."""
+    from lucivant_sim_gb300 import _lib, engine
+
+    code = engine.precision_code(precision)
+    ops = engine.dm_oplist(circuit, noises[:1])
+    passes = _lib.plan_passes(2 * QUBITS, code, ops)
+    elt = 8 if precision == "c64" else 16
+    member = elt << (2 * QUBITS)
+    diag = (1 << QUBITS) * elt
+    # 2 x member per pass, 1 x member to reset, the diagonal read by probabilities and 23 Z terms
+    return 2 * member * passes + member + 24 * diag, passes
+
+
+# ------------------------------------------------------------------------------ CPU legs
+
+
+def _oracle_sample(args: tuple[int, int, int]) -> tuple[float, float]:
+    """Time the oracle on the first u3 and cx gate+channel operations of one instance; returns
+    the seconds per u3 operation and per cx operation."""
+    n_u3, n_cx, instance = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    import numpy as np
+
+    from lucivant_sim_gb300 import workloads as wl
+    from oracle import dense
+
+    circuit, _ = workload()
+    noise = wl.dm_noise_instances(INSTANCES, seed=SEED)[instance % INSTANCES]
+    n = QUBITS
+    rho = np.zeros(1 << (2 * n), dtype=np.complex128)
+    rho[0] = 1
+    gates = [op for op in circuit.operations if op.kind == "gate"]
+    u3 = [g for g in gates if len(g.qubits) == 1][:n_u3]
+    cx = [g for g in gates if len(g.qubits) == 2][:n_cx]
+    times = []
+    for group in (u3, cx):
+        t0 = time.perf_counter()
+        for op in group:
+            rho = dense.apply_bits(rho, 2 * n, op.matrix, [n + q for q in op.qubits])
+            rho = dense.apply_bits(rho, 2 * n, op.matrix.conj(), list(op.qubits))
+            ch = noise.gate_error(op.name, op.qubits)
+            if ch is not None:
+                rho = dense.dm_channel(rho, n, ch, op.qubits)
+        times.append((time.perf_counter() - t0) / max(len(group), 1))
+    return times[0], times[1]
+
+
+def _project(t_u3: float, t_cx: float, circuit) -> float:
+    gates = [op for op in circuit.operations if op.kind == "gate"]
+    n1 = sum(1 for g in gates if len(g.qubits) == 1)
+    return n1 * t_u3 + (len(gates) - n1) * t_cx
+
+
+def cpu_baseline(circuit, bytes_inst: int) -> dict:
+    """The oracle (a port of Orrery's algorithm) on one host thread, on a bounded sample."""
+    code = (
+        "import sys, json; sys.path.insert(0, %r); import bench; "
+        "print(json.dumps(bench._oracle_sample((%d, %d, 0))))" % (str(ROOT), CPU_SAMPLE_U3, CPU_SAMPLE_CX)
+    )
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    t0 = time.perf_counter()
+    proc = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    wall = time.perf_counter() - t0
+    if proc.returncode != 0:
+        return {"value": None, "unit": "GB/s", "error": proc.stderr.strip()[-300:]}
+    t_u3, t_cx = json.loads(proc.stdout.strip().splitlines()[-1])
+    per_circuit = _project(t_u3, t_cx, circuit)
+    return {
+        "value": bytes_inst / per_circuit / 1e9,
+        "unit": "GB/s",
+        "cores": 1,
+        "kind": "port",
+        "sample": f"oracle density-matrix evolution of instance 0: first {CPU_SAMPLE_U3} u3 and {CPU_SAMPLE_CX} cx "
+        f"gate+channel ops timed ({wall:.1f} s wall), projected to the full circuit "
+        f"({per_circuit:.1f} s per instance, {1 / per_circuit:.4f} circuits/s)",
+        "circuits_per_s": 1 / per_circuit,
+    }
+
+
+def reference_arm(args: argparse.Namespace) -> None:
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    circuit, _ = workload()
+    from lucivant_sim_gb300 import workloads as wl
+
+    noises = wl.dm_noise_instances(INSTANCES, seed=SEED)
+    bytes_inst, _ = bytes_per_instance(circuit, noises, args.precision)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"  # inherited by the spawned workers: one thread each
+    with ctx.Pool(cores) as pool:
+        jobs = [(REF_SAMPLE_U3, REF_SAMPLE_CX, i) for i in range(cores)]
+        for _ in range(args.warmup):
+            pool.map(_oracle_sample, jobs)
+        per_step, circuits = [], 0.0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_sample, jobs)
+            dt = time.perf_counter() - t0
+            # each worker did a fraction of one circuit: fraction = sampled time / projected time
+            frac = sum((REF_SAMPLE_U3 * a + REF_SAMPLE_CX * b) / _project(a, b, circuit) for a, b in res)
+            circuits += frac
+            per_step.append(dt)
+    elapsed = sum(per_step)
+    cps = circuits / elapsed
+    value = cps * bytes_inst / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "statevector HBM GB/s",
+        "value": value,
+        "unit": "GB/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000 * elapsed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c128",
+        "data": "synthetic",
+        "config": config_block(args),
+        "circuits_per_s": cps,
+        "cpu_baseline": {
+            "value": value,
+            "unit": "GB/s",
+            "cores": cores,
+            "kind": "port",
+            "sample": f"each step: {cores} processes, each evolving the first {REF_SAMPLE_U3} u3 and {REF_SAMPLE_CX} cx "
+            "gate+channel ops of one instance with the oracle; circuits = sampled fraction of the full circuit",
+        },
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_block(args: argparse.Namespace) -> dict:
+    return {
+        "workload": f"density_matrix {QUBITS}q x {LAYERS} brickwork layers, {args.instances} noise instances per GPU",
+        "qubits": QUBITS,
+        "layers": LAYERS,
+        "instances_per_gpu": args.instances,
+        "precision": args.precision,
+        "noise": "thermal_relaxation(120, 90, 0.05) composed with depolarising U[1e-4,5e-3] on u3; "
+        "depolarising U[1e-3,3e-2] on cx; readout 2e-2",
+        "outputs": "probabilities (2^12) and 23 Z observables per instance",
+        "l2": f"register {((8 if args.precision == 'c64' else 16) * args.instances << 24) / 2**30:.0f} GiB > L2: no flush",
+        "parallelism": f"replicas x{args.gpus} (independent instances per GPU)",
+    }
+
+
+# ------------------------------------------------------------------------------ GPU arm
+
+
+def gb300_arm(args: argparse.Namespace) -> None:
+    rank, world, local = dist_info()
+    dist = Dist(world)
+    import numpy as np
+    import torch
+
+    from lucivant_sim_gb300 import _lib, workloads as wl
+    from lucivant_sim_gb300.batch import DensityBatch, run_density_batch
+
+    _lib.set_device(local)
+    torch.cuda.set_device(local)
+    circuit, labels = workload()
+    noises = wl.dm_noise_instances(args.instances, seed=SEED + rank)
+    bytes_inst, passes = bytes_per_instance(circuit, noises, args.precision)
+    bytes_step = bytes_inst * args.instances
+
+    batch = DensityBatch(circuit, noises, precision=args.precision)
+    assert batch.program.passes == passes
+    stream = torch.cuda.ExternalStream(batch.reg.stream())
+
+    def step(timed: list | None = None) -> tuple:
+        if timed is None:
+            batch.evolve()
+        else:
+            timed.append(batch.evolve_timed())
+        return batch.expectations(labels), batch.probabilities()
+
+    for _ in range(args.warmup):
+        step()
+    batch.reg.sync()
+    dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    pass_ms: list = []
+    torch.cuda.synchronize()
+    t_start.record(stream)
+    for _ in range(args.steps):
+        exps, probs = step(pass_ms)
+    t_end.record(stream)
+    t_end.synchronize()
+    batch.reg.sync()
+    clock_info = clocks.stop()
+    dist.barrier()
+    elapsed = dist.max(t_start.elapsed_time(t_end) / 1000.0)
+    value = bytes_step * args.steps * world / elapsed / 1e9
+    cps = args.instances * args.steps * world / elapsed
+    launches_per_step = 1 + passes + 2 + args.instances  # reset, passes, expectation (2), probabilities per member
+
+    all_pass = np.concatenate(pass_ms)
+    avg_launch_s = float(all_pass.mean()) / 1000.0
+    launch_bytes = 2 * batch.register_bytes
+    peak, peak_kind = measured_peak()
+    achieved = launch_bytes / avg_launch_s / 1e9
+    traffic = ncu_traffic(args.precision)
+    roofline = {
+        "kernel": f"k_tile_pass<{'float' if args.precision == 'c64' else 'double'}>",
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+        "traffic": traffic,
+        "bytes_per_launch": launch_bytes,
+        "avg_launch_ms": avg_launch_s * 1000,
+        "launches": int(all_pass.size),
+        "share_of_step": float(all_pass.sum()) / 1000.0 / (elapsed / 1.0) if world == 1 else None,
+    }
+
+    # plain complex128 path on the same GPU: one instance at a time (instance 0)
+    plain = DensityBatch(circuit, noises[:1], precision="c128")
+    for _ in range(2):
+        plain.evolve()
+        plain.expectations(labels)
+        p_ref = plain.probabilities()
+    plain.reg.sync()
+    reps = max(3, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        plain.evolve()
+        e_ref = plain.expectations(labels)
+        p_ref = plain.probabilities()
+    plain.reg.sync()
+    plain_s = (time.perf_counter() - t0) / reps
+    plain.free()
+    tvd = 0.5 * float(np.abs(probs[0] - p_ref[0]).sum())
+    exp_err = float(np.max(np.abs(exps[:, 0] - e_ref[:, 0])))
+
+    # end to end through the public batched API: host inputs in, host results out, every step
+    e2e_steps = max(2, args.steps // 2)
+    batch.free()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        probs_h, exps_h = run_density_batch(circuit, noises, labels, precision=args.precision)
+    e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
+    from lucivant_sim_gb300 import engine
+
+    ops = engine.dm_oplist(circuit, noises)
+    h2d = int(ops.size * 16 + len(ops) * _lib.OP_DTYPE.itemsize + 2 * 8 * len(labels))
+    d2h = int(probs_h.nbytes + exps_h.nbytes)
+
+    if rank == 0:
+        line = {
+            "metric": "statevector HBM GB/s",
+            "value": value,
+            "unit": "GB/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": 1000 * elapsed / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": args.precision,
+            "data": "synthetic",
+            "config": config_block(args),
+            "circuits_per_s": cps,
+            "fused_passes": passes,
+            "plain_c128": {
+                "circuits_per_s": world / plain_s,
+                "ms_per_circuit": 1000 * plain_s,
+                "speedup_of_batched": cps / (world / plain_s),
+            },
+            "accuracy": {"probability_tvd_vs_c128": tvd, "max_expectation_error_vs_c128": exp_err},
+            "roofline": roofline,
+            "e2e": {
+                "value": bytes_step * world / e2e_s / 1e9,
+                "unit": "GB/s",
+                "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "circuits_per_s": args.instances * world / e2e_s,
+                "api": "lucivant_sim_gb300.batch.run_density_batch",
+            },
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clock_info,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(circuit, bytes_inst)
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main() -> None:
+    args = parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gb300_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -86,9 +86,33 @@ int lsg_state_bytes(lsg_state s, int64_t* out);
  * (re, im) pairs; complex64 registers round it once. */
 int lsg_apply(lsg_state s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries);
 
+/* ---- programs: planned, uploaded operator lists ---------------------------------------------
+ * lsg_program_create plans and uploads `ops` once for registers shaped like `shape` (same bits,
+ * precision and batch); lsg_program_run then enqueues the passes on the register's stream without
+ * any host synchronisation, so a circuit template is launched repeatedly (and can be captured
+ * in a CUDA graph) at kernel-launch cost. The complex64 pool is rounded once at creation. */
+typedef struct lsg_program_s* lsg_program;
+int lsg_program_create(lsg_state shape, const lsg_op* ops, int32_t nops, const double* pool,
+                       int64_t pool_entries, lsg_program* out);
+int lsg_program_run(lsg_program p, lsg_state s);
+/* Run once with CUDA events around every pass (on the register's stream) and wait: pass_ms gets
+ * one device time per pass, in milliseconds. */
+int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms);
+/* Number of fused passes, and algorithmic HBM bytes of one run (2 x register bytes per pass). */
+int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run);
+int lsg_program_free(lsg_program p);
+/* Host-only: the number of fused passes lsg_apply would run for these operators on a register of
+ * nbits bits (no device is touched; used for sizing and for algorithmic-byte accounting). */
+int lsg_plan(int nbits, int precision, const lsg_op* ops, int32_t nops, int32_t* passes);
+/* Wait for the register's queued work; reports a device-side timeout if one occurred. */
+int lsg_state_sync(lsg_state s);
+/* The register's CUDA stream (a cudaStream_t), for callers that order their own work after it. */
+int lsg_state_stream(lsg_state s, void** stream);
+
 /* ---- reductions (FP64 accumulation for both precisions) -------------------------------------
  * Probabilities of member `member`: |a|^2 for a statevector register (dm_qubits = 0), the
- * clipped real diagonal for a density register of dm_qubits qubits. out has 2^n doubles.
+ * clipped real diagonal for a density register of dm_qubits qubits. out has 2^n doubles; with
+ * member < 0 it gets every member's, one after another (batch x 2^n).
  * Replaces Statevector.probabilities / DensityMatrix.probabilities (engines.py:207-209, :257-260). */
 int lsg_probabilities(lsg_state s, int dm_qubits, int64_t member, double* out);
 

@@ -62,12 +62,29 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_sample": (C.c_int, [_P, C.c_int, _I64, _PI32, _I32, _PD, _I64, _I32, _PI32, _PI32, _PD, _PD, _PD, _PU8, _PU8, _PI64]),
     "lsg_expect_pauli": (C.c_int, [_P, C.c_int, _PU64, _PU64, _I32, _PD]),
     "lsg_prob_one": (C.c_int, [_P, C.c_int, _I64, _PD]),
+    "lsg_program_create": (C.c_int, [_P, _P, _I32, _PD, _I64, C.POINTER(_P)]),
+    "lsg_program_run": (C.c_int, [_P, _P]),
+    "lsg_program_run_timed": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
+    "lsg_program_info": (C.c_int, [_P, _PI32, _PI64]),
+    "lsg_program_free": (C.c_int, [_P]),
+    "lsg_plan": (C.c_int, [C.c_int, C.c_int, _P, _I32, _PI32]),
+    "lsg_state_sync": (C.c_int, [_P]),
+    "lsg_state_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lsg_collapse": (C.c_int, [_P, C.c_int, C.c_int, _D, _I64]),
 }
 
 _lib: C.CDLL | None = None
 _lock = threading.Lock()
 _initialised: set[int] = set()
+_default_device = 0
+
+
+def set_device(device: int) -> None:
+    """The device new registers go to (one process drives one GPU; ranks pick theirs)."""
+    global _default_device
+    _default_device = int(device)
+    _initialised.discard(_default_device)
+    ensure_device(_default_device)
 
 
 def library() -> C.CDLL:
@@ -104,10 +121,20 @@ def check(code: int) -> None:
     raise EngineError(f"engine error {code}: {msg}")
 
 
-def ensure_device(device: int = 0) -> None:
-    if device not in _initialised:
-        check(library().lsg_init(device))
-        _initialised.add(device)
+def ensure_device(device: int | None = None) -> None:
+    dev = _default_device if device is None else device
+    if dev not in _initialised:
+        check(library().lsg_init(dev))
+        _initialised.clear()
+        _initialised.add(dev)
+
+
+def plan_passes(nbits: int, precision: int, ops: "OpList") -> int:
+    """Fused passes the engine plans for ``ops`` (host only, no device)."""
+    table, _ = ops.packed()
+    out = C.c_int32(0)
+    check(library().lsg_plan(nbits, precision, table.ctypes.data, len(table), C.byref(out)))
+    return int(out.value)
 
 
 def ptr(a: np.ndarray, ctype: Any) -> Any:
@@ -156,7 +183,7 @@ class OpList:
 class Register:
     """A device register of ``batch`` members of 2^nbits amplitudes."""
 
-    def __init__(self, nbits: int, precision: int = C128, batch: int = 1, device: int = 0) -> None:
+    def __init__(self, nbits: int, precision: int = C128, batch: int = 1, device: int | None = None) -> None:
         ensure_device(device)
         self.lib = library()
         self.nbits, self.precision, self.batch = nbits, precision, batch
@@ -200,10 +227,12 @@ class Register:
         check(self.lib.lsg_state_upload(self.handle, ptr(a.view(np.float64), C.c_double), a.nbytes))
 
     def probabilities(self, dm_qubits: int = 0, member: int = 0) -> np.ndarray:
+        """One member's probabilities, or every member's (shape (batch, 2^n)) when member < 0."""
         n = dm_qubits if dm_qubits else self.nbits
-        out = np.empty(1 << n, dtype=np.float64)
+        rows = self.batch if member < 0 else 1
+        out = np.empty(rows << n, dtype=np.float64)
         check(self.lib.lsg_probabilities(self.handle, dm_qubits, member, ptr(out, C.c_double)))
-        return out
+        return out.reshape(self.batch, -1) if member < 0 else out
 
     def sample(
         self,
@@ -252,7 +281,51 @@ class Register:
     def collapse(self, qubit: int, outcome: int, probability: float, member: int = 0) -> None:
         check(self.lib.lsg_collapse(self.handle, qubit, outcome, probability, member))
 
+    def sync(self) -> None:
+        check(self.lib.lsg_state_sync(self.handle))
+
+    def stream(self) -> int:
+        """The register's CUDA stream handle (an integer cudaStream_t)."""
+        out = C.c_void_p()
+        check(self.lib.lsg_state_stream(self.handle, C.byref(out)))
+        return int(out.value or 0)
+
     def device_bytes(self) -> int:
         out = C.c_int64(0)
         check(self.lib.lsg_state_bytes(self.handle, C.byref(out)))
         return int(out.value)
+
+
+class Program:
+    """A planned, uploaded operator list for registers shaped like ``shape``: run it repeatedly
+    without re-planning, re-uploading or synchronising."""
+
+    def __init__(self, shape: Register, ops: OpList) -> None:
+        self.lib = library()
+        table, pool = ops.packed()
+        handle = C.c_void_p()
+        check(self.lib.lsg_program_create(shape.handle, table.ctypes.data, len(table), ptr(pool, C.c_double),
+                                          pool.size // 2, C.byref(handle)))  # fmt: skip
+        self.handle = handle
+        passes, nbytes = C.c_int32(0), C.c_int64(0)
+        check(self.lib.lsg_program_info(handle, C.byref(passes), C.byref(nbytes)))
+        self.passes, self.bytes_per_run = int(passes.value), int(nbytes.value)
+
+    def run(self, reg: Register) -> None:
+        check(self.lib.lsg_program_run(self.handle, reg.handle))
+
+    def run_timed(self, reg: Register) -> np.ndarray:
+        out = np.zeros(max(self.passes, 1), dtype=np.float32)
+        check(self.lib.lsg_program_run_timed(self.handle, reg.handle, ptr(out, C.c_float)))
+        return out[: self.passes]
+
+    def free(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.lsg_program_free(self.handle)
+            self.handle = None
+
+    def __del__(self) -> None:
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -1,0 +1,70 @@
+"""Batched execution: one circuit template, many instances, one register.
+
+Noise-parameter instances (or shots, or repeated runs) of one circuit share every pass: the
+register holds ``batch`` members contiguously and each operator carries per-member data where
+the instances differ, so a pass over all members is one kernel launch. The template is planned
+and uploaded once (:class:`~lucivant_sim_gb300._lib.Program`) and re-run without host
+synchronisation.
+"""
+
+from __future__ import annotations
+
+from typing import Any
+
+import numpy as np
+
+from lucivant_sim_gb300 import _lib, engine
+from lucivant_sim_gb300.engine import pauli_masks
+
+
+class DensityBatch:
+    """``len(noises)`` noisy density-matrix instances of one static circuit."""
+
+    def __init__(self, circuit: Any, noises: list[Any], precision: str | None = "c64") -> None:
+        if circuit.is_dynamic():
+            raise engine.SimulationError("a density matrix needs a circuit without mid-circuit measurement or conditions")
+        self.circuit = circuit
+        self.n = circuit.num_qubits
+        self.batch = len(noises)
+        self.reg = engine.new_density(self.n, engine.precision_code(precision), self.batch)
+        self.ops = engine.dm_oplist(circuit, noises)
+        self.program = _lib.Program(self.reg, self.ops)
+        self.upload_bytes = int(self.ops.size * 16 + len(self.ops) * _lib.OP_DTYPE.itemsize)
+
+    @property
+    def register_bytes(self) -> int:
+        return (8 if self.reg.precision == _lib.C64 else 16) * self.batch << (2 * self.n)
+
+    def evolve(self) -> None:
+        """Reset every member to |0><0| and run the circuit (queued; returns before completion)."""
+        self.reg.set_basis(0)
+        self.program.run(self.reg)
+
+    def evolve_timed(self) -> np.ndarray:
+        """As :meth:`evolve`, returning each fused pass's device time in ms."""
+        self.reg.set_basis(0)
+        return self.program.run_timed(self.reg)
+
+    def probabilities(self) -> np.ndarray:
+        """(batch, 2^n) exact probabilities."""
+        return self.reg.probabilities(self.n, member=-1)
+
+    def expectations(self, labels: list[str]) -> np.ndarray:
+        """(terms, batch) Pauli expectations."""
+        masks = [pauli_masks(lab) for lab in labels]
+        return self.reg.expect(self.n, [m[0] for m in masks], [m[1] for m in masks])
+
+    def free(self) -> None:
+        self.program.free()
+        self.reg.free()
+
+
+def run_density_batch(circuit: Any, noises: list[Any], observables: list[str], precision: str | None = "c64"):
+    """One call from host inputs to host results: probabilities (batch, 2^n) and expectations
+    (terms, batch) of every noise instance."""
+    b = DensityBatch(circuit, noises, precision)
+    try:
+        b.evolve()
+        return b.probabilities(), b.expectations(observables)
+    finally:
+        b.free()

@@ -83,11 +83,6 @@ void release(Scratch& s) {
 
 // ------------------------------------------------------------------------ tile kernel
 
-template <typename R>
-struct Smem {
-    // Cx<R> tile[1 << K] follows in dynamic shared memory
-};
-
 // Deposit the bits of x into the register positions listed in pos[0..n) (ascending).
 __device__ __forceinline__ uint64_t deposit(uint64_t x, const int* pos, int n) {
     uint64_t out = 0;
@@ -95,65 +90,125 @@ __device__ __forceinline__ uint64_t deposit(uint64_t x, const int* pos, int n) {
     return out;
 }
 
-template <typename R, int KB>
-__device__ __forceinline__ void op_matrix(Cx<R>* tile, int tbits, const TileOp& op, const Cx<R>* m) {
-    constexpr int D = 1 << KB;
-    uint64_t offs[D];
-#pragma unroll
-    for (int j = 0; j < D; ++j) {
-        uint64_t o = 0;
-#pragma unroll
-        for (int i = 0; i < KB; ++i) o |= (uint64_t)((j >> (KB - 1 - i)) & 1) << op.lb[i];
-        offs[j] = o;
-    }
-    const int groups = 1 << (tbits - KB);
+// Insert a zero bit at position b.
+__device__ __forceinline__ uint32_t ins0(uint32_t g, int b) {
+    const uint32_t low = g & ((1u << b) - 1);
+    return ((g >> b) << (b + 1)) | low;
+}
+
+template <typename R>
+__device__ __forceinline__ Cx<R> ldm(const Cx<R>* m, int i) {
+    return m[i];
+}
+
+// 1-bit dense: the common case (fused one-qubit gates; one-qubit density superoperators use 2).
+template <typename R>
+__device__ __forceinline__ void dense1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
+    const Cx<R> m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+    const int groups = 1 << (tbits - 1);
     for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        uint64_t base = spread((uint64_t)g, op.sorted, KB);
-        Cx<R> v[D];
+        const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
+        const Cx<R> a0 = t[i0], a1 = t[i1];
+        t[i0] = cfma(m01, a1, cmul(m00, a0));
+        t[i1] = cfma(m11, a1, cmul(m10, a0));
+    }
+}
+
+// 2-bit dense on (hi_bit = matrix MSB b0, b1); lo/hi are the sorted positions.
+template <typename R>
+__device__ __forceinline__ void dense2(Cx<R>* t, int tbits, int b0, int b1, const Cx<R>* m) {
+    const int lo = min(b0, b1), hi = max(b0, b1);
+    const uint32_t o1 = 1u << b1, o2 = 1u << b0;
+    const int groups = 1 << (tbits - 2);
+    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+        const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
+        const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
 #pragma unroll
-        for (int j = 0; j < D; ++j) v[j] = tile[base | offs[j]];
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            Cx<R> acc;
-#pragma unroll
-            for (int c = 0; c < D; ++c) acc = cfma(m[r * D + c], v[c], acc);
-            tile[base | offs[r]] = acc;
+        for (int r = 0; r < 4; ++r) {
+            Cx<R> acc = cmul(ldm(m, 4 * r), v0);
+            acc = cfma(ldm(m, 4 * r + 1), v1, acc);
+            acc = cfma(ldm(m, 4 * r + 2), v2, acc);
+            acc = cfma(ldm(m, 4 * r + 3), v3, acc);
+            const uint32_t at = base | ((r & 1) ? o1 : 0u) | ((r & 2) ? o2 : 0u);
+            t[at] = acc;
         }
     }
 }
 
-template <typename R, int KB>
-__device__ __forceinline__ void op_perm(Cx<R>* tile, int tbits, const TileOp& op, const Cx<R>* m) {
-    constexpr int D = 1 << KB;
-    uint64_t offs[D];
-    int src[D];
-    Cx<R> ph[D];
-#pragma unroll
-    for (int j = 0; j < D; ++j) {
-        uint64_t o = 0;
-#pragma unroll
-        for (int i = 0; i < KB; ++i) o |= (uint64_t)((j >> (KB - 1 - i)) & 1) << op.lb[i];
-        offs[j] = o;
-        ph[j] = m[j];
-        src[j] = (int)m[D + j].re;
-    }
-    const int groups = 1 << (tbits - KB);
+template <typename R>
+__device__ __forceinline__ Cx<R> pick4(const Cx<R>& v0, const Cx<R>& v1, const Cx<R>& v2, const Cx<R>& v3, int s) {
+    const Cx<R> a = (s & 1) ? v1 : v0;
+    const Cx<R> b = (s & 1) ? v3 : v2;
+    return (s & 2) ? b : a;
+}
+
+// permutations with phases on 1 or 2 bits (x, cx, swap and their phased forms)
+template <typename R>
+__device__ __forceinline__ void perm1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
+    const Cx<R> p0 = m[0], p1 = m[1];
+    const int s0 = (int)m[2].re;
+    const int groups = 1 << (tbits - 1);
     for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        uint64_t base = spread((uint64_t)g, op.sorted, KB);
-        Cx<R> v[D];
-#pragma unroll
-        for (int j = 0; j < D; ++j) v[j] = tile[base | offs[j]];
-#pragma unroll
-        for (int r = 0; r < D; ++r) tile[base | offs[r]] = cmul(ph[r], v[src[r]]);
+        const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
+        const Cx<R> a0 = t[i0], a1 = t[i1];
+        t[i0] = cmul(p0, s0 ? a1 : a0);
+        t[i1] = cmul(p1, s0 ? a0 : a1);
     }
 }
 
 template <typename R>
-__device__ __forceinline__ void op_diag(Cx<R>* tile, int tbits, const TileOp& op, const Cx<R>* m) {
+__device__ __forceinline__ void perm2(Cx<R>* t, int tbits, int b0, int b1, const Cx<R>* m) {
+    const int lo = min(b0, b1), hi = max(b0, b1);
+    const uint32_t o1 = 1u << b1, o2 = 1u << b0;
+    const Cx<R> p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
+    const int s0 = (int)m[4].re, s1 = (int)m[5].re, s2 = (int)m[6].re, s3 = (int)m[7].re;
+    const int groups = 1 << (tbits - 2);
+    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+        const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
+        const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
+        t[base] = cmul(p0, pick4(v0, v1, v2, v3, s0));
+        t[base | o1] = cmul(p1, pick4(v0, v1, v2, v3, s1));
+        t[base | o2] = cmul(p2, pick4(v0, v1, v2, v3, s2));
+        t[base | o1 | o2] = cmul(p3, pick4(v0, v1, v2, v3, s3));
+    }
+}
+
+// Wide operators (3 to 5 bits): rare (Toffoli-class gates, two-qubit Kraus superoperators), kept
+// out of line so their register needs don't shape the common path.
+template <typename R>
+__device__ __noinline__ void wide_op(Cx<R>* t, int tbits, int kind, int k, const int* lb, const int* sorted,
+                                     const Cx<R>* m) {
+    const int D = 1 << k;
+    uint32_t offs[32];
+    Cx<R> v[32];
+    for (int j = 0; j < D; ++j) {
+        uint32_t o = 0;
+        for (int i = 0; i < k; ++i) o |= (uint32_t)((j >> (k - 1 - i)) & 1) << lb[i];
+        offs[j] = o;
+    }
+    const int groups = 1 << (tbits - k);
+    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+        uint32_t base = (uint32_t)g;
+        for (int i = 0; i < k; ++i) base = ins0(base, sorted[i]);
+        for (int j = 0; j < D; ++j) v[j] = t[base | offs[j]];
+        if (kind == LSG_OP_MATRIX) {
+            for (int r = 0; r < D; ++r) {
+                Cx<R> acc;
+                for (int c = 0; c < D; ++c) acc = cfma(m[r * D + c], v[c], acc);
+                t[base | offs[r]] = acc;
+            }
+        } else {
+            for (int r = 0; r < D; ++r) t[base | offs[r]] = cmul(m[r], v[(int)m[D + r].re]);
+        }
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void op_diag(Cx<R>* tile, int tbits, int k, const int* lb, const Cx<R>* m) {
     const int n = 1 << tbits;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         int j = 0;
-        for (int b = 0; b < op.k; ++b) j = (j << 1) | ((i >> op.lb[b]) & 1);
+        for (int b = 0; b < k; ++b) j = (j << 1) | ((i >> lb[b]) & 1);
         tile[i] = cmul(m[j], tile[i]);
     }
 }
@@ -165,42 +220,49 @@ __device__ __forceinline__ void op_scale(Cx<R>* tile, int tbits, const Cx<R>* m)
     for (int i = threadIdx.x; i < n; i += blockDim.x) tile[i] = cmul(f, tile[i]);
 }
 
-// (1-p) rho + (p/d) I (x) Tr_t(rho): k row bits then k column bits (k = 1 or 2).
+// (1-p) rho + (p/d) I (x) Tr_t(rho) on kq row bits then kq column bits (kq = 1 or 2).
 template <typename R, int KQ>
-__device__ __forceinline__ void op_depol(Cx<R>* tile, int tbits, const TileOp& op, const Cx<R>* m) {
+__device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, const int* sorted, const Cx<R>* m) {
     constexpr int KB = 2 * KQ;
     constexpr int D = 1 << KB;
     constexpr int d = 1 << KQ;
-    uint64_t offs[D];
+    int l[KB], srt[KB];
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-        uint64_t o = 0;
-#pragma unroll
-        for (int i = 0; i < KB; ++i) o |= (uint64_t)((j >> (KB - 1 - i)) & 1) << op.lb[i];
-        offs[j] = o;
+    for (int i = 0; i < KB; ++i) {
+        l[i] = lb[i];
+        srt[i] = sorted[i];
     }
     const R p = m[0].re;
     const R keep = R(1) - p;
     const R share = p / R(d);
     const int groups = 1 << (tbits - KB);
     for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        uint64_t base = spread((uint64_t)g, op.sorted, KB);
+        uint32_t base = (uint32_t)g;
+#pragma unroll
+        for (int i = 0; i < KB; ++i) base = ins0(base, srt[i]);
         Cx<R> tr;
 #pragma unroll
-        for (int t = 0; t < d; ++t) {
-            Cx<R> v = tile[base | offs[(t << KQ) | t]];
+        for (int s = 0; s < d; ++s) {
+            const int j = (s << KQ) | s;
+            uint32_t o = 0;
+#pragma unroll
+            for (int i = 0; i < KB; ++i) o |= (uint32_t)((j >> (KB - 1 - i)) & 1) << l[i];
+            const Cx<R> v = t[base | o];
             tr.re += v.re;
             tr.im += v.im;
         }
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-            Cx<R> v = tile[base | offs[j]];
-            Cx<R> o(v.re * keep, v.im * keep);
+            uint32_t o = 0;
+#pragma unroll
+            for (int i = 0; i < KB; ++i) o |= (uint32_t)((j >> (KB - 1 - i)) & 1) << l[i];
+            const Cx<R> v = t[base | o];
+            Cx<R> out(v.re * keep, v.im * keep);
             if ((j >> KQ) == (j & (d - 1))) {
-                o.re += share * tr.re;
-                o.im += share * tr.im;
+                out.re += share * tr.re;
+                out.im += share * tr.im;
             }
-            tile[base | offs[j]] = o;
+            t[base | o] = out;
         }
     }
 }
@@ -209,37 +271,27 @@ template <typename R>
 __device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, int nops,
                         const Cx<R>* __restrict__ data, int64_t member) {
     for (int o = 0; o < nops; ++o) {
-        TileOp op = ops[o];
+        const TileOp& op = ops[o];  // staged in shared memory
+        const int kind = op.kind, k = op.k;
         const Cx<R>* m = data + op.data + member * op.stride;
         __syncthreads();
-        switch (op.kind) {
-            case LSG_OP_MATRIX:
-                switch (op.k) {
-                    case 1: op_matrix<R, 1>(tile, tbits, op, m); break;
-                    case 2: op_matrix<R, 2>(tile, tbits, op, m); break;
-                    case 3: op_matrix<R, 3>(tile, tbits, op, m); break;
-                    case 4: op_matrix<R, 4>(tile, tbits, op, m); break;
-                    case 5: op_matrix<R, 5>(tile, tbits, op, m); break;
-                    default: break;
-                }
-                break;
-            case LSG_OP_PERM:
-                switch (op.k) {
-                    case 1: op_perm<R, 1>(tile, tbits, op, m); break;
-                    case 2: op_perm<R, 2>(tile, tbits, op, m); break;
-                    case 3: op_perm<R, 3>(tile, tbits, op, m); break;
-                    case 4: op_perm<R, 4>(tile, tbits, op, m); break;
-                    case 5: op_perm<R, 5>(tile, tbits, op, m); break;
-                    default: break;
-                }
-                break;
-            case LSG_OP_DIAG: op_diag<R>(tile, tbits, op, m); break;
-            case LSG_OP_DEPOL:
-                if (op.k == 2) op_depol<R, 1>(tile, tbits, op, m);
-                else op_depol<R, 2>(tile, tbits, op, m);
-                break;
-            case LSG_OP_SCALE: op_scale<R>(tile, tbits, m); break;
-            default: break;
+        if (kind == LSG_OP_MATRIX && k == 1) {
+            dense1<R>(tile, tbits, op.lb[0], m);
+        } else if (kind == LSG_OP_MATRIX && k == 2) {
+            dense2<R>(tile, tbits, op.lb[0], op.lb[1], m);
+        } else if (kind == LSG_OP_PERM && k == 1) {
+            perm1<R>(tile, tbits, op.lb[0], m);
+        } else if (kind == LSG_OP_PERM && k == 2) {
+            perm2<R>(tile, tbits, op.lb[0], op.lb[1], m);
+        } else if (kind == LSG_OP_DIAG) {
+            op_diag<R>(tile, tbits, k, op.lb, m);
+        } else if (kind == LSG_OP_DEPOL) {
+            if (k == 2) op_depol<R, 1>(tile, tbits, op.lb, op.sorted, m);
+            else op_depol<R, 2>(tile, tbits, op.lb, op.sorted, m);
+        } else if (kind == LSG_OP_SCALE) {
+            op_scale<R>(tile, tbits, m);
+        } else {
+            wide_op<R>(tile, tbits, kind, k, op.lb, op.sorted, m);
         }
     }
     __syncthreads();
@@ -248,7 +300,7 @@ __device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, 
 // One fused pass over every tile of every member. Tiles are visited grid-stride; each CTA
 // handles one tile at a time (CTAs co-resident on an SM overlap each other's copies).
 template <typename R>
-__global__ void __launch_bounds__(256) k_tile_pass(Cx<R>* __restrict__ state, int64_t member_elems,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) k_tile_pass(Cx<R>* __restrict__ state, int64_t member_elems,
                                                    const PassDesc* __restrict__ pass_g,
                                                    const TileOp* __restrict__ ops,
                                                    const Cx<R>* __restrict__ data, int64_t tiles_per_member,
@@ -257,7 +309,16 @@ __global__ void __launch_bounds__(256) k_tile_pass(Cx<R>* __restrict__ state, in
     __shared__ uint64_t bar;
     __shared__ PassDesc pd;
     Cx<R>* tile = reinterpret_cast<Cx<R>*>(smem_raw);
+    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + (sizeof(Cx<R>) << pass_g->K));
     if (threadIdx.x == 0) pd = *pass_g;
+    {
+        // stage this pass's operators in shared memory (the same for every tile of the pass)
+        const int nops = pass_g->nops;
+        const int* src = reinterpret_cast<const int*>(ops + pass_g->first_op);
+        int* dst = reinterpret_cast<int*>(sops);
+        const int words = nops * (int)(sizeof(TileOp) / sizeof(int));
+        for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    }
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -293,7 +354,7 @@ __global__ void __launch_bounds__(256) k_tile_pass(Cx<R>* __restrict__ state, in
             }
         }
         // ---- compute
-        run_ops<R>(tile, K, ops + pd.first_op, pd.nops, data, member);
+        run_ops<R>(tile, K, sops, pd.nops, data, member);
         // ---- store
         if (use_bulk) {
             fence_proxy_async_smem();
@@ -422,97 +483,168 @@ static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L) {
     return plan;
 }
 
-int tile_bits_for(const lsg_state_s* s) {
-    int K = s->precision == LSG_C128 ? 10 : 11;
+// ------------------------------------------------------------------------ programs
+
+int tile_bits_for(int nbits, int precision) {
+    int K = precision == LSG_C128 ? 10 : 11;
     if (const char* env = getenv("LSG_TILE_BITS")) K = atoi(env);
-    return std::max(0, std::min(K, s->nbits));
+    return std::max(0, std::min(K, nbits));
 }
 
 // Register bits every tile keeps: 2^L contiguous amplitudes = 512 bytes per copy.
-int low_bits_for(const lsg_state_s* s) {
-    int L = s->precision == LSG_C128 ? 5 : 6;
+int low_bits_for(int nbits, int precision) {
+    int L = precision == LSG_C128 ? 5 : 6;
     if (const char* env = getenv("LSG_LOW_BITS")) L = atoi(env);
-    return std::max(0, std::min(L, s->nbits));
+    return std::max(0, std::min(L, nbits));
 }
 
-template <typename R>
-static int launch_passes(lsg_state_s* s, const Plan& plan, const void* pool_dev) {
-    const int K = plan.passes.empty() ? 0 : plan.passes[0].K;
-    const size_t smem = sizeof(Cx<R>) << K;
-    auto kern = k_tile_pass<R>;
-    if (smem > 48 * 1024) LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t tiles_per_member = 1ll << (s->nbits - K);
-    const int64_t total = tiles_per_member * s->batch;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
-    int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
-    int* status = device_status();
-    if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
-    const PassDesc* pd_dev = reinterpret_cast<const PassDesc*>(s->program.ptr);
-    const TileOp* ops_dev = reinterpret_cast<const TileOp*>(pd_dev + plan.passes.size());
-    for (size_t p = 0; p < plan.passes.size(); ++p) {
-        kern<<<(unsigned)grid, 256, smem, s->stream>>>(reinterpret_cast<Cx<R>*>(s->data), s->elems, pd_dev + p,
-                                                        ops_dev, reinterpret_cast<const Cx<R>*>(pool_dev),
-                                                        tiles_per_member, total, status);
-    }
-    LSG_CUDA(cudaGetLastError());
-    return LSG_OK;
-}
-
-int apply_ops(lsg_state_s* s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries) {
+static int validate_ops(int nbits, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                        int64_t pool_entries) {
     if (nops < 0 || (nops > 0 && !ops) || pool_entries < 0 || (pool_entries > 0 && !pool))
-        return fail(LSG_E_ARG, "lsg_apply: bad operator list or pool");
+        return fail(LSG_E_ARG, "bad operator list or pool");
     for (int i = 0; i < nops; ++i) {
         const lsg_op& op = ops[i];
-        if (!op_bits_ok(op, s->nbits)) return fail(LSG_E_ARG, "lsg_apply: operator %d has bad kind or bits", i);
+        if (!op_bits_ok(op, nbits)) return fail(LSG_E_ARG, "operator %d has a bad kind or bits", i);
         int64_t need = 1;
         const int64_t d = 1ll << (op.kind == LSG_OP_DEPOL ? 0 : op.nbits);
         if (op.kind == LSG_OP_MATRIX) need = d * d;
         else if (op.kind == LSG_OP_DIAG) need = d;
         else if (op.kind == LSG_OP_PERM) need = 2 * d;
-        int64_t last = op.data + need + (s->batch - 1) * op.batch_stride;
+        const int64_t last = op.data + need + (batch - 1) * op.batch_stride;
         if (op.data < 0 || op.batch_stride < 0 || last > pool_entries)
-            return fail(LSG_E_ARG, "lsg_apply: operator %d reads outside the pool", i);
+            return fail(LSG_E_ARG, "operator %d reads outside the pool", i);
         if (op.kind == LSG_OP_PERM) {
-            for (int64_t b = 0; b < s->batch; ++b)
+            for (int64_t b = 0; b < batch; ++b)
                 for (int64_t r = 0; r < d; ++r) {
-                    double srcv = pool[2 * (op.data + b * op.batch_stride + d + r)];
-                    if (!(srcv >= 0 && srcv < (double)d) || srcv != (double)(int64_t)srcv)
-                        return fail(LSG_E_ARG, "lsg_apply: operator %d has a bad permutation", i);
+                    const double src = pool[2 * (op.data + b * op.batch_stride + d + r)];
+                    if (!(src >= 0 && src < (double)d) || src != (double)(int64_t)src)
+                        return fail(LSG_E_ARG, "operator %d has a bad permutation", i);
                 }
         }
     }
-    if (nops == 0) return LSG_OK;
-    const int K = tile_bits_for(s);
-    const int L = std::min(K, low_bits_for(s));
-    Plan plan = plan_passes(ops, nops, s->nbits, K, L);
-    if (plan.passes.empty())
-        return fail(LSG_E_ARG, "lsg_apply: an operator does not fit a tile of %d bits (%d kept low)", K, L);
-    // upload: pass descriptors, tile ops, then the pool in the register's precision
-    const size_t head = plan.passes.size() * sizeof(PassDesc) + plan.ops.size() * sizeof(TileOp);
-    const size_t head_aligned = (head + 255) & ~size_t(255);
-    const size_t elt = s->precision == LSG_C128 ? 16 : 8;
-    const size_t total = head_aligned + (size_t)pool_entries * elt;
-    std::vector<unsigned char> blob(total);
-    std::memcpy(blob.data(), plan.passes.data(), plan.passes.size() * sizeof(PassDesc));
-    std::memcpy(blob.data() + plan.passes.size() * sizeof(PassDesc), plan.ops.data(),
-                plan.ops.size() * sizeof(TileOp));
-    if (s->precision == LSG_C128) {
-        std::memcpy(blob.data() + head_aligned, pool, (size_t)pool_entries * 16);
-    } else {
-        float* f = reinterpret_cast<float*>(blob.data() + head_aligned);
-        for (int64_t i = 0; i < 2 * pool_entries; ++i) f[i] = (float)pool[i];
+    return LSG_OK;
+}
+
+}  // namespace lsg
+
+// A planned and uploaded operator list: the passes, their operators and the data pool in the
+// register precision, resident on the device, ready to launch on any register of the same shape.
+struct lsg_program_s {
+    int nbits = 0, precision = 0;
+    int64_t batch = 1;
+    lsg::Plan plan;
+    lsg::Scratch dev;
+    size_t head_aligned = 0;
+    size_t smem = 0;
+    int K = 0;
+    std::vector<cudaEvent_t> events;
+};
+
+namespace lsg {
+
+template <typename R>
+static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
+    auto kern = k_tile_pass<R>;
+    if (p->smem > 48 * 1024)
+        LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+    const int64_t tiles_per_member = 1ll << (s->nbits - p->K);
+    const int64_t total = tiles_per_member * s->batch;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, p->smem);
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
+    int* status = device_status();
+    if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
+    const PassDesc* pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
+    const TileOp* ops_dev = reinterpret_cast<const TileOp*>(pd_dev + p->plan.passes.size());
+    const Cx<R>* pool_dev =
+        reinterpret_cast<const Cx<R>*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
+    for (size_t i = 0; i < p->plan.passes.size(); ++i) {
+        if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
+        kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(reinterpret_cast<Cx<R>*>(s->data), s->elems, pd_dev + i,
+                                                          ops_dev, pool_dev, tiles_per_member, total, status);
     }
-    LSG_CHECK(ensure(s->program, total));
-    LSG_CUDA(cudaMemcpyAsync(s->program.ptr, blob.data(), total, cudaMemcpyHostToDevice, s->stream));
-    const void* pool_dev = static_cast<unsigned char*>(s->program.ptr) + head_aligned;
-    int rc = s->precision == LSG_C128 ? launch_passes<double>(s, plan, pool_dev)
-                                      : launch_passes<float>(s, plan, pool_dev);
+    if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
+    LSG_CUDA(cudaGetLastError());
+    return LSG_OK;
+}
+
+static int program_create(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
+                          const double* pool, int64_t pool_entries, lsg_program_s** out) {
+    LSG_CHECK(validate_ops(nbits, batch, ops, nops, pool, pool_entries));
+    auto* p = new lsg_program_s();
+    p->nbits = nbits;
+    p->precision = precision;
+    p->batch = batch;
+    p->K = tile_bits_for(nbits, precision);
+    const int L = std::min(p->K, low_bits_for(nbits, precision));
+    if (nops > 0) {
+        p->plan = plan_passes(ops, nops, nbits, p->K, L);
+        if (p->plan.passes.empty()) {
+            delete p;
+            return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits (%d kept low)", tile_bits_for(nbits, precision), L);
+        }
+    }
+    int max_ops = 0;
+    for (const PassDesc& pd : p->plan.passes) max_ops = std::max(max_ops, pd.nops);
+    const size_t elt = precision == LSG_C128 ? 16 : 8;
+    p->smem = (elt << p->K) + (size_t)max_ops * sizeof(TileOp);
+    if (p->smem > 220 * 1024) {
+        delete p;
+        return fail(LSG_E_ARG, "a pass needs %zu bytes of shared memory", (size_t)((elt << tile_bits_for(nbits, precision)) + (size_t)max_ops * sizeof(TileOp)));
+    }
+    const size_t head = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp);
+    p->head_aligned = (head + 255) & ~size_t(255);
+    const size_t total = p->head_aligned + (size_t)pool_entries * elt;
+    std::vector<unsigned char> blob(std::max<size_t>(total, 1));
+    std::memcpy(blob.data(), p->plan.passes.data(), p->plan.passes.size() * sizeof(PassDesc));
+    std::memcpy(blob.data() + p->plan.passes.size() * sizeof(PassDesc), p->plan.ops.data(),
+                p->plan.ops.size() * sizeof(TileOp));
+    if (precision == LSG_C128) {
+        if (pool_entries) std::memcpy(blob.data() + p->head_aligned, pool, (size_t)pool_entries * 16);
+    } else {
+        float* f = reinterpret_cast<float*>(blob.data() + p->head_aligned);
+        for (int64_t i = 0; i < 2 * pool_entries; ++i) f[i] = (float)pool[i];  // rounded once
+    }
+    int rc = ensure(p->dev, total);
+    if (rc == LSG_OK) {
+        cudaError_t e = cudaMemcpy(p->dev.ptr, blob.data(), total, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = fail(LSG_E_CUDA, "uploading the program failed: %s", cudaGetErrorString(e));
+    }
+    if (rc != LSG_OK) {
+        release(p->dev);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return LSG_OK;
+}
+
+static void program_destroy(lsg_program_s* p) {
+    if (!p) return;
+    for (cudaEvent_t e : p->events) cudaEventDestroy(e);
+    release(p->dev);
+    delete p;
+}
+
+static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
+    if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
+        return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
+                    p->nbits, p->precision, (long long)p->batch);
+    if (p->plan.passes.empty()) return LSG_OK;
+    return s->precision == LSG_C128 ? launch_passes<double>(p, s, marks) : launch_passes<float>(p, s, marks);
+}
+
+int apply_ops(lsg_state_s* s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries) {
+    if (nops == 0) return validate_ops(s->nbits, s->batch, ops, nops, pool, pool_entries);
+    lsg_program_s* p = nullptr;
+    LSG_CHECK(program_create(s->nbits, s->precision, s->batch, ops, nops, pool, pool_entries, &p));
+    int rc = program_run(p, s, nullptr);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    program_destroy(p);
     LSG_CHECK(rc);
-    // the host blob is released on return: make sure the copy has consumed it
-    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    if (e != cudaSuccess) return fail(LSG_E_CUDA, "the passes failed: %s", cudaGetErrorString(e));
     return check_device_status(s->stream);
 }
 
@@ -665,6 +797,79 @@ int lsg_apply(lsg_state s, const lsg_op* ops, int32_t nops, const double* pool, 
     clear_error();
     if (!s) return fail(LSG_E_ARG, "null register");
     return apply_ops(s, ops, nops, pool, pool_entries);
+}
+
+
+int lsg_state_sync(lsg_state s) {
+    clear_error();
+    if (!s) return fail(LSG_E_ARG, "null register");
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    return check_device_status(s->stream);
+}
+
+int lsg_state_stream(lsg_state s, void** stream) {
+    clear_error();
+    if (!s || !stream) return fail(LSG_E_ARG, "null argument");
+    *stream = (void*)s->stream;
+    return LSG_OK;
+}
+
+int lsg_program_create(lsg_state shape, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries,
+                       lsg_program* out) {
+    clear_error();
+    if (!shape || !out) return fail(LSG_E_ARG, "null argument");
+    *out = nullptr;
+    return program_create(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out);
+}
+
+int lsg_program_run(lsg_program p, lsg_state s) {
+    clear_error();
+    if (!p || !s) return fail(LSG_E_ARG, "null argument");
+    return program_run(p, s, nullptr);
+}
+
+int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms) {
+    clear_error();
+    if (!p || !s || !pass_ms) return fail(LSG_E_ARG, "null argument");
+    const size_t need = p->plan.passes.size() + 1;
+    while (p->events.size() < need) {
+        cudaEvent_t e;
+        LSG_CUDA(cudaEventCreate(&e));
+        p->events.push_back(e);
+    }
+    LSG_CHECK(program_run(p, s, p->events.data()));
+    LSG_CUDA(cudaEventSynchronize(p->events[need - 1]));
+    for (size_t i = 0; i + 1 < need; ++i) LSG_CUDA(cudaEventElapsedTime(&pass_ms[i], p->events[i], p->events[i + 1]));
+    return check_device_status(s->stream);
+}
+
+int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run) {
+    clear_error();
+    if (!p) return fail(LSG_E_ARG, "null program");
+    const int64_t member = (int64_t)(p->precision == LSG_C128 ? 16 : 8) << p->nbits;
+    if (passes) *passes = (int32_t)p->plan.passes.size();
+    if (bytes_per_run) *bytes_per_run = 2 * member * p->batch * (int64_t)p->plan.passes.size();
+    return LSG_OK;
+}
+
+int lsg_plan(int nbits, int precision, const lsg_op* ops, int32_t nops, int32_t* passes) {
+    clear_error();
+    if (!passes || nops < 0 || (nops > 0 && !ops)) return fail(LSG_E_ARG, "bad arguments");
+    if (nbits < 0 || nbits > kMaxBits) return fail(LSG_E_CAPACITY, "a register of %d bits exceeds the engine's %d", nbits, kMaxBits);
+    for (int i = 0; i < nops; ++i)
+        if (!op_bits_ok(ops[i], nbits)) return fail(LSG_E_ARG, "operator %d has a bad kind or bits", i);
+    const int K = tile_bits_for(nbits, precision);
+    const int L = std::min(K, low_bits_for(nbits, precision));
+    Plan plan = plan_passes(ops, nops, nbits, K, L);
+    if (nops > 0 && plan.passes.empty()) return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits", K);
+    *passes = (int32_t)plan.passes.size();
+    return LSG_OK;
+}
+
+int lsg_program_free(lsg_program p) {
+    clear_error();
+    program_destroy(p);
+    return LSG_OK;
 }
 
 }  // extern "C"

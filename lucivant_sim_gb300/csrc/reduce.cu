@@ -173,10 +173,11 @@ __global__ void k_search(const double* __restrict__ cum, int64_t n, const double
     }
 }
 
-// <P> partial sums: each block adds its share of every term; partials[t * nblocks + block]
+// <P> partial sums for every member (grid.y) and term: partials[(member * nterms + t) * gridDim.x + block]
 template <typename R>
 __global__ void k_expect(const Cx<R>* __restrict__ a, int64_t elems, int dm_n, const uint64_t* __restrict__ xm,
-                         const uint64_t* __restrict__ zm, int nterms, double* __restrict__ partials, int64_t member) {
+                         const uint64_t* __restrict__ zm, int nterms, double* __restrict__ partials) {
+    const int64_t member = blockIdx.y;
     const Cx<R>* s = a + member * elems;
     const int64_t count = dm_n ? (1ll << dm_n) : elems;
     for (int t = 0; t < nterms; ++t) {
@@ -205,17 +206,18 @@ __global__ void k_expect(const Cx<R>* __restrict__ a, int64_t elems, int dm_n, c
             acc += term;
         }
         double tot = block_sum(acc);
-        if (threadIdx.x == 0) partials[(int64_t)t * gridDim.x + blockIdx.x] = tot;
+        if (threadIdx.x == 0) partials[(member * nterms + t) * gridDim.x + blockIdx.x] = tot;
     }
 }
 
-__global__ void k_sum_rows(const double* __restrict__ partials, int64_t ncols, int nrows, double* __restrict__ out) {
-    const int row = blockIdx.x;
-    if (row >= nrows) return;
-    double acc = 0.0;
-    for (int64_t c = threadIdx.x; c < ncols; c += blockDim.x) acc += partials[row * ncols + c];
-    double tot = block_sum(acc);
-    if (threadIdx.x == 0) out[row] = tot;
+// one block per row: out[row] = sum of partials[row * ncols .. + ncols) in a fixed order
+__global__ void k_sum_rows(const double* __restrict__ partials, int64_t ncols, int64_t nrows, double* __restrict__ out) {
+    for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
+        double acc = 0.0;
+        for (int64_t c = threadIdx.x; c < ncols; c += blockDim.x) acc += partials[row * ncols + c];
+        double tot = block_sum(acc);
+        if (threadIdx.x == 0) out[row] = tot;
+    }
 }
 
 template <typename R>
@@ -282,6 +284,16 @@ int lsg_probabilities(lsg_state s, int dm_qubits, int64_t member, double* out) {
     clear_error();
     if (!s || !out) return fail(LSG_E_ARG, "null argument");
     const int64_t n = dm_qubits ? (1ll << dm_qubits) : s->elems;
+    if (member < 0) {  // every member, one after another in `out`
+        LSG_CHECK(ensure(s->scratch, (size_t)n * 8 * s->batch));
+        for (int64_t b = 0; b < s->batch; ++b) {
+            int64_t got = 0;
+            LSG_CHECK(probs_device(s, dm_qubits, b, (double*)s->scratch.ptr + b * n, &got));
+        }
+        LSG_CUDA(cudaMemcpyAsync(out, s->scratch.ptr, (size_t)n * 8 * s->batch, cudaMemcpyDeviceToHost, s->stream));
+        LSG_CUDA(cudaStreamSynchronize(s->stream));
+        return LSG_OK;
+    }
     LSG_CHECK(ensure(s->scratch, (size_t)n * 8));
     int64_t got = 0;
     LSG_CHECK(probs_device(s, dm_qubits, member, (double*)s->scratch.ptr, &got));
@@ -390,33 +402,33 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
     for (int t = 0; t < nterms; ++t)
         if ((xmask[t] | zmask[t]) & ~limit) return fail(LSG_E_ARG, "lsg_expect_pauli: term %d names a missing qubit", t);
     const int64_t count = dm_qubits ? (1ll << dm_qubits) : s->elems;
-    const unsigned grid = reduce_grid(count);
+    const unsigned grid = std::max(1u, std::min(reduce_grid(count), (unsigned)std::max<int64_t>(1, 4096 / s->batch)));
     size_t off = 0;
     auto take = [&](size_t bytes) {
         size_t at = off;
         off += (bytes + 255) & ~size_t(255);
         return at;
     };
-    const size_t o_x = take(nterms * 8), o_z = take(nterms * 8), o_part = take((size_t)nterms * grid * 8),
-                 o_out = take((size_t)nterms * s->batch * 8);
+    const int64_t rows = (int64_t)nterms * s->batch;
+    const size_t o_x = take(nterms * 8), o_z = take(nterms * 8), o_part = take((size_t)rows * grid * 8),
+                 o_out = take((size_t)rows * 8);
     LSG_CHECK(ensure(s->scratch, off));
     char* base = (char*)s->scratch.ptr;
     LSG_CUDA(cudaMemcpyAsync(base + o_x, xmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
     LSG_CUDA(cudaMemcpyAsync(base + o_z, zmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
-    for (int64_t b = 0; b < s->batch; ++b) {
-        if (s->precision == LSG_C128)
-            k_expect<double><<<grid, kThreads, 0, s->stream>>>((const Cx<double>*)s->data, s->elems, dm_qubits,
-                                                              (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
-                                                              nterms, (double*)(base + o_part), b);
-        else
-            k_expect<float><<<grid, kThreads, 0, s->stream>>>((const Cx<float>*)s->data, s->elems, dm_qubits,
-                                                             (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
-                                                             nterms, (double*)(base + o_part), b);
-        k_sum_rows<<<nterms, kThreads, 0, s->stream>>>((const double*)(base + o_part), grid, nterms,
-                                                       (double*)(base + o_out) + b * nterms);
-    }
+    const dim3 g2(grid, (unsigned)s->batch);
+    if (s->precision == LSG_C128)
+        k_expect<double><<<g2, kThreads, 0, s->stream>>>((const Cx<double>*)s->data, s->elems, dm_qubits,
+                                                        (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                                                        nterms, (double*)(base + o_part));
+    else
+        k_expect<float><<<g2, kThreads, 0, s->stream>>>((const Cx<float>*)s->data, s->elems, dm_qubits,
+                                                       (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                                                       nterms, (double*)(base + o_part));
+    k_sum_rows<<<(unsigned)std::min<int64_t>(rows, 152 * 16), kThreads, 0, s->stream>>>((const double*)(base + o_part), grid,
+                                                                                      rows, (double*)(base + o_out));
     LSG_CUDA(cudaGetLastError());
-    std::vector<double> tmp((size_t)nterms * s->batch);
+    std::vector<double> tmp((size_t)rows);
     LSG_CUDA(cudaMemcpyAsync(tmp.data(), base + o_out, tmp.size() * 8, cudaMemcpyDeviceToHost, s->stream));
     LSG_CUDA(cudaStreamSynchronize(s->stream));
     for (int64_t b = 0; b < s->batch; ++b)
@@ -436,7 +448,7 @@ int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out) {
         k_prob_one<double><<<grid, kThreads, 0, s->stream>>>((const Cx<double>*)s->data + member * s->elems, s->elems, qubit, part);
     else
         k_prob_one<float><<<grid, kThreads, 0, s->stream>>>((const Cx<float>*)s->data + member * s->elems, s->elems, qubit, part);
-    k_sum_rows<<<1, kThreads, 0, s->stream>>>(part, grid, 1, part + grid);
+    k_sum_rows<<<1, kThreads, 0, s->stream>>>(part, grid, (int64_t)1, part + grid);
     LSG_CUDA(cudaGetLastError());
     LSG_CUDA(cudaMemcpyAsync(out, part + grid, 8, cudaMemcpyDeviceToHost, s->stream));
     LSG_CUDA(cudaStreamSynchronize(s->stream));

@@ -156,6 +156,15 @@ def dm_oplist(circuit: Any, noises: list[Any]) -> OpList:
     n = circuit.num_qubits
     ops = OpList()
     batched = len(noises) > 1
+    chan_cache: dict[int, tuple[Any, np.ndarray]] = {}
+
+    def chan_superop(ch: Any) -> np.ndarray:
+        hit = chan_cache.get(id(ch))
+        if hit is None or hit[0] is not ch:
+            s = depolarizing_superop(ch.params[0], 1) if ch.analytic_depolarizing else superop(ch.kraus)
+            hit = chan_cache[id(ch)] = (ch, s)
+        return hit[1]
+
     for op in circuit.operations:
         if op.kind == "gate":
             qs = tuple(op.qubits)
@@ -171,13 +180,7 @@ def dm_oplist(circuit: Any, noises: list[Any]) -> OpList:
                     kind, data = classify(gate_s)
                     ops.add(kind, [n + q, q], data)
                     continue
-                mats = []
-                for ch in chans:
-                    if ch.analytic_depolarizing:
-                        s = depolarizing_superop(ch.params[0], 1)
-                    else:
-                        s = superop(ch.kraus)
-                    mats.append(s @ gate_s)
+                mats = [chan_superop(ch) @ gate_s for ch in chans]
                 if batched:
                     ops.add_batched(OP_MATRIX, [n + q, q], np.stack(mats))
                 else:

@@ -152,3 +152,42 @@ def stabilizer_noise(p: float = 1e-3) -> NoiseModel:
     model.add_gate_error(depolarizing(p, 2))
     model.add_readout_error(ReadoutError(0.01, 0.03))
     return model
+
+
+def thermal_depolarizing(single: float, t1: float = 120, t2: float = 90, time: float = 0.05):
+    """Depolarising error of average infidelity ``single`` followed by thermal relaxation, as one
+    Kraus channel (products T_j @ D_i): the reading of "uniform noise plus thermal relaxation on
+    every u3" in which both act, so the one-qubit error parameter matters."""
+    from lucivant_sim_gb300.noise import Channel, from_gate_error
+
+    th = thermal_relaxation(t1, t2, time)
+    dp = from_gate_error(single, 1)
+    kraus = tuple(t @ d for d in dp.kraus for t in th.kraus)
+    return Channel("thermal_relaxation+depolarizing", 1, kraus, (t1, t2, time, dp.params[0]))
+
+
+def dm_noise_instances(count: int, seed: int = 7, readout: float = 2e-2) -> list[NoiseModel]:
+    """``count`` noise instances: one-qubit error uniform in [1e-4, 5e-3] and two-qubit error
+    uniform in [1e-3, 3e-2], seeded; thermal relaxation composed with the one-qubit error on u3."""
+    rng = np.random.default_rng(seed)
+    singles = rng.uniform(1e-4, 5e-3, size=count)
+    twos = rng.uniform(1e-3, 3e-2, size=count)
+    return [
+        NoiseModel.uniform(two=float(t), readout=readout).add_gate_error(thermal_depolarizing(float(s)), gates="u3")
+        for s, t in zip(singles, twos, strict=True)
+    ]
+
+
+def z_observables(n: int) -> list[str]:
+    """<Z_i> for every qubit and <Z_i Z_{i+1}> for neighbours (qubit 0 rightmost)."""
+    labels = []
+    for i in range(n):
+        lab = ["I"] * n
+        lab[n - 1 - i] = "Z"
+        labels.append("".join(lab))
+    for i in range(n - 1):
+        lab = ["I"] * n
+        lab[n - 1 - i] = "Z"
+        lab[n - 2 - i] = "Z"
+        labels.append("".join(lab))
+    return labels
