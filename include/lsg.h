@@ -143,6 +143,25 @@ int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out);
  * probability > 0 (engines.py:195-201). */
 int lsg_collapse(lsg_state s, int qubit, int outcome, double probability, int64_t member);
 
+/* ---- allocation-free expectations ---------------------------------------------------------
+ * No counterpart in the reference: an extra entry point for callers that cannot let the library
+ * allocate device memory (a runtime or framework that owns the whole GPU through its own memory
+ * pool and budget, or a latency-bound loop that cannot take cudaMalloc/cudaFree's device-wide
+ * synchronisation). Same results as lsg_expect_pauli, but the caller passes device pointers:
+ * `amplitudes` (batch members of 2^nbits complex128 or complex64 values, contiguous) and
+ * `out_device` (nterms x batch doubles, out[t * batch + b]). It calls no cudaMalloc/cudaFree: its
+ * only working memory is one file-scope __device__ array of LSG_NOALLOC_SCRATCH_BYTES, which every
+ * GPU that loads the library holds until the process exits. The masks and nterms x batch partial
+ * sums must fit in it; larger requests fail with LSG_E_ARG. The first call on a device looks up
+ * the array's device address on that device (call it once, with the device current, before any
+ * latency-critical use). Every call shares the array, so calls that overlap on the GPU race:
+ * serialise them (one stream, or wait between calls). The call waits for its own stream before
+ * returning. `stream` is a cudaStream_t (NULL: the legacy default stream). */
+#define LSG_NOALLOC_SCRATCH_BYTES (1u << 20)
+int lsg_expect_pauli_noalloc(const void* amplitudes, int precision, int nbits, int64_t batch, int dm_qubits,
+                             const uint64_t* xmask, const uint64_t* zmask, int32_t nterms, double* out_device,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

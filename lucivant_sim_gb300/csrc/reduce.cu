@@ -8,6 +8,7 @@
 //  * Pauli expectations  — expectation (simulator.py:489-527)
 //  * p(1) and collapse   — Statevector.probability_of_one / collapse (engines.py:185-201)
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -474,3 +475,108 @@ int lsg_collapse(lsg_state s, int qubit, int outcome, double probability, int64_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free Pauli expectations.
+//
+// For callers that cannot let a library allocate device memory: a serving runtime or a host
+// framework that owns every byte of the GPU through its own pool (and must keep a hard memory
+// budget), or a latency-sensitive loop that cannot afford cudaMalloc/cudaFree, which take a
+// device-wide lock and synchronise the device. The caller passes device pointers for the
+// amplitudes and the results; the only other device memory used is the file-scope array below,
+// of a fixed maximum size, which every GPU that loads the library holds until the process exits.
+
+namespace lsg {
+
+constexpr size_t kNoAllocScratchBytes = LSG_NOALLOC_SCRATCH_BYTES;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// The array's device address on each device. Host code must not use the symbol itself: on the
+// host it names a host-side stand-in, not device memory.
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[64] = {};
+
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    LSG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(LSG_E_ARG, "device %d is out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(LSG_E_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
+        g_noalloc_addr[dev] = ptr;
+    }
+    *out = g_noalloc_addr[dev];
+    return LSG_OK;
+}
+
+// Sum each row of partials (row = member * nterms + t) in a fixed order and store it at
+// out[t * batch + member], the layout lsg_expect_pauli returns.
+__global__ void k_sum_rows_to_terms(const double* __restrict__ partials, int64_t ncols, int nterms, int64_t batch,
+                                    double* __restrict__ out) {
+    const int64_t rows = (int64_t)nterms * batch;
+    for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+        double acc = 0.0;
+        for (int64_t c = threadIdx.x; c < ncols; c += blockDim.x) acc += partials[row * ncols + c];
+        double tot = block_sum(acc);
+        if (threadIdx.x == 0) {
+            const int64_t member = row / nterms, t = row % nterms;
+            out[t * batch + member] = tot;
+        }
+    }
+}
+
+}  // namespace lsg
+
+extern "C" int lsg_expect_pauli_noalloc(const void* amplitudes, int precision, int nbits, int64_t batch, int dm_qubits,
+                                        const uint64_t* xmask, const uint64_t* zmask, int32_t nterms,
+                                        double* out_device, void* stream) {
+    using namespace lsg;
+    clear_error();
+    if (!amplitudes || !out_device || nterms < 1 || !xmask || !zmask || batch < 1)
+        return fail(LSG_E_ARG, "lsg_expect_pauli_noalloc: bad arguments");
+    if (precision != LSG_C128 && precision != LSG_C64) return fail(LSG_E_ARG, "unknown precision %d", precision);
+    if (nbits < 0 || nbits > kMaxBits) return fail(LSG_E_CAPACITY, "a register of %d bits exceeds the engine's %d", nbits, kMaxBits);
+    if (dm_qubits && 2 * dm_qubits != nbits) return fail(LSG_E_STATE, "density register size mismatch");
+    const int nq = dm_qubits ? dm_qubits : nbits;
+    const uint64_t limit = nq >= 64 ? ~0ull : ((1ull << nq) - 1);
+    for (int t = 0; t < nterms; ++t)
+        if ((xmask[t] | zmask[t]) & ~limit) return fail(LSG_E_ARG, "term %d names a missing qubit", t);
+    // scratch layout: x masks | z masks | partial sums (rows x grid), each 256-byte aligned
+    const size_t mask_bytes = ((size_t)nterms * 8 + 255) & ~size_t(255);
+    const int64_t rows = (int64_t)nterms * batch;
+    const size_t room = kNoAllocScratchBytes - 2 * std::min(mask_bytes, kNoAllocScratchBytes / 2);
+    if (2 * mask_bytes >= kNoAllocScratchBytes || (size_t)rows * 8 > room)
+        return fail(LSG_E_ARG,
+                    "lsg_expect_pauli_noalloc: %d terms x %lld members need more than the %zu-byte scratch array "
+                    "(at most %zu partial sums)", nterms, (long long)batch, kNoAllocScratchBytes, room / 8);
+    const int64_t count = dm_qubits ? (1ll << dm_qubits) : (1ll << nbits);
+    const int64_t fit = (int64_t)(room / 8 / (size_t)rows);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>({(int64_t)reduce_grid(count), fit,
+                                                                             std::max<int64_t>(1, 4096 / batch)}));
+    void* base = nullptr;
+    LSG_CHECK(noalloc_scratch(&base));
+    char* scratch = static_cast<char*>(base);
+    uint64_t* dx = reinterpret_cast<uint64_t*>(scratch);
+    uint64_t* dz = reinterpret_cast<uint64_t*>(scratch + mask_bytes);
+    double* part = reinterpret_cast<double*>(scratch + 2 * mask_bytes);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    LSG_CUDA(cudaMemcpyAsync(dx, xmask, (size_t)nterms * 8, cudaMemcpyHostToDevice, st));
+    LSG_CUDA(cudaMemcpyAsync(dz, zmask, (size_t)nterms * 8, cudaMemcpyHostToDevice, st));
+    const dim3 g2(grid, (unsigned)batch);
+    const int64_t elems = 1ll << nbits;
+    if (precision == LSG_C128)
+        k_expect<double><<<g2, kThreads, 0, st>>>(static_cast<const Cx<double>*>(amplitudes), elems, dm_qubits, dx, dz,
+                                                 nterms, part);
+    else
+        k_expect<float><<<g2, kThreads, 0, st>>>(static_cast<const Cx<float>*>(amplitudes), elems, dm_qubits, dx, dz,
+                                                nterms, part);
+    k_sum_rows_to_terms<<<(unsigned)std::min<int64_t>(rows, 152 * 16), kThreads, 0, st>>>(part, grid, nterms, batch,
+                                                                                        out_device);
+    LSG_CUDA(cudaGetLastError());
+    // the masks are copied from the caller's host memory: wait, so the caller may reuse it
+    LSG_CUDA(cudaStreamSynchronize(st));
+    return LSG_OK;
+}
