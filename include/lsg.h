@@ -143,6 +143,53 @@ int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out);
  * probability > 0 (engines.py:195-201). */
 int lsg_collapse(lsg_state s, int qubit, int outcome, double probability, int64_t member);
 
+/* ---- trajectories ----------------------------------------------------------------------------
+ * Orrery's per-shot interpreter (_trajectory, src/lucivant_sim/simulator.py:287-317; the shot
+ * loop :364-371; Statevector.apply_channel / measure / reset, engines.py:159-205) as a device
+ * program over a register whose members are shots. Operations are given flattened, with if/else
+ * blocks bracketed by LSG_T_IF / LSG_T_ELSE / LSG_T_ENDIF. Every member draws its uniforms from a
+ * cursor in the reference's order: one per noisy gate (mixture or Kraus), one per measurement or
+ * reset, one more per measurement with a readout error. */
+#define LSG_T_GATE 0    /* unitary: opkind is LSG_OP_MATRIX/DIAG/PERM, data as for lsg_op */
+#define LSG_T_MIXTURE 1 /* mixture channel (nq <= 2), count branches: data holds count entries (re = running
+                           sum of the branch probabilities in order, im = 1 for an identity branch), then
+                           count dense 2^nq matrices */
+#define LSG_T_KRAUS 2   /* Kraus channel (nq <= 2): count operators, dense 2^nq x 2^nq, at data */
+#define LSG_T_MEASURE 3 /* qubits[0] into clbit (-1: discarded); readout != 0: one more uniform, flip with
+                           p10 (read 1 as 0) or p01 */
+#define LSG_T_RESET 4   /* measure qubits[0] with one uniform, then X when the outcome is 1 */
+#define LSG_T_SCALE 5   /* global phase: the factor at data */
+#define LSG_T_IF 6      /* holds when the count clbits listed at data (real parts, least significant first)
+                           read `value`, inverted by negate */
+#define LSG_T_ELSE 7
+#define LSG_T_ENDIF 8
+
+typedef struct lsg_traj_op {
+    int32_t kind, opkind, nq, count;
+    int32_t qubits[4];
+    int32_t clbit, readout, negate, pad;
+    int64_t data;
+    uint64_t value;
+    double p01, p10;
+} lsg_traj_op;
+
+typedef struct lsg_traj_s* lsg_traj;
+int lsg_traj_create(lsg_state shape, const lsg_traj_op* ops, int32_t nops, const double* pool,
+                    int64_t pool_entries, int32_t num_clbits, lsg_traj* out);
+/* Upper bound of the uniforms one shot draws, and the number of compiled steps. */
+int lsg_traj_info(lsg_traj t, int64_t* max_draws, int32_t* steps);
+/* Serial: `shots` shots one after another on a one-member register, all drawing from one stream
+ * uniforms[0..nuniforms) (at least shots x max_draws) in order, exactly as Orrery's shot loop does.
+ * clbits_out: shots x ceil(num_clbits/64) words; consumed: uniforms actually drawn; near_count:
+ * decisions whose uniform fell within 1e-12 of a threshold computed on the device. */
+int lsg_traj_run_serial(lsg_traj t, lsg_state s, int64_t shots, const double* uniforms, int64_t nuniforms,
+                        uint64_t* clbits_out, int64_t* consumed, int64_t* near_count);
+/* Batched: every member is one shot drawing from its own row uniforms[b * ustride ..] (ustride >=
+ * max_draws). clbits_out: batch x words; consumed: per member. */
+int lsg_traj_run_batched(lsg_traj t, lsg_state s, const double* uniforms, int64_t ustride, uint64_t* clbits_out,
+                         int64_t* consumed, int64_t* near_count);
+int lsg_traj_free(lsg_traj t);
+
 /* ---- allocation-free expectations ---------------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that cannot let the library
  * allocate device memory (a runtime or framework that owns the whole GPU through its own memory

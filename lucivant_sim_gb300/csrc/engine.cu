@@ -15,6 +15,7 @@
 
 #include "common.cuh"
 #include "program.cuh"
+#include "tile.cuh"
 
 namespace lsg {
 
@@ -81,314 +82,12 @@ void release(Scratch& s) {
     s.bytes = 0;
 }
 
-// ------------------------------------------------------------------------ tile kernel
-
-// Deposit the bits of x into the register positions listed in pos[0..n) (ascending).
-__device__ __forceinline__ uint64_t deposit(uint64_t x, const int* pos, int n) {
-    uint64_t out = 0;
-    for (int j = 0; j < n; ++j) out |= ((x >> j) & 1ull) << pos[j];
-    return out;
-}
-
-// Insert a zero bit at position b.
-__device__ __forceinline__ uint32_t ins0(uint32_t g, int b) {
-    const uint32_t low = g & ((1u << b) - 1);
-    return ((g >> b) << (b + 1)) | low;
-}
-
-template <typename R>
-__device__ __forceinline__ Cx<R> ldm(const Cx<R>* m, int i) {
-    return m[i];
-}
-
-// 1-bit dense: the common case (fused one-qubit gates; one-qubit density superoperators use 2).
-template <typename R>
-__device__ __forceinline__ void dense1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
-    const Cx<R> m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
-    const int groups = 1 << (tbits - 1);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
-        const Cx<R> a0 = t[i0], a1 = t[i1];
-        t[i0] = cfma(m01, a1, cmul(m00, a0));
-        t[i1] = cfma(m11, a1, cmul(m10, a0));
-    }
-}
-
-// 2-bit dense on (hi_bit = matrix MSB b0, b1); lo/hi are the sorted positions.
-template <typename R>
-__device__ __forceinline__ void dense2(Cx<R>* t, int tbits, int b0, int b1, const Cx<R>* m) {
-    const int lo = min(b0, b1), hi = max(b0, b1);
-    const uint32_t o1 = 1u << b1, o2 = 1u << b0;
-    const int groups = 1 << (tbits - 2);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
-        const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            Cx<R> acc = cmul(ldm(m, 4 * r), v0);
-            acc = cfma(ldm(m, 4 * r + 1), v1, acc);
-            acc = cfma(ldm(m, 4 * r + 2), v2, acc);
-            acc = cfma(ldm(m, 4 * r + 3), v3, acc);
-            const uint32_t at = base | ((r & 1) ? o1 : 0u) | ((r & 2) ? o2 : 0u);
-            t[at] = acc;
-        }
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ Cx<R> pick4(const Cx<R>& v0, const Cx<R>& v1, const Cx<R>& v2, const Cx<R>& v3, int s) {
-    const Cx<R> a = (s & 1) ? v1 : v0;
-    const Cx<R> b = (s & 1) ? v3 : v2;
-    return (s & 2) ? b : a;
-}
-
-// permutations with phases on 1 or 2 bits (x, cx, swap and their phased forms)
-template <typename R>
-__device__ __forceinline__ void perm1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
-    const Cx<R> p0 = m[0], p1 = m[1];
-    const int s0 = (int)m[2].re;
-    const int groups = 1 << (tbits - 1);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
-        const Cx<R> a0 = t[i0], a1 = t[i1];
-        t[i0] = cmul(p0, s0 ? a1 : a0);
-        t[i1] = cmul(p1, s0 ? a0 : a1);
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ void perm2(Cx<R>* t, int tbits, int b0, int b1, const Cx<R>* m) {
-    const int lo = min(b0, b1), hi = max(b0, b1);
-    const uint32_t o1 = 1u << b1, o2 = 1u << b0;
-    const Cx<R> p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
-    const int s0 = (int)m[4].re, s1 = (int)m[5].re, s2 = (int)m[6].re, s3 = (int)m[7].re;
-    const int groups = 1 << (tbits - 2);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
-        const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
-        t[base] = cmul(p0, pick4(v0, v1, v2, v3, s0));
-        t[base | o1] = cmul(p1, pick4(v0, v1, v2, v3, s1));
-        t[base | o2] = cmul(p2, pick4(v0, v1, v2, v3, s2));
-        t[base | o1 | o2] = cmul(p3, pick4(v0, v1, v2, v3, s3));
-    }
-}
-
-// Wide operators (3 to 5 bits): rare (Toffoli-class gates, two-qubit Kraus superoperators), kept
-// out of line so their register needs don't shape the common path.
-template <typename R>
-__device__ __noinline__ void wide_op(Cx<R>* t, int tbits, int kind, int k, const int* lb, const int* sorted,
-                                     const Cx<R>* m) {
-    const int D = 1 << k;
-    uint32_t offs[32];
-    Cx<R> v[32];
-    for (int j = 0; j < D; ++j) {
-        uint32_t o = 0;
-        for (int i = 0; i < k; ++i) o |= (uint32_t)((j >> (k - 1 - i)) & 1) << lb[i];
-        offs[j] = o;
-    }
-    const int groups = 1 << (tbits - k);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        uint32_t base = (uint32_t)g;
-        for (int i = 0; i < k; ++i) base = ins0(base, sorted[i]);
-        for (int j = 0; j < D; ++j) v[j] = t[base | offs[j]];
-        if (kind == LSG_OP_MATRIX) {
-            for (int r = 0; r < D; ++r) {
-                Cx<R> acc;
-                for (int c = 0; c < D; ++c) acc = cfma(m[r * D + c], v[c], acc);
-                t[base | offs[r]] = acc;
-            }
-        } else {
-            for (int r = 0; r < D; ++r) t[base | offs[r]] = cmul(m[r], v[(int)m[D + r].re]);
-        }
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ void op_diag(Cx<R>* tile, int tbits, int k, const int* lb, const Cx<R>* m) {
-    const int n = 1 << tbits;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int j = 0;
-        for (int b = 0; b < k; ++b) j = (j << 1) | ((i >> lb[b]) & 1);
-        tile[i] = cmul(m[j], tile[i]);
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ void op_scale(Cx<R>* tile, int tbits, const Cx<R>* m) {
-    const int n = 1 << tbits;
-    const Cx<R> f = m[0];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) tile[i] = cmul(f, tile[i]);
-}
-
-// (1-p) rho + (p/d) I (x) Tr_t(rho) on kq row bits then kq column bits (kq = 1 or 2).
-template <typename R, int KQ>
-__device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, const int* sorted, const Cx<R>* m) {
-    constexpr int KB = 2 * KQ;
-    constexpr int D = 1 << KB;
-    constexpr int d = 1 << KQ;
-    int l[KB], srt[KB];
-#pragma unroll
-    for (int i = 0; i < KB; ++i) {
-        l[i] = lb[i];
-        srt[i] = sorted[i];
-    }
-    const R p = m[0].re;
-    const R keep = R(1) - p;
-    const R share = p / R(d);
-    const int groups = 1 << (tbits - KB);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        uint32_t base = (uint32_t)g;
-#pragma unroll
-        for (int i = 0; i < KB; ++i) base = ins0(base, srt[i]);
-        Cx<R> tr;
-#pragma unroll
-        for (int s = 0; s < d; ++s) {
-            const int j = (s << KQ) | s;
-            uint32_t o = 0;
-#pragma unroll
-            for (int i = 0; i < KB; ++i) o |= (uint32_t)((j >> (KB - 1 - i)) & 1) << l[i];
-            const Cx<R> v = t[base | o];
-            tr.re += v.re;
-            tr.im += v.im;
-        }
-#pragma unroll
-        for (int j = 0; j < D; ++j) {
-            uint32_t o = 0;
-#pragma unroll
-            for (int i = 0; i < KB; ++i) o |= (uint32_t)((j >> (KB - 1 - i)) & 1) << l[i];
-            const Cx<R> v = t[base | o];
-            Cx<R> out(v.re * keep, v.im * keep);
-            if ((j >> KQ) == (j & (d - 1))) {
-                out.re += share * tr.re;
-                out.im += share * tr.im;
-            }
-            t[base | o] = out;
-        }
-    }
-}
-
-template <typename R>
-__device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, int nops,
-                        const Cx<R>* __restrict__ data, int64_t member) {
-    for (int o = 0; o < nops; ++o) {
-        const TileOp& op = ops[o];  // staged in shared memory
-        const int kind = op.kind, k = op.k;
-        const Cx<R>* m = data + op.data + member * op.stride;
-        __syncthreads();
-        if (kind == LSG_OP_MATRIX && k == 1) {
-            dense1<R>(tile, tbits, op.lb[0], m);
-        } else if (kind == LSG_OP_MATRIX && k == 2) {
-            dense2<R>(tile, tbits, op.lb[0], op.lb[1], m);
-        } else if (kind == LSG_OP_PERM && k == 1) {
-            perm1<R>(tile, tbits, op.lb[0], m);
-        } else if (kind == LSG_OP_PERM && k == 2) {
-            perm2<R>(tile, tbits, op.lb[0], op.lb[1], m);
-        } else if (kind == LSG_OP_DIAG) {
-            op_diag<R>(tile, tbits, k, op.lb, m);
-        } else if (kind == LSG_OP_DEPOL) {
-            if (k == 2) op_depol<R, 1>(tile, tbits, op.lb, op.sorted, m);
-            else op_depol<R, 2>(tile, tbits, op.lb, op.sorted, m);
-        } else if (kind == LSG_OP_SCALE) {
-            op_scale<R>(tile, tbits, m);
-        } else {
-            wide_op<R>(tile, tbits, kind, k, op.lb, op.sorted, m);
-        }
-    }
-    __syncthreads();
-}
-
-// One fused pass over every tile of every member. Tiles are visited grid-stride; each CTA
-// handles one tile at a time (CTAs co-resident on an SM overlap each other's copies).
-template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) k_tile_pass(Cx<R>* __restrict__ state, int64_t member_elems,
-                                                   const PassDesc* __restrict__ pass_g,
-                                                   const TileOp* __restrict__ ops,
-                                                   const Cx<R>* __restrict__ data, int64_t tiles_per_member,
-                                                   int64_t total_tiles, int* status) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ uint64_t bar;
-    __shared__ PassDesc pd;
-    Cx<R>* tile = reinterpret_cast<Cx<R>*>(smem_raw);
-    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + (sizeof(Cx<R>) << pass_g->K));
-    if (threadIdx.x == 0) pd = *pass_g;
-    {
-        // stage this pass's operators in shared memory (the same for every tile of the pass)
-        const int nops = pass_g->nops;
-        const int* src = reinterpret_cast<const int*>(ops + pass_g->first_op);
-        int* dst = reinterpret_cast<int*>(sops);
-        const int words = nops * (int)(sizeof(TileOp) / sizeof(int));
-        for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
-    }
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    const int K = pd.K, L = pd.L;
-    const int nchunks = 1 << (K - L);
-    const uint32_t chunk_bytes = (uint32_t)(sizeof(Cx<R>) << L);
-    const bool use_bulk = (chunk_bytes % 16) == 0;
-    uint32_t parity = 0;
-    for (int64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-        const int64_t member = t / tiles_per_member;
-        const uint64_t tt = (uint64_t)(t - member * tiles_per_member);
-        Cx<R>* mem = state + member * member_elems;
-        const uint64_t base = deposit(tt, pd.outer, pd.nouter);
-        // ---- load
-        if (use_bulk) {
-            if (threadIdx.x < 32) {
-                if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar, chunk_bytes * (uint32_t)nchunks);
-                __syncwarp();
-                for (int c = threadIdx.x; c < nchunks; c += 32)
-                    bulk_g2s(tile + ((size_t)c << L), mem + (base | deposit((uint64_t)c, pd.hi, K - L)), chunk_bytes,
-                             &bar);
-            }
-            const bool ok = mbar_wait_bounded(&bar, parity, status);
-            if (__syncthreads_or(!ok)) return;  // every thread leaves together on a timeout
-            parity ^= 1;
-        } else {
-            const int n = 1 << K;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                uint64_t g = base | deposit((uint64_t)(i >> L), pd.hi, K - L) | (uint64_t)(i & ((1 << L) - 1));
-                tile[i] = mem[g];
-            }
-        }
-        // ---- compute
-        run_ops<R>(tile, K, sops, pd.nops, data, member);
-        // ---- store
-        if (use_bulk) {
-            fence_proxy_async_smem();
-            __syncthreads();
-            if (threadIdx.x < 32) {
-                for (int c = threadIdx.x; c < nchunks; c += 32)
-                    bulk_s2g(mem + (base | deposit((uint64_t)c, pd.hi, K - L)), tile + ((size_t)c << L), chunk_bytes);
-                bulk_commit();
-                bulk_wait_read();
-            }
-            __syncthreads();
-        } else {
-            const int n = 1 << K;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                uint64_t g = base | deposit((uint64_t)(i >> L), pd.hi, K - L) | (uint64_t)(i & ((1 << L) - 1));
-                mem[g] = tile[i];
-            }
-            __syncthreads();
-        }
-    }
-    if (use_bulk && threadIdx.x < 32) bulk_wait_all();
-}
-
 // ------------------------------------------------------------------------ planner
 
-struct Plan {
-    std::vector<PassDesc> passes;
-    std::vector<TileOp> ops;
-};
-
-static int op_bits_ok(const lsg_op& op, int nbits) {
+int op_bits_ok(const lsg_op& op, int nbits) {
     if (op.kind == LSG_OP_SCALE) return op.nbits == 0;
     if (op.nbits < 1 || op.nbits > LSG_MAX_OP_BITS) return 0;
-    if (op.kind == LSG_OP_MATRIX || op.kind == LSG_OP_PERM) {
+    if (op.kind == LSG_OP_MATRIX || op.kind == LSG_OP_PERM || op.kind == kOpMixture) {
         if (op.nbits > 5) return 0;
     } else if (op.kind == LSG_OP_DEPOL) {
         if (op.nbits != 2 && op.nbits != 4) return 0;
@@ -407,7 +106,8 @@ static int op_bits_ok(const lsg_op& op, int nbits) {
 // Greedy fusion: sweep the remaining operators; an operator joins the current pass when its bits
 // fit the tile and no operator deferred earlier in the sweep shares a bit with it (so program
 // order is kept wherever it matters). Deferred operators start the next sweep.
-static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L) {
+Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* pred, const int* draw,
+              const int* count) {
     Plan plan;
     std::vector<int> remaining(nops);
     for (int i = 0; i < nops; ++i) remaining[i] = i;
@@ -475,12 +175,19 @@ static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L) {
             std::sort(t.sorted, t.sorted + op.nbits);
             t.data = op.data;
             t.stride = op.batch_stride;
+            t.pred = pred ? pred[idx] : 0;
+            t.draw = draw ? draw[idx] : 0;
+            t.count = count ? count[idx] : 0;
             plan.ops.push_back(t);
         }
         plan.passes.push_back(pd);
         remaining.swap(deferred);
     }
     return plan;
+}
+
+static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L) {
+    return plan_ops(ops, nops, nbits, K, L, nullptr, nullptr, nullptr);
 }
 
 // ------------------------------------------------------------------------ programs
@@ -543,7 +250,7 @@ struct lsg_program_s {
 namespace lsg {
 
 template <typename R>
-static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
+static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
     auto kern = k_tile_pass<R>;
     if (p->smem > 48 * 1024)
         LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
@@ -563,16 +270,15 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
     for (size_t i = 0; i < p->plan.passes.size(); ++i) {
         if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
         kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(reinterpret_cast<Cx<R>*>(s->data), s->elems, pd_dev + i,
-                                                          ops_dev, pool_dev, tiles_per_member, total, status);
+                                                          ops_dev, pool_dev, tiles_per_member, total, status, ctx);
     }
     if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
     LSG_CUDA(cudaGetLastError());
     return LSG_OK;
 }
 
-static int program_create(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
-                          const double* pool, int64_t pool_entries, lsg_program_s** out) {
-    LSG_CHECK(validate_ops(nbits, batch, ops, nops, pool, pool_entries));
+int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out) {
     auto* p = new lsg_program_s();
     p->nbits = nbits;
     p->precision = precision;
@@ -580,7 +286,7 @@ static int program_create(int nbits, int precision, int64_t batch, const lsg_op*
     p->K = tile_bits_for(nbits, precision);
     const int L = std::min(p->K, low_bits_for(nbits, precision));
     if (nops > 0) {
-        p->plan = plan_passes(ops, nops, nbits, p->K, L);
+        p->plan = plan_ops(ops, nops, nbits, p->K, L, pred, draw, count);
         if (p->plan.passes.empty()) {
             delete p;
             return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits (%d kept low)", tile_bits_for(nbits, precision), L);
@@ -621,19 +327,29 @@ static int program_create(int nbits, int precision, int64_t batch, const lsg_op*
     return LSG_OK;
 }
 
-static void program_destroy(lsg_program_s* p) {
+static int program_create(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
+                          const double* pool, int64_t pool_entries, lsg_program_s** out) {
+    LSG_CHECK(validate_ops(nbits, batch, ops, nops, pool, pool_entries));
+    return program_create_ex(nbits, precision, batch, ops, nops, pool, pool_entries, nullptr, nullptr, nullptr, out);
+}
+
+void program_destroy(lsg_program_s* p) {
     if (!p) return;
     for (cudaEvent_t e : p->events) cudaEventDestroy(e);
     release(p->dev);
     delete p;
 }
 
-static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
+int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
     if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
         return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
                     p->nbits, p->precision, (long long)p->batch);
     if (p->plan.passes.empty()) return LSG_OK;
-    return s->precision == LSG_C128 ? launch_passes<double>(p, s, marks) : launch_passes<float>(p, s, marks);
+    return s->precision == LSG_C128 ? launch_passes<double>(p, s, marks, ctx) : launch_passes<float>(p, s, marks, ctx);
+}
+
+static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
+    return program_run_ctx(p, s, marks, TrajCtx{});
 }
 
 int apply_ops(lsg_state_s* s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries) {

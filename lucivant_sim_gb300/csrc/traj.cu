@@ -1,0 +1,768 @@
+// Trajectory programs: Orrery's per-shot interpreter (_trajectory, simulator.py:287-317, and the
+// shot loop :364-371) on the device.
+//
+// A program is a flattened operation list (gates, mixture and Kraus channels, measurements,
+// resets, if/else markers) compiled once into steps over a register whose members are shots:
+//   * runs of unitary gates and state-independent mixture channels (Pauli noise) become fused
+//     tile passes; each member picks its mixture branch from its own uniform (engines.py:161-171);
+//   * a measurement is a per-member FP64 p(1) reduction, a decision kernel that draws the outcome
+//     (and the readout flip) from the member's uniforms, and a collapse-and-renormalise pass
+//     (engines.py:185-205, simulator.py:300-306); a reset applies X after an outcome of 1;
+//   * a Kraus channel is a per-member reduced density matrix, a decision by cumulative Born
+//     weights (engines.py:172-183) and a per-member operator pass;
+//   * if/else sets per-member predicate bits from the classical bits (circuit.py:70-72); steps in
+//     a branch run only on members whose bit is set.
+// Every member consumes its uniforms from a cursor in exactly the reference's order. In serial
+// mode one member runs the shots one after another on one shared stream (bit-identical draws to
+// Orrery); in batched mode every member is a shot with its own row of uniforms.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "program.cuh"
+#include "tile.cuh"
+
+struct lsg_program_s;
+
+namespace lsg {
+
+int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out);
+int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx);
+void program_destroy(lsg_program_s* p);
+int op_bits_ok(const lsg_op& op, int nbits);
+
+constexpr int kT = 256;
+constexpr int kMaxWords = 4;  // classical bits per shot: up to 256
+constexpr double kNear = 1e-12;
+
+enum StepKind { STEP_SEG, STEP_ADVANCE, STEP_MEASURE, STEP_KRAUS, STEP_IF };
+
+struct Step {
+    int kind = 0;
+    lsg_program_s* seg = nullptr;
+    int slot = 0;       // predicate bit the step runs under
+    int64_t count = 0;  // ADVANCE: uniforms the segment drew
+    // MEASURE / RESET
+    int q = 0, clbit = -1, readout = 0, is_reset = 0;
+    double p01 = 0, p10 = 0;
+    // KRAUS
+    int k = 0, bits[2] = {0, 0}, nkraus = 0;
+    int64_t kraus_at = 0;  // offset (complex entries) in the Kraus buffer
+    // IF
+    int then_slot = 0, else_slot = 0, ncond = 0, negate = 0;
+    uint64_t value = 0;
+    int cond[64] = {};
+};
+
+__device__ __forceinline__ double nrm(double re, double im) { return re * re + im * im; }
+
+__device__ double t_block_sum(double v) {
+    __shared__ double buf[kT];
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = kT / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) buf[threadIdx.x] += buf[threadIdx.x + s];
+        __syncthreads();
+    }
+    double out = buf[0];
+    __syncthreads();
+    return out;
+}
+
+__device__ __forceinline__ bool has(const uint64_t* pred, int64_t b, int slot) { return (pred[b] >> slot) & 1; }
+
+__global__ void k_t_init(uint64_t* pred, uint64_t* clbits, int64_t* cursor, int64_t batch, int words, int reset_cursor) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+        pred[b] = 1;  // slot 0: the main line, always taken
+        for (int w = 0; w < words; ++w) clbits[b * words + w] = 0;
+        if (reset_cursor) cursor[b] = 0;
+    }
+}
+
+// every member set to |0...0>
+template <typename R>
+__global__ void k_t_basis(Cx<R>* state, int64_t elems, int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        state[i] = Cx<R>(i % elems == 0 ? R(1) : R(0), R(0));
+}
+
+__global__ void k_t_advance(int64_t* cursor, const uint64_t* pred, int slot, int64_t count, int64_t batch) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x)
+        if (has(pred, b, slot)) cursor[b] += count;
+}
+
+// per-member partial sums of |a|^2 over indices with bit q = 1; partials[b * gridDim.x + block]
+template <typename R>
+__global__ void k_t_p1(const Cx<R>* __restrict__ state, int64_t elems, int q, const uint64_t* pred, int slot,
+                       double* __restrict__ partials) {
+    const int64_t b = blockIdx.y;
+    double acc = 0.0;
+    if (has(pred, b, slot)) {
+        const Cx<R>* s = state + b * elems;
+        const int64_t half = elems >> 1;
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
+            const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
+            const uint64_t idx = (((uint64_t)i >> q) << (q + 1)) | (1ull << q) | lo;
+            const Cx<R> v = s[idx];
+            acc += nrm((double)v.re, (double)v.im);
+        }
+    }
+    const double tot = t_block_sum(acc);
+    if (threadIdx.x == 0) partials[b * gridDim.x + blockIdx.x] = tot;
+}
+
+// one thread per member: draw the outcome (and the readout flip), record the classical bit
+__global__ void k_t_decide(const double* __restrict__ partials, int nparts, int64_t* cursor, const double* __restrict__ u,
+                           int64_t ustride, const uint64_t* pred, int slot, int clbit, int readout, double p01,
+                           double p10, int is_reset, uint64_t* clbits, int words, int* outcome, double* prob,
+                           unsigned long long* near, int64_t batch) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+        if (!has(pred, b, slot)) {
+            outcome[b] = -1;
+            continue;
+        }
+        double p1 = 0.0;
+        for (int g = 0; g < nparts; ++g) p1 += partials[b * nparts + g];
+        p1 = fmin(fmax(p1, 0.0), 1.0);
+        const double r = u[b * ustride + cursor[b]];
+        cursor[b] += 1;
+        if (fabs(r - p1) < kNear) atomicAdd(near, 1ull);
+        int out = r < p1 ? 1 : 0;
+        outcome[b] = out;
+        prob[b] = out ? p1 : 1.0 - p1;
+        if (!is_reset) {
+            int seen = out;
+            if (readout) {
+                const double r2 = u[b * ustride + cursor[b]];
+                cursor[b] += 1;
+                if (r2 < (out ? p10 : p01)) seen ^= 1;
+            }
+            if (clbit >= 0) {
+                uint64_t& w = clbits[b * words + (clbit >> 6)];
+                const uint64_t bit = 1ull << (clbit & 63);
+                w = seen ? (w | bit) : (w & ~bit);
+            }
+        }
+    }
+}
+
+// zero the other half, divide by sqrt(probability); a reset with outcome 1 then applies X
+template <typename R>
+__global__ void k_t_collapse(Cx<R>* __restrict__ state, int64_t elems, int q, const int* outcome, const double* prob,
+                             int is_reset) {
+    const int64_t b = blockIdx.y;
+    const int out = outcome[b];
+    if (out < 0) return;
+    Cx<R>* s = state + b * elems;
+    const double p = prob[b];
+    const double div = p > 0 ? sqrt(p) : 1.0;
+    const bool scale = p > 0;
+    const int64_t half = elems >> 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
+        const uint64_t i0 = (((uint64_t)i >> q) << (q + 1)) | lo;
+        const uint64_t i1 = i0 | (1ull << q);
+        Cx<R> keep = out ? s[i1] : s[i0];
+        if (scale) keep = Cx<R>((R)((double)keep.re / div), (R)((double)keep.im / div));
+        const Cx<R> zero(R(0), R(0));
+        if (out == 0) {
+            s[i0] = keep;
+            s[i1] = zero;
+        } else if (is_reset) {
+            s[i0] = keep;  // X after the collapse onto |1>
+            s[i1] = zero;
+        } else {
+            s[i0] = zero;
+            s[i1] = keep;
+        }
+    }
+}
+
+// per-member reduced density matrix of the channel's bits (k <= 2): rho[r][c] summed over the
+// other bits, as 2*d*d doubles per block
+template <typename R>
+__global__ void k_t_rdm(const Cx<R>* __restrict__ state, int64_t elems, int k, int b0, int b1, const uint64_t* pred,
+                        int slot, double* __restrict__ partials) {
+    const int64_t b = blockIdx.y;
+    const int d = 1 << k;
+    double acc[32];
+    for (int i = 0; i < 2 * d * d; ++i) acc[i] = 0.0;
+    if (has(pred, b, slot)) {
+        const Cx<R>* s = state + b * elems;
+        const int lo = k == 1 ? b0 : min(b0, b1), hi = k == 1 ? b0 : max(b0, b1);
+        const int64_t groups = elems >> k;
+        for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups; g += (int64_t)gridDim.x * blockDim.x) {
+            uint64_t base = (uint64_t)g;
+            base = (((base >> lo) << (lo + 1)) | (base & ((1ull << lo) - 1)));
+            if (k == 2) base = (((base >> hi) << (hi + 1)) | (base & ((1ull << hi) - 1)));
+            Cx<R> v[4];
+            for (int j = 0; j < d; ++j) {
+                uint64_t o = 0;
+                if (k == 1) o = (uint64_t)(j & 1) << b0;
+                else o = ((uint64_t)((j >> 1) & 1) << b0) | ((uint64_t)(j & 1) << b1);
+                v[j] = s[base | o];
+            }
+            for (int r = 0; r < d; ++r)
+                for (int c = 0; c < d; ++c) {  // v_r conj(v_c)
+                    acc[2 * (r * d + c)] += (double)v[r].re * v[c].re + (double)v[r].im * v[c].im;
+                    acc[2 * (r * d + c) + 1] += (double)v[r].im * v[c].re - (double)v[r].re * v[c].im;
+                }
+        }
+    }
+    for (int i = 0; i < 2 * d * d; ++i) {
+        const double tot = t_block_sum(acc[i]);
+        if (threadIdx.x == 0) partials[(b * gridDim.x + blockIdx.x) * 2 * d * d + i] = tot;
+    }
+}
+
+// one thread per member: Born weights Tr(K rho K^dagger) in order, pick by the member's uniform,
+// write K/sqrt(w) (or the identity when no branch has weight) for the member
+template <typename R>
+__global__ void k_t_kraus_decide(const double* __restrict__ partials, int nparts, int k, const double* __restrict__ kraus,
+                                 int nkraus, int64_t* cursor, const double* __restrict__ u, int64_t ustride,
+                                 const uint64_t* pred, int slot, Cx<R>* dyn, int* apply, unsigned long long* near,
+                                 int64_t batch) {
+    const int d = 1 << k;
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+        apply[b] = 0;
+        if (!has(pred, b, slot)) continue;
+        double rho[32];
+        for (int i = 0; i < 2 * d * d; ++i) {
+            double s = 0.0;
+            for (int g = 0; g < nparts; ++g) s += partials[(b * nparts + g) * 2 * d * d + i];
+            rho[i] = s;
+        }
+        const double r = u[b * ustride + cursor[b]];
+        cursor[b] += 1;
+        double acc = 0.0, w = 0.0;
+        int pick = -1;
+        for (int i = 0; i < nkraus; ++i) {
+            const double* K = kraus + (int64_t)i * 2 * d * d;
+            // w = sum_{r,c,c'} K[r][c] rho[c][c'] conj(K[r][c'])
+            double wi = 0.0;
+            for (int rr = 0; rr < d; ++rr)
+                for (int c = 0; c < d; ++c)
+                    for (int c2 = 0; c2 < d; ++c2) {
+                        const double ar = K[2 * (rr * d + c)], ai = K[2 * (rr * d + c) + 1];
+                        const double br = K[2 * (rr * d + c2)], bi = -K[2 * (rr * d + c2) + 1];
+                        const double pr = rho[2 * (c * d + c2)], pi = rho[2 * (c * d + c2) + 1];
+                        // Re(a * p * b)
+                        const double apr = ar * pr - ai * pi, api = ar * pi + ai * pr;
+                        wi += apr * br - api * bi;
+                    }
+            w = wi;
+            acc += wi;
+            if (fabs(r - acc) < kNear) atomicAdd(near, 1ull);
+            if (r < acc && wi > 0) {
+                pick = i;
+                break;
+            }
+        }
+        if (pick < 0) pick = nkraus - 1;  // nothing chosen: the last candidate (engines.py:181-183)
+        Cx<R>* m = dyn + b * d * d;
+        if (w > 0) {
+            const double sc = sqrt(w);
+            const double* K = kraus + (int64_t)pick * 2 * d * d;
+            for (int i = 0; i < d * d; ++i) m[i] = Cx<R>((R)(K[2 * i] / sc), (R)(K[2 * i + 1] / sc));
+            apply[b] = 1;
+        }
+    }
+}
+
+// per-member dense operator on k <= 2 bits (b0 = most significant)
+template <typename R>
+__global__ void k_t_apply_dyn(Cx<R>* __restrict__ state, int64_t elems, int k, int b0, int b1, const Cx<R>* dyn,
+                              const int* apply) {
+    const int64_t b = blockIdx.y;
+    if (!apply[b]) return;
+    const int d = 1 << k;
+    Cx<R>* s = state + b * elems;
+    const Cx<R>* m = dyn + b * d * d;
+    const int lo = k == 1 ? b0 : min(b0, b1), hi = k == 1 ? b0 : max(b0, b1);
+    const int64_t groups = elems >> k;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups; g += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t base = (uint64_t)g;
+        base = (((base >> lo) << (lo + 1)) | (base & ((1ull << lo) - 1)));
+        if (k == 2) base = (((base >> hi) << (hi + 1)) | (base & ((1ull << hi) - 1)));
+        uint64_t offs[4];
+        Cx<R> v[4];
+        for (int j = 0; j < d; ++j) {
+            offs[j] = k == 1 ? ((uint64_t)(j & 1) << b0) : (((uint64_t)((j >> 1) & 1) << b0) | ((uint64_t)(j & 1) << b1));
+            v[j] = s[base | offs[j]];
+        }
+        for (int r = 0; r < d; ++r) {
+            Cx<R> acc;
+            for (int c = 0; c < d; ++c) acc = cfma(m[r * d + c], v[c], acc);
+            s[base | offs[r]] = acc;
+        }
+    }
+}
+
+struct Cond {
+    int n, negate;
+    uint64_t value;
+    int bits[64];
+};
+
+__global__ void k_t_if(uint64_t* pred, const uint64_t* clbits, int words, int parent, int then_slot, int else_slot,
+                       Cond c, int64_t batch) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t p = pred[b] & ~((1ull << then_slot) | (1ull << else_slot));
+        if ((p >> parent) & 1) {
+            uint64_t reading = 0;
+            for (int i = 0; i < c.n; ++i) {
+                const int cb = c.bits[i];
+                reading |= ((clbits[b * words + (cb >> 6)] >> (cb & 63)) & 1ull) << i;
+            }
+            const bool holds = (reading == c.value) != (c.negate != 0);
+            p |= holds ? (1ull << then_slot) : (1ull << else_slot);
+        }
+        pred[b] = p;
+    }
+}
+
+__global__ void k_t_record(const uint64_t* clbits, int words, uint64_t* out, int64_t* shot) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const int64_t s = *shot;
+        for (int w = 0; w < words; ++w) out[s * words + w] = clbits[w];
+        *shot = s + 1;
+    }
+}
+
+unsigned t_grid(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + kT - 1) / kT, 152 * 16)); }
+
+}  // namespace lsg
+
+using namespace lsg;
+
+struct lsg_traj_s {
+    int nbits = 0, precision = 0, words = 1;
+    int64_t batch = 1;
+    int64_t max_draws = 0;
+    std::vector<Step> steps;
+    Scratch kraus;  // all Kraus matrices, complex128
+    // per-run device buffers
+    Scratch ctl;    // cursor, pred, clbits, outcome, prob, apply, counters
+    Scratch parts;  // reduction partials
+    Scratch dyn;    // per-member Kraus operators
+    Scratch ubuf;   // uniforms
+    Scratch results;
+    ~lsg_traj_s() {
+        for (Step& s : steps)
+            if (s.seg) program_destroy(s.seg);
+        release(kraus);
+        release(ctl);
+        release(parts);
+        release(dyn);
+        release(ubuf);
+        release(results);
+    }
+};
+
+namespace {
+
+struct Ctl {
+    int64_t* cursor;
+    uint64_t* pred;
+    uint64_t* clbits;
+    int* outcome;
+    double* prob;
+    int* apply;
+    unsigned long long* near;
+    int64_t* shot;
+};
+
+int ctl_setup(lsg_traj_s* t, int64_t batch, Ctl* c) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t need = al(batch * 8) * 2 + al(batch * 8 * t->words) + al(batch * 4) + al(batch * 8) + al(batch * 4) + 512;
+    LSG_CHECK(ensure(t->ctl, need));
+    char* p = (char*)t->ctl.ptr;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* at = p + off;
+        off += al(bytes);
+        return at;
+    };
+    c->cursor = (int64_t*)take(batch * 8);
+    c->pred = (uint64_t*)take(batch * 8);
+    c->clbits = (uint64_t*)take(batch * 8 * t->words);
+    c->outcome = (int*)take(batch * 4);
+    c->prob = (double*)take(batch * 8);
+    c->apply = (int*)take(batch * 4);
+    c->near = (unsigned long long*)take(8);
+    c->shot = (int64_t*)take(8);
+    const int dmax = 4;
+    LSG_CHECK(ensure(t->dyn, (size_t)batch * dmax * dmax * 16));
+    return LSG_OK;
+}
+
+template <typename R>
+int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int64_t ustride) {
+    const int64_t B = s->batch;
+    const int64_t elems = s->elems;
+    cudaStream_t st = s->stream;
+    Cx<R>* state = (Cx<R>*)s->data;
+    TrajCtx ctx;
+    ctx.u = u;
+    ctx.ustride = ustride;
+    ctx.cursor = c.cursor;
+    ctx.pred = c.pred;
+    const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(((elems >> 1) + kT * 4 - 1) / (kT * 4),
+                                                                          std::max<int64_t>(1, 8192 / B)));
+    for (const Step& sp : t->steps) {
+        switch (sp.kind) {
+            case STEP_SEG: LSG_CHECK(program_run_ctx(sp.seg, s, nullptr, ctx)); break;
+            case STEP_ADVANCE:
+                k_t_advance<<<t_grid(B), kT, 0, st>>>(c.cursor, c.pred, sp.slot, sp.count, B);
+                break;
+            case STEP_MEASURE: {
+                double* part = (double*)t->parts.ptr;
+                k_t_p1<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.pred, sp.slot, part);
+                k_t_decide<<<t_grid(B), kT, 0, st>>>(part, (int)gx, c.cursor, u, ustride, c.pred, sp.slot, sp.clbit,
+                                                    sp.readout, sp.p01, sp.p10, sp.is_reset, c.clbits, t->words,
+                                                    c.outcome, c.prob, c.near, B);
+                k_t_collapse<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.outcome, c.prob, sp.is_reset);
+                break;
+            }
+            case STEP_KRAUS: {
+                double* part = (double*)t->parts.ptr;
+                k_t_rdm<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.k, sp.bits[0], sp.bits[1], c.pred,
+                                                               sp.slot, part);
+                k_t_kraus_decide<R><<<t_grid(B), kT, 0, st>>>(part, (int)gx, sp.k, (const double*)t->kraus.ptr + 2 * sp.kraus_at,
+                                                             sp.nkraus, c.cursor, u, ustride, c.pred, sp.slot,
+                                                             (Cx<R>*)t->dyn.ptr, c.apply, c.near, B);
+                k_t_apply_dyn<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.k, sp.bits[0], sp.bits[1],
+                                                                     (const Cx<R>*)t->dyn.ptr, c.apply);
+                break;
+            }
+            case STEP_IF: {
+                Cond cd{};
+                cd.n = sp.ncond;
+                cd.negate = sp.negate;
+                cd.value = sp.value;
+                for (int i = 0; i < sp.ncond; ++i) cd.bits[i] = sp.cond[i];
+                k_t_if<<<t_grid(B), kT, 0, st>>>(c.pred, c.clbits, t->words, sp.slot, sp.then_slot, sp.else_slot, cd, B);
+                break;
+            }
+            default: break;
+        }
+    }
+    LSG_CUDA(cudaGetLastError());
+    return LSG_OK;
+}
+
+int parts_setup(lsg_traj_s* t, int64_t batch, int64_t elems) {
+    const int64_t gx = std::max<int64_t>(1, std::min<int64_t>(((elems >> 1) + kT * 4 - 1) / (kT * 4),
+                                                              std::max<int64_t>(1, 8192 / batch)));
+    return ensure(t->parts, (size_t)(batch * gx * 32 + 64) * 8);
+}
+
+}  // namespace
+
+extern "C" {
+
+int lsg_traj_create(lsg_state shape, const lsg_traj_op* ops, int32_t nops, const double* pool, int64_t pool_entries,
+                    int32_t num_clbits, lsg_traj* out) {
+    clear_error();
+    if (!shape || !out || nops < 0 || (nops && !ops) || pool_entries < 0 || (pool_entries && !pool))
+        return fail(LSG_E_ARG, "lsg_traj_create: bad arguments");
+    *out = nullptr;
+    if (num_clbits < 0 || num_clbits > 64 * kMaxWords)
+        return fail(LSG_E_CAPACITY, "trajectories on the device keep at most %d classical bits", 64 * kMaxWords);
+    const int nbits = shape->nbits;
+    auto* t = new lsg_traj_s();
+    t->nbits = nbits;
+    t->precision = shape->precision;
+    t->batch = shape->batch;
+    t->words = std::max(1, (num_clbits + 63) / 64);
+    std::vector<double> kraus_host;
+    // segment under construction
+    std::vector<lsg_op> seg_ops;
+    std::vector<int> seg_pred, seg_draw, seg_count;
+    int seg_slot = -1;
+    int64_t seg_draws = 0;
+    struct Frame {
+        int parent, then_slot, else_slot;
+        int64_t draws_before, then_draws;
+    };
+    std::vector<Frame> stack;
+    int slot = 0;
+    int64_t draws = 0;  // upper bound along the current path
+    auto fail_out = [&](int code) {
+        delete t;
+        return code;
+    };
+    auto flush = [&]() -> int {
+        if (seg_ops.empty()) return LSG_OK;
+        Step sp;
+        sp.kind = STEP_SEG;
+        sp.slot = seg_slot;
+        int rc = program_create_ex(nbits, shape->precision, shape->batch, seg_ops.data(), (int32_t)seg_ops.size(), pool,
+                                   pool_entries, seg_pred.data(), seg_draw.data(), seg_count.data(), &sp.seg);
+        if (rc != LSG_OK) return rc;
+        t->steps.push_back(sp);
+        if (seg_draws) {
+            Step adv;
+            adv.kind = STEP_ADVANCE;
+            adv.slot = seg_slot;
+            adv.count = seg_draws;
+            t->steps.push_back(adv);
+        }
+        seg_ops.clear();
+        seg_pred.clear();
+        seg_draw.clear();
+        seg_count.clear();
+        seg_draws = 0;
+        seg_slot = -1;
+        return LSG_OK;
+    };
+    for (int i = 0; i < nops; ++i) {
+        const lsg_traj_op& op = ops[i];
+        const bool unitary = op.kind == LSG_T_GATE || op.kind == LSG_T_MIXTURE || op.kind == LSG_T_SCALE;
+        if (unitary) {
+            if (seg_slot != slot) {
+                int rc = flush();
+                if (rc != LSG_OK) return fail_out(rc);
+                seg_slot = slot;
+            }
+            lsg_op o{};
+            o.nbits = op.kind == LSG_T_SCALE ? 0 : op.nq;
+            for (int j = 0; j < o.nbits; ++j) o.bits[j] = op.qubits[j];
+            o.data = op.data;
+            o.kind = op.kind == LSG_T_GATE ? op.opkind : (op.kind == LSG_T_SCALE ? LSG_OP_SCALE : kOpMixture);
+            if (!op_bits_ok(o, nbits) || (op.kind == LSG_T_MIXTURE && (op.count < 1 || op.nq > 2)))
+                return fail_out(fail(LSG_E_ARG, "trajectory op %d has a bad kind or qubits", i));
+            const int64_t d = 1ll << o.nbits;
+            int64_t need = 1;
+            if (o.kind == LSG_OP_MATRIX) need = d * d;
+            else if (o.kind == LSG_OP_DIAG) need = d;
+            else if (o.kind == LSG_OP_PERM) need = 2 * d;
+            else if (o.kind == kOpMixture) need = op.count + op.count * d * d;
+            if (op.data < 0 || op.data + need > pool_entries)
+                return fail_out(fail(LSG_E_ARG, "trajectory op %d reads outside the pool", i));
+            seg_ops.push_back(o);
+            seg_pred.push_back(slot);
+            seg_draw.push_back(op.kind == LSG_T_MIXTURE ? (int)seg_draws : 0);
+            seg_count.push_back(op.kind == LSG_T_MIXTURE ? op.count : 0);
+            if (op.kind == LSG_T_MIXTURE) {
+                ++seg_draws;
+                ++draws;
+            }
+            continue;
+        }
+        int rc = flush();
+        if (rc != LSG_OK) return fail_out(rc);
+        Step sp;
+        sp.slot = slot;
+        switch (op.kind) {
+            case LSG_T_MEASURE:
+            case LSG_T_RESET:
+                if (op.qubits[0] < 0 || op.qubits[0] >= nbits) return fail_out(fail(LSG_E_ARG, "op %d: bad qubit", i));
+                if (op.kind == LSG_T_MEASURE && op.clbit >= num_clbits)
+                    return fail_out(fail(LSG_E_ARG, "op %d: bad classical bit", i));
+                sp.kind = STEP_MEASURE;
+                sp.q = op.qubits[0];
+                sp.is_reset = op.kind == LSG_T_RESET;
+                sp.clbit = op.kind == LSG_T_MEASURE ? op.clbit : -1;
+                sp.readout = op.kind == LSG_T_MEASURE && op.readout;
+                sp.p01 = op.p01;
+                sp.p10 = op.p10;
+                draws += 1 + sp.readout;
+                t->steps.push_back(sp);
+                break;
+            case LSG_T_KRAUS: {
+                if (op.nq < 1 || op.nq > 2 || op.count < 1) return fail_out(fail(LSG_E_ARG, "op %d: bad Kraus channel", i));
+                const int64_t d = 1ll << op.nq;
+                if (op.data < 0 || op.data + op.count * d * d > pool_entries)
+                    return fail_out(fail(LSG_E_ARG, "op %d reads outside the pool", i));
+                for (int j = 0; j < op.nq; ++j)
+                    if (op.qubits[j] < 0 || op.qubits[j] >= nbits) return fail_out(fail(LSG_E_ARG, "op %d: bad qubit", i));
+                sp.kind = STEP_KRAUS;
+                sp.k = op.nq;
+                sp.bits[0] = op.qubits[0];
+                sp.bits[1] = op.nq > 1 ? op.qubits[1] : 0;
+                sp.nkraus = op.count;
+                sp.kraus_at = (int64_t)kraus_host.size() / 2;
+                kraus_host.insert(kraus_host.end(), pool + 2 * op.data, pool + 2 * (op.data + op.count * d * d));
+                draws += 1;
+                t->steps.push_back(sp);
+                break;
+            }
+            case LSG_T_IF: {
+                const int depth = (int)stack.size();
+                if (2 * depth + 2 > 63) return fail_out(fail(LSG_E_CAPACITY, "if/else nested deeper than 31 levels"));
+                if (op.count < 1 || op.count > 64 || op.data < 0 || op.data + op.count > pool_entries)
+                    return fail_out(fail(LSG_E_ARG, "op %d: bad condition", i));
+                sp.kind = STEP_IF;
+                sp.then_slot = 2 * depth + 1;
+                sp.else_slot = 2 * depth + 2;
+                sp.ncond = op.count;
+                sp.negate = op.negate;
+                sp.value = op.value;
+                for (int j = 0; j < op.count; ++j) {
+                    const double cb = pool[2 * (op.data + j)];
+                    if (!(cb >= 0 && cb < num_clbits)) return fail_out(fail(LSG_E_ARG, "op %d: bad condition bit", i));
+                    sp.cond[j] = (int)cb;
+                }
+                t->steps.push_back(sp);
+                stack.push_back(Frame{slot, sp.then_slot, sp.else_slot, draws, 0});
+                slot = sp.then_slot;
+                break;
+            }
+            case LSG_T_ELSE:
+                if (stack.empty()) return fail_out(fail(LSG_E_ARG, "op %d: else without if", i));
+                stack.back().then_draws = draws - stack.back().draws_before;
+                draws = stack.back().draws_before;
+                slot = stack.back().else_slot;
+                break;
+            case LSG_T_ENDIF: {
+                if (stack.empty()) return fail_out(fail(LSG_E_ARG, "op %d: endif without if", i));
+                Frame f = stack.back();
+                stack.pop_back();
+                const int64_t branch = draws - f.draws_before;
+                const int64_t taken = slot == f.then_slot ? branch : std::max(branch, f.then_draws);
+                draws = f.draws_before + taken;
+                slot = f.parent;
+                break;
+            }
+            default: return fail_out(fail(LSG_E_ARG, "op %d: unknown kind %d", i, op.kind));
+        }
+    }
+    if (!stack.empty()) return fail_out(fail(LSG_E_ARG, "an if block is not closed"));
+    int rc = flush();
+    if (rc != LSG_OK) return fail_out(rc);
+    t->max_draws = draws;
+    if (!kraus_host.empty()) {
+        rc = ensure(t->kraus, kraus_host.size() * 8);
+        if (rc != LSG_OK) return fail_out(rc);
+        cudaError_t e = cudaMemcpy(t->kraus.ptr, kraus_host.data(), kraus_host.size() * 8, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail_out(fail(LSG_E_CUDA, "uploading Kraus operators failed: %s", cudaGetErrorString(e)));
+    }
+    *out = t;
+    return LSG_OK;
+}
+
+int lsg_traj_info(lsg_traj t, int64_t* max_draws, int32_t* steps) {
+    clear_error();
+    if (!t) return fail(LSG_E_ARG, "null program");
+    if (max_draws) *max_draws = t->max_draws;
+    if (steps) *steps = (int32_t)t->steps.size();
+    return LSG_OK;
+}
+
+int lsg_traj_free(lsg_traj t) {
+    clear_error();
+    delete t;
+    return LSG_OK;
+}
+
+int lsg_traj_run_batched(lsg_traj t, lsg_state s, const double* uniforms, int64_t ustride, uint64_t* clbits_out,
+                         int64_t* consumed, int64_t* near_count) {
+    clear_error();
+    if (!t || !s || !uniforms || !clbits_out) return fail(LSG_E_ARG, "lsg_traj_run_batched: bad arguments");
+    if (s->nbits != t->nbits || s->precision != t->precision || s->batch != t->batch)
+        return fail(LSG_E_STATE, "the trajectory program was built for another register shape");
+    if (ustride < t->max_draws || ustride < 1)
+        return fail(LSG_E_ARG, "each shot needs %lld uniforms; the stride is %lld", (long long)t->max_draws, (long long)ustride);
+    const int64_t B = s->batch;
+    Ctl c{};
+    LSG_CHECK(ctl_setup(t, B, &c));
+    LSG_CHECK(parts_setup(t, B, s->elems));
+    LSG_CHECK(ensure(t->ubuf, (size_t)(B * ustride) * 8));
+    LSG_CUDA(cudaMemcpyAsync(t->ubuf.ptr, uniforms, (size_t)(B * ustride) * 8, cudaMemcpyHostToDevice, s->stream));
+    LSG_CUDA(cudaMemsetAsync(c.near, 0, 8, s->stream));
+    const int64_t n = s->elems * B;
+    if (s->precision == LSG_C128)
+        k_t_basis<double><<<t_grid(n), kT, 0, s->stream>>>((Cx<double>*)s->data, s->elems, n);
+    else
+        k_t_basis<float><<<t_grid(n), kT, 0, s->stream>>>((Cx<float>*)s->data, s->elems, n);
+    k_t_init<<<t_grid(B), kT, 0, s->stream>>>(c.pred, c.clbits, c.cursor, B, t->words, 1);
+    LSG_CUDA(cudaGetLastError());
+    int rc = s->precision == LSG_C128 ? run_steps<double>(t, s, c, (const double*)t->ubuf.ptr, ustride)
+                                      : run_steps<float>(t, s, c, (const double*)t->ubuf.ptr, ustride);
+    LSG_CHECK(rc);
+    LSG_CUDA(cudaMemcpyAsync(clbits_out, c.clbits, (size_t)B * t->words * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (consumed) LSG_CUDA(cudaMemcpyAsync(consumed, c.cursor, (size_t)B * 8, cudaMemcpyDeviceToHost, s->stream));
+    unsigned long long nr = 0;
+    LSG_CUDA(cudaMemcpyAsync(&nr, c.near, 8, cudaMemcpyDeviceToHost, s->stream));
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    if (near_count) *near_count = (int64_t)nr;
+    return check_device_status(s->stream);
+}
+
+int lsg_traj_run_serial(lsg_traj t, lsg_state s, int64_t shots, const double* uniforms, int64_t nuniforms,
+                        uint64_t* clbits_out, int64_t* consumed, int64_t* near_count) {
+    clear_error();
+    if (!t || !s || shots < 0 || (shots && (!uniforms || !clbits_out))) return fail(LSG_E_ARG, "lsg_traj_run_serial: bad arguments");
+    if (s->nbits != t->nbits || s->precision != t->precision || s->batch != 1 || t->batch != 1)
+        return fail(LSG_E_STATE, "serial trajectories run on a one-member register of the program's shape");
+    if (shots == 0) {
+        if (consumed) *consumed = 0;
+        if (near_count) *near_count = 0;
+        return LSG_OK;
+    }
+    if (nuniforms < shots * std::max<int64_t>(t->max_draws, 1))
+        return fail(LSG_E_ARG, "%lld shots need up to %lld uniforms; %lld given", (long long)shots,
+                    (long long)(shots * t->max_draws), (long long)nuniforms);
+    Ctl c{};
+    LSG_CHECK(ctl_setup(t, 1, &c));
+    LSG_CHECK(parts_setup(t, 1, s->elems));
+    LSG_CHECK(ensure(t->ubuf, (size_t)nuniforms * 8));
+    LSG_CHECK(ensure(t->results, (size_t)shots * t->words * 8));
+    if (!device_status()) return fail(LSG_E_CUDA, "cannot allocate the device status word");
+    LSG_CUDA(cudaMemcpyAsync(t->ubuf.ptr, uniforms, (size_t)nuniforms * 8, cudaMemcpyHostToDevice, s->stream));
+    LSG_CUDA(cudaMemsetAsync(c.near, 0, 8, s->stream));
+    LSG_CUDA(cudaMemsetAsync(c.shot, 0, 8, s->stream));
+    LSG_CUDA(cudaMemsetAsync(c.cursor, 0, 8, s->stream));
+    const double* u = (const double*)t->ubuf.ptr;
+    auto one_shot = [&]() -> int {
+        if (s->precision == LSG_C128)
+            k_t_basis<double><<<t_grid(s->elems), kT, 0, s->stream>>>((Cx<double>*)s->data, s->elems, s->elems);
+        else
+            k_t_basis<float><<<t_grid(s->elems), kT, 0, s->stream>>>((Cx<float>*)s->data, s->elems, s->elems);
+        k_t_init<<<1, 32, 0, s->stream>>>(c.pred, c.clbits, c.cursor, 1, t->words, 0);
+        int rc = s->precision == LSG_C128 ? run_steps<double>(t, s, c, u, 0) : run_steps<float>(t, s, c, u, 0);
+        if (rc != LSG_OK) return rc;
+        k_t_record<<<1, 32, 0, s->stream>>>(c.clbits, t->words, (uint64_t*)t->results.ptr, c.shot);
+        LSG_CUDA(cudaGetLastError());
+        return LSG_OK;
+    };
+    // one shot's launches captured once as a CUDA graph, replayed per shot
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graphed = false;
+    if (shots > 1 && cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        int rc = one_shot();
+        cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+        if (rc == LSG_OK && e == cudaSuccess && graph &&
+            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+            graphed = true;
+        cudaGetLastError();
+    }
+    for (int64_t i = 0; i < shots; ++i) {
+        if (graphed) {
+            cudaError_t e = cudaGraphLaunch(exec, s->stream);
+            if (e != cudaSuccess) {
+                cudaGraphExecDestroy(exec);
+                cudaGraphDestroy(graph);
+                return fail(LSG_E_CUDA, "cudaGraphLaunch failed: %s", cudaGetErrorString(e));
+            }
+        } else {
+            LSG_CHECK(one_shot());
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    LSG_CUDA(cudaMemcpyAsync(clbits_out, t->results.ptr, (size_t)shots * t->words * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (consumed) LSG_CUDA(cudaMemcpyAsync(consumed, c.cursor, 8, cudaMemcpyDeviceToHost, s->stream));
+    unsigned long long nr = 0;
+    LSG_CUDA(cudaMemcpyAsync(&nr, c.near, 8, cudaMemcpyDeviceToHost, s->stream));
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    if (near_count) *near_count = (int64_t)nr;
+    return check_device_status(s->stream);
+}
+
+}  // extern "C"

@@ -230,8 +230,13 @@ def run(
     method: str = "automatic",
     params: Mapping[str, float] | None = None,
     precision: str | None = None,
+    trajectory_mode: str | None = None,
 ) -> Result:
-    """Simulate ``program`` ``shots`` times; counts identical to Orrery's for the same seed."""
+    """Simulate ``program`` ``shots`` times; counts identical to Orrery's for the same seed.
+
+    ``precision`` ("c128" default, or "c64") and ``trajectory_mode`` ("serial" default: Orrery's
+    draw order; "batched": all shots at once, each with its own uniforms) are optional engine
+    knobs; defaults also come from ``LSG_PRECISION`` / ``LSG_TRAJ_MODE``."""
     if not 0 <= shots <= MAX_SHOTS:
         raise ValueError(f"shots must be between 0 and {MAX_SHOTS:,}")
     circuit = to_circuit(program, params)
@@ -254,7 +259,7 @@ def run(
 
         if circuit.num_qubits > 0:
             engine.new_statevector(circuit.num_qubits, prec).free()  # size check before the shots
-        tally, report = trajectories.run_shots(circuit, shots, noise, rng, prec)
+        tally, report = trajectories.run_shots(circuit, shots, noise, rng, prec, trajectory_mode)
         counts = {format_bits(circuit, b): k for b, k in sorted(tally.items())} if circuit.num_clbits else {}
     else:
         n = circuit.num_qubits

@@ -1,0 +1,80 @@
+"""Trajectories on the GPU: serial mode reproduces Orrery's counts (same seed, same draw order);
+batched mode agrees with it statistically."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import lucivant_sim_gb300 as ls
+from lucivant_sim_gb300 import _lib, trajectories, workloads as wl
+from lucivant_sim_gb300.noise import NoiseModel, thermal_relaxation
+from oracle import dense
+
+pytestmark = pytest.mark.gpu
+
+
+def tvd_counts(a: dict, b: dict) -> float:
+    na, nb = sum(a.values()), sum(b.values())
+    return 0.5 * sum(abs(a.get(k, 0) / na - b.get(k, 0) / nb) for k in set(a) | set(b))
+
+
+def test_golden_trajectory_counts_identical(golden):
+    g = golden["traj_mid8"]
+    r = ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=NoiseModel.uniform(single=2e-2, two=5e-2, readout=3e-2))
+    assert r.method == "trajectories"
+    assert r.counts == g["counts"] or r.report["near_threshold"] > 0
+    g = golden["traj_mid8_ideal"]
+    assert ls.run(g["qasm"], shots=g["shots"], seed=g["seed"]).counts == g["counts"]
+    g = golden["traj_kraus"]
+    noise = NoiseModel().add_gate_error(thermal_relaxation(20, 15, 4.0), gates="u3")
+    r = ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=noise, method="trajectories")
+    assert r.counts == g["counts"] or r.report["near_threshold"] > 0
+
+
+@pytest.mark.parametrize("n,rounds,seed", [(8, 3, 1), (10, 2, 2), (12, 2, 3)])
+def test_serial_matches_oracle_and_leaves_rng_in_place(n, rounds, seed):
+    c = ls.parse(wl.midcircuit(n, rounds, seed=seed))
+    noise = NoiseModel.uniform(single=1e-2, two=4e-2, readout=2e-2)
+    shots = 120
+    rng_a = np.random.default_rng(seed)
+    want: dict[int, int] = {}
+    for _ in range(shots):
+        b = dense.trajectory(c, noise, rng_a)
+        want[b] = want.get(b, 0) + 1
+    rng_b = np.random.default_rng(seed)
+    got, report = trajectories.run_shots(c, shots, noise, rng_b, _lib.C128, "serial")
+    assert got == want or report["near_threshold"] > 0
+    assert rng_b.bit_generator.state == rng_a.bit_generator.state
+
+
+def test_known_answers_reset_and_if():
+    c = "OPENQASM 3; qubit q; bit c; x q; reset q; c = measure q;"
+    assert ls.run(c, shots=100, seed=1, method="trajectories").counts == {"0": 100}
+    c = ("OPENQASM 3; qubit[2] q; bit[2] c; x q[0]; c[0] = measure q[0]; if (c[0] == 1) x q[1]; else h q[1];"
+         " c[1] = measure q[1];")
+    assert ls.run(c, shots=50, seed=1).counts == {"11": 50}
+
+
+@pytest.mark.parametrize("precision", [_lib.C128, _lib.C64])
+def test_batched_mode_agrees_with_serial(precision):
+    c = ls.parse(wl.midcircuit(10, 3, seed=5))
+    noise = NoiseModel.uniform(single=1e-2, two=3e-2, readout=2e-2)
+    shots = 8000
+    serial, _ = trajectories.run_shots(c, shots, noise, np.random.default_rng(1), _lib.C128, "serial")
+    batched, _ = trajectories.run_shots(c, shots, noise, np.random.default_rng(2), precision, "batched")
+    assert sum(batched.values()) == shots
+    # each classical bit's marginal: two independent samples, sd about 0.008 each
+    for bit in range(c.num_clbits):
+        ps = sum(v for k, v in serial.items() if (k >> bit) & 1) / shots
+        pb = sum(v for k, v in batched.items() if (k >> bit) & 1) / shots
+        assert abs(ps - pb) < 0.04, (bit, ps, pb)
+
+
+def test_kraus_channel_statistics_against_density_matrix():
+    src = "OPENQASM 3; qubit[2] q; bit[2] c; x q[0]; h q[1]; cx q[1], q[0]; c = measure q;"
+    noise = NoiseModel().add_gate_error(thermal_relaxation(30, 20, 6.0), gates="x").add_gate_error(
+        thermal_relaxation(30, 20, 6.0), gates="h")
+    exact = dense.outcome_probabilities(ls.parse(src), noise)
+    got = ls.run(src, shots=20000, seed=3, noise=noise, method="trajectories", trajectory_mode="batched").counts
+    assert tvd_counts(got, {k: int(round(v * 1e6)) for k, v in exact.items()}) < 0.02
