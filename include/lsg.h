@@ -190,6 +190,58 @@ int lsg_traj_run_batched(lsg_traj t, lsg_state s, const double* uniforms, int64_
                          int64_t* consumed, int64_t* near_count);
 int lsg_traj_free(lsg_traj t);
 
+/* ---- stabilizer ------------------------------------------------------------------------------
+ * The Aaronson-Gottesman tableau of src/lucivant_sim/stabilizer.py on the device. Gates are given
+ * as codes: 0 id, 1 h, 2 s, 3 sdg, 4 x, 5 y, 6 z, 7 cx, 8 cz (the update rules of
+ * stabilizer.py:224-254), or 16 + t for conjugation table t (:256-264). A table record is 65
+ * bytes: the width k (1..3), then 64 entries indexed by the Pauli bits (x0 z0 x1 z1 ...), first
+ * qubit most significant, each (sign << 7) | image bits in the same order. */
+typedef struct lsg_cgate {
+    int16_t code;  /* gate code */
+    int16_t noise; /* Pauli-noise table after the gate, -1 for none (frames only) */
+    int16_t a, b, c;
+    int16_t nq; /* qubits of a table gate */
+    int32_t pad;
+} lsg_cgate;
+
+/* Pauli noise as branches (stabilizer.py:173-187): cumulative = np.cumsum(p) / sum(p), and per
+ * branch the (x, z) bits of each qubit, first qubit in the highest pair. */
+typedef struct lsg_noise_table {
+    int32_t k, nbranch;
+    double cumulative[16];
+    uint8_t label[16];
+} lsg_noise_table;
+
+typedef struct lsg_tab_s* lsg_tab;
+/* |0...0> on n <= 2048 qubits (Tableau.__init__, stabilizer.py:196-208). */
+int lsg_tab_create(int n, lsg_tab* out);
+int lsg_tab_free(lsg_tab t);
+/* Apply gates in order (noise fields ignored). */
+int lsg_tab_apply(lsg_tab t, const lsg_cgate* gates, int64_t ngates, const uint8_t* tables, int32_t ntables);
+/* The tableau as Orrery holds it: x, z as (n, 2n) uint8, r as (2n). */
+int lsg_tab_download(lsg_tab t, uint8_t* x, uint8_t* z, uint8_t* r);
+/* Tableau.support (stabilizer.py:333-365): x0 (m bytes) and the basis (rank x m bytes, may be
+ * NULL) of the outcomes on `qubits`. */
+int lsg_tab_support(lsg_tab t, const int32_t* qubits, int32_t m, uint8_t* x0, uint8_t* basis, int32_t* rank);
+/* _frames (stabilizer.py:514-563) plus _count's readout flips (:622-643): the noisy static
+ * circuit's Pauli frames over `shots`, drawing from the PCG64 generator state `rng_state`
+ * (state hi, state lo, inc hi, inc lo; no uint32 buffered) in Orrery's order: the frame bits, one
+ * uniform per shot per noisy gate, one per shot per readout pair with an error (pair_err >= 0).
+ * bits_out: shots x nclbits outcome bytes; raw_used: 64-bit draws consumed. */
+int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t* tables, int32_t ntables,
+                   const lsg_noise_table* noise, int32_t nnoise, int64_t shots, const uint64_t* rng_state,
+                   int32_t npairs, const int32_t* pair_qubit, const int32_t* pair_clbit, const uint8_t* pair_x0,
+                   const int32_t* pair_err, const double* p01, const double* p10, int32_t nclbits,
+                   uint8_t* bits_out, int64_t* raw_used);
+/* _sampled (stabilizer.py:597-619) plus readout: x0 XOR basis combinations chosen by the stream's
+ * uint8 integers, then the readout flips. */
+int lsg_stab_sample(int m, const uint8_t* x0, const uint8_t* basis, int32_t nb, int64_t shots,
+                    const uint64_t* rng_state, int32_t npairs, const int32_t* pair_pos, const int32_t* pair_clbit,
+                    const int32_t* pair_err, const double* p01, const double* p10, int32_t nclbits,
+                    uint8_t* bits_out, int64_t* raw_used);
+/* Host-side check of the generator: raw draw number `index` after the state (4 words as above). */
+int lsg_pcg_raw(const uint64_t* state, uint64_t index, uint64_t* out);
+
 /* ---- allocation-free expectations ---------------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that cannot let the library
  * allocate device memory (a runtime or framework that owns the whole GPU through its own memory

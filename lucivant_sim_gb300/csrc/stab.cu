@@ -1,0 +1,995 @@
+// The stabilizer engine (Orrery's src/lucivant_sim/stabilizer.py) on the device.
+//
+//  * Tableau: x, z bit-packed qubit-major — word w of qubit q holds rows 32w..32w+31 — and the
+//    sign bits r; rows 0..n-1 destabilizers, n..2n-1 stabilizers (stabilizer.py:193-208). Gates
+//    are applied moment by moment (gates of a moment act on disjoint qubits): one CTA per 32-row
+//    word column keeps that column of x and z in shared memory and its threads take the gates of
+//    a moment in parallel; sign updates are XOR-combined. Named gates use the update rules of
+//    stabilizer.py:224-254, other Clifford gates the conjugation table (:256-264).
+//  * support(): GF(2) elimination on the stabilizer rows packed row-major in 64-bit words, with
+//    the reference's pivot rule (first unused row with the bit set, qubits ascending) and the
+//    popcount phase arithmetic of _rowsum_packed (stabilizer.py:333-395); then the Z constraints
+//    (:398-422) and, for a subset of qubits, the row basis (:425-440).
+//  * Pauli frames (stabilizer.py:514-563): one CTA per 32-shot word keeps every qubit's frame
+//    word in shared memory; noise branches come from a device PCG64 that regenerates the run's
+//    NumPy stream bit for bit (128-bit LCG, XSL-RR output, jump-ahead), so counts are identical.
+//  * Ideal sampling (stabilizer.py:597-619): x0 plus combinations of the basis picked by the
+//    same stream's uint8 integers.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace lsg {
+
+typedef unsigned __int128 u128;
+
+__host__ __device__ __forceinline__ u128 pcg_mult() {
+    return ((u128)0x2360ED051FC65DA4ull << 64) | (u128)0x4385DF649FCCF645ull;
+}
+
+__host__ __device__ __forceinline__ uint64_t pcg_output(u128 s) {
+    const uint64_t hi = (uint64_t)(s >> 64), lo = (uint64_t)s;
+    const uint64_t x = hi ^ lo;
+    const unsigned r = (unsigned)(hi >> 58);
+    return (x >> r) | (x << ((64 - r) & 63));
+}
+
+// jump coefficients: advancing by delta steps maps s to mult * s + plus (Brown, "Random number
+// generation with arbitrary strides", 1994)
+__host__ __device__ inline void pcg_jump(u128 inc, uint64_t delta, u128* mult, u128* plus) {
+    u128 am = 1, ap = 0, cm = pcg_mult(), cp = inc;
+    while (delta > 0) {
+        if (delta & 1) {
+            am *= cm;
+            ap = ap * cm + cp;
+        }
+        cp = (cm + 1) * cp;
+        cm *= cm;
+        delta >>= 1;
+    }
+    *mult = am;
+    *plus = ap;
+}
+
+__host__ __device__ inline u128 pcg_advance(u128 s, u128 inc, uint64_t delta) {
+    u128 m, p;
+    pcg_jump(inc, delta, &m, &p);
+    return m * s + p;
+}
+
+// raw draw number i (0-based) of a generator whose current state is s
+__host__ __device__ inline uint64_t pcg_raw(u128 s, u128 inc, uint64_t i) { return pcg_output(pcg_advance(s, inc, i + 1)); }
+
+__host__ __device__ __forceinline__ double pcg_double(uint64_t raw) { return (double)(raw >> 11) * (1.0 / 9007199254740992.0); }
+
+// the uint8 integers(0, 2) value number t of a run that starts with no buffered uint32: the top
+// bit of byte t%4 of uint32 number t/4; uint32 2j is the low half of raw j, 2j+1 the high half
+__host__ __device__ inline int pcg_bit_at(u128 s, u128 inc, uint64_t t) {
+    const uint64_t raw = pcg_raw(s, inc, t >> 3);
+    const uint32_t word = ((t >> 2) & 1) ? (uint32_t)(raw >> 32) : (uint32_t)raw;
+    return (word >> (8 * (t & 3) + 7)) & 1;
+}
+
+constexpr int kS = 256;
+
+struct GateRec {  // lsg_cgate on the device
+    int16_t code, noise, a, b, c, pad;
+    int32_t nk;  // index among the noisy gates (frames), -1 if none
+};
+
+struct CTable {  // a generic Clifford conjugation table
+    int32_t k, pad;
+    uint8_t e[64];  // (sign << 7) | image bits, index = Pauli bits (x0 z0 x1 z1 ...), first qubit MSB
+};
+
+struct NTable {  // Pauli noise branches: normalised cumulative probabilities and labels
+    int32_t k, nb;
+    double cum[16];
+    uint8_t label[16];  // per qubit i (first qubit bit 2(k-1-i)): x bit then z bit
+};
+
+__device__ __forceinline__ uint32_t xor_reduce_block(uint32_t v) {
+    __shared__ uint32_t red[32];
+    for (int off = 16; off > 0; off >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    uint32_t out = 0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) out ^= red[i];
+    __syncthreads();
+    return out;
+}
+
+// apply one gate to one 32-row word column held in X, Z (shared); returns the sign flips
+__device__ __forceinline__ uint32_t tab_gate(uint32_t* X, uint32_t* Z, const GateRec& g, const CTable* tables) {
+    const int a = g.a;
+    uint32_t r = 0;
+    switch (g.code) {
+        case 0: break;
+        case 1: {  // h
+            const uint32_t x = X[a], z = Z[a];
+            r = x & z;
+            X[a] = z;
+            Z[a] = x;
+            break;
+        }
+        case 2: r = X[a] & Z[a]; Z[a] ^= X[a]; break;   // s
+        case 3: r = X[a] & ~Z[a]; Z[a] ^= X[a]; break;  // sdg
+        case 4: r = Z[a]; break;                        // x
+        case 5: r = X[a] ^ Z[a]; break;                 // y
+        case 6: r = X[a]; break;                        // z
+        case 7: {                                       // cx a -> b
+            const int b = g.b;
+            r = X[a] & Z[b] & ~(X[b] ^ Z[a]);
+            X[b] ^= X[a];
+            Z[a] ^= Z[b];
+            break;
+        }
+        case 8: {  // cz
+            const int b = g.b;
+            r = X[a] & X[b] & (Z[a] ^ Z[b]);
+            Z[a] ^= X[b];
+            Z[b] ^= X[a];
+            break;
+        }
+        default: {  // conjugation table, row by row
+            const CTable& t = tables[g.code - 16];
+            const int k = t.k;
+            const int q[3] = {g.a, g.b, g.c};
+            uint32_t nx[3] = {0, 0, 0}, nz[3] = {0, 0, 0};
+            for (int j = 0; j < 32; ++j) {
+                int idx = 0;
+                for (int i = 0; i < k; ++i) idx = (idx << 2) | (((X[q[i]] >> j) & 1) << 1) | ((Z[q[i]] >> j) & 1);
+                const uint8_t e = t.e[idx];
+                r |= (uint32_t)(e >> 7) << j;
+                for (int i = 0; i < k; ++i) {
+                    nx[i] |= (uint32_t)((e >> (2 * (k - 1 - i) + 1)) & 1) << j;
+                    nz[i] |= (uint32_t)((e >> (2 * (k - 1 - i))) & 1) << j;
+                }
+            }
+            for (int i = 0; i < k; ++i) {
+                X[q[i]] = nx[i];
+                Z[q[i]] = nz[i];
+            }
+            break;
+        }
+    }
+    return r;
+}
+
+// frames: conjugation without signs (stabilizer.py:566-594)
+__device__ __forceinline__ void frame_gate(uint32_t* X, uint32_t* Z, const GateRec& g, const CTable* tables) {
+    const int a = g.a;
+    switch (g.code) {
+        case 0: case 4: case 5: case 6: break;
+        case 1: {
+            const uint32_t x = X[a];
+            X[a] = Z[a];
+            Z[a] = x;
+            break;
+        }
+        case 2: case 3: Z[a] ^= X[a]; break;
+        case 7: X[g.b] ^= X[a]; Z[a] ^= Z[g.b]; break;
+        case 8: Z[a] ^= X[g.b]; Z[g.b] ^= X[a]; break;
+        default: tab_gate(X, Z, g, tables); break;  // the table's sign output is ignored
+    }
+}
+
+// Tableau: one CTA per 32-row column; gates of a moment in parallel.
+__global__ void k_tab_apply(uint32_t* __restrict__ xg, uint32_t* __restrict__ zg, uint32_t* __restrict__ rg, int n, int words,
+                            const GateRec* __restrict__ gates, const int64_t* __restrict__ moments, int64_t nmoments,
+                            const CTable* __restrict__ tables) {
+    extern __shared__ uint32_t sm[];
+    uint32_t* X = sm;
+    uint32_t* Z = sm + n;
+    const int w = blockIdx.x;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        X[q] = xg[(int64_t)q * words + w];
+        Z[q] = zg[(int64_t)q * words + w];
+    }
+    __syncthreads();
+    uint32_t racc = 0;
+    for (int64_t m = 0; m < nmoments; ++m) {
+        const int64_t lo = moments[m], hi = moments[m + 1];
+        for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) racc ^= tab_gate(X, Z, gates[i], tables);
+        __syncthreads();
+    }
+    const uint32_t flips = xor_reduce_block(racc);
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        xg[(int64_t)q * words + w] = X[q];
+        zg[(int64_t)q * words + w] = Z[q];
+    }
+    if (threadIdx.x == 0) rg[w] ^= flips;
+}
+
+// stabilizer rows n..2n-1 to row-major 64-bit words: sx[i * W + v] bit j = x[64v + j][n + i]
+__global__ void k_tab_rows(const uint32_t* __restrict__ xg, const uint32_t* __restrict__ zg, const uint32_t* __restrict__ rg,
+                           int n, int words, int W, uint64_t* sx, uint64_t* sz, uint8_t* sr) {
+    const int64_t total = (int64_t)n * W;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t / W), v = (int)(t % W);
+        const int row = n + i;
+        uint64_t bx = 0, bz = 0;
+        for (int j = 0; j < 64; ++j) {
+            const int q = 64 * v + j;
+            if (q >= n) break;
+            bx |= (uint64_t)((xg[(int64_t)q * words + (row >> 5)] >> (row & 31)) & 1) << j;
+            bz |= (uint64_t)((zg[(int64_t)q * words + (row >> 5)] >> (row & 31)) & 1) << j;
+        }
+        sx[t] = bx;
+        sz[t] = bz;
+        if (v == 0) sr[i] = (rg[row >> 5] >> (row & 31)) & 1;
+    }
+}
+
+// pivot for column q: the first row with bit q set that is not used (rows in index order)
+__global__ void k_elim_pivot(const uint64_t* __restrict__ mat, int rows, int W, int q, uint8_t* used, int* pivot,
+                             int* pivots, int* npiv, int use_flags) {
+    __shared__ int best;
+    if (threadIdx.x == 0) best = 0x7fffffff;
+    __syncthreads();
+    for (int i = threadIdx.x; i < rows; i += blockDim.x)
+        if (((mat[(int64_t)i * W + (q >> 6)] >> (q & 63)) & 1) && !(use_flags && used[i])) atomicMin(&best, i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (best == 0x7fffffff) {
+            *pivot = -1;
+        } else {
+            *pivot = best;
+            if (use_flags) used[best] = 1;
+            pivots[*npiv] = best;
+            *npiv += 1;
+        }
+    }
+}
+
+// rowsum of the pivot row into every other row with bit q set (a warp per row), with the phase
+// exponent summed mod 4 from popcounts (stabilizer.py:381-395)
+__global__ void k_sup_rowsum(uint64_t* __restrict__ sx, uint64_t* __restrict__ sz, uint8_t* __restrict__ sr, int rows, int W,
+                             int q, const int* pivot) {
+    const int p = *pivot;
+    if (p < 0) return;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int t = warp; t < rows; t += nwarps) {
+        if (t == p || !((sx[(int64_t)t * W + (q >> 6)] >> (q & 63)) & 1)) continue;
+        int g = 0;
+        for (int v = lane; v < W; v += 32) {
+            const uint64_t x1 = sx[(int64_t)p * W + v], z1 = sz[(int64_t)p * W + v];
+            const uint64_t x2 = sx[(int64_t)t * W + v], z2 = sz[(int64_t)t * W + v];
+            const uint64_t plus = (x1 & z1 & ~x2 & z2) | (x1 & ~z1 & x2 & z2) | (~x1 & z1 & x2 & ~z2);
+            const uint64_t minus = (x1 & z1 & x2 & ~z2) | (x1 & ~z1 & ~x2 & z2) | (~x1 & z1 & x2 & z2);
+            g += __popcll(plus) - __popcll(minus);
+        }
+        for (int off = 16; off > 0; off >>= 1) g += __shfl_xor_sync(0xffffffffu, g, off);
+        __syncwarp();
+        for (int v = lane; v < W; v += 32) {
+            sx[(int64_t)t * W + v] ^= sx[(int64_t)p * W + v];
+            sz[(int64_t)t * W + v] ^= sz[(int64_t)p * W + v];
+        }
+        if (lane == 0) {
+            const long long total = 2ll * sr[t] + 2ll * sr[p] + g;
+            sr[t] = (((total % 4) + 4) % 4) == 2 ? 1 : 0;
+        }
+    }
+}
+
+// plain elimination (no phase): every other row with bit q ^= the pivot row, and its
+// right-hand side with it (stabilizer.py:405-419)
+__global__ void k_elim_xor(uint64_t* __restrict__ m, uint8_t* __restrict__ rhs, int rows, int W, int q, const int* pivot) {
+    const int p = *pivot;
+    if (p < 0) return;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int t = warp; t < rows; t += nwarps) {
+        if (t == p || !((m[(int64_t)t * W + (q >> 6)] >> (q & 63)) & 1)) continue;
+        __syncwarp();
+        for (int v = lane; v < W; v += 32) m[(int64_t)t * W + v] ^= m[(int64_t)p * W + v];
+        if (lane == 0 && rhs) rhs[t] ^= rhs[p];
+    }
+}
+
+// Pauli frames: one CTA per 32-shot word.
+struct FrameArgs {
+    int n, shots;
+    const GateRec* gates;
+    const int64_t* moments;
+    int64_t nmoments;
+    const CTable* tables;
+    const NTable* noise;
+    const u128* gate_states;  // per noisy gate: the generator state before its block of uniforms
+    u128 inc;
+    u128 jmul, jplus;  // jump by 32 * blockIdx.x steps is computed per block from these per-word tables
+    const u128* word_mult;
+    const u128* word_plus;
+    u128 s0;  // generator state at the start of the run (no uint32 buffered)
+    // outputs
+    uint32_t* fx;  // n x words (the final X parts of the frames)
+    int words;
+};
+
+__global__ void k_frames(FrameArgs A) {
+    extern __shared__ uint32_t sm[];
+    const int n = A.n;
+    uint32_t* X = sm;
+    uint32_t* Z = sm + n;
+    const int w = blockIdx.x;
+    const int shot0 = 32 * w;
+    const int valid = min(32, A.shots - shot0);
+    // initial frames: X = 0, Z = integers(0, 2, size=(n, shots), dtype=uint8): value (q, s) is
+    // uint8 number q * shots + s of the stream
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        uint32_t zw = 0;
+        const uint64_t base = (uint64_t)q * A.shots + shot0;
+        uint64_t cur_raw_index = ~0ull;
+        uint64_t raw = 0;
+        for (int j = 0; j < valid; ++j) {
+            const uint64_t t = base + j;
+            const uint64_t ri = t >> 3;
+            if (ri != cur_raw_index) {
+                raw = pcg_raw(A.s0, A.inc, ri);
+                cur_raw_index = ri;
+            }
+            const uint32_t word = ((t >> 2) & 1) ? (uint32_t)(raw >> 32) : (uint32_t)raw;
+            zw |= (uint32_t)((word >> (8 * (t & 3) + 7)) & 1) << j;
+        }
+        X[q] = 0;
+        Z[q] = zw;
+    }
+    __syncthreads();
+    const u128 wm = A.word_mult[w], wp = A.word_plus[w];
+    const u128 mult = pcg_mult();
+    for (int64_t m = 0; m < A.nmoments; ++m) {
+        const int64_t lo = A.moments[m], hi = A.moments[m + 1];
+        for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            const GateRec g = A.gates[i];
+            frame_gate(X, Z, g, A.tables);
+            if (g.noise < 0) continue;
+            const NTable& nt = A.noise[g.noise];
+            // this word's shots draw uniforms number shot0 .. shot0+31 of the gate's block
+            u128 st = wm * A.gate_states[g.nk] + wp;
+            uint32_t mx[2] = {0, 0}, mz[2] = {0, 0};
+            for (int j = 0; j < valid; ++j) {
+                st = st * mult + A.inc;
+                const double u = pcg_double(pcg_output(st));
+                int pick = 0;  // searchsorted(cumulative, u, side='right'), clamped
+                while (pick < nt.nb && nt.cum[pick] <= u) ++pick;
+                if (pick > nt.nb - 1) pick = nt.nb - 1;
+                const uint8_t lab = nt.label[pick];
+                for (int qi = 0; qi < nt.k; ++qi) {
+                    const int sh = 2 * (nt.k - 1 - qi);
+                    mx[qi] |= (uint32_t)((lab >> (sh + 1)) & 1) << j;
+                    mz[qi] |= (uint32_t)((lab >> sh) & 1) << j;
+                }
+            }
+            const int qs[2] = {g.a, g.b};
+            for (int qi = 0; qi < nt.k; ++qi) {
+                X[qs[qi]] ^= mx[qi];
+                Z[qs[qi]] ^= mz[qi];
+            }
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < n; q += blockDim.x) A.fx[(int64_t)q * A.words + w] = X[q];
+}
+
+// outcome bits: bit (shot, pair) = x0[pos] ^ frame X of the qubit, then readout flips drawn at
+// raw index flip_base + e * shots + shot for the e-th pair with an error (stabilizer.py:622-643)
+__global__ void k_frames_out(const uint32_t* __restrict__ fx, int words, int shots, int npairs, const int* __restrict__ pq,
+                             const int* __restrict__ pc, const int* __restrict__ perr, const double* __restrict__ p01,
+                             const double* __restrict__ p10, const uint8_t* __restrict__ x0pos, u128 s0, u128 inc,
+                             uint64_t flip_base, int nclbits, uint8_t* __restrict__ out) {
+    const int64_t total = (int64_t)shots * npairs;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(t % shots), j = (int)(t / shots);
+        const int q = pq[j];
+        int v = ((fx ? (fx[(int64_t)q * words + (s >> 5)] >> (s & 31)) & 1 : 0)) ^ x0pos[j];
+        if (perr[j] >= 0) {
+            const double u = pcg_double(pcg_raw(s0, inc, flip_base + (uint64_t)perr[j] * shots + s));
+            if (u < (v ? p10[j] : p01[j])) v ^= 1;
+        }
+        out[(int64_t)s * nclbits + pc[j]] = (uint8_t)v;
+    }
+}
+
+// ideal sampling: outcome of shot s = x0 ^ XOR of basis rows i where integer (s * nb + i) is 1;
+// one block per shot: the shot's coefficient bits first (one jump per raw draw), then the XORs
+__global__ void k_sampled(const uint64_t* __restrict__ basis, int nb, int W, const uint64_t* __restrict__ x0, int shots,
+                          u128 s0, u128 inc, uint64_t* __restrict__ outw) {
+    __shared__ uint32_t coef[64];  // up to 2048 basis rows
+    for (int s = blockIdx.x; s < shots; s += gridDim.x) {
+        for (int i = threadIdx.x; i < 64; i += blockDim.x) coef[i] = 0;
+        __syncthreads();
+        const uint64_t t0 = (uint64_t)s * nb, t1 = t0 + nb;  // integers [t0, t1)
+        const uint64_t r0 = t0 >> 3, r1 = (t1 + 7) >> 3;     // raw draws covering them
+        for (uint64_t ri = r0 + threadIdx.x; ri < r1; ri += blockDim.x) {
+            const uint64_t raw = pcg_raw(s0, inc, ri);
+            for (int j = 0; j < 8; ++j) {
+                const uint64_t t = 8 * ri + j;
+                if (t < t0 || t >= t1) continue;
+                const uint32_t word = (j >> 2) ? (uint32_t)(raw >> 32) : (uint32_t)raw;
+                if ((word >> (8 * (j & 3) + 7)) & 1) atomicOr(&coef[(t - t0) >> 5], 1u << ((t - t0) & 31));
+            }
+        }
+        __syncthreads();
+        for (int v = threadIdx.x; v < W; v += blockDim.x) {
+            uint64_t acc = x0[v];
+            for (int i = 0; i < nb; ++i)
+                if ((coef[i >> 5] >> (i & 31)) & 1) acc ^= basis[(int64_t)i * W + v];
+            outw[(int64_t)s * W + v] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_words_to_pairs(const uint64_t* __restrict__ outw, int W, int shots, int npairs, const int* __restrict__ ppos,
+                                 const int* __restrict__ pc, const int* __restrict__ perr, const double* __restrict__ p01,
+                                 const double* __restrict__ p10, u128 s0, u128 inc, uint64_t flip_base, int nclbits,
+                                 uint8_t* __restrict__ out) {
+    const int64_t total = (int64_t)shots * npairs;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(t % shots), j = (int)(t / shots);
+        const int pos = ppos[j];
+        int v = (int)((outw[(int64_t)s * W + (pos >> 6)] >> (pos & 63)) & 1);
+        if (perr[j] >= 0) {
+            const double u = pcg_double(pcg_raw(s0, inc, flip_base + (uint64_t)perr[j] * shots + s));
+            if (u < (v ? p10[j] : p01[j])) v ^= 1;
+        }
+        out[(int64_t)s * nclbits + pc[j]] = (uint8_t)v;
+    }
+}
+
+__global__ void k_gate_states(u128 s0, u128 inc, uint64_t base, uint64_t stride, int64_t count, u128* out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = pcg_advance(s0, inc, base + (uint64_t)k * stride);
+}
+
+// ASAP moments of a gate list: a gate's moment is one past the latest moment among its qubits
+static void moments_of(const GateRec* g, int64_t ng, int n, const int8_t* arity, std::vector<int64_t>& order,
+                       std::vector<int64_t>& starts) {
+    std::vector<int64_t> last(n, -1), level(ng);
+    int64_t maxl = -1;
+    for (int64_t i = 0; i < ng; ++i) {
+        int64_t l = last[g[i].a];
+        if (arity[i] > 1) l = std::max(l, last[g[i].b]);
+        if (arity[i] > 2) l = std::max(l, last[g[i].c]);
+        level[i] = l + 1;
+        last[g[i].a] = level[i];
+        if (arity[i] > 1) last[g[i].b] = level[i];
+        if (arity[i] > 2) last[g[i].c] = level[i];
+        maxl = std::max(maxl, level[i]);
+    }
+    std::vector<int64_t> count(maxl + 2, 0);
+    for (int64_t i = 0; i < ng; ++i) count[level[i] + 1]++;
+    for (int64_t l = 0; l <= maxl; ++l) count[l + 1] += count[l];
+    starts.assign(count.begin(), count.end());
+    order.assign(ng, 0);
+    std::vector<int64_t> fill(count.begin(), count.end() - 1);
+    for (int64_t i = 0; i < ng; ++i) order[fill[level[i]]++] = i;
+}
+
+}  // namespace lsg
+
+using namespace lsg;
+
+struct lsg_tab_s {
+    int n = 0, words = 0;  // words: 32-row words per qubit (2n rows)
+    uint32_t *x = nullptr, *z = nullptr, *r = nullptr;
+    cudaStream_t stream = nullptr;
+    Scratch work, work2;
+};
+
+namespace {
+
+int gate_records(int n, const lsg_cgate* gates, int64_t ng, int32_t ntables, int32_t nnoise, std::vector<GateRec>& recs,
+                 std::vector<int8_t>& arity) {
+    recs.resize(ng);
+    arity.resize(ng);
+    for (int64_t i = 0; i < ng; ++i) {
+        const lsg_cgate& g = gates[i];
+        int k = 1;
+        if (g.code == 7 || g.code == 8) k = 2;
+        else if (g.code >= 16) {
+            if (g.code - 16 >= ntables) return fail(LSG_E_ARG, "gate %lld names a missing table", (long long)i);
+            k = g.nq;
+            if (k < 1 || k > 3) return fail(LSG_E_ARG, "gate %lld has a bad arity", (long long)i);
+        } else if (g.code < 0 || g.code > 8) {
+            return fail(LSG_E_ARG, "gate %lld has a bad code", (long long)i);
+        }
+        const int q[3] = {g.a, g.b, g.c};
+        for (int j = 0; j < k; ++j)
+            if (q[j] < 0 || q[j] >= n) return fail(LSG_E_ARG, "gate %lld names a missing qubit", (long long)i);
+        if (g.noise >= nnoise) return fail(LSG_E_ARG, "gate %lld names a missing noise table", (long long)i);
+        recs[i] = GateRec{(int16_t)g.code, (int16_t)g.noise, (int16_t)g.a, (int16_t)g.b, (int16_t)g.c, 0, -1};
+        arity[i] = (int8_t)k;
+    }
+    return LSG_OK;
+}
+
+int upload(Scratch& s, const void* host, size_t bytes, cudaStream_t st) {
+    LSG_CHECK(ensure(s, bytes));
+    if (bytes) LSG_CUDA(cudaMemcpyAsync(s.ptr, host, bytes, cudaMemcpyHostToDevice, st));
+    return LSG_OK;
+}
+
+int tables_device(const uint8_t* tables, int32_t ntables, std::vector<CTable>& out) {
+    out.resize(std::max(ntables, 1));
+    for (int i = 0; i < ntables; ++i) {
+        std::memset(&out[i], 0, sizeof(CTable));
+        out[i].k = tables[i * 65];
+        if (out[i].k < 1 || out[i].k > 3) return fail(LSG_E_ARG, "Clifford table %d has a bad width", i);
+        std::memcpy(out[i].e, tables + i * 65 + 1, 64);
+    }
+    return LSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lsg_pcg_raw(const uint64_t* state, uint64_t index, uint64_t* out) {
+    clear_error();
+    if (!state || !out) return fail(LSG_E_ARG, "null argument");
+    const u128 s = ((u128)state[0] << 64) | state[1];
+    const u128 inc = ((u128)state[2] << 64) | state[3];
+    *out = pcg_raw(s, inc, index);
+    return LSG_OK;
+}
+
+int lsg_tab_create(int n, lsg_tab* out) {
+    clear_error();
+    if (!out) return fail(LSG_E_ARG, "null output");
+    *out = nullptr;
+    if (n < 1 || n > 2048) return fail(LSG_E_CAPACITY, "%d qubits are more than the stabilizer engine allows (up to 2048)", n);
+    auto* t = new lsg_tab_s();
+    t->n = n;
+    t->words = (2 * n + 31) / 32;
+    const size_t bytes = (size_t)n * t->words * 4;
+    if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&t->x, bytes) != cudaSuccess || cudaMalloc(&t->z, bytes) != cudaSuccess ||
+        cudaMalloc(&t->r, (size_t)t->words * 4) != cudaSuccess) {
+        cudaGetLastError();
+        lsg_tab_free(t);
+        return fail(LSG_E_MEMORY, "cannot allocate the tableau");
+    }
+    // destabilizer i = X_i (row i), stabilizer i = Z_i (row n + i)
+    std::vector<uint32_t> hx((size_t)n * t->words, 0), hz((size_t)n * t->words, 0);
+    for (int i = 0; i < n; ++i) {
+        hx[(size_t)i * t->words + (i >> 5)] |= 1u << (i & 31);
+        const int row = n + i;
+        hz[(size_t)i * t->words + (row >> 5)] |= 1u << (row & 31);
+    }
+    LSG_CUDA(cudaMemcpy(t->x, hx.data(), bytes, cudaMemcpyHostToDevice));
+    LSG_CUDA(cudaMemcpy(t->z, hz.data(), bytes, cudaMemcpyHostToDevice));
+    LSG_CUDA(cudaMemset(t->r, 0, (size_t)t->words * 4));
+    *out = t;
+    return LSG_OK;
+}
+
+int lsg_tab_free(lsg_tab t) {
+    clear_error();
+    if (!t) return LSG_OK;
+    if (t->stream) cudaStreamSynchronize(t->stream);
+    cudaFree(t->x);
+    cudaFree(t->z);
+    cudaFree(t->r);
+    release(t->work);
+    release(t->work2);
+    if (t->stream) cudaStreamDestroy(t->stream);
+    delete t;
+    return LSG_OK;
+}
+
+int lsg_tab_apply(lsg_tab t, const lsg_cgate* gates, int64_t ngates, const uint8_t* tables, int32_t ntables) {
+    clear_error();
+    if (!t || ngates < 0 || (ngates && !gates) || ntables < 0 || (ntables && !tables)) return fail(LSG_E_ARG, "bad arguments");
+    if (ngates == 0) return LSG_OK;
+    std::vector<GateRec> recs;
+    std::vector<int8_t> arity;
+    LSG_CHECK(gate_records(t->n, gates, ngates, ntables, 0x7fff, recs, arity));
+    std::vector<int64_t> order, starts;
+    moments_of(recs.data(), ngates, t->n, arity.data(), order, starts);
+    std::vector<GateRec> sorted(ngates);
+    for (int64_t i = 0; i < ngates; ++i) sorted[i] = recs[order[i]];
+    std::vector<CTable> ct;
+    LSG_CHECK(tables_device(tables, ntables, ct));
+    const size_t gb = ngates * sizeof(GateRec), mb = starts.size() * 8, tb = ct.size() * sizeof(CTable);
+    const size_t o_m = (gb + 255) & ~size_t(255), o_t = o_m + ((mb + 255) & ~size_t(255));
+    LSG_CHECK(ensure(t->work, o_t + tb));
+    char* base = (char*)t->work.ptr;
+    LSG_CUDA(cudaMemcpyAsync(base, sorted.data(), gb, cudaMemcpyHostToDevice, t->stream));
+    LSG_CUDA(cudaMemcpyAsync(base + o_m, starts.data(), mb, cudaMemcpyHostToDevice, t->stream));
+    LSG_CUDA(cudaMemcpyAsync(base + o_t, ct.data(), tb, cudaMemcpyHostToDevice, t->stream));
+    const size_t smem = (size_t)2 * t->n * 4;
+    k_tab_apply<<<t->words, kS, smem, t->stream>>>(t->x, t->z, t->r, t->n, t->words, (const GateRec*)base,
+                                                   (const int64_t*)(base + o_m), (int64_t)starts.size() - 1,
+                                                   (const CTable*)(base + o_t));
+    LSG_CUDA(cudaGetLastError());
+    LSG_CUDA(cudaStreamSynchronize(t->stream));
+    return LSG_OK;
+}
+
+int lsg_tab_download(lsg_tab t, uint8_t* x, uint8_t* z, uint8_t* r) {
+    clear_error();
+    if (!t || !x || !z || !r) return fail(LSG_E_ARG, "null argument");
+    const int n = t->n, W = t->words;
+    std::vector<uint32_t> hx((size_t)n * W), hz((size_t)n * W), hr(W);
+    LSG_CUDA(cudaMemcpyAsync(hx.data(), t->x, hx.size() * 4, cudaMemcpyDeviceToHost, t->stream));
+    LSG_CUDA(cudaMemcpyAsync(hz.data(), t->z, hz.size() * 4, cudaMemcpyDeviceToHost, t->stream));
+    LSG_CUDA(cudaMemcpyAsync(hr.data(), t->r, hr.size() * 4, cudaMemcpyDeviceToHost, t->stream));
+    LSG_CUDA(cudaStreamSynchronize(t->stream));
+    for (int q = 0; q < n; ++q)
+        for (int row = 0; row < 2 * n; ++row) {
+            x[(size_t)q * 2 * n + row] = (hx[(size_t)q * W + (row >> 5)] >> (row & 31)) & 1;
+            z[(size_t)q * 2 * n + row] = (hz[(size_t)q * W + (row >> 5)] >> (row & 31)) & 1;
+        }
+    for (int row = 0; row < 2 * n; ++row) r[row] = (hr[row >> 5] >> (row & 31)) & 1;
+    return LSG_OK;
+}
+
+int lsg_tab_support(lsg_tab t, const int32_t* qubits, int32_t m, uint8_t* x0, uint8_t* basis, int32_t* rank) {
+    clear_error();
+    if (!t || !qubits || !x0 || m < 1 || !rank) return fail(LSG_E_ARG, "bad arguments");
+    const int n = t->n;
+    for (int i = 0; i < m; ++i)
+        if (qubits[i] < 0 || qubits[i] >= n) return fail(LSG_E_ARG, "support: qubit out of range");
+    const int W = (n + 63) / 64;
+    cudaStream_t st = t->stream;
+    // device work: sx | sz | sr | used | pivot | pivots | npiv | solve buffers
+    auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t rowsb = (size_t)n * W * 8;
+    size_t off = 0;
+    const size_t o_sx = off; off += al(rowsb);
+    const size_t o_sz = off; off += al(rowsb);
+    const size_t o_sr = off; off += al(n);
+    const size_t o_used = off; off += al(n);
+    const size_t o_piv = off; off += al(8);
+    const size_t o_pivots = off; off += al((size_t)n * 4);
+    const size_t o_np = off; off += al(8);
+    const size_t o_zm = off; off += al(rowsb);
+    const size_t o_zb = off; off += al(n);
+    const size_t o_zp = off; off += al((size_t)n * 4);
+    const size_t o_znp = off; off += al(8);
+    const size_t o_zused = off; off += al(n);
+    LSG_CHECK(ensure(t->work2, off));
+    char* b = (char*)t->work2.ptr;
+    uint64_t* sx = (uint64_t*)(b + o_sx);
+    uint64_t* sz = (uint64_t*)(b + o_sz);
+    uint8_t* sr = (uint8_t*)(b + o_sr);
+    k_tab_rows<<<std::max(1, std::min(152 * 8, (n * W + kS - 1) / kS)), kS, 0, st>>>(t->x, t->z, t->r, n, t->words, W, sx,
+                                                                                   sz, sr);
+    LSG_CUDA(cudaMemsetAsync(b + o_used, 0, n, st));
+    LSG_CUDA(cudaMemsetAsync(b + o_np, 0, 8, st));
+    const unsigned rg = (unsigned)std::max(1, std::min(152 * 4, (n * 32 + kS - 1) / kS));
+    for (int q = 0; q < n; ++q) {
+        k_elim_pivot<<<1, 1024, 0, st>>>(sx, n, W, q, (uint8_t*)(b + o_used), (int*)(b + o_piv), (int*)(b + o_pivots),
+                                        (int*)(b + o_np), 1);
+        k_sup_rowsum<<<rg, kS, 0, st>>>(sx, sz, sr, n, W, q, (const int*)(b + o_piv));
+    }
+    LSG_CUDA(cudaGetLastError());
+    // Z constraints of the unused rows, in row order (stabilizer.py:359-360, :398-422)
+    std::vector<uint8_t> used(n);
+    int npiv = 0;
+    LSG_CUDA(cudaMemcpyAsync(used.data(), b + o_used, n, cudaMemcpyDeviceToHost, st));
+    LSG_CUDA(cudaMemcpyAsync(&npiv, b + o_np, 4, cudaMemcpyDeviceToHost, st));
+    LSG_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> pivots(npiv);
+    if (npiv) LSG_CUDA(cudaMemcpy(pivots.data(), b + o_pivots, (size_t)npiv * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint64_t> hsz((size_t)n * W), hsx((size_t)n * W);
+    std::vector<uint8_t> hsr(n);
+    LSG_CUDA(cudaMemcpy(hsz.data(), sz, rowsb, cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(hsx.data(), sx, rowsb, cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(hsr.data(), sr, n, cudaMemcpyDeviceToHost));
+    std::vector<uint64_t> zm;
+    std::vector<uint8_t> zb;
+    for (int i = 0; i < n; ++i)
+        if (!used[i]) {
+            zm.insert(zm.end(), hsz.begin() + (size_t)i * W, hsz.begin() + (size_t)(i + 1) * W);
+            zb.push_back(hsr[i]);
+        }
+    const int zr = (int)zb.size();
+    std::vector<uint8_t> xfull(n, 0);
+    if (zr > 0) {
+        LSG_CUDA(cudaMemcpyAsync(b + o_zm, zm.data(), zm.size() * 8, cudaMemcpyHostToDevice, st));
+        LSG_CUDA(cudaMemcpyAsync(b + o_zb, zb.data(), zr, cudaMemcpyHostToDevice, st));
+        LSG_CUDA(cudaMemsetAsync(b + o_zused, 0, zr, st));
+        LSG_CUDA(cudaMemsetAsync(b + o_znp, 0, 8, st));
+        const unsigned zg = (unsigned)std::max(1, std::min(152 * 4, (zr * 32 + kS - 1) / kS));
+        std::vector<int> zpiv_q;
+        for (int q = 0; q < n; ++q) {
+            k_elim_pivot<<<1, 1024, 0, st>>>((uint64_t*)(b + o_zm), zr, W, q, (uint8_t*)(b + o_zused), (int*)(b + o_piv),
+                                            (int*)(b + o_zp), (int*)(b + o_znp), 1);
+            k_elim_xor<<<zg, kS, 0, st>>>((uint64_t*)(b + o_zm), (uint8_t*)(b + o_zb), zr, W, q, (const int*)(b + o_piv));
+        }
+        LSG_CUDA(cudaGetLastError());
+        // which column each pivot belongs to: replay the pivot order on the host from the final
+        // matrix is not possible, so recover it from the pivot list (pivots are taken for
+        // ascending columns)
+        int nz = 0;
+        LSG_CUDA(cudaMemcpyAsync(&nz, b + o_znp, 4, cudaMemcpyDeviceToHost, st));
+        LSG_CUDA(cudaStreamSynchronize(st));
+        std::vector<int> zp(nz);
+        std::vector<uint8_t> fb(zr);
+        std::vector<uint64_t> fm((size_t)zr * W);
+        if (nz) LSG_CUDA(cudaMemcpy(zp.data(), b + o_zp, (size_t)nz * 4, cudaMemcpyDeviceToHost));
+        LSG_CUDA(cudaMemcpy(fb.data(), b + o_zb, zr, cudaMemcpyDeviceToHost));
+        LSG_CUDA(cudaMemcpy(fm.data(), b + o_zm, (size_t)zr * W * 8, cudaMemcpyDeviceToHost));
+        // after full reduction each pivot row has exactly one pivot column: its lowest set bit
+        // among pivot columns is the column it was chosen for; columns were visited ascending,
+        // so pivot j belongs to the j-th column that received a pivot: the lowest set bit of the
+        // reduced row (every earlier pivot column was cleared from it)
+        for (int j = 0; j < nz; ++j) {
+            const int p = zp[j];
+            int col = -1;
+            for (int v = 0; v < W && col < 0; ++v)
+                if (fm[(size_t)p * W + v]) col = 64 * v + __builtin_ctzll(fm[(size_t)p * W + v]);
+            if (col >= 0 && col < n) xfull[col] = fb[p];
+        }
+    }
+    for (int i = 0; i < m; ++i) x0[i] = xfull[qubits[i]];
+    // basis: X parts of the pivot rows restricted to `qubits` (stabilizer.py:361-365)
+    bool identity = m == n;
+    for (int i = 0; identity && i < m; ++i) identity = qubits[i] == i;
+    std::vector<uint8_t> vec((size_t)npiv * m);
+    for (int j = 0; j < npiv; ++j)
+        for (int i = 0; i < m; ++i) {
+            const int q = qubits[i];
+            vec[(size_t)j * m + i] = (hsx[(size_t)pivots[j] * W + (q >> 6)] >> (q & 63)) & 1;
+        }
+    if (identity) {
+        *rank = npiv;
+        if (basis) std::memcpy(basis, vec.data(), vec.size());
+        return LSG_OK;
+    }
+    // row basis of the restricted vectors (stabilizer.py:425-440), on the host: npiv x m bits
+    const int Wm = (m + 63) / 64;
+    std::vector<uint64_t> mm((size_t)npiv * Wm, 0);
+    for (int j = 0; j < npiv; ++j)
+        for (int i = 0; i < m; ++i)
+            if (vec[(size_t)j * m + i]) mm[(size_t)j * Wm + (i >> 6)] |= 1ull << (i & 63);
+    std::vector<uint64_t> out;
+    int nb = 0;
+    for (int col = 0; col < m && nb < m; ++col) {
+        int p = -1;
+        for (int j = 0; j < npiv; ++j)
+            if ((mm[(size_t)j * Wm + (col >> 6)] >> (col & 63)) & 1) {
+                p = j;
+                break;
+            }
+        if (p < 0) continue;
+        std::vector<uint64_t> row(mm.begin() + (size_t)p * Wm, mm.begin() + (size_t)(p + 1) * Wm);
+        out.insert(out.end(), row.begin(), row.end());
+        ++nb;
+        for (int j = 0; j < npiv; ++j)
+            if ((mm[(size_t)j * Wm + (col >> 6)] >> (col & 63)) & 1)
+                for (int v = 0; v < Wm; ++v) mm[(size_t)j * Wm + v] ^= row[v];
+    }
+    *rank = nb;
+    if (basis)
+        for (int j = 0; j < nb; ++j)
+            for (int i = 0; i < m; ++i) basis[(size_t)j * m + i] = (out[(size_t)j * Wm + (i >> 6)] >> (i & 63)) & 1;
+    return LSG_OK;
+}
+
+int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t* tables, int32_t ntables,
+                   const lsg_noise_table* noise, int32_t nnoise, int64_t shots, const uint64_t* rng_state,
+                   int32_t npairs, const int32_t* pair_qubit, const int32_t* pair_clbit, const uint8_t* pair_x0,
+                   const int32_t* pair_err, const double* p01, const double* p10, int32_t nclbits, uint8_t* bits_out,
+                   int64_t* raw_used) {
+    clear_error();
+    if (n < 1 || n > 2048 || ngates < 0 || (ngates && !gates) || shots < 1 || !rng_state || npairs < 1 || !pair_qubit ||
+        !pair_clbit || !pair_x0 || !pair_err || !p01 || !p10 || !bits_out || nclbits < 1 || nnoise < 0 ||
+        (nnoise && !noise))
+        return fail(LSG_E_ARG, "lsg_frames_run: bad arguments");
+    if (shots > (1ll << 30)) return fail(LSG_E_ARG, "too many shots for one frames run");
+    std::vector<GateRec> recs;
+    std::vector<int8_t> arity;
+    LSG_CHECK(gate_records(n, gates, ngates, ntables, nnoise, recs, arity));
+    int64_t nk = 0;
+    for (int64_t i = 0; i < ngates; ++i)
+        if (recs[i].noise >= 0) recs[i].nk = (int32_t)nk++;
+    for (int j = 0; j < npairs; ++j)
+        if (pair_qubit[j] < 0 || pair_qubit[j] >= n || pair_clbit[j] < 0 || pair_clbit[j] >= nclbits)
+            return fail(LSG_E_ARG, "lsg_frames_run: bad measurement pair %d", j);
+    std::vector<NTable> nt(std::max(nnoise, 1));
+    for (int i = 0; i < nnoise; ++i) {
+        const lsg_noise_table& s = noise[i];
+        if (s.k < 1 || s.k > 2 || s.nbranch < 1 || s.nbranch > 16) return fail(LSG_E_ARG, "noise table %d is malformed", i);
+        nt[i].k = s.k;
+        nt[i].nb = s.nbranch;
+        for (int j = 0; j < 16; ++j) {
+            nt[i].cum[j] = s.cumulative[j];
+            nt[i].label[j] = s.label[j];
+        }
+    }
+    std::vector<int64_t> order, starts;
+    moments_of(recs.data(), ngates, n, arity.data(), order, starts);
+    std::vector<GateRec> sorted(ngates);
+    for (int64_t i = 0; i < ngates; ++i) sorted[i] = recs[order[i]];
+    std::vector<CTable> ct;
+    LSG_CHECK(tables_device(tables, ntables, ct));
+    const u128 s0 = ((u128)rng_state[0] << 64) | rng_state[1];
+    const u128 inc = ((u128)rng_state[2] << 64) | rng_state[3];
+    // draw layout: the frame bits (n * shots uint8 = ceil(n*shots/8) raw draws), then shots
+    // uniforms per noisy gate in circuit order, then shots uniforms per readout pair with an error
+    const uint64_t n8 = (uint64_t)n * shots;
+    const uint64_t n32 = (n8 + 3) / 4;
+    const uint64_t base_noise = (n32 + 1) / 2;
+    const uint64_t base_flip = base_noise + (uint64_t)nk * shots;
+    int nerr = 0;
+    for (int j = 0; j < npairs; ++j)
+        if (pair_err[j] >= 0) ++nerr;
+    if (raw_used) *raw_used = (int64_t)(base_flip + (uint64_t)nerr * shots);
+    const int words = (int)((shots + 31) / 32);
+    std::vector<u128> wmul(words), wplus(words);
+    for (int w = 0; w < words; ++w) pcg_jump(inc, (uint64_t)32 * w, &wmul[w], &wplus[w]);
+    cudaStream_t st = nullptr;
+    LSG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
+    size_t off = 0;
+    const size_t o_g = off; off += al(ngates * sizeof(GateRec));
+    const size_t o_m = off; off += al(starts.size() * 8);
+    const size_t o_t = off; off += al(ct.size() * sizeof(CTable));
+    const size_t o_n = off; off += al(nt.size() * sizeof(NTable));
+    const size_t o_s = off; off += al((size_t)std::max<int64_t>(nk, 1) * 16);
+    const size_t o_wm = off; off += al((size_t)words * 16);
+    const size_t o_wp = off; off += al((size_t)words * 16);
+    const size_t o_fx = off; off += al((size_t)n * words * 4);
+    const size_t o_pq = off; off += al((size_t)npairs * 4);
+    const size_t o_pc = off; off += al((size_t)npairs * 4);
+    const size_t o_pe = off; off += al((size_t)npairs * 4);
+    const size_t o_p0 = off; off += al((size_t)npairs * 8);
+    const size_t o_p1 = off; off += al((size_t)npairs * 8);
+    const size_t o_x0 = off; off += al((size_t)npairs);
+    const size_t o_out = off; off += al((size_t)shots * nclbits);
+    Scratch work;
+    int rc = ensure(work, off);
+    if (rc != LSG_OK) {
+        cudaStreamDestroy(st);
+        return rc;
+    }
+    char* b = (char*)work.ptr;
+    std::vector<int32_t> perr(npairs);
+    {
+        int e = 0;
+        for (int j = 0; j < npairs; ++j) perr[j] = pair_err[j] >= 0 ? e++ : -1;
+    }
+    cudaError_t ce = cudaSuccess;
+    auto H2D = [&](size_t o, const void* src, size_t bytes) {
+        if (bytes && ce == cudaSuccess) ce = cudaMemcpyAsync(b + o, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    H2D(o_g, sorted.data(), ngates * sizeof(GateRec));
+    H2D(o_m, starts.data(), starts.size() * 8);
+    H2D(o_t, ct.data(), ct.size() * sizeof(CTable));
+    H2D(o_n, nt.data(), nt.size() * sizeof(NTable));
+    H2D(o_wm, wmul.data(), (size_t)words * 16);
+    H2D(o_wp, wplus.data(), (size_t)words * 16);
+    H2D(o_pq, pair_qubit, (size_t)npairs * 4);
+    H2D(o_pc, pair_clbit, (size_t)npairs * 4);
+    H2D(o_pe, perr.data(), (size_t)npairs * 4);
+    H2D(o_p0, p01, (size_t)npairs * 8);
+    H2D(o_p1, p10, (size_t)npairs * 8);
+    H2D(o_x0, pair_x0, (size_t)npairs);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(b + o_out, 0, (size_t)shots * nclbits, st);
+    if (ce == cudaSuccess && nk)
+        k_gate_states<<<std::max<int64_t>(1, std::min<int64_t>((nk + kS - 1) / kS, 152 * 64)), kS, 0, st>>>(
+            s0, inc, base_noise, (uint64_t)shots, nk, (u128*)(b + o_s));
+    FrameArgs A{};
+    A.n = n;
+    A.shots = (int)shots;
+    A.gates = (const GateRec*)(b + o_g);
+    A.moments = (const int64_t*)(b + o_m);
+    A.nmoments = (int64_t)starts.size() - 1;
+    A.tables = (const CTable*)(b + o_t);
+    A.noise = (const NTable*)(b + o_n);
+    A.gate_states = (const u128*)(b + o_s);
+    A.inc = inc;
+    A.word_mult = (const u128*)(b + o_wm);
+    A.word_plus = (const u128*)(b + o_wp);
+    A.s0 = s0;
+    A.fx = (uint32_t*)(b + o_fx);
+    A.words = words;
+    if (ce == cudaSuccess) {
+        k_frames<<<words, kS, (size_t)2 * n * 4, st>>>(A);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) {
+        const int64_t tot = shots * npairs;
+        k_frames_out<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((tot + kS - 1) / kS, 152 * 64)), kS, 0, st>>>(
+            (const uint32_t*)(b + o_fx), words, (int)shots, npairs, (const int*)(b + o_pq), (const int*)(b + o_pc),
+            (const int*)(b + o_pe), (const double*)(b + o_p0), (const double*)(b + o_p1), (const uint8_t*)(b + o_x0), s0,
+            inc, base_flip, nclbits, (uint8_t*)(b + o_out));
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(bits_out, b + o_out, (size_t)shots * nclbits, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    release(work);
+    cudaStreamDestroy(st);
+    if (ce != cudaSuccess) return fail(LSG_E_CUDA, "the frames run failed: %s", cudaGetErrorString(ce));
+    return LSG_OK;
+}
+
+int lsg_stab_sample(int m, const uint8_t* x0, const uint8_t* basis, int32_t nb, int64_t shots, const uint64_t* rng_state,
+                    int32_t npairs, const int32_t* pair_pos, const int32_t* pair_clbit, const int32_t* pair_err,
+                    const double* p01, const double* p10, int32_t nclbits, uint8_t* bits_out, int64_t* raw_used) {
+    clear_error();
+    if (m < 1 || !x0 || nb < 0 || (nb && !basis) || shots < 1 || !rng_state || npairs < 1 || !pair_pos || !pair_clbit ||
+        !pair_err || !p01 || !p10 || nclbits < 1 || !bits_out)
+        return fail(LSG_E_ARG, "lsg_stab_sample: bad arguments");
+    for (int j = 0; j < npairs; ++j)
+        if (pair_pos[j] < 0 || pair_pos[j] >= m || pair_clbit[j] < 0 || pair_clbit[j] >= nclbits)
+            return fail(LSG_E_ARG, "lsg_stab_sample: bad pair %d", j);
+    const int W = (m + 63) / 64;
+    std::vector<uint64_t> bx((size_t)std::max(nb, 1) * W, 0), xw(W, 0);
+    for (int i = 0; i < m; ++i)
+        if (x0[i]) xw[i >> 6] |= 1ull << (i & 63);
+    for (int j = 0; j < nb; ++j)
+        for (int i = 0; i < m; ++i)
+            if (basis[(size_t)j * m + i]) bx[(size_t)j * W + (i >> 6)] |= 1ull << (i & 63);
+    const u128 s0 = ((u128)rng_state[0] << 64) | rng_state[1];
+    const u128 inc = ((u128)rng_state[2] << 64) | rng_state[3];
+    const uint64_t n8 = (uint64_t)shots * nb;
+    const uint64_t base_flip = nb ? ((n8 + 3) / 4 + 1) / 2 : 0;
+    std::vector<int32_t> perr(npairs);
+    int nerr = 0;
+    for (int j = 0; j < npairs; ++j) perr[j] = pair_err[j] >= 0 ? nerr++ : -1;
+    if (raw_used) *raw_used = (int64_t)(base_flip + (uint64_t)nerr * shots);
+    cudaStream_t st = nullptr;
+    LSG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
+    size_t off = 0;
+    const size_t o_b = off; off += al(bx.size() * 8);
+    const size_t o_x = off; off += al((size_t)W * 8);
+    const size_t o_w = off; off += al((size_t)shots * W * 8);
+    const size_t o_pp = off; off += al((size_t)npairs * 4);
+    const size_t o_pc = off; off += al((size_t)npairs * 4);
+    const size_t o_pe = off; off += al((size_t)npairs * 4);
+    const size_t o_p0 = off; off += al((size_t)npairs * 8);
+    const size_t o_p1 = off; off += al((size_t)npairs * 8);
+    const size_t o_out = off; off += al((size_t)shots * nclbits);
+    Scratch work;
+    int rc = ensure(work, off);
+    if (rc != LSG_OK) {
+        cudaStreamDestroy(st);
+        return rc;
+    }
+    char* b = (char*)work.ptr;
+    cudaError_t ce = cudaSuccess;
+    auto H2D = [&](size_t o, const void* src, size_t bytes) {
+        if (bytes && ce == cudaSuccess) ce = cudaMemcpyAsync(b + o, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    H2D(o_b, bx.data(), bx.size() * 8);
+    H2D(o_x, xw.data(), (size_t)W * 8);
+    H2D(o_pp, pair_pos, (size_t)npairs * 4);
+    H2D(o_pc, pair_clbit, (size_t)npairs * 4);
+    H2D(o_pe, perr.data(), (size_t)npairs * 4);
+    H2D(o_p0, p01, (size_t)npairs * 8);
+    H2D(o_p1, p10, (size_t)npairs * 8);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(b + o_out, 0, (size_t)shots * nclbits, st);
+    if (ce == cudaSuccess) {
+        k_sampled<<<(unsigned)std::min<int64_t>(shots, 152 * 16), 64, 0, st>>>((const uint64_t*)(b + o_b), nb, W,
+                                                                             (const uint64_t*)(b + o_x), (int)shots, s0,
+                                                                             inc, (uint64_t*)(b + o_w));
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) {
+        const int64_t tot = shots * npairs;
+        k_words_to_pairs<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((tot + kS - 1) / kS, 152 * 64)), kS, 0, st>>>(
+            (const uint64_t*)(b + o_w), W, (int)shots, npairs, (const int*)(b + o_pp), (const int*)(b + o_pc),
+            (const int*)(b + o_pe), (const double*)(b + o_p0), (const double*)(b + o_p1), s0, inc, base_flip, nclbits,
+            (uint8_t*)(b + o_out));
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(bits_out, b + o_out, (size_t)shots * nclbits, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    release(work);
+    cudaStreamDestroy(st);
+    if (ce != cudaSuccess) return fail(LSG_E_CUDA, "stabilizer sampling failed: %s", cudaGetErrorString(ce));
+    return LSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+"""The stabilizer engine on the GPU: tableaux, support and counts bit-exact against Orrery's
+golden vectors and the oracle."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import lucivant_sim_gb300 as ls
+from lucivant_sim_gb300 import stabilizer as st, workloads as wl
+from lucivant_sim_gb300.clifford import all_gates
+from lucivant_sim_gb300.noise import NoiseModel, ReadoutError, depolarizing
+from oracle import tableau
+
+pytestmark = pytest.mark.gpu
+
+
+def _tab(circuit):
+    enc = st.Encoder(None)
+    t = st.Tableau(circuit.num_qubits)
+    t.apply(enc.encode(all_gates(circuit.operations), False), enc)
+    return t
+
+
+def test_tableau_and_support_golden(golden, golden_arrays):
+    c = ls.parse(golden["stab_frames64"]["qasm"])
+    t = _tab(c)
+    x, z, r = t.arrays()
+    assert np.array_equal(x, golden_arrays["stab64_x"])
+    assert np.array_equal(z, golden_arrays["stab64_z"])
+    assert np.array_equal(r, golden_arrays["stab64_r"])
+    x0, basis = t.support(list(range(64)))
+    assert np.array_equal(x0, golden_arrays["stab64_x0"])
+    assert np.array_equal(basis, golden_arrays["stab64_basis"])
+    t.free()
+
+
+@pytest.mark.parametrize("n,layers,seed", [(5, 6, 1), (37, 5, 2), (130, 3, 3)])
+def test_tableau_generic_gates_against_oracle(n, layers, seed):
+    rng = np.random.default_rng(seed)
+    lines = ["OPENQASM 3.0;", 'include "stdgates.inc";', f"qubit[{n}] q;"]
+    names1 = ["h", "s", "sdg", "x", "y", "z", "sx", "sxdg", "id"]
+    names2 = ["cx", "cz", "cy", "swap", "iswap", "ecr", "dcx"]
+    for _ in range(layers):
+        for q in range(n):
+            lines.append(f"{names1[rng.integers(len(names1))]} q[{q}];")
+        perm = rng.permutation(n)
+        for i in range(0, n - 1, 2):
+            lines.append(f"{names2[rng.integers(len(names2))]} q[{perm[i]}], q[{perm[i + 1]}];")
+    c = ls.parse("\n".join(lines))
+    ref = tableau.reference_tableau(c)
+    t = _tab(c)
+    x, z, r = t.arrays()
+    assert np.array_equal(x, ref.x) and np.array_equal(z, ref.z) and np.array_equal(r, ref.r)
+    qs = sorted(rng.choice(n, size=max(1, n // 3), replace=False).tolist())
+    want_x0, want_basis = ref.copy().support(qs)
+    x0, basis = t.support(qs)
+    assert np.array_equal(x0, want_x0) and np.array_equal(basis, want_basis)
+    t.free()
+
+
+def test_counts_golden(golden):
+    g = golden["stab_frames64"]
+    noise = NoiseModel()
+    noise.add_gate_error(depolarizing(1e-2, 1)).add_gate_error(depolarizing(1e-2, 2))
+    noise.add_readout_error(ReadoutError(0.01, 0.03))
+    r = ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=noise)
+    assert r.method == "stabilizer" and r.counts == g["counts"]
+    g = golden["stab_sampled30"]
+    assert ls.run(g["qasm"], shots=g["shots"], seed=g["seed"]).counts == g["counts"]
+    g = golden["stab_partial"]
+    assert ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=NoiseModel().add_readout_error(0.05)).counts == g["counts"]
+
+
+def test_frames_against_oracle_and_rng_position():
+    c = wl.clifford_layers_circuit(100, 6, seed=9)
+    noise = wl.stabilizer_noise(2e-2)
+    rng_a = np.random.default_rng(21)
+    want = tableau.frames(c, 333, noise, rng_a)
+    rng_b = np.random.default_rng(21)
+    got = st.frames(c, 333, noise, rng_b)
+    assert got == want
+    assert rng_b.bit_generator.state == rng_a.bit_generator.state
+
+
+def test_sampled_against_oracle_and_rng_position():
+    c = ls.parse(wl.clifford_layers(45, 4, seed=8))
+    rng_a = np.random.default_rng(5)
+    want = tableau.sampled(c, 701, NoiseModel().add_readout_error(0.1), rng_a)
+    rng_b = np.random.default_rng(5)
+    got = st.sampled(c, 701, NoiseModel().add_readout_error(0.1), rng_b)
+    assert got == want
+    assert rng_b.bit_generator.state == rng_a.bit_generator.state

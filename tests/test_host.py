@@ -126,3 +126,27 @@ def test_no_oracle_in_product():
     for path in (ROOT / "lucivant_sim_gb300").rglob("*.py"):
         text = path.read_text()
         assert "import oracle" not in text and "from oracle" not in text, path
+
+
+def test_library_pcg64_matches_numpy():
+    """The engine's PCG64 (host build of the device code) regenerates NumPy's stream."""
+    from lucivant_sim_gb300 import stabilizer as st
+
+    for seed in (0, 7, 11, 2**40 + 3):
+        rng = np.random.default_rng(seed)
+        probe = np.random.default_rng(seed)
+        raw = probe.bit_generator.random_raw(2000)
+        for i in (0, 1, 2, 17, 999, 1999):
+            assert st.pcg_raw(rng, i) == int(raw[i])
+
+
+def test_uint8_integers_stream_layout():
+    """integers(0, 2, uint8) is the top bit of each byte of the buffered uint32 stream."""
+    rng = np.random.default_rng(3)
+    vals = rng.integers(0, 2, size=37, dtype=np.uint8)
+    raw = np.random.default_rng(3).bit_generator.random_raw(5)
+    words = []
+    for r in raw:
+        words += [int(r) & 0xFFFFFFFF, int(r) >> 32]
+    bytes_ = [(w >> (8 * i)) & 0xFF for w in words for i in range(4)]
+    assert list(vals) == [b >> 7 for b in bytes_[:37]]
