@@ -239,6 +239,28 @@ int lsg_stab_sample(int m, const uint8_t* x0, const uint8_t* basis, int32_t nb, 
                     const uint64_t* rng_state, int32_t npairs, const int32_t* pair_pos, const int32_t* pair_clbit,
                     const int32_t* pair_err, const double* p01, const double* p10, int32_t nclbits,
                     uint8_t* bits_out, int64_t* raw_used);
+/* _per_shot (stabilizer.py:653-694): dynamic Clifford circuits, one tableau per shot after the
+ * noiseless prefix `prefix`, shots in order. ops: gate codes (noise = Pauli-noise table, -1 none),
+ * or 100 measure (a = qubit, clbit, noise = readout row of `readout` = (p01, p10) pairs, -1 none),
+ * 101 reset (a), 102 if (c = condition index, aux = op to jump to when it fails), 103 else (aux =
+ * op after the matching endif), 104 endif. rng_state: 7 words (state hi/lo, inc hi/lo, the
+ * buffered-uint32 flag, the buffered value, raw draws): in, the generator at the start; out, where
+ * NumPy's generator would be after the same draws. clbits_out: shots x 4 words. */
+typedef struct lsg_shot_op {
+    int16_t code, noise, a, b, c, clbit;
+    int32_t aux;
+    int16_t nq, pad0;
+    int32_t pad1;
+} lsg_shot_op;
+typedef struct lsg_shot_cond {
+    int32_t n, negate;
+    uint64_t value;
+    int32_t bits[64];
+} lsg_shot_cond;
+int lsg_per_shot_run(int n, const lsg_cgate* prefix, int64_t nprefix, const lsg_shot_op* ops, int32_t nops,
+                     const uint8_t* tables, int32_t ntables, const lsg_noise_table* noise, int32_t nnoise,
+                     const double* readout, int32_t nreadout, const lsg_shot_cond* conds, int32_t nconds,
+                     int32_t num_clbits, int64_t shots, uint64_t* rng_state, uint64_t* clbits_out);
 /* Host-side check of the generator: raw draw number `index` after the state (4 words as above). */
 int lsg_pcg_raw(const uint64_t* state, uint64_t index, uint64_t* out);
 

@@ -993,3 +993,503 @@ int lsg_stab_sample(int m, const uint8_t* x0, const uint8_t* basis, int32_t nb, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Dynamic Clifford circuits, one tableau per shot (stabilizer.py:653-694), in Orrery's draw order.
+//
+// One CTA walks the shots in order. The tableau lives in global memory, qubit-major in 64-bit
+// words (word w of qubit q holds rows 64w..64w+63); a shot starts from a copy of the noiseless
+// prefix. Thread 0 owns the generator: the PCG64 state, and NumPy's buffered uint32 half, since
+// measurements draw integers(2) (the top bit of a uint32) between the doubles of noise and readout.
+
+namespace lsg {
+
+struct ShotOp {
+    int16_t code;   // gate code, or 100 measure, 101 reset, 102 if, 103 else, 104 endif
+    int16_t noise;  // gate: noise table; measure: readout table (-1: none)
+    int16_t a, b, c;
+    int16_t clbit;  // measure target (-1: discarded)
+    int32_t aux;    // if: condition index; if/else: index to jump to
+};
+
+struct ShotCond {
+    int32_t n, negate;
+    uint64_t value;
+    int32_t bits[64];
+};
+
+struct RngCtl {
+    u128 s, inc;       // current state
+    uint64_t pos;      // raw draws so far
+    uint32_t has32, buf32;
+};
+
+__device__ __forceinline__ uint64_t rng_next64(RngCtl& g) {
+    g.s = g.s * pcg_mult() + g.inc;
+    g.pos++;
+    return pcg_output(g.s);
+}
+
+__device__ __forceinline__ double rng_double(RngCtl& g) { return pcg_double(rng_next64(g)); }
+
+__device__ __forceinline__ uint32_t rng_uint32(RngCtl& g) {
+    if (g.has32) {
+        g.has32 = 0;
+        return g.buf32;
+    }
+    const uint64_t raw = rng_next64(g);
+    g.buf32 = (uint32_t)(raw >> 32);
+    g.has32 = 1;
+    return (uint32_t)raw;
+}
+
+// a gate on one 64-row word of a qubit-major tableau (stabilizer.py:224-264)
+__device__ __forceinline__ uint64_t tab_gate64(uint64_t* X, uint64_t* Z, int W, int w, const ShotOp& g,
+                                               const CTable* tables) {
+    const int a = g.a;
+    uint64_t& xa = X[(int64_t)a * W + w];
+    uint64_t& za = Z[(int64_t)a * W + w];
+    uint64_t r = 0;
+    switch (g.code) {
+        case 0: break;
+        case 1: { const uint64_t x = xa; r = x & za; xa = za; za = x; break; }
+        case 2: r = xa & za; za ^= xa; break;
+        case 3: r = xa & ~za; za ^= xa; break;
+        case 4: r = za; break;
+        case 5: r = xa ^ za; break;
+        case 6: r = xa; break;
+        case 7: {
+            uint64_t& xb = X[(int64_t)g.b * W + w];
+            uint64_t& zb = Z[(int64_t)g.b * W + w];
+            r = xa & zb & ~(xb ^ za);
+            xb ^= xa;
+            za ^= zb;
+            break;
+        }
+        case 8: {
+            uint64_t& xb = X[(int64_t)g.b * W + w];
+            uint64_t& zb = Z[(int64_t)g.b * W + w];
+            r = xa & xb & (za ^ zb);
+            za ^= xb;
+            zb ^= xa;
+            break;
+        }
+        default: {
+            const CTable& t = tables[g.code - 16];
+            const int k = t.k;
+            const int q[3] = {g.a, g.b, g.c};
+            uint64_t nx[3] = {0, 0, 0}, nz[3] = {0, 0, 0};
+            for (int j = 0; j < 64; ++j) {
+                int idx = 0;
+                for (int i = 0; i < k; ++i)
+                    idx = (idx << 2) | (int)(((X[(int64_t)q[i] * W + w] >> j) & 1) << 1) | (int)((Z[(int64_t)q[i] * W + w] >> j) & 1);
+                const uint8_t e = t.e[idx];
+                r |= (uint64_t)(e >> 7) << j;
+                for (int i = 0; i < k; ++i) {
+                    nx[i] |= (uint64_t)((e >> (2 * (k - 1 - i) + 1)) & 1) << j;
+                    nz[i] |= (uint64_t)((e >> (2 * (k - 1 - i))) & 1) << j;
+                }
+            }
+            for (int i = 0; i < k; ++i) {
+                X[(int64_t)q[i] * W + w] = nx[i];
+                Z[(int64_t)q[i] * W + w] = nz[i];
+            }
+            break;
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ int getbit(const uint64_t* M, int W, int q, int row) {
+    return (int)((M[(int64_t)q * W + (row >> 6)] >> (row & 63)) & 1);
+}
+
+__device__ __forceinline__ void setbit(uint64_t* M, int W, int q, int row, int v) {
+    uint64_t& w = M[(int64_t)q * W + (row >> 6)];
+    const uint64_t bit = 1ull << (row & 63);
+    w = v ? (w | bit) : (w & ~bit);
+}
+
+__device__ int block_sum_int(int v) {
+    __shared__ int red[32];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int out = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) out += red[i];
+    __syncthreads();
+    return out;
+}
+
+struct ShotArgs {
+    int n, W, nops, ncl_words;
+    int64_t shots;
+    const ShotOp* ops;
+    const ShotCond* conds;
+    const CTable* tables;
+    const NTable* noise;
+    const double* readout;  // pairs (p01, p10)
+    const uint64_t *px, *pz, *pr;  // prefix tableau
+    uint64_t *X, *Z, *R;           // working tableau
+    uint8_t* sx;                   // scratch row for deterministic outcomes: 2n bytes
+    uint64_t* out;                 // shots x ncl_words
+    RngCtl* rng;                   // in: start state; out: final state
+};
+
+// Measure qubit a of the working tableau; thread 0's generator draws when the outcome is random.
+__device__ int shot_measure(const ShotArgs& A, int a, RngCtl& g) {
+    const int n = A.n, W = A.W;
+    uint64_t *X = A.X, *Z = A.Z, *R = A.R;
+    __shared__ int pivot;
+    __shared__ int outcome;
+    if (threadIdx.x == 0) pivot = 0x7fffffff;
+    __syncthreads();
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+        uint64_t bits = X[(int64_t)a * W + w];
+        // stabilizer rows only: rows >= n
+        const int lo = 64 * w;
+        if (lo + 63 < n) continue;
+        if (lo < n) bits &= ~0ull << (n - lo);
+        if (bits) atomicMin(&pivot, lo + __ffsll((long long)bits) - 1);
+    }
+    __syncthreads();
+    const int p = pivot;
+    if (p == 0x7fffffff) {
+        // deterministic (stabilizer.py:288-301): rowsum the stabilizers of destabilizers with x[a]
+        uint8_t* sx = A.sx;
+        uint8_t* sz = A.sx + n;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) sx[q] = sz[q] = 0;
+        __shared__ int sr;
+        if (threadIdx.x == 0) sr = 0;
+        __syncthreads();
+        for (int i = 0; i < n; ++i) {
+            if (!getbit(X, W, a, i)) continue;  // uniform across the block
+            const int row = i + n;
+            int gsum = 0;
+            for (int q = threadIdx.x; q < n; q += blockDim.x) {
+                const int xs = getbit(X, W, q, row), zs = getbit(Z, W, q, row);
+                const int cx = sx[q], cz = sz[q];
+                gsum += (xs & zs) * (cz - cx) + (xs & (1 - zs)) * (cz * (2 * cx - 1)) + ((1 - xs) & zs) * (cx * (1 - 2 * cz));
+            }
+            const int gt = block_sum_int(gsum);
+            if (threadIdx.x == 0) {
+                const int tot = 2 * sr + 2 * getbit(R, W, 0, row) + gt;
+                sr = (((tot % 4) + 4) % 4) == 2 ? 1 : 0;
+            }
+            for (int q = threadIdx.x; q < n; q += blockDim.x) {
+                sx[q] ^= (uint8_t)getbit(X, W, q, row);
+                sz[q] ^= (uint8_t)getbit(Z, W, q, row);
+            }
+            __syncthreads();
+        }
+        const int out = sr;
+        __syncthreads();
+        return out;
+    }
+    // random outcome (stabilizer.py:308-327): rowsum row p into every other row with x[a] set
+    const int rp = getbit(R, W, 0, p);
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+        const uint64_t tmask = X[(int64_t)a * W + w] & ~((p >> 6) == w ? (1ull << (p & 63)) : 0ull);
+        if (!tmask) continue;
+        uint64_t c0 = 0, c1 = 0;  // per-row phase exponent mod 4, bit sliced
+        for (int q = 0; q < n; ++q) {
+            const int xs = getbit(X, W, q, p), zs = getbit(Z, W, q, p);
+            if (!xs && !zs) continue;
+            const uint64_t xt = X[(int64_t)q * W + w], zt = Z[(int64_t)q * W + w];
+            uint64_t P, M;
+            if (xs && zs) {
+                P = ~xt & zt;
+                M = xt & ~zt;
+            } else if (xs) {
+                P = xt & zt;
+                M = ~xt & zt;
+            } else {
+                P = xt & ~zt;
+                M = xt & zt;
+            }
+            c1 ^= c0 & P;
+            c0 ^= P;
+            c1 ^= c0 & M;  // + 3 = + 1 then + 2
+            c0 ^= M;
+            c1 ^= M;
+        }
+        const uint64_t rt = R[w];
+        const uint64_t rpm = rp ? ~0ull : 0ull;
+        const uint64_t newr = ~c0 & (c1 ^ rt ^ rpm);
+        R[w] = (rt & ~tmask) | (newr & tmask);
+        for (int q = 0; q < n; ++q) {
+            if (getbit(X, W, q, p)) X[(int64_t)q * W + w] ^= tmask;
+            if (getbit(Z, W, q, p)) Z[(int64_t)q * W + w] ^= tmask;
+        }
+    }
+    __syncthreads();
+    // row p-n := row p; row p := Z_a; r[p] := outcome
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        setbit(X, W, q, p - n, getbit(X, W, q, p));
+        setbit(Z, W, q, p - n, getbit(Z, W, q, p));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        setbit(R, W, 0, p - n, getbit(R, W, 0, p));
+        outcome = (int)(rng_uint32(g) >> 31);  // integers(2): top bit of a uint32
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        setbit(X, W, q, p, 0);
+        setbit(Z, W, q, p, q == a ? 1 : 0);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) setbit(R, W, 0, p, outcome);
+    __syncthreads();
+    return outcome;
+}
+
+__global__ void k_per_shot(ShotArgs A) {
+    const int n = A.n, W = A.W;
+    __shared__ RngCtl g;
+    __shared__ uint64_t clb[4];
+    __shared__ int pc_next;
+    __shared__ uint32_t racc_all;
+    if (threadIdx.x == 0) g = *A.rng;
+    __syncthreads();
+    const int64_t tw = (int64_t)n * W;
+    for (int64_t s = 0; s < A.shots; ++s) {
+        for (int64_t i = threadIdx.x; i < tw; i += blockDim.x) {
+            A.X[i] = A.px[i];
+            A.Z[i] = A.pz[i];
+        }
+        for (int w = threadIdx.x; w < W; w += blockDim.x) A.R[w] = A.pr[w];
+        if (threadIdx.x < 4) clb[threadIdx.x] = 0;
+        __syncthreads();
+        int pc = 0;
+        while (pc < A.nops) {
+            const ShotOp op = A.ops[pc];
+            int next = pc + 1;
+            if (op.code < 100) {
+                for (int w = threadIdx.x; w < W; w += blockDim.x) A.R[w] ^= tab_gate64(A.X, A.Z, W, w, op, A.tables);
+                __syncthreads();
+                if (op.noise >= 0) {
+                    const NTable& nt = A.noise[op.noise];
+                    __shared__ int pick;
+                    if (threadIdx.x == 0) {
+                        const double u = rng_double(g);
+                        int k = 0;
+                        while (k < nt.nb && nt.cum[k] <= u) ++k;
+                        pick = k > nt.nb - 1 ? nt.nb - 1 : k;
+                    }
+                    __syncthreads();
+                    const uint8_t lab = nt.label[pick];
+                    const int qs[2] = {op.a, op.b};
+                    for (int w = threadIdx.x; w < W; w += blockDim.x)
+                        for (int qi = 0; qi < nt.k; ++qi) {
+                            const int sh = 2 * (nt.k - 1 - qi);
+                            if ((lab >> (sh + 1)) & 1) A.R[w] ^= A.Z[(int64_t)qs[qi] * W + w];
+                            if ((lab >> sh) & 1) A.R[w] ^= A.X[(int64_t)qs[qi] * W + w];
+                        }
+                    __syncthreads();
+                }
+            } else if (op.code == 100 || op.code == 101) {
+                int out = shot_measure(A, op.a, g);
+                if (op.code == 101) {
+                    if (out) {  // X on a after the measurement (Tableau.reset, stabilizer.py:329-331)
+                        for (int w = threadIdx.x; w < W; w += blockDim.x) A.R[w] ^= A.Z[(int64_t)op.a * W + w];
+                    }
+                    __syncthreads();
+                } else {
+                    if (threadIdx.x == 0) {
+                        if (op.noise >= 0) {
+                            const double u = rng_double(g);
+                            if (u < (out ? A.readout[2 * op.noise + 1] : A.readout[2 * op.noise])) out ^= 1;
+                        }
+                        if (op.clbit >= 0) {
+                            uint64_t& word = clb[op.clbit >> 6];
+                            const uint64_t bit = 1ull << (op.clbit & 63);
+                            word = out ? (word | bit) : (word & ~bit);
+                        }
+                    }
+                    __syncthreads();
+                }
+            } else if (op.code == 102) {
+                if (threadIdx.x == 0) {
+                    const ShotCond& c = A.conds[op.c];
+                    uint64_t reading = 0;
+                    for (int i = 0; i < c.n; ++i) reading |= ((clb[c.bits[i] >> 6] >> (c.bits[i] & 63)) & 1ull) << i;
+                    const bool holds = (reading == c.value) != (c.negate != 0);
+                    pc_next = holds ? pc + 1 : op.aux;
+                }
+                __syncthreads();
+                next = pc_next;
+                __syncthreads();
+            } else if (op.code == 103) {
+                next = op.aux;  // the end of the then-branch skips the else-branch
+            }
+            pc = next;
+        }
+        if (threadIdx.x < A.ncl_words) A.out[s * A.ncl_words + threadIdx.x] = clb[threadIdx.x];
+        __syncthreads();
+    }
+    (void)racc_all;
+    if (threadIdx.x == 0) *A.rng = g;
+}
+
+}  // namespace lsg
+
+extern "C" int lsg_per_shot_run(int n, const lsg_cgate* prefix, int64_t nprefix, const lsg_shot_op* ops, int32_t nops,
+                                const uint8_t* tables, int32_t ntables, const lsg_noise_table* noise, int32_t nnoise,
+                                const double* readout, int32_t nreadout, const lsg_shot_cond* conds, int32_t nconds,
+                                int32_t num_clbits, int64_t shots, uint64_t* rng_state, uint64_t* clbits_out) {
+    using namespace lsg;
+    clear_error();
+    if (n < 1 || n > 2048 || nprefix < 0 || nops < 0 || shots < 0 || !rng_state || !clbits_out || num_clbits < 0 ||
+        num_clbits > 256 || (nops && !ops) || (nprefix && !prefix))
+        return fail(LSG_E_ARG, "lsg_per_shot_run: bad arguments");
+    if (shots == 0) return LSG_OK;
+    // validate the program
+    for (int i = 0; i < nops; ++i) {
+        const lsg_shot_op& o = ops[i];
+        const bool gate = o.code < 100;
+        if (gate) {
+            const int k = (o.code == 7 || o.code == 8) ? 2 : (o.code >= 16 ? o.nq : 1);
+            if ((o.code > 8 && o.code < 16) || (o.code >= 16 && o.code - 16 >= ntables) || k < 1 || k > 3)
+                return fail(LSG_E_ARG, "op %d: bad gate", i);
+            const int q[3] = {o.a, o.b, o.c};
+            for (int j = 0; j < k; ++j)
+                if (q[j] < 0 || q[j] >= n) return fail(LSG_E_ARG, "op %d: bad qubit", i);
+            if (o.noise >= nnoise) return fail(LSG_E_ARG, "op %d: bad noise table", i);
+        } else if (o.code == 100 || o.code == 101) {
+            if (o.a < 0 || o.a >= n || o.clbit >= num_clbits || o.noise >= nreadout) return fail(LSG_E_ARG, "op %d: bad measurement", i);
+        } else if (o.code == 102) {
+            if (o.c < 0 || o.c >= nconds || o.aux <= i || o.aux > nops) return fail(LSG_E_ARG, "op %d: bad if", i);
+        } else if (o.code == 103) {
+            if (o.aux <= i || o.aux > nops) return fail(LSG_E_ARG, "op %d: bad else", i);
+        } else if (o.code != 104) {
+            return fail(LSG_E_ARG, "op %d: unknown code", i);
+        }
+    }
+    for (int i = 0; i < nconds; ++i) {
+        if (conds[i].n < 1 || conds[i].n > 64) return fail(LSG_E_ARG, "condition %d is malformed", i);
+        for (int j = 0; j < conds[i].n; ++j)
+            if (conds[i].bits[j] < 0 || conds[i].bits[j] >= num_clbits) return fail(LSG_E_ARG, "condition %d names a missing bit", i);
+    }
+    // the prefix tableau, then qubit-major 64-bit words
+    lsg_tab t = nullptr;
+    LSG_CHECK(lsg_tab_create(n, &t));
+    int rc = lsg_tab_apply(t, prefix, nprefix, tables, ntables);
+    if (rc != LSG_OK) {
+        lsg_tab_free(t);
+        return rc;
+    }
+    const int W = (2 * n + 63) / 64;
+    std::vector<uint8_t> hx((size_t)n * 2 * n), hz((size_t)n * 2 * n), hr(2 * n);
+    rc = lsg_tab_download(t, hx.data(), hz.data(), hr.data());
+    lsg_tab_free(t);
+    LSG_CHECK(rc);
+    std::vector<uint64_t> px((size_t)n * W, 0), pz((size_t)n * W, 0), pr(W, 0);
+    for (int q = 0; q < n; ++q)
+        for (int row = 0; row < 2 * n; ++row) {
+            if (hx[(size_t)q * 2 * n + row]) px[(size_t)q * W + (row >> 6)] |= 1ull << (row & 63);
+            if (hz[(size_t)q * 2 * n + row]) pz[(size_t)q * W + (row >> 6)] |= 1ull << (row & 63);
+        }
+    for (int row = 0; row < 2 * n; ++row)
+        if (hr[row]) pr[row >> 6] |= 1ull << (row & 63);
+    std::vector<ShotOp> dops(std::max(nops, 1));
+    for (int i = 0; i < nops; ++i)
+        dops[i] = ShotOp{ops[i].code, ops[i].noise, ops[i].a, ops[i].b, ops[i].c, ops[i].clbit, ops[i].aux};
+    std::vector<ShotCond> dconds(std::max(nconds, 1));
+    for (int i = 0; i < nconds; ++i) {
+        dconds[i].n = conds[i].n;
+        dconds[i].negate = conds[i].negate;
+        dconds[i].value = conds[i].value;
+        for (int j = 0; j < 64; ++j) dconds[i].bits[j] = conds[i].bits[j];
+    }
+    std::vector<CTable> ct;
+    LSG_CHECK(tables_device(tables, ntables, ct));
+    std::vector<NTable> nt(std::max(nnoise, 1));
+    for (int i = 0; i < nnoise; ++i) {
+        nt[i].k = noise[i].k;
+        nt[i].nb = noise[i].nbranch;
+        for (int j = 0; j < 16; ++j) {
+            nt[i].cum[j] = noise[i].cumulative[j];
+            nt[i].label[j] = noise[i].label[j];
+        }
+    }
+    RngCtl g0{};
+    g0.s = ((u128)rng_state[0] << 64) | rng_state[1];
+    g0.inc = ((u128)rng_state[2] << 64) | rng_state[3];
+    g0.pos = 0;
+    g0.has32 = (uint32_t)rng_state[4];
+    g0.buf32 = (uint32_t)rng_state[5];
+    const int words = std::max(1, (num_clbits + 63) / 64);
+    auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
+    size_t off = 0;
+    const size_t tb = (size_t)n * W * 8;
+    const size_t o_px = off; off += al(tb);
+    const size_t o_pz = off; off += al(tb);
+    const size_t o_pr = off; off += al((size_t)W * 8);
+    const size_t o_x = off; off += al(tb);
+    const size_t o_z = off; off += al(tb);
+    const size_t o_r = off; off += al((size_t)W * 8);
+    const size_t o_sx = off; off += al((size_t)2 * n);
+    const size_t o_ops = off; off += al(dops.size() * sizeof(ShotOp));
+    const size_t o_c = off; off += al(dconds.size() * sizeof(ShotCond));
+    const size_t o_t = off; off += al(ct.size() * sizeof(CTable));
+    const size_t o_n = off; off += al(nt.size() * sizeof(NTable));
+    const size_t o_ro = off; off += al((size_t)std::max(nreadout, 1) * 16);
+    const size_t o_out = off; off += al((size_t)shots * words * 8);
+    const size_t o_g = off; off += al(sizeof(RngCtl));
+    Scratch work;
+    LSG_CHECK(ensure(work, off));
+    char* b = (char*)work.ptr;
+    cudaError_t ce = cudaSuccess;
+    auto H2D = [&](size_t o, const void* src, size_t bytes) {
+        if (bytes && ce == cudaSuccess) ce = cudaMemcpy(b + o, src, bytes, cudaMemcpyHostToDevice);
+    };
+    H2D(o_px, px.data(), tb);
+    H2D(o_pz, pz.data(), tb);
+    H2D(o_pr, pr.data(), (size_t)W * 8);
+    H2D(o_ops, dops.data(), dops.size() * sizeof(ShotOp));
+    H2D(o_c, dconds.data(), dconds.size() * sizeof(ShotCond));
+    H2D(o_t, ct.data(), ct.size() * sizeof(CTable));
+    H2D(o_n, nt.data(), nt.size() * sizeof(NTable));
+    if (nreadout) H2D(o_ro, readout, (size_t)nreadout * 16);
+    H2D(o_g, &g0, sizeof(RngCtl));
+    ShotArgs A{};
+    A.n = n;
+    A.W = W;
+    A.nops = nops;
+    A.ncl_words = words;
+    A.shots = shots;
+    A.ops = (const ShotOp*)(b + o_ops);
+    A.conds = (const ShotCond*)(b + o_c);
+    A.tables = (const CTable*)(b + o_t);
+    A.noise = (const NTable*)(b + o_n);
+    A.readout = (const double*)(b + o_ro);
+    A.px = (const uint64_t*)(b + o_px);
+    A.pz = (const uint64_t*)(b + o_pz);
+    A.pr = (const uint64_t*)(b + o_pr);
+    A.X = (uint64_t*)(b + o_x);
+    A.Z = (uint64_t*)(b + o_z);
+    A.R = (uint64_t*)(b + o_r);
+    A.sx = (uint8_t*)(b + o_sx);
+    A.out = (uint64_t*)(b + o_out);
+    A.rng = (RngCtl*)(b + o_g);
+    if (ce == cudaSuccess) {
+        k_per_shot<<<1, 512>>>(A);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+    std::vector<uint64_t> out((size_t)shots * words);
+    RngCtl gend{};
+    if (ce == cudaSuccess) ce = cudaMemcpy(out.data(), b + o_out, out.size() * 8, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&gend, b + o_g, sizeof(RngCtl), cudaMemcpyDeviceToHost);
+    release(work);
+    if (ce != cudaSuccess) return fail(LSG_E_CUDA, "the per-shot run failed: %s", cudaGetErrorString(ce));
+    for (int64_t s = 0; s < shots; ++s)
+        for (int w = 0; w < 4; ++w) clbits_out[s * 4 + w] = w < words ? out[(size_t)s * words + w] : 0;
+    rng_state[0] = (uint64_t)(gend.s >> 64);
+    rng_state[1] = (uint64_t)gend.s;
+    rng_state[4] = gend.has32;
+    rng_state[5] = gend.buf32;
+    rng_state[6] = gend.pos;
+    return LSG_OK;
+}

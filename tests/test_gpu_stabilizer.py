@@ -91,3 +91,22 @@ def test_sampled_against_oracle_and_rng_position():
     got = st.sampled(c, 701, NoiseModel().add_readout_error(0.1), rng_b)
     assert got == want
     assert rng_b.bit_generator.state == rng_a.bit_generator.state
+
+
+def test_per_shot_golden_and_oracle(golden):
+    g = golden["stab_pershot"]
+    noise = NoiseModel().add_gate_error(depolarizing(0.05))
+    assert ls.run(g["qasm"], shots=g["shots"], seed=g["seed"], noise=noise).counts == g["counts"]
+    # more shapes against the oracle, with readout and the generator's final state
+    src = g["qasm"].replace("c = measure q;", "c[3] = measure q[3]; if (c[3] == 1) { x q[5]; } else { h q[5]; }\nc = measure q;")
+    c = ls.parse(src)
+    noise = NoiseModel().add_gate_error(depolarizing(0.1)).add_gate_error(depolarizing(0.05, 2))
+    noise.add_readout_error(ReadoutError(0.02, 0.05))
+    from lucivant_sim_gb300 import stabilizer_shots
+
+    rng_a = np.random.default_rng(77)
+    want = tableau.per_shot(c, 150, noise, rng_a)
+    rng_b = np.random.default_rng(77)
+    got = stabilizer_shots.per_shot(c, 150, noise, rng_b)
+    assert got == want
+    assert rng_b.bit_generator.state == rng_a.bit_generator.state
