@@ -103,11 +103,109 @@ int op_bits_ok(const lsg_op& op, int nbits) {
     return 1;
 }
 
+// Register blocks: consecutive operators of a pass (already in a valid order) grouped while the
+// union of their bits stays within umax bits. A two-qubit depolarising operator fixes its block's
+// bit order (row a, row b, col a, col b); everything else takes ascending order.
+static bool block_kind(const TileOp& t, int umax) {
+    switch (t.kind) {
+        case LSG_OP_MATRIX: return t.k == 1 || (t.k == 2 && umax >= 2);
+        case LSG_OP_PERM: return t.k == 1 || (t.k == 2 && umax >= 2);
+        case LSG_OP_DEPOL: return t.k == 2 || (t.k == 4 && umax >= 4);
+        case LSG_OP_DIAG: return t.k <= umax;
+        case LSG_OP_SCALE: return true;
+        case kOpMixture: return t.k == 1 || (t.k == 2 && umax >= 2);
+        default: return false;
+    }
+}
+
+static void finish_block(Plan& plan, int pass_first, int first, int count, std::vector<int>& bits, int depol2) {
+    BlockDesc b{};
+    b.first = first - pass_first;  // the kernel indexes the pass's operators from 0
+    b.nops = count;
+    b.generic = 0;
+    std::vector<int> order;
+    if (depol2 >= 0) {
+        for (int i = 0; i < 4; ++i) order.push_back(plan.ops[depol2].lb[i]);
+    } else {
+        order = bits;
+        std::sort(order.begin(), order.end());
+    }
+    if (order.empty()) order.push_back(0);  // operators with no bits (a global phase)
+    b.u = (int)order.size();
+    for (int i = 0; i < b.u; ++i) {
+        b.bits[i] = order[i];
+        b.sorted[i] = order[i];
+    }
+    std::sort(b.sorted, b.sorted + b.u);
+    for (int o = first; o < first + count; ++o) {
+        TileOp& t = plan.ops[o];
+        int P[8] = {0};
+        for (int i = 0; i < t.k; ++i)
+            for (int j = 0; j < b.u; ++j)
+                if (order[j] == t.lb[i]) P[i] = j;
+        for (int i = 0; i < 8; ++i) t.pos[i] = P[i];
+        switch (t.kind) {
+            case LSG_OP_MATRIX: t.tmpl = t.k == 1 ? kT_DENSE1 + P[0] : kT_DENSE2 + 4 * P[0] + P[1]; break;
+            case LSG_OP_PERM: t.tmpl = t.k == 1 ? kT_PERM1 + P[0] : kT_PERM2 + 4 * P[0] + P[1]; break;
+            case LSG_OP_DEPOL: t.tmpl = t.k == 2 ? kT_DEPOL1 + 4 * P[0] + P[1] : kT_DEPOL2; break;
+            case LSG_OP_DIAG: t.tmpl = kT_DIAG; break;
+            case LSG_OP_SCALE: t.tmpl = kT_SCALE; break;
+            case kOpMixture: t.tmpl = t.k == 1 ? kT_MIX1 + P[0] : kT_MIX2 + 4 * P[0] + P[1]; break;
+            default: t.tmpl = kT_GENERIC; break;
+        }
+    }
+    plan.blocks.push_back(b);
+}
+
+static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
+    pd.first_block = (int)plan.blocks.size();
+    std::vector<int> bits;
+    int start = pd.first_op, count = 0, depol2 = -1;
+    auto flush = [&]() {
+        if (count) finish_block(plan, pd.first_op, start, count, bits, depol2);
+        bits.clear();
+        count = 0;
+        depol2 = -1;
+    };
+    for (int o = pd.first_op; o < pd.first_op + pd.nops; ++o) {
+        TileOp& t = plan.ops[o];
+        if (umax < 1 || !block_kind(t, umax)) {
+            flush();
+            BlockDesc g{};
+            g.first = o - pd.first_op;
+            g.nops = 1;
+            g.generic = 1;
+            t.tmpl = kT_GENERIC;
+            plan.blocks.push_back(g);
+            start = o + 1;
+            continue;
+        }
+        std::vector<int> grown = bits;
+        for (int i = 0; i < t.k; ++i)
+            if (std::find(grown.begin(), grown.end(), t.lb[i]) == grown.end()) grown.push_back(t.lb[i]);
+        const bool is_d2 = t.kind == LSG_OP_DEPOL && t.k == 4;
+        bool fits = (int)grown.size() <= umax;
+        if (fits && is_d2 && (depol2 >= 0 || (int)grown.size() != 4)) fits = false;
+        if (fits && depol2 >= 0 && (int)grown.size() != 4) fits = false;
+        if (!fits) {
+            flush();
+            start = o;
+            grown.clear();
+            for (int i = 0; i < t.k; ++i) grown.push_back(t.lb[i]);
+        }
+        bits = grown;
+        if (is_d2) depol2 = o;
+        ++count;
+    }
+    flush();
+    pd.nblocks = (int)plan.blocks.size() - pd.first_block;
+}
+
 // Greedy fusion: sweep the remaining operators; an operator joins the current pass when its bits
 // fit the tile and no operator deferred earlier in the sweep shares a bit with it (so program
 // order is kept wherever it matters). Deferred operators start the next sweep.
 Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* pred, const int* draw,
-              const int* count) {
+              const int* count, int umax) {
     Plan plan;
     std::vector<int> remaining(nops);
     for (int i = 0; i < nops; ++i) remaining[i] = i;
@@ -180,17 +278,50 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
             t.count = count ? count[idx] : 0;
             plan.ops.push_back(t);
         }
+        form_blocks(plan, pd, umax);
         plan.passes.push_back(pd);
         remaining.swap(deferred);
     }
     return plan;
 }
 
-static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L) {
-    return plan_ops(ops, nops, nbits, K, L, nullptr, nullptr, nullptr);
+// Widest register block per precision: 16 complex64 or 8 complex128 amplitudes per thread.
+int block_bits_for(int precision) {
+    int u = precision == LSG_C128 ? 3 : 4;
+    if (const char* env = getenv("LSG_BLOCK_BITS")) u = atoi(env);
+    return std::max(0, std::min(u, precision == LSG_C128 ? 3 : 4));
+}
+
+static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L, int umax) {
+    return plan_ops(ops, nops, nbits, K, L, nullptr, nullptr, nullptr, umax);
 }
 
 // ------------------------------------------------------------------------ programs
+
+// Every block indexes inside its pass's operators and covers them exactly; every operator bit
+// lies inside its tile; every tile bit is a register bit.
+static int check_plan(const Plan& plan) {
+    for (const PassDesc& pd : plan.passes) {
+        int covered = 0;
+        for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
+            if (bi < 0 || bi >= (int)plan.blocks.size()) return fail(LSG_E_ARG, "internal planning error: block index");
+            const BlockDesc& b = plan.blocks[bi];
+            if (b.first != covered || b.nops < 1 || b.first + b.nops > pd.nops || (!b.generic && (b.u < 1 || b.u > 4)))
+                return fail(LSG_E_ARG, "internal planning error: a block outside its pass");
+            for (int i = 0; !b.generic && i < b.u; ++i)
+                if (b.bits[i] < 0 || b.bits[i] >= pd.K) return fail(LSG_E_ARG, "internal planning error: block bit");
+            covered += b.nops;
+        }
+        if (covered != pd.nops) return fail(LSG_E_ARG, "internal planning error: blocks do not cover the pass");
+        for (int o = pd.first_op; o < pd.first_op + pd.nops; ++o) {
+            const TileOp& t = plan.ops[o];
+            for (int i = 0; i < t.k; ++i)
+                if (t.lb[i] < 0 || t.lb[i] >= pd.K) return fail(LSG_E_ARG, "internal planning error: operator bit");
+        }
+        if (pd.L < 0 || pd.L > pd.K || pd.nouter < 0) return fail(LSG_E_ARG, "internal planning error: tile shape");
+    }
+    return LSG_OK;
+}
 
 int tile_bits_for(int nbits, int precision) {
     int K = precision == LSG_C128 ? 10 : 11;
@@ -265,12 +396,13 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
     const PassDesc* pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
     const TileOp* ops_dev = reinterpret_cast<const TileOp*>(pd_dev + p->plan.passes.size());
+    const BlockDesc* blk_dev = reinterpret_cast<const BlockDesc*>(ops_dev + p->plan.ops.size());
     const Cx<R>* pool_dev =
         reinterpret_cast<const Cx<R>*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
     for (size_t i = 0; i < p->plan.passes.size(); ++i) {
         if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
         kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(reinterpret_cast<Cx<R>*>(s->data), s->elems, pd_dev + i,
-                                                          ops_dev, pool_dev, tiles_per_member, total, status, ctx);
+                                                          ops_dev, blk_dev, pool_dev, tiles_per_member, total, status, ctx);
     }
     if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
     LSG_CUDA(cudaGetLastError());
@@ -286,27 +418,35 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
     p->K = tile_bits_for(nbits, precision);
     const int L = std::min(p->K, low_bits_for(nbits, precision));
     if (nops > 0) {
-        p->plan = plan_ops(ops, nops, nbits, p->K, L, pred, draw, count);
+        p->plan = plan_ops(ops, nops, nbits, p->K, L, pred, draw, count, block_bits_for(precision));
         if (p->plan.passes.empty()) {
             delete p;
             return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits (%d kept low)", tile_bits_for(nbits, precision), L);
         }
     }
-    int max_ops = 0;
-    for (const PassDesc& pd : p->plan.passes) max_ops = std::max(max_ops, pd.nops);
+    if (check_plan(p->plan) != LSG_OK) {
+        delete p;
+        return LSG_E_ARG;
+    }
+    size_t max_meta = 0;
+    for (const PassDesc& pd : p->plan.passes)
+        max_meta = std::max(max_meta, (size_t)pd.nops * sizeof(TileOp) + (size_t)pd.nblocks * sizeof(BlockDesc));
     const size_t elt = precision == LSG_C128 ? 16 : 8;
-    p->smem = (elt << p->K) + (size_t)max_ops * sizeof(TileOp);
+    p->smem = (elt << p->K) + max_meta;
     if (p->smem > 220 * 1024) {
         delete p;
-        return fail(LSG_E_ARG, "a pass needs %zu bytes of shared memory", (size_t)((elt << tile_bits_for(nbits, precision)) + (size_t)max_ops * sizeof(TileOp)));
+        return fail(LSG_E_ARG, "a pass needs more than 220 KB of shared memory");
     }
-    const size_t head = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp);
+    const size_t head = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp) +
+                        p->plan.blocks.size() * sizeof(BlockDesc);
     p->head_aligned = (head + 255) & ~size_t(255);
     const size_t total = p->head_aligned + (size_t)pool_entries * elt;
     std::vector<unsigned char> blob(std::max<size_t>(total, 1));
     std::memcpy(blob.data(), p->plan.passes.data(), p->plan.passes.size() * sizeof(PassDesc));
     std::memcpy(blob.data() + p->plan.passes.size() * sizeof(PassDesc), p->plan.ops.data(),
                 p->plan.ops.size() * sizeof(TileOp));
+    std::memcpy(blob.data() + p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp),
+                p->plan.blocks.data(), p->plan.blocks.size() * sizeof(BlockDesc));
     if (precision == LSG_C128) {
         if (pool_entries) std::memcpy(blob.data() + p->head_aligned, pool, (size_t)pool_entries * 16);
     } else {
@@ -576,8 +716,9 @@ int lsg_plan(int nbits, int precision, const lsg_op* ops, int32_t nops, int32_t*
         if (!op_bits_ok(ops[i], nbits)) return fail(LSG_E_ARG, "operator %d has a bad kind or bits", i);
     const int K = tile_bits_for(nbits, precision);
     const int L = std::min(K, low_bits_for(nbits, precision));
-    Plan plan = plan_passes(ops, nops, nbits, K, L);
+    Plan plan = plan_passes(ops, nops, nbits, K, L, block_bits_for(precision));
     if (nops > 0 && plan.passes.empty()) return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits", K);
+    LSG_CHECK(check_plan(plan));
     *passes = (int32_t)plan.passes.size();
     return LSG_OK;
 }

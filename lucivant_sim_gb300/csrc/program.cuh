@@ -12,8 +12,20 @@ namespace lsg {
 // tile (outer[]) enumerate the tiles.
 struct PassDesc {
     int K, L, nouter, nops, first_op, pad;
+    int first_block, nblocks;
     int hi[32];
     int outer[32];
+};
+
+// A register block: consecutive operators of a pass whose bits together span u <= 4 tile bits.
+// Each thread loads groups of 2^u amplitudes into registers once, applies every operator of the
+// block with compile-time positions, and stores once. bits[i] is the tile bit of block position i
+// (position 0 = most significant bit of the group index); sorted[] the same bits ascending.
+// generic = 1: a single operator run by the shared-memory path (wider than a register block).
+struct BlockDesc {
+    int u, first, nops, generic;
+    int bits[4];
+    int sorted[4];
 };
 
 // Operator kinds beyond the public LSG_OP_* set, used by trajectory programs.
@@ -29,17 +41,32 @@ struct TileOp {
     int pred;       // predicate bit the member must have set (0: always set)
     int draw;       // trajectory ops: uniform offset from the member's cursor
     int count;      // mixture branches
-    int pad;
+    int tmpl;       // register-block code: kind and positions (see tile.cuh)
+    int pos[8];     // positions of the operator's bits within its block (0 = block MSB)
 };
 
 struct Plan {
     std::vector<PassDesc> passes;
     std::vector<TileOp> ops;
+    std::vector<BlockDesc> blocks;
 };
+
+// register-block codes (TileOp::tmpl)
+constexpr int kT_DENSE1 = 0;    // + P
+constexpr int kT_DENSE2 = 4;    // + 4 * P0 + P1
+constexpr int kT_PERM1 = 20;    // + P
+constexpr int kT_PERM2 = 24;    // + 4 * P0 + P1
+constexpr int kT_DEPOL1 = 40;   // + 4 * Prow + Pcol
+constexpr int kT_DEPOL2 = 56;   // canonical positions (row a, row b, col a, col b) = (0, 1, 2, 3)
+constexpr int kT_DIAG = 57;
+constexpr int kT_SCALE = 58;
+constexpr int kT_MIX1 = 60;     // + P
+constexpr int kT_MIX2 = 64;     // + 4 * P0 + P1
+constexpr int kT_GENERIC = -1;
 // The greedy fusion planner (csrc/engine.cu): lsg_op list -> passes of tile-local operators.
 // pred/draw/count (may be null) give trajectory operators their predicate bit, uniform offset and
 // branch count.
 Plan plan_ops(const struct lsg_op* ops, int nops, int nbits, int K, int L, const int* pred, const int* draw,
-              const int* count);
+              const int* count, int umax);
 
 }  // namespace lsg

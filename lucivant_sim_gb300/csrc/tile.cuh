@@ -224,6 +224,220 @@ __device__ __forceinline__ void op_mixture(Cx<R>* t, int tbits, const TileOp& op
     else wide_op<R>(t, tbits, LSG_OP_MATRIX, op.k, op.lb, op.sorted, mat);
 }
 
+
+// ------------------------------------------------------------------ register blocks
+//
+// v[e] holds the amplitude at group offset e of a block of U bits; bit (U-1-P) of e is block
+// position P. Every function below is fully unrolled over e, so v stays in registers.
+
+template <typename R, int U, int P>
+__device__ __forceinline__ void rb_dense1(Cx<R>* v, const Cx<R>* m) {
+    constexpr int B = 1 << (U - 1 - P);
+    const Cx<R> m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & B) continue;
+        const Cx<R> a0 = v[e], a1 = v[e | B];
+        v[e] = cfma(m01, a1, cmul(m00, a0));
+        v[e | B] = cfma(m11, a1, cmul(m10, a0));
+    }
+}
+
+template <typename R, int U, int P0, int P1>
+__device__ __forceinline__ void rb_dense2(Cx<R>* v, const Cx<R>* m) {
+    constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & (B0 | B1)) continue;
+        const Cx<R> a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            Cx<R> acc = cmul(m[4 * r], a0);
+            acc = cfma(m[4 * r + 1], a1, acc);
+            acc = cfma(m[4 * r + 2], a2, acc);
+            acc = cfma(m[4 * r + 3], a3, acc);
+            v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
+        }
+    }
+}
+
+template <typename R, int U, int P>
+__device__ __forceinline__ void rb_perm1(Cx<R>* v, const Cx<R>* m) {
+    constexpr int B = 1 << (U - 1 - P);
+    const Cx<R> p0 = m[0], p1 = m[1];
+    const bool swap = m[2].re != R(0);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & B) continue;
+        const Cx<R> a0 = v[e], a1 = v[e | B];
+        v[e] = cmul(p0, swap ? a1 : a0);
+        v[e | B] = cmul(p1, swap ? a0 : a1);
+    }
+}
+
+template <typename R, int U, int P0, int P1>
+__device__ __forceinline__ void rb_perm2(Cx<R>* v, const Cx<R>* m) {
+    constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+    const Cx<R> p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
+    const int s0 = (int)m[4].re, s1 = (int)m[5].re, s2 = (int)m[6].re, s3 = (int)m[7].re;
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & (B0 | B1)) continue;
+        const Cx<R> a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+        v[e] = cmul(p0, pick4(a0, a1, a2, a3, s0));
+        v[e | B1] = cmul(p1, pick4(a0, a1, a2, a3, s1));
+        v[e | B0] = cmul(p2, pick4(a0, a1, a2, a3, s2));
+        v[e | B0 | B1] = cmul(p3, pick4(a0, a1, a2, a3, s3));
+    }
+}
+
+// (1-p) rho + (p/2) I Tr on one row bit (position PR) and its column bit (PC)
+template <typename R, int U, int PR, int PC>
+__device__ __forceinline__ void rb_depol1(Cx<R>* v, const Cx<R>* m) {
+    constexpr int BR = 1 << (U - 1 - PR), BC = 1 << (U - 1 - PC);
+    const R p = m[0].re, keep = R(1) - p, share = p / R(2);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & (BR | BC)) continue;
+        const Cx<R> d0 = v[e], d1 = v[e | BR | BC];
+        const Cx<R> tr(d0.re + d1.re, d0.im + d1.im);
+        v[e] = Cx<R>(d0.re * keep + share * tr.re, d0.im * keep + share * tr.im);
+        v[e | BR | BC] = Cx<R>(d1.re * keep + share * tr.re, d1.im * keep + share * tr.im);
+        const Cx<R> o1 = v[e | BC], o2 = v[e | BR];
+        v[e | BC] = Cx<R>(o1.re * keep, o1.im * keep);
+        v[e | BR] = Cx<R>(o2.re * keep, o2.im * keep);
+    }
+}
+
+// two-qubit form on positions (row a, row b, col a, col b) = (0, 1, 2, 3) of a 4-bit block
+template <typename R>
+__device__ __forceinline__ void rb_depol2(Cx<R>* v, const Cx<R>* m) {
+    const R p = m[0].re, keep = R(1) - p, share = p / R(4);
+    Cx<R> tr;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        tr.re += v[(t << 2) | t].re;
+        tr.im += v[(t << 2) | t].im;
+    }
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        Cx<R> o(v[e].re * keep, v[e].im * keep);
+        if ((e >> 2) == (e & 3)) {
+            o.re += share * tr.re;
+            o.im += share * tr.im;
+        }
+        v[e] = o;
+    }
+}
+
+template <typename R, int U>
+__device__ __forceinline__ void rb_diag(Cx<R>* v, const TileOp& op, const Cx<R>* m) {
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        int j = 0;
+        for (int b = 0; b < op.k; ++b) j = (j << 1) | ((e >> (U - 1 - op.pos[b])) & 1);
+        v[e] = cmul(m[j], v[e]);
+    }
+}
+
+template <typename R, int U>
+__device__ __forceinline__ void rb_scale(Cx<R>* v, const Cx<R>* m) {
+    const Cx<R> f = m[0];
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) v[e] = cmul(f, v[e]);
+}
+
+// the branch matrix a member's uniform picks from a mixture channel, or nullptr for identity
+template <typename R>
+__device__ __forceinline__ const Cx<R>* mixture_pick(const TileOp& op, const Cx<R>* m, double u) {
+    const int nb = op.count;
+    int pick = -1;
+    for (int i = 0; i < nb; ++i)
+        if (u < (double)m[i].re) {
+            pick = i;
+            break;
+        }
+    if (pick < 0 || m[pick].im != R(0)) return nullptr;
+    const int d = 1 << op.k;
+    return m + nb + (int64_t)pick * d * d;
+}
+
+#define LSG_P1(X, BASE)                                    \
+    case BASE + 0: if (U > 0) X<R, U, (0 < U ? 0 : 0)>(v, m); break; \
+    case BASE + 1: if (U > 1) X<R, U, (1 < U ? 1 : 0)>(v, m); break; \
+    case BASE + 2: if (U > 2) X<R, U, (2 < U ? 2 : 0)>(v, m); break; \
+    case BASE + 3: if (U > 3) X<R, U, (3 < U ? 3 : 0)>(v, m); break;
+
+#define LSG_P2ONE(X, BASE, A, B) \
+    case BASE + 4 * A + B: if (U > A && U > B) X<R, U, (A < U ? A : 0), (B < U ? B : 0)>(v, m); break;
+
+#define LSG_P2(X, BASE)                                                                                  \
+    LSG_P2ONE(X, BASE, 0, 1) LSG_P2ONE(X, BASE, 0, 2) LSG_P2ONE(X, BASE, 0, 3) LSG_P2ONE(X, BASE, 1, 0) \
+    LSG_P2ONE(X, BASE, 1, 2) LSG_P2ONE(X, BASE, 1, 3) LSG_P2ONE(X, BASE, 2, 0) LSG_P2ONE(X, BASE, 2, 1) \
+    LSG_P2ONE(X, BASE, 2, 3) LSG_P2ONE(X, BASE, 3, 0) LSG_P2ONE(X, BASE, 3, 1) LSG_P2ONE(X, BASE, 3, 2)
+
+template <typename R, int U>
+__device__ __forceinline__ void rb_apply(Cx<R>* v, int code, const TileOp& op, const Cx<R>* m) {
+    switch (code) {
+        LSG_P1(rb_dense1, kT_DENSE1)
+        LSG_P2(rb_dense2, kT_DENSE2)
+        LSG_P1(rb_perm1, kT_PERM1)
+        LSG_P2(rb_perm2, kT_PERM2)
+        LSG_P2(rb_depol1, kT_DEPOL1)
+        case kT_DEPOL2:
+            if (U == 4) rb_depol2<R>(v, m);
+            break;
+        case kT_DIAG: rb_diag<R, U>(v, op, m); break;
+        case kT_SCALE: rb_scale<R, U>(v, m); break;
+        default: break;
+    }
+}
+
+// one register block over the whole tile: each thread takes groups of 2^U amplitudes
+template <typename R, int U>
+__device__ void run_block(Cx<R>* tile, int tbits, const BlockDesc& blk, const TileOp* __restrict__ ops,
+                          const Cx<R>* __restrict__ data, int64_t member, uint64_t pred, const TrajCtx& ctx,
+                          int64_t cur) {
+    uint32_t mask[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) mask[i] = i < U ? (1u << blk.bits[i]) : 0u;
+    const int groups = 1 << (tbits - U);
+    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+        uint32_t base = (uint32_t)g;
+#pragma unroll
+        for (int i = 0; i < U; ++i) base = ins0(base, blk.sorted[i]);
+        Cx<R> v[1 << U];
+#pragma unroll
+        for (int e = 0; e < (1 << U); ++e) {
+            uint32_t off = base;
+#pragma unroll
+            for (int i = 0; i < U; ++i)
+                if ((e >> (U - 1 - i)) & 1) off |= mask[i];
+            v[e] = tile[off];
+        }
+        for (int o = 0; o < blk.nops; ++o) {
+            const TileOp& op = ops[blk.first + o];
+            if (!((pred >> op.pred) & 1)) continue;
+            const Cx<R>* m = data + op.data + member * op.stride;
+            int code = op.tmpl;
+            if (op.kind == kOpMixture) {
+                m = mixture_pick<R>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
+                if (!m) continue;
+                code = (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2));
+            }
+            rb_apply<R, U>(v, code, op, m);
+        }
+#pragma unroll
+        for (int e = 0; e < (1 << U); ++e) {
+            uint32_t off = base;
+#pragma unroll
+            for (int i = 0; i < U; ++i)
+                if ((e >> (U - 1 - i)) & 1) off |= mask[i];
+            tile[off] = v[e];
+        }
+    }
+}
+
 template <typename R>
 __device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, int nops,
                         const Cx<R>* __restrict__ data, int64_t member, const TrajCtx& ctx) {
@@ -262,9 +476,9 @@ __device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, 
 // One fused pass over every tile of every member. Tiles are visited grid-stride; each CTA
 // handles one tile at a time (CTAs co-resident on an SM overlap each other's copies).
 template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) k_tile_pass(Cx<R>* __restrict__ state, int64_t member_elems,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_tile_pass(Cx<R>* __restrict__ state, int64_t member_elems,
                                                    const PassDesc* __restrict__ pass_g,
-                                                   const TileOp* __restrict__ ops,
+                                                   const TileOp* __restrict__ ops, const BlockDesc* __restrict__ blocks,
                                                    const Cx<R>* __restrict__ data, int64_t tiles_per_member,
                                                    int64_t total_tiles, int* status, TrajCtx ctx) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -272,14 +486,19 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) k_tile_pass(Cx<R>
     __shared__ PassDesc pd;
     Cx<R>* tile = reinterpret_cast<Cx<R>*>(smem_raw);
     TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + (sizeof(Cx<R>) << pass_g->K));
+    BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
     if (threadIdx.x == 0) pd = *pass_g;
     {
-        // stage this pass's operators in shared memory (the same for every tile of the pass)
+        // stage this pass's operators and blocks in shared memory (the same for every tile)
         const int nops = pass_g->nops;
         const int* src = reinterpret_cast<const int*>(ops + pass_g->first_op);
         int* dst = reinterpret_cast<int*>(sops);
         const int words = nops * (int)(sizeof(TileOp) / sizeof(int));
         for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+        const int* bsrc = reinterpret_cast<const int*>(blocks + pass_g->first_block);
+        int* bdst = reinterpret_cast<int*>(sblk);
+        const int bwords = pass_g->nblocks * (int)(sizeof(BlockDesc) / sizeof(int));
+        for (int i = threadIdx.x; i < bwords; i += blockDim.x) bdst[i] = bsrc[i];
     }
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -315,8 +534,28 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) k_tile_pass(Cx<R>
                 tile[i] = mem[g];
             }
         }
-        // ---- compute
-        run_ops<R>(tile, K, sops, pd.nops, data, member, ctx);
+        // ---- compute: register blocks, or one shared-memory operator for a wide block
+        {
+            const uint64_t pred = ctx.u ? ctx.pred[member] : ~0ull;
+            const int64_t cur = ctx.u ? ctx.cursor[member] : 0;
+            for (int bi = 0; bi < pd.nblocks; ++bi) {
+                const BlockDesc& blk = sblk[bi];
+                __syncthreads();
+                if (blk.generic) {
+                    run_ops<R>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
+                    continue;
+                }
+                switch (blk.u) {
+                    case 1: run_block<R, 1>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+                    case 2: run_block<R, 2>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+                    case 3: run_block<R, 3>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+                    default:
+                        if constexpr (sizeof(R) == 4) run_block<R, 4>(tile, K, blk, sops, data, member, pred, ctx, cur);
+                        break;
+                }
+            }
+            __syncthreads();
+        }
         // ---- store
         if (use_bulk) {
             fence_proxy_async_smem();

@@ -150,3 +150,26 @@ def test_uint8_integers_stream_layout():
         words += [int(r) & 0xFFFFFFFF, int(r) >> 32]
     bytes_ = [(w >> (8 * i)) & 0xFF for w in words for i in range(4)]
     assert list(vals) == [b >> 7 for b in bytes_[:37]]
+
+
+@pytest.mark.parametrize("tile,low", [(None, None), ("7", "3"), ("8", "3"), ("5", "2"), ("12", "6")])
+def test_plans_are_well_formed(monkeypatch, tile, low):
+    """The host planner's passes and register blocks are checked (lsg_plan validates them) for
+    every shape the GPU tests force, for statevector, density and wide-gate operator lists."""
+    if tile:
+        monkeypatch.setenv("LSG_TILE_BITS", tile)
+        monkeypatch.setenv("LSG_LOW_BITS", low)
+    cases = [
+        (engine.sv_oplist(ls.parse(wl.brickwork(9, 4, seed=1))), 9),
+        (engine.dm_oplist(ls.parse(wl.brickwork(4, 3, seed=2, measure=False)), [wl.dm_noise()]), 8),
+        (engine.dm_oplist(ls.parse(wl.brickwork(5, 2, seed=3, measure=False)),
+                          [NoiseModel().add_gate_error(ls.pauli_channel({"XY": 0.1}), gates="cx")]), 10),
+        (engine.sv_oplist(ls.parse("OPENQASM 3; qubit[6] q; h q; ccx q[0], q[3], q[5]; c4x q[5], q[1], q[2], q[0], q[4]; "
+                                   "rz(0.3) q[2]; gphase(0.2); rzz(0.4) q[1], q[4];")), 6),
+    ]
+    for ops, nbits in cases:
+        for precision in (_lib.C128, _lib.C64):
+            try:
+                assert _lib.plan_passes(nbits, precision, ops) >= 1
+            except ValueError as exc:  # a tile too small for a wide operator is refused, never malformed
+                assert "does not fit" in str(exc), exc
