@@ -118,7 +118,8 @@ static bool block_kind(const TileOp& t, int umax) {
     }
 }
 
-static void finish_block(Plan& plan, int pass_first, int first, int count, std::vector<int>& bits, int depol2) {
+static void finish_block(Plan& plan, int pass_first, int first, int count, std::vector<int>& bits, int depol2,
+                         int K, int rb) {
     BlockDesc b{};
     b.first = first - pass_first;  // the kernel indexes the pass's operators from 0
     b.nops = count;
@@ -130,7 +131,11 @@ static void finish_block(Plan& plan, int pass_first, int first, int count, std::
         order = bits;
         std::sort(order.begin(), order.end());
     }
-    if (order.empty()) order.push_back(0);  // operators with no bits (a global phase)
+    // fill up to the register width with the highest unused tile bits: every thread then owns
+    // 2^rb amplitudes and the warp's lanes stay on the lowest tile bits
+    for (int bit = K - 1; bit >= 0 && (int)order.size() < std::min(rb, K); --bit)
+        if (std::find(order.begin(), order.end(), bit) == order.end()) order.push_back(bit);
+    if (order.empty()) order.push_back(0);
     b.u = (int)order.size();
     for (int i = 0; i < b.u; ++i) {
         b.bits[i] = order[i];
@@ -162,7 +167,7 @@ static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
     std::vector<int> bits;
     int start = pd.first_op, count = 0, depol2 = -1;
     auto flush = [&]() {
-        if (count) finish_block(plan, pd.first_op, start, count, bits, depol2);
+        if (count) finish_block(plan, pd.first_op, start, count, bits, depol2, pd.K, umax);
         bits.clear();
         count = 0;
         depol2 = -1;
@@ -199,6 +204,23 @@ static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
     }
     flush();
     pd.nblocks = (int)plan.blocks.size() - pd.first_block;
+    // shared-memory layouts: linear where the bulk copies and wide operators need it, swizzled
+    // between consecutive register blocks when each thread holds one group (K - u <= 8)
+    bool swizzled = false;  // the tile arrives linear
+    for (int i = 0; i < pd.nblocks; ++i) {
+        BlockDesc& b = plan.blocks[pd.first_block + i];
+        const bool next_reg = i + 1 < pd.nblocks && !plan.blocks[pd.first_block + i + 1].generic;
+        if (b.generic) {
+            b.in_swz = b.out_swz = 0;
+            swizzled = false;
+            continue;
+        }
+        const bool can = pd.K - b.u <= 8;
+        b.in_swz = swizzled ? 1 : 0;
+        b.out_swz = (can && next_reg) ? 1 : 0;
+        if (b.in_swz != b.out_swz && !can) b.out_swz = b.in_swz;  // never happens: in_swz implies can
+        swizzled = b.out_swz != 0;
+    }
 }
 
 // Greedy fusion: sweep the remaining operators; an operator joins the current pass when its bits
@@ -310,6 +332,11 @@ static int check_plan(const Plan& plan) {
                 return fail(LSG_E_ARG, "internal planning error: a block outside its pass");
             for (int i = 0; !b.generic && i < b.u; ++i)
                 if (b.bits[i] < 0 || b.bits[i] >= pd.K) return fail(LSG_E_ARG, "internal planning error: block bit");
+            if (!b.generic && b.in_swz != b.out_swz && pd.K - b.u > 8)
+                return fail(LSG_E_ARG, "internal planning error: a relayout with several groups per thread");
+            const bool first = bi == pd.first_block, last = bi == pd.first_block + pd.nblocks - 1;
+            if ((first && b.in_swz) || (last && b.out_swz) || (b.generic && (b.in_swz || b.out_swz)))
+                return fail(LSG_E_ARG, "internal planning error: a swizzled layout at a pass boundary");
             covered += b.nops;
         }
         if (covered != pd.nops) return fail(LSG_E_ARG, "internal planning error: blocks do not cover the pass");
@@ -324,7 +351,7 @@ static int check_plan(const Plan& plan) {
 }
 
 int tile_bits_for(int nbits, int precision) {
-    int K = precision == LSG_C128 ? 10 : 11;
+    int K = precision == LSG_C128 ? 11 : 12;
     if (const char* env = getenv("LSG_TILE_BITS")) K = atoi(env);
     return std::max(0, std::min(K, nbits));
 }
@@ -382,16 +409,16 @@ namespace lsg {
 
 template <typename R>
 static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
-    auto kern = k_tile_pass<R>;
-    if (p->smem > 48 * 1024)
-        LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+    const size_t tile_bytes = sizeof(Cx<R>) << p->K;
+    const size_t meta = p->smem - tile_bytes;
+    const int L = p->plan.passes.empty() ? 0 : p->plan.passes[0].L;
+    const bool bulk = ((sizeof(Cx<R>) << L) % 16) == 0;
+    const bool pipe = bulk && getenv("LSG_NO_PIPELINE") == nullptr && 2 * tile_bytes + meta <= 200 * 1024;
     const int64_t tiles_per_member = 1ll << (s->nbits - p->K);
     const int64_t total = tiles_per_member * s->batch;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, p->smem);
-    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
     int* status = device_status();
     if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
     const PassDesc* pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
@@ -399,10 +426,29 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     const BlockDesc* blk_dev = reinterpret_cast<const BlockDesc*>(ops_dev + p->plan.ops.size());
     const Cx<R>* pool_dev =
         reinterpret_cast<const Cx<R>*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
-    for (size_t i = 0; i < p->plan.passes.size(); ++i) {
-        if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
-        kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(reinterpret_cast<Cx<R>*>(s->data), s->elems, pd_dev + i,
-                                                          ops_dev, blk_dev, pool_dev, tiles_per_member, total, status, ctx);
+    Cx<R>* state = reinterpret_cast<Cx<R>*>(s->data);
+    if (pipe) {
+        auto kern = k_tile_pipe<R>;
+        const size_t smem = 2 * tile_bytes + meta;
+        if (smem > 48 * 1024) LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPipeThreads, smem);
+        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
+        for (size_t i = 0; i < p->plan.passes.size(); ++i) {
+            if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
+            kern<<<(unsigned)grid, kPipeThreads, smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
+                                                                    tiles_per_member, total, status, ctx);
+        }
+    } else {
+        auto kern = k_tile_pass<R>;
+        if (p->smem > 48 * 1024)
+            LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, p->smem);
+        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
+        for (size_t i = 0; i < p->plan.passes.size(); ++i) {
+            if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
+            kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
+                                                              tiles_per_member, total, status, ctx);
+        }
     }
     if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
     LSG_CUDA(cudaGetLastError());
@@ -427,6 +473,25 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
     if (check_plan(p->plan) != LSG_OK) {
         delete p;
         return LSG_E_ARG;
+    }
+    // permutations with unit phases shared by all members are register renames
+    for (TileOp& t : p->plan.ops) {
+        if (t.kind != LSG_OP_PERM || t.stride != 0 || t.tmpl == kT_GENERIC) continue;
+        const int d = 1 << t.k;
+        bool unit = true;
+        int src[4] = {0, 0, 0, 0};
+        for (int r = 0; r < d && unit; ++r) {
+            unit = pool[2 * (t.data + r)] == 1.0 && pool[2 * (t.data + r) + 1] == 0.0;
+            src[r] = (int)pool[2 * (t.data + d + r)];
+        }
+        if (!unit) continue;
+        if (t.k == 1 && src[0] == 1 && src[1] == 0) t.tmpl = kT_X1 + t.pos[0];
+        if (t.k == 2) {
+            const int P0 = t.pos[0], P1 = t.pos[1];
+            if (src[0] == 0 && src[1] == 1 && src[2] == 3 && src[3] == 2) t.tmpl = kT_CX + 4 * P0 + P1;  // first controls
+            else if (src[0] == 0 && src[1] == 3 && src[2] == 2 && src[3] == 1) t.tmpl = kT_CX + 4 * P1 + P0;
+            else if (src[0] == 0 && src[1] == 2 && src[2] == 1 && src[3] == 3) t.tmpl = kT_SWAP + 4 * P0 + P1;
+        }
     }
     size_t max_meta = 0;
     for (const PassDesc& pd : p->plan.passes)

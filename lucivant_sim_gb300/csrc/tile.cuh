@@ -18,6 +18,27 @@ struct TrajCtx {
     const uint64_t* pred = nullptr;
 };
 
+// Threads that compute on a tile (the pipelined kernel adds a producer warp beyond them).
+constexpr int kCompute = 256;
+
+// Barrier over the 256 compute threads only (named barrier 1): the pipelined kernel's producer
+// warp never joins it. In the 256-thread kernel it spans the whole CTA.
+__device__ __forceinline__ void cbar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// The same barrier, returning whether any compute thread passed true.
+__device__ __forceinline__ bool cbar_or(bool v) {
+    uint32_t out;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, 256, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(out)
+        : "r"((uint32_t)v)
+        : "memory");
+    return out != 0;
+}
+
 // Deposit the bits of x into the register positions listed in pos[0..n) (ascending).
 __device__ __forceinline__ uint64_t deposit(uint64_t x, const int* pos, int n) {
     uint64_t out = 0;
@@ -41,7 +62,7 @@ template <typename R>
 __device__ __forceinline__ void dense1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
     const Cx<R> m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
     const int groups = 1 << (tbits - 1);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
         const Cx<R> a0 = t[i0], a1 = t[i1];
         t[i0] = cfma(m01, a1, cmul(m00, a0));
@@ -55,7 +76,7 @@ __device__ __forceinline__ void dense2(Cx<R>* t, int tbits, int b0, int b1, cons
     const int lo = min(b0, b1), hi = max(b0, b1);
     const uint32_t o1 = 1u << b1, o2 = 1u << b0;
     const int groups = 1 << (tbits - 2);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
         const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
 #pragma unroll
@@ -83,7 +104,7 @@ __device__ __forceinline__ void perm1(Cx<R>* t, int tbits, int b, const Cx<R>* m
     const Cx<R> p0 = m[0], p1 = m[1];
     const int s0 = (int)m[2].re;
     const int groups = 1 << (tbits - 1);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
         const Cx<R> a0 = t[i0], a1 = t[i1];
         t[i0] = cmul(p0, s0 ? a1 : a0);
@@ -98,7 +119,7 @@ __device__ __forceinline__ void perm2(Cx<R>* t, int tbits, int b0, int b1, const
     const Cx<R> p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
     const int s0 = (int)m[4].re, s1 = (int)m[5].re, s2 = (int)m[6].re, s3 = (int)m[7].re;
     const int groups = 1 << (tbits - 2);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
         const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
         t[base] = cmul(p0, pick4(v0, v1, v2, v3, s0));
@@ -122,7 +143,7 @@ __device__ __noinline__ void wide_op(Cx<R>* t, int tbits, int kind, int k, const
         offs[j] = o;
     }
     const int groups = 1 << (tbits - k);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         uint32_t base = (uint32_t)g;
         for (int i = 0; i < k; ++i) base = ins0(base, sorted[i]);
         for (int j = 0; j < D; ++j) v[j] = t[base | offs[j]];
@@ -141,7 +162,7 @@ __device__ __noinline__ void wide_op(Cx<R>* t, int tbits, int kind, int k, const
 template <typename R>
 __device__ __forceinline__ void op_diag(Cx<R>* tile, int tbits, int k, const int* lb, const Cx<R>* m) {
     const int n = 1 << tbits;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = threadIdx.x; i < n; i += kCompute) {
         int j = 0;
         for (int b = 0; b < k; ++b) j = (j << 1) | ((i >> lb[b]) & 1);
         tile[i] = cmul(m[j], tile[i]);
@@ -152,7 +173,7 @@ template <typename R>
 __device__ __forceinline__ void op_scale(Cx<R>* tile, int tbits, const Cx<R>* m) {
     const int n = 1 << tbits;
     const Cx<R> f = m[0];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) tile[i] = cmul(f, tile[i]);
+    for (int i = threadIdx.x; i < n; i += kCompute) tile[i] = cmul(f, tile[i]);
 }
 
 // (1-p) rho + (p/d) I (x) Tr_t(rho) on kq row bits then kq column bits (kq = 1 or 2).
@@ -171,7 +192,7 @@ __device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, con
     const R keep = R(1) - p;
     const R share = p / R(d);
     const int groups = 1 << (tbits - KB);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         uint32_t base = (uint32_t)g;
 #pragma unroll
         for (int i = 0; i < KB; ++i) base = ins0(base, srt[i]);
@@ -291,6 +312,44 @@ __device__ __forceinline__ void rb_perm2(Cx<R>* v, const Cx<R>* m) {
     }
 }
 
+// Unit-phase permutations are register renames: no arithmetic at all.
+template <typename R, int U, int P>
+__device__ __forceinline__ void rb_x(Cx<R>* v) {
+    constexpr int B = 1 << (U - 1 - P);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e)
+        if (!(e & B)) {
+            const Cx<R> t = v[e];
+            v[e] = v[e | B];
+            v[e | B] = t;
+        }
+}
+
+// controlled X: control at position PC, target at PT
+template <typename R, int U, int PC, int PT>
+__device__ __forceinline__ void rb_cx(Cx<R>* v) {
+    constexpr int BC = 1 << (U - 1 - PC), BT = 1 << (U - 1 - PT);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e)
+        if ((e & BC) && !(e & BT)) {
+            const Cx<R> t = v[e];
+            v[e] = v[e | BT];
+            v[e | BT] = t;
+        }
+}
+
+template <typename R, int U, int P0, int P1>
+__device__ __forceinline__ void rb_swap(Cx<R>* v) {
+    constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e)
+        if ((e & B0) && !(e & B1)) {
+            const Cx<R> t = v[e];
+            v[e] = v[(e & ~B0) | B1];
+            v[(e & ~B0) | B1] = t;
+        }
+}
+
 // (1-p) rho + (p/2) I Tr on one row bit (position PR) and its column bit (PC)
 template <typename R, int U, int PR, int PC>
 __device__ __forceinline__ void rb_depol1(Cx<R>* v, const Cx<R>* m) {
@@ -371,6 +430,20 @@ __device__ __forceinline__ const Cx<R>* mixture_pick(const TileOp& op, const Cx<
 #define LSG_P2ONE(X, BASE, A, B) \
     case BASE + 4 * A + B: if (U > A && U > B) X<R, U, (A < U ? A : 0), (B < U ? B : 0)>(v, m); break;
 
+#define LSG_R1(X, BASE)                                    \
+    case BASE + 0: if (U > 0) X<R, U, (0 < U ? 0 : 0)>(v); break; \
+    case BASE + 1: if (U > 1) X<R, U, (1 < U ? 1 : 0)>(v); break; \
+    case BASE + 2: if (U > 2) X<R, U, (2 < U ? 2 : 0)>(v); break; \
+    case BASE + 3: if (U > 3) X<R, U, (3 < U ? 3 : 0)>(v); break;
+
+#define LSG_R2ONE(X, BASE, A, B) \
+    case BASE + 4 * A + B: if (U > A && U > B) X<R, U, (A < U ? A : 0), (B < U ? B : 0)>(v); break;
+
+#define LSG_R2(X, BASE)                                                                                  \
+    LSG_R2ONE(X, BASE, 0, 1) LSG_R2ONE(X, BASE, 0, 2) LSG_R2ONE(X, BASE, 0, 3) LSG_R2ONE(X, BASE, 1, 0) \
+    LSG_R2ONE(X, BASE, 1, 2) LSG_R2ONE(X, BASE, 1, 3) LSG_R2ONE(X, BASE, 2, 0) LSG_R2ONE(X, BASE, 2, 1) \
+    LSG_R2ONE(X, BASE, 2, 3) LSG_R2ONE(X, BASE, 3, 0) LSG_R2ONE(X, BASE, 3, 1) LSG_R2ONE(X, BASE, 3, 2)
+
 #define LSG_P2(X, BASE)                                                                                  \
     LSG_P2ONE(X, BASE, 0, 1) LSG_P2ONE(X, BASE, 0, 2) LSG_P2ONE(X, BASE, 0, 3) LSG_P2ONE(X, BASE, 1, 0) \
     LSG_P2ONE(X, BASE, 1, 2) LSG_P2ONE(X, BASE, 1, 3) LSG_P2ONE(X, BASE, 2, 0) LSG_P2ONE(X, BASE, 2, 1) \
@@ -387,53 +460,88 @@ __device__ __forceinline__ void rb_apply(Cx<R>* v, int code, const TileOp& op, c
         case kT_DEPOL2:
             if (U == 4) rb_depol2<R>(v, m);
             break;
+        LSG_R1(rb_x, kT_X1)
+        LSG_R2(rb_cx, kT_CX)
+        LSG_R2(rb_swap, kT_SWAP)
         case kT_DIAG: rb_diag<R, U>(v, op, m); break;
         case kT_SCALE: rb_scale<R, U>(v, m); break;
         default: break;
     }
 }
 
-// one register block over the whole tile: each thread takes groups of 2^U amplitudes
+// Swizzled shared-memory position of tile element i: the bits above a 128-byte bank row are
+// folded into the bank bits by XOR, so the strided group accesses of a register block spread
+// over all banks. A bijection; the linear layout is kept for the bulk copies in and out.
+template <typename R>
+__device__ __forceinline__ uint32_t swz(uint32_t i) {
+    constexpr int SH = sizeof(R) == 4 ? 4 : 3;  // complex64: 16 per bank row, complex128: 8
+    constexpr uint32_t M = (1u << SH) - 1;
+    const uint32_t x = i >> SH;
+    return i ^ ((x ^ (x >> SH) ^ (x >> (2 * SH))) & M);
+}
+
+// One register block over the whole tile: each thread takes groups of 2^U amplitudes (the block's
+// U register bits), reads them in the block's input layout, applies the block's operators and
+// writes them in its output layout. A change of layout needs every read done before any write:
+// the host only asks for one when each thread has at most one group.
 template <typename R, int U>
 __device__ void run_block(Cx<R>* tile, int tbits, const BlockDesc& blk, const TileOp* __restrict__ ops,
                           const Cx<R>* __restrict__ data, int64_t member, uint64_t pred, const TrajCtx& ctx,
                           int64_t cur) {
-    uint32_t mask[4];
+    const bool sin = blk.in_swz != 0, sout = blk.out_swz != 0;
+    const bool relayout = sin != sout;
+    // the swizzle is linear over GF(2): position(base | bits) = position(base) ^ position(bits), so
+    // each element's offset is a fixed XOR of per-bit offsets, built once per block
+    uint32_t min_[4], mout[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) mask[i] = i < U ? (1u << blk.bits[i]) : 0u;
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t m = i < U ? (1u << blk.bits[i]) : 0u;
+        min_[i] = sin ? swz<R>(m) : m;
+        mout[i] = sout ? swz<R>(m) : m;
+    }
+    uint32_t oin[1 << U], oout[1 << U];
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        uint32_t a = 0, b = 0;
+#pragma unroll
+        for (int i = 0; i < U; ++i)
+            if ((e >> (U - 1 - i)) & 1) {
+                a ^= min_[i];
+                b ^= mout[i];
+            }
+        oin[e] = a;
+        oout[e] = b;
+    }
     const int groups = 1 << (tbits - U);
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    for (int g0 = 0; g0 < groups; g0 += kCompute) {
+        const int g = g0 + threadIdx.x;
+        const bool active = g < groups;
         uint32_t base = (uint32_t)g;
 #pragma unroll
         for (int i = 0; i < U; ++i) base = ins0(base, blk.sorted[i]);
+        const uint32_t bin = sin ? swz<R>(base) : base;
+        const uint32_t bout = sout ? swz<R>(base) : base;
         Cx<R> v[1 << U];
+        if (active) {
 #pragma unroll
-        for (int e = 0; e < (1 << U); ++e) {
-            uint32_t off = base;
-#pragma unroll
-            for (int i = 0; i < U; ++i)
-                if ((e >> (U - 1 - i)) & 1) off |= mask[i];
-            v[e] = tile[off];
-        }
-        for (int o = 0; o < blk.nops; ++o) {
-            const TileOp& op = ops[blk.first + o];
-            if (!((pred >> op.pred) & 1)) continue;
-            const Cx<R>* m = data + op.data + member * op.stride;
-            int code = op.tmpl;
-            if (op.kind == kOpMixture) {
-                m = mixture_pick<R>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
-                if (!m) continue;
-                code = (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2));
+            for (int e = 0; e < (1 << U); ++e) v[e] = tile[bin ^ oin[e]];
+            for (int o = 0; o < blk.nops; ++o) {
+                const TileOp& op = ops[blk.first + o];
+                if (!((pred >> op.pred) & 1)) continue;
+                const Cx<R>* m = data + op.data + member * op.stride;
+                int code = op.tmpl;
+                if (op.kind == kOpMixture) {
+                    m = mixture_pick<R>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
+                    if (!m) continue;
+                    code = (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2));
+                }
+                rb_apply<R, U>(v, code, op, m);
             }
-            rb_apply<R, U>(v, code, op, m);
         }
+        if (relayout) cbar();  // uniform: relayout blocks run exactly one round
+        if (active) {
 #pragma unroll
-        for (int e = 0; e < (1 << U); ++e) {
-            uint32_t off = base;
-#pragma unroll
-            for (int i = 0; i < U; ++i)
-                if ((e >> (U - 1 - i)) & 1) off |= mask[i];
-            tile[off] = v[e];
+            for (int e = 0; e < (1 << U); ++e) tile[bout ^ oout[e]] = v[e];
         }
     }
 }
@@ -448,7 +556,7 @@ __device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, 
         const int kind = op.kind, k = op.k;
         const Cx<R>* m = data + op.data + member * op.stride;
         if (!((pred >> op.pred) & 1)) continue;  // a branch this member did not take (CTA-uniform)
-        __syncthreads();
+        cbar();
         if (kind == kOpMixture) {
             op_mixture<R>(tile, tbits, op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
         } else if (kind == LSG_OP_MATRIX && k == 1) {
@@ -470,7 +578,150 @@ __device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, 
             wide_op<R>(tile, tbits, kind, k, op.lb, op.sorted, m);
         }
     }
+    cbar();
+}
+
+// All blocks of a pass on one tile (the 256 compute threads).
+template <typename R>
+__device__ __forceinline__ void compute_tile(Cx<R>* tile, int K, const PassDesc& pd, const BlockDesc* sblk,
+                                             const TileOp* sops, const Cx<R>* __restrict__ data, int64_t member,
+                                             const TrajCtx& ctx) {
+    const uint64_t pred = ctx.u ? ctx.pred[member] : ~0ull;
+    const int64_t cur = ctx.u ? ctx.cursor[member] : 0;
+    for (int bi = 0; bi < pd.nblocks; ++bi) {
+        const BlockDesc& blk = sblk[bi];
+        cbar();
+        if (blk.generic) {
+            run_ops<R>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
+            continue;
+        }
+        switch (blk.u) {
+            case 1: run_block<R, 1>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            case 2: run_block<R, 2>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            case 3: run_block<R, 3>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            default:
+                if constexpr (sizeof(R) == 4) run_block<R, 4>(tile, K, blk, sops, data, member, pred, ctx, cur);
+                break;
+        }
+    }
+    cbar();
+}
+
+template <typename R>
+__device__ __forceinline__ void stage_pass(const PassDesc* __restrict__ pass_g, const TileOp* __restrict__ ops,
+                                           const BlockDesc* __restrict__ blocks, TileOp* sops, BlockDesc* sblk) {
+    const int nops = pass_g->nops;
+    const int* src = reinterpret_cast<const int*>(ops + pass_g->first_op);
+    int* dst = reinterpret_cast<int*>(sops);
+    const int words = nops * (int)(sizeof(TileOp) / sizeof(int));
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    const int* bsrc = reinterpret_cast<const int*>(blocks + pass_g->first_block);
+    int* bdst = reinterpret_cast<int*>(sblk);
+    const int bwords = pass_g->nblocks * (int)(sizeof(BlockDesc) / sizeof(int));
+    for (int i = threadIdx.x; i < bwords; i += blockDim.x) bdst[i] = bsrc[i];
+}
+
+// Pipelined fused pass: warps 0-7 compute, warp 8 is the producer. The producer streams every
+// tile of this CTA through a two-buffer ring: bulk loads complete on full[b]; when the compute
+// warps have finished buffer b they arrive on empty[b]; the producer then bulk-stores it, waits
+// for the store to have read shared memory, and loads the CTA's next-but-one tile into it. Loads,
+// compute and stores of consecutive tiles overlap. Every wait is bounded.
+constexpr int kPipeThreads = 288;
+
+template <typename R>
+__global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict__ state, int64_t member_elems,
+                                                               const PassDesc* __restrict__ pass_g,
+                                                               const TileOp* __restrict__ ops,
+                                                               const BlockDesc* __restrict__ blocks,
+                                                               const Cx<R>* __restrict__ data, int64_t tiles_per_member,
+                                                               int64_t total_tiles, int* status, TrajCtx ctx) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t full[2], empty[2];
+    __shared__ PassDesc pd;
+    const size_t tile_bytes = sizeof(Cx<R>) << pass_g->K;
+    Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
+    Cx<R>* buf1 = reinterpret_cast<Cx<R>*>(smem_raw + tile_bytes);
+    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + 2 * tile_bytes);
+    BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
+    if (threadIdx.x == 0) pd = *pass_g;
+    stage_pass<R>(pass_g, ops, blocks, sops, sblk);
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], 256);
+        mbar_init(&empty[1], 256);
+        fence_mbar_init();
+    }
     __syncthreads();
+    const int K = pd.K, L = pd.L;
+    const int nchunks = 1 << (K - L);
+    const uint32_t chunk_bytes = (uint32_t)(sizeof(Cx<R>) << L);
+    const int64_t stride = gridDim.x;
+    if (threadIdx.x >= 256) {
+        // ---------------- producer warp
+        const int lane = threadIdx.x - 256;
+        auto tile_at = [&](int64_t t, Cx<R>** mem, uint64_t* base) {
+            const int64_t member = t / tiles_per_member;
+            const uint64_t tt = (uint64_t)(t - member * tiles_per_member);
+            *mem = state + member * member_elems;
+            *base = deposit(tt, pd.outer, pd.nouter);
+        };
+        auto store = [&](int64_t t, Cx<R>* buf) {
+            Cx<R>* mem;
+            uint64_t base;
+            tile_at(t, &mem, &base);
+            for (int c = lane; c < nchunks; c += 32)
+                bulk_s2g(mem + (base | deposit((uint64_t)c, pd.hi, K - L)), buf + ((size_t)c << L), chunk_bytes);
+            bulk_commit();
+            bulk_wait_read();
+            __syncwarp();
+        };
+        int64_t it = 0;
+        for (int64_t t = blockIdx.x; t < total_tiles; t += stride, ++it) {
+            const int b = (int)(it & 1);
+            Cx<R>* buf = b ? buf1 : buf0;
+            if (it >= 2) {  // buffer b still holds tile it-2: wait for its compute, store it
+                const bool ok = mbar_wait_bounded(&empty[b], (uint32_t)(((it >> 1) - 1) & 1), status);
+                if (!ok) {
+                    bulk_wait_all();  // our own stores in flight, then leave
+                    return;
+                }
+                store(t - 2 * stride, buf);
+            }
+            Cx<R>* mem;
+            uint64_t base;
+            tile_at(t, &mem, &base);
+            if (lane == 0) mbar_arrive_expect_tx(&full[b], chunk_bytes * (uint32_t)nchunks);
+            __syncwarp();
+            for (int c = lane; c < nchunks; c += 32)
+                bulk_g2s(buf + ((size_t)c << L), mem + (base | deposit((uint64_t)c, pd.hi, K - L)), chunk_bytes, &full[b]);
+        }
+        // the last one or two tiles
+        const int64_t n_it = it;
+        for (int64_t j = (n_it >= 2 ? n_it - 2 : 0); j < n_it; ++j) {
+            const int b = (int)(j & 1);
+            const bool ok = mbar_wait_bounded(&empty[b], (uint32_t)((j >> 1) & 1), status);
+            if (!ok) {
+                bulk_wait_all();
+                return;
+            }
+            store(blockIdx.x + j * stride, b ? buf1 : buf0);
+        }
+        bulk_wait_all();
+        return;
+    }
+    // ---------------- compute warps
+    int64_t it = 0;
+    for (int64_t t = blockIdx.x; t < total_tiles; t += stride, ++it) {
+        const int b = (int)(it & 1);
+        Cx<R>* tile = b ? buf1 : buf0;
+        const bool ok = mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), status);
+        if (cbar_or(!ok)) return;  // every compute thread leaves together on a timeout
+        const int64_t member = t / tiles_per_member;
+        compute_tile<R>(tile, K, pd, sblk, sops, data, member, ctx);
+        fence_proxy_async_smem();  // this thread's writes, before the producer's bulk store reads them
+        mbar_arrive(&empty[b]);
+    }
 }
 
 // One fused pass over every tile of every member. Tiles are visited grid-stride; each CTA
@@ -535,27 +786,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_tile_pass(Cx<R>
             }
         }
         // ---- compute: register blocks, or one shared-memory operator for a wide block
-        {
-            const uint64_t pred = ctx.u ? ctx.pred[member] : ~0ull;
-            const int64_t cur = ctx.u ? ctx.cursor[member] : 0;
-            for (int bi = 0; bi < pd.nblocks; ++bi) {
-                const BlockDesc& blk = sblk[bi];
-                __syncthreads();
-                if (blk.generic) {
-                    run_ops<R>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
-                    continue;
-                }
-                switch (blk.u) {
-                    case 1: run_block<R, 1>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-                    case 2: run_block<R, 2>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-                    case 3: run_block<R, 3>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-                    default:
-                        if constexpr (sizeof(R) == 4) run_block<R, 4>(tile, K, blk, sops, data, member, pred, ctx, cur);
-                        break;
-                }
-            }
-            __syncthreads();
-        }
+        __syncthreads();
+        compute_tile<R>(tile, K, pd, sblk, sops, data, member, ctx);
+        __syncthreads();
         // ---- store
         if (use_bulk) {
             fence_proxy_async_smem();

@@ -189,3 +189,28 @@ def test_capacity_errors():
         ls.statevector("OPENQASM 3; qubit[27] q; h q[0];")
     with pytest.raises(ls.SimulationError, match="up to 13"):
         ls.density_matrix("OPENQASM 3; qubit[14] q; h q[0];", NoiseModel.uniform(single=0.01))
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64"])
+@pytest.mark.parametrize("tile", [None, "13"])
+def test_wide_operators_on_large_tiles(precision, tile, monkeypatch):
+    """Operators wider than a register block (c3x, c4x, ccz, rccx, two-qubit Kraus channels) run
+    through the shared-memory path on tiles with more groups than compute threads."""
+    if tile:
+        monkeypatch.setenv("LSG_TILE_BITS", tile)
+    src = ("OPENQASM 3; include \"stdgates.inc\"; qubit[14] q;"
+           + "".join(f"u3({0.3 + 0.1 * i}, {0.2 * i}, {0.7 - 0.05 * i}) q[{i}];" for i in range(14))
+           + "ccx q[0], q[7], q[13]; c3x q[1], q[5], q[9], q[12]; c4x q[13], q[2], q[4], q[6], q[8];"
+           + "ccz q[3], q[10], q[11]; rccx q[12], q[0], q[6]; cswap q[2], q[9], q[1]; cx q[13], q[0];")
+    c = ls.parse(src)
+    want = dense.evolve_sv(c)
+    got = ls.statevector(c, precision=precision)
+    tol = ATOL_C128 if precision == "c128" else 1e-5
+    assert np.max(np.abs(got - want)) < tol
+    dm_src = ("OPENQASM 3; include \"stdgates.inc\"; qubit[6] q;"
+              + "".join(f"ry({0.4 + 0.3 * i}) q[{i}]; cx q[{i}], q[{(i + 1) % 6}];" for i in range(6)))
+    noise = NoiseModel().add_gate_error(nz.pauli_channel({"XY": 0.05, "ZX": 0.03, "YY": 0.02}), gates="cx")
+    cd = ls.parse(dm_src)
+    want = dense.evolve_dm(cd, noise).reshape(64, 64)
+    got = ls.density_matrix(cd, noise, precision=precision)
+    assert np.max(np.abs(got - want)) < tol
