@@ -50,6 +50,10 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--precision", choices=("c64", "c128"), default="c64")
     ap.add_argument("--instances", type=int, default=INSTANCES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=("dm-batch", "serve"), default="dm-batch",
+                    help="dm-batch: the batched density-matrix step (default); serve: the served mix")
+    ap.add_argument("--jobs", type=int, default=400, help="serve: jobs in the served mix")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: offered arrivals per second")
     return ap.parse_args()
 
 
@@ -165,13 +169,18 @@ def bytes_per_instance(circuit, noises, precision: str) -> tuple[int, int]:
     from lucivant_sim_gb300 import _lib, engine
 
     code = engine.precision_code(precision)
-    ops = engine.dm_oplist(circuit, noises[:1])
+    if engine.dm_form(circuit, noises[:1]) == "ptm":
+        code = engine.REAL_OF[code]
+        ops = engine.ptm_oplist(circuit, noises[:1])
+        reads = (1 << QUBITS) + 23  # the diagonal Paulis (probabilities), one coefficient per Z term
+    else:
+        ops = engine.dm_oplist(circuit, noises[:1])
+        reads = 24 << QUBITS  # the diagonal, read by probabilities and by each of the 23 Z terms
     passes = _lib.plan_passes(2 * QUBITS, code, ops)
-    elt = 8 if precision == "c64" else 16
+    elt = _lib.ELEM_BYTES[code]
     member = elt << (2 * QUBITS)
-    diag = (1 << QUBITS) * elt
-    # 2 x member per pass, 1 x member to reset, the diagonal read by probabilities and 23 Z terms
-    return 2 * member * passes + member + 24 * diag, passes
+    # 2 x member per pass, 1 x member to reset, and the reduction reads
+    return 2 * member * passes + member + reads * elt, passes
 
 
 # ------------------------------------------------------------------------------ CPU legs
@@ -335,6 +344,10 @@ def gb300_arm(args: argparse.Namespace) -> None:
 
     batch = DensityBatch(circuit, noises, precision=args.precision)
     assert batch.program.passes == passes
+    form, upload_bytes, reg_bytes = batch.form, batch.upload_bytes, batch.register_bytes
+    real = batch.reg.real
+    kernel = f"k_tile_pipe<{'float' if args.precision == 'c64' else 'double'}>" if real else \
+        f"k_tile_pipe<Cx<{'float' if args.precision == 'c64' else 'double'}>>"
     stream = torch.cuda.ExternalStream(batch.reg.stream())
 
     def step(timed: list | None = None) -> tuple:
@@ -374,7 +387,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     achieved = launch_bytes / avg_launch_s / 1e9
     traffic = ncu_traffic(args.precision)
     roofline = {
-        "kernel": f"k_tile_pass<{'float' if args.precision == 'c64' else 'double'}>",
+        "kernel": kernel,
         "bound": "hbm",
         "achieved": achieved,
         "peak": peak,
@@ -417,8 +430,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
     from lucivant_sim_gb300 import engine
 
-    ops = engine.dm_oplist(circuit, noises)
-    h2d = int(ops.size * 16 + len(ops) * _lib.OP_DTYPE.itemsize + 2 * 8 * len(labels))
+    h2d = int(upload_bytes + 2 * 8 * len(labels))  # operator table and data pool, Pauli masks
     d2h = int(probs_h.nbytes + exps_h.nbytes)
 
     if rank == 0:
@@ -433,9 +445,9 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": args.precision,
+            "dtype": ("f32" if args.precision == "c64" else "f64") if real else args.precision,
             "data": "synthetic",
-            "config": config_block(args),
+            "config": dict(config_block(args), form=form, l2=f"register {reg_bytes / 2**30:.0f} GiB > L2: no flush"),
             "circuits_per_s": cps,
             "fused_passes": passes,
             "plain_c128": {
@@ -462,10 +474,103 @@ def gb300_arm(args: argparse.Namespace) -> None:
     dist.close()
 
 
+# ------------------------------------------------------------------------------ served mix
+
+
+def _circuits(job: dict) -> int:
+    return len(job["params"]) if job["kind"] == "expect" else 1
+
+
+def _plain_c128(job: dict):
+    """One job through the direct API at complex128, one circuit at a time."""
+    import lucivant_sim_gb300 as ls
+    from lucivant_sim_gb300 import serve
+
+    if job["kind"] == "expect":
+        return [ls.expectation(ls.parse(job["qasm"], p), job["observable"], precision="c128") for p in job["params"]]
+    noise = ls.NoiseModel.uniform(**serve.DEFAULT_NOISE) if job["kind"] == "density" else None
+    return ls.run(job["qasm"], shots=job["shots"], seed=job["seed"], noise=noise, precision="c128").counts
+
+
+def serve_arm(args: argparse.Namespace) -> None:
+    """The served mix on one GPU: offered at ``--rate`` jobs/s for p50/p99 latency, then all at
+    once for throughput; the same jobs run one at a time through the direct complex128 API for
+    the plain rate, and the complex64 results are checked against complex128."""
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    import numpy as np
+
+    import lucivant_sim_gb300 as ls
+    from lucivant_sim_gb300 import _lib, serve, workloads as wl
+
+    _lib.set_device(local)
+    jobs = wl.served_mix(args.jobs, rate=args.rate, seed=5)
+    warm = wl.served_mix(max(args.warmup, 3) * 8, rate=args.rate, seed=99)
+    circuits = sum(_circuits(j) for j in jobs)
+    with serve.Server(precision=args.precision) as srv:
+        serve.replay(warm, srv, realtime=False)
+        clocks = Clocks(local)
+        clocks.start()
+        offered = serve.replay(jobs, srv, realtime=True)
+        burst = serve.replay(jobs, srv, realtime=False)
+        clock_info = clocks.stop()
+    # plain complex128, one job at a time, on a bounded prefix of the same mix
+    sample = jobs[: max(8, min(len(jobs), 60))]
+    _plain_c128(sample[0])
+    t0 = time.perf_counter()
+    plain = [_plain_c128(j) for j in sample]
+    plain_s = time.perf_counter() - t0
+    plain_cps = sum(_circuits(j) for j in sample) / plain_s
+    # complex64 accuracy against complex128 on the prefix
+    tvd, exp_err, same_counts = 0.0, 0.0, 0
+    for job, res, ref in zip(sample, burst["results"], plain, strict=False):
+        if job["kind"] == "expect":
+            exp_err = max(exp_err, float(np.max(np.abs(np.asarray(res["values"]) - np.asarray(ref)))))
+        else:
+            same_counts += int(res["counts"] == ref)
+            if job["kind"] == "sample" and job["width"] <= 20:
+                c = ls.parse(job["qasm"])
+                p64 = ls.probabilities_array(c, precision="c64")
+                p128 = ls.probabilities_array(c, precision="c128")
+                tvd = max(tvd, 0.5 * float(np.abs(p64 - p128).sum()))
+    cps = circuits / burst["elapsed_s"]
+    line = {
+        "metric": "served circuits/s",
+        "value": cps,
+        "unit": "circuits/s",
+        "n_gpus": 1,
+        "steps": 1,
+        "warmup": len(warm),
+        "ms_per_step": 1000 * burst["elapsed_s"],
+        "higher_is_better": True,
+        "scaling": "replicas only",
+        "vs_baseline": None,
+        "dtype": args.precision,
+        "data": "synthetic",
+        "config": {
+            "workload": f"served mix: {args.jobs} jobs ({circuits} circuits), widths 8..26, depths 10..100, "
+            "30% 8-point HEA sweeps with 20-term Pauli sums, 20% noisy density matrices, 50% sampled (1000 shots)",
+            "precision": args.precision,
+            "offered_rate_jobs_per_s": args.rate,
+        },
+        "latency_at_offered_rate": {"p50_s": offered["p50_s"], "p99_s": offered["p99_s"],
+                                    "circuits_per_s": circuits / offered["elapsed_s"]},  # fmt: skip
+        "latency_all_at_once": {"p50_s": burst["p50_s"], "p99_s": burst["p99_s"]},
+        "plain_c128": {"circuits_per_s": plain_cps, "jobs_timed": len(sample), "speedup_of_served": cps / plain_cps},
+        "accuracy": {"max_probability_tvd_vs_c128": tvd, "max_expectation_error_vs_c128": exp_err,
+                     "counts_identical_to_c128": f"{same_counts} of {sum(j['kind'] != 'expect' for j in sample)}"},  # fmt: skip
+        "clocks": clock_info,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "serve":
+        serve_arm(args)
     else:
         gb300_arm(args)
 

@@ -33,6 +33,14 @@ extern "C" {
 /* precisions */
 #define LSG_C128 0 /* complex128 amplitudes, FP64 arithmetic */
 #define LSG_C64 1  /* complex64 amplitudes, FP32 arithmetic; reductions stay FP64 */
+/* Real registers hold density matrices in Pauli-transfer form: a register of 2n bits holds the
+ * 4^n real coefficients r_P = Tr(P rho) of an n-qubit density matrix, qubit q's Pauli digit in
+ * register bits (n+q, q) = (x, z): I = (0,0), Z = (0,1), X = (1,0), Y = (1,1). Channels act on
+ * them as real matrices (Pauli transfer matrices) through the same operator kinds (MATRIX, DIAG,
+ * PERM, SCALE; pool entries must be real). Reductions with dm_qubits = n read them as the density
+ * matrix they stand for. */
+#define LSG_R64 2 /* real FP64 coefficients */
+#define LSG_R32 3 /* real FP32 coefficients; reductions stay FP64 */
 
 /* operator kinds for lsg_apply */
 #define LSG_OP_MATRIX 0 /* dense 2^k x 2^k complex matrix, row-major, on bits[0..k), k <= 5 */
@@ -62,6 +70,8 @@ int lsg_version(void);
 int lsg_init(int device);
 /* Largest register a state handle accepts, in bits (26: 2^26 amplitudes). */
 int lsg_max_bits(void);
+/* Free and total device memory of the calling thread's device (admission control). */
+int lsg_mem_info(int64_t* free_bytes, int64_t* total_bytes);
 
 /* ---- registers ------------------------------------------------------------------------------
  * A register holds `batch` independent members of 2^nbits amplitudes each, contiguous in HBM.
@@ -71,9 +81,15 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out);
 int lsg_state_free(lsg_state s);
 /* Every member set to the basis state |index>. */
 int lsg_state_set_basis(lsg_state s, int64_t index);
-/* Copy all members in / out as complex128 (converted when the register is complex64). */
+/* Copy all members in / out as complex128 (converted when the register is complex64), or as
+ * float64 for a real register. A real register's basis state `index` is |index><index| of its
+ * nbits/2 qubits, in Pauli-transfer form. */
 int lsg_state_upload(lsg_state s, const double* host_c128, int64_t nbytes);
 int lsg_state_download(lsg_state s, double* host_c128, int64_t nbytes);
+/* Member `member` of a real (Pauli-transfer) register copied into member 0 of a complex register
+ * of the same bits, as real amplitudes: applying the per-qubit change of basis to the complex
+ * register then yields the density matrix. Not in Orrery (its density matrices are complex). */
+int lsg_state_to_complex(lsg_state src, int64_t member, lsg_state dst);
 /* Bytes of device memory the handle holds. */
 int lsg_state_bytes(lsg_state s, int64_t* out);
 

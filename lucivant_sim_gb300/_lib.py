@@ -19,6 +19,8 @@ LIB_PATH = Path(__file__).resolve().parent / "liblsg.so"
 
 LSG_OK, LSG_E_ARG, LSG_E_CAPACITY, LSG_E_MEMORY, LSG_E_CUDA, LSG_E_TIMEOUT, LSG_E_STATE = 0, -1, -2, -3, -4, -5, -6
 C128, C64 = 0, 1
+R64, R32 = 2, 3  # real registers: density matrices in Pauli-transfer form
+ELEM_BYTES = {C128: 16, C64: 8, R64: 8, R32: 4}
 OP_MATRIX, OP_DIAG, OP_PERM, OP_DEPOL, OP_SCALE = 0, 1, 2, 3, 4
 MAX_OP_BITS = 8
 
@@ -51,12 +53,14 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_version": (C.c_int, []),
     "lsg_init": (C.c_int, [C.c_int]),
     "lsg_max_bits": (C.c_int, []),
+    "lsg_mem_info": (C.c_int, [_PI64, _PI64]),
     "lsg_state_create": (C.c_int, [C.c_int, C.c_int, _I64, C.POINTER(_P)]),
     "lsg_state_free": (C.c_int, [_P]),
     "lsg_state_set_basis": (C.c_int, [_P, _I64]),
     "lsg_state_upload": (C.c_int, [_P, _PD, _I64]),
     "lsg_state_download": (C.c_int, [_P, _PD, _I64]),
     "lsg_state_bytes": (C.c_int, [_P, _PI64]),
+    "lsg_state_to_complex": (C.c_int, [_P, _I64, _P]),
     "lsg_apply": (C.c_int, [_P, _P, _I32, _PD, _I64]),
     "lsg_probabilities": (C.c_int, [_P, C.c_int, _I64, _PD]),
     "lsg_sample": (C.c_int, [_P, C.c_int, _I64, _PI32, _I32, _PD, _I64, _I32, _PI32, _PI32, _PD, _PD, _PD, _PU8, _PU8, _PI64]),
@@ -75,7 +79,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
 
 _lib: C.CDLL | None = None
 _lock = threading.Lock()
-_initialised: set[int] = set()
+_tls = threading.local()  # the CUDA current device is per thread: bind each thread once
 _default_device = 0
 
 
@@ -83,7 +87,7 @@ def set_device(device: int) -> None:
     """The device new registers go to (one process drives one GPU; ranks pick theirs)."""
     global _default_device
     _default_device = int(device)
-    _initialised.discard(_default_device)
+    _tls.device = None
     ensure_device(_default_device)
 
 
@@ -123,10 +127,17 @@ def check(code: int) -> None:
 
 def ensure_device(device: int | None = None) -> None:
     dev = _default_device if device is None else device
-    if dev not in _initialised:
+    if getattr(_tls, "device", None) != dev:
         check(library().lsg_init(dev))
-        _initialised.clear()
-        _initialised.add(dev)
+        _tls.device = dev
+
+
+def mem_info() -> tuple[int, int]:
+    """(free, total) bytes of this thread's device."""
+    ensure_device()
+    f, t = C.c_int64(0), C.c_int64(0)
+    check(library().lsg_mem_info(C.byref(f), C.byref(t)))
+    return int(f.value), int(t.value)
 
 
 def plan_passes(nbits: int, precision: int, ops: "OpList") -> int:
@@ -217,14 +228,24 @@ class Register:
         table, pool = ops.packed()
         check(self.lib.lsg_apply(self.handle, table.ctypes.data, len(table), ptr(pool, C.c_double), pool.size // 2))
 
+    @property
+    def real(self) -> bool:
+        """A Pauli-transfer (real) density register."""
+        return self.precision in (R64, R32)
+
     def download(self) -> np.ndarray:
-        out = np.empty(self.batch << self.nbits, dtype=np.complex128)
+        """(batch, 2^nbits) complex128 amplitudes, or float64 coefficients of a real register."""
+        out = np.empty(self.batch << self.nbits, dtype=np.float64 if self.real else np.complex128)
         check(self.lib.lsg_state_download(self.handle, ptr(out.view(np.float64), C.c_double), out.nbytes))
         return out.reshape(self.batch, -1)
 
     def upload(self, data: np.ndarray) -> None:
-        a = np.ascontiguousarray(data, dtype=np.complex128).reshape(-1)
+        a = np.ascontiguousarray(data, dtype=np.float64 if self.real else np.complex128).reshape(-1)
         check(self.lib.lsg_state_upload(self.handle, ptr(a.view(np.float64), C.c_double), a.nbytes))
+
+    def to_complex(self, member: int, out: Register) -> None:
+        """Member ``member`` of this real register into member 0 of complex register ``out``."""
+        check(self.lib.lsg_state_to_complex(self.handle, member, out.handle))
 
     def probabilities(self, dm_qubits: int = 0, member: int = 0) -> np.ndarray:
         """One member's probabilities, or every member's (shape (batch, 2^n)) when member < 0."""

@@ -26,14 +26,20 @@ class DensityBatch:
         self.circuit = circuit
         self.n = circuit.num_qubits
         self.batch = len(noises)
-        self.reg = engine.new_density(self.n, engine.precision_code(precision), self.batch)
-        self.ops = engine.dm_oplist(circuit, noises)
+        prec = engine.precision_code(precision)
+        self.form = engine.dm_form(circuit, noises)
+        if self.form == "ptm":  # Pauli-transfer form: real coefficients, real channel matrices
+            self.reg = engine.new_density(self.n, engine.REAL_OF[prec], self.batch)
+            self.ops = engine.ptm_oplist(circuit, noises)
+        else:
+            self.reg = engine.new_density(self.n, prec, self.batch)
+            self.ops = engine.dm_oplist(circuit, noises)
         self.program = _lib.Program(self.reg, self.ops)
         self.upload_bytes = int(self.ops.size * 16 + len(self.ops) * _lib.OP_DTYPE.itemsize)
 
     @property
     def register_bytes(self) -> int:
-        return (8 if self.reg.precision == _lib.C64 else 16) * self.batch << (2 * self.n)
+        return _lib.ELEM_BYTES[self.reg.precision] * self.batch << (2 * self.n)
 
     def evolve(self) -> None:
         """Reset every member to |0><0| and run the circuit (queued; returns before completion)."""

@@ -46,15 +46,23 @@ constexpr int kMaxBits = 26;  // 2^26 amplitudes per member (Orrery's statevecto
 
 // ---------------------------------------------------------------- register handle
 
+// A device buffer that grows on demand. With a stream it is stream-ordered (cudaMallocAsync /
+// cudaFreeAsync): no device-wide synchronisation, so independent registers keep overlapping.
 struct Scratch {
     void* ptr = nullptr;
     size_t bytes = 0;
+    cudaStream_t stream = nullptr;
 };
 
 int ensure(Scratch& s, size_t bytes);
 void release(Scratch& s);
 
 }  // namespace lsg
+
+// Bytes per register element: complex128 16, complex64 8, real64 8, real32 4.
+inline size_t lsg_elem_bytes(int precision) {
+    return precision == LSG_C128 ? 16 : precision == LSG_R32 ? 4 : 8;
+}
 
 struct lsg_state_s {
     int nbits = 0;
@@ -66,7 +74,8 @@ struct lsg_state_s {
     lsg::Scratch program;  // uploaded pass programs
     lsg::Scratch scratch;  // reduction partials, CDFs, sampling buffers
     lsg::Scratch scratch2;
-    size_t elem_bytes() const { return precision == LSG_C128 ? 16 : 8; }
+    size_t elem_bytes() const { return lsg_elem_bytes(precision); }
+    bool real() const { return precision == LSG_R64 || precision == LSG_R32; }
     size_t member_bytes() const { return elem_bytes() * (size_t)elems; }
 };
 
@@ -105,6 +114,37 @@ __device__ __forceinline__ Cx<R> cfma(Cx<R> a, Cx<R> b, Cx<R> acc) {
     acc.im = fma(a.im, b.re, acc.im);
     return acc;
 }
+
+// The same operations on real elements (Pauli-transfer registers), so the tile code is written
+// once for an element type T: Cx<float>, Cx<double>, float or double.
+__device__ __forceinline__ float cmul(float a, float b) { return a * b; }
+__device__ __forceinline__ double cmul(double a, double b) { return a * b; }
+__device__ __forceinline__ float cfma(float a, float b, float acc) { return fmaf(a, b, acc); }
+__device__ __forceinline__ double cfma(double a, double b, double acc) { return fma(a, b, acc); }
+
+template <typename T>
+struct Elem {  // complex elements
+    using R = decltype(T::re);
+    static constexpr bool complex = true;
+};
+template <>
+struct Elem<float> {
+    using R = float;
+    static constexpr bool complex = false;
+};
+template <>
+struct Elem<double> {
+    using R = double;
+    static constexpr bool complex = false;
+};
+
+// real part (a real element is its own)
+template <typename R>
+__host__ __device__ __forceinline__ R re_of(Cx<R> a) {
+    return a.re;
+}
+__host__ __device__ __forceinline__ float re_of(float a) { return a; }
+__host__ __device__ __forceinline__ double re_of(double a) { return a; }
 
 // Insert zero bits at the (ascending) positions in `pos` into x: spreads x over the other bits.
 __device__ __forceinline__ uint64_t spread(uint64_t x, const int* pos, int k) {

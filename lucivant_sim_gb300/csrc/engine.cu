@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <set>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -67,17 +69,19 @@ int check_device_status(cudaStream_t stream) {
 
 int ensure(Scratch& s, size_t bytes) {
     if (s.bytes >= bytes) return LSG_OK;
-    if (s.ptr) cudaFree(s.ptr);
-    s.ptr = nullptr;
-    s.bytes = 0;
+    release(s);
     size_t want = std::max<size_t>(bytes, 4096);
-    LSG_CUDA(cudaMalloc(&s.ptr, want));
+    if (s.stream) LSG_CUDA(cudaMallocAsync(&s.ptr, want, s.stream));
+    else LSG_CUDA(cudaMalloc(&s.ptr, want));
     s.bytes = want;
     return LSG_OK;
 }
 
 void release(Scratch& s) {
-    if (s.ptr) cudaFree(s.ptr);
+    if (s.ptr) {
+        if (s.stream) cudaFreeAsync(s.ptr, s.stream);
+        else cudaFree(s.ptr);
+    }
     s.ptr = nullptr;
     s.bytes = 0;
 }
@@ -223,9 +227,13 @@ static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
     }
 }
 
+// Operators per pass at most: their descriptors are staged in shared memory beside the tile
+// (192 x 136 B + blocks stays under 40 KB, so two pipelined CTAs still share an SM).
+constexpr int kMaxPassOps = 192;
+
 // Greedy fusion: sweep the remaining operators; an operator joins the current pass when its bits
-// fit the tile and no operator deferred earlier in the sweep shares a bit with it (so program
-// order is kept wherever it matters). Deferred operators start the next sweep.
+// fit the tile, the pass has room, and no operator deferred earlier in the sweep shares a bit with
+// it (so program order is kept wherever it matters). Deferred operators start the next sweep.
 Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* pred, const int* draw,
               const int* count, int umax) {
     Plan plan;
@@ -240,7 +248,7 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
             const lsg_op& op = ops[idx];
             uint64_t mask = 0;
             for (int i = 0; i < op.nbits; ++i) mask |= 1ull << op.bits[i];
-            if (mask & blocked) {
+            if ((mask & blocked) || (int)taken.size() >= kMaxPassOps) {
                 deferred.push_back(idx);
                 blocked |= mask;
                 continue;
@@ -307,11 +315,12 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
     return plan;
 }
 
-// Widest register block per precision: 16 complex64 or 8 complex128 amplitudes per thread.
+// Widest register block: 16 elements per thread for 4- and 8-byte elements, 8 complex128.
 int block_bits_for(int precision) {
-    int u = precision == LSG_C128 ? 3 : 4;
+    const int top = lsg_elem_bytes(precision) == 16 ? 3 : 4;
+    int u = top;
     if (const char* env = getenv("LSG_BLOCK_BITS")) u = atoi(env);
-    return std::max(0, std::min(u, precision == LSG_C128 ? 3 : 4));
+    return std::max(0, std::min(u, top));
 }
 
 static Plan plan_passes(const lsg_op* ops, int nops, int nbits, int K, int L, int umax) {
@@ -350,23 +359,34 @@ static int check_plan(const Plan& plan) {
     return LSG_OK;
 }
 
+// Tile bits: 32 KB tiles of complex64 or real64 (2^12), 2^11 complex128, 2^13 real32.
 int tile_bits_for(int nbits, int precision) {
-    int K = precision == LSG_C128 ? 11 : 12;
+    const size_t eb = lsg_elem_bytes(precision);
+    int K = eb == 16 ? 11 : eb == 8 ? 12 : 13;
     if (const char* env = getenv("LSG_TILE_BITS")) K = atoi(env);
     return std::max(0, std::min(K, nbits));
 }
 
-// Register bits every tile keeps: 2^L contiguous amplitudes = 512 bytes per copy.
+// Register bits every tile keeps: 2^L contiguous elements, 512 bytes per copy (256 for real32).
 int low_bits_for(int nbits, int precision) {
-    int L = precision == LSG_C128 ? 5 : 6;
+    const size_t eb = lsg_elem_bytes(precision);
+    int L = eb == 16 ? 5 : 6;
     if (const char* env = getenv("LSG_LOW_BITS")) L = atoi(env);
     return std::max(0, std::min(L, nbits));
 }
 
-static int validate_ops(int nbits, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
-                        int64_t pool_entries) {
+static int validate_ops(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
+                        const double* pool, int64_t pool_entries) {
     if (nops < 0 || (nops > 0 && !ops) || pool_entries < 0 || (pool_entries > 0 && !pool))
         return fail(LSG_E_ARG, "bad operator list or pool");
+    const bool real = precision == LSG_R64 || precision == LSG_R32;
+    if (real) {  // Pauli-transfer registers: real matrices only, channels already in transfer form
+        for (int i = 0; i < nops; ++i)
+            if (ops[i].kind == LSG_OP_DEPOL)
+                return fail(LSG_E_ARG, "operator %d: a real register takes depolarising channels as DIAG operators", i);
+        for (int64_t i = 0; i < pool_entries; ++i)
+            if (pool[2 * i + 1] != 0.0) return fail(LSG_E_ARG, "a real register takes real operator data only");
+    }
     for (int i = 0; i < nops; ++i) {
         const lsg_op& op = ops[i];
         if (!op_bits_ok(op, nbits)) return fail(LSG_E_ARG, "operator %d has a bad kind or bits", i);
@@ -407,12 +427,34 @@ struct lsg_program_s {
 
 namespace lsg {
 
-template <typename R>
+// Let a kernel take all the dynamic shared memory the device allows, once per kernel and
+// device (the attribute is global to the function: setting it per launch would race between
+// threads launching the same kernel with different sizes).
+static std::mutex g_smem_mu;
+static std::set<std::pair<const void*, int>> g_smem_done;  // (kernel, device) pairs already raised
+
+template <typename K>
+static int allow_smem(K kern) {
+    int dev = 0;
+    LSG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_smem_mu);
+    const auto key = std::make_pair(reinterpret_cast<const void*>(kern), dev);
+    if (g_smem_done.count(key)) return LSG_OK;
+    int optin = 0;
+    LSG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa{};
+    LSG_CUDA(cudaFuncGetAttributes(&fa, kern));
+    LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    g_smem_done.insert(key);
+    return LSG_OK;
+}
+
+template <typename T>
 static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
-    const size_t tile_bytes = sizeof(Cx<R>) << p->K;
+    const size_t tile_bytes = sizeof(T) << p->K;
     const size_t meta = p->smem - tile_bytes;
     const int L = p->plan.passes.empty() ? 0 : p->plan.passes[0].L;
-    const bool bulk = ((sizeof(Cx<R>) << L) % 16) == 0;
+    const bool bulk = ((sizeof(T) << L) % 16) == 0;
     const bool pipe = bulk && getenv("LSG_NO_PIPELINE") == nullptr && 2 * tile_bytes + meta <= 200 * 1024;
     const int64_t tiles_per_member = 1ll << (s->nbits - p->K);
     const int64_t total = tiles_per_member * s->batch;
@@ -424,13 +466,12 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     const PassDesc* pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
     const TileOp* ops_dev = reinterpret_cast<const TileOp*>(pd_dev + p->plan.passes.size());
     const BlockDesc* blk_dev = reinterpret_cast<const BlockDesc*>(ops_dev + p->plan.ops.size());
-    const Cx<R>* pool_dev =
-        reinterpret_cast<const Cx<R>*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
-    Cx<R>* state = reinterpret_cast<Cx<R>*>(s->data);
+    const T* pool_dev = reinterpret_cast<const T*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
+    T* state = reinterpret_cast<T*>(s->data);
     if (pipe) {
-        auto kern = k_tile_pipe<R>;
+        auto kern = k_tile_pipe<T>;
         const size_t smem = 2 * tile_bytes + meta;
-        if (smem > 48 * 1024) LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LSG_CHECK(allow_smem(kern));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPipeThreads, smem);
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
         for (size_t i = 0; i < p->plan.passes.size(); ++i) {
@@ -439,9 +480,8 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
                                                                     tiles_per_member, total, status, ctx);
         }
     } else {
-        auto kern = k_tile_pass<R>;
-        if (p->smem > 48 * 1024)
-            LSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+        auto kern = k_tile_pass<T>;
+        LSG_CHECK(allow_smem(kern));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, p->smem);
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
         for (size_t i = 0; i < p->plan.passes.size(); ++i) {
@@ -456,11 +496,13 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
 }
 
 int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
-                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out) {
+                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out,
+                      cudaStream_t stream) {
     auto* p = new lsg_program_s();
     p->nbits = nbits;
     p->precision = precision;
     p->batch = batch;
+    p->dev.stream = stream;
     p->K = tile_bits_for(nbits, precision);
     const int L = std::min(p->K, low_bits_for(nbits, precision));
     if (nops > 0) {
@@ -496,7 +538,7 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
     size_t max_meta = 0;
     for (const PassDesc& pd : p->plan.passes)
         max_meta = std::max(max_meta, (size_t)pd.nops * sizeof(TileOp) + (size_t)pd.nblocks * sizeof(BlockDesc));
-    const size_t elt = precision == LSG_C128 ? 16 : 8;
+    const size_t elt = lsg_elem_bytes(precision);
     p->smem = (elt << p->K) + max_meta;
     if (p->smem > 220 * 1024) {
         delete p;
@@ -512,15 +554,25 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
                 p->plan.ops.size() * sizeof(TileOp));
     std::memcpy(blob.data() + p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp),
                 p->plan.blocks.data(), p->plan.blocks.size() * sizeof(BlockDesc));
+    unsigned char* dst = blob.data() + p->head_aligned;
     if (precision == LSG_C128) {
-        if (pool_entries) std::memcpy(blob.data() + p->head_aligned, pool, (size_t)pool_entries * 16);
-    } else {
-        float* f = reinterpret_cast<float*>(blob.data() + p->head_aligned);
+        if (pool_entries) std::memcpy(dst, pool, (size_t)pool_entries * 16);
+    } else if (precision == LSG_C64) {
+        float* f = reinterpret_cast<float*>(dst);
         for (int64_t i = 0; i < 2 * pool_entries; ++i) f[i] = (float)pool[i];  // rounded once
+    } else if (precision == LSG_R64) {
+        double* d = reinterpret_cast<double*>(dst);
+        for (int64_t i = 0; i < pool_entries; ++i) d[i] = pool[2 * i];  // real parts (the others are zero)
+    } else {
+        float* f = reinterpret_cast<float*>(dst);
+        for (int64_t i = 0; i < pool_entries; ++i) f[i] = (float)pool[2 * i];
     }
     int rc = ensure(p->dev, total);
     if (rc == LSG_OK) {
-        cudaError_t e = cudaMemcpy(p->dev.ptr, blob.data(), total, cudaMemcpyHostToDevice);
+        // the host blob is released on return: the copy must have consumed it
+        cudaError_t e = stream ? cudaMemcpyAsync(p->dev.ptr, blob.data(), total, cudaMemcpyHostToDevice, stream)
+                               : cudaMemcpy(p->dev.ptr, blob.data(), total, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && stream) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) rc = fail(LSG_E_CUDA, "uploading the program failed: %s", cudaGetErrorString(e));
     }
     if (rc != LSG_OK) {
@@ -533,9 +585,10 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
 }
 
 static int program_create(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
-                          const double* pool, int64_t pool_entries, lsg_program_s** out) {
-    LSG_CHECK(validate_ops(nbits, batch, ops, nops, pool, pool_entries));
-    return program_create_ex(nbits, precision, batch, ops, nops, pool, pool_entries, nullptr, nullptr, nullptr, out);
+                          const double* pool, int64_t pool_entries, lsg_program_s** out, cudaStream_t stream) {
+    LSG_CHECK(validate_ops(nbits, precision, batch, ops, nops, pool, pool_entries));
+    return program_create_ex(nbits, precision, batch, ops, nops, pool, pool_entries, nullptr, nullptr, nullptr, out,
+                             stream);
 }
 
 void program_destroy(lsg_program_s* p) {
@@ -550,7 +603,12 @@ int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const 
         return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
                     p->nbits, p->precision, (long long)p->batch);
     if (p->plan.passes.empty()) return LSG_OK;
-    return s->precision == LSG_C128 ? launch_passes<double>(p, s, marks, ctx) : launch_passes<float>(p, s, marks, ctx);
+    switch (s->precision) {
+        case LSG_C128: return launch_passes<Cx<double>>(p, s, marks, ctx);
+        case LSG_C64: return launch_passes<Cx<float>>(p, s, marks, ctx);
+        case LSG_R64: return launch_passes<double>(p, s, marks, ctx);
+        default: return launch_passes<float>(p, s, marks, ctx);
+    }
 }
 
 static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
@@ -558,9 +616,9 @@ static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
 }
 
 int apply_ops(lsg_state_s* s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries) {
-    if (nops == 0) return validate_ops(s->nbits, s->batch, ops, nops, pool, pool_entries);
+    if (nops == 0) return validate_ops(s->nbits, s->precision, s->batch, ops, nops, pool, pool_entries);
     lsg_program_s* p = nullptr;
-    LSG_CHECK(program_create(s->nbits, s->precision, s->batch, ops, nops, pool, pool_entries, &p));
+    LSG_CHECK(program_create(s->nbits, s->precision, s->batch, ops, nops, pool, pool_entries, &p, s->stream));
     int rc = program_run(p, s, nullptr);
     cudaError_t e = cudaStreamSynchronize(s->stream);
     program_destroy(p);
@@ -578,6 +636,34 @@ __global__ void k_set_basis(Cx<R>* state, int64_t elems, int64_t batch, int64_t 
         const int64_t j = i % elems;
         state[i] = Cx<R>(j == index ? R(1) : R(0), R(0));
     }
+}
+
+// Pauli-transfer form of |b><b| on n qubits: r_P = <b|P|b>, which is (-1)^{|z & b|} for the
+// diagonal Paulis (x = 0: register index z below 2^n) and 0 for every other.
+template <typename R>
+__global__ void k_set_basis_ptm(R* state, int64_t elems, int64_t batch, int n, int64_t b) {
+    const int64_t total = elems * batch;
+    const int64_t zmax = 1ll << n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = i % elems;
+        state[i] = j < zmax ? ((__popcll((unsigned long long)(j & b)) & 1) ? R(-1) : R(1)) : R(0);
+    }
+}
+
+template <typename R, typename C>
+__global__ void k_real_to_complex(const R* in, Cx<C>* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = Cx<C>((C)in[i], C(0));
+}
+
+__global__ void k_r32_to_r64(const float* in, double* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+__global__ void k_r64_to_r32(const double* in, float* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
 }
 
 __global__ void k_c128_to_c64(const double2* in, float2* out, int64_t n) {
@@ -611,10 +697,24 @@ int lsg_init(int device) {
     LSG_CUDA(cudaGetDeviceCount(&count));
     if (device < 0 || device >= count) return fail(LSG_E_ARG, "device %d does not exist (%d visible)", device, count);
     LSG_CUDA(cudaSetDevice(device));
+    cudaMemPool_t mp;
+    if (cudaDeviceGetDefaultMemPool(&mp, device) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     return LSG_OK;
 }
 
 int lsg_max_bits(void) { return kMaxBits; }
+
+int lsg_mem_info(int64_t* free_bytes, int64_t* total_bytes) {
+    clear_error();
+    size_t f = 0, t = 0;
+    LSG_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = (int64_t)f;
+    if (total_bytes) *total_bytes = (int64_t)t;
+    return LSG_OK;
+}
 
 int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
     clear_error();
@@ -622,7 +722,9 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
     *out = nullptr;
     if (nbits < 0) return fail(LSG_E_ARG, "lsg_state_create: negative bit count");
     if (nbits > kMaxBits) return fail(LSG_E_CAPACITY, "a register of %d bits exceeds the engine's %d", nbits, kMaxBits);
-    if (precision != LSG_C128 && precision != LSG_C64) return fail(LSG_E_ARG, "unknown precision %d", precision);
+    if (precision < LSG_C128 || precision > LSG_R32) return fail(LSG_E_ARG, "unknown precision %d", precision);
+    if ((precision == LSG_R64 || precision == LSG_R32) && (nbits & 1))
+        return fail(LSG_E_ARG, "a Pauli-transfer register has an even number of bits (two per qubit)");
     if (batch < 1) return fail(LSG_E_ARG, "lsg_state_create: batch must be at least 1");
     auto* s = new lsg_state_s();
     s->nbits = nbits;
@@ -634,7 +736,8 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
         delete s;
         return fail(LSG_E_CUDA, "cudaStreamCreate failed: %s", cudaGetErrorString(e));
     }
-    e = cudaMalloc(&s->data, s->member_bytes() * (size_t)batch);
+    s->program.stream = s->scratch.stream = s->scratch2.stream = s->stream;
+    e = cudaMallocAsync(&s->data, s->member_bytes() * (size_t)batch, s->stream);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s->stream);
         delete s;
@@ -649,11 +752,11 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
 int lsg_state_free(lsg_state s) {
     clear_error();
     if (!s) return LSG_OK;
-    cudaStreamSynchronize(s->stream);
-    cudaFree(s->data);
+    cudaFreeAsync(s->data, s->stream);
     release(s->program);
     release(s->scratch);
     release(s->scratch2);
+    cudaStreamSynchronize(s->stream);
     cudaStreamDestroy(s->stream);
     delete s;
     return LSG_OK;
@@ -662,12 +765,17 @@ int lsg_state_free(lsg_state s) {
 int lsg_state_set_basis(lsg_state s, int64_t index) {
     clear_error();
     if (!s) return fail(LSG_E_ARG, "null register");
-    if (index < 0 || index >= s->elems) return fail(LSG_E_ARG, "basis index %lld out of range", (long long)index);
+    const int64_t limit = s->real() ? (1ll << (s->nbits / 2)) : s->elems;  // real: |index><index| of nbits/2 qubits
+    if (index < 0 || index >= limit) return fail(LSG_E_ARG, "basis index %lld out of range", (long long)index);
     const int64_t n = s->elems * s->batch;
     if (s->precision == LSG_C128)
         k_set_basis<double><<<grid_for(n), 256, 0, s->stream>>>((Cx<double>*)s->data, s->elems, s->batch, index);
-    else
+    else if (s->precision == LSG_C64)
         k_set_basis<float><<<grid_for(n), 256, 0, s->stream>>>((Cx<float>*)s->data, s->elems, s->batch, index);
+    else if (s->precision == LSG_R64)
+        k_set_basis_ptm<double><<<grid_for(n), 256, 0, s->stream>>>((double*)s->data, s->elems, s->batch, s->nbits / 2, index);
+    else
+        k_set_basis_ptm<float><<<grid_for(n), 256, 0, s->stream>>>((float*)s->data, s->elems, s->batch, s->nbits / 2, index);
     LSG_CUDA(cudaGetLastError());
     LSG_CUDA(cudaStreamSynchronize(s->stream));
     return LSG_OK;
@@ -677,13 +785,17 @@ int lsg_state_upload(lsg_state s, const double* host, int64_t nbytes) {
     clear_error();
     if (!s || !host) return fail(LSG_E_ARG, "null argument");
     const int64_t n = s->elems * s->batch;
-    if (nbytes != n * 16) return fail(LSG_E_ARG, "upload expects %lld bytes, got %lld", (long long)(n * 16), (long long)nbytes);
-    if (s->precision == LSG_C128) {
+    const int64_t want = n * (s->real() ? 8 : 16);  // float64 per element for real registers
+    if (nbytes != want) return fail(LSG_E_ARG, "upload expects %lld bytes, got %lld", (long long)want, (long long)nbytes);
+    if (s->precision == LSG_C128 || s->precision == LSG_R64) {
         LSG_CUDA(cudaMemcpyAsync(s->data, host, (size_t)nbytes, cudaMemcpyHostToDevice, s->stream));
     } else {
         LSG_CHECK(ensure(s->scratch2, (size_t)nbytes));
         LSG_CUDA(cudaMemcpyAsync(s->scratch2.ptr, host, (size_t)nbytes, cudaMemcpyHostToDevice, s->stream));
-        k_c128_to_c64<<<grid_for(n), 256, 0, s->stream>>>((const double2*)s->scratch2.ptr, (float2*)s->data, n);
+        if (s->precision == LSG_R32)
+            k_r64_to_r32<<<grid_for(n), 256, 0, s->stream>>>((const double*)s->scratch2.ptr, (float*)s->data, n);
+        else
+            k_c128_to_c64<<<grid_for(n), 256, 0, s->stream>>>((const double2*)s->scratch2.ptr, (float2*)s->data, n);
         LSG_CUDA(cudaGetLastError());
     }
     LSG_CUDA(cudaStreamSynchronize(s->stream));
@@ -694,12 +806,16 @@ int lsg_state_download(lsg_state s, double* host, int64_t nbytes) {
     clear_error();
     if (!s || !host) return fail(LSG_E_ARG, "null argument");
     const int64_t n = s->elems * s->batch;
-    if (nbytes != n * 16) return fail(LSG_E_ARG, "download expects %lld bytes, got %lld", (long long)(n * 16), (long long)nbytes);
-    if (s->precision == LSG_C128) {
+    const int64_t want = n * (s->real() ? 8 : 16);
+    if (nbytes != want) return fail(LSG_E_ARG, "download expects %lld bytes, got %lld", (long long)want, (long long)nbytes);
+    if (s->precision == LSG_C128 || s->precision == LSG_R64) {
         LSG_CUDA(cudaMemcpyAsync(host, s->data, (size_t)nbytes, cudaMemcpyDeviceToHost, s->stream));
     } else {
         LSG_CHECK(ensure(s->scratch2, (size_t)nbytes));
-        k_c64_to_c128<<<grid_for(n), 256, 0, s->stream>>>((const float2*)s->data, (double2*)s->scratch2.ptr, n);
+        if (s->precision == LSG_R32)
+            k_r32_to_r64<<<grid_for(n), 256, 0, s->stream>>>((const float*)s->data, (double*)s->scratch2.ptr, n);
+        else
+            k_c64_to_c128<<<grid_for(n), 256, 0, s->stream>>>((const float2*)s->data, (double2*)s->scratch2.ptr, n);
         LSG_CUDA(cudaGetLastError());
         LSG_CUDA(cudaMemcpyAsync(host, s->scratch2.ptr, (size_t)nbytes, cudaMemcpyDeviceToHost, s->stream));
     }
@@ -735,12 +851,35 @@ int lsg_state_stream(lsg_state s, void** stream) {
     return LSG_OK;
 }
 
+int lsg_state_to_complex(lsg_state src, int64_t member, lsg_state dst) {
+    clear_error();
+    if (!src || !dst) return fail(LSG_E_ARG, "null register");
+    if (!src->real() || dst->real()) return fail(LSG_E_ARG, "lsg_state_to_complex: from a real register to a complex one");
+    if (src->nbits != dst->nbits) return fail(LSG_E_ARG, "lsg_state_to_complex: registers of different sizes");
+    if (member < 0 || member >= src->batch) return fail(LSG_E_ARG, "member %lld out of range", (long long)member);
+    LSG_CUDA(cudaStreamSynchronize(src->stream));  // dst's stream reads what src's stream wrote
+    const int64_t n = src->elems;
+    const unsigned g = grid_for(n);
+    if (src->precision == LSG_R64 && dst->precision == LSG_C128)
+        k_real_to_complex<double, double><<<g, 256, 0, dst->stream>>>((const double*)src->data + member * n, (Cx<double>*)dst->data, n);
+    else if (src->precision == LSG_R64)
+        k_real_to_complex<double, float><<<g, 256, 0, dst->stream>>>((const double*)src->data + member * n, (Cx<float>*)dst->data, n);
+    else if (dst->precision == LSG_C128)
+        k_real_to_complex<float, double><<<g, 256, 0, dst->stream>>>((const float*)src->data + member * n, (Cx<double>*)dst->data, n);
+    else
+        k_real_to_complex<float, float><<<g, 256, 0, dst->stream>>>((const float*)src->data + member * n, (Cx<float>*)dst->data, n);
+    LSG_CUDA(cudaGetLastError());
+    LSG_CUDA(cudaStreamSynchronize(dst->stream));
+    return LSG_OK;
+}
+
 int lsg_program_create(lsg_state shape, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries,
                        lsg_program* out) {
     clear_error();
     if (!shape || !out) return fail(LSG_E_ARG, "null argument");
     *out = nullptr;
-    return program_create(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out);
+    return program_create(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out,
+                          shape->stream);
 }
 
 int lsg_program_run(lsg_program p, lsg_state s) {
@@ -767,7 +906,7 @@ int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms) {
 int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run) {
     clear_error();
     if (!p) return fail(LSG_E_ARG, "null program");
-    const int64_t member = (int64_t)(p->precision == LSG_C128 ? 16 : 8) << p->nbits;
+    const int64_t member = (int64_t)lsg_elem_bytes(p->precision) << p->nbits;
     if (passes) *passes = (int32_t)p->plan.passes.size();
     if (bytes_per_run) *bytes_per_run = 2 * member * p->batch * (int64_t)p->plan.passes.size();
     return LSG_OK;

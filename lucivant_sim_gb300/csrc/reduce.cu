@@ -247,6 +247,71 @@ __global__ void k_collapse(Cx<R>* __restrict__ a, int64_t elems, int q, int outc
     }
 }
 
+// Probabilities of Pauli-transfer members: p(s) = 2^-n sum_z r[z] (-1)^{|z & s|} over the 2^n
+// diagonal coefficients (register indices below 2^n), a Walsh-Hadamard transform done in FP64 in
+// shared memory, one CTA per member, in a fixed butterfly order. Clipped at 0 like the diagonal.
+template <typename R>
+__global__ void k_probs_ptm(const R* __restrict__ r, int64_t elems, int n, int64_t member0, double* __restrict__ out) {
+    extern __shared__ double w[];
+    const int64_t member = member0 + blockIdx.x;
+    const R* src = r + member * elems;
+    const int d = 1 << n;
+    for (int i = threadIdx.x; i < d; i += blockDim.x) w[i] = (double)src[i];
+    __syncthreads();
+    for (int h = 1; h < d; h <<= 1) {
+        for (int j = threadIdx.x; j < d / 2; j += blockDim.x) {
+            const int i0 = ((j / h) * 2 * h) + (j % h), i1 = i0 + h;
+            const double a = w[i0], b = w[i1];
+            w[i0] = a + b;
+            w[i1] = a - b;
+        }
+        __syncthreads();
+    }
+    const double scale = 1.0 / (double)d;
+    double* dst = out + (int64_t)blockIdx.x * d;
+    for (int i = threadIdx.x; i < d; i += blockDim.x) {
+        const double v = w[i] * scale;
+        dst[i] = v > 0.0 ? v : 0.0;
+    }
+}
+
+// <P> of Pauli-transfer members: the coefficient itself, at register index (x << n) | z.
+template <typename R>
+__global__ void k_expect_ptm(const R* __restrict__ r, int64_t elems, int n, const uint64_t* __restrict__ xm,
+                             const uint64_t* __restrict__ zm, int nterms, int64_t batch, double* __restrict__ out) {
+    const int64_t total = (int64_t)nterms * batch;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = i / nterms;
+        const int t = (int)(i - b * nterms);
+        out[i] = (double)r[b * elems + (int64_t)((xm[t] << n) | zm[t])];
+    }
+}
+
+static int launch_probs_ptm(lsg_state_s* s, int n, int64_t member0, int64_t members, double* dev_out) {
+    const size_t smem = (size_t)8 << n;
+    static std::mutex mu;
+    static bool done[2][64] = {};
+    int dev = 0;
+    LSG_CUDA(cudaGetDevice(&dev));
+    const int which = s->precision == LSG_R64 ? 0 : 1;
+    if (smem > 48 * 1024) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (dev >= 0 && dev < 64 && !done[which][dev]) {
+            if (which == 0)
+                LSG_CUDA(cudaFuncSetAttribute(k_probs_ptm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 14));
+            else
+                LSG_CUDA(cudaFuncSetAttribute(k_probs_ptm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 14));
+            done[which][dev] = true;
+        }
+    }
+    if (which == 0)
+        k_probs_ptm<double><<<(unsigned)members, 512, smem, s->stream>>>((const double*)s->data, s->elems, n, member0, dev_out);
+    else
+        k_probs_ptm<float><<<(unsigned)members, 512, smem, s->stream>>>((const float*)s->data, s->elems, n, member0, dev_out);
+    LSG_CUDA(cudaGetLastError());
+    return LSG_OK;
+}
+
 static unsigned reduce_grid(int64_t n) {
     int64_t g = (n + kThreads - 1) / kThreads;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 8));
@@ -255,6 +320,13 @@ static unsigned reduce_grid(int64_t n) {
 // Probabilities of one member into a device buffer of 2^n doubles.
 static int probs_device(lsg_state_s* s, int dm_n, int64_t member, double* dev_out, int64_t* n_out) {
     if (member < 0 || member >= s->batch) return fail(LSG_E_ARG, "member %lld out of range", (long long)member);
+    if (s->real()) {
+        if (2 * dm_n != s->nbits) return fail(LSG_E_STATE, "a Pauli-transfer register of %d bits holds %d qubits", s->nbits, s->nbits / 2);
+        if (dm_n > 14) return fail(LSG_E_CAPACITY, "Pauli-transfer probabilities up to 14 qubits");
+        LSG_CHECK(launch_probs_ptm(s, dm_n, member, 1, dev_out));
+        *n_out = 1ll << dm_n;
+        return LSG_OK;
+    }
     if (dm_n) {
         if (2 * dm_n != s->nbits) return fail(LSG_E_STATE, "a %d-qubit density register needs %d bits", dm_n, 2 * dm_n);
         const int64_t d = 1ll << dm_n;
@@ -284,12 +356,18 @@ extern "C" {
 int lsg_probabilities(lsg_state s, int dm_qubits, int64_t member, double* out) {
     clear_error();
     if (!s || !out) return fail(LSG_E_ARG, "null argument");
+    if (s->real() && 2 * dm_qubits != s->nbits)
+        return fail(LSG_E_STATE, "a Pauli-transfer register of %d bits holds %d qubits", s->nbits, s->nbits / 2);
     const int64_t n = dm_qubits ? (1ll << dm_qubits) : s->elems;
     if (member < 0) {  // every member, one after another in `out`
         LSG_CHECK(ensure(s->scratch, (size_t)n * 8 * s->batch));
-        for (int64_t b = 0; b < s->batch; ++b) {
-            int64_t got = 0;
-            LSG_CHECK(probs_device(s, dm_qubits, b, (double*)s->scratch.ptr + b * n, &got));
+        if (s->real() && 2 * dm_qubits == s->nbits && dm_qubits <= 14) {  // one launch for all members
+            LSG_CHECK(launch_probs_ptm(s, dm_qubits, 0, s->batch, (double*)s->scratch.ptr));
+        } else {
+            for (int64_t b = 0; b < s->batch; ++b) {
+                int64_t got = 0;
+                LSG_CHECK(probs_device(s, dm_qubits, b, (double*)s->scratch.ptr + b * n, &got));
+            }
         }
         LSG_CUDA(cudaMemcpyAsync(out, s->scratch.ptr, (size_t)n * 8 * s->batch, cudaMemcpyDeviceToHost, s->stream));
         LSG_CUDA(cudaStreamSynchronize(s->stream));
@@ -402,6 +480,30 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
     const uint64_t limit = nq >= 64 ? ~0ull : ((1ull << nq) - 1);
     for (int t = 0; t < nterms; ++t)
         if ((xmask[t] | zmask[t]) & ~limit) return fail(LSG_E_ARG, "lsg_expect_pauli: term %d names a missing qubit", t);
+    if (s->real()) {  // Pauli-transfer register: each expectation is one coefficient
+        if (2 * dm_qubits != s->nbits) return fail(LSG_E_STATE, "a Pauli-transfer register of %d bits holds %d qubits", s->nbits, s->nbits / 2);
+        const int64_t rows = (int64_t)nterms * s->batch;
+        const size_t o_x = 0, o_z = ((size_t)nterms * 8 + 255) & ~size_t(255), o_out = 2 * o_z;
+        LSG_CHECK(ensure(s->scratch, o_out + (size_t)rows * 8));
+        char* base = (char*)s->scratch.ptr;
+        LSG_CUDA(cudaMemcpyAsync(base + o_x, xmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
+        LSG_CUDA(cudaMemcpyAsync(base + o_z, zmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
+        if (s->precision == LSG_R64)
+            k_expect_ptm<double><<<reduce_grid(rows), kThreads, 0, s->stream>>>(
+                (const double*)s->data, s->elems, dm_qubits, (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                nterms, s->batch, (double*)(base + o_out));
+        else
+            k_expect_ptm<float><<<reduce_grid(rows), kThreads, 0, s->stream>>>(
+                (const float*)s->data, s->elems, dm_qubits, (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                nterms, s->batch, (double*)(base + o_out));
+        LSG_CUDA(cudaGetLastError());
+        std::vector<double> tmp((size_t)rows);
+        LSG_CUDA(cudaMemcpyAsync(tmp.data(), base + o_out, tmp.size() * 8, cudaMemcpyDeviceToHost, s->stream));
+        LSG_CUDA(cudaStreamSynchronize(s->stream));
+        for (int64_t b = 0; b < s->batch; ++b)
+            for (int t = 0; t < nterms; ++t) out[(int64_t)t * s->batch + b] = tmp[b * nterms + t];
+        return LSG_OK;
+    }
     const int64_t count = dm_qubits ? (1ll << dm_qubits) : s->elems;
     const unsigned grid = std::max(1u, std::min(reduce_grid(count), (unsigned)std::max<int64_t>(1, 4096 / s->batch)));
     size_t off = 0;
@@ -440,6 +542,7 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
 int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out) {
     clear_error();
     if (!s || !out) return fail(LSG_E_ARG, "null argument");
+    if (s->real()) return fail(LSG_E_STATE, "lsg_prob_one takes a statevector register");
     if (qubit < 0 || qubit >= s->nbits) return fail(LSG_E_ARG, "qubit %d out of range", qubit);
     if (member < 0 || member >= s->batch) return fail(LSG_E_ARG, "member out of range");
     const unsigned grid = reduce_grid(s->elems >> 1);
@@ -458,6 +561,7 @@ int lsg_prob_one(lsg_state s, int qubit, int64_t member, double* out) {
 
 int lsg_collapse(lsg_state s, int qubit, int outcome, double probability, int64_t member) {
     clear_error();
+    if (s && s->real()) return fail(LSG_E_STATE, "lsg_collapse takes a statevector register");
     if (!s) return fail(LSG_E_ARG, "null register");
     if (qubit < 0 || qubit >= s->nbits || (outcome != 0 && outcome != 1)) return fail(LSG_E_ARG, "bad qubit or outcome");
     if (member < 0 || member >= s->batch) return fail(LSG_E_ARG, "member out of range");

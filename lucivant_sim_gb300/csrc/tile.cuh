@@ -52,36 +52,36 @@ __device__ __forceinline__ uint32_t ins0(uint32_t g, int b) {
     return ((g >> b) << (b + 1)) | low;
 }
 
-template <typename R>
-__device__ __forceinline__ Cx<R> ldm(const Cx<R>* m, int i) {
+template <typename T>
+__device__ __forceinline__ T ldm(const T* m, int i) {
     return m[i];
 }
 
 // 1-bit dense: the common case (fused one-qubit gates; one-qubit density superoperators use 2).
-template <typename R>
-__device__ __forceinline__ void dense1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
-    const Cx<R> m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+template <typename T>
+__device__ __forceinline__ void dense1(T* t, int tbits, int b, const T* m) {
+    const T m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
     const int groups = 1 << (tbits - 1);
     for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
-        const Cx<R> a0 = t[i0], a1 = t[i1];
+        const T a0 = t[i0], a1 = t[i1];
         t[i0] = cfma(m01, a1, cmul(m00, a0));
         t[i1] = cfma(m11, a1, cmul(m10, a0));
     }
 }
 
 // 2-bit dense on (hi_bit = matrix MSB b0, b1); lo/hi are the sorted positions.
-template <typename R>
-__device__ __forceinline__ void dense2(Cx<R>* t, int tbits, int b0, int b1, const Cx<R>* m) {
+template <typename T>
+__device__ __forceinline__ void dense2(T* t, int tbits, int b0, int b1, const T* m) {
     const int lo = min(b0, b1), hi = max(b0, b1);
     const uint32_t o1 = 1u << b1, o2 = 1u << b0;
     const int groups = 1 << (tbits - 2);
     for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
-        const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
+        const T v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            Cx<R> acc = cmul(ldm(m, 4 * r), v0);
+            T acc = cmul(ldm(m, 4 * r), v0);
             acc = cfma(ldm(m, 4 * r + 1), v1, acc);
             acc = cfma(ldm(m, 4 * r + 2), v2, acc);
             acc = cfma(ldm(m, 4 * r + 3), v3, acc);
@@ -91,37 +91,37 @@ __device__ __forceinline__ void dense2(Cx<R>* t, int tbits, int b0, int b1, cons
     }
 }
 
-template <typename R>
-__device__ __forceinline__ Cx<R> pick4(const Cx<R>& v0, const Cx<R>& v1, const Cx<R>& v2, const Cx<R>& v3, int s) {
-    const Cx<R> a = (s & 1) ? v1 : v0;
-    const Cx<R> b = (s & 1) ? v3 : v2;
+template <typename T>
+__device__ __forceinline__ T pick4(const T& v0, const T& v1, const T& v2, const T& v3, int s) {
+    const T a = (s & 1) ? v1 : v0;
+    const T b = (s & 1) ? v3 : v2;
     return (s & 2) ? b : a;
 }
 
 // permutations with phases on 1 or 2 bits (x, cx, swap and their phased forms)
-template <typename R>
-__device__ __forceinline__ void perm1(Cx<R>* t, int tbits, int b, const Cx<R>* m) {
-    const Cx<R> p0 = m[0], p1 = m[1];
-    const int s0 = (int)m[2].re;
+template <typename T>
+__device__ __forceinline__ void perm1(T* t, int tbits, int b, const T* m) {
+    const T p0 = m[0], p1 = m[1];
+    const int s0 = (int)re_of(m[2]);
     const int groups = 1 << (tbits - 1);
     for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t i0 = ins0((uint32_t)g, b), i1 = i0 | (1u << b);
-        const Cx<R> a0 = t[i0], a1 = t[i1];
+        const T a0 = t[i0], a1 = t[i1];
         t[i0] = cmul(p0, s0 ? a1 : a0);
         t[i1] = cmul(p1, s0 ? a0 : a1);
     }
 }
 
-template <typename R>
-__device__ __forceinline__ void perm2(Cx<R>* t, int tbits, int b0, int b1, const Cx<R>* m) {
+template <typename T>
+__device__ __forceinline__ void perm2(T* t, int tbits, int b0, int b1, const T* m) {
     const int lo = min(b0, b1), hi = max(b0, b1);
     const uint32_t o1 = 1u << b1, o2 = 1u << b0;
-    const Cx<R> p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
-    const int s0 = (int)m[4].re, s1 = (int)m[5].re, s2 = (int)m[6].re, s3 = (int)m[7].re;
+    const T p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
+    const int s0 = (int)re_of(m[4]), s1 = (int)re_of(m[5]), s2 = (int)re_of(m[6]), s3 = (int)re_of(m[7]);
     const int groups = 1 << (tbits - 2);
     for (int g = threadIdx.x; g < groups; g += kCompute) {
         const uint32_t base = ins0(ins0((uint32_t)g, lo), hi);
-        const Cx<R> v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
+        const T v0 = t[base], v1 = t[base | o1], v2 = t[base | o2], v3 = t[base | o1 | o2];
         t[base] = cmul(p0, pick4(v0, v1, v2, v3, s0));
         t[base | o1] = cmul(p1, pick4(v0, v1, v2, v3, s1));
         t[base | o2] = cmul(p2, pick4(v0, v1, v2, v3, s2));
@@ -131,12 +131,12 @@ __device__ __forceinline__ void perm2(Cx<R>* t, int tbits, int b0, int b1, const
 
 // Wide operators (3 to 5 bits): rare (Toffoli-class gates, two-qubit Kraus superoperators), kept
 // out of line so their register needs don't shape the common path.
-template <typename R>
-__device__ __noinline__ void wide_op(Cx<R>* t, int tbits, int kind, int k, const int* lb, const int* sorted,
-                                     const Cx<R>* m) {
+template <typename T>
+__device__ __noinline__ void wide_op(T* t, int tbits, int kind, int k, const int* lb, const int* sorted,
+                                     const T* m) {
     const int D = 1 << k;
     uint32_t offs[32];
-    Cx<R> v[32];
+    T v[32];
     for (int j = 0; j < D; ++j) {
         uint32_t o = 0;
         for (int i = 0; i < k; ++i) o |= (uint32_t)((j >> (k - 1 - i)) & 1) << lb[i];
@@ -149,18 +149,18 @@ __device__ __noinline__ void wide_op(Cx<R>* t, int tbits, int kind, int k, const
         for (int j = 0; j < D; ++j) v[j] = t[base | offs[j]];
         if (kind == LSG_OP_MATRIX) {
             for (int r = 0; r < D; ++r) {
-                Cx<R> acc;
+                T acc{};
                 for (int c = 0; c < D; ++c) acc = cfma(m[r * D + c], v[c], acc);
                 t[base | offs[r]] = acc;
             }
         } else {
-            for (int r = 0; r < D; ++r) t[base | offs[r]] = cmul(m[r], v[(int)m[D + r].re]);
+            for (int r = 0; r < D; ++r) t[base | offs[r]] = cmul(m[r], v[(int)re_of(m[D + r])]);
         }
     }
 }
 
-template <typename R>
-__device__ __forceinline__ void op_diag(Cx<R>* tile, int tbits, int k, const int* lb, const Cx<R>* m) {
+template <typename T>
+__device__ __forceinline__ void op_diag(T* tile, int tbits, int k, const int* lb, const T* m) {
     const int n = 1 << tbits;
     for (int i = threadIdx.x; i < n; i += kCompute) {
         int j = 0;
@@ -169,16 +169,18 @@ __device__ __forceinline__ void op_diag(Cx<R>* tile, int tbits, int k, const int
     }
 }
 
-template <typename R>
-__device__ __forceinline__ void op_scale(Cx<R>* tile, int tbits, const Cx<R>* m) {
+template <typename T>
+__device__ __forceinline__ void op_scale(T* tile, int tbits, const T* m) {
     const int n = 1 << tbits;
-    const Cx<R> f = m[0];
+    const T f = m[0];
     for (int i = threadIdx.x; i < n; i += kCompute) tile[i] = cmul(f, tile[i]);
 }
 
 // (1-p) rho + (p/d) I (x) Tr_t(rho) on kq row bits then kq column bits (kq = 1 or 2).
-template <typename R, int KQ>
-__device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, const int* sorted, const Cx<R>* m) {
+template <typename T, int KQ>
+__device__ __forceinline__ void op_depol(T* t, int tbits, const int* lb, const int* sorted, const T* m) {
+    using R = typename Elem<T>::R;
+    if constexpr (Elem<T>::complex) {
     constexpr int KB = 2 * KQ;
     constexpr int D = 1 << KB;
     constexpr int d = 1 << KQ;
@@ -196,14 +198,14 @@ __device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, con
         uint32_t base = (uint32_t)g;
 #pragma unroll
         for (int i = 0; i < KB; ++i) base = ins0(base, srt[i]);
-        Cx<R> tr;
+        T tr;
 #pragma unroll
         for (int s = 0; s < d; ++s) {
             const int j = (s << KQ) | s;
             uint32_t o = 0;
 #pragma unroll
             for (int i = 0; i < KB; ++i) o |= (uint32_t)((j >> (KB - 1 - i)) & 1) << l[i];
-            const Cx<R> v = t[base | o];
+            const T v = t[base | o];
             tr.re += v.re;
             tr.im += v.im;
         }
@@ -212,8 +214,8 @@ __device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, con
             uint32_t o = 0;
 #pragma unroll
             for (int i = 0; i < KB; ++i) o |= (uint32_t)((j >> (KB - 1 - i)) & 1) << l[i];
-            const Cx<R> v = t[base | o];
-            Cx<R> out(v.re * keep, v.im * keep);
+            const T v = t[base | o];
+            T out(v.re * keep, v.im * keep);
             if ((j >> KQ) == (j & (d - 1))) {
                 out.re += share * tr.re;
                 out.im += share * tr.im;
@@ -221,14 +223,17 @@ __device__ __forceinline__ void op_depol(Cx<R>* t, int tbits, const int* lb, con
             t[base | o] = out;
         }
     }
+    }
 }
 
 // A state-independent noise channel in a trajectory: the member picks branch i, the first with
 // u < cum[i] (cum = running sums of the branch probabilities, as engines.py:163-171 accumulates
 // them), and applies that branch's unitary unless it is the identity. Data: `count` entries
 // (re = cumulative probability, im = 1 for an identity branch), then `count` dense 2^k matrices.
-template <typename R>
-__device__ __forceinline__ void op_mixture(Cx<R>* t, int tbits, const TileOp& op, const Cx<R>* m, double u) {
+template <typename T>
+__device__ __forceinline__ void op_mixture(T* t, int tbits, const TileOp& op, const T* m, double u) {
+    using R = typename Elem<T>::R;
+    if constexpr (Elem<T>::complex) {
     const int nb = op.count;
     int pick = -1;
     for (int i = 0; i < nb; ++i) {
@@ -239,10 +244,11 @@ __device__ __forceinline__ void op_mixture(Cx<R>* t, int tbits, const TileOp& op
     }
     if (pick < 0 || m[pick].im != R(0)) return;  // nothing drawn, or the identity branch
     const int d = 1 << op.k;
-    const Cx<R>* mat = m + nb + (int64_t)pick * d * d;
-    if (op.k == 1) dense1<R>(t, tbits, op.lb[0], mat);
-    else if (op.k == 2) dense2<R>(t, tbits, op.lb[0], op.lb[1], mat);
-    else wide_op<R>(t, tbits, LSG_OP_MATRIX, op.k, op.lb, op.sorted, mat);
+    const T* mat = m + nb + (int64_t)pick * d * d;
+    if (op.k == 1) dense1<T>(t, tbits, op.lb[0], mat);
+    else if (op.k == 2) dense2<T>(t, tbits, op.lb[0], op.lb[1], mat);
+    else wide_op<T>(t, tbits, LSG_OP_MATRIX, op.k, op.lb, op.sorted, mat);
+    }
 }
 
 
@@ -251,29 +257,29 @@ __device__ __forceinline__ void op_mixture(Cx<R>* t, int tbits, const TileOp& op
 // v[e] holds the amplitude at group offset e of a block of U bits; bit (U-1-P) of e is block
 // position P. Every function below is fully unrolled over e, so v stays in registers.
 
-template <typename R, int U, int P>
-__device__ __forceinline__ void rb_dense1(Cx<R>* v, const Cx<R>* m) {
+template <typename T, int U, int P>
+__device__ __forceinline__ void rb_dense1(T* v, const T* m) {
     constexpr int B = 1 << (U - 1 - P);
-    const Cx<R> m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+    const T m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & B) continue;
-        const Cx<R> a0 = v[e], a1 = v[e | B];
+        const T a0 = v[e], a1 = v[e | B];
         v[e] = cfma(m01, a1, cmul(m00, a0));
         v[e | B] = cfma(m11, a1, cmul(m10, a0));
     }
 }
 
-template <typename R, int U, int P0, int P1>
-__device__ __forceinline__ void rb_dense2(Cx<R>* v, const Cx<R>* m) {
+template <typename T, int U, int P0, int P1>
+__device__ __forceinline__ void rb_dense2(T* v, const T* m) {
     constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & (B0 | B1)) continue;
-        const Cx<R> a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+        const T a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            Cx<R> acc = cmul(m[4 * r], a0);
+            T acc = cmul(m[4 * r], a0);
             acc = cfma(m[4 * r + 1], a1, acc);
             acc = cfma(m[4 * r + 2], a2, acc);
             acc = cfma(m[4 * r + 3], a3, acc);
@@ -282,29 +288,29 @@ __device__ __forceinline__ void rb_dense2(Cx<R>* v, const Cx<R>* m) {
     }
 }
 
-template <typename R, int U, int P>
-__device__ __forceinline__ void rb_perm1(Cx<R>* v, const Cx<R>* m) {
+template <typename T, int U, int P>
+__device__ __forceinline__ void rb_perm1(T* v, const T* m) {
     constexpr int B = 1 << (U - 1 - P);
-    const Cx<R> p0 = m[0], p1 = m[1];
-    const bool swap = m[2].re != R(0);
+    const T p0 = m[0], p1 = m[1];
+    const bool swap = re_of(m[2]) != 0;
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & B) continue;
-        const Cx<R> a0 = v[e], a1 = v[e | B];
+        const T a0 = v[e], a1 = v[e | B];
         v[e] = cmul(p0, swap ? a1 : a0);
         v[e | B] = cmul(p1, swap ? a0 : a1);
     }
 }
 
-template <typename R, int U, int P0, int P1>
-__device__ __forceinline__ void rb_perm2(Cx<R>* v, const Cx<R>* m) {
+template <typename T, int U, int P0, int P1>
+__device__ __forceinline__ void rb_perm2(T* v, const T* m) {
     constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
-    const Cx<R> p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
-    const int s0 = (int)m[4].re, s1 = (int)m[5].re, s2 = (int)m[6].re, s3 = (int)m[7].re;
+    const T p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
+    const int s0 = (int)re_of(m[4]), s1 = (int)re_of(m[5]), s2 = (int)re_of(m[6]), s3 = (int)re_of(m[7]);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & (B0 | B1)) continue;
-        const Cx<R> a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+        const T a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
         v[e] = cmul(p0, pick4(a0, a1, a2, a3, s0));
         v[e | B1] = cmul(p1, pick4(a0, a1, a2, a3, s1));
         v[e | B0] = cmul(p2, pick4(a0, a1, a2, a3, s2));
@@ -313,66 +319,71 @@ __device__ __forceinline__ void rb_perm2(Cx<R>* v, const Cx<R>* m) {
 }
 
 // Unit-phase permutations are register renames: no arithmetic at all.
-template <typename R, int U, int P>
-__device__ __forceinline__ void rb_x(Cx<R>* v) {
+template <typename T, int U, int P>
+__device__ __forceinline__ void rb_x(T* v) {
     constexpr int B = 1 << (U - 1 - P);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e)
         if (!(e & B)) {
-            const Cx<R> t = v[e];
+            const T t = v[e];
             v[e] = v[e | B];
             v[e | B] = t;
         }
 }
 
 // controlled X: control at position PC, target at PT
-template <typename R, int U, int PC, int PT>
-__device__ __forceinline__ void rb_cx(Cx<R>* v) {
+template <typename T, int U, int PC, int PT>
+__device__ __forceinline__ void rb_cx(T* v) {
     constexpr int BC = 1 << (U - 1 - PC), BT = 1 << (U - 1 - PT);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e)
         if ((e & BC) && !(e & BT)) {
-            const Cx<R> t = v[e];
+            const T t = v[e];
             v[e] = v[e | BT];
             v[e | BT] = t;
         }
 }
 
-template <typename R, int U, int P0, int P1>
-__device__ __forceinline__ void rb_swap(Cx<R>* v) {
+template <typename T, int U, int P0, int P1>
+__device__ __forceinline__ void rb_swap(T* v) {
     constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e)
         if ((e & B0) && !(e & B1)) {
-            const Cx<R> t = v[e];
+            const T t = v[e];
             v[e] = v[(e & ~B0) | B1];
             v[(e & ~B0) | B1] = t;
         }
 }
 
 // (1-p) rho + (p/2) I Tr on one row bit (position PR) and its column bit (PC)
-template <typename R, int U, int PR, int PC>
-__device__ __forceinline__ void rb_depol1(Cx<R>* v, const Cx<R>* m) {
+template <typename T, int U, int PR, int PC>
+__device__ __forceinline__ void rb_depol1(T* v, const T* m) {
+    using R = typename Elem<T>::R;
+    if constexpr (Elem<T>::complex) {
     constexpr int BR = 1 << (U - 1 - PR), BC = 1 << (U - 1 - PC);
     const R p = m[0].re, keep = R(1) - p, share = p / R(2);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & (BR | BC)) continue;
-        const Cx<R> d0 = v[e], d1 = v[e | BR | BC];
-        const Cx<R> tr(d0.re + d1.re, d0.im + d1.im);
-        v[e] = Cx<R>(d0.re * keep + share * tr.re, d0.im * keep + share * tr.im);
-        v[e | BR | BC] = Cx<R>(d1.re * keep + share * tr.re, d1.im * keep + share * tr.im);
-        const Cx<R> o1 = v[e | BC], o2 = v[e | BR];
-        v[e | BC] = Cx<R>(o1.re * keep, o1.im * keep);
-        v[e | BR] = Cx<R>(o2.re * keep, o2.im * keep);
+        const T d0 = v[e], d1 = v[e | BR | BC];
+        const T tr(d0.re + d1.re, d0.im + d1.im);
+        v[e] = T(d0.re * keep + share * tr.re, d0.im * keep + share * tr.im);
+        v[e | BR | BC] = T(d1.re * keep + share * tr.re, d1.im * keep + share * tr.im);
+        const T o1 = v[e | BC], o2 = v[e | BR];
+        v[e | BC] = T(o1.re * keep, o1.im * keep);
+        v[e | BR] = T(o2.re * keep, o2.im * keep);
+    }
     }
 }
 
 // two-qubit form on positions (row a, row b, col a, col b) = (0, 1, 2, 3) of a 4-bit block
-template <typename R>
-__device__ __forceinline__ void rb_depol2(Cx<R>* v, const Cx<R>* m) {
+template <typename T>
+__device__ __forceinline__ void rb_depol2(T* v, const T* m) {
+    using R = typename Elem<T>::R;
+    if constexpr (Elem<T>::complex) {
     const R p = m[0].re, keep = R(1) - p, share = p / R(4);
-    Cx<R> tr;
+    T tr;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
         tr.re += v[(t << 2) | t].re;
@@ -380,17 +391,18 @@ __device__ __forceinline__ void rb_depol2(Cx<R>* v, const Cx<R>* m) {
     }
 #pragma unroll
     for (int e = 0; e < 16; ++e) {
-        Cx<R> o(v[e].re * keep, v[e].im * keep);
+        T o(v[e].re * keep, v[e].im * keep);
         if ((e >> 2) == (e & 3)) {
             o.re += share * tr.re;
             o.im += share * tr.im;
         }
         v[e] = o;
     }
+    }
 }
 
-template <typename R, int U>
-__device__ __forceinline__ void rb_diag(Cx<R>* v, const TileOp& op, const Cx<R>* m) {
+template <typename T, int U>
+__device__ __forceinline__ void rb_diag(T* v, const TileOp& op, const T* m) {
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         int j = 0;
@@ -399,16 +411,18 @@ __device__ __forceinline__ void rb_diag(Cx<R>* v, const TileOp& op, const Cx<R>*
     }
 }
 
-template <typename R, int U>
-__device__ __forceinline__ void rb_scale(Cx<R>* v, const Cx<R>* m) {
-    const Cx<R> f = m[0];
+template <typename T, int U>
+__device__ __forceinline__ void rb_scale(T* v, const T* m) {
+    const T f = m[0];
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) v[e] = cmul(f, v[e]);
 }
 
 // the branch matrix a member's uniform picks from a mixture channel, or nullptr for identity
-template <typename R>
-__device__ __forceinline__ const Cx<R>* mixture_pick(const TileOp& op, const Cx<R>* m, double u) {
+template <typename T>
+__device__ __forceinline__ const T* mixture_pick(const TileOp& op, const T* m, double u) {
+    using R = typename Elem<T>::R;
+    if constexpr (Elem<T>::complex) {
     const int nb = op.count;
     int pick = -1;
     for (int i = 0; i < nb; ++i)
@@ -419,25 +433,27 @@ __device__ __forceinline__ const Cx<R>* mixture_pick(const TileOp& op, const Cx<
     if (pick < 0 || m[pick].im != R(0)) return nullptr;
     const int d = 1 << op.k;
     return m + nb + (int64_t)pick * d * d;
+    }
+    return nullptr;
 }
 
 #define LSG_P1(X, BASE)                                    \
-    case BASE + 0: if (U > 0) X<R, U, (0 < U ? 0 : 0)>(v, m); break; \
-    case BASE + 1: if (U > 1) X<R, U, (1 < U ? 1 : 0)>(v, m); break; \
-    case BASE + 2: if (U > 2) X<R, U, (2 < U ? 2 : 0)>(v, m); break; \
-    case BASE + 3: if (U > 3) X<R, U, (3 < U ? 3 : 0)>(v, m); break;
+    case BASE + 0: if (U > 0) X<T, U, (0 < U ? 0 : 0)>(v, m); break; \
+    case BASE + 1: if (U > 1) X<T, U, (1 < U ? 1 : 0)>(v, m); break; \
+    case BASE + 2: if (U > 2) X<T, U, (2 < U ? 2 : 0)>(v, m); break; \
+    case BASE + 3: if (U > 3) X<T, U, (3 < U ? 3 : 0)>(v, m); break;
 
 #define LSG_P2ONE(X, BASE, A, B) \
-    case BASE + 4 * A + B: if (U > A && U > B) X<R, U, (A < U ? A : 0), (B < U ? B : 0)>(v, m); break;
+    case BASE + 4 * A + B: if (U > A && U > B) X<T, U, (A < U ? A : 0), (B < U ? B : 0)>(v, m); break;
 
 #define LSG_R1(X, BASE)                                    \
-    case BASE + 0: if (U > 0) X<R, U, (0 < U ? 0 : 0)>(v); break; \
-    case BASE + 1: if (U > 1) X<R, U, (1 < U ? 1 : 0)>(v); break; \
-    case BASE + 2: if (U > 2) X<R, U, (2 < U ? 2 : 0)>(v); break; \
-    case BASE + 3: if (U > 3) X<R, U, (3 < U ? 3 : 0)>(v); break;
+    case BASE + 0: if (U > 0) X<T, U, (0 < U ? 0 : 0)>(v); break; \
+    case BASE + 1: if (U > 1) X<T, U, (1 < U ? 1 : 0)>(v); break; \
+    case BASE + 2: if (U > 2) X<T, U, (2 < U ? 2 : 0)>(v); break; \
+    case BASE + 3: if (U > 3) X<T, U, (3 < U ? 3 : 0)>(v); break;
 
 #define LSG_R2ONE(X, BASE, A, B) \
-    case BASE + 4 * A + B: if (U > A && U > B) X<R, U, (A < U ? A : 0), (B < U ? B : 0)>(v); break;
+    case BASE + 4 * A + B: if (U > A && U > B) X<T, U, (A < U ? A : 0), (B < U ? B : 0)>(v); break;
 
 #define LSG_R2(X, BASE)                                                                                  \
     LSG_R2ONE(X, BASE, 0, 1) LSG_R2ONE(X, BASE, 0, 2) LSG_R2ONE(X, BASE, 0, 3) LSG_R2ONE(X, BASE, 1, 0) \
@@ -449,8 +465,8 @@ __device__ __forceinline__ const Cx<R>* mixture_pick(const TileOp& op, const Cx<
     LSG_P2ONE(X, BASE, 1, 2) LSG_P2ONE(X, BASE, 1, 3) LSG_P2ONE(X, BASE, 2, 0) LSG_P2ONE(X, BASE, 2, 1) \
     LSG_P2ONE(X, BASE, 2, 3) LSG_P2ONE(X, BASE, 3, 0) LSG_P2ONE(X, BASE, 3, 1) LSG_P2ONE(X, BASE, 3, 2)
 
-template <typename R, int U>
-__device__ __forceinline__ void rb_apply(Cx<R>* v, int code, const TileOp& op, const Cx<R>* m) {
+template <typename T, int U>
+__device__ __forceinline__ void rb_apply(T* v, int code, const TileOp& op, const T* m) {
     switch (code) {
         LSG_P1(rb_dense1, kT_DENSE1)
         LSG_P2(rb_dense2, kT_DENSE2)
@@ -458,13 +474,13 @@ __device__ __forceinline__ void rb_apply(Cx<R>* v, int code, const TileOp& op, c
         LSG_P2(rb_perm2, kT_PERM2)
         LSG_P2(rb_depol1, kT_DEPOL1)
         case kT_DEPOL2:
-            if (U == 4) rb_depol2<R>(v, m);
+            if (U == 4) rb_depol2<T>(v, m);
             break;
         LSG_R1(rb_x, kT_X1)
         LSG_R2(rb_cx, kT_CX)
         LSG_R2(rb_swap, kT_SWAP)
-        case kT_DIAG: rb_diag<R, U>(v, op, m); break;
-        case kT_SCALE: rb_scale<R, U>(v, m); break;
+        case kT_DIAG: rb_diag<T, U>(v, op, m); break;
+        case kT_SCALE: rb_scale<T, U>(v, m); break;
         default: break;
     }
 }
@@ -472,9 +488,10 @@ __device__ __forceinline__ void rb_apply(Cx<R>* v, int code, const TileOp& op, c
 // Swizzled shared-memory position of tile element i: the bits above a 128-byte bank row are
 // folded into the bank bits by XOR, so the strided group accesses of a register block spread
 // over all banks. A bijection; the linear layout is kept for the bulk copies in and out.
-template <typename R>
+template <typename T>
 __device__ __forceinline__ uint32_t swz(uint32_t i) {
-    constexpr int SH = sizeof(R) == 4 ? 4 : 3;  // complex64: 16 per bank row, complex128: 8
+    // elements per 128-byte bank row: 32 (4 bytes), 16 (8 bytes) or 8 (16 bytes)
+    constexpr int SH = sizeof(T) == 4 ? 5 : sizeof(T) == 8 ? 4 : 3;
     constexpr uint32_t M = (1u << SH) - 1;
     const uint32_t x = i >> SH;
     return i ^ ((x ^ (x >> SH) ^ (x >> (2 * SH))) & M);
@@ -484,9 +501,9 @@ __device__ __forceinline__ uint32_t swz(uint32_t i) {
 // U register bits), reads them in the block's input layout, applies the block's operators and
 // writes them in its output layout. A change of layout needs every read done before any write:
 // the host only asks for one when each thread has at most one group.
-template <typename R, int U>
-__device__ void run_block(Cx<R>* tile, int tbits, const BlockDesc& blk, const TileOp* __restrict__ ops,
-                          const Cx<R>* __restrict__ data, int64_t member, uint64_t pred, const TrajCtx& ctx,
+template <typename T, int U>
+__device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp* __restrict__ ops,
+                          const T* __restrict__ data, int64_t member, uint64_t pred, const TrajCtx& ctx,
                           int64_t cur) {
     const bool sin = blk.in_swz != 0, sout = blk.out_swz != 0;
     const bool relayout = sin != sout;
@@ -496,8 +513,8 @@ __device__ void run_block(Cx<R>* tile, int tbits, const BlockDesc& blk, const Ti
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const uint32_t m = i < U ? (1u << blk.bits[i]) : 0u;
-        min_[i] = sin ? swz<R>(m) : m;
-        mout[i] = sout ? swz<R>(m) : m;
+        min_[i] = sin ? swz<T>(m) : m;
+        mout[i] = sout ? swz<T>(m) : m;
     }
     uint32_t oin[1 << U], oout[1 << U];
 #pragma unroll
@@ -519,23 +536,23 @@ __device__ void run_block(Cx<R>* tile, int tbits, const BlockDesc& blk, const Ti
         uint32_t base = (uint32_t)g;
 #pragma unroll
         for (int i = 0; i < U; ++i) base = ins0(base, blk.sorted[i]);
-        const uint32_t bin = sin ? swz<R>(base) : base;
-        const uint32_t bout = sout ? swz<R>(base) : base;
-        Cx<R> v[1 << U];
+        const uint32_t bin = sin ? swz<T>(base) : base;
+        const uint32_t bout = sout ? swz<T>(base) : base;
+        T v[1 << U];
         if (active) {
 #pragma unroll
             for (int e = 0; e < (1 << U); ++e) v[e] = tile[bin ^ oin[e]];
             for (int o = 0; o < blk.nops; ++o) {
                 const TileOp& op = ops[blk.first + o];
                 if (!((pred >> op.pred) & 1)) continue;
-                const Cx<R>* m = data + op.data + member * op.stride;
+                const T* m = data + op.data + member * op.stride;
                 int code = op.tmpl;
                 if (op.kind == kOpMixture) {
-                    m = mixture_pick<R>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
+                    m = mixture_pick<T>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
                     if (!m) continue;
                     code = (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2));
                 }
-                rb_apply<R, U>(v, code, op, m);
+                rb_apply<T, U>(v, code, op, m);
             }
         }
         if (relayout) cbar();  // uniform: relayout blocks run exactly one round
@@ -546,45 +563,45 @@ __device__ void run_block(Cx<R>* tile, int tbits, const BlockDesc& blk, const Ti
     }
 }
 
-template <typename R>
-__device__ void run_ops(Cx<R>* tile, int tbits, const TileOp* __restrict__ ops, int nops,
-                        const Cx<R>* __restrict__ data, int64_t member, const TrajCtx& ctx) {
+template <typename T>
+__device__ void run_ops(T* tile, int tbits, const TileOp* __restrict__ ops, int nops,
+                        const T* __restrict__ data, int64_t member, const TrajCtx& ctx) {
     const uint64_t pred = ctx.u ? ctx.pred[member] : ~0ull;
     const int64_t cur = ctx.u ? ctx.cursor[member] : 0;
     for (int o = 0; o < nops; ++o) {
         const TileOp& op = ops[o];  // staged in shared memory
         const int kind = op.kind, k = op.k;
-        const Cx<R>* m = data + op.data + member * op.stride;
+        const T* m = data + op.data + member * op.stride;
         if (!((pred >> op.pred) & 1)) continue;  // a branch this member did not take (CTA-uniform)
         cbar();
         if (kind == kOpMixture) {
-            op_mixture<R>(tile, tbits, op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
+            op_mixture<T>(tile, tbits, op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
         } else if (kind == LSG_OP_MATRIX && k == 1) {
-            dense1<R>(tile, tbits, op.lb[0], m);
+            dense1<T>(tile, tbits, op.lb[0], m);
         } else if (kind == LSG_OP_MATRIX && k == 2) {
-            dense2<R>(tile, tbits, op.lb[0], op.lb[1], m);
+            dense2<T>(tile, tbits, op.lb[0], op.lb[1], m);
         } else if (kind == LSG_OP_PERM && k == 1) {
-            perm1<R>(tile, tbits, op.lb[0], m);
+            perm1<T>(tile, tbits, op.lb[0], m);
         } else if (kind == LSG_OP_PERM && k == 2) {
-            perm2<R>(tile, tbits, op.lb[0], op.lb[1], m);
+            perm2<T>(tile, tbits, op.lb[0], op.lb[1], m);
         } else if (kind == LSG_OP_DIAG) {
-            op_diag<R>(tile, tbits, k, op.lb, m);
+            op_diag<T>(tile, tbits, k, op.lb, m);
         } else if (kind == LSG_OP_DEPOL) {
-            if (k == 2) op_depol<R, 1>(tile, tbits, op.lb, op.sorted, m);
-            else op_depol<R, 2>(tile, tbits, op.lb, op.sorted, m);
+            if (k == 2) op_depol<T, 1>(tile, tbits, op.lb, op.sorted, m);
+            else op_depol<T, 2>(tile, tbits, op.lb, op.sorted, m);
         } else if (kind == LSG_OP_SCALE) {
-            op_scale<R>(tile, tbits, m);
+            op_scale<T>(tile, tbits, m);
         } else {
-            wide_op<R>(tile, tbits, kind, k, op.lb, op.sorted, m);
+            wide_op<T>(tile, tbits, kind, k, op.lb, op.sorted, m);
         }
     }
     cbar();
 }
 
 // All blocks of a pass on one tile (the 256 compute threads).
-template <typename R>
-__device__ __forceinline__ void compute_tile(Cx<R>* tile, int K, const PassDesc& pd, const BlockDesc* sblk,
-                                             const TileOp* sops, const Cx<R>* __restrict__ data, int64_t member,
+template <typename T>
+__device__ __forceinline__ void compute_tile(T* tile, int K, const PassDesc& pd, const BlockDesc* sblk,
+                                             const TileOp* sops, const T* __restrict__ data, int64_t member,
                                              const TrajCtx& ctx) {
     const uint64_t pred = ctx.u ? ctx.pred[member] : ~0ull;
     const int64_t cur = ctx.u ? ctx.cursor[member] : 0;
@@ -592,22 +609,22 @@ __device__ __forceinline__ void compute_tile(Cx<R>* tile, int K, const PassDesc&
         const BlockDesc& blk = sblk[bi];
         cbar();
         if (blk.generic) {
-            run_ops<R>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
+            run_ops<T>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
             continue;
         }
         switch (blk.u) {
-            case 1: run_block<R, 1>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-            case 2: run_block<R, 2>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-            case 3: run_block<R, 3>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            case 1: run_block<T, 1>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            case 2: run_block<T, 2>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            case 3: run_block<T, 3>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
             default:
-                if constexpr (sizeof(R) == 4) run_block<R, 4>(tile, K, blk, sops, data, member, pred, ctx, cur);
+                if constexpr (sizeof(T) <= 8) run_block<T, 4>(tile, K, blk, sops, data, member, pred, ctx, cur);
                 break;
         }
     }
     cbar();
 }
 
-template <typename R>
+template <typename T>
 __device__ __forceinline__ void stage_pass(const PassDesc* __restrict__ pass_g, const TileOp* __restrict__ ops,
                                            const BlockDesc* __restrict__ blocks, TileOp* sops, BlockDesc* sblk) {
     const int nops = pass_g->nops;
@@ -628,23 +645,30 @@ __device__ __forceinline__ void stage_pass(const PassDesc* __restrict__ pass_g, 
 // compute and stores of consecutive tiles overlap. Every wait is bounded.
 constexpr int kPipeThreads = 288;
 
-template <typename R>
-__global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict__ state, int64_t member_elems,
+// CTAs per SM the kernels are compiled for: elements of 8 bytes or more in FP64 (complex128,
+// real64) get the larger register budget; the FP64 path is bound by FP64 issue, not occupancy.
+template <typename T>
+constexpr int wide_regs() {
+    return sizeof(typename Elem<T>::R) == 8 ? 1 : 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPipeThreads, 2 - wide_regs<T>()) k_tile_pipe(T* __restrict__ state, int64_t member_elems,
                                                                const PassDesc* __restrict__ pass_g,
                                                                const TileOp* __restrict__ ops,
                                                                const BlockDesc* __restrict__ blocks,
-                                                               const Cx<R>* __restrict__ data, int64_t tiles_per_member,
+                                                               const T* __restrict__ data, int64_t tiles_per_member,
                                                                int64_t total_tiles, int* status, TrajCtx ctx) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t full[2], empty[2];
     __shared__ PassDesc pd;
-    const size_t tile_bytes = sizeof(Cx<R>) << pass_g->K;
-    Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
-    Cx<R>* buf1 = reinterpret_cast<Cx<R>*>(smem_raw + tile_bytes);
+    const size_t tile_bytes = sizeof(T) << pass_g->K;
+    T* buf0 = reinterpret_cast<T*>(smem_raw);
+    T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
     TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + 2 * tile_bytes);
     BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
     if (threadIdx.x == 0) pd = *pass_g;
-    stage_pass<R>(pass_g, ops, blocks, sops, sblk);
+    stage_pass<T>(pass_g, ops, blocks, sops, sblk);
     if (threadIdx.x == 0) {
         mbar_init(&full[0], 1);
         mbar_init(&full[1], 1);
@@ -655,19 +679,19 @@ __global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict
     __syncthreads();
     const int K = pd.K, L = pd.L;
     const int nchunks = 1 << (K - L);
-    const uint32_t chunk_bytes = (uint32_t)(sizeof(Cx<R>) << L);
+    const uint32_t chunk_bytes = (uint32_t)(sizeof(T) << L);
     const int64_t stride = gridDim.x;
     if (threadIdx.x >= 256) {
         // ---------------- producer warp
         const int lane = threadIdx.x - 256;
-        auto tile_at = [&](int64_t t, Cx<R>** mem, uint64_t* base) {
+        auto tile_at = [&](int64_t t, T** mem, uint64_t* base) {
             const int64_t member = t / tiles_per_member;
             const uint64_t tt = (uint64_t)(t - member * tiles_per_member);
             *mem = state + member * member_elems;
             *base = deposit(tt, pd.outer, pd.nouter);
         };
-        auto store = [&](int64_t t, Cx<R>* buf) {
-            Cx<R>* mem;
+        auto store = [&](int64_t t, T* buf) {
+            T* mem;
             uint64_t base;
             tile_at(t, &mem, &base);
             for (int c = lane; c < nchunks; c += 32)
@@ -679,7 +703,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict
         int64_t it = 0;
         for (int64_t t = blockIdx.x; t < total_tiles; t += stride, ++it) {
             const int b = (int)(it & 1);
-            Cx<R>* buf = b ? buf1 : buf0;
+            T* buf = b ? buf1 : buf0;
             if (it >= 2) {  // buffer b still holds tile it-2: wait for its compute, store it
                 const bool ok = mbar_wait_bounded(&empty[b], (uint32_t)(((it >> 1) - 1) & 1), status);
                 if (!ok) {
@@ -688,7 +712,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict
                 }
                 store(t - 2 * stride, buf);
             }
-            Cx<R>* mem;
+            T* mem;
             uint64_t base;
             tile_at(t, &mem, &base);
             if (lane == 0) mbar_arrive_expect_tx(&full[b], chunk_bytes * (uint32_t)nchunks);
@@ -714,11 +738,11 @@ __global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict
     int64_t it = 0;
     for (int64_t t = blockIdx.x; t < total_tiles; t += stride, ++it) {
         const int b = (int)(it & 1);
-        Cx<R>* tile = b ? buf1 : buf0;
+        T* tile = b ? buf1 : buf0;
         const bool ok = mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), status);
         if (cbar_or(!ok)) return;  // every compute thread leaves together on a timeout
         const int64_t member = t / tiles_per_member;
-        compute_tile<R>(tile, K, pd, sblk, sops, data, member, ctx);
+        compute_tile<T>(tile, K, pd, sblk, sops, data, member, ctx);
         fence_proxy_async_smem();  // this thread's writes, before the producer's bulk store reads them
         mbar_arrive(&empty[b]);
     }
@@ -726,17 +750,17 @@ __global__ void __launch_bounds__(kPipeThreads, 2) k_tile_pipe(Cx<R>* __restrict
 
 // One fused pass over every tile of every member. Tiles are visited grid-stride; each CTA
 // handles one tile at a time (CTAs co-resident on an SM overlap each other's copies).
-template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_tile_pass(Cx<R>* __restrict__ state, int64_t member_elems,
+template <typename T>
+__global__ void __launch_bounds__(256, 3 - wide_regs<T>()) k_tile_pass(T* __restrict__ state, int64_t member_elems,
                                                    const PassDesc* __restrict__ pass_g,
                                                    const TileOp* __restrict__ ops, const BlockDesc* __restrict__ blocks,
-                                                   const Cx<R>* __restrict__ data, int64_t tiles_per_member,
+                                                   const T* __restrict__ data, int64_t tiles_per_member,
                                                    int64_t total_tiles, int* status, TrajCtx ctx) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t bar;
     __shared__ PassDesc pd;
-    Cx<R>* tile = reinterpret_cast<Cx<R>*>(smem_raw);
-    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + (sizeof(Cx<R>) << pass_g->K));
+    T* tile = reinterpret_cast<T*>(smem_raw);
+    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + (sizeof(T) << pass_g->K));
     BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
     if (threadIdx.x == 0) pd = *pass_g;
     {
@@ -758,13 +782,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_tile_pass(Cx<R>
     __syncthreads();
     const int K = pd.K, L = pd.L;
     const int nchunks = 1 << (K - L);
-    const uint32_t chunk_bytes = (uint32_t)(sizeof(Cx<R>) << L);
+    const uint32_t chunk_bytes = (uint32_t)(sizeof(T) << L);
     const bool use_bulk = (chunk_bytes % 16) == 0;
     uint32_t parity = 0;
     for (int64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
         const int64_t member = t / tiles_per_member;
         const uint64_t tt = (uint64_t)(t - member * tiles_per_member);
-        Cx<R>* mem = state + member * member_elems;
+        T* mem = state + member * member_elems;
         const uint64_t base = deposit(tt, pd.outer, pd.nouter);
         // ---- load
         if (use_bulk) {
@@ -787,7 +811,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_tile_pass(Cx<R>
         }
         // ---- compute: register blocks, or one shared-memory operator for a wide block
         __syncthreads();
-        compute_tile<R>(tile, K, pd, sblk, sops, data, member, ctx);
+        compute_tile<T>(tile, K, pd, sblk, sops, data, member, ctx);
         __syncthreads();
         // ---- store
         if (use_bulk) {

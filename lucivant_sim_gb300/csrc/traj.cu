@@ -29,7 +29,8 @@ struct lsg_program_s;
 namespace lsg {
 
 int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
-                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out);
+                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out,
+                      cudaStream_t stream);
 int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx);
 void program_destroy(lsg_program_s* p);
 int op_bits_ok(const lsg_op& op, int nbits);
@@ -470,6 +471,7 @@ int lsg_traj_create(lsg_state shape, const lsg_traj_op* ops, int32_t nops, const
     if (!shape || !out || nops < 0 || (nops && !ops) || pool_entries < 0 || (pool_entries && !pool))
         return fail(LSG_E_ARG, "lsg_traj_create: bad arguments");
     *out = nullptr;
+    if (shape->real()) return fail(LSG_E_ARG, "trajectories run on statevector registers");
     if (num_clbits < 0 || num_clbits > 64 * kMaxWords)
         return fail(LSG_E_CAPACITY, "trajectories on the device keep at most %d classical bits", 64 * kMaxWords);
     const int nbits = shape->nbits;
@@ -501,7 +503,8 @@ int lsg_traj_create(lsg_state shape, const lsg_traj_op* ops, int32_t nops, const
         sp.kind = STEP_SEG;
         sp.slot = seg_slot;
         int rc = program_create_ex(nbits, shape->precision, shape->batch, seg_ops.data(), (int32_t)seg_ops.size(), pool,
-                                   pool_entries, seg_pred.data(), seg_draw.data(), seg_count.data(), &sp.seg);
+                                   pool_entries, seg_pred.data(), seg_draw.data(), seg_count.data(), &sp.seg,
+                                   shape->stream);
         if (rc != LSG_OK) return rc;
         t->steps.push_back(sp);
         if (seg_draws) {

@@ -198,6 +198,247 @@ def dm_oplist(circuit: Any, noises: list[Any]) -> OpList:
     return ops
 
 
+# ---------------------------------------------------------------------------- Pauli-transfer form
+#
+# A density register in Pauli-transfer form holds r_P = Tr(P rho) for every n-qubit Pauli P: real,
+# 4^n of them, in a register of 2n bits where qubit q's Pauli digit sits in bits (n+q, q) = (x, z)
+# (I = 00, Z = 01, X = 10, Y = 11). A channel E on k qubits acts as the real 4^k x 4^k matrix
+# R[P', P] = 2^-k Tr(P' E(P)) on the digits of its qubits, listed (x bits, then z bits) the way
+# the vectorised form lists (row bits, then column bits). Half the bytes of the complex
+# vectorised form, and a one-qubit channel costs 4 real multiply-adds per element instead of 16.
+
+PAULI_DIGITS = (
+    np.eye(2, dtype=np.complex128),  # I: x=0 z=0
+    np.array([[1, 0], [0, -1]], dtype=np.complex128),  # Z: x=0 z=1
+    np.array([[0, 1], [1, 0]], dtype=np.complex128),  # X: x=1 z=0
+    np.array([[0, -1j], [1j, 0]], dtype=np.complex128),  # Y: x=1 z=1
+)
+
+REAL_OF = {_lib.C128: _lib.R64, _lib.C64: _lib.R32}
+
+
+def _pauli_basis(k: int) -> list[np.ndarray]:
+    """The 4^k Paulis in digit-index order: index bits (x_0..x_{k-1}, z_0..z_{k-1}), MSB first;
+    qubit 0 of the operator is the most significant tensor factor (as in gate matrices)."""
+    out = []
+    for j in range(4**k):
+        xs = [(j >> (2 * k - 1 - i)) & 1 for i in range(k)]
+        zs = [(j >> (k - 1 - i)) & 1 for i in range(k)]
+        m = np.ones((1, 1), dtype=np.complex128)
+        for x, z in zip(xs, zs, strict=True):
+            m = np.kron(m, PAULI_DIGITS[2 * x + z])
+        out.append(m)
+    return out
+
+
+_BASIS_CACHE: dict[int, tuple[np.ndarray, np.ndarray]] = {}
+
+
+def _basis(k: int) -> tuple[np.ndarray, np.ndarray]:
+    """(B, Bc): B[j] = vec(P_j) row-major, Bc = conj for the trace."""
+    hit = _BASIS_CACHE.get(k)
+    if hit is None:
+        b = np.stack([p.reshape(-1) for p in _pauli_basis(k)])
+        hit = _BASIS_CACHE[k] = (b, b.conj())
+    return hit
+
+
+def ptm_of_superop(s: np.ndarray, k: int) -> np.ndarray:
+    """Real Pauli-transfer matrix of a superoperator given on vectorised (row-major) matrices."""
+    b, _bc = _basis(k)
+    # R[a, c] = 2^-k Tr(P_a E(P_c)) = 2^-k sum_ij P_a[j, i] E(P_c)[i, j] = 2^-k vec(P_a^T) . (S vec(P_c))
+    bt = np.stack([p.T.reshape(-1) for p in _pauli_basis(k)])
+    r = (bt @ s @ b.T) / (1 << k)
+    if np.max(np.abs(r.imag), initial=0.0) > 1e-12:
+        raise SimulationError("a channel without a real Pauli-transfer matrix (not Hermiticity-preserving)")
+    return np.ascontiguousarray(r.real)
+
+
+def ptm_of_unitary(u: np.ndarray) -> np.ndarray:
+    k = int(np.log2(u.shape[0]))
+    return ptm_of_superop(np.kron(u, u.conj()), k)
+
+
+def ptm_of_kraus(kraus: Any, k: int) -> np.ndarray:
+    return ptm_of_superop(superop(kraus), k)
+
+
+def ptm_depolarizing(p: float, k: int) -> np.ndarray:
+    """(1-p) rho + p I/d Tr rho: r_I kept, every other coefficient scaled by 1-p."""
+    d = np.full(4**k, 1.0 - p)
+    d[0] = 1.0
+    return np.diag(d)
+
+
+def _signed_perm(r: np.ndarray) -> tuple[np.ndarray, np.ndarray] | None:
+    """(src, phase) with R[i, src[i]] = phase[i] the only nonzero of row i, or None."""
+    nz = r != 0
+    if not ((nz.sum(axis=1) == 1).all() and (nz.sum(axis=0) == 1).all()):
+        return None
+    src = nz.argmax(axis=1)
+    return src, r[np.arange(r.shape[0]), src]
+
+
+def _renames(src: np.ndarray, nbits: int) -> list[tuple[str, int, int]] | None:
+    """Decompose a permutation of bit patterns (out[r] = in[src[r]]) that is linear over GF(2)
+    into bit CX / SWAP renames, in application order: [("cx", control, target) | ("swap", a, b)]
+    on operator positions (0 = most significant). None when src is not linear."""
+    d = 1 << nbits
+    if src[0] != 0:
+        return None
+    for r in range(d):
+        acc = 0
+        for pbit in range(nbits):
+            if (r >> pbit) & 1:
+                acc ^= int(src[1 << pbit])
+        if acc != int(src[r]):
+            return None
+
+    def vec(x: int) -> list[int]:
+        return [(x >> (nbits - 1 - p)) & 1 for p in range(nbits)]
+
+    # B[:, p] = vec(src(e_p)) where e_p has only position p set
+    cols = [vec(int(src[1 << (nbits - 1 - p)])) for p in range(nbits)]
+    b = np.array(cols, dtype=np.uint8).T  # b[row, col]
+    steps: list[tuple[str, int, int]] = []  # column operations F_1.. reducing B to I
+    for i in range(nbits):
+        piv = next(j for j in range(i, nbits) if b[i, j])
+        if piv != i:
+            b[:, [i, piv]] = b[:, [piv, i]]
+            steps.append(("swap", i, piv))
+        for c in range(nbits):
+            if c != i and b[i, c]:
+                b[:, c] ^= b[:, i]
+                steps.append(("cx", c, i))  # F = I + E[i, c]: adds column i into column c
+    assert (b == np.eye(nbits, dtype=np.uint8)).all()
+    return steps[::-1]
+
+
+_CX_SRC = np.array([1, 1, 1, 1, 0, 1, 3, 2], dtype=np.complex128)  # unit phases, src [0, 1, 3, 2]
+_SWAP_SRC = np.array([1, 1, 1, 1, 0, 2, 1, 3], dtype=np.complex128)
+
+
+def _add_ptm(ops: OpList, bits: list[int], mats: list[np.ndarray]) -> None:
+    """Append one Pauli-transfer operator (one matrix per member, or one shared), as the cheapest
+    kind that represents it exactly: diagonal, bit renames plus a diagonal, or dense."""
+    first = mats[0]
+    nb = len(bits)
+    shared = all(m is first or np.array_equal(m, first) for m in mats[1:])
+    if all(not np.any(m - np.diag(np.diagonal(m))) for m in mats):
+        diags = [np.diagonal(m).astype(np.complex128) for m in mats]
+        if shared:
+            if not np.all(diags[0] == 1.0):
+                ops.add(OP_DIAG, bits, diags[0])
+        else:
+            ops.add_batched(OP_DIAG, bits, np.stack(diags))
+        return
+    sp = [_signed_perm(m) for m in mats]
+    if all(x is not None for x in sp) and all(np.array_equal(x[0], sp[0][0]) for x in sp[1:]):
+        src = sp[0][0]
+        steps = _renames(src, nb)
+        if steps is not None:
+            for kind, a, b in steps:
+                ops.add(OP_PERM, [bits[a], bits[b]], _CX_SRC if kind == "cx" else _SWAP_SRC)
+            phases = [x[1].astype(np.complex128) for x in sp]
+            if shared or all(np.array_equal(ph, phases[0]) for ph in phases[1:]):
+                if not np.all(phases[0] == 1.0):
+                    ops.add(OP_DIAG, bits, phases[0])
+            else:
+                ops.add_batched(OP_DIAG, bits, np.stack(phases))
+            return
+    if shared:
+        ops.add(OP_MATRIX, bits, first.astype(np.complex128))
+    else:
+        ops.add_batched(OP_MATRIX, bits, np.stack(mats).astype(np.complex128))
+
+
+def ptm_capable(circuit: Any, noises: list[Any]) -> bool:
+    """The Pauli-transfer form takes gates and channels on up to two qubits (wider ones would be
+    4^k-dense real operators); otherwise the complex vectorised form is used."""
+    for op in circuit.operations:
+        if op.kind == "gate" and len(op.qubits) > 2:
+            return False
+    return True
+
+
+def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
+    """The noisy static evolution of :func:`dm_oplist` as Pauli-transfer operators: each gate
+    with its channel is ONE real operator on the (x, z) digits of its qubits."""
+    n = circuit.num_qubits
+    ops = OpList()
+    cache: dict[int, tuple[Any, np.ndarray]] = {}
+
+    def chan_ptm(ch: Any, k: int) -> np.ndarray:
+        hit = cache.get(id(ch))
+        if hit is None or hit[0] is not ch:
+            r = ptm_depolarizing(ch.params[0], k) if ch.analytic_depolarizing else ptm_of_kraus(ch.kraus, k)
+            hit = cache[id(ch)] = (ch, r)
+        return hit[1]
+
+    for op in circuit.operations:
+        if op.kind == "gate":
+            qs = tuple(op.qubits)
+            k = len(qs)
+            if k > 2:
+                raise SimulationError("the Pauli-transfer form takes gates on up to two qubits")
+            chans = [nm.gate_error(op.name, qs) if nm is not None else None for nm in noises]
+            present = [c is not None for c in chans]
+            if any(present) and not all(present):
+                raise ValueError("batched noise models must attach channels to the same gates")
+            r_gate = ptm_of_unitary(np.asarray(op.matrix, dtype=np.complex128))
+            mats = [chan_ptm(ch, k) @ r_gate for ch in chans] if chans[0] is not None else [r_gate]
+            _add_ptm(ops, [n + q for q in qs] + list(qs), mats)
+        elif op.kind == "reset":
+            _add_ptm(ops, [n + op.qubit, op.qubit], [ptm_of_kraus(RESET_KRAUS, 1)])
+        # measurements are deferred; a global phase leaves a density matrix unchanged
+    return ops
+
+
+def ptm_to_density_ops(n: int) -> OpList:
+    """Per-qubit change of basis from Pauli-transfer coefficients (loaded as real amplitudes of a
+    complex register) to the vectorised density matrix: rho[row, col] = 2^-n sum_P r_P P[row, col]."""
+    t = np.zeros((4, 4), dtype=np.complex128)
+    for d, pm in enumerate(PAULI_DIGITS):
+        for row in range(2):
+            for col in range(2):
+                t[2 * row + col, d] = pm[row, col] / 2
+    ops = OpList()
+    for q in range(n):
+        ops.add(OP_MATRIX, [n + q, q], t)
+    return ops
+
+
+def dm_form(circuit: Any, noises: list[Any]) -> str:
+    """"ptm" (the default) or "superop", from ``LSG_DM_FORM`` and what the circuit needs."""
+    want = os.environ.get("LSG_DM_FORM", "ptm")
+    if want not in ("ptm", "superop"):
+        raise ValueError("LSG_DM_FORM must be ptm or superop")
+    return "ptm" if want == "ptm" and ptm_capable(circuit, noises) else "superop"
+
+
+def evolve_density(circuit: Any, noises: list[Any], precision: int) -> _lib.Register:
+    """A density register (one member per noise model) evolved through ``circuit``."""
+    n = circuit.num_qubits
+    if dm_form(circuit, noises) == "ptm":
+        reg = new_density(n, REAL_OF[precision], len(noises))
+        reg.apply(ptm_oplist(circuit, noises))
+    else:
+        reg = new_density(n, precision, len(noises))
+        reg.apply(dm_oplist(circuit, noises))
+    return reg
+
+
+def density_download(reg: _lib.Register, member: int = 0) -> np.ndarray:
+    """Member ``member`` of a density register as a (2^n, 2^n) complex128 matrix."""
+    n = reg.nbits // 2
+    if reg.precision in (_lib.C128, _lib.C64):
+        return reg.download()[member].reshape(1 << n, 1 << n)
+    with _lib.Register(reg.nbits, _lib.C128) as out:
+        reg.to_complex(member, out)
+        out.apply(ptm_to_density_ops(n))
+        return out.download()[0].reshape(1 << n, 1 << n)
+
+
 def pauli_masks(label: str) -> tuple[int, int]:
     """(x mask, z mask) of a Pauli label, qubit 0 rightmost; Y sets both."""
     xm = zm = 0
@@ -218,6 +459,7 @@ def new_statevector(n: int, precision: int = _lib.C128, batch: int = 1) -> _lib.
 
 
 def new_density(n: int, precision: int = _lib.C128, batch: int = 1) -> _lib.Register:
+    """A density register of n qubits: complex vectorised (C128/C64) or Pauli-transfer (R64/R32)."""
     if n > MAX_DENSITY_QUBITS:
         raise SimulationError(
             f"{n} qubits need more memory than the density-matrix engine allows "

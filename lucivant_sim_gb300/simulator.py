@@ -213,9 +213,7 @@ def _evolved(circuit: Any, noise: Any, precision: int) -> tuple[_lib.Register, i
     """The final static state on the device: statevector if ideal, density matrix if gate noise."""
     n = circuit.num_qubits
     if noise is not None and noise.has_gate_errors():
-        reg = engine.new_density(n, precision)
-        reg.apply(engine.dm_oplist(circuit, [noise]))
-        return reg, n
+        return engine.evolve_density(circuit, [noise], precision), n
     reg = engine.new_statevector(n, precision)
     reg.apply(engine.sv_oplist(circuit, fuse=True))
     return reg, 0
@@ -268,8 +266,7 @@ def run(
             reg.apply(engine.sv_oplist(circuit, fuse=True))
             dm = 0
         else:
-            reg = engine.new_density(n, prec)
-            reg.apply(engine.dm_oplist(circuit, [noise]))
+            reg = engine.evolve_density(circuit, [noise], prec)
             dm = n
         with reg:
             if chosen == "statevector":
@@ -312,9 +309,8 @@ def density_matrix(program: Any, noise: Any = None, params: Mapping[str, float] 
     circuit = to_circuit(program, params)
     _static(circuit, "a density matrix")
     n = circuit.num_qubits
-    with engine.new_density(n, engine.precision_code(precision)) as reg:
-        reg.apply(engine.dm_oplist(circuit, [noise]))
-        return reg.download()[0].reshape(1 << n, 1 << n)
+    with engine.evolve_density(circuit, [noise], engine.precision_code(precision)) as reg:
+        return engine.density_download(reg)
 
 
 def probabilities_array(program: Any, noise: Any = None, params: Mapping[str, float] | None = None, *,

@@ -191,3 +191,52 @@ def z_observables(n: int) -> list[str]:
         lab[n - 2 - i] = "Z"
         labels.append("".join(lab))
     return labels
+
+
+def hea_template(n: int, layers: int) -> str:
+    """A hardware-efficient ansatz with one ``input float`` per rotation (p0, p1, ...): ry and rz
+    on every qubit per layer, then a linear cx chain."""
+    names = [f"p{i}" for i in range(2 * n * layers)]
+    lines = ["OPENQASM 3.0;", 'include "stdgates.inc";'] + [f"input float {v};" for v in names] + [f"qubit[{n}] q;"]
+    k = 0
+    for _layer in range(layers):
+        for q in range(n):
+            lines.append(f"ry({names[k]}) q[{q}];")
+            lines.append(f"rz({names[k + 1]}) q[{q}];")
+            k += 2
+        for a in range(n - 1):
+            lines.append(f"cx q[{a}], q[{a + 1}];")
+    return "\n".join(lines) + "\n"
+
+
+def served_mix(jobs: int = 2000, rate: float = 200.0, seed: int = 5, shots: int = 1000, sweep: int = 8,
+               widths: tuple[int, int] = (8, 26), depths: tuple[int, int] = (10, 100)) -> list[dict]:  # fmt: skip
+    """The served mix: Poisson arrivals at ``rate`` jobs/s; widths uniform over ``widths`` (8..26)
+    and depths over ``depths`` (10..100), u3+cx brickwork. 30% are hardware-efficient-ansatz sweeps (``sweep`` parameter
+    sets of one template, angles U[0, 2π)) measured on a 20-term random Pauli sum with N(0, 1)
+    coefficients; 20% carry uniform noise (1e-3, 1e-2, readout 2e-2) on the density-matrix path
+    at the three smallest widths (8..10); the rest are sampled with ``shots`` shots. Every job is OpenQASM text."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=jobs))
+    out = []
+    for i in range(jobs):
+        u = rng.uniform()
+        depth = int(rng.integers(depths[0], depths[1] + 1))
+        job_seed = int(rng.integers(0, 2**31))
+        if u < 0.3:
+            n = int(rng.integers(widths[0], widths[1] + 1))
+            layers = max(1, depth // 10)
+            params = [dict(zip([f"p{k}" for k in range(2 * n * layers)],
+                               np.random.default_rng(job_seed + s).uniform(0, TWO_PI, size=2 * n * layers).tolist()))
+                      for s in range(sweep)]  # fmt: skip
+            out.append(dict(kind="expect", arrival=float(arrivals[i]), qasm=hea_template(n, layers), params=params,
+                            observable=random_pauli_sum(n, 20, job_seed), width=n, depth=layers))
+        elif u < 0.5:
+            n = int(rng.integers(widths[0], min(widths[0] + 2, widths[1]) + 1))
+            out.append(dict(kind="density", arrival=float(arrivals[i]), qasm=brickwork(n, depth, seed=job_seed),
+                            shots=shots, seed=job_seed, width=n, depth=depth))
+        else:
+            n = int(rng.integers(widths[0], widths[1] + 1))
+            out.append(dict(kind="sample", arrival=float(arrivals[i]), qasm=brickwork(n, depth, seed=job_seed),
+                            shots=shots, seed=job_seed, width=n, depth=depth))
+    return out

@@ -30,6 +30,13 @@ def tile_bits(request, monkeypatch):
     return request.param
 
 
+@pytest.fixture(params=["ptm", "superop"])
+def dm_form(request, monkeypatch):
+    """Density matrices in Pauli-transfer form (real, the default) and complex vectorised form."""
+    monkeypatch.setenv("LSG_DM_FORM", request.param)
+    return request.param
+
+
 def test_statevector_golden(golden, golden_arrays, tile_bits):
     for case, key in (("sv_bw8", "sv_bw8_state"), ("sv_gates", "sv_gates_state")):
         got = ls.statevector(golden[case]["qasm"])
@@ -53,7 +60,7 @@ def _dm_noise():
     )
 
 
-def test_density_matrix_golden(golden, golden_arrays, tile_bits):
+def test_density_matrix_golden(golden, golden_arrays, tile_bits, dm_form):
     g = golden["dm_bw4"]
     rho = ls.density_matrix(g["qasm"], _dm_noise())
     assert np.max(np.abs(rho - golden_arrays["dm_bw4_rho"])) < ATOL_C128
@@ -66,7 +73,7 @@ def test_density_matrix_golden(golden, golden_arrays, tile_bits):
     assert all(abs(got[k] - v) < ATOL_C128 for k, v in g["outcome_probabilities"].items())
 
 
-def test_every_channel_kind(golden, golden_arrays):
+def test_every_channel_kind(golden, golden_arrays, dm_form):
     g = golden["dm_channels"]
     noise = (
         NoiseModel()
@@ -83,7 +90,7 @@ def test_every_channel_kind(golden, golden_arrays):
     assert np.max(np.abs(rho - golden_arrays["dm_channels_rho"])) < ATOL_C128
 
 
-def test_expectation_golden(golden):
+def test_expectation_golden(golden, dm_form):
     g = golden["expect_hea6"]
     assert abs(ls.expectation(g["qasm"], g["observable"]) - g["ideal"]) < ATOL_C128
     assert abs(ls.expectation(g["qasm"], g["observable"], NoiseModel.uniform(single=5e-3, two=2e-2)) - g["noisy"]) < ATOL_C128
@@ -101,7 +108,7 @@ def test_random_brickwork_against_oracle(n, tile_bits):
 
 
 @pytest.mark.parametrize("n", [3, 7])
-def test_noisy_dm_against_oracle(n, tile_bits):
+def test_noisy_dm_against_oracle(n, tile_bits, dm_form):
     src = wl.brickwork(n, 3, seed=200 + n)
     c = ls.parse(src)
     noise = _dm_noise()
@@ -117,7 +124,7 @@ def test_complex64_statevector_tvd():
     assert tvd(got, want) < TVD_C64
 
 
-def test_complex64_density_tvd():
+def test_complex64_density_tvd(dm_form):
     c = ls.parse(wl.brickwork(6, 6, seed=6))
     want = dense.probabilities_array(c, _dm_noise())
     got = ls.probabilities_array(c, _dm_noise(), precision="c64")
@@ -170,6 +177,50 @@ def test_batched_noise_instances():
         assert np.max(np.abs(out[b] - dense.evolve_dm(c, nm))) < ATOL_C128
 
 
+@pytest.mark.parametrize("precision", ["c128", "c64"])
+def test_batched_pauli_transfer_instances(precision):
+    """Noise instances of one circuit in one Pauli-transfer register: probabilities and Z
+    observables of every member against the oracle's density matrix."""
+    from lucivant_sim_gb300.batch import DensityBatch
+
+    c = ls.parse(wl.brickwork(5, 4, seed=31, measure=False))
+    noises = wl.dm_noise_instances(6, seed=3)
+    labels = wl.z_observables(5)
+    b = DensityBatch(c, noises, precision=precision)
+    try:
+        assert b.form == "ptm" and b.reg.real
+        b.evolve()
+        probs, exps = b.probabilities(), b.expectations(labels)
+    finally:
+        b.free()
+    tol = ATOL_C128 if precision == "c128" else 2e-6
+    for i, nm in enumerate(noises):
+        want = dense.probabilities_array(c, nm)
+        assert (np.max(np.abs(probs[i] - want)) < tol) if precision == "c128" else (tvd(probs[i], want) < TVD_C64)
+        for t, lab in enumerate(labels):
+            assert abs(exps[t, i] - dense.expectation(c, lab, nm)) < tol
+
+
+def test_pauli_transfer_register_basics():
+    """Basis states, downloads and conversion of a real register; statevector-only calls refuse it."""
+    with _lib.Register(6, _lib.R64) as reg:
+        reg.set_basis(5)  # |101><101| on 3 qubits
+        r = reg.download()[0]
+        z = np.arange(8)
+        want = np.zeros(64)
+        want[:8] = [(-1) ** bin(int(v) & 5).count("1") for v in z]
+        assert np.array_equal(r, want)
+        rho = engine.density_download(reg)
+        expect = np.zeros((8, 8), dtype=np.complex128)
+        expect[5, 5] = 1
+        assert np.max(np.abs(rho - expect)) < 1e-15
+        assert np.allclose(reg.probabilities(3), np.eye(8)[5])
+        with pytest.raises(_lib.EngineError, match="statevector register"):
+            reg.prob_one(0)
+    with pytest.raises(ValueError, match="even number"):
+        _lib.Register(5, _lib.R32)
+
+
 def test_full_size_config1_parity():
     """20 qubits x 20 brickwork layers, 10,000 shots, seed 7: statevector to 1e-12, counts identical."""
     src = wl.brickwork(20, 20, seed=7)
@@ -182,6 +233,15 @@ def test_full_size_config1_parity():
     # any difference must come from a shot flagged as lying on a CDF boundary
     assert not diff or r.report.get("near_boundary", 0) > 0
     assert abs(np.vdot(r.statevector, r.statevector).real - 1) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64"])
+def test_deep_circuit_on_few_qubits(precision):
+    """More operators than one pass holds: the plan splits them and the state is unchanged."""
+    c = ls.parse(wl.brickwork(10, 150, seed=12))
+    want = dense.evolve_sv(c)
+    got = ls.statevector(c, precision=precision)
+    assert np.max(np.abs(got - want)) < (ATOL_C128 if precision == "c128" else 2e-5)
 
 
 def test_capacity_errors():

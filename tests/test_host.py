@@ -34,14 +34,14 @@ def test_library_exports_every_declared_symbol():
     assert lib.lsg_version() >= 1 and lib.lsg_max_bits() == 26
 
 
-def run_oplist(ops: _lib.OpList, nbits: int, state: np.ndarray) -> np.ndarray:
+def run_oplist(ops: _lib.OpList, nbits: int, state: np.ndarray, member: int = 0) -> np.ndarray:
     """Reference interpreter of an operator list (what the device does, one operator at a time)."""
     table, pool = ops.packed()
     cpool = pool.view(np.complex128)
     v = state.astype(np.complex128).copy()
     for row in table:
         kind, k, bits = int(row["kind"]), int(row["nbits"]), [int(b) for b in row["bits"][: row["nbits"]]]
-        at = int(row["data"])
+        at = int(row["data"]) + member * int(row["batch_stride"])
         if kind == _lib.OP_SCALE:
             v = v * cpool[at]
             continue
@@ -85,6 +85,76 @@ def test_density_oplist_means_the_circuit(golden):
     rho0[0] = 1
     got = run_oplist(engine.dm_oplist(c, [noise]), 2 * n, rho0)
     assert np.max(np.abs(got - dense.evolve_dm(c, noise))) < 1e-12
+
+
+def _ptm_density(ops: _lib.OpList, n: int) -> np.ndarray:
+    """Run a Pauli-transfer operator list from |0><0| and convert to the density matrix."""
+    r0 = np.zeros(1 << (2 * n), dtype=np.complex128)
+    r0[: 1 << n] = 1  # Tr(P |0><0|) = 1 for the diagonal Paulis
+    r = run_oplist(ops, 2 * n, r0)
+    assert not np.any(r.imag)
+    return run_oplist(engine.ptm_to_density_ops(n), 2 * n, r)
+
+
+def test_pauli_transfer_oplist_means_the_circuit(golden):
+    """The real Pauli-transfer operators evolve the same density matrix as Orrery (every channel
+    kind of the golden case, resets, Clifford and non-Clifford two-qubit gates)."""
+    c = ls.parse(golden["dm_channels"]["qasm"])
+    noise = (
+        NoiseModel()
+        .add_gate_error(ls.amplitude_damping(0.1), gates="h")
+        .add_gate_error(ls.pauli_channel({"XY": 0.03, "ZZ": 0.02}), gates="cx")
+        .add_gate_error(depolarizing(0.2, 2), gates="cz")
+        .add_gate_error(thermal_relaxation(50, 40, 3.0), qubits=[2])
+    )
+    assert engine.ptm_capable(c, [noise])
+    got = _ptm_density(engine.ptm_oplist(c, [noise]), c.num_qubits)
+    assert np.max(np.abs(got - dense.evolve_dm(c, noise).reshape(-1))) < 1e-12
+    src = ("OPENQASM 3; include \"stdgates.inc\"; qubit[3] q; h q[0]; s q[1]; cx q[0], q[2]; cz q[1], q[2];"
+           " swap q[0], q[1]; rzz(0.3) q[0], q[2]; cy q[2], q[0]; sx q[1]; t q[2]; reset q[1]; crx(0.4) q[1], q[0];"
+           " ecr q[0], q[2];")
+    c = ls.parse(src)
+    for nm in (None, wl.dm_noise()):
+        got = _ptm_density(engine.ptm_oplist(c, [nm]), 3)
+        assert np.max(np.abs(got - dense.evolve_dm(c, nm).reshape(-1))) < 1e-12
+    assert not engine.ptm_capable(ls.parse("OPENQASM 3; qubit[3] q; ccx q[0], q[1], q[2];"), [None])
+
+
+def test_pauli_transfer_cx_is_renames_and_signs():
+    """A noisy cx becomes bit renames (no arithmetic) plus one diagonal: signs and the
+    depolarising factor; a noisy u3 one dense 4x4 real operator."""
+    c = ls.parse("OPENQASM 3; include \"stdgates.inc\"; qubit[2] q; cx q[0], q[1]; u3(0.1, 0.2, 0.3) q[0];")
+    ops = engine.ptm_oplist(c, [wl.dm_noise()])
+    kinds = [row[0] for row in ops.rows]
+    assert kinds.count(_lib.OP_PERM) >= 2 and kinds.count(_lib.OP_DIAG) == 1 and kinds[-1] == _lib.OP_MATRIX
+    assert all(row[1] == 2 for row in ops.rows if row[0] == _lib.OP_PERM)
+
+
+def test_gf2_linear_permutations_decompose_into_renames():
+    rng = np.random.default_rng(1)
+    for nb in (2, 3, 4):
+        for _ in range(20):
+            while True:
+                m = rng.integers(0, 2, size=(nb, nb))
+                if round(abs(np.linalg.det(m))) % 2 == 1:
+                    break
+            def apply(mat, r):
+                v = np.array([(r >> (nb - 1 - p)) & 1 for p in range(nb)])
+                w = mat.dot(v) % 2
+                return int(sum(int(b) << (nb - 1 - p) for p, b in enumerate(w)))
+            src = np.array([apply(m, r) for r in range(1 << nb)])
+            steps = engine._renames(src, nb)
+            cur = np.arange(1 << nb)  # out[r] = in[cur[r]] after the steps so far
+            for kind, a, b in steps:
+                def one(r, kind=kind, a=a, b=b):
+                    ba, bb = (r >> (nb - 1 - a)) & 1, (r >> (nb - 1 - b)) & 1
+                    if kind == "cx":
+                        return r ^ (ba << (nb - 1 - b))
+                    return r ^ ((ba ^ bb) << (nb - 1 - a)) ^ ((ba ^ bb) << (nb - 1 - b))
+                cur = np.array([cur[one(r)] for r in range(1 << nb)])
+            assert np.array_equal(cur, src)
+    assert engine._renames(np.array([1, 0, 2, 3]), 2) is None  # moves 0: not linear
+    assert engine._renames(np.array([0, 1, 2, 4, 3, 5, 6, 7]), 3) is None
 
 
 def test_matrix_classes():
@@ -167,9 +237,49 @@ def test_plans_are_well_formed(monkeypatch, tile, low):
         (engine.sv_oplist(ls.parse("OPENQASM 3; qubit[6] q; h q; ccx q[0], q[3], q[5]; c4x q[5], q[1], q[2], q[0], q[4]; "
                                    "rz(0.3) q[2]; gphase(0.2); rzz(0.4) q[1], q[4];")), 6),
     ]
+    cases.append((engine.ptm_oplist(ls.parse(wl.brickwork(4, 3, seed=2, measure=False)), [wl.dm_noise()]), 8))
     for ops, nbits in cases:
-        for precision in (_lib.C128, _lib.C64):
+        for precision in (_lib.C128, _lib.C64, _lib.R64, _lib.R32):
             try:
                 assert _lib.plan_passes(nbits, precision, ops) >= 1
             except ValueError as exc:  # a tile too small for a wide operator is refused, never malformed
                 assert "does not fit" in str(exc), exc
+
+
+def test_served_jobs_prepare_to_their_circuits():
+    """A served parameter sweep is one batched operator list whose member b is parameter set b;
+    sampled and noisy jobs carry the same operator lists as the direct API."""
+    from lucivant_sim_gb300 import serve
+
+    jobs = wl.served_mix(40, seed=11, widths=(3, 6), depths=(2, 12), sweep=3)
+    kinds = {j["kind"] for j in jobs}
+    assert kinds == {"expect", "density", "sample"}
+    for job in jobs:
+        prep = serve.prepare(job)
+        if job["kind"] == "expect":
+            sweep = serve.sweep_oplist([ls.parse(job["qasm"], p) for p in job["params"]])
+            n = prep["nbits"]
+            v0 = np.zeros(1 << n, dtype=np.complex128)
+            v0[0] = 1
+            for b, params in enumerate(job["params"]):
+                want = dense.evolve_sv(ls.parse(job["qasm"], params))
+                got = run_oplist(sweep, n, v0, member=b)
+                assert abs(abs(np.vdot(want, got)) - 1) < 1e-12
+            assert prep["batch"] == len(job["params"]) and len(prep["xmask"]) == 20
+        else:
+            c = ls.parse(job["qasm"])
+            want = engine.sv_oplist(c) if job["kind"] == "sample" else engine.ptm_oplist(
+                c, [NoiseModel.uniform(**serve.DEFAULT_NOISE)])
+            assert prep.get("real", False) == (job["kind"] == "density")
+            t0, p0 = want.packed()
+            t1, p1 = prep["ops"]
+            assert np.array_equal(t0, t1) and np.array_equal(p0, p1)
+
+
+def test_deep_circuits_split_into_bounded_passes():
+    """A pass holds at most 192 operators (their descriptors sit in shared memory beside the tile),
+    so a deep circuit on few qubits plans into several passes instead of one oversized one."""
+    ops = engine.sv_oplist(ls.parse(wl.brickwork(10, 120, seed=4)))
+    assert len(ops) > 192 * 3
+    for precision in (_lib.C128, _lib.C64):
+        assert _lib.plan_passes(10, precision, ops) >= -(-len(ops) // 192)
