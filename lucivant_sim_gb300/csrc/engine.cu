@@ -109,7 +109,7 @@ int op_bits_ok(const lsg_op& op, int nbits) {
 
 // Register blocks: consecutive operators of a pass (already in a valid order) grouped while the
 // union of their bits stays within umax bits. A two-qubit depolarising operator fixes its block's
-// bit order (row a, row b, col a, col b); everything else takes ascending order.
+// bit order (row a, row b, col a, col b); everything else takes the order of first appearance.
 static bool block_kind(const TileOp& t, int umax) {
     switch (t.kind) {
         case LSG_OP_MATRIX: return t.k == 1 || (t.k == 2 && umax >= 2);
@@ -132,8 +132,17 @@ static void finish_block(Plan& plan, int pass_first, int first, int count, std::
     if (depol2 >= 0) {
         for (int i = 0; i < 4; ++i) order.push_back(plan.ops[depol2].lb[i]);
     } else {
-        order = bits;
-        std::sort(order.begin(), order.end());
+        // dense operators' bits first, in operator order, then the rest in order of appearance:
+        // each dense operator takes adjacent positions, so blocks of the same shape (a qubit pair
+        // of a Pauli-transfer register, say) run the same few compiled cases
+        for (int o = first; o < first + count; ++o) {
+            const TileOp& t = plan.ops[o];
+            if (t.kind != LSG_OP_MATRIX) continue;
+            for (int i = 0; i < t.k; ++i)
+                if (std::find(order.begin(), order.end(), t.lb[i]) == order.end()) order.push_back(t.lb[i]);
+        }
+        for (int b : bits)
+            if (std::find(order.begin(), order.end(), b) == order.end()) order.push_back(b);
     }
     // fill up to the register width with the highest unused tile bits: every thread then owns
     // 2^rb amplitudes and the warp's lanes stay on the lowest tile bits
@@ -164,6 +173,58 @@ static void finish_block(Plan& plan, int pass_first, int first, int count, std::
         }
     }
     plan.blocks.push_back(b);
+}
+
+// Reorder a pass's operators so register blocks come out large: operators on disjoint bits
+// commute, so an operator may move ahead of every skipped operator it shares no bit with. Greedy:
+// seed a block with the first remaining operator, sweep the rest in program order, and pull in
+// each one whose bits keep the block within umax bits and that no skipped operator before it
+// touches. Operators keep their program order relative to every operator they share a bit with.
+static void reorder_for_blocks(Plan& plan, const PassDesc& pd, int umax) {
+    if (umax < 1 || pd.nops < 3) return;
+    std::vector<TileOp> in(plan.ops.begin() + pd.first_op, plan.ops.begin() + pd.first_op + pd.nops);
+    auto mask_of = [](const TileOp& t) {
+        uint64_t m = 0;
+        for (int i = 0; i < t.k; ++i) m |= 1ull << t.lb[i];
+        return m;
+    };
+    std::vector<int> rest(in.size());
+    for (size_t i = 0; i < in.size(); ++i) rest[i] = (int)i;
+    std::vector<TileOp> out;
+    out.reserve(in.size());
+    while (!rest.empty()) {
+        const TileOp& seed = in[rest[0]];
+        std::vector<int> take{rest[0]}, left;
+        if (!block_kind(seed, umax)) {
+            out.push_back(seed);
+            rest.erase(rest.begin());
+            continue;
+        }
+        uint64_t bits = mask_of(seed), blocked = 0;
+        bool has_d2 = seed.kind == LSG_OP_DEPOL && seed.k == 4;
+        for (size_t r = 1; r < rest.size(); ++r) {
+            const TileOp& t = in[rest[r]];
+            const uint64_t m = mask_of(t);
+            bool ok = block_kind(t, umax) && !(m & blocked);
+            const uint64_t grown = bits | m;
+            const int gsz = __builtin_popcountll(grown);
+            const bool d2 = t.kind == LSG_OP_DEPOL && t.k == 4;
+            if (ok && gsz > umax) ok = false;
+            if (ok && d2 && (has_d2 || gsz != 4)) ok = false;
+            if (ok && has_d2 && gsz != 4) ok = false;
+            if (ok) {
+                take.push_back(rest[r]);
+                bits = grown;
+                has_d2 = has_d2 || d2;
+            } else {
+                left.push_back(rest[r]);
+                blocked |= m;
+            }
+        }
+        for (int i : take) out.push_back(in[i]);
+        rest.swap(left);
+    }
+    std::copy(out.begin(), out.end(), plan.ops.begin() + pd.first_op);
 }
 
 static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
@@ -208,23 +269,6 @@ static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
     }
     flush();
     pd.nblocks = (int)plan.blocks.size() - pd.first_block;
-    // shared-memory layouts: linear where the bulk copies and wide operators need it, swizzled
-    // between consecutive register blocks when each thread holds one group (K - u <= 8)
-    bool swizzled = false;  // the tile arrives linear
-    for (int i = 0; i < pd.nblocks; ++i) {
-        BlockDesc& b = plan.blocks[pd.first_block + i];
-        const bool next_reg = i + 1 < pd.nblocks && !plan.blocks[pd.first_block + i + 1].generic;
-        if (b.generic) {
-            b.in_swz = b.out_swz = 0;
-            swizzled = false;
-            continue;
-        }
-        const bool can = pd.K - b.u <= 8;
-        b.in_swz = swizzled ? 1 : 0;
-        b.out_swz = (can && next_reg) ? 1 : 0;
-        if (b.in_swz != b.out_swz && !can) b.out_swz = b.in_swz;  // never happens: in_swz implies can
-        swizzled = b.out_swz != 0;
-    }
 }
 
 // Operators per pass at most: their descriptors are staged in shared memory beside the tile
@@ -308,6 +352,7 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
             t.count = count ? count[idx] : 0;
             plan.ops.push_back(t);
         }
+        reorder_for_blocks(plan, pd, umax);
         form_blocks(plan, pd, umax);
         plan.passes.push_back(pd);
         remaining.swap(deferred);
@@ -337,15 +382,11 @@ static int check_plan(const Plan& plan) {
         for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
             if (bi < 0 || bi >= (int)plan.blocks.size()) return fail(LSG_E_ARG, "internal planning error: block index");
             const BlockDesc& b = plan.blocks[bi];
-            if (b.first != covered || b.nops < 1 || b.first + b.nops > pd.nops || (!b.generic && (b.u < 1 || b.u > 4)))
+            if (b.first != covered || b.nops < 1 || b.first + b.nops > pd.nops || b.generic < 0 || b.generic > 1 ||
+                (!b.generic && (b.u < 1 || b.u > 4)))
                 return fail(LSG_E_ARG, "internal planning error: a block outside its pass");
             for (int i = 0; !b.generic && i < b.u; ++i)
                 if (b.bits[i] < 0 || b.bits[i] >= pd.K) return fail(LSG_E_ARG, "internal planning error: block bit");
-            if (!b.generic && b.in_swz != b.out_swz && pd.K - b.u > 8)
-                return fail(LSG_E_ARG, "internal planning error: a relayout with several groups per thread");
-            const bool first = bi == pd.first_block, last = bi == pd.first_block + pd.nblocks - 1;
-            if ((first && b.in_swz) || (last && b.out_swz) || (b.generic && (b.in_swz || b.out_swz)))
-                return fail(LSG_E_ARG, "internal planning error: a swizzled layout at a pass boundary");
             covered += b.nops;
         }
         if (covered != pd.nops) return fail(LSG_E_ARG, "internal planning error: blocks do not cover the pass");
@@ -535,9 +576,84 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
             else if (src[0] == 0 && src[1] == 2 && src[2] == 1 && src[3] == 3) t.tmpl = kT_SWAP + 4 * P0 + P1;
         }
     }
+    // Register-block operator data, copied once here into an extension of the pool: diagonals
+    // re-indexed in block order (the kernel multiplies v[e] by m[e] with no index arithmetic), and
+    // dense matrices, diagonals and mixture matrices placed on 16-byte boundaries (the kernel reads
+    // them with 16-byte loads), per member when the data differs per member.
+    std::vector<double> ext;
+    const int64_t per = 16 / (int64_t)lsg_elem_bytes(precision);  // entries per 16 bytes
+    auto round_up = [&](int64_t x) { return (x + per - 1) / per * per; };
+    auto pad_ext = [&](int64_t lead) {  // pad so that entry (end + lead) is 16-byte aligned
+        while ((pool_entries + (int64_t)ext.size() / 2 + lead) % per) {
+            ext.push_back(0.0);
+            ext.push_back(0.0);
+        }
+    };
+    for (const PassDesc& pd : p->plan.passes)
+        for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
+            const BlockDesc& blk = p->plan.blocks[bi];
+            if (blk.generic) continue;
+            for (int o = blk.first; o < blk.first + blk.nops; ++o) {
+                TileOp& t = p->plan.ops[pd.first_op + o];
+                const int64_t members = t.stride ? batch : 1;
+                if (t.tmpl == kT_DIAG) {
+                    const int u = blk.u, d = 1 << u;
+                    const int64_t stride = round_up(d);
+                    pad_ext(0);
+                    const int64_t at = pool_entries + (int64_t)ext.size() / 2;
+                    for (int64_t b = 0; b < members; ++b) {
+                        for (int e = 0; e < d; ++e) {
+                            int j = 0;
+                            for (int i = 0; i < t.k; ++i) j = (j << 1) | ((e >> (u - 1 - t.pos[i])) & 1);
+                            const int64_t src = t.data + b * t.stride + j;
+                            ext.push_back(pool[2 * src]);
+                            ext.push_back(pool[2 * src + 1]);
+                        }
+                        for (int64_t e = d; e < stride; ++e) {
+                            ext.push_back(0.0);
+                            ext.push_back(0.0);
+                        }
+                    }
+                    t.data = at;
+                    t.stride = t.stride ? stride : 0;
+                    t.tmpl = kT_DIAGB;
+                    continue;
+                }
+                const bool dense = t.tmpl >= kT_DENSE1 && t.tmpl < kT_DENSE2 + 16;
+                const bool mix = t.tmpl >= kT_MIX1 && t.tmpl < kT_MIX2 + 16;
+                if (!dense && !mix) continue;
+                const int64_t d = 1ll << t.k;
+                const int64_t lead = mix ? t.count : 0;  // a mixture's branch table precedes its matrices
+                const int64_t len = mix ? t.count + t.count * d * d : d * d;
+                const int64_t stride = round_up(len);
+                pad_ext(lead);
+                const int64_t at = pool_entries + (int64_t)ext.size() / 2;
+                for (int64_t b = 0; b < members; ++b) {
+                    for (int64_t e = 0; e < len; ++e) {
+                        const int64_t src = t.data + b * t.stride + e;
+                        ext.push_back(pool[2 * src]);
+                        ext.push_back(pool[2 * src + 1]);
+                    }
+                    for (int64_t e = len; e < stride; ++e) {
+                        ext.push_back(0.0);
+                        ext.push_back(0.0);
+                    }
+                }
+                t.data = at;
+                t.stride = t.stride ? stride : 0;
+            }
+        }
+    const int64_t all_entries = pool_entries + (int64_t)ext.size() / 2;
+    std::vector<double> merged;
+    if (!ext.empty()) {
+        merged.assign(pool, pool + 2 * pool_entries);
+        merged.insert(merged.end(), ext.begin(), ext.end());
+        pool = merged.data();
+    }
+    pool_entries = all_entries;
     size_t max_meta = 0;
     for (const PassDesc& pd : p->plan.passes)
-        max_meta = std::max(max_meta, (size_t)pd.nops * sizeof(TileOp) + (size_t)pd.nblocks * sizeof(BlockDesc));
+        max_meta = std::max(max_meta, (size_t)pd.nops * (sizeof(TileOp) + 16) + (size_t)pd.nblocks * sizeof(BlockDesc));
     const size_t elt = lsg_elem_bytes(precision);
     p->smem = (elt << p->K) + max_meta;
     if (p->smem > 220 * 1024) {
@@ -924,6 +1040,24 @@ int lsg_plan(int nbits, int precision, const lsg_op* ops, int32_t nops, int32_t*
     if (nops > 0 && plan.passes.empty()) return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits", K);
     LSG_CHECK(check_plan(plan));
     *passes = (int32_t)plan.passes.size();
+    if (getenv("LSG_PLAN_DUMP")) {  // diagnostics: the plan on stderr
+        for (size_t pi = 0; pi < plan.passes.size(); ++pi) {
+            const PassDesc& pd = plan.passes[pi];
+            std::fprintf(stderr, "pass %zu: K=%d L=%d hi=[", pi, pd.K, pd.L);
+            for (int j = 0; j < pd.K - pd.L; ++j) std::fprintf(stderr, "%s%d", j ? "," : "", pd.hi[j]);
+            std::fprintf(stderr, "] ops=%d blocks=%d\n", pd.nops, pd.nblocks);
+            for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
+                const BlockDesc& b = plan.blocks[bi];
+                std::fprintf(stderr, "  block u=%d generic=%d bits=[%d,%d,%d,%d] ops:", b.u, b.generic, b.bits[0],
+                             b.bits[1], b.bits[2], b.bits[3]);
+                for (int o = b.first; o < b.first + b.nops; ++o) {
+                    const TileOp& t = plan.ops[pd.first_op + o];
+                    std::fprintf(stderr, " %d/%d@%d", t.kind, t.k, t.tmpl);
+                }
+                std::fprintf(stderr, "\n");
+            }
+        }
+    }
     return LSG_OK;
 }
 

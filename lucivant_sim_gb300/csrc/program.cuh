@@ -26,7 +26,6 @@ struct BlockDesc {
     int u, first, nops, generic;
     int bits[4];
     int sorted[4];
-    int in_swz, out_swz;  // shared-memory layout read and written: 0 linear, 1 swizzled
 };
 
 // Operator kinds beyond the public LSG_OP_* set, used by trajectory programs.
@@ -66,6 +65,7 @@ constexpr int kT_MIX2 = 64;     // + 4 * P0 + P1
 constexpr int kT_X1 = 80;       // + P: unit-phase X (register swap)
 constexpr int kT_CX = 84;       // + 4 * Pcontrol + Ptarget: unit-phase CX (register swap)
 constexpr int kT_SWAP = 100;    // + 4 * P0 + P1
+constexpr int kT_DIAGB = 116;   // diagonal re-indexed by the host in block order: v[e] *= m[e]
 constexpr int kT_GENERIC = -1;
 // The greedy fusion planner (csrc/engine.cu): lsg_op list -> passes of tile-local operators.
 // pred/draw/count (may be null) give trajectory operators their predicate bit, uniform offset and

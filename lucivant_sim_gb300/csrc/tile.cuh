@@ -257,10 +257,39 @@ __device__ __forceinline__ void op_mixture(T* t, int tbits, const TileOp& op, co
 // v[e] holds the amplitude at group offset e of a block of U bits; bit (U-1-P) of e is block
 // position P. Every function below is fully unrolled over e, so v stays in registers.
 
+// N operator entries into registers with 16-byte loads (the host places register-block operator
+// data on 16-byte boundaries).
+__device__ __forceinline__ void ld16(const float* p, float* o) {
+    const float4 w = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = w.x, o[1] = w.y, o[2] = w.z, o[3] = w.w;
+}
+__device__ __forceinline__ void ld16(const double* p, double* o) {
+    const double2 w = __ldg(reinterpret_cast<const double2*>(p));
+    o[0] = w.x, o[1] = w.y;
+}
+__device__ __forceinline__ void ld16(const Cx<float>* p, Cx<float>* o) {
+    const float4 w = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = Cx<float>(w.x, w.y), o[1] = Cx<float>(w.z, w.w);
+}
+__device__ __forceinline__ void ld16(const Cx<double>* p, Cx<double>* o) {
+    const double2 w = __ldg(reinterpret_cast<const double2*>(p));
+    o[0] = Cx<double>(w.x, w.y);
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void ldv(const T* __restrict__ m, T* out) {
+    static_assert((N * sizeof(T)) % 16 == 0, "whole 16-byte words");
+    constexpr int per = 16 / sizeof(T);
+#pragma unroll
+    for (int i = 0; i < N / per; ++i) ld16(m + i * per, out + i * per);
+}
+
 template <typename T, int U, int P>
 __device__ __forceinline__ void rb_dense1(T* v, const T* m) {
     constexpr int B = 1 << (U - 1 - P);
-    const T m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+    T mm[4];
+    ldv<T, 4>(m, mm);
+    const T m00 = mm[0], m01 = mm[1], m10 = mm[2], m11 = mm[3];
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & B) continue;
@@ -273,16 +302,18 @@ __device__ __forceinline__ void rb_dense1(T* v, const T* m) {
 template <typename T, int U, int P0, int P1>
 __device__ __forceinline__ void rb_dense2(T* v, const T* m) {
     constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+    T mm[16];
+    ldv<T, 16>(m, mm);
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & (B0 | B1)) continue;
         const T a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            T acc = cmul(m[4 * r], a0);
-            acc = cfma(m[4 * r + 1], a1, acc);
-            acc = cfma(m[4 * r + 2], a2, acc);
-            acc = cfma(m[4 * r + 3], a3, acc);
+            T acc = cmul(mm[4 * r], a0);
+            acc = cfma(mm[4 * r + 1], a1, acc);
+            acc = cfma(mm[4 * r + 2], a2, acc);
+            acc = cfma(mm[4 * r + 3], a3, acc);
             v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
         }
     }
@@ -401,13 +432,17 @@ __device__ __forceinline__ void rb_depol2(T* v, const T* m) {
     }
 }
 
+// a diagonal whose 2^U entries the host laid out in block order (no index arithmetic)
 template <typename T, int U>
-__device__ __forceinline__ void rb_diag(T* v, const TileOp& op, const T* m) {
+__device__ __forceinline__ void rb_diagb(T* v, const T* m) {
+    if constexpr (((1 << U) * sizeof(T)) % 16 == 0) {
+        T mm[1 << U];
+        ldv<T, (1 << U)>(m, mm);
 #pragma unroll
-    for (int e = 0; e < (1 << U); ++e) {
-        int j = 0;
-        for (int b = 0; b < op.k; ++b) j = (j << 1) | ((e >> (U - 1 - op.pos[b])) & 1);
-        v[e] = cmul(m[j], v[e]);
+        for (int e = 0; e < (1 << U); ++e) v[e] = cmul(mm[e], v[e]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < (1 << U); ++e) v[e] = cmul(m[e], v[e]);
     }
 }
 
@@ -437,23 +472,28 @@ __device__ __forceinline__ const T* mixture_pick(const TileOp& op, const T* m, d
     return nullptr;
 }
 
-#define LSG_P1(X, BASE)                                    \
+// Case lists of rb_apply: a register-block code names the operator's positions P in the block.
+#define LSG_P1(X, BASE)                                                                  \
     case BASE + 0: if (U > 0) X<T, U, (0 < U ? 0 : 0)>(v, m); break; \
     case BASE + 1: if (U > 1) X<T, U, (1 < U ? 1 : 0)>(v, m); break; \
     case BASE + 2: if (U > 2) X<T, U, (2 < U ? 2 : 0)>(v, m); break; \
     case BASE + 3: if (U > 3) X<T, U, (3 < U ? 3 : 0)>(v, m); break;
 
-#define LSG_P2ONE(X, BASE, A, B) \
-    case BASE + 4 * A + B: if (U > A && U > B) X<T, U, (A < U ? A : 0), (B < U ? B : 0)>(v, m); break;
+#define LSG_P2ONE(X, BASE, A, B)                                                                        \
+    case BASE + 4 * A + B:                                                                              \
+        if (U > A && U > B) X<T, U, (A < U ? A : 0), (B < U ? B : 0)>(v, m); \
+        break;
 
-#define LSG_R1(X, BASE)                                    \
+#define LSG_R1(X, BASE)                                                               \
     case BASE + 0: if (U > 0) X<T, U, (0 < U ? 0 : 0)>(v); break; \
     case BASE + 1: if (U > 1) X<T, U, (1 < U ? 1 : 0)>(v); break; \
     case BASE + 2: if (U > 2) X<T, U, (2 < U ? 2 : 0)>(v); break; \
     case BASE + 3: if (U > 3) X<T, U, (3 < U ? 3 : 0)>(v); break;
 
-#define LSG_R2ONE(X, BASE, A, B) \
-    case BASE + 4 * A + B: if (U > A && U > B) X<T, U, (A < U ? A : 0), (B < U ? B : 0)>(v); break;
+#define LSG_R2ONE(X, BASE, A, B)                                                                     \
+    case BASE + 4 * A + B:                                                                           \
+        if (U > A && U > B) X<T, U, (A < U ? A : 0), (B < U ? B : 0)>(v); \
+        break;
 
 #define LSG_R2(X, BASE)                                                                                  \
     LSG_R2ONE(X, BASE, 0, 1) LSG_R2ONE(X, BASE, 0, 2) LSG_R2ONE(X, BASE, 0, 3) LSG_R2ONE(X, BASE, 1, 0) \
@@ -466,7 +506,7 @@ __device__ __forceinline__ const T* mixture_pick(const TileOp& op, const T* m, d
     LSG_P2ONE(X, BASE, 2, 3) LSG_P2ONE(X, BASE, 3, 0) LSG_P2ONE(X, BASE, 3, 1) LSG_P2ONE(X, BASE, 3, 2)
 
 template <typename T, int U>
-__device__ __forceinline__ void rb_apply(T* v, int code, const TileOp& op, const T* m) {
+__device__ __forceinline__ void rb_apply(T* v, int code, const T* m) {
     switch (code) {
         LSG_P1(rb_dense1, kT_DENSE1)
         LSG_P2(rb_dense2, kT_DENSE2)
@@ -474,74 +514,55 @@ __device__ __forceinline__ void rb_apply(T* v, int code, const TileOp& op, const
         LSG_P2(rb_perm2, kT_PERM2)
         LSG_P2(rb_depol1, kT_DEPOL1)
         case kT_DEPOL2:
-            if (U == 4) rb_depol2<T>(v, m);
+            if constexpr (U == 4) rb_depol2<T>(v, m);
             break;
         LSG_R1(rb_x, kT_X1)
         LSG_R2(rb_cx, kT_CX)
         LSG_R2(rb_swap, kT_SWAP)
-        case kT_DIAG: rb_diag<T, U>(v, op, m); break;
+        case kT_DIAGB: rb_diagb<T, U>(v, m); break;
         case kT_SCALE: rb_scale<T, U>(v, m); break;
         default: break;
     }
 }
 
-// Swizzled shared-memory position of tile element i: the bits above a 128-byte bank row are
-// folded into the bank bits by XOR, so the strided group accesses of a register block spread
-// over all banks. A bijection; the linear layout is kept for the bulk copies in and out.
-template <typename T>
-__device__ __forceinline__ uint32_t swz(uint32_t i) {
-    // elements per 128-byte bank row: 32 (4 bytes), 16 (8 bytes) or 8 (16 bytes)
-    constexpr int SH = sizeof(T) == 4 ? 5 : sizeof(T) == 8 ? 4 : 3;
-    constexpr uint32_t M = (1u << SH) - 1;
-    const uint32_t x = i >> SH;
-    return i ^ ((x ^ (x >> SH) ^ (x >> (2 * SH))) & M);
-}
+// A register-block operator resolved for the tile's member: its code and data pointer (built
+// once per tile in shared memory, so the inner loop reads one 16-byte record per operator).
+struct OpRec {
+    int code, pad;
+    const void* m;
+};
 
-// One register block over the whole tile: each thread takes groups of 2^U amplitudes (the block's
-// U register bits), reads them in the block's input layout, applies the block's operators and
-// writes them in its output layout. A change of layout needs every read done before any write:
-// the host only asks for one when each thread has at most one group.
-template <typename T, int U>
+// One register block over the whole tile: each thread takes groups of 2^U elements (the block's
+// U register bits), reads them, applies the block's operators in registers and writes them back.
+// PLAIN: a gate program (records, no predicates or mixtures); otherwise a trajectory program.
+template <typename T, int U, bool PLAIN>
 __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp* __restrict__ ops,
-                          const T* __restrict__ data, int64_t member, uint64_t pred, const TrajCtx& ctx,
-                          int64_t cur) {
-    const bool sin = blk.in_swz != 0, sout = blk.out_swz != 0;
-    const bool relayout = sin != sout;
-    // the swizzle is linear over GF(2): position(base | bits) = position(base) ^ position(bits), so
-    // each element's offset is a fixed XOR of per-bit offsets, built once per block
-    uint32_t min_[4], mout[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const uint32_t m = i < U ? (1u << blk.bits[i]) : 0u;
-        min_[i] = sin ? swz<T>(m) : m;
-        mout[i] = sout ? swz<T>(m) : m;
-    }
-    uint32_t oin[1 << U], oout[1 << U];
+                          const OpRec* __restrict__ recs, const T* __restrict__ data, int64_t member, uint64_t pred,
+                          const TrajCtx& ctx, int64_t cur) {
+    // element e of a group sits at base | off[e]: the block's bits of e deposited at its tile bits
+    uint32_t off[1 << U];
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
-        uint32_t a = 0, b = 0;
+        uint32_t a = 0;
 #pragma unroll
         for (int i = 0; i < U; ++i)
-            if ((e >> (U - 1 - i)) & 1) {
-                a ^= min_[i];
-                b ^= mout[i];
-            }
-        oin[e] = a;
-        oout[e] = b;
+            if ((e >> (U - 1 - i)) & 1) a |= 1u << blk.bits[i];
+        off[e] = a;
     }
     const int groups = 1 << (tbits - U);
-    for (int g0 = 0; g0 < groups; g0 += kCompute) {
-        const int g = g0 + threadIdx.x;
-        const bool active = g < groups;
+    for (int g = threadIdx.x; g < groups; g += kCompute) {
         uint32_t base = (uint32_t)g;
 #pragma unroll
         for (int i = 0; i < U; ++i) base = ins0(base, blk.sorted[i]);
-        const uint32_t bin = sin ? swz<T>(base) : base;
-        const uint32_t bout = sout ? swz<T>(base) : base;
         T v[1 << U];
-        if (active) {
 #pragma unroll
-            for (int e = 0; e < (1 << U); ++e) v[e] = tile[bin ^ oin[e]];
+        for (int e = 0; e < (1 << U); ++e) v[e] = tile[base | off[e]];
+        if constexpr (PLAIN) {
+            for (int o = 0; o < blk.nops; ++o) {
+                const OpRec r = recs[blk.first + o];
+                rb_apply<T, U>(v, r.code, static_cast<const T*>(r.m));
+            }
+        } else {
             for (int o = 0; o < blk.nops; ++o) {
                 const TileOp& op = ops[blk.first + o];
                 if (!((pred >> op.pred) & 1)) continue;
@@ -552,14 +573,11 @@ __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp
                     if (!m) continue;
                     code = (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2));
                 }
-                rb_apply<T, U>(v, code, op, m);
+                rb_apply<T, U>(v, code, m);
             }
         }
-        if (relayout) cbar();  // uniform: relayout blocks run exactly one round
-        if (active) {
 #pragma unroll
-            for (int e = 0; e < (1 << U); ++e) tile[bout ^ oout[e]] = v[e];
-        }
+        for (int e = 0; e < (1 << U); ++e) tile[base | off[e]] = v[e];
     }
 }
 
@@ -601,10 +619,14 @@ __device__ void run_ops(T* tile, int tbits, const TileOp* __restrict__ ops, int 
 // All blocks of a pass on one tile (the 256 compute threads).
 template <typename T>
 __device__ __forceinline__ void compute_tile(T* tile, int K, const PassDesc& pd, const BlockDesc* sblk,
-                                             const TileOp* sops, const T* __restrict__ data, int64_t member,
-                                             const TrajCtx& ctx) {
-    const uint64_t pred = ctx.u ? ctx.pred[member] : ~0ull;
-    const int64_t cur = ctx.u ? ctx.cursor[member] : 0;
+                                             const TileOp* sops, OpRec* recs, const T* __restrict__ data,
+                                             int64_t member, const TrajCtx& ctx) {
+    const bool plain = ctx.u == nullptr;
+    const uint64_t pred = plain ? ~0ull : ctx.pred[member];
+    const int64_t cur = plain ? 0 : ctx.cursor[member];
+    if (plain)  // this tile's member: resolve every operator's data pointer once
+        for (int o = threadIdx.x; o < pd.nops; o += kCompute)
+            recs[o] = OpRec{sops[o].tmpl, 0, data + sops[o].data + member * sops[o].stride};
     for (int bi = 0; bi < pd.nblocks; ++bi) {
         const BlockDesc& blk = sblk[bi];
         cbar();
@@ -612,14 +634,20 @@ __device__ __forceinline__ void compute_tile(T* tile, int K, const PassDesc& pd,
             run_ops<T>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
             continue;
         }
+#define LSG_RUN(UU)                                                                                   \
+    if (plain) run_block<T, UU, true>(tile, K, blk, sops, recs, data, member, pred, ctx, cur);      \
+    else run_block<T, UU, false>(tile, K, blk, sops, recs, data, member, pred, ctx, cur);
         switch (blk.u) {
-            case 1: run_block<T, 1>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-            case 2: run_block<T, 2>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
-            case 3: run_block<T, 3>(tile, K, blk, sops, data, member, pred, ctx, cur); break;
+            case 1: LSG_RUN(1) break;
+            case 2: LSG_RUN(2) break;
+            case 3: LSG_RUN(3) break;
             default:
-                if constexpr (sizeof(T) <= 8) run_block<T, 4>(tile, K, blk, sops, data, member, pred, ctx, cur);
+                if constexpr (sizeof(T) <= 8) {
+                    LSG_RUN(4)
+                }
                 break;
         }
+#undef LSG_RUN
     }
     cbar();
 }
@@ -645,8 +673,8 @@ __device__ __forceinline__ void stage_pass(const PassDesc* __restrict__ pass_g, 
 // compute and stores of consecutive tiles overlap. Every wait is bounded.
 constexpr int kPipeThreads = 288;
 
-// CTAs per SM the kernels are compiled for: elements of 8 bytes or more in FP64 (complex128,
-// real64) get the larger register budget; the FP64 path is bound by FP64 issue, not occupancy.
+// CTAs per SM the kernels are compiled for: FP64 elements (complex128, real64) get the larger
+// register budget; that path is bound by FP64 issue, not occupancy.
 template <typename T>
 constexpr int wide_regs() {
     return sizeof(typename Elem<T>::R) == 8 ? 1 : 0;
@@ -667,6 +695,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2 - wide_regs<T>()) k_tile_pipe(
     T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
     TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + 2 * tile_bytes);
     BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
+    OpRec* recs = reinterpret_cast<OpRec*>(sblk + pass_g->nblocks);
     if (threadIdx.x == 0) pd = *pass_g;
     stage_pass<T>(pass_g, ops, blocks, sops, sblk);
     if (threadIdx.x == 0) {
@@ -742,7 +771,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2 - wide_regs<T>()) k_tile_pipe(
         const bool ok = mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), status);
         if (cbar_or(!ok)) return;  // every compute thread leaves together on a timeout
         const int64_t member = t / tiles_per_member;
-        compute_tile<T>(tile, K, pd, sblk, sops, data, member, ctx);
+        compute_tile<T>(tile, K, pd, sblk, sops, recs, data, member, ctx);
         fence_proxy_async_smem();  // this thread's writes, before the producer's bulk store reads them
         mbar_arrive(&empty[b]);
     }
@@ -762,6 +791,7 @@ __global__ void __launch_bounds__(256, 3 - wide_regs<T>()) k_tile_pass(T* __rest
     T* tile = reinterpret_cast<T*>(smem_raw);
     TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + (sizeof(T) << pass_g->K));
     BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
+    OpRec* recs = reinterpret_cast<OpRec*>(sblk + pass_g->nblocks);
     if (threadIdx.x == 0) pd = *pass_g;
     {
         // stage this pass's operators and blocks in shared memory (the same for every tile)
@@ -811,7 +841,7 @@ __global__ void __launch_bounds__(256, 3 - wide_regs<T>()) k_tile_pass(T* __rest
         }
         // ---- compute: register blocks, or one shared-memory operator for a wide block
         __syncthreads();
-        compute_tile<T>(tile, K, pd, sblk, sops, data, member, ctx);
+        compute_tile<T>(tile, K, pd, sblk, sops, recs, data, member, ctx);
         __syncthreads();
         // ---- store
         if (use_bulk) {

@@ -124,8 +124,11 @@ def test_complex64_statevector_tvd():
     assert tvd(got, want) < TVD_C64
 
 
-def test_complex64_density_tvd(dm_form):
-    c = ls.parse(wl.brickwork(6, 6, seed=6))
+@pytest.mark.parametrize("n", [6, 7])
+def test_complex64_density_tvd(dm_form, n):
+    """7 qubits: a 14-bit Pauli-transfer register in FP32 takes 2^13-element tiles with two
+    register groups per thread."""
+    c = ls.parse(wl.brickwork(n, 6, seed=6))
     want = dense.probabilities_array(c, _dm_noise())
     got = ls.probabilities_array(c, _dm_noise(), precision="c64")
     assert tvd(got, want) < TVD_C64
