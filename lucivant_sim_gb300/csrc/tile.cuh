@@ -673,15 +673,21 @@ __device__ __forceinline__ void stage_pass(const PassDesc* __restrict__ pass_g, 
 // compute and stores of consecutive tiles overlap. Every wait is bounded.
 constexpr int kPipeThreads = 288;
 
-// CTAs per SM the kernels are compiled for: FP64 elements (complex128, real64) get the larger
-// register budget; that path is bound by FP64 issue, not occupancy.
+// CTAs per SM the kernels are compiled for. FP64 elements (complex128, real64) get the larger
+// register budget: that path is bound by FP64 issue, not occupancy. Real32 tiles (32 KB, two per
+// CTA) leave room for three pipelined CTAs per SM, and the latency-bound passes gain more from the
+// third CTA's warps than they lose to the smaller register budget.
 template <typename T>
 constexpr int wide_regs() {
     return sizeof(typename Elem<T>::R) == 8 ? 1 : 0;
 }
+template <typename T>
+constexpr int pipe_ctas() {
+    return sizeof(T) == 4 ? 3 : 2 - wide_regs<T>();
+}
 
 template <typename T>
-__global__ void __launch_bounds__(kPipeThreads, 2 - wide_regs<T>()) k_tile_pipe(T* __restrict__ state, int64_t member_elems,
+__global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe(T* __restrict__ state, int64_t member_elems,
                                                                const PassDesc* __restrict__ pass_g,
                                                                const TileOp* __restrict__ ops,
                                                                const BlockDesc* __restrict__ blocks,
