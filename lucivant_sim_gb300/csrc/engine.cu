@@ -143,6 +143,15 @@ static void finish_block(Plan& plan, int pass_first, int first, int count, std::
         }
         for (int b : bits)
             if (std::find(order.begin(), order.end(), b) == order.end()) order.push_back(b);
+        // tile bits 1 and 0 go last: a group then holds runs of consecutive elements, read and
+        // written with vector shared-memory accesses (which also avoids their bank conflicts)
+        for (int low : {1, 0}) {
+            auto it = std::find(order.begin(), order.end(), low);
+            if (it != order.end()) {
+                order.erase(it);
+                order.push_back(low);
+            }
+        }
     }
     // fill up to the register width with the highest unused tile bits: every thread then owns
     // 2^rb amplitudes and the warp's lanes stay on the lowest tile bits
@@ -154,6 +163,8 @@ static void finish_block(Plan& plan, int pass_first, int first, int count, std::
         b.bits[i] = order[i];
         b.sorted[i] = order[i];
     }
+    b.vec = 1;
+    if (b.u >= 1 && order[b.u - 1] == 0) b.vec = (b.u >= 2 && order[b.u - 2] == 1) ? 4 : 2;
     std::sort(b.sorted, b.sorted + b.u);
     for (int o = first; o < first + count; ++o) {
         TileOp& t = plan.ops[o];
@@ -557,6 +568,16 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
         delete p;
         return LSG_E_ARG;
     }
+    // real (Pauli-transfer) 4x4 operators whose first row is (1,0,0,0) for every member: trace
+    // preserving; the kernel skips that row
+    if (precision == LSG_R64 || precision == LSG_R32)
+        for (TileOp& t : p->plan.ops) {
+            if (t.kind != LSG_OP_MATRIX || t.k != 2 || t.tmpl < kT_DENSE2 || t.tmpl >= kT_DENSE2 + 16) continue;
+            bool tp = true;
+            for (int64_t b = 0; b < (t.stride ? batch : 1) && tp; ++b)
+                for (int c = 0; c < 4 && tp; ++c) tp = pool[2 * (t.data + b * t.stride + c)] == (c == 0 ? 1.0 : 0.0);
+            if (tp) t.tmpl = kT_TPD2 + (t.tmpl - kT_DENSE2);
+        }
     // permutations with unit phases shared by all members are register renames
     for (TileOp& t : p->plan.ops) {
         if (t.kind != LSG_OP_PERM || t.stride != 0 || t.tmpl == kT_GENERIC) continue;
@@ -619,7 +640,7 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
                     t.tmpl = kT_DIAGB;
                     continue;
                 }
-                const bool dense = t.tmpl >= kT_DENSE1 && t.tmpl < kT_DENSE2 + 16;
+                const bool dense = (t.tmpl >= kT_DENSE1 && t.tmpl < kT_DENSE2 + 16) || (t.tmpl >= kT_TPD2 && t.tmpl < kT_TPD2 + 16);
                 const bool mix = t.tmpl >= kT_MIX1 && t.tmpl < kT_MIX2 + 16;
                 if (!dense && !mix) continue;
                 const int64_t d = 1ll << t.k;

@@ -26,6 +26,9 @@ struct BlockDesc {
     int u, first, nops, generic;
     int bits[4];
     int sorted[4];
+    int vec;  // 1, 2 or 4: the block's last positions are tile bits (1,) 0, so each group holds
+              // runs of `vec` consecutive elements (vector shared-memory accesses)
+    int pad;
 };
 
 // Operator kinds beyond the public LSG_OP_* set, used by trajectory programs.
@@ -66,6 +69,7 @@ constexpr int kT_X1 = 80;       // + P: unit-phase X (register swap)
 constexpr int kT_CX = 84;       // + 4 * Pcontrol + Ptarget: unit-phase CX (register swap)
 constexpr int kT_SWAP = 100;    // + 4 * P0 + P1
 constexpr int kT_DIAGB = 116;   // diagonal re-indexed by the host in block order: v[e] *= m[e]
+constexpr int kT_TPD2 = 120;    // + 4 * P0 + P1: real 4x4 transfer matrix whose row 0 is (1,0,0,0)
 constexpr int kT_GENERIC = -1;
 // The greedy fusion planner (csrc/engine.cu): lsg_op list -> passes of tile-local operators.
 // pred/draw/count (may be null) give trajectory operators their predicate bit, uniform offset and

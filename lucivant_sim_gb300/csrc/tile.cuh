@@ -319,6 +319,30 @@ __device__ __forceinline__ void rb_dense2(T* v, const T* m) {
     }
 }
 
+// A real 4x4 transfer matrix with first row (1,0,0,0) (trace preserving): output 0 keeps its
+// input, rows 1-3 are computed. 12 multiply-adds per 4 elements instead of 16.
+template <typename T, int U, int P0, int P1>
+__device__ __forceinline__ void rb_tpd2(T* v, const T* m) {
+    if constexpr (!Elem<T>::complex) {
+        constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+        T mm[12];
+        ldv<T, 12>(m + 4, mm);
+#pragma unroll
+        for (int e = 0; e < (1 << U); ++e) {
+            if (e & (B0 | B1)) continue;
+            const T a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+#pragma unroll
+            for (int r = 1; r < 4; ++r) {
+                T acc = cmul(mm[4 * r - 4], a0);
+                acc = cfma(mm[4 * r - 3], a1, acc);
+                acc = cfma(mm[4 * r - 2], a2, acc);
+                acc = cfma(mm[4 * r - 1], a3, acc);
+                v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
+            }
+        }
+    }
+}
+
 template <typename T, int U, int P>
 __device__ __forceinline__ void rb_perm1(T* v, const T* m) {
     constexpr int B = 1 << (U - 1 - P);
@@ -510,6 +534,7 @@ __device__ __forceinline__ void rb_apply(T* v, int code, const T* m) {
     switch (code) {
         LSG_P1(rb_dense1, kT_DENSE1)
         LSG_P2(rb_dense2, kT_DENSE2)
+        LSG_P2(rb_tpd2, kT_TPD2)
         LSG_P1(rb_perm1, kT_PERM1)
         LSG_P2(rb_perm2, kT_PERM2)
         LSG_P2(rb_depol1, kT_DEPOL1)
@@ -523,6 +548,81 @@ __device__ __forceinline__ void rb_apply(T* v, int code, const T* m) {
         case kT_SCALE: rb_scale<T, U>(v, m); break;
         default: break;
     }
+}
+
+// A group's 2^U elements between shared memory and registers. With vec = 2 or 4 the group's last
+// positions are tile bits (1,) 0: runs of consecutive elements, moved with 8- or 16-byte accesses
+// where the element size allows (the run's address is then aligned: base and off[] have those bits
+// clear).
+template <typename T, int U>
+__device__ __forceinline__ void load_group(const T* tile, uint32_t base, const uint32_t* off, int vec, T* v) {
+    if constexpr (sizeof(T) == 4 && U >= 2) {
+        if (vec == 4) {
+#pragma unroll
+            for (int e = 0; e < (1 << U); e += 4) {
+                const float4 w = *reinterpret_cast<const float4*>(tile + (base | off[e]));
+                v[e] = w.x, v[e + 1] = w.y, v[e + 2] = w.z, v[e + 3] = w.w;
+            }
+            return;
+        }
+    }
+    if constexpr (sizeof(T) == 8 && U >= 1) {
+        if (vec >= 2) {
+#pragma unroll
+            for (int e = 0; e < (1 << U); e += 2) {
+                const uint4 w = *reinterpret_cast<const uint4*>(tile + (base | off[e]));
+                memcpy(&v[e], &w.x, 8);
+                memcpy(&v[e + 1], &w.z, 8);
+            }
+            return;
+        }
+    }
+    if constexpr (sizeof(T) == 4 && U >= 1) {
+        if (vec == 2) {
+#pragma unroll
+            for (int e = 0; e < (1 << U); e += 2) {
+                const float2 w = *reinterpret_cast<const float2*>(tile + (base | off[e]));
+                v[e] = w.x, v[e + 1] = w.y;
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) v[e] = tile[base | off[e]];
+}
+
+template <typename T, int U>
+__device__ __forceinline__ void store_group(T* tile, uint32_t base, const uint32_t* off, int vec, const T* v) {
+    if constexpr (sizeof(T) == 4 && U >= 2) {
+        if (vec == 4) {
+#pragma unroll
+            for (int e = 0; e < (1 << U); e += 4)
+                *reinterpret_cast<float4*>(tile + (base | off[e])) = make_float4(v[e], v[e + 1], v[e + 2], v[e + 3]);
+            return;
+        }
+    }
+    if constexpr (sizeof(T) == 8 && U >= 1) {
+        if (vec >= 2) {
+#pragma unroll
+            for (int e = 0; e < (1 << U); e += 2) {
+                uint4 w;
+                memcpy(&w.x, &v[e], 8);
+                memcpy(&w.z, &v[e + 1], 8);
+                *reinterpret_cast<uint4*>(tile + (base | off[e])) = w;
+            }
+            return;
+        }
+    }
+    if constexpr (sizeof(T) == 4 && U >= 1) {
+        if (vec == 2) {
+#pragma unroll
+            for (int e = 0; e < (1 << U); e += 2)
+                *reinterpret_cast<float2*>(tile + (base | off[e])) = make_float2(v[e], v[e + 1]);
+            return;
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) tile[base | off[e]] = v[e];
 }
 
 // A register-block operator resolved for the tile's member: its code and data pointer (built
@@ -555,8 +655,7 @@ __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp
 #pragma unroll
         for (int i = 0; i < U; ++i) base = ins0(base, blk.sorted[i]);
         T v[1 << U];
-#pragma unroll
-        for (int e = 0; e < (1 << U); ++e) v[e] = tile[base | off[e]];
+        load_group<T, U>(tile, base, off, blk.vec, v);
         if constexpr (PLAIN) {
             for (int o = 0; o < blk.nops; ++o) {
                 const OpRec r = recs[blk.first + o];
@@ -576,8 +675,7 @@ __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp
                 rb_apply<T, U>(v, code, m);
             }
         }
-#pragma unroll
-        for (int e = 0; e < (1 << U); ++e) tile[base | off[e]] = v[e];
+        store_group<T, U>(tile, base, off, blk.vec, v);
     }
 }
 
