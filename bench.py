@@ -64,15 +64,17 @@ def dist_info() -> tuple[int, int, int]:
 
 
 class Dist:
-    """Barrier and max-over-ranks on the host (gloo) when launched by torchrun."""
+    """Barrier and max-over-ranks on the host (gloo) when launched by torchrun. A rank that never
+    joins, or leaves, ends the others' next collective with an error after ``timeout_s``."""
 
-    def __init__(self, world: int) -> None:
+    def __init__(self, world: int, timeout_s: float = 600.0) -> None:
         self.world = world
-        self.pg = None
         if world > 1:
+            import datetime
+
             import torch.distributed as td
 
-            td.init_process_group("gloo")
+            td.init_process_group("gloo", timeout=datetime.timedelta(seconds=timeout_s))
             self.td = td
 
     def barrier(self) -> None:
