@@ -60,6 +60,12 @@ struct Step {
 
 __device__ __forceinline__ double nrm(double re, double im) { return re * re + im * im; }
 
+// |a|^2 of one amplitude as a double: complex128 squares in FP64; a complex64 amplitude's square
+// is formed in FP32 (exact to its own precision) and accumulated in FP64 by the caller, so the
+// FP64 unit does one add per element instead of two multiply-adds.
+__device__ __forceinline__ double nrm2(Cx<double> a) { return nrm(a.re, a.im); }
+__device__ __forceinline__ double nrm2(Cx<float> a) { return (double)fmaf(a.re, a.re, a.im * a.im); }
+
 __device__ double t_block_sum(double v) {
     __shared__ double buf[kT];
     buf[threadIdx.x] = v;
@@ -107,8 +113,7 @@ __global__ void k_t_p1(const Cx<R>* __restrict__ state, int64_t elems, int q, co
         for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
             const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
             const uint64_t idx = (((uint64_t)i >> q) << (q + 1)) | (1ull << q) | lo;
-            const Cx<R> v = s[idx];
-            acc += nrm((double)v.re, (double)v.im);
+            acc += nrm2(s[idx]);
         }
     }
     const double tot = t_block_sum(acc);
@@ -161,13 +166,19 @@ __global__ void k_t_collapse(Cx<R>* __restrict__ state, int64_t elems, int q, co
     const double p = prob[b];
     const double div = p > 0 ? sqrt(p) : 1.0;
     const bool scale = p > 0;
+    // complex128 divides by the FP64 norm exactly as Orrery does; complex64 multiplies by its
+    // FP64 reciprocal rounded once (an FP64 division per element would bind the pass to FP64)
+    const R inv = (R)(1.0 / div);
     const int64_t half = elems >> 1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
         const uint64_t i0 = (((uint64_t)i >> q) << (q + 1)) | lo;
         const uint64_t i1 = i0 | (1ull << q);
         Cx<R> keep = out ? s[i1] : s[i0];
-        if (scale) keep = Cx<R>((R)((double)keep.re / div), (R)((double)keep.im / div));
+        if (scale) {
+            if constexpr (sizeof(R) == 8) keep = Cx<R>(keep.re / div, keep.im / div);
+            else keep = Cx<R>(keep.re * inv, keep.im * inv);
+        }
         const Cx<R> zero(R(0), R(0));
         if (out == 0) {
             s[i0] = keep;
