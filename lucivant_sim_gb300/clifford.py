@@ -165,12 +165,23 @@ def clifford_problem(circuit: Any, noise: Any = None) -> str | None:
     """Why the stabilizer engine can't run ``circuit`` exactly, or None."""
     if circuit.num_qubits > MAX_STABILIZER_QUBITS:
         return f"it has {circuit.num_qubits} qubits; the stabilizer engine allows up to {MAX_STABILIZER_QUBITS}"
+    # circuits repeat their gate matrices and noise rules: check each distinct one once
+    by_arity = noise is not None and all(r.qubits is None for r in getattr(noise, "rules", []))
+    seen_matrix: set[int] = set()
+    seen_noise: set[tuple] = set()
     for g in all_gates(circuit.operations):
-        if clifford_map(g.matrix) is None:
-            return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
-        ch = noise.gate_error(g.name, g.qubits) if noise else None
-        if ch is not None and pauli_noise(ch) is None:
-            return f"the {ch.name} noise after {g.name} isn't a Pauli channel"
+        if id(g.matrix) not in seen_matrix:
+            if clifford_map(g.matrix) is None:
+                return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
+            seen_matrix.add(id(g.matrix))
+        if noise:
+            key = (g.name, len(g.qubits)) if by_arity else (g.name, tuple(g.qubits))
+            if key in seen_noise:
+                continue
+            seen_noise.add(key)
+            ch = noise.gate_error(g.name, g.qubits)
+            if ch is not None and pauli_noise(ch) is None:
+                return f"the {ch.name} noise after {g.name} isn't a Pauli channel"
     return None
 
 

@@ -131,20 +131,33 @@ class Encoder:
 
     def encode(self, gates: list[Any], with_noise: bool) -> np.ndarray:
         out = np.zeros(len(gates), dtype=CGATE)
-        code = out["code"]
-        nz = out["noise"]
-        qa, qb, qc, nq = out["a"], out["b"], out["c"], out["nq"]
-        for i, g in enumerate(gates):
-            c, k = self.gate_code(g)
-            code[i] = c
-            nq[i] = k
+        # per distinct matrix and noise key once; the per-gate loop only gathers plain integers
+        codes, nqs, noise_idx = [], [], []
+        qa, qb, qc = [], [], []
+        by_id: dict[int, tuple[int, int]] = {}
+        by_key: dict[tuple, int] = {}
+        arity_keys = self.by_arity
+        for g in gates:
+            hit = by_id.get(id(g.matrix))
+            if hit is None:
+                hit = by_id[id(g.matrix)] = self.gate_code(g)
+            codes.append(hit[0])
+            nqs.append(hit[1])
             qs = g.qubits
-            qa[i] = qs[0]
-            if len(qs) > 1:
-                qb[i] = qs[1]
-            if len(qs) > 2:
-                qc[i] = qs[2]
-            nz[i] = self.noise_code(g) if with_noise else -1
+            n = len(qs)
+            qa.append(qs[0])
+            qb.append(qs[1] if n > 1 else 0)
+            qc.append(qs[2] if n > 2 else 0)
+            if with_noise:
+                key = (g.name, n) if arity_keys else (g.name, tuple(qs))
+                ni = by_key.get(key)
+                if ni is None:
+                    ni = by_key[key] = self.noise_code(g)
+                noise_idx.append(ni)
+        out["code"] = codes
+        out["nq"] = nqs
+        out["a"], out["b"], out["c"] = qa, qb, qc
+        out["noise"] = noise_idx if with_noise else -1
         return out
 
     def table_bytes(self) -> np.ndarray:
