@@ -163,9 +163,19 @@ static void finish_block(Plan& plan, int pass_first, int first, int count, std::
         b.bits[i] = order[i];
         b.sorted[i] = order[i];
     }
+    std::sort(b.sorted, b.sorted + b.u);
     b.vec = 1;
     if (b.u >= 1 && order[b.u - 1] == 0) b.vec = (b.u >= 2 && order[b.u - 2] == 1) ? 4 : 2;
-    std::sort(b.sorted, b.sorted + b.u);
+    // the group index's bits fill the tile bits around the block's: bits of g between the
+    // (i-1)-th and i-th block bit (ascending) move up by i
+    for (int i = 0; i <= b.u; ++i) {
+        const int lo = i == 0 ? 0 : b.sorted[i - 1] + 1;
+        const int hi = i == b.u ? K : b.sorted[i];
+        unsigned m = 0;
+        for (int t = lo; t < hi; ++t) m |= 1u << t;
+        b.dep[i] = m;
+    }
+    for (int i = b.u + 1; i < 5; ++i) b.dep[i] = 0;
     for (int o = first; o < first + count; ++o) {
         TileOp& t = plan.ops[o];
         int P[8] = {0};
@@ -398,6 +408,21 @@ static int check_plan(const Plan& plan) {
                 return fail(LSG_E_ARG, "internal planning error: a block outside its pass");
             for (int i = 0; !b.generic && i < b.u; ++i)
                 if (b.bits[i] < 0 || b.bits[i] >= pd.K) return fail(LSG_E_ARG, "internal planning error: block bit");
+            if (!b.generic) {  // the deposit masks place every group index where the insertion chain does
+                const uint32_t groups = 1u << (pd.K - b.u);
+                for (uint32_t g0 : {0u, 1u, groups / 2 + 1, groups - 1, 0x55555555u, 0xAAAAAAAAu}) {
+                    const uint32_t g = g0 & (groups - 1);
+                    uint32_t want = g, got = 0;
+                    for (int i = 0; i < b.u; ++i) {
+                        const int sb = b.sorted[i];
+                        want = ((want >> sb) << (sb + 1)) | (want & ((1u << sb) - 1));
+                    }
+                    for (int i = 0; i <= b.u; ++i) got |= (g << i) & b.dep[i];
+                    if (got != want) return fail(LSG_E_ARG, "internal planning error: block deposit masks");
+                    if (b.vec > 1 && (got & (uint32_t)(b.vec - 1)))
+                        return fail(LSG_E_ARG, "internal planning error: vector access misaligned");
+                }
+            }
             covered += b.nops;
         }
         if (covered != pd.nops) return fail(LSG_E_ARG, "internal planning error: blocks do not cover the pass");
@@ -521,12 +546,19 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     const T* pool_dev = reinterpret_cast<const T*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
     T* state = reinterpret_cast<T*>(s->data);
     if (pipe) {
+        // each pass gets the shared memory its own operators need: short passes fit more CTAs per SM
         auto kern = k_tile_pipe<T>;
-        const size_t smem = 2 * tile_bytes + meta;
         LSG_CHECK(allow_smem(kern));
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPipeThreads, smem);
-        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
+        size_t last_smem = 0;
+        int64_t grid = 1;
         for (size_t i = 0; i < p->plan.passes.size(); ++i) {
+            const PassDesc& pd = p->plan.passes[i];
+            const size_t smem = 2 * tile_bytes + (size_t)pd.nops * (sizeof(TileOp) + 16) + (size_t)pd.nblocks * sizeof(BlockDesc);
+            if (smem != last_smem) {
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPipeThreads, smem);
+                grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
+                last_smem = smem;
+            }
             if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
             kern<<<(unsigned)grid, kPipeThreads, smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
                                                                     tiles_per_member, total, status, ctx);

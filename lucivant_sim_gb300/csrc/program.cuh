@@ -28,7 +28,8 @@ struct BlockDesc {
     int sorted[4];
     int vec;  // 1, 2 or 4: the block's last positions are tile bits (1,) 0, so each group holds
               // runs of `vec` consecutive elements (vector shared-memory accesses)
-    int pad;
+    unsigned dep[5];  // group index g -> tile position of its first element: OR of (g << i) & dep[i]
+    int pad[2];
 };
 
 // Operator kinds beyond the public LSG_OP_* set, used by trajectory programs.
@@ -46,7 +47,14 @@ struct TileOp {
     int count;      // mixture branches
     int tmpl;       // register-block code: kind and positions (see tile.cuh)
     int pos[8];     // positions of the operator's bits within its block (0 = block MSB)
+    int pad[2];
 };
+
+// The descriptors are staged back to back in shared memory, followed by 16-byte operator records:
+// each size keeps the next array 16-byte aligned.
+static_assert(sizeof(PassDesc) % 16 == 0, "PassDesc keeps 16-byte alignment");
+static_assert(sizeof(TileOp) % 16 == 0, "TileOp keeps 16-byte alignment");
+static_assert(sizeof(BlockDesc) % 16 == 0, "BlockDesc keeps 16-byte alignment");
 
 struct Plan {
     std::vector<PassDesc> passes;

@@ -651,9 +651,9 @@ __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp
     }
     const int groups = 1 << (tbits - U);
     for (int g = threadIdx.x; g < groups; g += kCompute) {
-        uint32_t base = (uint32_t)g;
+        uint32_t base = 0;
 #pragma unroll
-        for (int i = 0; i < U; ++i) base = ins0(base, blk.sorted[i]);
+        for (int i = 0; i <= U; ++i) base |= ((uint32_t)g << i) & blk.dep[i];
         T v[1 << U];
         load_group<T, U>(tile, base, off, blk.vec, v);
         if constexpr (PLAIN) {
