@@ -231,23 +231,35 @@ def _pauli_basis(k: int) -> list[np.ndarray]:
     return out
 
 
-_BASIS_CACHE: dict[int, tuple[np.ndarray, np.ndarray]] = {}
+_BASIS_CACHE: dict[int, np.ndarray] = {}
 
 
-def _basis(k: int) -> tuple[np.ndarray, np.ndarray]:
-    """(B, Bc): B[j] = vec(P_j) row-major, Bc = conj for the trace."""
+def _paulis(k: int) -> np.ndarray:
+    """The 4^k Paulis stacked, shape (4^k, 2^k, 2^k) (cached)."""
     hit = _BASIS_CACHE.get(k)
     if hit is None:
-        b = np.stack([p.reshape(-1) for p in _pauli_basis(k)])
-        hit = _BASIS_CACHE[k] = (b, b.conj())
+        hit = _BASIS_CACHE[k] = np.stack(_pauli_basis(k))
     return hit
+
+
+def ptm_of_kraus_stack(kraus: np.ndarray) -> np.ndarray:
+    """Real Pauli-transfer matrices of channels given as Kraus stacks, shape (..., nk, d, d):
+    R[a, c] = d^-1 sum_K Tr(P_a K P_c K^dagger), as (..., d^2, d^2)."""
+    d = kraus.shape[-1]
+    k = d.bit_length() - 1
+    p = _paulis(k)
+    r = np.einsum("aij,...njl,clm,...nim->...ac", p, kraus, p, kraus.conj(), optimize=True) / d
+    if np.max(np.abs(r.imag), initial=0.0) > 1e-12:
+        raise SimulationError("a channel without a real Pauli-transfer matrix (not Hermiticity-preserving)")
+    return np.ascontiguousarray(r.real)
 
 
 def ptm_of_superop(s: np.ndarray, k: int) -> np.ndarray:
     """Real Pauli-transfer matrix of a superoperator given on vectorised (row-major) matrices."""
-    b, _bc = _basis(k)
+    p = _paulis(k)
+    b = p.reshape(len(p), -1)
     # R[a, c] = 2^-k Tr(P_a E(P_c)) = 2^-k sum_ij P_a[j, i] E(P_c)[i, j] = 2^-k vec(P_a^T) . (S vec(P_c))
-    bt = np.stack([p.T.reshape(-1) for p in _pauli_basis(k)])
+    bt = p.transpose(0, 2, 1).reshape(len(p), -1)
     r = (bt @ s @ b.T) / (1 << k)
     if np.max(np.abs(r.imag), initial=0.0) > 1e-12:
         raise SimulationError("a channel without a real Pauli-transfer matrix (not Hermiticity-preserving)")
@@ -255,12 +267,11 @@ def ptm_of_superop(s: np.ndarray, k: int) -> np.ndarray:
 
 
 def ptm_of_unitary(u: np.ndarray) -> np.ndarray:
-    k = int(np.log2(u.shape[0]))
-    return ptm_of_superop(np.kron(u, u.conj()), k)
+    return ptm_of_kraus_stack(np.asarray(u, dtype=np.complex128)[None])
 
 
 def ptm_of_kraus(kraus: Any, k: int) -> np.ndarray:
-    return ptm_of_superop(superop(kraus), k)
+    return ptm_of_kraus_stack(np.stack([np.asarray(m, dtype=np.complex128) for m in kraus]))
 
 
 def ptm_depolarizing(p: float, k: int) -> np.ndarray:
@@ -268,15 +279,6 @@ def ptm_depolarizing(p: float, k: int) -> np.ndarray:
     d = np.full(4**k, 1.0 - p)
     d[0] = 1.0
     return np.diag(d)
-
-
-def _signed_perm(r: np.ndarray) -> tuple[np.ndarray, np.ndarray] | None:
-    """(src, phase) with R[i, src[i]] = phase[i] the only nonzero of row i, or None."""
-    nz = r != 0
-    if not ((nz.sum(axis=1) == 1).all() and (nz.sum(axis=0) == 1).all()):
-        return None
-    src = nz.argmax(axis=1)
-    return src, r[np.arange(r.shape[0]), src]
 
 
 def _renames(src: np.ndarray, nbits: int) -> list[tuple[str, int, int]] | None:
@@ -318,38 +320,45 @@ _CX_SRC = np.array([1, 1, 1, 1, 0, 1, 3, 2], dtype=np.complex128)  # unit phases
 _SWAP_SRC = np.array([1, 1, 1, 1, 0, 2, 1, 3], dtype=np.complex128)
 
 
-def _add_ptm(ops: OpList, bits: list[int], mats: list[np.ndarray]) -> None:
-    """Append one Pauli-transfer operator (one matrix per member, or one shared), as the cheapest
-    kind that represents it exactly: diagonal, bit renames plus a diagonal, or dense."""
-    first = mats[0]
+def _add_ptm(ops: OpList, bits: list[int], mats: np.ndarray) -> None:
+    """Append one Pauli-transfer operator — ``mats`` (members, d, d), one matrix per member or a
+    single shared one — as the cheapest kind that represents it exactly: diagonal, bit renames
+    plus a diagonal, or dense."""
+    mats = np.asarray(mats, dtype=np.float64)
+    d = mats.shape[-1]
     nb = len(bits)
-    shared = all(m is first or np.array_equal(m, first) for m in mats[1:])
-    if all(not np.any(m - np.diag(np.diagonal(m))) for m in mats):
-        diags = [np.diagonal(m).astype(np.complex128) for m in mats]
+    shared = bool((mats == mats[0]).all())
+    if shared:
+        mats = mats[:1]
+    idx = np.arange(d)
+    nz = mats != 0
+    offdiag = nz.copy()
+    offdiag[:, idx, idx] = False
+    if not offdiag.any():
+        diags = mats[:, idx, idx].astype(np.complex128)
         if shared:
             if not np.all(diags[0] == 1.0):
                 ops.add(OP_DIAG, bits, diags[0])
         else:
-            ops.add_batched(OP_DIAG, bits, np.stack(diags))
+            ops.add_batched(OP_DIAG, bits, diags)
         return
-    sp = [_signed_perm(m) for m in mats]
-    if all(x is not None for x in sp) and all(np.array_equal(x[0], sp[0][0]) for x in sp[1:]):
-        src = sp[0][0]
+    if (nz.sum(axis=2) == 1).all() and (nz.sum(axis=1) == 1).all() and (nz == nz[0]).all():
+        src = nz[0].argmax(axis=1)
         steps = _renames(src, nb)
         if steps is not None:
             for kind, a, b in steps:
                 ops.add(OP_PERM, [bits[a], bits[b]], _CX_SRC if kind == "cx" else _SWAP_SRC)
-            phases = [x[1].astype(np.complex128) for x in sp]
-            if shared or all(np.array_equal(ph, phases[0]) for ph in phases[1:]):
+            phases = mats[:, idx, src].astype(np.complex128)
+            if shared or (phases == phases[0]).all():
                 if not np.all(phases[0] == 1.0):
                     ops.add(OP_DIAG, bits, phases[0])
             else:
-                ops.add_batched(OP_DIAG, bits, np.stack(phases))
+                ops.add_batched(OP_DIAG, bits, phases)
             return
     if shared:
-        ops.add(OP_MATRIX, bits, first.astype(np.complex128))
+        ops.add(OP_MATRIX, bits, mats[0].astype(np.complex128))
     else:
-        ops.add_batched(OP_MATRIX, bits, np.stack(mats).astype(np.complex128))
+        ops.add_batched(OP_MATRIX, bits, mats.astype(np.complex128))
 
 
 def ptm_capable(circuit: Any, noises: list[Any]) -> bool:
@@ -363,17 +372,28 @@ def ptm_capable(circuit: Any, noises: list[Any]) -> bool:
 
 def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
     """The noisy static evolution of :func:`dm_oplist` as Pauli-transfer operators: each gate
-    with its channel is ONE real operator on the (x, z) digits of its qubits."""
+    with its channel is ONE real operator on the (x, z) digits of its qubits. Channel matrices are
+    formed once per distinct channel and composed with the gate for all members in one product."""
     n = circuit.num_qubits
     ops = OpList()
-    cache: dict[int, tuple[Any, np.ndarray]] = {}
+    cache: dict[tuple[int, ...], np.ndarray] = {}
 
-    def chan_ptm(ch: Any, k: int) -> np.ndarray:
-        hit = cache.get(id(ch))
-        if hit is None or hit[0] is not ch:
-            r = ptm_depolarizing(ch.params[0], k) if ch.analytic_depolarizing else ptm_of_kraus(ch.kraus, k)
-            hit = cache[id(ch)] = (ch, r)
-        return hit[1]
+    def chan_stack(chans: list[Any], k: int) -> np.ndarray:
+        key = tuple(id(ch) for ch in chans)  # the noise models hold their channels for this call
+        hit = cache.get(key)
+        if hit is None:
+            mats = np.empty((len(chans), 4**k, 4**k))
+            todo: dict[int, list[int]] = {}
+            for i, ch in enumerate(chans):
+                if ch.analytic_depolarizing:
+                    mats[i] = ptm_depolarizing(ch.params[0], k)
+                else:
+                    todo.setdefault(len(ch.kraus), []).append(i)
+            for _nk, members in todo.items():  # one einsum per Kraus count
+                kr = np.stack([np.stack([np.asarray(m, dtype=np.complex128) for m in chans[i].kraus]) for i in members])
+                mats[members] = ptm_of_kraus_stack(kr)
+            hit = cache[key] = mats
+        return hit
 
     for op in circuit.operations:
         if op.kind == "gate":
@@ -386,10 +406,10 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
             if any(present) and not all(present):
                 raise ValueError("batched noise models must attach channels to the same gates")
             r_gate = ptm_of_unitary(np.asarray(op.matrix, dtype=np.complex128))
-            mats = [chan_ptm(ch, k) @ r_gate for ch in chans] if chans[0] is not None else [r_gate]
+            mats = chan_stack(chans, k) @ r_gate if chans[0] is not None else r_gate[None]
             _add_ptm(ops, [n + q for q in qs] + list(qs), mats)
         elif op.kind == "reset":
-            _add_ptm(ops, [n + op.qubit, op.qubit], [ptm_of_kraus(RESET_KRAUS, 1)])
+            _add_ptm(ops, [n + op.qubit, op.qubit], ptm_of_kraus(RESET_KRAUS, 1)[None])
         # measurements are deferred; a global phase leaves a density matrix unchanged
     return ops
 
