@@ -125,9 +125,15 @@ def _op_record(op: Any) -> object:
 def is_dynamic(circuit: Any) -> bool:
     """True when outcomes feed conditions, or a qubit is used after being measured or reset
     mid-circuit (``circuit.py:121-138``): such circuits run one shot at a time."""
+    ops = circuit.operations
+    kinds = [op.kind for op in ops]
+    # fast path: gates (and barriers, phases) first, then only measurements: static
+    first = next((i for i, k in enumerate(kinds) if k not in ("gate", "barrier", "gphase")), len(kinds))
+    if all(k in ("measure", "barrier") for k in kinds[first:]):
+        return False
     touched: set[int] = set()
     finished: set[int] = set()
-    for op in circuit.operations:
+    for op in ops:
         kind = op.kind
         if kind == "if":
             return True

@@ -130,34 +130,27 @@ class Encoder:
         return idx
 
     def encode(self, gates: list[Any], with_noise: bool) -> np.ndarray:
-        out = np.zeros(len(gates), dtype=CGATE)
-        # per distinct matrix and noise key once; the per-gate loop only gathers plain integers
-        codes, nqs, noise_idx = [], [], []
-        qa, qb, qc = [], [], []
-        by_id: dict[int, tuple[int, int]] = {}
-        by_key: dict[tuple, int] = {}
-        arity_keys = self.by_arity
-        for g in gates:
-            hit = by_id.get(id(g.matrix))
-            if hit is None:
-                hit = by_id[id(g.matrix)] = self.gate_code(g)
-            codes.append(hit[0])
-            nqs.append(hit[1])
-            qs = g.qubits
-            n = len(qs)
-            qa.append(qs[0])
-            qb.append(qs[1] if n > 1 else 0)
-            qc.append(qs[2] if n > 2 else 0)
-            if with_noise:
-                key = (g.name, n) if arity_keys else (g.name, tuple(qs))
-                ni = by_key.get(key)
-                if ni is None:
-                    ni = by_key[key] = self.noise_code(g)
-                noise_idx.append(ni)
-        out["code"] = codes
-        out["nq"] = nqs
-        out["a"], out["b"], out["c"] = qa, qb, qc
-        out["noise"] = noise_idx if with_noise else -1
+        n = len(gates)
+        out = np.zeros(n, dtype=CGATE)
+        # each distinct matrix and noise key once; per gate only attribute reads into NumPy arrays
+        ids = np.fromiter((id(g.matrix) for g in gates), dtype=np.int64, count=n)
+        _u, first, inv = np.unique(ids, return_index=True, return_inverse=True)
+        codes = np.array([self.gate_code(gates[int(f)]) for f in first], dtype=np.int32).reshape(-1, 2)
+        out["code"], out["nq"] = codes[inv, 0], codes[inv, 1]
+        qs = [g.qubits for g in gates]
+        out["a"] = np.fromiter((q[0] for q in qs), dtype=np.int16, count=n)
+        out["b"] = np.fromiter((q[1] if len(q) > 1 else 0 for q in qs), dtype=np.int16, count=n)
+        out["c"] = np.fromiter((q[2] if len(q) > 2 else 0 for q in qs), dtype=np.int16, count=n)
+        if not with_noise:
+            out["noise"] = -1
+        elif self.by_arity:  # rules by gate name only: key (name, arity)
+            name_id: dict[str, int] = {}
+            nid = np.fromiter((name_id.setdefault(g.name, len(name_id)) for g in gates), dtype=np.int64, count=n)
+            _k, kfirst, kinv = np.unique(nid * 8 + out["nq"], return_index=True, return_inverse=True)
+            idx = np.array([self.noise_code(gates[int(f)]) for f in kfirst], dtype=np.int16)
+            out["noise"] = idx[kinv]
+        else:
+            out["noise"] = [self.noise_code(g) for g in gates]
         return out
 
     def table_bytes(self) -> np.ndarray:
