@@ -696,6 +696,18 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
                 t.stride = t.stride ? stride : 0;
             }
         }
+    // every register-block operator now carries a kernel code (mixtures are resolved per member)
+    for (const PassDesc& pd : p->plan.passes)
+        for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
+            const BlockDesc& blk = p->plan.blocks[bi];
+            for (int o = blk.first; !blk.generic && o < blk.first + blk.nops; ++o) {
+                const int c = p->plan.ops[pd.first_op + o].tmpl;
+                if (!((c >= 0 && c < kT_CODES) || (c >= kT_MIX1 && c < kT_MIX2 + 16))) {
+                    delete p;
+                    return fail(LSG_E_ARG, "internal planning error: operator code %d", c);
+                }
+            }
+        }
     const int64_t all_entries = pool_entries + (int64_t)ext.size() / 2;
     std::vector<double> merged;
     if (!ext.empty()) {

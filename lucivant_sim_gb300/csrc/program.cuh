@@ -69,15 +69,18 @@ constexpr int kT_PERM1 = 20;    // + P
 constexpr int kT_PERM2 = 24;    // + 4 * P0 + P1
 constexpr int kT_DEPOL1 = 40;   // + 4 * Prow + Pcol
 constexpr int kT_DEPOL2 = 56;   // canonical positions (row a, row b, col a, col b) = (0, 1, 2, 3)
-constexpr int kT_DIAG = 57;
+constexpr int kT_DIAGB = 57;    // diagonal re-indexed by the host in block order: v[e] *= m[e]
 constexpr int kT_SCALE = 58;
-constexpr int kT_MIX1 = 60;     // + P
-constexpr int kT_MIX2 = 64;     // + 4 * P0 + P1
-constexpr int kT_X1 = 80;       // + P: unit-phase X (register swap)
-constexpr int kT_CX = 84;       // + 4 * Pcontrol + Ptarget: unit-phase CX (register swap)
-constexpr int kT_SWAP = 100;    // + 4 * P0 + P1
-constexpr int kT_DIAGB = 116;   // diagonal re-indexed by the host in block order: v[e] *= m[e]
-constexpr int kT_TPD2 = 120;    // + 4 * P0 + P1: real 4x4 transfer matrix whose row 0 is (1,0,0,0)
+constexpr int kT_TPD2 = 59;     // + 4 * P0 + P1: real 4x4 transfer matrix whose row 0 is (1,0,0,0)
+constexpr int kT_X1 = 75;       // + P: unit-phase X (register swap)
+constexpr int kT_CX = 79;       // + 4 * Pcontrol + Ptarget: unit-phase CX (register swap)
+constexpr int kT_SWAP = 95;     // + 4 * P0 + P1
+constexpr int kT_CODES = 111;   // the kernel's codes are exactly 0 .. kT_CODES-1 (a dense switch)
+// host-side markers, rewritten before upload: mixtures become dense codes per member in the kernel,
+// diagonals become kT_DIAGB
+constexpr int kT_MIX1 = 111;    // + P
+constexpr int kT_MIX2 = 115;    // + 4 * P0 + P1
+constexpr int kT_DIAG = 131;
 constexpr int kT_GENERIC = -1;
 // The greedy fusion planner (csrc/engine.cu): lsg_op list -> passes of tile-local operators.
 // pred/draw/count (may be null) give trajectory operators their predicate bit, uniform offset and
