@@ -352,6 +352,9 @@ def gb300_arm(args: argparse.Namespace) -> None:
     real = batch.reg.real
     kernel = f"k_tile_pipe<{'float' if args.precision == 'c64' else 'double'}>" if real else \
         f"k_tile_pipe<Cx<{'float' if args.precision == 'c64' else 'double'}>>"
+    specialized = batch.program.specialized
+    if specialized:  # the passes run as kernels compiled for this circuit at run time
+        kernel = f"lsg_pass_0..{passes - 1} (pipe_kernel specializations of {kernel})"
     stream = torch.cuda.ExternalStream(batch.reg.stream())
 
     def step(timed: list | None = None) -> tuple:
@@ -456,6 +459,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "config": dict(config_block(args), form=form, l2=f"register {reg_bytes / 2**30:.0f} GiB > L2: no flush"),
             "circuits_per_s": cps,
             "fused_passes": passes,
+            "specialized_passes": specialized,
             "plain_c128": {
                 "circuits_per_s": world / plain_s,
                 "ms_per_circuit": 1000 * plain_s,

@@ -116,6 +116,15 @@ int lsg_program_run(lsg_program p, lsg_state s);
 int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms);
 /* Number of fused passes, and algorithmic HBM bytes of one run (2 x register bytes per pass). */
 int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run);
+/* 1 when the program's passes run as kernels specialized for it at creation (NVRTC, LSG_JIT=1),
+ * 0 when the generic pass kernel interprets its operator records, negative on error. */
+int lsg_program_specialized(lsg_program p);
+/* Host-only diagnostic (no device is touched): the CUDA source of the specialized passes a
+ * program of these operators would get (into buf, at most cap bytes with the terminating zero;
+ * *len = full length, 0 when the program would be interpreted), and with `compile` != 0 its NVRTC
+ * compilation for sm_103a (LSG_E_ARG with the compiler log when it fails). */
+int lsg_program_source(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                       int64_t pool_entries, int compile, char* buf, int64_t cap, int64_t* len);
 int lsg_program_free(lsg_program p);
 /* Host-only: the number of fused passes lsg_apply would run for these operators on a register of
  * nbits bits (no device is touched; used for sizing and for algorithmic-byte accounting). */

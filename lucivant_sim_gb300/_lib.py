@@ -70,8 +70,10 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_program_run": (C.c_int, [_P, _P]),
     "lsg_program_run_timed": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     "lsg_program_info": (C.c_int, [_P, _PI32, _PI64]),
+    "lsg_program_specialized": (C.c_int, [_P]),
     "lsg_program_free": (C.c_int, [_P]),
     "lsg_plan": (C.c_int, [C.c_int, C.c_int, _P, _I32, _PI32]),
+    "lsg_program_source": (C.c_int, [C.c_int, C.c_int, _I64, _P, _I32, _PD, _I64, C.c_int, C.c_char_p, _I64, _PI64]),
     "lsg_state_sync": (C.c_int, [_P]),
     "lsg_state_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lsg_collapse": (C.c_int, [_P, C.c_int, C.c_int, _D, _I64]),
@@ -146,6 +148,19 @@ def plan_passes(nbits: int, precision: int, ops: "OpList") -> int:
     out = C.c_int32(0)
     check(library().lsg_plan(nbits, precision, table.ctypes.data, len(table), C.byref(out)))
     return int(out.value)
+
+
+def specialized_source(nbits: int, precision: int, batch: int, ops: "OpList", compile: bool = False) -> str:
+    """The CUDA source of the passes a program of ``ops`` would be specialized to ("" when it
+    would be interpreted); with ``compile`` also compiled with NVRTC (host only, no device)."""
+    table, pool = ops.packed()
+    n = C.c_int64(0)
+    lib = library()
+    args = (nbits, precision, batch, table.ctypes.data, len(table), ptr(pool, C.c_double), pool.size // 2)
+    check(lib.lsg_program_source(*args, 0, None, 0, C.byref(n)))
+    buf = C.create_string_buffer(int(n.value) + 1)
+    check(lib.lsg_program_source(*args, int(compile), buf, len(buf), C.byref(n)))
+    return buf.value.decode()
 
 
 def ptr(a: np.ndarray, ctype: Any) -> Any:
@@ -331,6 +346,10 @@ class Program:
         passes, nbytes = C.c_int32(0), C.c_int64(0)
         check(self.lib.lsg_program_info(handle, C.byref(passes), C.byref(nbytes)))
         self.passes, self.bytes_per_run = int(passes.value), int(nbytes.value)
+        rc = self.lib.lsg_program_specialized(handle)
+        if rc < 0:
+            check(rc)
+        self.specialized = rc == 1
 
     def run(self, reg: Register) -> None:
         check(self.lib.lsg_program_run(self.handle, reg.handle))

@@ -3,12 +3,14 @@
 // copies) the tile kernels are built on.
 #pragma once
 
+#ifndef __CUDACC_RTC__  // (run-time compiled passes see the device parts only)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <cstdarg>
 #include <cstdio>
 #include <string>
+#endif
 
 #include "../../include/lsg.h"
 
@@ -33,10 +35,12 @@ void clear_error();
         if (s_ != LSG_OK) return s_; \
     } while (0)
 
+#ifndef __CUDACC_RTC__
 // Device-side status word (one per device, in global memory): kernels that give up on a
 // bounded wait record a code there. Read and cleared by check_device_status().
 int* device_status();
 int check_device_status(cudaStream_t stream);
+#endif
 
 // Iteration limit for every spin-wait in the engine's kernels (mbarrier waits). A wait that
 // exhausts it records LSG_E_TIMEOUT in g_device_status and the kernel returns early.
@@ -44,6 +48,7 @@ constexpr long long kSpinLimit = 1ll << 28;
 
 constexpr int kMaxBits = 26;  // 2^26 amplitudes per member (Orrery's statevector guard)
 
+#ifndef __CUDACC_RTC__
 // ---------------------------------------------------------------- register handle
 
 // A device buffer that grows on demand. With a stream it is stream-ordered (cudaMallocAsync /
@@ -78,6 +83,9 @@ struct lsg_state_s {
     bool real() const { return precision == LSG_R64 || precision == LSG_R32; }
     size_t member_bytes() const { return elem_bytes() * (size_t)elems; }
 };
+#else
+}  // namespace lsg
+#endif  // !__CUDACC_RTC__
 
 namespace lsg {
 

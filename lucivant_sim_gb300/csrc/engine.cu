@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "jit.cuh"
 #include "program.cuh"
 #include "tile.cuh"
 
@@ -500,6 +501,7 @@ struct lsg_program_s {
     size_t smem = 0;
     int K = 0;
     std::vector<cudaEvent_t> events;
+    std::shared_ptr<lsg::JitPasses> jit;  // specialized passes, when the program could be specialized
 };
 
 namespace lsg {
@@ -545,6 +547,12 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     const BlockDesc* blk_dev = reinterpret_cast<const BlockDesc*>(ops_dev + p->plan.ops.size());
     const T* pool_dev = reinterpret_cast<const T*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
     T* state = reinterpret_cast<T*>(s->data);
+    if (p->jit && bulk && ctx.u == nullptr) {
+        LSG_CHECK(jit_launch(*p->jit, p->plan, state, s->elems, pd_dev, sizeof(PassDesc), pool_dev, tiles_per_member,
+                             total, status, tile_bytes, s->stream, marks));
+        if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
+        return LSG_OK;
+    }
     if (pipe) {
         // each pass gets the shared memory its own operators need: short passes fit more CTAs per SM
         auto kern = k_tile_pipe<T>;
@@ -579,9 +587,11 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     return LSG_OK;
 }
 
-int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
-                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out,
-                      cudaStream_t stream) {
+// Plan and lower `ops`; with `upload`, copy the program to the device (otherwise only the host
+// plan is made: no device call).
+static int program_build(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                         int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out,
+                         cudaStream_t stream, bool upload) {
     auto* p = new lsg_program_s();
     p->nbits = nbits;
     p->precision = precision;
@@ -725,6 +735,10 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
         delete p;
         return fail(LSG_E_ARG, "a pass needs more than 220 KB of shared memory");
     }
+    if (!upload) {
+        *out = p;
+        return LSG_OK;
+    }
     const size_t head = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp) +
                         p->plan.blocks.size() * sizeof(BlockDesc);
     p->head_aligned = (head + 255) & ~size_t(255);
@@ -765,11 +779,45 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
     return LSG_OK;
 }
 
+int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                      int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out,
+                      cudaStream_t stream) {
+    return program_build(nbits, precision, batch, ops, nops, pool, pool_entries, pred, draw, count, out, stream, true);
+}
+
+// Launch bound of specialized passes: CTAs per SM (the interpreter's pipe_ctas for the element).
+static int jit_ctas(int precision) {
+    return (precision == LSG_C128 || precision == LSG_R64) ? 1 : lsg_elem_bytes(precision) == 4 ? 3 : 2;
+}
+
 static int program_create(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
                           const double* pool, int64_t pool_entries, lsg_program_s** out, cudaStream_t stream) {
     LSG_CHECK(validate_ops(nbits, precision, batch, ops, nops, pool, pool_entries));
     return program_create_ex(nbits, precision, batch, ops, nops, pool, pool_entries, nullptr, nullptr, nullptr, out,
                              stream);
+}
+
+// A program for repeated runs (lsg_program_create): planned, uploaded, and its passes
+// specialized at run time when they can be (the compiled module is cached by its source, so
+// programs of the same shape share it).
+static int program_create_jit(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops,
+                              const double* pool, int64_t pool_entries, lsg_program_s** out, cudaStream_t stream) {
+    LSG_CHECK(program_create(nbits, precision, batch, ops, nops, pool, pool_entries, out, stream));
+    lsg_program_s* p = *out;
+    const size_t eb = lsg_elem_bytes(precision);
+    bool bulk = true;
+    for (const PassDesc& pd : p->plan.passes) bulk = bulk && ((eb << pd.L) % 16) == 0;
+    const int ctas = jit_ctas(precision);
+    const int64_t bytes_per_run = 2 * ((int64_t)eb << nbits) * batch * (int64_t)p->plan.passes.size();
+    if (bulk && jit_wanted(bytes_per_run)) p->jit = jit_build(p->plan, precision, ctas);
+    if (const char* path = getenv("LSG_JIT_DUMP")) {  // diagnostics: the specialized source of this program
+        if (FILE* f = std::fopen(path, "w")) {
+            const std::string src = jit_source(p->plan, precision, ctas);
+            std::fwrite(src.data(), 1, src.size(), f);
+            std::fclose(f);
+        }
+    }
+    return LSG_OK;
 }
 
 void program_destroy(lsg_program_s* p) {
@@ -1059,7 +1107,7 @@ int lsg_program_create(lsg_state shape, const lsg_op* ops, int32_t nops, const d
     clear_error();
     if (!shape || !out) return fail(LSG_E_ARG, "null argument");
     *out = nullptr;
-    return program_create(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out,
+    return program_create_jit(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out,
                           shape->stream);
 }
 
@@ -1090,6 +1138,32 @@ int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run) {
     const int64_t member = (int64_t)lsg_elem_bytes(p->precision) << p->nbits;
     if (passes) *passes = (int32_t)p->plan.passes.size();
     if (bytes_per_run) *bytes_per_run = 2 * member * p->batch * (int64_t)p->plan.passes.size();
+    return LSG_OK;
+}
+
+int lsg_program_specialized(lsg_program p) {
+    clear_error();
+    if (!p) return fail(LSG_E_ARG, "null program");
+    return p->jit ? 1 : 0;
+}
+
+int lsg_program_source(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
+                       int64_t pool_entries, int compile, char* buf, int64_t cap, int64_t* len) {
+    clear_error();
+    if (nbits < 0 || nbits > kMaxBits || batch < 1) return fail(LSG_E_ARG, "bad register shape");
+    LSG_CHECK(validate_ops(nbits, precision, batch, ops, nops, pool, pool_entries));
+    lsg_program_s* p = nullptr;
+    LSG_CHECK(program_build(nbits, precision, batch, ops, nops, pool, pool_entries, nullptr, nullptr, nullptr, &p,
+                            nullptr, false));
+    const std::string src = jit_source(p->plan, precision, jit_ctas(precision));
+    delete p;
+    if (len) *len = (int64_t)src.size();
+    if (buf && cap > 0) {
+        const size_t n = std::min<size_t>(src.size(), (size_t)cap - 1);
+        std::memcpy(buf, src.data(), n);
+        buf[n] = '\0';
+    }
+    if (compile && !src.empty()) return jit_compile_check(src);
     return LSG_OK;
 }
 

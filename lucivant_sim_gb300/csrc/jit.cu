@@ -1,0 +1,355 @@
+// Passes specialized at run time. A planned program's passes are written out as CUDA source —
+// for every register block its tile bits, group offsets, operators and data offsets as
+// compile-time constants, the operators as a straight-line sequence of the register-block
+// functions of tile.cuh — compiled once with NVRTC for sm_103a and launched through the driver
+// API on the register's stream. The interpreter (k_tile_pipe) decodes each operator at run time:
+// a dispatch per operator and group, register moves where the cases merge, address arithmetic for
+// run-time bit positions. Specialized passes keep only the loads, the arithmetic and the stores.
+//
+// NVRTC and the driver entry points are looked up at run time (dlopen, cudaGetDriverEntryPoint):
+// the library loads without them and programs fall back to the interpreter when they are
+// missing. Compiled modules are cached by their source for the life of the process.
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "jit.cuh"
+#include "jit_headers.inc"  // generated by build.py: the device headers as strings
+
+namespace lsg {
+namespace {
+
+struct Nvrtc {
+    bool ok = false;
+    decltype(&nvrtcCreateProgram) create = nullptr;
+    decltype(&nvrtcCompileProgram) compile = nullptr;
+    decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+    decltype(&nvrtcGetProgramLog) log = nullptr;
+    decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+    decltype(&nvrtcGetCUBIN) cubin = nullptr;
+    decltype(&nvrtcDestroyProgram) destroy = nullptr;
+};
+
+const Nvrtc& nvrtc() {
+    static Nvrtc n = [] {
+        Nvrtc r;
+        void* h = nullptr;
+        for (const char* name : {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13"})
+            if ((h = dlopen(name, RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) return r;
+        r.create = reinterpret_cast<decltype(r.create)>(dlsym(h, "nvrtcCreateProgram"));
+        r.compile = reinterpret_cast<decltype(r.compile)>(dlsym(h, "nvrtcCompileProgram"));
+        r.log_size = reinterpret_cast<decltype(r.log_size)>(dlsym(h, "nvrtcGetProgramLogSize"));
+        r.log = reinterpret_cast<decltype(r.log)>(dlsym(h, "nvrtcGetProgramLog"));
+        r.cubin_size = reinterpret_cast<decltype(r.cubin_size)>(dlsym(h, "nvrtcGetCUBINSize"));
+        r.cubin = reinterpret_cast<decltype(r.cubin)>(dlsym(h, "nvrtcGetCUBIN"));
+        r.destroy = reinterpret_cast<decltype(r.destroy)>(dlsym(h, "nvrtcDestroyProgram"));
+        r.ok = r.create && r.compile && r.log_size && r.log && r.cubin_size && r.cubin && r.destroy;
+        return r;
+    }();
+    return n;
+}
+
+struct Driver {
+    bool ok = false;
+    CUresult (*module_load)(CUmodule*, const void*) = nullptr;
+    CUresult (*get_function)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
+                       void**, void**) = nullptr;
+    CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+};
+
+const Driver& driver() {
+    static Driver d = [] {
+        Driver r;
+        auto get = [](const char* sym, void** fp) {
+            cudaDriverEntryPointQueryResult q;
+            return cudaGetDriverEntryPointByVersion(sym, fp, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+                   q == cudaDriverEntryPointSuccess && *fp;
+        };
+        r.ok = get("cuModuleLoadData", reinterpret_cast<void**>(&r.module_load)) &&
+               get("cuModuleGetFunction", reinterpret_cast<void**>(&r.get_function)) &&
+               get("cuLaunchKernel", reinterpret_cast<void**>(&r.launch)) &&
+               get("cuFuncSetAttribute", reinterpret_cast<void**>(&r.set_attribute)) &&
+               get("cuOccupancyMaxActiveBlocksPerMultiprocessor", reinterpret_cast<void**>(&r.occupancy));
+        cudaGetLastError();
+        return r;
+    }();
+    return d;
+}
+
+const char* type_name(int precision) {
+    switch (precision) {
+        case LSG_C128: return "lsg::Cx<double>";
+        case LSG_C64: return "lsg::Cx<float>";
+        case LSG_R64: return "double";
+        default: return "float";
+    }
+}
+
+// One register-block operator as a call with compile-time positions; false for kinds that
+// specialized passes do not take (mixtures and other trajectory operators).
+bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int at) {
+    const int c = t.tmpl;
+    auto two = [&](const char* fn, int base) {
+        const int r = c - base;
+        o << fn << "<" << T << ", " << U << ", " << r / 4 << ", " << r % 4 << ">";
+    };
+    auto one = [&](const char* fn, int base) { o << fn << "<" << T << ", " << U << ", " << (c - base) << ">"; };
+    bool data = true;
+    if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) one("rb_dense1", kT_DENSE1);
+    else if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) two("rb_dense2", kT_DENSE2);
+    else if (c >= kT_TPD2 && c < kT_TPD2 + 16) two("rb_tpd2", kT_TPD2);
+    else if (c >= kT_PERM1 && c < kT_PERM1 + 4) one("rb_perm1", kT_PERM1);
+    else if (c >= kT_PERM2 && c < kT_PERM2 + 16) two("rb_perm2", kT_PERM2);
+    else if (c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) two("rb_depol1", kT_DEPOL1);
+    else if (c == kT_DEPOL2 && U == 4) o << "rb_depol2<" << T << ">";
+    else if (c == kT_DIAGB) o << "rb_diagb<" << T << ", " << U << ">";
+    else if (c == kT_SCALE) o << "rb_scale<" << T << ", " << U << ">";
+    else if (c >= kT_X1 && c < kT_X1 + 4) one("rb_x", kT_X1), data = false;
+    else if (c >= kT_CX && c < kT_CX + 16) two("rb_cx", kT_CX), data = false;
+    else if (c >= kT_SWAP && c < kT_SWAP + 16) two("rb_swap", kT_SWAP), data = false;
+    else return false;
+    const std::string v = at ? "v + " + std::to_string(at) : std::string("v");
+    if (data) o << "(" << v << ", data + " << t.data << "LL + member * " << t.stride << "LL);\n";
+    else o << "(" << v << ");\n";
+    return true;
+}
+
+// The 32-bit registers a thread may spend on its blocks' amplitudes at `ctas` CTAs per SM.
+int state_reg_budget(int ctas) { return ctas >= 3 ? 32 : ctas == 2 ? 64 : 128; }
+
+std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_bytes, int ctas) {
+    const PassDesc& pd = plan.passes[pi];
+    const char* T = type_name(precision);
+    std::ostringstream o;
+    o << "struct Body" << pi << " {\n  static __device__ __forceinline__ void run(" << T << "* tile, const " << T
+      << "* __restrict__ data, long long member) {\n";
+    for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
+        const BlockDesc& b = plan.blocks[bi];
+        if (b.generic) return "";
+        const int U = b.u, n = 1 << U, groups = 1 << (pd.K - U);
+        // Two groups per thread when tile bit 0 is not a block bit: the pair (tile bit 0 = 0, 1)
+        // moves as one wider shared-memory access and every operator's coefficients, loaded once,
+        // serve both groups (the two calls read the same addresses).
+        const int W = (b.sorted[0] != 0 && groups >= 2 && 2 * n * elem_bytes / 4 <= state_reg_budget(ctas)) ? 2 : 1;
+        const int run = W == 2 ? 1 : std::min(std::max(b.vec, 1), std::max(1, 16 / elem_bytes));
+        o << "    cbar();\n    for (int g = threadIdx.x; g < " << groups / W << "; g += kCompute) {\n";
+        o << "      const uint32_t G = uint32_t(g)" << (W == 2 ? " << 1" : "") << ";\n";
+        o << "      const uint32_t base =";
+        for (int i = 0; i <= U; ++i) o << (i ? " |" : "") << " ((G << " << i << ") & " << b.dep[i] << "u)";
+        o << ";\n      " << T << " v[" << n * W << "];\n";
+        std::vector<uint32_t> off(n);
+        for (int e = 0; e < n; ++e) {
+            uint32_t a = 0;
+            for (int i = 0; i < U; ++i)
+                if ((e >> (U - 1 - i)) & 1) a |= 1u << b.bits[i];
+            off[e] = a;
+        }
+        for (int e = 0; e < n; e += run) {
+            if (W == 2)
+                o << "      ld_split<" << T << ">(tile + (base + " << off[e] << "u), v[" << e << "], v[" << n + e << "]);\n";
+            else
+                o << "      ld_run<" << T << ", " << run << ">(tile + (base + " << off[e] << "u), v + " << e << ");\n";
+        }
+        for (int k = b.first; k < b.first + b.nops; ++k) {
+            for (int w = 0; w < W; ++w) {
+                o << "      ";
+                if (!op_call(o, plan.ops[pd.first_op + k], U, T, w * n)) return "";
+            }
+        }
+        for (int e = 0; e < n; e += run) {
+            if (W == 2)
+                o << "      st_split<" << T << ">(tile + (base + " << off[e] << "u), v[" << e << "], v[" << n + e << "]);\n";
+            else
+                o << "      st_run<" << T << ", " << run << ">(tile + (base + " << off[e] << "u), v + " << e << ");\n";
+        }
+        o << "    }\n";
+    }
+    o << "    cbar();\n  }\n};\n";
+    return o.str();
+}
+
+std::mutex g_mu;
+std::map<std::string, std::shared_ptr<JitPasses>> g_cache;
+
+}  // namespace
+
+int jit_mode() {
+    const char* env = getenv("LSG_JIT");
+    if (!env || !env[0]) return 2;
+    return env[0] == '0' ? 0 : 1;
+}
+
+bool jit_wanted(int64_t bytes_per_run) {
+    const int mode = jit_mode();
+    if (mode != 2) return mode == 1;
+    const char* env = getenv("LSG_JIT_MIN_BYTES");
+    const int64_t min_bytes = env ? std::atoll(env) : (256ll << 30);
+    return bytes_per_run >= min_bytes;
+}
+
+namespace {
+
+// Pass i's body and kernel, or "" when the specializer does not take one of its blocks.
+std::string pass_kernel_source(const Plan& plan, size_t i, int precision, int ctas) {
+    const char* T = type_name(precision);
+    const std::string body = pass_source(plan, i, precision, (int)lsg_elem_bytes(precision), ctas);
+    if (body.empty()) return "";
+    std::ostringstream o;
+    o << body << "extern \"C\" __global__ void __launch_bounds__(" << kPipeThreadsHost << ", " << ctas
+      << ") lsg_pass_" << i << "(" << T << "* state, long long me, const PassDesc* pg, const " << T
+      << "* data, long long tpm, long long total, int* status) {\n  pipe_kernel<" << T << ", Body" << i
+      << ">(state, me, pg, data, tpm, total, status);\n}\n";
+    return o.str();
+}
+
+const char* const kPrelude = "#include \"tile.cuh\"\nusing namespace lsg;\n";
+
+// One translation unit to a cubin (empty on failure; the log into `log`, or on stderr with
+// LSG_JIT_LOG).
+std::vector<char> compile_unit(const std::string& source, std::string* log_out = nullptr) {
+    const Nvrtc& rt = nvrtc();
+    std::vector<char> cubin;
+    nvrtcProgram prog;
+    if (rt.create(&prog, source.c_str(), "lsg_passes.cu", kJitHeaderCount, kJitHeaderSources, kJitHeaderNames) !=
+        NVRTC_SUCCESS)
+        return cubin;
+    // -default-device: the public header's host declarations are harmless device ones here
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device"};
+    const nvrtcResult cr = rt.compile(prog, 3, opts);
+    size_t bytes = 0;
+    if (cr == NVRTC_SUCCESS && rt.cubin_size(prog, &bytes) == NVRTC_SUCCESS && bytes) {
+        cubin.resize(bytes);
+        if (rt.cubin(prog, cubin.data()) != NVRTC_SUCCESS) cubin.clear();
+    } else if (log_out || getenv("LSG_JIT_LOG")) {
+        size_t n = 0;
+        rt.log_size(prog, &n);
+        std::string log(n, '\0');
+        rt.log(prog, &log[0]);
+        if (log_out) *log_out = log;
+        else std::fprintf(stderr, "pass specialization failed:\n%s\n", log.c_str());
+    }
+    rt.destroy(&prog);
+    return cubin;
+}
+
+}  // namespace
+
+int jit_compile_check(const std::string& source) {
+    if (!nvrtc().ok) return fail(LSG_E_STATE, "NVRTC (libnvrtc.so.13) is not available");
+    std::string log;
+    if (compile_unit(source, &log).empty()) return fail(LSG_E_ARG, "specialized passes do not compile: %.900s", log.c_str());
+    return LSG_OK;
+}
+
+std::string jit_source(const Plan& plan, int precision, int ctas) {
+    std::string src = kPrelude;
+    for (size_t i = 0; i < plan.passes.size(); ++i) {
+        const std::string k = pass_kernel_source(plan, i, precision, ctas);
+        if (k.empty()) return "";  // a pass the specializer does not take: interpret them all
+        src += k;
+    }
+    return src;
+}
+
+std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas) {
+    const size_t np = plan.passes.size();
+    if (np == 0) return nullptr;
+    std::vector<std::string> kernels(np);
+    size_t total_len = 0;
+    for (size_t i = 0; i < np; ++i) {
+        kernels[i] = pass_kernel_source(plan, i, precision, ctas);
+        if (kernels[i].empty()) return nullptr;  // a pass the specializer does not take: interpret them all
+        total_len += kernels[i].size();
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::string key = std::to_string(dev) + "\n";
+    key.reserve(total_len + 16);
+    for (const std::string& k : kernels) key += k;
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto hit = g_cache.find(key);
+    if (hit != g_cache.end()) return hit->second;
+    const Nvrtc& rt = nvrtc();
+    const Driver& drv = driver();
+    std::shared_ptr<JitPasses> out;
+    if (rt.ok && drv.ok) {
+        // passes are independent translation units: compile them in parallel, in chunks of
+        // about equal source length (NVRTC programs are compiled concurrently on host threads)
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const size_t nchunks = std::min<size_t>({np, (size_t)hw, 16});
+        std::vector<std::string> units(nchunks, kPrelude);
+        std::vector<std::vector<size_t>> members(nchunks);
+        std::vector<size_t> load(nchunks, 0);
+        for (size_t i = 0; i < np; ++i) {
+            const size_t c = std::min_element(load.begin(), load.end()) - load.begin();
+            units[c] += kernels[i];
+            members[c].push_back(i);
+            load[c] += kernels[i].size();
+        }
+        std::vector<std::vector<char>> cubins(nchunks);
+        std::vector<std::thread> workers;
+        for (size_t c = 1; c < nchunks; ++c) workers.emplace_back([&, c] { cubins[c] = compile_unit(units[c]); });
+        cubins[0] = compile_unit(units[0]);
+        for (std::thread& w : workers) w.join();
+        auto jp = std::make_shared<JitPasses>();
+        jp->fns.resize(np);
+        jp->per_sm.resize(np, 1);
+        const size_t eb = lsg_elem_bytes(precision);
+        bool ok = true;
+        for (size_t c = 0; c < nchunks && ok; ++c) {
+            CUmodule mod;
+            ok = !cubins[c].empty() && drv.module_load(&mod, cubins[c].data()) == CUDA_SUCCESS;
+            for (size_t j = 0; j < members[c].size() && ok; ++j) {
+                const size_t i = members[c][j];
+                const std::string name = "lsg_pass_" + std::to_string(i);
+                CUfunction f;
+                const size_t smem = 2 * (eb << plan.passes[i].K);  // the two-tile ring
+                ok = drv.get_function(&f, mod, name.c_str()) == CUDA_SUCCESS &&
+                     drv.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) == CUDA_SUCCESS &&
+                     drv.occupancy(&jp->per_sm[i], f, kPipeThreadsHost, smem) == CUDA_SUCCESS;
+                jp->fns[i] = f;
+            }
+        }
+        if (ok) out = jp;
+    }
+    g_cache[key] = out;  // a failure is remembered too: the interpreter runs those programs
+    return out;
+}
+
+int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t member_elems, const void* pass_dev,
+               size_t pass_stride, const void* data, int64_t tiles_per_member, int64_t total, int* status,
+               size_t tile_bytes, cudaStream_t stream, cudaEvent_t* marks) {
+    const Driver& drv = driver();
+    int dev = 0, sms = 0;
+    LSG_CUDA(cudaGetDevice(&dev));
+    LSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t smem = 2 * tile_bytes;
+    for (size_t i = 0; i < plan.passes.size(); ++i) {
+        CUfunction f = reinterpret_cast<CUfunction>(jp.fns[i]);
+        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(jp.per_sm[i], 1)));
+        const void* pg = static_cast<const unsigned char*>(pass_dev) + i * pass_stride;
+        long long me = member_elems, tpm = tiles_per_member, tot = total;
+        void* args[] = {&state, &me, &pg, &data, &tpm, &tot, &status};
+        if (marks) LSG_CUDA(cudaEventRecord(marks[i], stream));
+        if (drv.launch(f, (unsigned)grid, 1, 1, kPipeThreadsHost, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr) !=
+            CUDA_SUCCESS)
+            return fail(LSG_E_CUDA, "launching a specialized pass failed");
+    }
+    return LSG_OK;
+}
+
+}  // namespace lsg

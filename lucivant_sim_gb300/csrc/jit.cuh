@@ -1,0 +1,45 @@
+// Run-time specialized passes (csrc/jit.cu): host interface.
+#pragma once
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "program.cuh"
+
+namespace lsg {
+
+// Threads of a pipelined pass CTA (256 compute threads and the producer warp; tile.cuh).
+constexpr int kPipeThreadsHost = 288;
+
+// The compiled kernels of one program's passes (CUfunction handles, one per pass).
+struct JitPasses {
+    std::vector<void*> fns;     // CUfunction per pass
+    std::vector<int> per_sm;    // resident CTAs per SM of each pass at its shared memory
+};
+
+// LSG_JIT: 0 never specialize, 1 always, unset: programs whose one run moves at least
+// LSG_JIT_MIN_BYTES of HBM traffic (default 256 GiB, about 0.15 s interpreted, where the second or
+// so of compilation is recovered within a few dozen runs).
+int jit_mode();
+bool jit_wanted(int64_t bytes_per_run);
+
+// The CUDA source of a planned gate program's specialized passes, or "" when a pass can't be.
+std::string jit_source(const Plan& plan, int precision, int ctas);
+
+// Compile `source` with NVRTC only (no device needed): LSG_OK, or an error with NVRTC's log.
+int jit_compile_check(const std::string& source);
+
+// Specialize a planned gate program (no trajectory operators, no shared-memory operators), or
+// nullptr when it can't be (unsupported operators, no NVRTC, compilation failure): the
+// interpreter then runs it. `ctas` is the launch bound's CTAs per SM. Passes compile in parallel
+// on host threads; modules are cached by source for the life of the process.
+std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas);
+
+// Launch every pass on `stream` (events before each pass when `marks` is given).
+int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t member_elems, const void* pass_dev,
+               size_t pass_stride, const void* data, int64_t tiles_per_member, int64_t total, int* status,
+               size_t tile_bytes, cudaStream_t stream, cudaEvent_t* marks);
+
+}  // namespace lsg

@@ -3,7 +3,9 @@
 
 #include <stdint.h>
 
+#ifndef __CUDACC_RTC__
 #include <vector>
+#endif
 
 namespace lsg {
 
@@ -56,11 +58,13 @@ static_assert(sizeof(PassDesc) % 16 == 0, "PassDesc keeps 16-byte alignment");
 static_assert(sizeof(TileOp) % 16 == 0, "TileOp keeps 16-byte alignment");
 static_assert(sizeof(BlockDesc) % 16 == 0, "BlockDesc keeps 16-byte alignment");
 
+#ifndef __CUDACC_RTC__
 struct Plan {
     std::vector<PassDesc> passes;
     std::vector<TileOp> ops;
     std::vector<BlockDesc> blocks;
 };
+#endif
 
 // register-block codes (TileOp::tmpl)
 constexpr int kT_DENSE1 = 0;    // + P
@@ -85,7 +89,9 @@ constexpr int kT_GENERIC = -1;
 // The greedy fusion planner (csrc/engine.cu): lsg_op list -> passes of tile-local operators.
 // pred/draw/count (may be null) give trajectory operators their predicate bit, uniform offset and
 // branch count.
+#ifndef __CUDACC_RTC__
 Plan plan_ops(const struct lsg_op* ops, int nops, int nbits, int K, int L, const int* pred, const int* draw,
               const int* count, int umax);
+#endif
 
 }  // namespace lsg

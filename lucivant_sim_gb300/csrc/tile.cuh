@@ -790,32 +790,14 @@ constexpr int pipe_ctas() {
     return sizeof(T) == 4 ? 3 : 2 - wide_regs<T>();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe(T* __restrict__ state, int64_t member_elems,
-                                                               const PassDesc* __restrict__ pass_g,
-                                                               const TileOp* __restrict__ ops,
-                                                               const BlockDesc* __restrict__ blocks,
-                                                               const T* __restrict__ data, int64_t tiles_per_member,
-                                                               int64_t total_tiles, int* status, TrajCtx ctx) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ uint64_t full[2], empty[2];
-    __shared__ PassDesc pd;
-    const size_t tile_bytes = sizeof(T) << pass_g->K;
-    T* buf0 = reinterpret_cast<T*>(smem_raw);
-    T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
-    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + 2 * tile_bytes);
-    BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
-    OpRec* recs = reinterpret_cast<OpRec*>(sblk + pass_g->nblocks);
-    if (threadIdx.x == 0) pd = *pass_g;
-    stage_pass<T>(pass_g, ops, blocks, sops, sblk);
-    if (threadIdx.x == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
-        mbar_init(&empty[0], 256);
-        mbar_init(&empty[1], 256);
-        fence_mbar_init();
-    }
-    __syncthreads();
+// The pipelined pass loop, shared by the operator interpreter (k_tile_pipe) and by passes the
+// host specializes at run time: `compute(tile, member)` runs on the 256 compute threads for every
+// tile of this CTA; the producer warp streams the tiles. `pd` is the pass (in shared memory),
+// buf0/buf1 the two tile buffers, full/empty the ring's mbarriers (initialised by the caller).
+template <typename T, typename F>
+__device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_elems, const PassDesc& pd, T* buf0,
+                                         T* buf1, uint64_t* full, uint64_t* empty, int64_t tiles_per_member,
+                                         int64_t total_tiles, int* status, F&& compute) {
     const int K = pd.K, L = pd.L;
     const int nchunks = 1 << (K - L);
     const uint32_t chunk_bytes = (uint32_t)(sizeof(T) << L);
@@ -880,10 +862,134 @@ __global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe(T* _
         T* tile = b ? buf1 : buf0;
         const bool ok = mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), status);
         if (cbar_or(!ok)) return;  // every compute thread leaves together on a timeout
-        const int64_t member = t / tiles_per_member;
-        compute_tile<T>(tile, K, pd, sblk, sops, recs, data, member, ctx);
+        compute(tile, t / tiles_per_member);
         fence_proxy_async_smem();  // this thread's writes, before the producer's bulk store reads them
         mbar_arrive(&empty[b]);
+    }
+}
+
+// Barriers of the two-buffer ring: `full` completes on the bulk loads, `empty` when all 256
+// compute threads are done with the buffer.
+__device__ __forceinline__ void pipe_init(uint64_t* full, uint64_t* empty) {
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], 256);
+        mbar_init(&empty[1], 256);
+        fence_mbar_init();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe(T* __restrict__ state, int64_t member_elems,
+                                                               const PassDesc* __restrict__ pass_g,
+                                                               const TileOp* __restrict__ ops,
+                                                               const BlockDesc* __restrict__ blocks,
+                                                               const T* __restrict__ data, int64_t tiles_per_member,
+                                                               int64_t total_tiles, int* status, TrajCtx ctx) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t full[2], empty[2];
+    __shared__ PassDesc pd;
+    const size_t tile_bytes = sizeof(T) << pass_g->K;
+    T* buf0 = reinterpret_cast<T*>(smem_raw);
+    T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
+    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + 2 * tile_bytes);
+    BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
+    OpRec* recs = reinterpret_cast<OpRec*>(sblk + pass_g->nblocks);
+    if (threadIdx.x == 0) pd = *pass_g;
+    stage_pass<T>(pass_g, ops, blocks, sops, sblk);
+    pipe_init(full, empty);
+    __syncthreads();
+    pipe_run<T>(state, member_elems, pd, buf0, buf1, full, empty, tiles_per_member, total_tiles, status,
+                [&](T* tile, int64_t member) { compute_tile<T>(tile, pd.K, pd, sblk, sops, recs, data, member, ctx); });
+}
+
+// A pass specialized by the host: `Body::run(tile, data, member)` is generated straight-line code
+// (compile-time block bits, operator kinds, positions and data offsets; no operator dispatch).
+template <typename T, typename Body>
+__device__ __forceinline__ void pipe_kernel(T* __restrict__ state, int64_t member_elems, const PassDesc* __restrict__ pass_g,
+                                            const T* __restrict__ data, int64_t tiles_per_member, int64_t total_tiles,
+                                            int* status) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t full[2], empty[2];
+    __shared__ PassDesc pd;
+    const size_t tile_bytes = sizeof(T) << pass_g->K;
+    T* buf0 = reinterpret_cast<T*>(smem_raw);
+    T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
+    if (threadIdx.x == 0) pd = *pass_g;
+    pipe_init(full, empty);
+    __syncthreads();
+    pipe_run<T>(state, member_elems, pd, buf0, buf1, full, empty, tiles_per_member, total_tiles, status,
+                [&](T* tile, int64_t member) { Body::run(tile, data, member); });
+}
+
+// Runs of N consecutive elements between shared memory and registers (16-, 8- or 4-byte
+// accesses by size), for specialized passes whose group offsets are compile-time constants.
+template <typename T, int N>
+__device__ __forceinline__ void ld_run(const T* p, T* v) {
+    if constexpr (sizeof(T) * N == 16 && sizeof(T) == 4) {
+        const float4 w = *reinterpret_cast<const float4*>(p);
+        v[0] = w.x, v[1] = w.y, v[2] = w.z, v[3] = w.w;
+    } else if constexpr (sizeof(T) * N == 8 && sizeof(T) == 4) {
+        const float2 w = *reinterpret_cast<const float2*>(p);
+        v[0] = w.x, v[1] = w.y;
+    } else if constexpr (sizeof(T) * N == 16 && sizeof(T) == 8) {
+        const uint4 w = *reinterpret_cast<const uint4*>(p);
+        memcpy(&v[0], &w.x, 8);
+        memcpy(&v[1], &w.z, 8);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = p[i];
+    }
+}
+
+// Two consecutive elements into (a, b) and back: the same tile offset of two neighbouring groups.
+template <typename T>
+__device__ __forceinline__ void ld_split(const T* p, T& a, T& b) {
+    if constexpr (sizeof(T) == 4) {
+        const float2 w = *reinterpret_cast<const float2*>(p);
+        memcpy(&a, &w.x, 4);
+        memcpy(&b, &w.y, 4);
+    } else if constexpr (sizeof(T) == 8) {
+        const uint4 w = *reinterpret_cast<const uint4*>(p);
+        memcpy(&a, &w.x, 8);
+        memcpy(&b, &w.z, 8);
+    } else {
+        a = p[0], b = p[1];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void st_split(T* p, const T& a, const T& b) {
+    if constexpr (sizeof(T) == 4) {
+        float2 w;
+        memcpy(&w.x, &a, 4);
+        memcpy(&w.y, &b, 4);
+        *reinterpret_cast<float2*>(p) = w;
+    } else if constexpr (sizeof(T) == 8) {
+        uint4 w;
+        memcpy(&w.x, &a, 8);
+        memcpy(&w.z, &b, 8);
+        *reinterpret_cast<uint4*>(p) = w;
+    } else {
+        p[0] = a, p[1] = b;
+    }
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void st_run(T* p, const T* v) {
+    if constexpr (sizeof(T) * N == 16 && sizeof(T) == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else if constexpr (sizeof(T) * N == 8 && sizeof(T) == 4) {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    } else if constexpr (sizeof(T) * N == 16 && sizeof(T) == 8) {
+        uint4 w;
+        memcpy(&w.x, &v[0], 8);
+        memcpy(&w.z, &v[1], 8);
+        *reinterpret_cast<uint4*>(p) = w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = v[i];
     }
 }
 

@@ -325,6 +325,10 @@ def _add_ptm(ops: OpList, bits: list[int], mats: np.ndarray) -> None:
     single shared one — as the cheapest kind that represents it exactly: diagonal, bit renames
     plus a diagonal, or dense."""
     mats = np.asarray(mats, dtype=np.float64)
+    # rounding residue of the transfer-matrix products (|x| ~ 1e-16) is snapped to the exact 0 and
+    # +-1 entries it stands for, so trace preservation and permutation structure are recognised
+    mats = np.where(np.abs(mats) < 1e-14, 0.0, mats)
+    mats = np.where(np.abs(np.abs(mats) - 1.0) < 1e-14, np.sign(mats), mats)
     d = mats.shape[-1]
     nb = len(bits)
     shared = bool((mats == mats[0]).all())

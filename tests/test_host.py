@@ -283,3 +283,24 @@ def test_deep_circuits_split_into_bounded_passes():
     assert len(ops) > 192 * 3
     for precision in (_lib.C128, _lib.C64):
         assert _lib.plan_passes(10, precision, ops) >= -(-len(ops) // 192)
+
+
+def test_specialized_pass_source_compiles():
+    """The run-time specializer's source for a Pauli-transfer program (two groups per thread,
+    trace-preserving 4x4 operators, renames, diagonals) and a statevector program compiles with
+    NVRTC for sm_103a; wide operators leave a program to the interpreter."""
+    pytest.importorskip("ctypes")
+    from lucivant_sim_gb300 import _lib, engine
+    from lucivant_sim_gb300 import workloads as wl
+    from lucivant_sim_gb300.qasm import parse
+
+    c = parse(wl.brickwork(7, 2, seed=3, measure=False))
+    ptm = engine.ptm_oplist(c, wl.dm_noise_instances(2, seed=3))
+    src = _lib.specialized_source(14, _lib.R32, 2, ptm, compile=True)
+    assert "rb_tpd2<float" in src and "ld_split<float>" in src and "lsg_pass_0" in src
+    sv = engine.sv_oplist(parse(wl.brickwork(14, 2, seed=3, measure=False)))
+    src = _lib.specialized_source(14, _lib.C64, 1, sv, compile=True)
+    assert "lsg::Cx<float>" in src
+    wide = _lib.OpList()
+    wide.add(_lib.OP_MATRIX, [0, 1, 2, 3, 4], np.eye(32, dtype=complex))
+    assert _lib.specialized_source(14, _lib.C64, 1, wide) == ""
