@@ -391,7 +391,11 @@ def gb300_arm(args: argparse.Namespace) -> None:
 
     all_pass = np.concatenate(pass_ms)
     avg_launch_s = float(all_pass.mean()) / 1000.0
-    launch_bytes = 2 * batch.register_bytes
+    # bytes the passes actually move: a run from |0><0| skips tiles the circuit has not reached
+    # (still zero), so early passes move less than 2 x register bytes
+    nominal_launch_bytes = 2 * batch.register_bytes
+    moved_per_run = batch.bytes_per_evolve
+    launch_bytes = moved_per_run / passes
     peak, peak_kind = measured_peak()
     achieved = launch_bytes / avg_launch_s / 1e9
     traffic = ncu_traffic(args.precision)
@@ -405,6 +409,8 @@ def gb300_arm(args: argparse.Namespace) -> None:
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
         "traffic": traffic,
         "bytes_per_launch": launch_bytes,
+        "nominal_bytes_per_launch": nominal_launch_bytes,
+        "skipped_zero_tile_bytes_frac": 1.0 - moved_per_run / (nominal_launch_bytes * passes),
         "avg_launch_ms": avg_launch_s * 1000,
         "launches": int(all_pass.size),
         "share_of_step": float(all_pass.sum()) / 1000.0 / (elapsed / 1.0) if world == 1 else None,

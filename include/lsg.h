@@ -114,6 +114,14 @@ int lsg_program_run(lsg_program p, lsg_state s);
 /* Run once with CUDA events around every pass (on the register's stream) and wait: pass_ms gets
  * one device time per pass, in milliseconds. */
 int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms);
+/* Set every member to basis state `index` (as lsg_state_set_basis) and run the program from it,
+ * visiting only tiles that can be nonzero: register bits no earlier non-diagonal operator has
+ * touched still hold the basis state's values (all bits of a complex register; the Pauli x digits
+ * of a real one), so tiles that differ there stay zero and are skipped. The result equals
+ * set_basis + lsg_program_run. With pass_ms non-NULL, as lsg_program_run_timed. */
+int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float* pass_ms);
+/* HBM bytes (2 x tile bytes per tile visited) and tiles of one lsg_program_run_from_basis. */
+int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run);
 /* Number of fused passes, and algorithmic HBM bytes of one run (2 x register bytes per pass). */
 int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run);
 /* 1 when the program's passes run as kernels specialized for it at creation (NVRTC, LSG_JIT=1),

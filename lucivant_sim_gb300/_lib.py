@@ -71,6 +71,8 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_program_run_timed": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     "lsg_program_info": (C.c_int, [_P, _PI32, _PI64]),
     "lsg_program_specialized": (C.c_int, [_P]),
+    "lsg_program_run_from_basis": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_float)]),
+    "lsg_program_basis_info": (C.c_int, [_P, _PI64, _PI64]),
     "lsg_program_free": (C.c_int, [_P]),
     "lsg_plan": (C.c_int, [C.c_int, C.c_int, _P, _I32, _PI32]),
     "lsg_program_source": (C.c_int, [C.c_int, C.c_int, _I64, _P, _I32, _PD, _I64, C.c_int, C.c_char_p, _I64, _PI64]),
@@ -353,6 +355,24 @@ class Program:
 
     def run(self, reg: Register) -> None:
         check(self.lib.lsg_program_run(self.handle, reg.handle))
+
+    def run_from_basis(self, reg: Register, index: int = 0, timed: bool = False) -> np.ndarray | None:
+        """Set every member to basis state ``index`` and run, skipping tiles that are still zero
+        (same result as ``reg.set_basis(index); self.run(reg)``). ``timed``: wait and return each
+        pass's device time in ms."""
+        if not timed:
+            check(self.lib.lsg_program_run_from_basis(self.handle, reg.handle, index, None))
+            return None
+        out = np.zeros(max(self.passes, 1), dtype=np.float32)
+        check(self.lib.lsg_program_run_from_basis(self.handle, reg.handle, index, ptr(out, C.c_float)))
+        return out[: self.passes]
+
+    @property
+    def basis_bytes_per_run(self) -> int:
+        """HBM bytes one :meth:`run_from_basis` moves (2 x tile bytes per tile visited)."""
+        nbytes = C.c_int64(0)
+        check(self.lib.lsg_program_basis_info(self.handle, C.byref(nbytes), None))
+        return int(nbytes.value)
 
     def run_timed(self, reg: Register) -> np.ndarray:
         out = np.zeros(max(self.passes, 1), dtype=np.float32)

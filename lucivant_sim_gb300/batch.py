@@ -42,14 +42,18 @@ class DensityBatch:
         return _lib.ELEM_BYTES[self.reg.precision] * self.batch << (2 * self.n)
 
     def evolve(self) -> None:
-        """Reset every member to |0><0| and run the circuit (queued; returns before completion)."""
-        self.reg.set_basis(0)
-        self.program.run(self.reg)
+        """Reset every member to |0><0| and run the circuit (queued; returns before completion).
+        Tiles that the circuit has not reached yet are still zero and are skipped."""
+        self.program.run_from_basis(self.reg, 0)
 
     def evolve_timed(self) -> np.ndarray:
         """As :meth:`evolve`, returning each fused pass's device time in ms."""
-        self.reg.set_basis(0)
-        return self.program.run_timed(self.reg)
+        return self.program.run_from_basis(self.reg, 0, timed=True)
+
+    @property
+    def bytes_per_evolve(self) -> int:
+        """HBM bytes the passes of one :meth:`evolve` move."""
+        return self.program.basis_bytes_per_run
 
     def probabilities(self) -> np.ndarray:
         """(batch, 2^n) exact probabilities."""

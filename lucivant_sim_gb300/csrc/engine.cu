@@ -445,10 +445,12 @@ int tile_bits_for(int nbits, int precision) {
     return std::max(0, std::min(K, nbits));
 }
 
-// Register bits every tile keeps: 2^L contiguous elements, 512 bytes per copy (256 for real32).
+// Register bits every tile keeps: 2^L contiguous elements, 512 bytes per copy (smaller copies
+// leave HBM well below its streaming rate: a real32 pass with 256-byte copies took twice as long
+// as the same work with 512-byte copies).
 int low_bits_for(int nbits, int precision) {
     const size_t eb = lsg_elem_bytes(precision);
-    int L = eb == 16 ? 5 : 6;
+    int L = eb == 16 ? 5 : eb == 8 ? 6 : 7;
     if (const char* env = getenv("LSG_LOW_BITS")) L = atoi(env);
     return std::max(0, std::min(L, nbits));
 }
@@ -502,6 +504,11 @@ struct lsg_program_s {
     int K = 0;
     std::vector<cudaEvent_t> events;
     std::shared_ptr<lsg::JitPasses> jit;  // specialized passes, when the program could be specialized
+    // runs from a basis state: the passes restricted to tiles that can be nonzero (uploaded after
+    // the block descriptors, for the basis index `basis_index`)
+    std::vector<lsg::PassDesc> basis_passes;
+    int64_t basis_index = -1;
+    size_t basis_off = 0;
 };
 
 namespace lsg {
@@ -529,27 +536,31 @@ static int allow_smem(K kern) {
 }
 
 template <typename T>
-static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
+static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx, bool from_basis) {
     const size_t tile_bytes = sizeof(T) << p->K;
     const size_t meta = p->smem - tile_bytes;
     const int L = p->plan.passes.empty() ? 0 : p->plan.passes[0].L;
     const bool bulk = ((sizeof(T) << L) % 16) == 0;
     const bool pipe = bulk && getenv("LSG_NO_PIPELINE") == nullptr && 2 * tile_bytes + meta <= 200 * 1024;
-    const int64_t tiles_per_member = 1ll << (s->nbits - p->K);
-    const int64_t total = tiles_per_member * s->batch;
+    // the passes as launched: all tiles, or (from a basis state) the tiles that can be nonzero
+    const std::vector<PassDesc>& host_pd = from_basis ? p->basis_passes : p->plan.passes;
+    std::vector<int64_t> tpm(host_pd.size());
+    for (size_t i = 0; i < host_pd.size(); ++i) tpm[i] = 1ll << host_pd[i].nouter;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int* status = device_status();
     if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
-    const PassDesc* pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
-    const TileOp* ops_dev = reinterpret_cast<const TileOp*>(pd_dev + p->plan.passes.size());
+    const PassDesc* plan_pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
+    const TileOp* ops_dev = reinterpret_cast<const TileOp*>(plan_pd_dev + p->plan.passes.size());
     const BlockDesc* blk_dev = reinterpret_cast<const BlockDesc*>(ops_dev + p->plan.ops.size());
+    const PassDesc* pd_dev =
+        from_basis ? reinterpret_cast<const PassDesc*>(static_cast<unsigned char*>(p->dev.ptr) + p->basis_off) : plan_pd_dev;
     const T* pool_dev = reinterpret_cast<const T*>(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned);
     T* state = reinterpret_cast<T*>(s->data);
     if (p->jit && bulk && ctx.u == nullptr) {
-        LSG_CHECK(jit_launch(*p->jit, p->plan, state, s->elems, pd_dev, sizeof(PassDesc), pool_dev, tiles_per_member,
-                             total, status, tile_bytes, s->stream, marks));
+        LSG_CHECK(jit_launch(*p->jit, p->plan, state, s->elems, pd_dev, sizeof(PassDesc), pool_dev, tpm, s->batch, status,
+                             tile_bytes, s->stream, marks));
         if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
         return LSG_OK;
     }
@@ -561,30 +572,69 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
         int64_t grid = 1;
         for (size_t i = 0; i < p->plan.passes.size(); ++i) {
             const PassDesc& pd = p->plan.passes[i];
+            const int64_t total = tpm[i] * s->batch;
             const size_t smem = 2 * tile_bytes + (size_t)pd.nops * (sizeof(TileOp) + 16) + (size_t)pd.nblocks * sizeof(BlockDesc);
             if (smem != last_smem) {
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPipeThreads, smem);
-                grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
                 last_smem = smem;
             }
+            grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
             if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
             kern<<<(unsigned)grid, kPipeThreads, smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
-                                                                    tiles_per_member, total, status, ctx);
+                                                                    tpm[i], total, status, ctx);
         }
     } else {
         auto kern = k_tile_pass<T>;
         LSG_CHECK(allow_smem(kern));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, p->smem);
-        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
         for (size_t i = 0; i < p->plan.passes.size(); ++i) {
+            const int64_t total = tpm[i] * s->batch;
+            const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
             if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
             kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
-                                                              tiles_per_member, total, status, ctx);
+                                                              tpm[i], total, status, ctx);
         }
     }
     if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
     LSG_CUDA(cudaGetLastError());
     return LSG_OK;
+}
+
+// The passes of a run that starts from basis state `index` (lsg_state_set_basis), restricted to
+// the tiles that can be nonzero. A basis state fixes register bits: every bit of a complex
+// register (the amplitude index), the Pauli x digits of a real Pauli-transfer register (bits
+// n..2n-1 are 0; its z digits are free). An operator that is not diagonal frees its bits for the
+// passes after it; a diagonal one keeps them. Tiles of pass p whose outer bits differ from the
+// fixed values hold zeros and pass p's operators (acting on tile bits only) keep them zero, so pass
+// p enumerates the free outer bits only and ORs the fixed values into every tile's base.
+static std::vector<PassDesc> basis_passes(const Plan& plan, int nbits, int precision, int64_t index) {
+    const bool real = precision == LSG_R64 || precision == LSG_R32;
+    uint64_t fixed = nbits >= 64 ? ~0ull : ((1ull << nbits) - 1);
+    uint64_t value = real ? 0 : (uint64_t)index;
+    if (real) fixed &= ~((1ull << (nbits / 2)) - 1);  // z digits are free
+    std::vector<PassDesc> out(plan.passes.begin(), plan.passes.end());
+    for (size_t i = 0; i < out.size(); ++i) {
+        PassDesc& pd = out[i];
+        const PassDesc& src = plan.passes[i];
+        pd.nouter = 0;
+        pd.fix = 0;
+        for (int j = 0; j < src.nouter; ++j) {
+            const int bit = src.outer[j];
+            if ((fixed >> bit) & 1) pd.fix |= value & (1ull << bit);
+            else pd.outer[pd.nouter++] = bit;
+        }
+        for (int j = pd.nouter; j < 32; ++j) pd.outer[j] = 0;
+        for (int o = src.first_op; o < src.first_op + src.nops; ++o) {
+            const TileOp& t = plan.ops[o];
+            if (t.kind == LSG_OP_DIAG || t.kind == LSG_OP_SCALE) continue;
+            for (int k = 0; k < t.k; ++k) {
+                const int lb = t.lb[k];
+                const int reg = lb < src.L ? lb : src.hi[lb - src.L];
+                fixed &= ~(1ull << reg);
+            }
+        }
+    }
+    return out;
 }
 
 // Plan and lower `ops`; with `upload`, copy the program to the device (otherwise only the host
@@ -739,8 +789,12 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
         *out = p;
         return LSG_OK;
     }
-    const size_t head = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp) +
-                        p->plan.blocks.size() * sizeof(BlockDesc);
+    const size_t head0 = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp) +
+                         p->plan.blocks.size() * sizeof(BlockDesc);
+    p->basis_off = (head0 + 15) & ~size_t(15);
+    p->basis_passes = basis_passes(p->plan, nbits, precision, 0);
+    p->basis_index = 0;
+    const size_t head = p->basis_off + p->basis_passes.size() * sizeof(PassDesc);
     p->head_aligned = (head + 255) & ~size_t(255);
     const size_t total = p->head_aligned + (size_t)pool_entries * elt;
     std::vector<unsigned char> blob(std::max<size_t>(total, 1));
@@ -749,6 +803,7 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
                 p->plan.ops.size() * sizeof(TileOp));
     std::memcpy(blob.data() + p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp),
                 p->plan.blocks.data(), p->plan.blocks.size() * sizeof(BlockDesc));
+    std::memcpy(blob.data() + p->basis_off, p->basis_passes.data(), p->basis_passes.size() * sizeof(PassDesc));
     unsigned char* dst = blob.data() + p->head_aligned;
     if (precision == LSG_C128) {
         if (pool_entries) std::memcpy(dst, pool, (size_t)pool_entries * 16);
@@ -827,17 +882,39 @@ void program_destroy(lsg_program_s* p) {
     delete p;
 }
 
-int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
+static int program_launch(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx, bool from_basis) {
     if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
         return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
                     p->nbits, p->precision, (long long)p->batch);
     if (p->plan.passes.empty()) return LSG_OK;
     switch (s->precision) {
-        case LSG_C128: return launch_passes<Cx<double>>(p, s, marks, ctx);
-        case LSG_C64: return launch_passes<Cx<float>>(p, s, marks, ctx);
-        case LSG_R64: return launch_passes<double>(p, s, marks, ctx);
-        default: return launch_passes<float>(p, s, marks, ctx);
+        case LSG_C128: return launch_passes<Cx<double>>(p, s, marks, ctx, from_basis);
+        case LSG_C64: return launch_passes<Cx<float>>(p, s, marks, ctx, from_basis);
+        case LSG_R64: return launch_passes<double>(p, s, marks, ctx, from_basis);
+        default: return launch_passes<float>(p, s, marks, ctx, from_basis);
     }
+}
+
+int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const TrajCtx& ctx) {
+    return program_launch(p, s, marks, ctx, false);
+}
+
+// Set every member to basis state `index`, then run the passes on the tiles that can be nonzero.
+static int program_run_basis(lsg_program_s* p, lsg_state_s* s, int64_t index, cudaEvent_t* marks) {
+    if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
+        return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
+                    p->nbits, p->precision, (long long)p->batch);
+    LSG_CHECK(lsg_state_set_basis(s, index));
+    const bool real = s->real();
+    if (!real && index != p->basis_index) {  // the fixed values are the index's bits: re-upload
+        p->basis_passes = basis_passes(p->plan, p->nbits, p->precision, index);
+        void* dst = static_cast<unsigned char*>(p->dev.ptr) + p->basis_off;
+        // pageable source: the copy is staged before the call returns
+        LSG_CUDA(cudaMemcpyAsync(dst, p->basis_passes.data(), p->basis_passes.size() * sizeof(PassDesc),
+                                 cudaMemcpyHostToDevice, s->stream));
+        p->basis_index = index;
+    }
+    return program_launch(p, s, marks, TrajCtx{}, true);
 }
 
 static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
@@ -1130,6 +1207,32 @@ int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms) {
     LSG_CUDA(cudaEventSynchronize(p->events[need - 1]));
     for (size_t i = 0; i + 1 < need; ++i) LSG_CUDA(cudaEventElapsedTime(&pass_ms[i], p->events[i], p->events[i + 1]));
     return check_device_status(s->stream);
+}
+
+int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float* pass_ms) {
+    clear_error();
+    if (!p || !s) return fail(LSG_E_ARG, "null argument");
+    if (!pass_ms) return program_run_basis(p, s, index, nullptr);
+    const size_t need = p->plan.passes.size() + 1;
+    while (p->events.size() < need) {
+        cudaEvent_t e;
+        LSG_CUDA(cudaEventCreate(&e));
+        p->events.push_back(e);
+    }
+    LSG_CHECK(program_run_basis(p, s, index, p->events.data()));
+    LSG_CUDA(cudaEventSynchronize(p->events[need - 1]));
+    for (size_t i = 0; i + 1 < need; ++i) LSG_CUDA(cudaEventElapsedTime(&pass_ms[i], p->events[i], p->events[i + 1]));
+    return check_device_status(s->stream);
+}
+
+int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run) {
+    clear_error();
+    if (!p) return fail(LSG_E_ARG, "null program");
+    int64_t tiles = 0;
+    for (const PassDesc& pd : p->basis_passes) tiles += (1ll << pd.nouter) * p->batch;
+    if (tiles_per_run) *tiles_per_run = tiles;
+    if (bytes_per_run) *bytes_per_run = 2 * tiles * ((int64_t)lsg_elem_bytes(p->precision) << p->K);
+    return LSG_OK;
 }
 
 int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run) {

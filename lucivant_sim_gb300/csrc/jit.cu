@@ -128,55 +128,203 @@ bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int a
     return true;
 }
 
+constexpr int kComputeHost = 256;  // compute threads of a pipelined pass CTA (tile.cuh kCompute)
+
 // The 32-bit registers a thread may spend on its blocks' amplitudes at `ctas` CTAs per SM.
 int state_reg_budget(int ctas) { return ctas >= 3 ? 32 : ctas == 2 ? 64 : 128; }
+
+// A rename of tile offsets: the register-block renames (X, CX, SWAP codes) lifted to tile bits.
+// Each is an involution x -> x ^ (bit a of x) << b (CX), a swap of bits a and b, or x ^ 1 << a (X).
+struct Rename {
+    int kind;  // 0 CX (control a, target b), 1 SWAP, 2 X (bit a)
+    int a, b;
+    uint32_t apply(uint32_t x) const {
+        if (kind == 0) return x ^ (((x >> a) & 1u) << b);
+        if (kind == 1) {
+            const uint32_t d = ((x >> a) ^ (x >> b)) & 1u;
+            return x ^ ((d << a) | (d << b));
+        }
+        return x ^ (1u << a);
+    }
+    // the bits that can be set after this rename when `may` can be set before it
+    uint32_t may(uint32_t m) const {
+        if (kind == 0) return m | (((m >> a) & 1u) << b);
+        if (kind == 1) {
+            const uint32_t ba = (m >> a) & 1u, bb = (m >> b) & 1u;
+            return (m & ~((1u << a) | (1u << b))) | (ba << b) | (bb << a);
+        }
+        return m | (1u << a);
+    }
+    uint32_t bits() const { return kind == 2 ? 1u << a : (1u << a) | (1u << b); }
+    void emit(std::ostringstream& o, const char* var) const {
+        if (kind == 0) o << "      " << var << " ^= ((" << var << " >> " << a << ") & 1u) << " << b << ";\n";
+        else if (kind == 1)
+            o << "      { const uint32_t d = ((" << var << " >> " << a << ") ^ (" << var << " >> " << b << ")) & 1u; " << var
+              << " ^= (d << " << a << ") | (d << " << b << "); }\n";
+        else o << "      " << var << " ^= " << (1u << a) << "u;\n";
+    }
+};
+
+// The renames of a block made only of X/CX/SWAP operators, in program order, or false.
+bool pure_renames(const Plan& plan, const PassDesc& pd, const BlockDesc& b, std::vector<Rename>* out) {
+    if (b.nops == 0) return false;
+    for (int k = b.first; k < b.first + b.nops; ++k) {
+        const int c = plan.ops[pd.first_op + k].tmpl;
+        if (c >= kT_X1 && c < kT_X1 + 4) out->push_back({2, b.bits[c - kT_X1], 0});
+        else if (c >= kT_CX && c < kT_CX + 16) out->push_back({0, b.bits[(c - kT_CX) / 4], b.bits[(c - kT_CX) % 4]});
+        else if (c >= kT_SWAP && c < kT_SWAP + 16) out->push_back({1, b.bits[(c - kT_SWAP) / 4], b.bits[(c - kT_SWAP) % 4]});
+        else return false;
+    }
+    return true;
+}
+
+// One register block as generated: its access shape, and the renames folded into its loads
+// (applied to the load addresses, last rename first) and stores (in program order).
+struct BlockGen {
+    const BlockDesc* b = nullptr;
+    int U = 0, n = 0, groups = 0, W = 1, run = 1;
+    std::vector<uint32_t> off;
+    uint32_t vec_bits = 0;  // tile bits inside one shared-memory access (renames must keep them)
+    std::vector<Rename> load_map, store_map;
+    // A folded map moves elements between groups: every group must be in registers (one group
+    // per compute thread) before any is stored, so the block takes one barrier between its loads
+    // and its stores, and folding needs at most one group (pair) per compute thread.
+    bool takes(const std::vector<Rename>& rn) const {
+        if (groups / W > kComputeHost) return false;
+        for (const Rename& r : rn)
+            if (r.bits() & vec_bits) return false;
+        return true;
+    }
+    bool folded() const { return !load_map.empty() || !store_map.empty(); }
+};
+
+BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int ctas) {
+    BlockGen g;
+    g.b = &b;
+    g.U = b.u, g.n = 1 << b.u, g.groups = 1 << (pd.K - b.u);
+    // Two groups per thread when tile bit 0 is not a block bit: the pair (tile bit 0 = 0, 1)
+    // moves as one wider shared-memory access and every operator's coefficients, loaded once,
+    // serve both groups (the two calls read the same addresses).
+    g.W = (b.sorted[0] != 0 && g.groups >= 2 && 2 * g.n * elem_bytes / 4 <= state_reg_budget(ctas)) ? 2 : 1;
+    g.run = g.W == 2 ? 1 : std::min(std::max((int)b.vec, 1), std::max(1, 16 / elem_bytes));
+    g.vec_bits = g.W == 2 ? 1u : g.run == 4 ? 3u : g.run == 2 ? 1u : 0u;
+    g.off.resize(g.n);
+    for (int e = 0; e < g.n; ++e) {
+        uint32_t a = 0;
+        for (int i = 0; i < g.U; ++i)
+            if ((e >> (g.U - 1 - i)) & 1) a |= 1u << b.bits[i];
+        g.off[e] = a;
+    }
+    return g;
+}
+
+// The address expressions of a block's elements under a folded rename map: the runtime part
+// (the group base, renamed) in `var`, a constant per element, joined by + where they cannot share
+// a bit (an immediate offset) and by ^ where they can.
+std::vector<std::string> mapped_addresses(std::ostringstream& o, const BlockGen& g, const std::vector<Rename>& map,
+                                          const char* var, uint32_t tile_mask) {
+    std::vector<std::string> addr(g.n);
+    if (map.empty()) {
+        for (int e = 0; e < g.n; ++e) addr[e] = "base + " + std::to_string(g.off[e]) + "u";
+        return addr;
+    }
+    uint32_t block_bits = 0;
+    for (int i = 0; i < g.U; ++i) block_bits |= 1u << g.b->bits[i];
+    uint32_t may = tile_mask & ~block_bits & ~(g.W == 2 ? 1u : 0u) & ~g.vec_bits;
+    o << "      uint32_t " << var << " = base;\n";
+    uint32_t zero = 0;
+    for (const Rename& r : map) {
+        r.emit(o, var);
+        may = r.may(may);
+        zero = r.apply(zero);
+    }
+    for (int e = 0; e < g.n; ++e) {
+        uint32_t c = g.off[e];
+        for (const Rename& r : map) c = r.apply(c);
+        c ^= zero;  // the map is affine: map(base ^ off) = map(base) ^ map(off) ^ map(0)
+        addr[e] = std::string(var) + ((c & may) ? " ^ " : " + ") + std::to_string(c) + "u";
+    }
+    return addr;
+}
+
+void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, const PassDesc& pd, const char* T, bool* ok) {
+    const BlockDesc& b = *g.b;
+    const uint32_t tile_mask = pd.K >= 32 ? ~0u : ((1u << pd.K) - 1u);
+    const bool fold = g.folded();
+    if (fold)  // one group (pair) per thread; threads past the last group only join the barriers
+        o << "    cbar();\n    {\n      const int g = threadIdx.x;\n      const bool act = g < " << g.groups / g.W << ";\n";
+    else
+        o << "    cbar();\n    for (int g = threadIdx.x; g < " << g.groups / g.W << "; g += kCompute) {\n";
+    o << "      const uint32_t G = uint32_t(g)" << (g.W == 2 ? " << 1" : "") << ";\n";
+    o << "      const uint32_t base =";
+    for (int i = 0; i <= g.U; ++i) o << (i ? " |" : "") << " ((G << " << i << ") & " << b.dep[i] << "u)";
+    o << ";\n      " << T << " v[" << g.n * g.W << "];\n";
+    const std::vector<std::string> la = mapped_addresses(o, g, g.load_map, "lb", tile_mask);
+    if (fold) o << "      if (act) {\n";
+    for (int e = 0; e < g.n; e += g.run) {
+        if (g.W == 2)
+            o << "      ld_split<" << T << ">(tile + (" << la[e] << "), v[" << e << "], v[" << g.n + e << "]);\n";
+        else
+            o << "      ld_run<" << T << ", " << g.run << ">(tile + (" << la[e] << "), v + " << e << ");\n";
+    }
+    for (int k = b.first; k < b.first + b.nops; ++k)
+        for (int w = 0; w < g.W; ++w) {
+            o << "      ";
+            if (!op_call(o, plan.ops[pd.first_op + k], g.U, T, w * g.n)) {
+                *ok = false;
+                return;
+            }
+        }
+    if (fold) o << "      }\n      cbar();  // every group is in registers: the renamed stores may land in any group\n      if (act) {\n";
+    const std::vector<std::string> sa = mapped_addresses(o, g, g.store_map, "sb", tile_mask);
+    for (int e = 0; e < g.n; e += g.run) {
+        if (g.W == 2)
+            o << "      st_split<" << T << ">(tile + (" << sa[e] << "), v[" << e << "], v[" << g.n + e << "]);\n";
+        else
+            o << "      st_run<" << T << ", " << g.run << ">(tile + (" << sa[e] << "), v + " << e << ");\n";
+    }
+    if (fold) o << "      }\n";
+    o << "    }\n";
+}
 
 std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_bytes, int ctas) {
     const PassDesc& pd = plan.passes[pi];
     const char* T = type_name(precision);
-    std::ostringstream o;
-    o << "struct Body" << pi << " {\n  static __device__ __forceinline__ void run(" << T << "* tile, const " << T
-      << "* __restrict__ data, long long member) {\n";
+    // Blocks made only of renames move no arithmetic: they fold into the neighbouring block's
+    // store addresses (or the next block's load addresses) unless they touch the bits inside
+    // that block's vector accesses, saving a shared-memory round trip and a barrier each.
+    std::vector<BlockGen> gens, held;
+    std::vector<Rename> pending;
     for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
         const BlockDesc& b = plan.blocks[bi];
         if (b.generic) return "";
-        const int U = b.u, n = 1 << U, groups = 1 << (pd.K - U);
-        // Two groups per thread when tile bit 0 is not a block bit: the pair (tile bit 0 = 0, 1)
-        // moves as one wider shared-memory access and every operator's coefficients, loaded once,
-        // serve both groups (the two calls read the same addresses).
-        const int W = (b.sorted[0] != 0 && groups >= 2 && 2 * n * elem_bytes / 4 <= state_reg_budget(ctas)) ? 2 : 1;
-        const int run = W == 2 ? 1 : std::min(std::max(b.vec, 1), std::max(1, 16 / elem_bytes));
-        o << "    cbar();\n    for (int g = threadIdx.x; g < " << groups / W << "; g += kCompute) {\n";
-        o << "      const uint32_t G = uint32_t(g)" << (W == 2 ? " << 1" : "") << ";\n";
-        o << "      const uint32_t base =";
-        for (int i = 0; i <= U; ++i) o << (i ? " |" : "") << " ((G << " << i << ") & " << b.dep[i] << "u)";
-        o << ";\n      " << T << " v[" << n * W << "];\n";
-        std::vector<uint32_t> off(n);
-        for (int e = 0; e < n; ++e) {
-            uint32_t a = 0;
-            for (int i = 0; i < U; ++i)
-                if ((e >> (U - 1 - i)) & 1) a |= 1u << b.bits[i];
-            off[e] = a;
-        }
-        for (int e = 0; e < n; e += run) {
-            if (W == 2)
-                o << "      ld_split<" << T << ">(tile + (base + " << off[e] << "u), v[" << e << "], v[" << n + e << "]);\n";
-            else
-                o << "      ld_run<" << T << ", " << run << ">(tile + (base + " << off[e] << "u), v + " << e << ");\n";
-        }
-        for (int k = b.first; k < b.first + b.nops; ++k) {
-            for (int w = 0; w < W; ++w) {
-                o << "      ";
-                if (!op_call(o, plan.ops[pd.first_op + k], U, T, w * n)) return "";
+        BlockGen g = block_gen(b, pd, elem_bytes, ctas);
+        std::vector<Rename> rn;
+        if (pure_renames(plan, pd, b, &rn)) {
+            if (held.empty() && !gens.empty() && gens.back().takes(rn)) {
+                gens.back().store_map.insert(gens.back().store_map.end(), rn.begin(), rn.end());
+                continue;
             }
+            held.push_back(g);
+            pending.insert(pending.end(), rn.begin(), rn.end());
+            continue;
         }
-        for (int e = 0; e < n; e += run) {
-            if (W == 2)
-                o << "      st_split<" << T << ">(tile + (base + " << off[e] << "u), v[" << e << "], v[" << n + e << "]);\n";
-            else
-                o << "      st_run<" << T << ", " << run << ">(tile + (base + " << off[e] << "u), v + " << e << ");\n";
+        if (!held.empty()) {
+            if (g.takes(pending)) g.load_map.assign(pending.rbegin(), pending.rend());
+            else gens.insert(gens.end(), held.begin(), held.end());
+            held.clear();
+            pending.clear();
         }
-        o << "    }\n";
+        gens.push_back(g);
+    }
+    gens.insert(gens.end(), held.begin(), held.end());
+    std::ostringstream o;
+    o << "struct Body" << pi << " {\n  static __device__ __forceinline__ void run(" << T << "* tile, const " << T
+      << "* __restrict__ data, long long member) {\n";
+    bool ok = true;
+    for (const BlockGen& g : gens) {
+        emit_block(o, g, plan, pd, T, &ok);
+        if (!ok) return "";
     }
     o << "    cbar();\n  }\n};\n";
     return o.str();
@@ -331,8 +479,8 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas) 
 }
 
 int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t member_elems, const void* pass_dev,
-               size_t pass_stride, const void* data, int64_t tiles_per_member, int64_t total, int* status,
-               size_t tile_bytes, cudaStream_t stream, cudaEvent_t* marks) {
+               size_t pass_stride, const void* data, const std::vector<int64_t>& tiles_per_member, int64_t batch,
+               int* status, size_t tile_bytes, cudaStream_t stream, cudaEvent_t* marks) {
     const Driver& drv = driver();
     int dev = 0, sms = 0;
     LSG_CUDA(cudaGetDevice(&dev));
@@ -340,9 +488,10 @@ int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t membe
     const size_t smem = 2 * tile_bytes;
     for (size_t i = 0; i < plan.passes.size(); ++i) {
         CUfunction f = reinterpret_cast<CUfunction>(jp.fns[i]);
+        const int64_t total = tiles_per_member[i] * batch;
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(jp.per_sm[i], 1)));
         const void* pg = static_cast<const unsigned char*>(pass_dev) + i * pass_stride;
-        long long me = member_elems, tpm = tiles_per_member, tot = total;
+        long long me = member_elems, tpm = tiles_per_member[i], tot = total;
         void* args[] = {&state, &me, &pg, &data, &tpm, &tot, &status};
         if (marks) LSG_CUDA(cudaEventRecord(marks[i], stream));
         if (drv.launch(f, (unsigned)grid, 1, 1, kPipeThreadsHost, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr) !=

@@ -38,8 +38,9 @@ int jit_compile_check(const std::string& source);
 std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas);
 
 // Launch every pass on `stream` (events before each pass when `marks` is given).
+// `tiles_per_member[i]`: the tiles pass i visits in each of the `batch` members.
 int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t member_elems, const void* pass_dev,
-               size_t pass_stride, const void* data, int64_t tiles_per_member, int64_t total, int* status,
-               size_t tile_bytes, cudaStream_t stream, cudaEvent_t* marks);
+               size_t pass_stride, const void* data, const std::vector<int64_t>& tiles_per_member, int64_t batch,
+               int* status, size_t tile_bytes, cudaStream_t stream, cudaEvent_t* marks);
 
 }  // namespace lsg

@@ -17,6 +17,11 @@ struct PassDesc {
     int first_block, nblocks;
     int hi[32];
     int outer[32];
+    // OR-ed into every tile's base. A run from a basis state skips tiles that are still zero:
+    // outer[] then lists only the register bits the earlier passes can have changed, and `fix`
+    // holds the basis state's values of the others.
+    unsigned long long fix;
+    unsigned long long pad2;
 };
 
 // A register block: consecutive operators of a pass whose bits together span u <= 4 tile bits.

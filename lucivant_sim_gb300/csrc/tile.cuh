@@ -809,7 +809,7 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
             const int64_t member = t / tiles_per_member;
             const uint64_t tt = (uint64_t)(t - member * tiles_per_member);
             *mem = state + member * member_elems;
-            *base = deposit(tt, pd.outer, pd.nouter);
+            *base = deposit(tt, pd.outer, pd.nouter) | pd.fix;
         };
         auto store = [&](int64_t t, T* buf) {
             T* mem;
@@ -1035,7 +1035,7 @@ __global__ void __launch_bounds__(256, 3 - wide_regs<T>()) k_tile_pass(T* __rest
         const int64_t member = t / tiles_per_member;
         const uint64_t tt = (uint64_t)(t - member * tiles_per_member);
         T* mem = state + member * member_elems;
-        const uint64_t base = deposit(tt, pd.outer, pd.nouter);
+        const uint64_t base = deposit(tt, pd.outer, pd.nouter) | pd.fix;
         // ---- load
         if (use_bulk) {
             if (threadIdx.x < 32) {
