@@ -133,6 +133,8 @@ int lsg_program_specialized(lsg_program p);
  * compilation for sm_103a (LSG_E_ARG with the compiler log when it fails). */
 int lsg_program_source(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
                        int64_t pool_entries, int compile, char* buf, int64_t cap, int64_t* len);
+/* Independent of the register the program was created with (either may be freed first); waits for
+ * the device before releasing the program's memory. */
 int lsg_program_free(lsg_program p);
 /* Host-only: the number of fused passes lsg_apply would run for these operators on a register of
  * nbits bits (no device is touched; used for sizing and for algorithmic-byte accounting). */

@@ -864,10 +864,11 @@ static int program_create_jit(int nbits, int precision, int64_t batch, const lsg
     for (const PassDesc& pd : p->plan.passes) bulk = bulk && ((eb << pd.L) % 16) == 0;
     const int ctas = jit_ctas(precision);
     const int64_t bytes_per_run = 2 * ((int64_t)eb << nbits) * batch * (int64_t)p->plan.passes.size();
-    if (bulk && jit_wanted(bytes_per_run)) p->jit = jit_build(p->plan, precision, ctas);
+    const bool swz = jit_swizzle_fits(p->plan, eb, ((int64_t)eb << nbits) * batch);
+    if (bulk && jit_wanted(bytes_per_run)) p->jit = jit_build(p->plan, precision, ctas, swz);
     if (const char* path = getenv("LSG_JIT_DUMP")) {  // diagnostics: the specialized source of this program
         if (FILE* f = std::fopen(path, "w")) {
-            const std::string src = jit_source(p->plan, precision, ctas);
+            const std::string src = jit_source(p->plan, precision, ctas, swz);
             std::fwrite(src.data(), 1, src.size(), f);
             std::fclose(f);
         }
@@ -1184,8 +1185,12 @@ int lsg_program_create(lsg_state shape, const lsg_op* ops, int32_t nops, const d
     clear_error();
     if (!shape || !out) return fail(LSG_E_ARG, "null argument");
     *out = nullptr;
-    return program_create_jit(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out,
-                          shape->stream);
+    LSG_CHECK(program_create_jit(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out,
+                                 shape->stream));
+    // The program outlives no stream of `shape`: the register may be freed first (its stream
+    // destroyed), so the program's memory is released with cudaFree, which waits for the device.
+    (*out)->dev.stream = nullptr;
+    return LSG_OK;
 }
 
 int lsg_program_run(lsg_program p, lsg_state s) {
@@ -1258,7 +1263,9 @@ int lsg_program_source(int nbits, int precision, int64_t batch, const lsg_op* op
     lsg_program_s* p = nullptr;
     LSG_CHECK(program_build(nbits, precision, batch, ops, nops, pool, pool_entries, nullptr, nullptr, nullptr, &p,
                             nullptr, false));
-    const std::string src = jit_source(p->plan, precision, jit_ctas(precision));
+    const size_t eb = lsg_elem_bytes(precision);
+    const std::string src =
+        jit_source(p->plan, precision, jit_ctas(precision), jit_swizzle_fits(p->plan, eb, ((int64_t)eb << nbits) * batch));
     delete p;
     if (len) *len = (int64_t)src.size();
     if (buf && cap > 0) {

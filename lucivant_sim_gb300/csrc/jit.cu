@@ -69,6 +69,9 @@ struct Driver {
                        void**, void**) = nullptr;
     CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
     CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+    CUresult (*encode)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                       const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                       CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;  // optional
 };
 
 const Driver& driver() {
@@ -84,6 +87,7 @@ const Driver& driver() {
                get("cuLaunchKernel", reinterpret_cast<void**>(&r.launch)) &&
                get("cuFuncSetAttribute", reinterpret_cast<void**>(&r.set_attribute)) &&
                get("cuOccupancyMaxActiveBlocksPerMultiprocessor", reinterpret_cast<void**>(&r.occupancy));
+        if (!get("cuTensorMapEncodeTiled", reinterpret_cast<void**>(&r.encode))) r.encode = nullptr;
         cudaGetLastError();
         return r;
     }();
@@ -178,6 +182,26 @@ bool pure_renames(const Plan& plan, const PassDesc& pd, const BlockDesc& b, std:
     return true;
 }
 
+// The shared-memory layout of tiles moved by swizzled tensor copies (common.cuh tma_load_box):
+// element offset x is stored at S(x) = x ^ (((x >> row) & 3) << unit), the 64-byte swizzle in
+// elements (16-byte units `unit` bits up, 64-byte rows `row` bits up). S is linear over GF(2):
+// S(a ^ b) = S(a) ^ S(b), so a group's runtime base and its constant offsets swizzle apart.
+struct Swizzle {
+    bool on = false;
+    int unit = 0, row = 0;
+    static Swizzle for_elem(bool on, int elem_bytes) {
+        Swizzle z;
+        z.on = on;
+        int lg = 0;
+        while ((1 << lg) < elem_bytes) ++lg;
+        z.unit = 4 - lg;
+        z.row = 7 - lg;
+        return z;
+    }
+    uint32_t apply(uint32_t x) const { return on ? x ^ (((x >> row) & 3u) << unit) : x; }
+    uint32_t may(uint32_t m) const { return on ? m | (((m >> row) & 3u) << unit) : m; }
+};
+
 // One register block as generated: its access shape, and the renames folded into its loads
 // (applied to the load addresses, last rename first) and stores (in program order).
 struct BlockGen {
@@ -198,7 +222,7 @@ struct BlockGen {
     bool folded() const { return !load_map.empty() || !store_map.empty(); }
 };
 
-BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int ctas) {
+BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int ctas, const Swizzle& sw) {
     BlockGen g;
     g.b = &b;
     g.U = b.u, g.n = 1 << b.u, g.groups = 1 << (pd.K - b.u);
@@ -206,7 +230,9 @@ BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int c
     // moves as one wider shared-memory access and every operator's coefficients, loaded once,
     // serve both groups (the two calls read the same addresses).
     g.W = (b.sorted[0] != 0 && g.groups >= 2 && 2 * g.n * elem_bytes / 4 <= state_reg_budget(ctas)) ? 2 : 1;
+    if (sw.on && sw.unit == 0) g.W = 1;  // a pair must share a 16-byte unit: the swizzle moves whole units
     g.run = g.W == 2 ? 1 : std::min(std::max((int)b.vec, 1), std::max(1, 16 / elem_bytes));
+    if (sw.on) g.run = std::min(g.run, 1 << sw.unit);
     g.vec_bits = g.W == 2 ? 1u : g.run == 4 ? 3u : g.run == 2 ? 1u : 0u;
     g.off.resize(g.n);
     for (int e = 0; e < g.n; ++e) {
@@ -218,13 +244,13 @@ BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int c
     return g;
 }
 
-// The address expressions of a block's elements under a folded rename map: the runtime part
-// (the group base, renamed) in `var`, a constant per element, joined by + where they cannot share
-// a bit (an immediate offset) and by ^ where they can.
+// The address expressions of a block's elements under a folded rename map and the tile's
+// swizzle: the runtime part (the group base, renamed, swizzled) in `var`, a constant per element,
+// joined by + where they cannot share a bit (an immediate offset) and by ^ where they can.
 std::vector<std::string> mapped_addresses(std::ostringstream& o, const BlockGen& g, const std::vector<Rename>& map,
-                                          const char* var, uint32_t tile_mask) {
+                                          const char* var, uint32_t tile_mask, const Swizzle& sw) {
     std::vector<std::string> addr(g.n);
-    if (map.empty()) {
+    if (map.empty() && !sw.on) {
         for (int e = 0; e < g.n; ++e) addr[e] = "base + " + std::to_string(g.off[e]) + "u";
         return addr;
     }
@@ -238,16 +264,21 @@ std::vector<std::string> mapped_addresses(std::ostringstream& o, const BlockGen&
         may = r.may(may);
         zero = r.apply(zero);
     }
+    if (sw.on) {
+        o << "      " << var << " ^= ((" << var << " >> " << sw.row << ") & 3u) << " << sw.unit << ";\n";
+        may = sw.may(may);
+    }
     for (int e = 0; e < g.n; ++e) {
         uint32_t c = g.off[e];
         for (const Rename& r : map) c = r.apply(c);
-        c ^= zero;  // the map is affine: map(base ^ off) = map(base) ^ map(off) ^ map(0)
+        c = sw.apply(c ^ zero);  // the map is affine: map(base ^ off) = map(base) ^ map(off) ^ map(0)
         addr[e] = std::string(var) + ((c & may) ? " ^ " : " + ") + std::to_string(c) + "u";
     }
     return addr;
 }
 
-void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, const PassDesc& pd, const char* T, bool* ok) {
+void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, const PassDesc& pd, const char* T,
+                const Swizzle& sw, bool* ok) {
     const BlockDesc& b = *g.b;
     const uint32_t tile_mask = pd.K >= 32 ? ~0u : ((1u << pd.K) - 1u);
     const bool fold = g.folded();
@@ -259,7 +290,7 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
     o << "      const uint32_t base =";
     for (int i = 0; i <= g.U; ++i) o << (i ? " |" : "") << " ((G << " << i << ") & " << b.dep[i] << "u)";
     o << ";\n      " << T << " v[" << g.n * g.W << "];\n";
-    const std::vector<std::string> la = mapped_addresses(o, g, g.load_map, "lb", tile_mask);
+    const std::vector<std::string> la = mapped_addresses(o, g, g.load_map, "lb", tile_mask, sw);
     if (fold) o << "      if (act) {\n";
     for (int e = 0; e < g.n; e += g.run) {
         if (g.W == 2)
@@ -276,7 +307,7 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
             }
         }
     if (fold) o << "      }\n      cbar();  // every group is in registers: the renamed stores may land in any group\n      if (act) {\n";
-    const std::vector<std::string> sa = mapped_addresses(o, g, g.store_map, "sb", tile_mask);
+    const std::vector<std::string> sa = mapped_addresses(o, g, g.store_map, "sb", tile_mask, sw);
     for (int e = 0; e < g.n; e += g.run) {
         if (g.W == 2)
             o << "      st_split<" << T << ">(tile + (" << sa[e] << "), v[" << e << "], v[" << g.n + e << "]);\n";
@@ -287,9 +318,10 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
     o << "    }\n";
 }
 
-std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_bytes, int ctas) {
+std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_bytes, int ctas, bool swz) {
     const PassDesc& pd = plan.passes[pi];
     const char* T = type_name(precision);
+    const Swizzle sw = Swizzle::for_elem(swz, elem_bytes);
     // Blocks made only of renames move no arithmetic: they fold into the neighbouring block's
     // store addresses (or the next block's load addresses) unless they touch the bits inside
     // that block's vector accesses, saving a shared-memory round trip and a barrier each.
@@ -298,7 +330,7 @@ std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_byt
     for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
         const BlockDesc& b = plan.blocks[bi];
         if (b.generic) return "";
-        BlockGen g = block_gen(b, pd, elem_bytes, ctas);
+        BlockGen g = block_gen(b, pd, elem_bytes, ctas, sw);
         std::vector<Rename> rn;
         if (pure_renames(plan, pd, b, &rn)) {
             if (held.empty() && !gens.empty() && gens.back().takes(rn)) {
@@ -323,7 +355,7 @@ std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_byt
       << "* __restrict__ data, long long member) {\n";
     bool ok = true;
     for (const BlockGen& g : gens) {
-        emit_block(o, g, plan, pd, T, &ok);
+        emit_block(o, g, plan, pd, T, sw, &ok);
         if (!ok) return "";
     }
     o << "    cbar();\n  }\n};\n";
@@ -352,15 +384,15 @@ bool jit_wanted(int64_t bytes_per_run) {
 namespace {
 
 // Pass i's body and kernel, or "" when the specializer does not take one of its blocks.
-std::string pass_kernel_source(const Plan& plan, size_t i, int precision, int ctas) {
+std::string pass_kernel_source(const Plan& plan, size_t i, int precision, int ctas, bool swz) {
     const char* T = type_name(precision);
-    const std::string body = pass_source(plan, i, precision, (int)lsg_elem_bytes(precision), ctas);
+    const std::string body = pass_source(plan, i, precision, (int)lsg_elem_bytes(precision), ctas, swz);
     if (body.empty()) return "";
     std::ostringstream o;
     o << body << "extern \"C\" __global__ void __launch_bounds__(" << kPipeThreadsHost << ", " << ctas
       << ") lsg_pass_" << i << "(" << T << "* state, long long me, const PassDesc* pg, const " << T
-      << "* data, long long tpm, long long total, int* status) {\n  pipe_kernel<" << T << ", Body" << i
-      << ">(state, me, pg, data, tpm, total, status);\n}\n";
+      << "* data, long long tpm, long long total, int* status, const __grid_constant__ lsg::Tmap tmap) {\n  pipe_kernel<"
+      << T << ", Body" << i << ", " << (swz ? "true" : "false") << ">(state, me, pg, data, tpm, total, status, &tmap);\n}\n";
     return o.str();
 }
 
@@ -403,23 +435,34 @@ int jit_compile_check(const std::string& source) {
     return LSG_OK;
 }
 
-std::string jit_source(const Plan& plan, int precision, int ctas) {
+bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_bytes) {
+    const char* env = getenv("LSG_SWIZZLE");
+    if (env && env[0] == '0') return false;
+    if (register_bytes <= 0 || register_bytes % 512 != 0 || (register_bytes >> 6) >= (1ll << 31)) return false;
+    for (const PassDesc& pd : plan.passes) {
+        const size_t chunk = elem_bytes << pd.L;
+        if (chunk < 512 || chunk % 512 != 0) return false;
+    }
+    return true;
+}
+
+std::string jit_source(const Plan& plan, int precision, int ctas, bool swz) {
     std::string src = kPrelude;
     for (size_t i = 0; i < plan.passes.size(); ++i) {
-        const std::string k = pass_kernel_source(plan, i, precision, ctas);
+        const std::string k = pass_kernel_source(plan, i, precision, ctas, swz);
         if (k.empty()) return "";  // a pass the specializer does not take: interpret them all
         src += k;
     }
     return src;
 }
 
-std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas) {
+std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz) {
     const size_t np = plan.passes.size();
     if (np == 0) return nullptr;
     std::vector<std::string> kernels(np);
     size_t total_len = 0;
     for (size_t i = 0; i < np; ++i) {
-        kernels[i] = pass_kernel_source(plan, i, precision, ctas);
+        kernels[i] = pass_kernel_source(plan, i, precision, ctas, swz);
         if (kernels[i].empty()) return nullptr;  // a pass the specializer does not take: interpret them all
         total_len += kernels[i].size();
     }
@@ -456,6 +499,7 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas) 
         auto jp = std::make_shared<JitPasses>();
         jp->fns.resize(np);
         jp->per_sm.resize(np, 1);
+        jp->swz = swz;
         const size_t eb = lsg_elem_bytes(precision);
         bool ok = true;
         for (size_t c = 0; c < nchunks && ok; ++c) {
@@ -465,7 +509,7 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas) 
                 const size_t i = members[c][j];
                 const std::string name = "lsg_pass_" + std::to_string(i);
                 CUfunction f;
-                const size_t smem = 2 * (eb << plan.passes[i].K);  // the two-tile ring
+                const size_t smem = 2 * (eb << plan.passes[i].K) + (swz ? 1024 : 0);  // the two-tile ring, aligned
                 ok = drv.get_function(&f, mod, name.c_str()) == CUDA_SUCCESS &&
                      drv.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) == CUDA_SUCCESS &&
                      drv.occupancy(&jp->per_sm[i], f, kPipeThreadsHost, smem) == CUDA_SUCCESS;
@@ -485,14 +529,46 @@ int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t membe
     int dev = 0, sms = 0;
     LSG_CUDA(cudaGetDevice(&dev));
     LSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const size_t smem = 2 * tile_bytes;
+    const size_t smem = 2 * tile_bytes + (jp.swz ? 1024 : 0);
+    // the register as rows of 64 bytes, copied in swizzled boxes of min(chunk, 16 KB) (tile.cuh
+    // pipe_run); a map per box height (unused without swizzle)
+    const uint64_t eb = (uint64_t)(tile_bytes >> plan.passes[0].K);
+    const uint64_t bytes = (uint64_t)member_elems * (uint64_t)batch * eb;
+    std::map<uint32_t, CUtensorMap> maps;
+    auto map_for = [&](uint32_t box_rows, CUtensorMap** out) -> int {
+        auto it = maps.find(box_rows);
+        if (it == maps.end()) {
+            CUtensorMap m;
+            std::memset(&m, 0, sizeof(m));
+            if (jp.swz) {
+                if (!drv.encode) return fail(LSG_E_STATE, "cuTensorMapEncodeTiled is not available");
+                if (bytes % 512 != 0 || (bytes >> 6) >= (1ull << 31))
+                    return fail(LSG_E_STATE, "a register of %llu bytes does not fit the swizzled tensor copies",
+                                (unsigned long long)bytes);
+                cuuint64_t dims[2] = {16, bytes >> 6};
+                cuuint64_t strides[1] = {64};
+                cuuint32_t box[2] = {16, box_rows};
+                cuuint32_t estr[2] = {1, 1};
+                if (drv.encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, state, dims, strides, box, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                    return fail(LSG_E_CUDA, "encoding the register's tensor map failed");
+            }
+            it = maps.emplace(box_rows, m).first;
+        }
+        *out = &it->second;
+        return LSG_OK;
+    };
     for (size_t i = 0; i < plan.passes.size(); ++i) {
+        const uint64_t chunk = eb << plan.passes[i].L;
+        CUtensorMap* map = nullptr;
+        LSG_CHECK(map_for((uint32_t)(std::min<uint64_t>(chunk, 16384) >> 6), &map));
         CUfunction f = reinterpret_cast<CUfunction>(jp.fns[i]);
         const int64_t total = tiles_per_member[i] * batch;
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(jp.per_sm[i], 1)));
         const void* pg = static_cast<const unsigned char*>(pass_dev) + i * pass_stride;
         long long me = member_elems, tpm = tiles_per_member[i], tot = total;
-        void* args[] = {&state, &me, &pg, &data, &tpm, &tot, &status};
+        void* args[] = {&state, &me, &pg, &data, &tpm, &tot, &status, map};
         if (marks) LSG_CUDA(cudaEventRecord(marks[i], stream));
         if (drv.launch(f, (unsigned)grid, 1, 1, kPipeThreadsHost, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr) !=
             CUDA_SUCCESS)

@@ -17,6 +17,7 @@ constexpr int kPipeThreadsHost = 288;
 struct JitPasses {
     std::vector<void*> fns;     // CUfunction per pass
     std::vector<int> per_sm;    // resident CTAs per SM of each pass at its shared memory
+    bool swz = false;           // tiles move by swizzled tensor copies (common.cuh tma_load_box)
 };
 
 // LSG_JIT: 0 never specialize, 1 always, unset: programs whose one run moves at least
@@ -26,16 +27,20 @@ int jit_mode();
 bool jit_wanted(int64_t bytes_per_run);
 
 // The CUDA source of a planned gate program's specialized passes, or "" when a pass can't be.
-std::string jit_source(const Plan& plan, int precision, int ctas);
+std::string jit_source(const Plan& plan, int precision, int ctas, bool swz);
 
 // Compile `source` with NVRTC only (no device needed): LSG_OK, or an error with NVRTC's log.
 int jit_compile_check(const std::string& source);
+
+// Whether a program's specialized passes can move tiles as swizzled 512-byte tensor boxes: every
+// pass's contiguous chunks are whole boxes and the register's 64-byte rows fit 31-bit coordinates.
+bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_bytes);
 
 // Specialize a planned gate program (no trajectory operators, no shared-memory operators), or
 // nullptr when it can't be (unsupported operators, no NVRTC, compilation failure): the
 // interpreter then runs it. `ctas` is the launch bound's CTAs per SM. Passes compile in parallel
 // on host threads; modules are cached by source for the life of the process.
-std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas);
+std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz);
 
 // Launch every pass on `stream` (events before each pass when `marks` is given).
 // `tiles_per_member[i]`: the tiles pass i visits in each of the `batch` members.

@@ -794,14 +794,22 @@ constexpr int pipe_ctas() {
 // host specializes at run time: `compute(tile, member)` runs on the 256 compute threads for every
 // tile of this CTA; the producer warp streams the tiles. `pd` is the pass (in shared memory),
 // buf0/buf1 the two tile buffers, full/empty the ring's mbarriers (initialised by the caller).
-template <typename T, typename F>
+// With Swz, the tile moves as 512-byte boxes of tensor copies through `tmap` with the 64-byte
+// swizzle (every chunk of the pass is a whole number of boxes; the compute side addresses the tile
+// through the same swizzle); otherwise as one plain bulk copy per chunk.
+template <typename T, bool Swz = false, typename F>
 __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_elems, const PassDesc& pd, T* buf0,
                                          T* buf1, uint64_t* full, uint64_t* empty, int64_t tiles_per_member,
-                                         int64_t total_tiles, int* status, F&& compute) {
+                                         int64_t total_tiles, int* status, F&& compute, const Tmap* tmap = nullptr) {
     const int K = pd.K, L = pd.L;
     const int nchunks = 1 << (K - L);
     const uint32_t chunk_bytes = (uint32_t)(sizeof(T) << L);
     const int64_t stride = gridDim.x;
+    // boxes of min(chunk, 16 KB): the pass's tensor map has that box height (host jit_launch)
+    const uint32_t box_bytes = chunk_bytes < 16384u ? chunk_bytes : 16384u;
+    const int box_elems = (int)(box_bytes / sizeof(T));
+    const int box_shift = Swz ? (__ffs((int)(chunk_bytes / box_bytes)) - 1) : 0;  // boxes per chunk = 1 << box_shift
+    const int nboxes = nchunks << box_shift;
     if (threadIdx.x >= 256) {
         // ---------------- producer warp
         const int lane = threadIdx.x - 256;
@@ -811,12 +819,23 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
             *mem = state + member * member_elems;
             *base = deposit(tt, pd.outer, pd.nouter) | pd.fix;
         };
+        // the register row (64 bytes) where box q of the tile at `mem + base` starts
+        auto box_row = [&](const T* mem, uint64_t base, int q) {
+            const uint64_t c = (uint64_t)(q >> box_shift);
+            const uint64_t sub = (uint64_t)(q & ((1 << box_shift) - 1)) * (uint64_t)box_elems;
+            const uint64_t elem = (uint64_t)(mem - state) + (base | deposit(c, pd.hi, K - L)) + sub;
+            return (int)((elem * sizeof(T)) >> 6);
+        };
         auto store = [&](int64_t t, T* buf) {
             T* mem;
             uint64_t base;
             tile_at(t, &mem, &base);
-            for (int c = lane; c < nchunks; c += 32)
-                bulk_s2g(mem + (base | deposit((uint64_t)c, pd.hi, K - L)), buf + ((size_t)c << L), chunk_bytes);
+            if constexpr (Swz) {
+                for (int q = lane; q < nboxes; q += 32) tma_store_box(tmap, box_row(mem, base, q), buf + (size_t)q * box_elems);
+            } else {
+                for (int c = lane; c < nchunks; c += 32)
+                    bulk_s2g(mem + (base | deposit((uint64_t)c, pd.hi, K - L)), buf + ((size_t)c << L), chunk_bytes);
+            }
             bulk_commit();
             bulk_wait_read();
             __syncwarp();
@@ -838,8 +857,14 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
             tile_at(t, &mem, &base);
             if (lane == 0) mbar_arrive_expect_tx(&full[b], chunk_bytes * (uint32_t)nchunks);
             __syncwarp();
-            for (int c = lane; c < nchunks; c += 32)
-                bulk_g2s(buf + ((size_t)c << L), mem + (base | deposit((uint64_t)c, pd.hi, K - L)), chunk_bytes, &full[b]);
+            if constexpr (Swz) {
+                for (int q = lane; q < nboxes; q += 32)
+                    tma_load_box(buf + (size_t)q * box_elems, tmap, box_row(mem, base, q), &full[b]);
+            } else {
+                for (int c = lane; c < nchunks; c += 32)
+                    bulk_g2s(buf + ((size_t)c << L), mem + (base | deposit((uint64_t)c, pd.hi, K - L)), chunk_bytes,
+                             &full[b]);
+            }
         }
         // the last one or two tiles
         const int64_t n_it = it;
@@ -906,21 +931,24 @@ __global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe(T* _
 
 // A pass specialized by the host: `Body::run(tile, data, member)` is generated straight-line code
 // (compile-time block bits, operator kinds, positions and data offsets; no operator dispatch).
-template <typename T, typename Body>
+// With Swz the dynamic shared memory holds 1 KB more than the two tiles: the tiles start on a
+// 1024-byte boundary (every 512-byte box then starts on a box boundary).
+template <typename T, typename Body, bool Swz>
 __device__ __forceinline__ void pipe_kernel(T* __restrict__ state, int64_t member_elems, const PassDesc* __restrict__ pass_g,
                                             const T* __restrict__ data, int64_t tiles_per_member, int64_t total_tiles,
-                                            int* status) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+                                            int* status, const Tmap* tmap) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ uint64_t full[2], empty[2];
     __shared__ PassDesc pd;
     const size_t tile_bytes = sizeof(T) << pass_g->K;
-    T* buf0 = reinterpret_cast<T*>(smem_raw);
-    T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
+    unsigned char* tiles = smem_raw + (Swz ? ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u) : 0u);
+    T* buf0 = reinterpret_cast<T*>(tiles);
+    T* buf1 = reinterpret_cast<T*>(tiles + tile_bytes);
     if (threadIdx.x == 0) pd = *pass_g;
     pipe_init(full, empty);
     __syncthreads();
-    pipe_run<T>(state, member_elems, pd, buf0, buf1, full, empty, tiles_per_member, total_tiles, status,
-                [&](T* tile, int64_t member) { Body::run(tile, data, member); });
+    pipe_run<T, Swz>(state, member_elems, pd, buf0, buf1, full, empty, tiles_per_member, total_tiles, status,
+                     [&](T* tile, int64_t member) { Body::run(tile, data, member); }, tmap);
 }
 
 // Runs of N consecutive elements between shared memory and registers (16-, 8- or 4-byte

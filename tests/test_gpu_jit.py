@@ -90,3 +90,19 @@ def test_pauli_transfer_run_from_basis(precision, jit, monkeypatch):
     for index in (0, 0b10_0110_1001):
         want, got = _from_basis_pair(2 * n, precision, 2, ops, index, jit, monkeypatch)
         assert np.array_equal(got, want), f"index {index}: max difference {np.max(np.abs(got - want))}"
+
+
+def test_program_outlives_its_register(monkeypatch):
+    """A program does not hold its creating register's stream: freeing the register first, then
+    running the program on another register and freeing it, is well defined."""
+    monkeypatch.setenv("LSG_JIT", "1")
+    ops = engine.sv_oplist(parse(wl.brickwork(12, 2, seed=1, measure=False)))
+    a = _lib.Register(12, _lib.C64)
+    prog = _lib.Program(a, ops)
+    a.free()
+    with _lib.Register(12, _lib.C64) as b, _lib.Register(12, _lib.C64) as c:
+        prog.run_from_basis(b, 0)
+        c.set_basis(0)
+        prog.run(c)
+        assert np.array_equal(b.download(), c.download())
+    prog.free()
