@@ -694,6 +694,7 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
     // dense matrices, diagonals and mixture matrices placed on 16-byte boundaries (the kernel reads
     // them with 16-byte loads), per member when the data differs per member.
     std::vector<double> ext;
+    ext.reserve((size_t)(2 * pool_entries + pool_entries) + 4096);  // relocated data: about the pool again
     const int64_t per = 16 / (int64_t)lsg_elem_bytes(precision);  // entries per 16 bytes
     auto round_up = [&](int64_t x) { return (x + per - 1) / per * per; };
     auto pad_ext = [&](int64_t lead) {  // pad so that entry (end + lead) is 16-byte aligned
@@ -742,15 +743,9 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
                 pad_ext(lead);
                 const int64_t at = pool_entries + (int64_t)ext.size() / 2;
                 for (int64_t b = 0; b < members; ++b) {
-                    for (int64_t e = 0; e < len; ++e) {
-                        const int64_t src = t.data + b * t.stride + e;
-                        ext.push_back(pool[2 * src]);
-                        ext.push_back(pool[2 * src + 1]);
-                    }
-                    for (int64_t e = len; e < stride; ++e) {
-                        ext.push_back(0.0);
-                        ext.push_back(0.0);
-                    }
+                    const double* src = pool + 2 * (t.data + b * t.stride);
+                    ext.insert(ext.end(), src, src + 2 * len);
+                    ext.resize(ext.size() + 2 * (stride - len), 0.0);
                 }
                 t.data = at;
                 t.stride = t.stride ? stride : 0;
@@ -768,14 +763,8 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
                 }
             }
         }
-    const int64_t all_entries = pool_entries + (int64_t)ext.size() / 2;
-    std::vector<double> merged;
-    if (!ext.empty()) {
-        merged.assign(pool, pool + 2 * pool_entries);
-        merged.insert(merged.end(), ext.begin(), ext.end());
-        pool = merged.data();
-    }
-    pool_entries = all_entries;
+    const int64_t base_entries = pool_entries;  // the caller's pool, then the relocated data
+    pool_entries = base_entries + (int64_t)ext.size() / 2;
     size_t max_meta = 0;
     for (const PassDesc& pd : p->plan.passes)
         max_meta = std::max(max_meta, (size_t)pd.nops * (sizeof(TileOp) + 16) + (size_t)pd.nblocks * sizeof(BlockDesc));
@@ -804,19 +793,25 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
     std::memcpy(blob.data() + p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp),
                 p->plan.blocks.data(), p->plan.blocks.size() * sizeof(BlockDesc));
     std::memcpy(blob.data() + p->basis_off, p->basis_passes.data(), p->basis_passes.size() * sizeof(PassDesc));
+    // the pool in the register precision: complex128 as is, complex64 rounded once, real
+    // registers take the real parts (the imaginary ones are zero)
+    auto put = [&](const double* src, int64_t n, unsigned char* dst) {
+        if (precision == LSG_C128) {
+            if (n) std::memcpy(dst, src, (size_t)n * 16);
+        } else if (precision == LSG_C64) {
+            float* f = reinterpret_cast<float*>(dst);
+            for (int64_t i = 0; i < 2 * n; ++i) f[i] = (float)src[i];
+        } else if (precision == LSG_R64) {
+            double* d = reinterpret_cast<double*>(dst);
+            for (int64_t i = 0; i < n; ++i) d[i] = src[2 * i];
+        } else {
+            float* f = reinterpret_cast<float*>(dst);
+            for (int64_t i = 0; i < n; ++i) f[i] = (float)src[2 * i];
+        }
+    };
     unsigned char* dst = blob.data() + p->head_aligned;
-    if (precision == LSG_C128) {
-        if (pool_entries) std::memcpy(dst, pool, (size_t)pool_entries * 16);
-    } else if (precision == LSG_C64) {
-        float* f = reinterpret_cast<float*>(dst);
-        for (int64_t i = 0; i < 2 * pool_entries; ++i) f[i] = (float)pool[i];  // rounded once
-    } else if (precision == LSG_R64) {
-        double* d = reinterpret_cast<double*>(dst);
-        for (int64_t i = 0; i < pool_entries; ++i) d[i] = pool[2 * i];  // real parts (the others are zero)
-    } else {
-        float* f = reinterpret_cast<float*>(dst);
-        for (int64_t i = 0; i < pool_entries; ++i) f[i] = (float)pool[2 * i];
-    }
+    put(pool, base_entries, dst);
+    put(ext.data(), (int64_t)ext.size() / 2, dst + (size_t)base_entries * elt);
     int rc = ensure(p->dev, total);
     if (rc == LSG_OK) {
         // the host blob is released on return: the copy must have consumed it
@@ -842,6 +837,7 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
 
 // Launch bound of specialized passes: CTAs per SM (the interpreter's pipe_ctas for the element).
 static int jit_ctas(int precision) {
+    if (const char* env = getenv("LSG_JIT_CTAS")) return std::max(1, std::min(4, atoi(env)));
     return (precision == LSG_C128 || precision == LSG_R64) ? 1 : lsg_elem_bytes(precision) == 4 ? 3 : 2;
 }
 

@@ -242,13 +242,32 @@ def _paulis(k: int) -> np.ndarray:
     return hit
 
 
+_BASIS_T_CACHE: dict[int, np.ndarray] = {}
+
+
+def _paulis_t(k: int) -> np.ndarray:
+    """vec(P_a^T) for the 4^k Paulis, shape (4^k, 4^k) (cached)."""
+    hit = _BASIS_T_CACHE.get(k)
+    if hit is None:
+        p = _paulis(k)
+        hit = _BASIS_T_CACHE[k] = np.ascontiguousarray(p.transpose(0, 2, 1).reshape(len(p), -1))
+    return hit
+
+
 def ptm_of_kraus_stack(kraus: np.ndarray) -> np.ndarray:
     """Real Pauli-transfer matrices of channels given as Kraus stacks, shape (..., nk, d, d):
     R[a, c] = d^-1 sum_K Tr(P_a K P_c K^dagger), as (..., d^2, d^2)."""
     d = kraus.shape[-1]
     k = d.bit_length() - 1
     p = _paulis(k)
-    r = np.einsum("aij,...njl,clm,...nim->...ac", p, kraus, p, kraus.conj(), optimize=True) / d
+    n4 = len(p)
+    # E(P_c) = sum_n K_n P_c K_n^dagger for every c, then R[a, c] = d^-1 vec(P_a^T) . vec(E(P_c))
+    kk = kraus[..., :, None, :, :]
+    e = (kk @ p @ np.swapaxes(kk, -1, -2).conj()).sum(axis=-4)
+    bt = _paulis_t(k)
+    r = (bt @ np.swapaxes(e.reshape(*e.shape[:-2], d * d), -1, -2)) / d
+    if r.shape[-2:] != (n4, n4):
+        raise AssertionError("Pauli-transfer shape")
     if np.max(np.abs(r.imag), initial=0.0) > 1e-12:
         raise SimulationError("a channel without a real Pauli-transfer matrix (not Hermiticity-preserving)")
     return np.ascontiguousarray(r.real)
@@ -320,46 +339,54 @@ _CX_SRC = np.array([1, 1, 1, 1, 0, 1, 3, 2], dtype=np.complex128)  # unit phases
 _SWAP_SRC = np.array([1, 1, 1, 1, 0, 2, 1, 3], dtype=np.complex128)
 
 
+def _snap(x: np.ndarray) -> np.ndarray:
+    """Rounding residue of the transfer-matrix products (|x| ~ 1e-16) snapped to the exact 0 and
+    +-1 entries it stands for, so trace preservation and permutation structure are recognised."""
+    x = np.array(x, dtype=np.float64)
+    a = np.abs(x)
+    x[a < 1e-14] = 0.0
+    near = np.abs(a - 1.0) < 1e-14
+    if near.any():
+        x[near] = np.sign(x[near])
+    return x
+
+
 def _add_ptm(ops: OpList, bits: list[int], mats: np.ndarray) -> None:
     """Append one Pauli-transfer operator — ``mats`` (members, d, d), one matrix per member or a
     single shared one — as the cheapest kind that represents it exactly: diagonal, bit renames
-    plus a diagonal, or dense."""
+    plus a diagonal, or dense. Structure is read with rounding residue taken as zero; the data
+    kept is snapped (:func:`_snap`)."""
     mats = np.asarray(mats, dtype=np.float64)
-    # rounding residue of the transfer-matrix products (|x| ~ 1e-16) is snapped to the exact 0 and
-    # +-1 entries it stands for, so trace preservation and permutation structure are recognised
-    mats = np.where(np.abs(mats) < 1e-14, 0.0, mats)
-    mats = np.where(np.abs(np.abs(mats) - 1.0) < 1e-14, np.sign(mats), mats)
     d = mats.shape[-1]
     nb = len(bits)
-    shared = bool((mats == mats[0]).all())
-    if shared:
-        mats = mats[:1]
     idx = np.arange(d)
-    nz = mats != 0
-    offdiag = nz.copy()
-    offdiag[:, idx, idx] = False
+    nz = np.abs(mats) >= 1e-14
+    nz_all = nz.any(axis=0)  # the union of the members' patterns
+    offdiag = nz_all.copy()
+    offdiag[idx, idx] = False
     if not offdiag.any():
-        diags = mats[:, idx, idx].astype(np.complex128)
-        if shared:
+        diags = _snap(mats[:, idx, idx])
+        if (diags == diags[0]).all():
             if not np.all(diags[0] == 1.0):
-                ops.add(OP_DIAG, bits, diags[0])
+                ops.add(OP_DIAG, bits, diags[0].astype(np.complex128))
         else:
-            ops.add_batched(OP_DIAG, bits, diags)
+            ops.add_batched(OP_DIAG, bits, diags.astype(np.complex128))
         return
-    if (nz.sum(axis=2) == 1).all() and (nz.sum(axis=1) == 1).all() and (nz == nz[0]).all():
-        src = nz[0].argmax(axis=1)
+    if (nz_all.sum(axis=1) == 1).all() and (nz_all.sum(axis=0) == 1).all() and (nz == nz_all).all():
+        src = nz_all.argmax(axis=1)
         steps = _renames(src, nb)
         if steps is not None:
             for kind, a, b in steps:
                 ops.add(OP_PERM, [bits[a], bits[b]], _CX_SRC if kind == "cx" else _SWAP_SRC)
-            phases = mats[:, idx, src].astype(np.complex128)
-            if shared or (phases == phases[0]).all():
+            phases = _snap(mats[:, idx, src])
+            if (phases == phases[0]).all():
                 if not np.all(phases[0] == 1.0):
-                    ops.add(OP_DIAG, bits, phases[0])
+                    ops.add(OP_DIAG, bits, phases[0].astype(np.complex128))
             else:
-                ops.add_batched(OP_DIAG, bits, phases)
+                ops.add_batched(OP_DIAG, bits, phases.astype(np.complex128))
             return
-    if shared:
+    mats = _snap(mats)
+    if (mats == mats[0]).all():
         ops.add(OP_MATRIX, bits, mats[0].astype(np.complex128))
     else:
         ops.add_batched(OP_MATRIX, bits, mats.astype(np.complex128))
@@ -382,9 +409,8 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
     ops = OpList()
     cache: dict[tuple[int, ...], np.ndarray] = {}
 
-    def chan_stack(chans: list[Any], k: int) -> np.ndarray:
-        key = tuple(id(ch) for ch in chans)  # the noise models hold their channels for this call
-        hit = cache.get(key)
+    def chan_stack(chans: list[Any], k: int, key: tuple[int, ...]) -> np.ndarray:
+        hit = cache.get(key)  # keyed by the channels' ids: the noise models hold them for this call
         if hit is None:
             mats = np.empty((len(chans), 4**k, 4**k))
             todo: dict[int, list[int]] = {}
@@ -399,18 +425,24 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
             hit = cache[key] = mats
         return hit
 
+    chans_of: dict[tuple[str, tuple[int, ...]], tuple[list[Any], tuple[int, ...]]] = {}  # channels per gate signature
     for op in circuit.operations:
         if op.kind == "gate":
             qs = tuple(op.qubits)
             k = len(qs)
             if k > 2:
                 raise SimulationError("the Pauli-transfer form takes gates on up to two qubits")
-            chans = [nm.gate_error(op.name, qs) if nm is not None else None for nm in noises]
+            sig = (op.name, qs)
+            got = chans_of.get(sig)
+            if got is None:
+                chans = [nm.gate_error(op.name, qs) if nm is not None else None for nm in noises]
+                got = chans_of[sig] = (chans, tuple(id(ch) for ch in chans))
+            chans, chan_key = got
             present = [c is not None for c in chans]
             if any(present) and not all(present):
                 raise ValueError("batched noise models must attach channels to the same gates")
             r_gate = ptm_of_unitary(np.asarray(op.matrix, dtype=np.complex128))
-            mats = chan_stack(chans, k) @ r_gate if chans[0] is not None else r_gate[None]
+            mats = chan_stack(chans, k, chan_key) @ r_gate if chans[0] is not None else r_gate[None]
             _add_ptm(ops, [n + q for q in qs] + list(qs), mats)
         elif op.kind == "reset":
             _add_ptm(ops, [n + op.qubit, op.qubit], ptm_of_kraus(RESET_KRAUS, 1)[None])
