@@ -297,35 +297,70 @@ static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
 // (192 x 136 B + blocks stays under 40 KB, so two pipelined CTAs still share an SM).
 constexpr int kMaxPassOps = 192;
 
+// Starting tiles the planner tries per pass (LSG_PLAN_SEEDS; 1 = the plain greedy sweep). More
+// than about 64 found no better plan for brickwork circuits of 12-20 qubits.
+static int plan_seeds() {
+    const char* env = getenv("LSG_PLAN_SEEDS");
+    return env ? std::max(1, atoi(env)) : 64;
+}
+
 // Greedy fusion: sweep the remaining operators; an operator joins the current pass when its bits
 // fit the tile, the pass has room, and no operator deferred earlier in the sweep shares a bit with
 // it (so program order is kept wherever it matters). Deferred operators start the next sweep.
+// Each pass tries several starting tiles and keeps the sweep that takes the most operators.
 Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* pred, const int* draw,
               const int* count, int umax) {
     Plan plan;
     std::vector<int> remaining(nops);
     for (int i = 0; i < nops; ++i) remaining[i] = i;
     const uint64_t low = (L >= 64) ? ~0ull : ((1ull << L) - 1);
-    while (!remaining.empty()) {
-        uint64_t tile = low;
-        uint64_t blocked = 0;
-        std::vector<int> taken, deferred;
+    auto op_mask = [&](int idx) {
+        uint64_t mask = 0;
+        for (int i = 0; i < ops[idx].nbits; ++i) mask |= 1ull << ops[idx].bits[i];
+        return mask;
+    };
+    // One pass by the greedy sweep from a starting tile: an operator joins when its bits fit and no
+    // operator deferred earlier in the sweep shares a bit with it (program order where it matters).
+    auto sweep = [&](uint64_t start, uint64_t* tile_out, std::vector<int>* taken, std::vector<int>* deferred) {
+        uint64_t tile = start, blocked = 0;
+        taken->clear();
+        deferred->clear();
         for (int idx : remaining) {
-            const lsg_op& op = ops[idx];
-            uint64_t mask = 0;
-            for (int i = 0; i < op.nbits; ++i) mask |= 1ull << op.bits[i];
-            if ((mask & blocked) || (int)taken.size() >= kMaxPassOps) {
-                deferred.push_back(idx);
+            const uint64_t mask = op_mask(idx);
+            if ((mask & blocked) || (int)taken->size() >= kMaxPassOps) {
+                deferred->push_back(idx);
                 blocked |= mask;
                 continue;
             }
-            uint64_t grown = tile | mask;
+            const uint64_t grown = tile | mask;
             if (__builtin_popcountll(grown) <= K) {
                 tile = grown;
-                taken.push_back(idx);
+                taken->push_back(idx);
             } else {
-                deferred.push_back(idx);
+                deferred->push_back(idx);
                 blocked |= mask;
+            }
+        }
+        *tile_out = tile;
+    };
+    const int seeds = plan_seeds();
+    while (!remaining.empty()) {
+        uint64_t tile = low;
+        std::vector<int> taken, deferred;
+        sweep(low, &tile, &taken, &deferred);
+        // Other starting tiles: the low bits plus the bits of one of the next operators, so the tile
+        // can form around later work instead of the first operators' bits; the sweep that takes the
+        // most operators wins (the first one on ties).
+        std::vector<int> t2, d2;
+        for (int j = 1; j < seeds && j < (int)remaining.size(); ++j) {
+            uint64_t start = low | op_mask(remaining[j]);
+            if (__builtin_popcountll(start) > K) continue;
+            uint64_t tile2;
+            sweep(start, &tile2, &t2, &d2);
+            if (t2.size() > taken.size()) {
+                tile = tile2;
+                taken.swap(t2);
+                deferred.swap(d2);
             }
         }
         if (taken.empty()) {  // an operator wider than the tile allows: no progress possible
