@@ -44,12 +44,25 @@ def precision_code(precision: str | None) -> int:
         raise ValueError(f"precision must be one of {', '.join(PRECISIONS)}") from None
 
 
+_OFFDIAG: dict[int, np.ndarray] = {}
+
+
 def classify(m: np.ndarray) -> tuple[int, np.ndarray]:
     """(kind, data) for a gate matrix: diagonal, phased permutation, or dense."""
     m = np.asarray(m, dtype=np.complex128)
-    nz = m != 0
     d = m.shape[0]
-    if not np.any(nz & ~np.eye(d, dtype=bool)):
+    if d == 2:  # the common one-qubit case without array passes
+        a, b, c, e = m.ravel().tolist()
+        if b == 0 and c == 0:
+            return OP_DIAG, np.array([a, e])
+        if a == 0 and e == 0 and b != 0 and c != 0:
+            return OP_PERM, np.array([b, c, 1.0, 0.0], dtype=np.complex128)
+        return OP_MATRIX, m
+    nz = m != 0
+    off = _OFFDIAG.get(d)
+    if off is None:
+        off = _OFFDIAG[d] = ~np.eye(d, dtype=bool)
+    if not np.any(nz & off):
         return OP_DIAG, np.diagonal(m).copy()
     if bool((nz.sum(axis=1) == 1).all() and (nz.sum(axis=0) == 1).all()):
         src = nz.argmax(axis=1)
