@@ -319,6 +319,8 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
         for (int i = 0; i < ops[idx].nbits; ++i) mask |= 1ull << ops[idx].bits[i];
         return mask;
     };
+    const char* ops_env = getenv("LSG_PASS_OPS");
+    const int max_ops = ops_env ? std::max(1, std::min(kMaxPassOps, atoi(ops_env))) : kMaxPassOps;
     // One pass by the greedy sweep from a starting tile: an operator joins when its bits fit and no
     // operator deferred earlier in the sweep shares a bit with it (program order where it matters).
     auto sweep = [&](uint64_t start, uint64_t* tile_out, std::vector<int>* taken, std::vector<int>* deferred) {
@@ -327,7 +329,7 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
         deferred->clear();
         for (int idx : remaining) {
             const uint64_t mask = op_mask(idx);
-            if ((mask & blocked) || (int)taken->size() >= kMaxPassOps) {
+            if ((mask & blocked) || (int)taken->size() >= max_ops) {
                 deferred->push_back(idx);
                 blocked |= mask;
                 continue;
@@ -931,12 +933,14 @@ int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const 
     return program_launch(p, s, marks, ctx, false);
 }
 
+int set_basis_async(lsg_state_s* s, int64_t index);
+
 // Set every member to basis state `index`, then run the passes on the tiles that can be nonzero.
 static int program_run_basis(lsg_program_s* p, lsg_state_s* s, int64_t index, cudaEvent_t* marks) {
     if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
         return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
                     p->nbits, p->precision, (long long)p->batch);
-    LSG_CHECK(lsg_state_set_basis(s, index));
+    LSG_CHECK(set_basis_async(s, index));  // stream-ordered: no host wait before the passes
     const bool real = s->real();
     if (!real && index != p->basis_index) {  // the fixed values are the index's bits: re-upload
         p->basis_passes = basis_passes(p->plan, p->nbits, p->precision, index);
@@ -967,24 +971,22 @@ int apply_ops(lsg_state_s* s, const lsg_op* ops, int32_t nops, const double* poo
 
 // ------------------------------------------------------------------------ register kernels
 
+// After a zero fill: member m's element `index` of a complex register set to 1.
 template <typename R>
-__global__ void k_set_basis(Cx<R>* state, int64_t elems, int64_t batch, int64_t index) {
-    const int64_t n = elems * batch;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = i % elems;
-        state[i] = Cx<R>(j == index ? R(1) : R(0), R(0));
-    }
+__global__ void k_basis_one(Cx<R>* state, int64_t elems, int64_t batch, int64_t index) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < batch; m += (int64_t)gridDim.x * blockDim.x)
+        state[m * elems + index] = Cx<R>(R(1), R(0));
 }
 
-// Pauli-transfer form of |b><b| on n qubits: r_P = <b|P|b>, which is (-1)^{|z & b|} for the
-// diagonal Paulis (x = 0: register index z below 2^n) and 0 for every other.
+// After a zero fill: the Pauli-transfer form of |b><b| on n qubits, r_P = <b|P|b>, which is
+// (-1)^{|z & b|} for the 2^n diagonal Paulis (x = 0: register index z below 2^n) of every member
+// (the others stay 0).
 template <typename R>
-__global__ void k_set_basis_ptm(R* state, int64_t elems, int64_t batch, int n, int64_t b) {
-    const int64_t total = elems * batch;
-    const int64_t zmax = 1ll << n;
+__global__ void k_basis_diag_ptm(R* state, int64_t elems, int64_t batch, int n, int64_t b) {
+    const int64_t zmax = 1ll << n, total = zmax * batch;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = i % elems;
-        state[i] = j < zmax ? ((__popcll((unsigned long long)(j & b)) & 1) ? R(-1) : R(1)) : R(0);
+        const int64_t m = i >> n, z = i & (zmax - 1);
+        state[m * elems + z] = (__popcll((unsigned long long)(z & b)) & 1) ? R(-1) : R(1);
     }
 }
 
@@ -1017,6 +1019,25 @@ __global__ void k_c64_to_c128(const float2* in, double2* out, int64_t n) {
 unsigned grid_for(int64_t n, int threads = 256) {
     int64_t g = (n + threads - 1) / threads;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
+}
+
+// Every member to basis state `index`, enqueued on the register's stream: a zero fill at the
+// copy engine's write rate, then the nonzero entries.
+int set_basis_async(lsg_state_s* s, int64_t index) {
+    const int64_t limit = s->real() ? (1ll << (s->nbits / 2)) : s->elems;  // real: |index><index| of nbits/2 qubits
+    if (index < 0 || index >= limit) return fail(LSG_E_ARG, "basis index %lld out of range", (long long)index);
+    LSG_CUDA(cudaMemsetAsync(s->data, 0, s->member_bytes() * (size_t)s->batch, s->stream));
+    const int n = s->nbits / 2;
+    if (s->precision == LSG_C128)
+        k_basis_one<double><<<grid_for(s->batch), 256, 0, s->stream>>>((Cx<double>*)s->data, s->elems, s->batch, index);
+    else if (s->precision == LSG_C64)
+        k_basis_one<float><<<grid_for(s->batch), 256, 0, s->stream>>>((Cx<float>*)s->data, s->elems, s->batch, index);
+    else if (s->precision == LSG_R64)
+        k_basis_diag_ptm<double><<<grid_for(s->batch << n), 256, 0, s->stream>>>((double*)s->data, s->elems, s->batch, n, index);
+    else
+        k_basis_diag_ptm<float><<<grid_for(s->batch << n), 256, 0, s->stream>>>((float*)s->data, s->elems, s->batch, n, index);
+    LSG_CUDA(cudaGetLastError());
+    return LSG_OK;
 }
 
 }  // namespace lsg
@@ -1103,18 +1124,7 @@ int lsg_state_free(lsg_state s) {
 int lsg_state_set_basis(lsg_state s, int64_t index) {
     clear_error();
     if (!s) return fail(LSG_E_ARG, "null register");
-    const int64_t limit = s->real() ? (1ll << (s->nbits / 2)) : s->elems;  // real: |index><index| of nbits/2 qubits
-    if (index < 0 || index >= limit) return fail(LSG_E_ARG, "basis index %lld out of range", (long long)index);
-    const int64_t n = s->elems * s->batch;
-    if (s->precision == LSG_C128)
-        k_set_basis<double><<<grid_for(n), 256, 0, s->stream>>>((Cx<double>*)s->data, s->elems, s->batch, index);
-    else if (s->precision == LSG_C64)
-        k_set_basis<float><<<grid_for(n), 256, 0, s->stream>>>((Cx<float>*)s->data, s->elems, s->batch, index);
-    else if (s->precision == LSG_R64)
-        k_set_basis_ptm<double><<<grid_for(n), 256, 0, s->stream>>>((double*)s->data, s->elems, s->batch, s->nbits / 2, index);
-    else
-        k_set_basis_ptm<float><<<grid_for(n), 256, 0, s->stream>>>((float*)s->data, s->elems, s->batch, s->nbits / 2, index);
-    LSG_CUDA(cudaGetLastError());
+    LSG_CHECK(set_basis_async(s, index));
     LSG_CUDA(cudaStreamSynchronize(s->stream));
     return LSG_OK;
 }
