@@ -101,7 +101,8 @@ __global__ void k_t_advance(int64_t* cursor, const uint64_t* pred, int slot, int
         if (has(pred, b, slot)) cursor[b] += count;
 }
 
-// per-member partial sums of |a|^2 over indices with bit q = 1; partials[b * gridDim.x + block]
+// per-member partial sums of |a|^2 over indices with bit q = 1; partials[b * gridDim.x + block].
+// complex64 reads 16 bytes (two amplitudes) at a time.
 template <typename R>
 __global__ void k_t_p1(const Cx<R>* __restrict__ state, int64_t elems, int q, const uint64_t* pred, int slot,
                        double* __restrict__ partials) {
@@ -109,11 +110,28 @@ __global__ void k_t_p1(const Cx<R>* __restrict__ state, int64_t elems, int q, co
     double acc = 0.0;
     if (has(pred, b, slot)) {
         const Cx<R>* s = state + b * elems;
-        const int64_t half = elems >> 1;
-        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
-            const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
-            const uint64_t idx = (((uint64_t)i >> q) << (q + 1)) | (1ull << q) | lo;
-            acc += nrm2(s[idx]);
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        if constexpr (sizeof(R) == 4) {
+            if (q == 0) {  // the odd amplitudes: the second half of every 16-byte pair
+                for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (elems >> 1); j += stride) {
+                    const float4 w = *reinterpret_cast<const float4*>(s + 2 * j);
+                    acc += nrm2(Cx<R>(w.z, w.w));
+                }
+            } else {  // two consecutive amplitudes with bit q set per load
+                for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (elems >> 2); j += stride) {
+                    const uint64_t i = 2 * (uint64_t)j;
+                    const uint64_t idx = ((i >> q) << (q + 1)) | (1ull << q) | (i & ((1ull << q) - 1));
+                    const float4 w = *reinterpret_cast<const float4*>(s + idx);
+                    acc += nrm2(Cx<R>(w.x, w.y)) + nrm2(Cx<R>(w.z, w.w));
+                }
+            }
+        } else {
+            const int64_t half = elems >> 1;
+            for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += stride) {
+                const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
+                const uint64_t idx = (((uint64_t)i >> q) << (q + 1)) | (1ull << q) | lo;
+                acc += nrm2(s[idx]);
+            }
         }
     }
     const double tot = t_block_sum(acc);
@@ -155,41 +173,105 @@ __global__ void k_t_decide(const double* __restrict__ partials, int nparts, int6
     }
 }
 
-// zero the other half, divide by sqrt(probability); a reset with outcome 1 then applies X
+// Collapse onto the drawn outcome: the outcome's half divided by sqrt(probability), the other half
+// zero (a reset with outcome 1 then applies X: the kept half moves to bit q = 0). With q_next >= 0
+// the same pass accumulates the next measurement's p(1) partials over the new amplitudes, as
+// k_t_p1 would (members this step skips keep their state and are summed too). complex64 moves 16
+// bytes (two amplitudes) per access and reads only the half it keeps.
 template <typename R>
 __global__ void k_t_collapse(Cx<R>* __restrict__ state, int64_t elems, int q, const int* outcome, const double* prob,
-                             int is_reset) {
+                             int is_reset, int q_next, const uint64_t* pred, int slot_next,
+                             double* __restrict__ partials) {
     const int64_t b = blockIdx.y;
     const int out = outcome[b];
-    if (out < 0) return;
+    const bool want = q_next >= 0 && has(pred, b, slot_next);
     Cx<R>* s = state + b * elems;
-    const double p = prob[b];
+    const double p = out >= 0 ? prob[b] : 1.0;
     const double div = p > 0 ? sqrt(p) : 1.0;
-    const bool scale = p > 0;
+    const bool scale = out >= 0 && p > 0;
     // complex128 divides by the FP64 norm exactly as Orrery does; complex64 multiplies by its
     // FP64 reciprocal rounded once (an FP64 division per element would bind the pass to FP64)
     const R inv = (R)(1.0 / div);
-    const int64_t half = elems >> 1;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
-        const uint64_t i0 = (((uint64_t)i >> q) << (q + 1)) | lo;
-        const uint64_t i1 = i0 | (1ull << q);
-        Cx<R> keep = out ? s[i1] : s[i0];
-        if (scale) {
-            if constexpr (sizeof(R) == 8) keep = Cx<R>(keep.re / div, keep.im / div);
-            else keep = Cx<R>(keep.re * inv, keep.im * inv);
-        }
-        const Cx<R> zero(R(0), R(0));
-        if (out == 0) {
-            s[i0] = keep;
-            s[i1] = zero;
-        } else if (is_reset) {
-            s[i0] = keep;  // X after the collapse onto |1>
-            s[i1] = zero;
+    auto fix = [&](Cx<R> a) {
+        if (!scale) return a;
+        if constexpr (sizeof(R) == 8) return Cx<R>(a.re / div, a.im / div);
+        else return Cx<R>(a.re * inv, a.im * inv);
+    };
+    const Cx<R> zero(R(0), R(0));
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    double acc = 0.0;
+    // new amplitudes of the pair (bit q = 0, bit q = 1) from the kept one
+    auto pair = [&](Cx<R> a0, Cx<R> a1, Cx<R>* n0, Cx<R>* n1) {
+        if (out == 0) *n0 = fix(a0), *n1 = zero;
+        else if (is_reset) *n0 = fix(a1), *n1 = zero;
+        else *n0 = zero, *n1 = fix(a1);
+    };
+    auto count = [&](uint64_t idx, Cx<R> a) {
+        if (want && ((idx >> q_next) & 1)) acc += nrm2(a);
+    };
+    if (out >= 0 || want) {
+        if constexpr (sizeof(R) == 4) {
+            if (q == 0) {  // one 16-byte load holds the pair
+                for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (elems >> 1); j += stride) {
+                    const uint64_t idx = 2 * (uint64_t)j;
+                    float4* at = reinterpret_cast<float4*>(s + idx);
+                    const float4 w = *at;
+                    Cx<R> n0(w.x, w.y), n1(w.z, w.w);
+                    if (out >= 0) {
+                        pair(n0, n1, &n0, &n1);
+                        *at = make_float4(n0.re, n0.im, n1.re, n1.im);
+                    }
+                    count(idx, n0);
+                    count(idx + 1, n1);
+                }
+            } else {  // two consecutive pairs: 16 bytes from each half
+                for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (elems >> 2); j += stride) {
+                    const uint64_t i = 2 * (uint64_t)j;
+                    const uint64_t i0 = ((i >> q) << (q + 1)) | (i & ((1ull << q) - 1));
+                    const uint64_t i1 = i0 | (1ull << q);
+                    float4* at0 = reinterpret_cast<float4*>(s + i0);
+                    float4* at1 = reinterpret_cast<float4*>(s + i1);
+                    Cx<R> a0, b0, a1, b1;  // (i0, i0+1), (i1, i1+1)
+                    if (out < 0 || out == 0 || want) {
+                        const float4 w = *at0;
+                        a0 = Cx<R>(w.x, w.y), b0 = Cx<R>(w.z, w.w);
+                    }
+                    if (out < 0 || out == 1 || want) {
+                        const float4 w = *at1;
+                        a1 = Cx<R>(w.x, w.y), b1 = Cx<R>(w.z, w.w);
+                    }
+                    if (out >= 0) {
+                        pair(a0, a1, &a0, &a1);
+                        pair(b0, b1, &b0, &b1);
+                        *at0 = make_float4(a0.re, a0.im, b0.re, b0.im);
+                        *at1 = make_float4(a1.re, a1.im, b1.re, b1.im);
+                    }
+                    count(i0, a0);
+                    count(i0 + 1, b0);
+                    count(i1, a1);
+                    count(i1 + 1, b1);
+                }
+            }
         } else {
-            s[i0] = zero;
-            s[i1] = keep;
+            const int64_t half = elems >> 1;
+            for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += stride) {
+                const uint64_t lo = (uint64_t)i & ((1ull << q) - 1);
+                const uint64_t i0 = (((uint64_t)i >> q) << (q + 1)) | lo;
+                const uint64_t i1 = i0 | (1ull << q);
+                Cx<R> n0 = s[i0], n1 = s[i1];
+                if (out >= 0) {
+                    pair(n0, n1, &n0, &n1);
+                    s[i0] = n0;
+                    s[i1] = n1;
+                }
+                count(i0, n0);
+                count(i1, n1);
+            }
         }
+    }
+    if (q_next >= 0) {
+        const double tot = t_block_sum(acc);
+        if (threadIdx.x == 0) partials[b * gridDim.x + blockIdx.x] = tot;
     }
 }
 
@@ -424,7 +506,10 @@ int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int6
     ctx.pred = c.pred;
     const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(((elems >> 1) + kT * 4 - 1) / (kT * 4),
                                                                           std::max<int64_t>(1, 8192 / B)));
-    for (const Step& sp : t->steps) {
+    bool p1_ready = false;  // the current step's p(1) partials were accumulated by the previous collapse
+    for (size_t si = 0; si < t->steps.size(); ++si) {
+        const Step& sp = t->steps[si];
+        bool next_p1_ready = false;
         switch (sp.kind) {
             case STEP_SEG: LSG_CHECK(program_run_ctx(sp.seg, s, nullptr, ctx)); break;
             case STEP_ADVANCE:
@@ -432,11 +517,17 @@ int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int6
                 break;
             case STEP_MEASURE: {
                 double* part = (double*)t->parts.ptr;
-                k_t_p1<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.pred, sp.slot, part);
+                if (!p1_ready)
+                    k_t_p1<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.pred, sp.slot, part);
                 k_t_decide<<<t_grid(B), kT, 0, st>>>(part, (int)gx, c.cursor, u, ustride, c.pred, sp.slot, sp.clbit,
                                                     sp.readout, sp.p01, sp.p10, sp.is_reset, c.clbits, t->words,
                                                     c.outcome, c.prob, c.near, B);
-                k_t_collapse<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.outcome, c.prob, sp.is_reset);
+                // a measurement right after this one: its p(1) partials come out of this collapse
+                const Step* nx = si + 1 < t->steps.size() ? &t->steps[si + 1] : nullptr;
+                const bool fuse = nx && nx->kind == STEP_MEASURE;
+                k_t_collapse<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.outcome, c.prob, sp.is_reset,
+                                                                    fuse ? nx->q : -1, c.pred, fuse ? nx->slot : 0, part);
+                next_p1_ready = fuse;
                 break;
             }
             case STEP_KRAUS: {
@@ -461,6 +552,7 @@ int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int6
             }
             default: break;
         }
+        p1_ready = next_p1_ready;
     }
     LSG_CUDA(cudaGetLastError());
     return LSG_OK;
