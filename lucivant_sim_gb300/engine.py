@@ -364,47 +364,6 @@ def _snap(x: np.ndarray) -> np.ndarray:
     return x
 
 
-def _add_ptm(ops: OpList, bits: list[int], mats: np.ndarray) -> None:
-    """Append one Pauli-transfer operator — ``mats`` (members, d, d), one matrix per member or a
-    single shared one — as the cheapest kind that represents it exactly: diagonal, bit renames
-    plus a diagonal, or dense. Structure is read with rounding residue taken as zero; the data
-    kept is snapped (:func:`_snap`)."""
-    mats = np.asarray(mats, dtype=np.float64)
-    d = mats.shape[-1]
-    nb = len(bits)
-    idx = np.arange(d)
-    nz = np.abs(mats) >= 1e-14
-    nz_all = nz.any(axis=0)  # the union of the members' patterns
-    offdiag = nz_all.copy()
-    offdiag[idx, idx] = False
-    if not offdiag.any():
-        diags = _snap(mats[:, idx, idx])
-        if (diags == diags[0]).all():
-            if not np.all(diags[0] == 1.0):
-                ops.add(OP_DIAG, bits, diags[0].astype(np.complex128))
-        else:
-            ops.add_batched(OP_DIAG, bits, diags.astype(np.complex128))
-        return
-    if (nz_all.sum(axis=1) == 1).all() and (nz_all.sum(axis=0) == 1).all() and (nz == nz_all).all():
-        src = nz_all.argmax(axis=1)
-        steps = _renames(src, nb)
-        if steps is not None:
-            for kind, a, b in steps:
-                ops.add(OP_PERM, [bits[a], bits[b]], _CX_SRC if kind == "cx" else _SWAP_SRC)
-            phases = _snap(mats[:, idx, src])
-            if (phases == phases[0]).all():
-                if not np.all(phases[0] == 1.0):
-                    ops.add(OP_DIAG, bits, phases[0].astype(np.complex128))
-            else:
-                ops.add_batched(OP_DIAG, bits, phases.astype(np.complex128))
-            return
-    mats = _snap(mats)
-    if (mats == mats[0]).all():
-        ops.add(OP_MATRIX, bits, mats[0].astype(np.complex128))
-    else:
-        ops.add_batched(OP_MATRIX, bits, mats.astype(np.complex128))
-
-
 def ptm_capable(circuit: Any, noises: list[Any]) -> bool:
     """The Pauli-transfer form takes gates and channels on up to two qubits (wider ones would be
     4^k-dense real operators); otherwise the complex vectorised form is used."""
@@ -414,12 +373,71 @@ def ptm_capable(circuit: Any, noises: list[Any]) -> bool:
     return True
 
 
+def _ptm_entries(mats: np.ndarray) -> list[tuple[str, Any]]:
+    """Classify a stack of Pauli-transfer operators, ``mats`` (gates, members, d, d), each as the
+    cheapest kind that represents it exactly: ("diag", diagonals), ("perm", (bit renames,
+    phases)) — a GF(2)-linear permutation of digit patterns with signs — or ("dense", matrices),
+    each with a leading member axis. Structure is read with rounding residue taken as zero and
+    only the data kept is snapped (:func:`_snap`)."""
+    g, _m, d, _ = mats.shape
+    idx = np.arange(d)
+    a = np.abs(mats)
+    big, small = a.max(axis=1) >= 1e-14, a.min(axis=1) >= 1e-14  # (gates, d, d)
+    nz_all = big  # the union of the members' patterns
+    same = (small | ~big).all(axis=(1, 2))  # every member has the union's pattern
+    diag_only = ~(nz_all & ~np.eye(d, dtype=bool)).any(axis=(1, 2))
+    perm_like = (nz_all.sum(axis=2) == 1).all(axis=1) & (nz_all.sum(axis=1) == 1).all(axis=1) & same
+    out: list[tuple[str, Any] | None] = [None] * g
+    dense = []
+    for i in range(g):
+        if diag_only[i]:
+            out[i] = ("diag", _snap(mats[i][:, idx, idx]))
+            continue
+        if perm_like[i]:
+            src = nz_all[i].argmax(axis=1)
+            steps = _renames(src, d.bit_length() - 1)
+            if steps is not None:
+                out[i] = ("perm", (steps, _snap(mats[i][:, idx, src])))
+                continue
+        dense.append(i)
+    if dense:
+        snapped = _snap(mats[dense])
+        for j, i in enumerate(dense):
+            out[i] = ("dense", snapped[j])
+    return out  # type: ignore[return-value]
+
+
+def _emit_ptm(ops: OpList, bits: list[int], entry: tuple[str, Any]) -> None:
+    """Append one classified Pauli-transfer operator: shared by all members when their data
+    agree, per member otherwise; identity diagonals are left out."""
+    kind, val = entry
+    if kind == "diag":
+        if (val == val[0]).all():
+            if not np.all(val[0] == 1.0):
+                ops.add(OP_DIAG, bits, val[0].astype(np.complex128))
+        else:
+            ops.add_batched(OP_DIAG, bits, val.astype(np.complex128))
+    elif kind == "perm":
+        steps, phases = val
+        for k, a, b in steps:
+            ops.add(OP_PERM, [bits[a], bits[b]], _CX_SRC if k == "cx" else _SWAP_SRC)
+        if (phases == phases[0]).all():
+            if not np.all(phases[0] == 1.0):
+                ops.add(OP_DIAG, bits, phases[0].astype(np.complex128))
+        else:
+            ops.add_batched(OP_DIAG, bits, phases.astype(np.complex128))
+    elif (val == val[0]).all():
+        ops.add(OP_MATRIX, bits, val[0].astype(np.complex128))
+    else:
+        ops.add_batched(OP_MATRIX, bits, val.astype(np.complex128))
+
+
 def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
     """The noisy static evolution of :func:`dm_oplist` as Pauli-transfer operators: each gate
     with its channel is ONE real operator on the (x, z) digits of its qubits. Channel matrices are
-    formed once per distinct channel and composed with the gate for all members in one product."""
+    formed once per distinct channel; the gates' transfer matrices, their products with the
+    channels and the classification run over all gates sharing a channel stack at once."""
     n = circuit.num_qubits
-    ops = OpList()
     cache: dict[tuple[int, ...], np.ndarray] = {}
 
     def chan_stack(chans: list[Any], k: int, key: tuple[int, ...]) -> np.ndarray:
@@ -432,13 +450,17 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
                     mats[i] = ptm_depolarizing(ch.params[0], k)
                 else:
                     todo.setdefault(len(ch.kraus), []).append(i)
-            for _nk, members in todo.items():  # one einsum per Kraus count
+            for _nk, members in todo.items():  # one product per Kraus count
                 kr = np.stack([np.stack([np.asarray(m, dtype=np.complex128) for m in chans[i].kraus]) for i in members])
                 mats[members] = ptm_of_kraus_stack(kr)
             hit = cache[key] = mats
         return hit
 
+    # 1. the gates and resets in order, grouped by (arity, channel stack)
     chans_of: dict[tuple[str, tuple[int, ...]], tuple[list[Any], tuple[int, ...]]] = {}  # channels per gate signature
+    items: list[tuple[list[int], tuple[Any, ...], int]] = []  # (bits, group key, index in group)
+    groups: dict[tuple[Any, ...], list[np.ndarray]] = {}
+    uniq: dict[tuple[Any, ...], dict[bytes, int]] = {}
     for op in circuit.operations:
         if op.kind == "gate":
             qs = tuple(op.qubits)
@@ -454,12 +476,38 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
             present = [c is not None for c in chans]
             if any(present) and not all(present):
                 raise ValueError("batched noise models must attach channels to the same gates")
-            r_gate = ptm_of_unitary(np.asarray(op.matrix, dtype=np.complex128))
-            mats = chan_stack(chans, k, chan_key) @ r_gate if chans[0] is not None else r_gate[None]
-            _add_ptm(ops, [n + q for q in qs] + list(qs), mats)
+            gkey = ("gate", k, chan_key if chans[0] is not None else None)
+            if gkey not in groups:
+                groups[gkey] = []
+                if chans[0] is not None:
+                    chan_stack(chans, k, chan_key)
+            u = np.asarray(op.matrix, dtype=np.complex128)
+            ukey = u.tobytes()  # equal gates (every cx) share their product and classification
+            at = uniq.setdefault(gkey, {}).get(ukey)
+            if at is None:
+                at = uniq[gkey][ukey] = len(groups[gkey])
+                groups[gkey].append(u)
+            items.append(([n + q for q in qs] + list(qs), gkey, at))
         elif op.kind == "reset":
-            _add_ptm(ops, [n + op.qubit, op.qubit], ptm_of_kraus(RESET_KRAUS, 1)[None])
+            items.append(([n + op.qubit, op.qubit], ("reset",), 0))
+            groups.setdefault(("reset",), [])
         # measurements are deferred; a global phase leaves a density matrix unchanged
+    # 2. per group: the gates' transfer matrices in one product, composed with the channel stack
+    entries: dict[tuple[Any, ...], list[tuple[str, Any]]] = {}
+    for gkey, us in groups.items():
+        if gkey[0] == "reset":
+            entries[gkey] = _ptm_entries(ptm_of_kraus(RESET_KRAUS, 1)[None, None])
+            continue
+        r_gates = ptm_of_kraus_stack(np.stack(us)[:, None])  # (gates, d, d)
+        if gkey[2] is None:
+            mats = r_gates[:, None]
+        else:
+            mats = cache[gkey[2]][None] @ r_gates[:, None]  # (gates, members, d, d)
+        entries[gkey] = _ptm_entries(mats)
+    # 3. the operators in circuit order
+    ops = OpList()
+    for bits, gkey, i in items:
+        _emit_ptm(ops, bits, entries[gkey][i])
     return ops
 
 
