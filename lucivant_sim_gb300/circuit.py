@@ -169,6 +169,28 @@ def format_bits(circuit: Any, bits: int) -> str:
     )
 
 
+def format_bits_many(circuit: Any, values: np.ndarray) -> list[str]:
+    """:func:`format_bits` of many packed outcomes (int64, fewer than 63 classical bits) at once:
+    the characters of every string are laid out in one byte array."""
+    values = np.asarray(values, dtype=np.int64)
+    regs = list(reversed(circuit.cregs)) if circuit.cregs else [None]
+    cols: list[np.ndarray] = []
+    for i, reg in enumerate(regs):
+        offset, size = (0, circuit.num_clbits) if reg is None else (reg.offset, reg.size)
+        if i:
+            cols.append(np.full((values.size, 1), ord(" "), dtype=np.uint8))
+        if size:
+            shifts = np.arange(offset + size - 1, offset - 1, -1, dtype=np.int64)  # most significant first
+            cols.append((((values[:, None] >> shifts) & 1) + ord("0")).astype(np.uint8))
+    if not cols or values.size == 0:
+        return ["" for _ in range(values.size)] if not cols else []
+    chars = np.ascontiguousarray(np.concatenate(cols, axis=1))
+    width = chars.shape[1]
+    if width == 0:
+        return ["" for _ in range(values.size)]
+    return [b.decode() for b in chars.view(f"S{width}").ravel()]
+
+
 @dataclass(frozen=True)
 class Circuit:
     num_qubits: int

@@ -26,7 +26,7 @@ import numpy as np
 from numpy.typing import NDArray
 
 from lucivant_sim_gb300 import _lib, engine
-from lucivant_sim_gb300.circuit import Circuit, final_measurements, format_bits
+from lucivant_sim_gb300.circuit import Circuit, final_measurements, format_bits, format_bits_many
 from lucivant_sim_gb300.clifford import clifford_problem
 from lucivant_sim_gb300.engine import MAX_DENSITY_QUBITS, SimulationError, pauli_masks
 from lucivant_sim_gb300.qasm import load, parse
@@ -206,6 +206,7 @@ def count_bits(circuit: Any, bits: np.ndarray, clbits: list[int]) -> dict[str, i
         for j, c in enumerate(clbits):
             packed |= bits[:, j].astype(np.int64) << c
         values, counts = np.unique(packed, return_counts=True)
+        return dict(zip(format_bits_many(circuit, values), counts.tolist(), strict=True))
     return {format_bits(circuit, int(v)): int(n) for v, n in zip(values, counts, strict=True)}
 
 

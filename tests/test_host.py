@@ -304,3 +304,18 @@ def test_specialized_pass_source_compiles():
     wide = _lib.OpList()
     wide.add(_lib.OP_MATRIX, [0, 1, 2, 3, 4], np.eye(32, dtype=complex))
     assert _lib.specialized_source(14, _lib.C64, 1, wide) == ""
+
+
+def test_format_bits_many_matches_format_bits():
+    from lucivant_sim_gb300.circuit import format_bits, format_bits_many
+
+    rng = np.random.default_rng(5)
+    for src in (
+        'OPENQASM 3; qubit[5] q; bit[5] c;',
+        'OPENQASM 3; qubit[6] q; bit[2] a; bit[3] b; bit[1] d;',
+        'OPENQASM 2.0; qreg q[4]; creg c[4];',
+    ):
+        c = ls.parse(src)
+        values = np.unique(rng.integers(0, 1 << c.num_clbits, size=40))
+        assert format_bits_many(c, values) == [format_bits(c, int(v)) for v in values]
+        assert format_bits_many(c, np.array([], dtype=np.int64)) == []
