@@ -639,12 +639,10 @@ struct OpRec {
 };
 
 // One register block over the whole tile: each thread takes groups of 2^U elements (the block's
-// U register bits), reads them, applies the block's operators in registers and writes them back.
-// PLAIN: a gate program (records, no predicates or mixtures); otherwise a trajectory program.
-template <typename T, int U, bool PLAIN>
-__device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp* __restrict__ ops,
-                          const OpRec* __restrict__ recs, const T* __restrict__ data, int64_t member, uint64_t pred,
-                          const TrajCtx& ctx, int64_t cur) {
+// U register bits), reads them, applies the block's operators (records resolved for the tile's
+// member) in registers and writes them back.
+template <typename T, int U>
+__device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const OpRec* __restrict__ recs) {
     // element e of a group sits at base | off[e]: the block's bits of e deposited at its tile bits
     uint32_t off[1 << U];
 #pragma unroll
@@ -662,24 +660,9 @@ __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const TileOp
         for (int i = 0; i <= U; ++i) base |= ((uint32_t)g << i) & blk.dep[i];
         T v[1 << U];
         load_group<T, U>(tile, base, off, blk.vec, v);
-        if constexpr (PLAIN) {
-            for (int o = 0; o < blk.nops; ++o) {
-                const OpRec r = recs[blk.first + o];
-                rb_apply<T, U>(v, r.code, static_cast<const T*>(r.m));
-            }
-        } else {
-            for (int o = 0; o < blk.nops; ++o) {
-                const TileOp& op = ops[blk.first + o];
-                if (!((pred >> op.pred) & 1)) continue;
-                const T* m = data + op.data + member * op.stride;
-                int code = op.tmpl;
-                if (op.kind == kOpMixture) {
-                    m = mixture_pick<T>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
-                    if (!m) continue;
-                    code = (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2));
-                }
-                rb_apply<T, U>(v, code, m);
-            }
+        for (int o = 0; o < blk.nops; ++o) {
+            const OpRec r = recs[blk.first + o];
+            rb_apply<T, U>(v, r.code, static_cast<const T*>(r.m));
         }
         store_group<T, U>(tile, base, off, blk.vec, v);
     }
@@ -728,9 +711,23 @@ __device__ __forceinline__ void compute_tile(T* tile, int K, const PassDesc& pd,
     const bool plain = ctx.u == nullptr;
     const uint64_t pred = plain ? ~0ull : ctx.pred[member];
     const int64_t cur = plain ? 0 : ctx.cursor[member];
-    if (plain)  // this tile's member: resolve every operator's data pointer once
-        for (int o = threadIdx.x; o < pd.nops; o += kCompute)
-            recs[o] = OpRec{sops[o].tmpl, 0, data + sops[o].data + member * sops[o].stride};
+    // this tile's member: resolve every operator once — its data pointer and, in a trajectory
+    // pass, its predicate (an untaken branch gets code -1: no operation) and its mixture branch
+    // (drawn from the member's uniform; the identity branch is skipped like an untaken one)
+    for (int o = threadIdx.x; o < pd.nops; o += kCompute) {
+        const TileOp& op = sops[o];
+        int code = op.tmpl;
+        const T* m = data + op.data + member * op.stride;
+        if (!plain) {
+            if (!((pred >> op.pred) & 1)) {
+                code = -1;
+            } else if (op.kind == kOpMixture) {
+                m = mixture_pick<T>(op, m, ctx.u[member * ctx.ustride + cur + op.draw]);
+                code = m ? (op.k == 1 ? kT_DENSE1 : kT_DENSE2) + (code - (op.k == 1 ? kT_MIX1 : kT_MIX2)) : -1;
+            }
+        }
+        recs[o] = OpRec{code, 0, m};
+    }
     for (int bi = 0; bi < pd.nblocks; ++bi) {
         const BlockDesc& blk = sblk[bi];
         cbar();
@@ -738,9 +735,7 @@ __device__ __forceinline__ void compute_tile(T* tile, int K, const PassDesc& pd,
             run_ops<T>(tile, K, sops + blk.first, blk.nops, data, member, ctx);
             continue;
         }
-#define LSG_RUN(UU)                                                                                   \
-    if (plain) run_block<T, UU, true>(tile, K, blk, sops, recs, data, member, pred, ctx, cur);      \
-    else run_block<T, UU, false>(tile, K, blk, sops, recs, data, member, pred, ctx, cur);
+#define LSG_RUN(UU) run_block<T, UU>(tile, K, blk, recs);
         switch (blk.u) {
             case 1: LSG_RUN(1) break;
             case 2: LSG_RUN(2) break;
