@@ -101,6 +101,11 @@ int lsg_state_bytes(lsg_state s, int64_t* out);
  * static loop of _evolve (src/lucivant_sim/simulator.py:229-251). `pool` holds complex128 data as
  * (re, im) pairs; complex64 registers round it once. */
 int lsg_apply(lsg_state s, const lsg_op* ops, int32_t nops, const double* pool, int64_t pool_entries);
+/* lsg_state_set_basis(s, index) then lsg_apply, in one call that skips tiles the operators have not
+ * reached yet (still zero; see lsg_program_run_from_basis): the evolution from |index> of
+ * Statevector(n) / DensityMatrix(n) (engines.py:139-148, :216-225). */
+int lsg_apply_from_basis(lsg_state s, int64_t index, const lsg_op* ops, int32_t nops, const double* pool,
+                         int64_t pool_entries);
 
 /* ---- programs: planned, uploaded operator lists ---------------------------------------------
  * lsg_program_create plans and uploads `ops` once for registers shaped like `shape` (same bits,

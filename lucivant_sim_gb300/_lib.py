@@ -71,6 +71,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_program_run_timed": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     "lsg_program_info": (C.c_int, [_P, _PI32, _PI64]),
     "lsg_program_specialized": (C.c_int, [_P]),
+    "lsg_apply_from_basis": (C.c_int, [_P, _I64, _P, _I32, _PD, _I64]),
     "lsg_program_run_from_basis": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_float)]),
     "lsg_program_basis_info": (C.c_int, [_P, _PI64, _PI64]),
     "lsg_program_free": (C.c_int, [_P]),
@@ -244,6 +245,13 @@ class Register:
             return
         table, pool = ops.packed()
         check(self.lib.lsg_apply(self.handle, table.ctypes.data, len(table), ptr(pool, C.c_double), pool.size // 2))
+
+    def apply_from_basis(self, ops: OpList, index: int = 0) -> None:
+        """Every member set to basis state ``index``, then ``ops`` applied, skipping tiles the
+        operators have not reached yet (the same result as ``set_basis`` + ``apply``)."""
+        table, pool = ops.packed()
+        check(self.lib.lsg_apply_from_basis(self.handle, index, table.ctypes.data, len(table), ptr(pool, C.c_double),
+                                            pool.size // 2))  # fmt: skip
 
     @property
     def real(self) -> bool:

@@ -969,6 +969,26 @@ int apply_ops(lsg_state_s* s, const lsg_op* ops, int32_t nops, const double* poo
     return check_device_status(s->stream);
 }
 
+// Set every member to basis state `index` and apply `ops` from it, skipping tiles that are still
+// zero (program_run_basis); the result equals set_basis + apply_ops.
+int apply_ops_basis(lsg_state_s* s, int64_t index, const lsg_op* ops, int32_t nops, const double* pool,
+                    int64_t pool_entries) {
+    if (nops == 0) {
+        LSG_CHECK(validate_ops(s->nbits, s->precision, s->batch, ops, nops, pool, pool_entries));
+        LSG_CHECK(set_basis_async(s, index));
+        LSG_CUDA(cudaStreamSynchronize(s->stream));
+        return LSG_OK;
+    }
+    lsg_program_s* p = nullptr;
+    LSG_CHECK(program_create(s->nbits, s->precision, s->batch, ops, nops, pool, pool_entries, &p, s->stream));
+    int rc = program_run_basis(p, s, index, nullptr);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    program_destroy(p);
+    LSG_CHECK(rc);
+    if (e != cudaSuccess) return fail(LSG_E_CUDA, "the passes failed: %s", cudaGetErrorString(e));
+    return check_device_status(s->stream);
+}
+
 // ------------------------------------------------------------------------ register kernels
 
 // After a zero fill: member m's element `index` of a complex register set to 1.
@@ -1182,6 +1202,13 @@ int lsg_apply(lsg_state s, const lsg_op* ops, int32_t nops, const double* pool, 
     clear_error();
     if (!s) return fail(LSG_E_ARG, "null register");
     return apply_ops(s, ops, nops, pool, pool_entries);
+}
+
+int lsg_apply_from_basis(lsg_state s, int64_t index, const lsg_op* ops, int32_t nops, const double* pool,
+                         int64_t pool_entries) {
+    clear_error();
+    if (!s) return fail(LSG_E_ARG, "null register");
+    return apply_ops_basis(s, index, ops, nops, pool, pool_entries);
 }
 
 

@@ -538,10 +538,10 @@ def evolve_density(circuit: Any, noises: list[Any], precision: int) -> _lib.Regi
     n = circuit.num_qubits
     if dm_form(circuit, noises) == "ptm":
         reg = new_density(n, REAL_OF[precision], len(noises))
-        reg.apply(ptm_oplist(circuit, noises))
+        reg.apply_from_basis(ptm_oplist(circuit, noises))
     else:
         reg = new_density(n, precision, len(noises))
-        reg.apply(dm_oplist(circuit, noises))
+        reg.apply_from_basis(dm_oplist(circuit, noises))
     return reg
 
 

@@ -134,11 +134,9 @@ def execute(prep: dict, precision: int, pool: _RegisterPool | None = None) -> di
         precision = engine.REAL_OF[precision]
     reg = pool.take(nbits, precision, batch) if pool else _lib.Register(nbits, precision, batch)
     try:
-        reg.set_basis(0)
-        table, flat = prep["ops"]
-        if len(table):
-            _lib.check(reg.lib.lsg_apply(reg.handle, table.ctypes.data, len(table),
-                                         _lib.ptr(flat, _lib.C.c_double), flat.size // 2))  # fmt: skip
+        table, flat = prep["ops"]  # |0...0> then the operators (tiles not reached yet are skipped)
+        _lib.check(reg.lib.lsg_apply_from_basis(reg.handle, 0, table.ctypes.data, len(table),
+                                                _lib.ptr(flat, _lib.C.c_double), flat.size // 2))  # fmt: skip
         if prep["kind"] == "expect":
             vals = reg.expect(0, prep["xmask"], prep["zmask"])  # (terms, batch)
             w = np.asarray(prep["weights"])

@@ -216,7 +216,7 @@ def _evolved(circuit: Any, noise: Any, precision: int) -> tuple[_lib.Register, i
     if noise is not None and noise.has_gate_errors():
         return engine.evolve_density(circuit, [noise], precision), n
     reg = engine.new_statevector(n, precision)
-    reg.apply(engine.sv_oplist(circuit, fuse=True))
+    reg.apply_from_basis(engine.sv_oplist(circuit, fuse=True))
     return reg, 0
 
 
@@ -264,7 +264,7 @@ def run(
         n = circuit.num_qubits
         if chosen == "statevector":
             reg = engine.new_statevector(n, prec)
-            reg.apply(engine.sv_oplist(circuit, fuse=True))
+            reg.apply_from_basis(engine.sv_oplist(circuit, fuse=True))
             dm = 0
         else:
             reg = engine.evolve_density(circuit, [noise], prec)
@@ -300,7 +300,7 @@ def statevector(program: Any, params: Mapping[str, float] | None = None, *, prec
     circuit = to_circuit(program, params)
     _static(circuit, "a statevector")
     with engine.new_statevector(circuit.num_qubits, engine.precision_code(precision)) as reg:
-        reg.apply(engine.sv_oplist(circuit, fuse=True))
+        reg.apply_from_basis(engine.sv_oplist(circuit, fuse=True))
         return reg.download()[0]
 
 

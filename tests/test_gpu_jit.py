@@ -106,3 +106,18 @@ def test_program_outlives_its_register(monkeypatch):
         prog.run(c)
         assert np.array_equal(b.download(), c.download())
     prog.free()
+
+
+@pytest.mark.parametrize("precision", [_lib.C128, _lib.C64])
+def test_apply_from_basis_equals_set_basis_and_apply(precision):
+    """The one-call evolution from a basis state (lsg_apply_from_basis) gives exactly the state of
+    set_basis + lsg_apply, for a statevector and a complex vectorised density matrix."""
+    sv_ops = engine.sv_oplist(parse(wl.brickwork(15, 3, seed=8, measure=False)))
+    c = parse(wl.brickwork(6, 2, seed=8, measure=False))
+    dm_ops = engine.dm_oplist(c, [wl.dm_noise()])
+    for nbits, ops, index in ((15, sv_ops, 0), (15, sv_ops, 12345), (12, dm_ops, 0)):
+        with _lib.Register(nbits, precision) as a, _lib.Register(nbits, precision) as b:
+            a.set_basis(index)
+            a.apply(ops)
+            b.apply_from_basis(ops, index)
+            assert np.array_equal(a.download(), b.download())
