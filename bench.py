@@ -322,7 +322,10 @@ def config_block(args: argparse.Namespace) -> dict:
         "noise": "thermal_relaxation(120, 90, 0.05) composed with depolarising U[1e-4,5e-3] on u3; "
         "depolarising U[1e-3,3e-2] on cx; readout 2e-2",
         "outputs": "probabilities (2^12) and 23 Z observables per instance",
-        "l2": f"register {((8 if args.precision == 'c64' else 16) * args.instances << 24) / 2**30:.0f} GiB > L2: no flush",
+        # the workload's gates act on at most two qubits: the Pauli-transfer form, real32 for a
+        # complex64 request (real64 for complex128)
+        "form": "ptm",
+        "l2": f"register {((4 if args.precision == 'c64' else 8) * args.instances << 24) / 2**30:.0f} GiB > L2: no flush",
         "parallelism": f"replicas x{args.gpus} (independent instances per GPU)",
     }
 
@@ -462,7 +465,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "vs_baseline": None,
             "dtype": ("f32" if args.precision == "c64" else "f64") if real else args.precision,
             "data": "synthetic",
-            "config": dict(config_block(args), form=form, l2=f"register {reg_bytes / 2**30:.0f} GiB > L2: no flush"),
+            "config": dict(config_block(args), form=form),
             "circuits_per_s": cps,
             "fused_passes": passes,
             "specialized_passes": specialized,
