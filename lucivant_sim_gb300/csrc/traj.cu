@@ -275,6 +275,176 @@ __global__ void k_t_collapse(Cx<R>* __restrict__ state, int64_t elems, int q, co
     }
 }
 
+// ---- consecutive measurements of distinct qubits in one group (batched mode)
+//
+// Measurements with nothing between them draw their outcomes from one joint distribution: one
+// pass sums |a|^2 per member into the 2^g bins of the group's bits, the decisions then run in
+// program order from the bins (each outcome's probability conditioned on the earlier ones, as the
+// collapsed and renormalised state would give it), and one pass moves the kept slice to its final
+// pattern (a reset's bit to 0) scaled to norm 1 and zeroes the rest: two passes instead of a
+// reduction and a collapse per measurement.
+constexpr int kGroupMax = 4;
+
+struct Group {
+    int g = 0;
+    int q[kGroupMax] = {};  // register bit of measurement i (group bit i)
+    int clbit[kGroupMax] = {}, readout[kGroupMax] = {}, is_reset[kGroupMax] = {};
+    double p01[kGroupMax] = {}, p10[kGroupMax] = {};
+};
+
+// the group's 2^g elements around `base` (group bits 0): element k has group bit i = bit i of k
+__device__ __forceinline__ uint64_t group_elem(uint64_t base, const Group& gr, int k) {
+    for (int i = 0; i < gr.g; ++i) base |= (uint64_t)((k >> i) & 1) << gr.q[i];
+    return base;
+}
+
+// Lanes map to (group, pattern): 2^g consecutive lanes hold the 2^g elements of one group (the
+// elements that differ only in the group's bits), each lane always the same pattern, so the
+// accesses of a warp are contiguous when the group's bits are the lowest ones.
+__device__ __forceinline__ void sort_bits(const Group& gr, int* sorted) {
+    for (int i = 0; i < gr.g; ++i) sorted[i] = gr.q[i];
+    for (int i = 1; i < gr.g; ++i)  // insertion sort: spread() wants ascending positions
+        for (int j = i; j > 0 && sorted[j - 1] > sorted[j]; --j) {
+            const int x = sorted[j];
+            sorted[j] = sorted[j - 1];
+            sorted[j - 1] = x;
+        }
+}
+
+constexpr int kGroupUnroll = 4;  // groups per lane per iteration: independent loads in flight
+
+// per-member partial sums of |a|^2 per group pattern: partials[(b * gridDim.x + block) * 16 + k]
+template <typename R>
+__global__ void k_t_hist(const Cx<R>* __restrict__ state, int64_t elems, Group gr, const uint64_t* pred, int slot,
+                         double* __restrict__ partials) {
+    __shared__ double buf[kT];
+    const int64_t b = blockIdx.y;
+    const int k = threadIdx.x & ((1 << gr.g) - 1);
+    double acc = 0.0;
+    if (has(pred, b, slot)) {
+        const Cx<R>* s = state + b * elems;
+        int sorted[kGroupMax];
+        sort_bits(gr, sorted);
+        const int64_t groups = elems >> gr.g, per_block = blockDim.x >> gr.g, step = (int64_t)gridDim.x * per_block;
+        for (int64_t r0 = blockIdx.x * per_block + (threadIdx.x >> gr.g); r0 < groups; r0 += step * kGroupUnroll) {
+            Cx<R> a[kGroupUnroll];
+#pragma unroll
+            for (int j = 0; j < kGroupUnroll; ++j) {
+                const int64_t r = r0 + j * step;
+                a[j] = r < groups ? s[group_elem(spread((uint64_t)r, sorted, gr.g), gr, k)] : Cx<R>(R(0), R(0));
+            }
+#pragma unroll
+            for (int j = 0; j < kGroupUnroll; ++j) acc += nrm2(a[j]);
+        }
+    }
+    buf[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < (1 << gr.g)) {  // lanes of one pattern: every 2^g-th entry
+        double tot = 0.0;
+        for (int t = threadIdx.x; t < (int)blockDim.x; t += 1 << gr.g) tot += buf[t];
+        partials[(b * gridDim.x + blockIdx.x) * (1 << kGroupMax) + threadIdx.x] = tot;
+    }
+}
+
+// one thread per member: the group's outcomes in program order from the joint bins, each with its
+// readout flip and classical bit as k_t_decide records them; outcome[b] = drawn pattern | final
+// pattern << 8 (-1: not taken), prob[b] = the scale that renormalises the kept slice
+__global__ void k_t_decide_group(const double* __restrict__ partials, int nparts, int64_t* cursor,
+                                 const double* __restrict__ u, int64_t ustride, const uint64_t* pred, int slot, Group gr,
+                                 uint64_t* clbits, int words, int* outcome, double* prob, unsigned long long* near,
+                                 int64_t batch) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+        if (!has(pred, b, slot)) {
+            outcome[b] = -1;
+            continue;
+        }
+        double bins[1 << kGroupMax];
+        double total = 0.0;
+        for (int k = 0; k < (1 << gr.g); ++k) {
+            double v = 0.0;
+            for (int p = 0; p < nparts; ++p) v += partials[((int64_t)b * nparts + p) * (1 << kGroupMax) + k];
+            bins[k] = v;
+            total += v;
+        }
+        int known = 0, val = 0, fin = 0;
+        for (int i = 0; i < gr.g; ++i) {
+            double num = 0.0, den = 0.0;
+            for (int k = 0; k < (1 << gr.g); ++k) {
+                if ((k & known) != val) continue;
+                den += bins[k];
+                if ((k >> i) & 1) num += bins[k];
+            }
+            const double p1 = den > 0.0 ? fmin(fmax(num / den, 0.0), 1.0) : 0.0;
+            const double r = u[b * ustride + cursor[b]];
+            cursor[b] += 1;
+            if (fabs(r - p1) < kNear) atomicAdd(near, 1ull);
+            const int out = r < p1 ? 1 : 0;
+            known |= 1 << i;
+            val |= out << i;
+            if (gr.is_reset[i]) continue;  // a reset ends with its bit at 0
+            fin |= out << i;
+            int seen = out;
+            if (gr.readout[i]) {
+                const double r2 = u[b * ustride + cursor[b]];
+                cursor[b] += 1;
+                if (r2 < (out ? gr.p10[i] : gr.p01[i])) seen ^= 1;
+            }
+            if (gr.clbit[i] >= 0) {
+                uint64_t& w = clbits[b * words + (gr.clbit[i] >> 6)];
+                const uint64_t bit = 1ull << (gr.clbit[i] & 63);
+                w = seen ? (w | bit) : (w & ~bit);
+            }
+        }
+        outcome[b] = val | (fin << 8);
+        prob[b] = bins[val] > 0.0 ? sqrt(total / bins[val]) : 1.0;
+    }
+}
+
+// the group's collapse: in every group of 2^g elements the element with the final pattern takes
+// the drawn pattern's amplitude times the scale and every other element becomes 0. Every lane of
+// a group reads the drawn pattern's element (one address for the 2^g lanes), the warp
+// synchronises, then every lane writes its own element: all lanes run the same iterations (work
+// past the last group is predicated off), so the full-warp barrier is well defined.
+template <typename R>
+__global__ void k_t_collapse_group(Cx<R>* __restrict__ state, int64_t elems, Group gr, const int* outcome,
+                                   const double* prob) {
+    const int64_t b = blockIdx.y;
+    const int oc = outcome[b];
+    if (oc < 0) return;  // the whole block leaves: the member is not in this branch
+    const int val = oc & 0xff, fin = oc >> 8;
+    const double sc = prob[b];
+    const R s1 = (R)sc;
+    Cx<R>* s = state + b * elems;
+    int sorted[kGroupMax];
+    sort_bits(gr, sorted);
+    const int k = threadIdx.x & ((1 << gr.g) - 1);
+    const int64_t groups = elems >> gr.g, per_block = blockDim.x >> gr.g, step = (int64_t)gridDim.x * per_block;
+    const int64_t first = blockIdx.x * per_block + (threadIdx.x >> gr.g);
+    const int64_t iters = (groups + step * kGroupUnroll - 1) / (step * kGroupUnroll);  // the same for every lane
+    for (int64_t it = 0; it < iters; ++it) {
+        Cx<R> a[kGroupUnroll];
+        uint64_t base[kGroupUnroll];
+#pragma unroll
+        for (int j = 0; j < kGroupUnroll; ++j) {
+            const int64_t r = first + (it * kGroupUnroll + j) * step;
+            base[j] = r < groups ? spread((uint64_t)r, sorted, gr.g) : ~0ull;
+            a[j] = base[j] != ~0ull ? s[group_elem(base[j], gr, val)] : Cx<R>(R(0), R(0));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < kGroupUnroll; ++j) {
+            if (base[j] == ~0ull) continue;
+            Cx<R> out(R(0), R(0));
+            if (k == fin) {
+                if constexpr (sizeof(R) == 8) out = Cx<R>(a[j].re * sc, a[j].im * sc);
+                else out = Cx<R>(a[j].re * s1, a[j].im * s1);
+            }
+            s[group_elem(base[j], gr, k)] = out;
+        }
+        __syncwarp();  // the next iteration's reads come after this one's writes in every lane
+    }
+}
+
 // per-member reduced density matrix of the channel's bits (k <= 2): rho[r][c] summed over the
 // other bits, as 2*d*d doubles per block
 template <typename R>
@@ -493,6 +663,19 @@ int ctl_setup(lsg_traj_s* t, int64_t batch, Ctl* c) {
     return LSG_OK;
 }
 
+// How many measurements from step `si` on form one group: consecutive, under the same predicate,
+// of distinct qubits, at most kGroupMax.
+int group_length(const std::vector<Step>& steps, size_t si) {
+    int n = 0;
+    uint64_t seen = 0;
+    for (size_t j = si; j < steps.size() && n < kGroupMax; ++j, ++n) {
+        const Step& m = steps[j];
+        if (m.kind != STEP_MEASURE || m.slot != steps[si].slot || ((seen >> m.q) & 1)) break;
+        seen |= 1ull << m.q;
+    }
+    return std::max(n, 1);
+}
+
 template <typename R>
 int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int64_t ustride) {
     const int64_t B = s->batch;
@@ -517,6 +700,26 @@ int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int6
                 break;
             case STEP_MEASURE: {
                 double* part = (double*)t->parts.ptr;
+                const int glen = B > 1 ? group_length(t->steps, si) : 1;
+                if (glen > 1) {  // this measurement and the next glen-1 as one group
+                    Group gr;
+                    gr.g = glen;
+                    for (int i = 0; i < glen; ++i) {
+                        const Step& m = t->steps[si + i];
+                        gr.q[i] = m.q;
+                        gr.clbit[i] = m.is_reset ? -1 : m.clbit;
+                        gr.readout[i] = m.is_reset ? 0 : m.readout;
+                        gr.is_reset[i] = m.is_reset;
+                        gr.p01[i] = m.p01;
+                        gr.p10[i] = m.p10;
+                    }
+                    k_t_hist<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, gr, c.pred, sp.slot, part);
+                    k_t_decide_group<<<t_grid(B), kT, 0, st>>>(part, (int)gx, c.cursor, u, ustride, c.pred, sp.slot, gr,
+                                                              c.clbits, t->words, c.outcome, c.prob, c.near, B);
+                    k_t_collapse_group<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, gr, c.outcome, c.prob);
+                    si += glen - 1;
+                    break;
+                }
                 if (!p1_ready)
                     k_t_p1<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.pred, sp.slot, part);
                 k_t_decide<<<t_grid(B), kT, 0, st>>>(part, (int)gx, c.cursor, u, ustride, c.pred, sp.slot, sp.clbit,
@@ -524,7 +727,7 @@ int run_steps(lsg_traj_s* t, lsg_state_s* s, const Ctl& c, const double* u, int6
                                                     c.outcome, c.prob, c.near, B);
                 // a measurement right after this one: its p(1) partials come out of this collapse
                 const Step* nx = si + 1 < t->steps.size() ? &t->steps[si + 1] : nullptr;
-                const bool fuse = nx && nx->kind == STEP_MEASURE;
+                const bool fuse = nx && nx->kind == STEP_MEASURE && (B == 1 || group_length(t->steps, si + 1) == 1);
                 k_t_collapse<R><<<dim3(gx, (unsigned)B), kT, 0, st>>>(state, elems, sp.q, c.outcome, c.prob, sp.is_reset,
                                                                     fuse ? nx->q : -1, c.pred, fuse ? nx->slot : 0, part);
                 next_p1_ready = fuse;
