@@ -326,12 +326,15 @@ __global__ void k_t_hist(const Cx<R>* __restrict__ state, int64_t elems, Group g
         int sorted[kGroupMax];
         sort_bits(gr, sorted);
         const int64_t groups = elems >> gr.g, per_block = blockDim.x >> gr.g, step = (int64_t)gridDim.x * per_block;
+        const uint64_t own = group_elem(0, gr, k);  // this lane's pattern, deposited at the group's bits
+        const bool low = sorted[gr.g - 1] == gr.g - 1;  // the group's bits are the lowest: base = r << g
         for (int64_t r0 = blockIdx.x * per_block + (threadIdx.x >> gr.g); r0 < groups; r0 += step * kGroupUnroll) {
             Cx<R> a[kGroupUnroll];
 #pragma unroll
             for (int j = 0; j < kGroupUnroll; ++j) {
                 const int64_t r = r0 + j * step;
-                a[j] = r < groups ? s[group_elem(spread((uint64_t)r, sorted, gr.g), gr, k)] : Cx<R>(R(0), R(0));
+                const uint64_t base = low ? (uint64_t)r << gr.g : spread((uint64_t)r, sorted, gr.g);
+                a[j] = r < groups ? s[base | own] : Cx<R>(R(0), R(0));
             }
 #pragma unroll
             for (int j = 0; j < kGroupUnroll; ++j) acc += nrm2(a[j]);
@@ -421,14 +424,16 @@ __global__ void k_t_collapse_group(Cx<R>* __restrict__ state, int64_t elems, Gro
     const int64_t groups = elems >> gr.g, per_block = blockDim.x >> gr.g, step = (int64_t)gridDim.x * per_block;
     const int64_t first = blockIdx.x * per_block + (threadIdx.x >> gr.g);
     const int64_t iters = (groups + step * kGroupUnroll - 1) / (step * kGroupUnroll);  // the same for every lane
+    const uint64_t own = group_elem(0, gr, k), src = group_elem(0, gr, val);  // at the group's bits
+    const bool low = sorted[gr.g - 1] == gr.g - 1;  // the group's bits are the lowest: base = r << g
     for (int64_t it = 0; it < iters; ++it) {
         Cx<R> a[kGroupUnroll];
         uint64_t base[kGroupUnroll];
 #pragma unroll
         for (int j = 0; j < kGroupUnroll; ++j) {
             const int64_t r = first + (it * kGroupUnroll + j) * step;
-            base[j] = r < groups ? spread((uint64_t)r, sorted, gr.g) : ~0ull;
-            a[j] = base[j] != ~0ull ? s[group_elem(base[j], gr, val)] : Cx<R>(R(0), R(0));
+            base[j] = r < groups ? (low ? (uint64_t)r << gr.g : spread((uint64_t)r, sorted, gr.g)) : ~0ull;
+            a[j] = base[j] != ~0ull ? s[base[j] | src] : Cx<R>(R(0), R(0));
         }
         __syncwarp();
 #pragma unroll
@@ -439,7 +444,7 @@ __global__ void k_t_collapse_group(Cx<R>* __restrict__ state, int64_t elems, Gro
                 if constexpr (sizeof(R) == 8) out = Cx<R>(a[j].re * sc, a[j].im * sc);
                 else out = Cx<R>(a[j].re * s1, a[j].im * s1);
             }
-            s[group_elem(base[j], gr, k)] = out;
+            s[base[j] | own] = out;
         }
         __syncwarp();  // the next iteration's reads come after this one's writes in every lane
     }
