@@ -319,3 +319,19 @@ def test_format_bits_many_matches_format_bits():
         values = np.unique(rng.integers(0, 1 << c.num_clbits, size=40))
         assert format_bits_many(c, values) == [format_bits(c, int(v)) for v in values]
         assert format_bits_many(c, np.array([], dtype=np.int64)) == []
+
+
+def test_pauli_transfer_oplist_batched_members():
+    """A batched Pauli-transfer operator list (one channel stack per gate signature, equal gates
+    classified once) gives every member its own noise model's density matrix."""
+    c = ls.parse(wl.brickwork(3, 3, seed=4, measure=False))
+    noises = wl.dm_noise_instances(3, seed=9)
+    ops = engine.ptm_oplist(c, noises)
+    assert any(row[4] for row in ops.rows)  # per-member data present
+    n = c.num_qubits
+    for m, nm in enumerate(noises):
+        r = np.zeros(1 << (2 * n))
+        r[: 1 << n] = 1.0  # |0..0><0..0|: every diagonal Pauli has coefficient 1
+        r = run_oplist(ops, 2 * n, r, member=m).real
+        got = run_oplist(engine.ptm_to_density_ops(n), 2 * n, r)
+        assert np.max(np.abs(got - dense.evolve_dm(c, nm).reshape(-1))) < 1e-12, m
