@@ -323,12 +323,25 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
     const int max_ops = ops_env ? std::max(1, std::min(kMaxPassOps, atoi(ops_env))) : kMaxPassOps;
     // One pass by the greedy sweep from a starting tile: an operator joins when its bits fit and no
     // operator deferred earlier in the sweep shares a bit with it (program order where it matters).
-    auto sweep = [&](uint64_t start, uint64_t* tile_out, std::vector<int>* taken, std::vector<int>* deferred) {
+    std::vector<uint64_t> masks(nops);
+    bool scalar_ops = false;  // operators on no bits (global phases) join any sweep at any point
+    for (int i = 0; i < nops; ++i) {
+        masks[i] = op_mask(i);
+        scalar_ops = scalar_ops || masks[i] == 0;
+    }
+    const uint64_t all = nbits >= 64 ? ~0ull : ((1ull << nbits) - 1);
+    // A sweep stops early once every register bit is blocked: no later operator can join. The
+    // operators from `*stop` on are then deferred as they stand.
+    auto sweep = [&](uint64_t start, uint64_t* tile_out, std::vector<int>* taken, std::vector<int>* deferred,
+                     size_t* stop) {
         uint64_t tile = start, blocked = 0;
         taken->clear();
         deferred->clear();
-        for (int idx : remaining) {
-            const uint64_t mask = op_mask(idx);
+        size_t i = 0;
+        for (; i < remaining.size(); ++i) {
+            if (blocked == all && !scalar_ops) break;
+            const int idx = remaining[i];
+            const uint64_t mask = masks[idx];
             if ((mask & blocked) || (int)taken->size() >= max_ops) {
                 deferred->push_back(idx);
                 blocked |= mask;
@@ -343,28 +356,33 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
                 blocked |= mask;
             }
         }
+        *stop = i;
         *tile_out = tile;
     };
     const int seeds = plan_seeds();
     while (!remaining.empty()) {
         uint64_t tile = low;
         std::vector<int> taken, deferred;
-        sweep(low, &tile, &taken, &deferred);
+        size_t stop = 0;
+        sweep(low, &tile, &taken, &deferred, &stop);
         // Other starting tiles: the low bits plus the bits of one of the next operators, so the tile
         // can form around later work instead of the first operators' bits; the sweep that takes the
         // most operators wins (the first one on ties).
         std::vector<int> t2, d2;
         for (int j = 1; j < seeds && j < (int)remaining.size(); ++j) {
-            uint64_t start = low | op_mask(remaining[j]);
+            uint64_t start = low | masks[remaining[j]];
             if (__builtin_popcountll(start) > K) continue;
             uint64_t tile2;
-            sweep(start, &tile2, &t2, &d2);
+            size_t stop2 = 0;
+            sweep(start, &tile2, &t2, &d2, &stop2);
             if (t2.size() > taken.size()) {
                 tile = tile2;
                 taken.swap(t2);
                 deferred.swap(d2);
+                stop = stop2;
             }
         }
+        deferred.insert(deferred.end(), remaining.begin() + (std::ptrdiff_t)stop, remaining.end());
         if (taken.empty()) {  // an operator wider than the tile allows: no progress possible
             plan.passes.clear();
             plan.ops.clear();
