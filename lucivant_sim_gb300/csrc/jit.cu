@@ -14,6 +14,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -69,6 +70,7 @@ struct Driver {
                        void**, void**) = nullptr;
     CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
     CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+    CUresult (*module_unload)(CUmodule) = nullptr;
     CUresult (*encode)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
                        const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                        CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;  // optional
@@ -86,7 +88,8 @@ const Driver& driver() {
                get("cuModuleGetFunction", reinterpret_cast<void**>(&r.get_function)) &&
                get("cuLaunchKernel", reinterpret_cast<void**>(&r.launch)) &&
                get("cuFuncSetAttribute", reinterpret_cast<void**>(&r.set_attribute)) &&
-               get("cuOccupancyMaxActiveBlocksPerMultiprocessor", reinterpret_cast<void**>(&r.occupancy));
+               get("cuOccupancyMaxActiveBlocksPerMultiprocessor", reinterpret_cast<void**>(&r.occupancy)) &&
+               get("cuModuleUnload", reinterpret_cast<void**>(&r.module_unload));
         if (!get("cuTensorMapEncodeTiled", reinterpret_cast<void**>(&r.encode))) r.encode = nullptr;
         cudaGetLastError();
         return r;
@@ -364,8 +367,20 @@ std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_byt
 
 std::mutex g_mu;
 std::map<std::string, std::shared_ptr<JitPasses>> g_cache;
+std::vector<std::string> g_order;  // cache keys, oldest first
+// programs of that many shapes keep their modules cached (LSG_JIT_CACHE_MAX, default 64)
+size_t jit_cache_max() {
+    const char* env = getenv("LSG_JIT_CACHE_MAX");
+    return env ? (size_t)std::max(1, atoi(env)) : 64;
+}
+bool g_exiting = false;            // set at exit: the driver may be gone, modules are not unloaded
 
 }  // namespace
+
+JitPasses::~JitPasses() {
+    if (g_exiting || !driver().module_unload) return;
+    for (void* m : modules) driver().module_unload(static_cast<CUmodule>(m));
+}
 
 int jit_mode() {
     const char* env = getenv("LSG_JIT");
@@ -476,6 +491,8 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, 
     if (hit != g_cache.end()) return hit->second;
     const Nvrtc& rt = nvrtc();
     const Driver& drv = driver();
+    static const bool at_exit = [] { return std::atexit([] { g_exiting = true; }) == 0; }();
+    (void)at_exit;
     std::shared_ptr<JitPasses> out;
     if (rt.ok && drv.ok) {
         // passes are independent translation units: compile them in parallel, in chunks of
@@ -505,6 +522,7 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, 
         for (size_t c = 0; c < nchunks && ok; ++c) {
             CUmodule mod;
             ok = !cubins[c].empty() && drv.module_load(&mod, cubins[c].data()) == CUDA_SUCCESS;
+            if (ok) jp->modules.push_back(mod);
             for (size_t j = 0; j < members[c].size() && ok; ++j) {
                 const size_t i = members[c][j];
                 const std::string name = "lsg_pass_" + std::to_string(i);
@@ -519,6 +537,11 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, 
         if (ok) out = jp;
     }
     g_cache[key] = out;  // a failure is remembered too: the interpreter runs those programs
+    g_order.push_back(key);
+    if (g_order.size() > jit_cache_max()) {  // forget the oldest shape (its programs keep their modules)
+        g_cache.erase(g_order.front());
+        g_order.erase(g_order.begin());
+    }
     return out;
 }
 

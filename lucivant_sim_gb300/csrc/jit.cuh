@@ -14,10 +14,17 @@ namespace lsg {
 constexpr int kPipeThreadsHost = 288;
 
 // The compiled kernels of one program's passes (CUfunction handles, one per pass).
+// The modules are unloaded with the last reference (the cache's or a program's; a program is
+// destroyed only after its kernels finished).
 struct JitPasses {
-    std::vector<void*> fns;     // CUfunction per pass
-    std::vector<int> per_sm;    // resident CTAs per SM of each pass at its shared memory
-    bool swz = false;           // tiles move by swizzled tensor copies (common.cuh tma_load_box)
+    std::vector<void*> fns;      // CUfunction per pass
+    std::vector<int> per_sm;     // resident CTAs per SM of each pass at its shared memory
+    bool swz = false;            // tiles move by swizzled tensor copies (common.cuh tma_load_box)
+    std::vector<void*> modules;  // CUmodule per compiled unit
+    JitPasses() = default;
+    JitPasses(const JitPasses&) = delete;
+    JitPasses& operator=(const JitPasses&) = delete;
+    ~JitPasses();
 };
 
 // LSG_JIT: 0 never specialize, 1 always, unset: programs whose one run moves at least

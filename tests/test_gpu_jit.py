@@ -121,3 +121,25 @@ def test_apply_from_basis_equals_set_basis_and_apply(precision):
             a.apply(ops)
             b.apply_from_basis(ops, index)
             assert np.array_equal(a.download(), b.download())
+
+
+def test_module_cache_eviction(monkeypatch):
+    """With room for two cached shapes, a third specialized program evicts the oldest; a program
+    still alive keeps its own kernels, and programs of evicted shapes recompile correctly."""
+    monkeypatch.setenv("LSG_JIT_CACHE_MAX", "2")
+    monkeypatch.setenv("LSG_JIT", "1")
+    rng = np.random.default_rng(7)
+    start = rng.normal(size=(1, 1 << 10)) + 1j * rng.normal(size=(1, 1 << 10))
+    opsets = [engine.sv_oplist(parse(wl.brickwork(10, 2, seed=40 + i, measure=False))) for i in range(4)]
+    with _lib.Register(10, _lib.C64) as keep_reg:
+        keep = _lib.Program(keep_reg, opsets[0])  # alive across the evictions
+        assert keep.specialized
+        for ops in opsets[1:] + opsets[:1]:
+            _run(10, _lib.C64, 1, ops, start, True, monkeypatch)
+        keep_reg.upload(start)
+        keep.run(keep_reg)
+        keep.run(keep_reg)  # twice, as _run does
+        got = keep_reg.download()
+        keep.free()
+    want = _run(10, _lib.C64, 1, opsets[0], start, False, monkeypatch)
+    assert np.array_equal(got, want)
