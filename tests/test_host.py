@@ -335,3 +335,44 @@ def test_pauli_transfer_oplist_batched_members():
         r = run_oplist(ops, 2 * n, r, member=m).real
         got = run_oplist(engine.ptm_to_density_ops(n), 2 * n, r)
         assert np.max(np.abs(got - dense.evolve_dm(c, nm).reshape(-1))) < 1e-12, m
+
+
+def test_planner_and_specializer_on_random_operator_lists():
+    """Random operator lists (1-5 bit matrices, diagonals, permutations, global phases) on registers
+    of 3-22 bits plan without an internal error in every precision (the planner checks every block's
+    deposit masks and vector alignment), and the specializer writes their passes (or leaves a
+    program with wide operators to the interpreter) for one and many starting tiles."""
+    import os
+
+    rng = np.random.default_rng(12)
+    written = 0
+    for trial in range(60):
+        nbits = int(rng.choice([3, 8, 14, 20, 22]))
+        wide = trial % 4 == 0  # a quarter of the programs may hold wider operators
+        ops = _lib.OpList()
+        for _ in range(int(rng.integers(1, 120))):
+            kind = int(rng.choice([_lib.OP_MATRIX, _lib.OP_DIAG, _lib.OP_PERM, _lib.OP_MATRIX]))
+            # register blocks take 1- and 2-bit operators (and diagonals); 3-5 bit matrices and
+            # permutations run on the shared-memory path, which keeps a program interpreted
+            k = int(rng.choice([1, 1, 2, 2, 2])) if not wide or rng.random() > 0.05 else int(rng.integers(3, 6))
+            k = min(k, nbits)
+            bits = [int(b) for b in rng.choice(nbits, size=k, replace=False)]
+            d = 1 << k
+            if kind == _lib.OP_MATRIX:
+                ops.add(kind, bits, np.linalg.qr(rng.normal(size=(d, d)))[0].astype(complex))
+            elif kind == _lib.OP_DIAG:  # real data: the real (Pauli-transfer) precisions take it too
+                ops.add(kind, bits, rng.choice([-1.0, 0.5, 2.0], size=d).astype(complex))
+            else:
+                src = rng.permutation(d)
+                ops.add(kind, bits, np.concatenate([np.ones(d), src]).astype(complex))
+        for seeds in ("1", "64"):
+            os.environ["LSG_PLAN_SEEDS"] = seeds
+            try:
+                for prec in (_lib.C128, _lib.C64, _lib.R64, _lib.R32):
+                    assert _lib.plan_passes(nbits, prec, ops) >= 1
+                    src = _lib.specialized_source(nbits, prec, 2, ops)
+                    assert src == "" or "lsg_pass_0" in src
+                    written += bool(src)
+            finally:
+                os.environ.pop("LSG_PLAN_SEEDS", None)
+    assert written > 150  # the programs without operators wider than a register block
