@@ -143,3 +143,38 @@ def test_module_cache_eviction(monkeypatch):
         keep.free()
     want = _run(10, _lib.C64, 1, opsets[0], start, False, monkeypatch)
     assert np.array_equal(got, want)
+
+
+def _random_ops(rng, nbits, real):
+    """1- and 2-bit matrices, diagonals and permutations (some unit-phase: renames) on random bits."""
+    ops = _lib.OpList()
+    for _ in range(int(rng.integers(20, 90))):
+        kind = int(rng.choice([_lib.OP_MATRIX, _lib.OP_DIAG, _lib.OP_PERM, _lib.OP_MATRIX]))
+        k = int(rng.choice([1, 2, 2]))
+        bits = [int(b) for b in rng.choice(nbits, size=k, replace=False)]
+        d = 1 << k
+        if kind == _lib.OP_MATRIX:
+            m = np.linalg.qr(rng.normal(size=(d, d)) + (0 if real else 1j * rng.normal(size=(d, d))))[0]
+            ops.add(kind, bits, np.asarray(m, dtype=complex))
+        elif kind == _lib.OP_DIAG:
+            ops.add(kind, bits, (rng.choice([-1.0, 1.0], size=d) if real else np.exp(1j * rng.uniform(0, 6.3, size=d))).astype(complex))
+        else:
+            phases = np.ones(d) if rng.random() < 0.5 else rng.choice([-1.0, 1.0], size=d)
+            ops.add(kind, bits, np.concatenate([phases, rng.permutation(d)]).astype(complex))
+    return ops
+
+
+@pytest.mark.parametrize("precision", [_lib.C128, _lib.C64, _lib.R32])
+def test_random_programs(precision, monkeypatch):
+    """Random programs (random bit positions: renames that fold or not, strided blocks, pairs,
+    vector accesses) give the interpreter's register exactly when specialized."""
+    rng = np.random.default_rng(100 + precision)
+    real = precision in (_lib.R64, _lib.R32)
+    for nbits in (14, 16, 18):  # even: a Pauli-transfer register holds two bits per qubit
+        ops = _random_ops(rng, nbits, real)
+        start = rng.normal(size=(2, 1 << nbits))
+        if not real:
+            start = start + 1j * rng.normal(size=(2, 1 << nbits))
+        want = _run(nbits, precision, 2, ops, start, False, monkeypatch)
+        got = _run(nbits, precision, 2, ops, start, True, monkeypatch)
+        assert np.array_equal(got, want), f"{nbits} bits: max difference {np.max(np.abs(got - want))}"
