@@ -4,14 +4,18 @@
 Workload (one step): 256 noise instances of a 12-qubit, 12-layer u3+cx brickwork circuit (angles
 U[0, 2π) from seed 7), each with thermal relaxation (T1 = 120, T2 = 90, t = 0.05) composed with a
 depolarising one-qubit error ~ U[1e-4, 5e-3] on every u3, depolarising two-qubit error
-~ U[1e-3, 3e-2] on every cx, evolved as one 256-member register of vectorised density matrices
-(24-bit registers, 32 GiB in complex64), then the exact probabilities and the 23 observables
-<Z_i>, <Z_i Z_i+1> of every instance. Inputs are larger than L2 (no flush needed).
+~ U[1e-3, 3e-2] on every cx, evolved as one 256-member register of density matrices in the
+Pauli-transfer form (24-bit registers of real32 coefficients for the complex64 request, 16 GiB),
+from |0><0| through passes compiled for the circuit at run time, then the exact probabilities and
+the 23 observables <Z_i>, <Z_i Z_i+1> of every instance. Inputs are larger than L2 (no flush
+needed).
 
 metric: statevector HBM GB/s — algorithmic HBM bytes of the step (2 x register bytes per fused
-pass, one register write to reset, the reduction reads) per second, whole job. Beside it: the
-instances (circuits) per second, and the same circuit as a plain complex128 single-instance run on
-the same GPU ("plain_c128"), with the complex64 path's error against it.
+pass, one register write to reset, the reduction reads) per second, whole job; the passes skip
+tiles the circuit has not reached yet, and the roofline counts the bytes they move. Beside it:
+the instances (circuits) per second, the end-to-end rate through the public batched call, and the
+same circuit as a plain complex128 single-instance run on the same GPU ("plain_c128"), with the
+complex64 path's error against it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
