@@ -226,18 +226,17 @@ __device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
-// An encoded 2-D tensor map (a CUtensorMap, 128 bytes) for tensor copies, passed to kernels as a
-// __grid_constant__ parameter: the register as rows of 64 bytes, copied in boxes of a whole number
-// of 512-byte row groups with the 64-byte swizzle (16-byte unit u of row r lands at unit
-// u ^ (r & 3), repeating every 8 rows), which spreads strided register-block accesses over the
-// shared-memory banks.
+// An encoded tensor map (a CUtensorMap, 128 bytes) for tensor copies, passed to kernels as a
+// __grid_constant__ parameter. The register is seen as rows of 128 bytes copied with the 128-byte
+// swizzle (16-byte unit u of row r lands at unit u ^ (r & 7), repeating every 1 KB), which spreads
+// strided register-block accesses over the shared-memory banks. Every box is a whole number of
+// 1 KB swizzle atoms and lands on a 1 KB boundary: a run of rows (2-D map), or two 512-byte chunks
+// that differ in one register bit h (3-D map: rows of 128 bytes, blocks of 2^h elements).
 struct alignas(64) Tmap {
     unsigned long long w[16];
 };
 
-// One box (the map's box height in rows of 64 bytes, starting at row `row`) global -> shared,
-// swizzled, completing on `bar`. dst must be 512-byte aligned.
-__device__ __forceinline__ void tma_load_box(void* dst, const Tmap* map, int row, uint64_t* bar) {
+__device__ __forceinline__ void tma_load_2d(void* dst, const Tmap* map, int row, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
         "[%4];" ::"r"(smem_u32(dst)),
@@ -245,11 +244,26 @@ __device__ __forceinline__ void tma_load_box(void* dst, const Tmap* map, int row
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(void* dst, const Tmap* map, int row, int block, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(row), "r"(block), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // One box shared -> global (un-swizzled back), in the current bulk group.
-__device__ __forceinline__ void tma_store_box(const Tmap* map, int row, const void* src) {
+__device__ __forceinline__ void tma_store_2d(const Tmap* map, int row, const void* src) {
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
                      reinterpret_cast<uint64_t>(map)),
                  "r"(0), "r"(row), "r"(smem_u32(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_store_3d(const Tmap* map, int row, int block, const void* src) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(0), "r"(row), "r"(block), "r"(smem_u32(src))
                  : "memory");
 }
 

@@ -185,9 +185,9 @@ bool pure_renames(const Plan& plan, const PassDesc& pd, const BlockDesc& b, std:
     return true;
 }
 
-// The shared-memory layout of tiles moved by swizzled tensor copies (common.cuh tma_load_box):
-// element offset x is stored at S(x) = x ^ (((x >> row) & 3) << unit), the 64-byte swizzle in
-// elements (16-byte units `unit` bits up, 64-byte rows `row` bits up). S is linear over GF(2):
+// The shared-memory layout of tiles moved by swizzled tensor copies (common.cuh Tmap):
+// element offset x is stored at S(x) = x ^ (((x >> row) & 7) << unit), the 128-byte swizzle in
+// elements (16-byte units `unit` bits up, 128-byte rows `row` bits up). S is linear over GF(2):
 // S(a ^ b) = S(a) ^ S(b), so a group's runtime base and its constant offsets swizzle apart.
 struct Swizzle {
     bool on = false;
@@ -201,8 +201,8 @@ struct Swizzle {
         z.row = 7 - lg;
         return z;
     }
-    uint32_t apply(uint32_t x) const { return on ? x ^ (((x >> row) & 3u) << unit) : x; }
-    uint32_t may(uint32_t m) const { return on ? m | (((m >> row) & 3u) << unit) : m; }
+    uint32_t apply(uint32_t x) const { return on ? x ^ (((x >> row) & 7u) << unit) : x; }
+    uint32_t may(uint32_t m) const { return on ? m | (((m >> row) & 7u) << unit) : m; }
 };
 
 // One register block as generated: its access shape, and the renames folded into its loads
@@ -268,7 +268,7 @@ std::vector<std::string> mapped_addresses(std::ostringstream& o, const BlockGen&
         zero = r.apply(zero);
     }
     if (sw.on) {
-        o << "      " << var << " ^= ((" << var << " >> " << sw.row << ") & 3u) << " << sw.unit << ";\n";
+        o << "      " << var << " ^= ((" << var << " >> " << sw.row << ") & 7u) << " << sw.unit << ";\n";
         may = sw.may(may);
     }
     for (int e = 0; e < g.n; ++e) {
@@ -453,10 +453,13 @@ int jit_compile_check(const std::string& source) {
 bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_bytes) {
     const char* env = getenv("LSG_SWIZZLE");
     if (env && env[0] == '0') return false;
-    if (register_bytes <= 0 || register_bytes % 512 != 0 || (register_bytes >> 6) >= (1ll << 31)) return false;
+    if (register_bytes <= 0 || register_bytes % 1024 != 0 || (register_bytes >> 7) >= (1ll << 31)) return false;
     for (const PassDesc& pd : plan.passes) {
+        // chunks of 512 bytes move in pairs (1 KB boxes), larger ones in whole 1 KB swizzle atoms
         const size_t chunk = elem_bytes << pd.L;
-        if (chunk < 512 || chunk % 512 != 0) return false;
+        if (chunk < 512 || chunk % 512 != 0 || pd.K <= pd.L) return false;
+        if (chunk == 512 && ((elem_bytes << pd.hi[0]) % 1024 != 0 || (register_bytes / (elem_bytes << pd.hi[0])) >= (1ll << 31)))
+            return false;
     }
     return true;
 }
@@ -553,39 +556,44 @@ int jit_launch(const JitPasses& jp, const Plan& plan, void* state, int64_t membe
     LSG_CUDA(cudaGetDevice(&dev));
     LSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem = 2 * tile_bytes + (jp.swz ? 1024 : 0);
-    // the register as rows of 64 bytes, copied in swizzled boxes of min(chunk, 16 KB) (tile.cuh
-    // pipe_run); a map per box height (unused without swizzle)
+    // the register as rows of 128 bytes, copied in boxes with the 128-byte swizzle (tile.cuh
+    // pipe_run): 2-D boxes of min(chunk, 16 KB) for chunks of 1 KB and more, one map per box
+    // height; 3-D boxes pairing two 512-byte chunks that differ in register bit h = hi[0], one map
+    // per h (rows of 128 bytes, blocks of 2^h elements). Unused without swizzle.
     const uint64_t eb = (uint64_t)(tile_bytes >> plan.passes[0].K);
     const uint64_t bytes = (uint64_t)member_elems * (uint64_t)batch * eb;
     std::map<uint32_t, CUtensorMap> maps;
-    auto map_for = [&](uint32_t box_rows, CUtensorMap** out) -> int {
-        auto it = maps.find(box_rows);
+    auto map_for = [&](const PassDesc& pd, CUtensorMap** out) -> int {
+        const uint64_t chunk = eb << pd.L;
+        const bool pair = chunk == 512;
+        const uint32_t key = pair ? (0x80000000u | (uint32_t)pd.hi[0]) : (uint32_t)(std::min<uint64_t>(chunk, 16384) >> 7);
+        auto it = maps.find(key);
         if (it == maps.end()) {
             CUtensorMap m;
             std::memset(&m, 0, sizeof(m));
             if (jp.swz) {
                 if (!drv.encode) return fail(LSG_E_STATE, "cuTensorMapEncodeTiled is not available");
-                if (bytes % 512 != 0 || (bytes >> 6) >= (1ull << 31))
+                const uint64_t block = pair ? eb << pd.hi[0] : 0;
+                if (bytes % 1024 != 0 || (bytes >> 7) >= (1ull << 31) || (pair && (block % 1024 != 0 || bytes % block != 0)))
                     return fail(LSG_E_STATE, "a register of %llu bytes does not fit the swizzled tensor copies",
                                 (unsigned long long)bytes);
-                cuuint64_t dims[2] = {16, bytes >> 6};
-                cuuint64_t strides[1] = {64};
-                cuuint32_t box[2] = {16, box_rows};
-                cuuint32_t estr[2] = {1, 1};
-                if (drv.encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, state, dims, strides, box, estr,
-                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                cuuint64_t dims[3] = {32, pair ? block >> 7 : bytes >> 7, pair ? bytes / block : 1};
+                cuuint64_t strides[2] = {128, block};
+                cuuint32_t box[3] = {32, pair ? 4u : key, 2};
+                cuuint32_t estr[3] = {1, 1, 1};
+                if (drv.encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT32, pair ? 3 : 2, state, dims, strides, box, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
                     return fail(LSG_E_CUDA, "encoding the register's tensor map failed");
             }
-            it = maps.emplace(box_rows, m).first;
+            it = maps.emplace(key, m).first;
         }
         *out = &it->second;
         return LSG_OK;
     };
     for (size_t i = 0; i < plan.passes.size(); ++i) {
-        const uint64_t chunk = eb << plan.passes[i].L;
         CUtensorMap* map = nullptr;
-        LSG_CHECK(map_for((uint32_t)(std::min<uint64_t>(chunk, 16384) >> 6), &map));
+        LSG_CHECK(map_for(plan.passes[i], &map));
         CUfunction f = reinterpret_cast<CUfunction>(jp.fns[i]);
         const int64_t total = tiles_per_member[i] * batch;
         const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(jp.per_sm[i], 1)));

@@ -39,8 +39,9 @@ std::string jit_source(const Plan& plan, int precision, int ctas, bool swz);
 // Compile `source` with NVRTC only (no device needed): LSG_OK, or an error with NVRTC's log.
 int jit_compile_check(const std::string& source);
 
-// Whether a program's specialized passes can move tiles as swizzled 512-byte tensor boxes: every
-// pass's contiguous chunks are whole boxes and the register's 64-byte rows fit 31-bit coordinates.
+// Whether a program's specialized passes can move tiles as tensor boxes with the 128-byte swizzle:
+// every pass's contiguous chunks are 512 bytes (moved in pairs across register bit hi[0]) or whole
+// 1 KB swizzle atoms, and the register's 128-byte rows fit 31-bit coordinates.
 bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_bytes);
 
 // Specialize a planned gate program (no trajectory operators, no shared-memory operators), or

@@ -789,9 +789,10 @@ constexpr int pipe_ctas() {
 // host specializes at run time: `compute(tile, member)` runs on the 256 compute threads for every
 // tile of this CTA; the producer warp streams the tiles. `pd` is the pass (in shared memory),
 // buf0/buf1 the two tile buffers, full/empty the ring's mbarriers (initialised by the caller).
-// With Swz, the tile moves as 512-byte boxes of tensor copies through `tmap` with the 64-byte
-// swizzle (every chunk of the pass is a whole number of boxes; the compute side addresses the tile
-// through the same swizzle); otherwise as one plain bulk copy per chunk.
+// With Swz, the tile moves in boxes of tensor copies through `tmap` with the 128-byte swizzle (the
+// compute side addresses the tile through the same swizzle): a pass whose chunks are 512 bytes
+// pairs chunks 2q and 2q+1 (they differ in register bit hi[0]) in one 3-D box of 1 KB; larger
+// chunks move as 2-D boxes of min(chunk, 16 KB). Otherwise one plain bulk copy per chunk.
 template <typename T, bool Swz = false, typename F>
 __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_elems, const PassDesc& pd, T* buf0,
                                          T* buf1, uint64_t* full, uint64_t* empty, int64_t tiles_per_member,
@@ -800,11 +801,13 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
     const int nchunks = 1 << (K - L);
     const uint32_t chunk_bytes = (uint32_t)(sizeof(T) << L);
     const int64_t stride = gridDim.x;
-    // boxes of min(chunk, 16 KB): the pass's tensor map has that box height (host jit_launch)
-    const uint32_t box_bytes = chunk_bytes < 16384u ? chunk_bytes : 16384u;
+    // the pass's tensor map has this box shape (host jit_launch)
+    const bool pair = chunk_bytes == 512u;
+    const uint32_t box_bytes = pair ? 1024u : (chunk_bytes < 16384u ? chunk_bytes : 16384u);
     const int box_elems = (int)(box_bytes / sizeof(T));
-    const int box_shift = Swz ? (__ffs((int)(chunk_bytes / box_bytes)) - 1) : 0;  // boxes per chunk = 1 << box_shift
-    const int nboxes = nchunks << box_shift;
+    const int box_shift = (Swz && !pair) ? (__ffs((int)(chunk_bytes / box_bytes)) - 1) : 0;  // boxes per chunk
+    const int nboxes = pair ? nchunks / 2 : nchunks << box_shift;
+    const int h = pd.hi[0];  // the register bit between the two chunks of a pair
     if (threadIdx.x >= 256) {
         // ---------------- producer warp
         const int lane = threadIdx.x - 256;
@@ -814,19 +817,31 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
             *mem = state + member * member_elems;
             *base = deposit(tt, pd.outer, pd.nouter) | pd.fix;
         };
-        // the register row (64 bytes) where box q of the tile at `mem + base` starts
-        auto box_row = [&](const T* mem, uint64_t base, int q) {
-            const uint64_t c = (uint64_t)(q >> box_shift);
-            const uint64_t sub = (uint64_t)(q & ((1 << box_shift) - 1)) * (uint64_t)box_elems;
-            const uint64_t elem = (uint64_t)(mem - state) + (base | deposit(c, pd.hi, K - L)) + sub;
-            return (int)((elem * sizeof(T)) >> 6);
+        // the register element where box q of the tile at `mem + base` starts
+        auto box_elem = [&](const T* mem, uint64_t base, int q) {
+            const uint64_t c = pair ? 2 * (uint64_t)q : (uint64_t)(q >> box_shift);
+            const uint64_t sub = pair ? 0 : (uint64_t)(q & ((1 << box_shift) - 1)) * (uint64_t)box_elems;
+            return (uint64_t)(mem - state) + (base | deposit(c, pd.hi, K - L)) + sub;
+        };
+        // coordinates: 2-D (row of 128 bytes), 3-D (row within the 2^h-element block, block)
+        auto copy_out = [&](uint64_t e, const T* src) {
+            if (pair)
+                tma_store_3d(tmap, (int)(((e & ((1ull << h) - 1)) * sizeof(T)) >> 7), (int)(e >> h), src);
+            else
+                tma_store_2d(tmap, (int)((e * sizeof(T)) >> 7), src);
+        };
+        auto copy_in = [&](uint64_t e, T* dst, uint64_t* bar) {
+            if (pair)
+                tma_load_3d(dst, tmap, (int)(((e & ((1ull << h) - 1)) * sizeof(T)) >> 7), (int)(e >> h), bar);
+            else
+                tma_load_2d(dst, tmap, (int)((e * sizeof(T)) >> 7), bar);
         };
         auto store = [&](int64_t t, T* buf) {
             T* mem;
             uint64_t base;
             tile_at(t, &mem, &base);
             if constexpr (Swz) {
-                for (int q = lane; q < nboxes; q += 32) tma_store_box(tmap, box_row(mem, base, q), buf + (size_t)q * box_elems);
+                for (int q = lane; q < nboxes; q += 32) copy_out(box_elem(mem, base, q), buf + (size_t)q * box_elems);
             } else {
                 for (int c = lane; c < nchunks; c += 32)
                     bulk_s2g(mem + (base | deposit((uint64_t)c, pd.hi, K - L)), buf + ((size_t)c << L), chunk_bytes);
@@ -853,8 +868,7 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
             if (lane == 0) mbar_arrive_expect_tx(&full[b], chunk_bytes * (uint32_t)nchunks);
             __syncwarp();
             if constexpr (Swz) {
-                for (int q = lane; q < nboxes; q += 32)
-                    tma_load_box(buf + (size_t)q * box_elems, tmap, box_row(mem, base, q), &full[b]);
+                for (int q = lane; q < nboxes; q += 32) copy_in(box_elem(mem, base, q), buf + (size_t)q * box_elems, &full[b]);
             } else {
                 for (int c = lane; c < nchunks; c += 32)
                     bulk_g2s(buf + ((size_t)c << L), mem + (base | deposit((uint64_t)c, pd.hi, K - L)), chunk_bytes,
