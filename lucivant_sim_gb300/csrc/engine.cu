@@ -1143,7 +1143,7 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
                     (long long)(s->member_bytes() * (size_t)batch));
     }
     *out = s;
-    return lsg_state_set_basis(s, 0);
+    return set_basis_async(s, 0);  // stream-ordered like all work on the register: no host wait
 }
 
 int lsg_state_free(lsg_state s) {

@@ -477,27 +477,43 @@ std::string jit_source(const Plan& plan, int precision, int ctas, bool swz) {
 std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz) {
     const size_t np = plan.passes.size();
     if (np == 0) return nullptr;
-    std::vector<std::string> kernels(np);
-    size_t total_len = 0;
-    for (size_t i = 0; i < np; ++i) {
-        kernels[i] = pass_kernel_source(plan, i, precision, ctas, swz);
-        if (kernels[i].empty()) return nullptr;  // a pass the specializer does not take: interpret them all
-        total_len += kernels[i].size();
-    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-    std::string key = std::to_string(dev) + "\n";
-    key.reserve(total_len + 16);
-    for (const std::string& k : kernels) key += k;
+    // The source is a function of the plan (its descriptors are value-initialised, padding
+    // included), the precision, the CTAs per SM and the swizzle: the cache is keyed by their bytes,
+    // so a program of a known shape (new data, same structure) skips source generation too.
+    std::string key;
+    {
+        const int head[4] = {dev, precision, ctas, swz ? 1 : 0};
+        const size_t sizes[3] = {plan.passes.size(), plan.ops.size(), plan.blocks.size()};
+        key.reserve(sizeof(head) + sizeof(sizes) + sizes[0] * sizeof(PassDesc) + sizes[1] * sizeof(TileOp) +
+                    sizes[2] * sizeof(BlockDesc));
+        key.append(reinterpret_cast<const char*>(head), sizeof(head));
+        key.append(reinterpret_cast<const char*>(sizes), sizeof(sizes));
+        key.append(reinterpret_cast<const char*>(plan.passes.data()), sizes[0] * sizeof(PassDesc));
+        key.append(reinterpret_cast<const char*>(plan.ops.data()), sizes[1] * sizeof(TileOp));
+        key.append(reinterpret_cast<const char*>(plan.blocks.data()), sizes[2] * sizeof(BlockDesc));
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        auto hit = g_cache.find(key);
+        if (hit != g_cache.end()) return hit->second;
+    }
+    std::vector<std::string> kernels(np);
+    for (size_t i = 0; i < np; ++i) {
+        kernels[i] = pass_kernel_source(plan, i, precision, ctas, swz);
+        if (kernels[i].empty()) break;  // a pass the specializer does not take: interpret them all
+    }
     std::lock_guard<std::mutex> lock(g_mu);
-    auto hit = g_cache.find(key);
+    auto hit = g_cache.find(key);  // another thread may have built it meanwhile
     if (hit != g_cache.end()) return hit->second;
     const Nvrtc& rt = nvrtc();
     const Driver& drv = driver();
     static const bool at_exit = [] { return std::atexit([] { g_exiting = true; }) == 0; }();
     (void)at_exit;
     std::shared_ptr<JitPasses> out;
-    if (rt.ok && drv.ok) {
+    const bool all = std::none_of(kernels.begin(), kernels.end(), [](const std::string& k) { return k.empty(); });
+    if (all && rt.ok && drv.ok) {
         // passes are independent translation units: compile them in parallel, in chunks of
         // about equal source length (NVRTC programs are compiled concurrently on host threads)
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());

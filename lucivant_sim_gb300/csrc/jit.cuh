@@ -47,7 +47,8 @@ bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_byte
 // Specialize a planned gate program (no trajectory operators, no shared-memory operators), or
 // nullptr when it can't be (unsupported operators, no NVRTC, compilation failure): the
 // interpreter then runs it. `ctas` is the launch bound's CTAs per SM. Passes compile in parallel
-// on host threads; modules are cached by source for the life of the process.
+// on host threads; modules are cached by plan (the descriptors the source is generated from) for
+// the life of the process, so a program of a known shape generates no source.
 std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz);
 
 // Launch every pass on `stream` (events before each pass when `marks` is given).

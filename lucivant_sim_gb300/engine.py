@@ -23,6 +23,7 @@ from typing import Any
 import numpy as np
 
 from lucivant_sim_gb300 import _lib
+from lucivant_sim_gb300 import noise as nm_mod
 from lucivant_sim_gb300._lib import OP_DEPOL, OP_DIAG, OP_MATRIX, OP_PERM, OP_SCALE, OpList, SimulationError
 
 MAX_STATEVECTOR_QUBITS = 26
@@ -178,11 +179,15 @@ def dm_oplist(circuit: Any, noises: list[Any]) -> OpList:
             hit = chan_cache[id(ch)] = (ch, s)
         return hit[1]
 
+    gate_errors = nm_mod.GateErrors(noises)
+    errors_of: dict[tuple[str, tuple[int, ...]], list[Any]] = {}
     for op in circuit.operations:
         if op.kind == "gate":
             qs = tuple(op.qubits)
             u = np.asarray(op.matrix, dtype=np.complex128)
-            chans = [nm.gate_error(op.name, qs) if nm is not None else None for nm in noises]
+            chans = errors_of.get((op.name, qs))
+            if chans is None:
+                chans = errors_of[(op.name, qs)] = gate_errors(op.name, qs)
             present = [c is not None for c in chans]
             if any(present) and not all(present):
                 raise ValueError("batched noise models must attach channels to the same gates")
@@ -355,13 +360,10 @@ _SWAP_SRC = np.array([1, 1, 1, 1, 0, 2, 1, 3], dtype=np.complex128)
 def _snap(x: np.ndarray) -> np.ndarray:
     """Rounding residue of the transfer-matrix products (|x| ~ 1e-16) snapped to the exact 0 and
     +-1 entries it stands for, so trace preservation and permutation structure are recognised."""
-    x = np.array(x, dtype=np.float64)
-    a = np.abs(x)
-    x[a < 1e-14] = 0.0
-    near = np.abs(a - 1.0) < 1e-14
-    if near.any():
-        x[near] = np.sign(x[near])
-    return x
+    x = np.asarray(x, dtype=np.float64)
+    r = np.rint(x)  # the candidate: |x| < 1e-14 -> 0, ||x| - 1| < 1e-14 -> sign(x)
+    keep = (np.abs(x - r) >= 1e-14) | (np.abs(r) > 1.0)
+    return np.where(keep, x, r + 0.0)  # + 0.0: -0.0 becomes 0.0
 
 
 def ptm_capable(circuit: Any, noises: list[Any]) -> bool:
@@ -451,12 +453,13 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
                 else:
                     todo.setdefault(len(ch.kraus), []).append(i)
             for _nk, members in todo.items():  # one product per Kraus count
-                kr = np.stack([np.stack([np.asarray(m, dtype=np.complex128) for m in chans[i].kraus]) for i in members])
+                kr = np.array([chans[i].kraus for i in members], dtype=np.complex128)
                 mats[members] = ptm_of_kraus_stack(kr)
             hit = cache[key] = mats
         return hit
 
     # 1. the gates and resets in order, grouped by (arity, channel stack)
+    gate_errors = nm_mod.GateErrors(noises)
     chans_of: dict[tuple[str, tuple[int, ...]], tuple[list[Any], tuple[int, ...]]] = {}  # channels per gate signature
     items: list[tuple[list[int], tuple[Any, ...], int]] = []  # (bits, group key, index in group)
     groups: dict[tuple[Any, ...], list[np.ndarray]] = {}
@@ -470,7 +473,7 @@ def ptm_oplist(circuit: Any, noises: list[Any]) -> OpList:
             sig = (op.name, qs)
             got = chans_of.get(sig)
             if got is None:
-                chans = [nm.gate_error(op.name, qs) if nm is not None else None for nm in noises]
+                chans = gate_errors(op.name, qs)
                 got = chans_of[sig] = (chans, tuple(id(ch) for ch in chans))
             chans, chan_key = got
             present = [c is not None for c in chans]

@@ -92,6 +92,36 @@ def depolarizing(p: float, num_qubits: int = 1) -> Channel:
     return Channel("depolarizing", num_qubits, base.kraus, (p,), base.mixture, analytic_depolarizing=True)
 
 
+class GateErrors:
+    """:meth:`NoiseModel.gate_error` over many models at once (``None`` entries: no noise). Models
+    sharing a rule shape share the winning rule's index, found once per gate signature, so a batch
+    of noise instances of one template costs one rule search per gate instead of one per model."""
+
+    def __init__(self, models: Sequence[NoiseModel | None]) -> None:
+        self.models = list(models)
+        shapes: dict[tuple[Any, ...], int] = {}
+        self.shape_of = [None if m is None else shapes.setdefault(m.rule_shape(), len(shapes)) for m in self.models]
+        self.first = {}
+        for i, sh in enumerate(self.shape_of):
+            if sh is not None:
+                self.first.setdefault(sh, i)
+
+    def __call__(self, name: str, qubits: tuple[int, ...]) -> list[Channel | None]:
+        winner: dict[int, int] = {}
+        for sh, i in self.first.items():
+            best, best_score = -1, -1.0
+            for j, rule in enumerate(self.models[i].rules):
+                s = rule.score(name, qubits)
+                if s >= 0 and s >= best_score:
+                    best, best_score = j, s
+            winner[sh] = best
+        out: list[Channel | None] = []
+        for m, sh in zip(self.models, self.shape_of):
+            j = -1 if sh is None else winner[sh]
+            out.append(None if j < 0 else m.rules[j].channel)  # type: ignore[union-attr]
+        return out
+
+
 def from_gate_error(error: float, num_qubits: int) -> Channel:
     """The depolarising channel with average gate infidelity ``error`` (p = r d/(d-1))."""
     d = 1 << num_qubits
@@ -206,6 +236,11 @@ class NoiseModel:
             if s >= 0 and s >= best_score:
                 best, best_score = rule.channel, s
         return best
+
+    def rule_shape(self) -> tuple[Any, ...]:
+        """What rule selection reads (each rule's gates, qubits and channel width, in order): models
+        of one shape pick the same rule for every gate."""
+        return tuple((r.gates, r.qubits, r.channel.num_qubits) for r in self.rules)
 
     def readout_error(self, qubit: int) -> ReadoutError | None:
         return self.readout.get(qubit, self.readout.get(None))

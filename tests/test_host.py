@@ -376,3 +376,33 @@ def test_planner_and_specializer_on_random_operator_lists():
             finally:
                 os.environ.pop("LSG_PLAN_SEEDS", None)
     assert written > 150  # the programs without operators wider than a register block
+
+
+def test_gate_errors_over_many_models_match_each_model():
+    """The batched rule lookup picks, for every model, the channel the model's own gate_error
+    picks: specific rules beat general ones, later rules win ties, shapes may differ per model."""
+    from lucivant_sim_gb300.noise import GateErrors
+
+    rng = np.random.default_rng(5)
+    models: list[NoiseModel | None] = []
+    for i in range(40):
+        if i % 13 == 7:
+            models.append(None)
+            continue
+        m = NoiseModel()
+        m.add_gate_error(depolarizing(float(rng.uniform(0, 0.1)), 1))
+        m.add_gate_error(depolarizing(float(rng.uniform(0, 0.1)), 2))
+        if i % 3 == 0:
+            m.add_gate_error(depolarizing(float(rng.uniform(0, 0.1)), 1), gates="h")
+        if i % 4 == 1:
+            m.add_gate_error(depolarizing(float(rng.uniform(0, 0.1)), 1), qubits=[2])
+            m.add_gate_error(depolarizing(float(rng.uniform(0, 0.1)), 2), gates=["cx"], qubits=[1, 0])
+        if i % 5 == 2:
+            m.add_gate_error(thermal_relaxation(50.0, 40.0, 0.1), gates=["x", "h"], qubits=[2])
+        models.append(m)
+    lookup = GateErrors(models)
+    for name, qubits in [("h", (0,)), ("h", (2,)), ("x", (2,)), ("rz", (1,)), ("cx", (0, 1)), ("cx", (1, 2)),
+                         ("u3", (2,)), ("cz", (1, 0)), ("ccx", (0, 1, 2))]:
+        want = [None if m is None else m.gate_error(name, qubits) for m in models]
+        got = lookup(name, qubits)
+        assert all(a is b for a, b in zip(got, want)), (name, qubits)
