@@ -337,6 +337,19 @@ def config_block(args: argparse.Namespace) -> dict:
 # ------------------------------------------------------------------------------ GPU arm
 
 
+def e2e_upload_bytes(circuit, noises, precision: str) -> int:
+    """Host-to-device bytes of one run_density_batch call: the operator table and data pool of
+    each batch it evolves (two halves for an even batch)."""
+    from lucivant_sim_gb300 import _lib, engine
+
+    parts = [noises[: len(noises) // 2], noises[len(noises) // 2 :]] if len(noises) % 2 == 0 else [noises]
+    total = 0
+    for part in parts:
+        ops = engine.ptm_oplist(circuit, part) if engine.dm_form(circuit, part) == "ptm" else engine.dm_oplist(circuit, part)
+        total += ops.size * 16 + len(ops) * _lib.OP_DTYPE.itemsize
+    return total
+
+
 def gb300_arm(args: argparse.Namespace) -> None:
     rank, world, local = dist_info()
     dist = Dist(world)
@@ -445,6 +458,9 @@ def gb300_arm(args: argparse.Namespace) -> None:
     # end to end through the public batched API: host inputs in, host results out, every step
     e2e_steps = max(2, args.steps // 2)
     batch.free()
+    # one untimed call: the halves the call evolves are programs of their own shape (specialized
+    # passes compiled once per process, like the whole batch's above)
+    run_density_batch(circuit, noises, labels, precision=args.precision)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -452,7 +468,8 @@ def gb300_arm(args: argparse.Namespace) -> None:
     e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
     from lucivant_sim_gb300 import engine
 
-    h2d = int(upload_bytes + 2 * 8 * len(labels))  # operator table and data pool, Pauli masks
+    # operator tables and data pools (one per half the call evolves), Pauli masks
+    h2d = int(e2e_upload_bytes(circuit, noises, args.precision) + 2 * 8 * len(labels))
     d2h = int(probs_h.nbytes + exps_h.nbytes)
 
     if rank == 0:

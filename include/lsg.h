@@ -132,6 +132,11 @@ int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run);
 /* 1 when the program's passes run as kernels specialized for it at creation (NVRTC, LSG_JIT=1),
  * 0 when the generic pass kernel interprets its operator records, negative on error. */
 int lsg_program_specialized(lsg_program p);
+/* 1 when the specialization policy (LSG_JIT, LSG_JIT_MIN_BYTES) takes a program whose run moves
+ * `bytes_per_run` algorithmic bytes (as lsg_program_info reports), 0 when not, negative on error.
+ * Lets a caller that splits one batch into several programs of the same shape keep them
+ * specialized when the whole batch would be. */
+int lsg_jit_wanted(int64_t bytes_per_run);
 /* Host-only diagnostic (no device is touched): the CUDA source of the specialized passes a
  * program of these operators would get (into buf, at most cap bytes with the terminating zero;
  * *len = full length, 0 when the program would be interpreted), and with `compile` != 0 its NVRTC

@@ -71,6 +71,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_program_run_timed": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     "lsg_program_info": (C.c_int, [_P, _PI32, _PI64]),
     "lsg_program_specialized": (C.c_int, [_P]),
+    "lsg_jit_wanted": (C.c_int, [C.c_int64]),
     "lsg_apply_from_basis": (C.c_int, [_P, _I64, _P, _I32, _PD, _I64]),
     "lsg_program_run_from_basis": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_float)]),
     "lsg_program_basis_info": (C.c_int, [_P, _PI64, _PI64]),
@@ -151,6 +152,14 @@ def plan_passes(nbits: int, precision: int, ops: "OpList") -> int:
     out = C.c_int32(0)
     check(library().lsg_plan(nbits, precision, table.ctypes.data, len(table), C.byref(out)))
     return int(out.value)
+
+
+def jit_wanted(bytes_per_run: int) -> bool:
+    """Whether the library specializes a program whose run moves ``bytes_per_run`` bytes."""
+    rc = library().lsg_jit_wanted(int(bytes_per_run))
+    if rc < 0:
+        check(rc)
+    return rc == 1
 
 
 def specialized_source(nbits: int, precision: int, batch: int, ops: "OpList", compile: bool = False) -> str:

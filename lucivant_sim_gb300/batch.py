@@ -69,12 +69,39 @@ class DensityBatch:
         self.reg.free()
 
 
-def run_density_batch(circuit: Any, noises: list[Any], observables: list[str], precision: str | None = "c64"):
+def run_density_batch(
+    circuit: Any, noises: list[Any], observables: list[str], precision: str | None = "c64", split: bool = True
+):
     """One call from host inputs to host results: probabilities (batch, 2^n) and expectations
-    (terms, batch) of every noise instance."""
-    b = DensityBatch(circuit, noises, precision)
+    (terms, batch) of every noise instance.
+
+    With ``split`` an even batch runs as two halves of one shape: the second half's operators are
+    built on the host while the first half evolves on the device, so most host work hides behind
+    device work. Every member's result is the same as in one whole batch (members evolve
+    independently). A half that the library would not specialize while the whole batch would be
+    (a run of the whole moves twice the bytes) is dropped for the whole batch."""
+    halves = [noises[: len(noises) // 2], noises[len(noises) // 2 :]] if split and len(noises) % 2 == 0 and noises else [noises]
+    done: list[DensityBatch] = []
     try:
-        b.evolve()
-        return b.probabilities(), b.expectations(observables)
+        first = DensityBatch(circuit, halves[0], precision)
+        done.append(first)
+        if len(halves) == 2 and not first.program.specialized:
+            nominal = first.program.bytes_per_run
+            if not _lib.jit_wanted(nominal) and _lib.jit_wanted(2 * nominal):
+                done.pop().free()  # the whole batch would be specialized: run it as one
+                halves = [noises]
+                first = DensityBatch(circuit, noises, precision)
+                done.append(first)
+        first.evolve()
+        for part in halves[1:]:
+            b = DensityBatch(circuit, part, precision)
+            done.append(b)
+            b.evolve()
+        probs = [b.probabilities() for b in done]
+        exps = [b.expectations(observables) for b in done]
+        if len(done) == 1:
+            return probs[0], exps[0]
+        return np.concatenate(probs, axis=0), np.concatenate(exps, axis=1)
     finally:
-        b.free()
+        for b in done:
+            b.free()

@@ -1341,6 +1341,12 @@ int lsg_program_specialized(lsg_program p) {
     return p->jit ? 1 : 0;
 }
 
+int lsg_jit_wanted(int64_t bytes_per_run) {
+    clear_error();
+    if (bytes_per_run < 0) return fail(LSG_E_ARG, "negative byte count");
+    return jit_wanted(bytes_per_run) ? 1 : 0;
+}
+
 int lsg_program_source(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
                        int64_t pool_entries, int compile, char* buf, int64_t cap, int64_t* len) {
     clear_error();

@@ -180,6 +180,22 @@ def test_batched_noise_instances():
         assert np.max(np.abs(out[b] - dense.evolve_dm(c, nm))) < ATOL_C128
 
 
+def test_density_batch_in_halves_matches_one_batch():
+    """run_density_batch evolves an even batch as two halves (the second built while the first
+    runs): every member's probabilities and expectations equal the whole batch's bit for bit."""
+    from lucivant_sim_gb300.batch import run_density_batch
+
+    c = ls.parse(wl.brickwork(6, 3, seed=12, measure=False))
+    noises = wl.dm_noise_instances(8, seed=4)
+    labels = wl.z_observables(6)
+    p2, e2 = run_density_batch(c, noises, labels, precision="c64", split=True)
+    p1, e1 = run_density_batch(c, noises, labels, precision="c64", split=False)
+    assert p2.shape == p1.shape == (8, 64) and e2.shape == e1.shape == (len(labels), 8)
+    assert np.array_equal(p1, p2) and np.array_equal(e1, e2)
+    p3, e3 = run_density_batch(c, noises[:7], labels, precision="c64")  # odd: one batch
+    assert np.array_equal(p3, p1[:7]) and np.array_equal(e3, e1[:, :7])
+
+
 @pytest.mark.parametrize("precision", ["c128", "c64"])
 def test_batched_pauli_transfer_instances(precision):
     """Noise instances of one circuit in one Pauli-transfer register: probabilities and Z
