@@ -916,10 +916,10 @@ static int program_create_jit(int nbits, int precision, int64_t batch, const lsg
     const int ctas = jit_ctas(precision);
     const int64_t bytes_per_run = 2 * ((int64_t)eb << nbits) * batch * (int64_t)p->plan.passes.size();
     const bool swz = jit_swizzle_fits(p->plan, eb, ((int64_t)eb << nbits) * batch);
-    if (bulk && jit_wanted(bytes_per_run)) p->jit = jit_build(p->plan, precision, ctas, swz);
+    if (bulk && jit_wanted(bytes_per_run)) p->jit = jit_build(p->plan, precision, ctas, swz, jit_packed(precision));
     if (const char* path = getenv("LSG_JIT_DUMP")) {  // diagnostics: the specialized source of this program
         if (FILE* f = std::fopen(path, "w")) {
-            const std::string src = jit_source(p->plan, precision, ctas, swz);
+            const std::string src = jit_source(p->plan, precision, ctas, swz, jit_packed(precision));
             std::fwrite(src.data(), 1, src.size(), f);
             std::fclose(f);
         }
@@ -1357,7 +1357,8 @@ int lsg_program_source(int nbits, int precision, int64_t batch, const lsg_op* op
                             nullptr, false));
     const size_t eb = lsg_elem_bytes(precision);
     const std::string src =
-        jit_source(p->plan, precision, jit_ctas(precision), jit_swizzle_fits(p->plan, eb, ((int64_t)eb << nbits) * batch));
+        jit_source(p->plan, precision, jit_ctas(precision), jit_swizzle_fits(p->plan, eb, ((int64_t)eb << nbits) * batch),
+                   jit_packed(precision));
     delete p;
     if (len) *len = (int64_t)src.size();
     if (buf && cap > 0) {

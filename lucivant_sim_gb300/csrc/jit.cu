@@ -71,6 +71,7 @@ struct Driver {
     CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
     CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
     CUresult (*module_unload)(CUmodule) = nullptr;
+    CUresult (*get_attribute)(int*, CUfunction_attribute, CUfunction) = nullptr;  // optional
     CUresult (*encode)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
                        const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                        CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;  // optional
@@ -91,6 +92,7 @@ const Driver& driver() {
                get("cuOccupancyMaxActiveBlocksPerMultiprocessor", reinterpret_cast<void**>(&r.occupancy)) &&
                get("cuModuleUnload", reinterpret_cast<void**>(&r.module_unload));
         if (!get("cuTensorMapEncodeTiled", reinterpret_cast<void**>(&r.encode))) r.encode = nullptr;
+        if (!get("cuFuncGetAttribute", reinterpret_cast<void**>(&r.get_attribute))) r.get_attribute = nullptr;
         cudaGetLastError();
         return r;
     }();
@@ -107,27 +109,38 @@ const char* type_name(int precision) {
 }
 
 // One register-block operator as a call with compile-time positions; false for kinds that
-// specialized passes do not take (mixtures and other trajectory operators).
-bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int at) {
+// specialized passes do not take (mixtures and other trajectory operators). `packed`: the
+// operands are real32 group pairs packed in 64-bit registers (tile.cuh F2, rp_* operators).
+bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int at, bool packed = false) {
     const int c = t.tmpl;
-    auto two = [&](const char* fn, int base) {
-        const int r = c - base;
-        o << fn << "<" << T << ", " << U << ", " << r / 4 << ", " << r % 4 << ">";
+    // data operators: rb_name<T, U, ...> or, packed, rp_name<U, ...>; renames: rb_name<T or F2, U, ...>
+    auto name = [&](const char* fn, bool data_op) {
+        if (packed && data_op) o << "rp_" << fn << "<" << U;
+        else o << "rb_" << fn << "<" << (packed ? "lsg::F2" : T) << ", " << U;
     };
-    auto one = [&](const char* fn, int base) { o << fn << "<" << T << ", " << U << ", " << (c - base) << ">"; };
+    auto two = [&](const char* fn, int base, bool data_op = true) {
+        const int r = c - base;
+        name(fn, data_op);
+        o << ", " << r / 4 << ", " << r % 4 << ">";
+    };
+    auto one = [&](const char* fn, int base, bool data_op = true) {
+        name(fn, data_op);
+        o << ", " << (c - base) << ">";
+    };
     bool data = true;
-    if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) one("rb_dense1", kT_DENSE1);
-    else if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) two("rb_dense2", kT_DENSE2);
-    else if (c >= kT_TPD2 && c < kT_TPD2 + 16) two("rb_tpd2", kT_TPD2);
-    else if (c >= kT_PERM1 && c < kT_PERM1 + 4) one("rb_perm1", kT_PERM1);
-    else if (c >= kT_PERM2 && c < kT_PERM2 + 16) two("rb_perm2", kT_PERM2);
-    else if (c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) two("rb_depol1", kT_DEPOL1);
+    if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) one("dense1", kT_DENSE1);
+    else if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) two("dense2", kT_DENSE2);
+    else if (c >= kT_TPD2 && c < kT_TPD2 + 16) two("tpd2", kT_TPD2);
+    else if (c >= kT_PERM1 && c < kT_PERM1 + 4) one("perm1", kT_PERM1);
+    else if (c >= kT_PERM2 && c < kT_PERM2 + 16) two("perm2", kT_PERM2);
+    else if (packed && ((c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) || c == kT_DEPOL2)) return false;  // complex only
+    else if (c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) two("depol1", kT_DEPOL1);
     else if (c == kT_DEPOL2 && U == 4) o << "rb_depol2<" << T << ">";
-    else if (c == kT_DIAGB) o << "rb_diagb<" << T << ", " << U << ">";
-    else if (c == kT_SCALE) o << "rb_scale<" << T << ", " << U << ">";
-    else if (c >= kT_X1 && c < kT_X1 + 4) one("rb_x", kT_X1), data = false;
-    else if (c >= kT_CX && c < kT_CX + 16) two("rb_cx", kT_CX), data = false;
-    else if (c >= kT_SWAP && c < kT_SWAP + 16) two("rb_swap", kT_SWAP), data = false;
+    else if (c == kT_DIAGB) name("diagb", true), o << ">";
+    else if (c == kT_SCALE) name("scale", true), o << ">";
+    else if (c >= kT_X1 && c < kT_X1 + 4) one("x", kT_X1, false), data = false;
+    else if (c >= kT_CX && c < kT_CX + 16) two("cx", kT_CX, false), data = false;
+    else if (c >= kT_SWAP && c < kT_SWAP + 16) two("swap", kT_SWAP, false), data = false;
     else return false;
     const std::string v = at ? "v + " + std::to_string(at) : std::string("v");
     if (data) o << "(" << v << ", data + " << t.data << "LL + member * " << t.stride << "LL);\n";
@@ -281,8 +294,9 @@ std::vector<std::string> mapped_addresses(std::ostringstream& o, const BlockGen&
 }
 
 void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, const PassDesc& pd, const char* T,
-                const Swizzle& sw, bool* ok) {
+                const Swizzle& sw, bool packed, bool* ok) {
     const BlockDesc& b = *g.b;
+    const bool pk = packed && g.W == 2;  // the group pair in packed 64-bit registers (real32)
     const uint32_t tile_mask = pd.K >= 32 ? ~0u : ((1u << pd.K) - 1u);
     const bool fold = g.folded();
     if (fold)  // one group (pair) per thread; threads past the last group only join the barriers
@@ -292,19 +306,22 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
     o << "      const uint32_t G = uint32_t(g)" << (g.W == 2 ? " << 1" : "") << ";\n";
     o << "      const uint32_t base =";
     for (int i = 0; i <= g.U; ++i) o << (i ? " |" : "") << " ((G << " << i << ") & " << b.dep[i] << "u)";
-    o << ";\n      " << T << " v[" << g.n * g.W << "];\n";
+    if (pk) o << ";\n      lsg::F2 v[" << g.n << "];\n";
+    else o << ";\n      " << T << " v[" << g.n * g.W << "];\n";
     const std::vector<std::string> la = mapped_addresses(o, g, g.load_map, "lb", tile_mask, sw);
     if (fold) o << "      if (act) {\n";
     for (int e = 0; e < g.n; e += g.run) {
-        if (g.W == 2)
+        if (pk)
+            o << "      v[" << e << "] = ld_f2(tile + (" << la[e] << "));\n";
+        else if (g.W == 2)
             o << "      ld_split<" << T << ">(tile + (" << la[e] << "), v[" << e << "], v[" << g.n + e << "]);\n";
         else
             o << "      ld_run<" << T << ", " << g.run << ">(tile + (" << la[e] << "), v + " << e << ");\n";
     }
     for (int k = b.first; k < b.first + b.nops; ++k)
-        for (int w = 0; w < g.W; ++w) {
+        for (int w = 0; w < (pk ? 1 : g.W); ++w) {
             o << "      ";
-            if (!op_call(o, plan.ops[pd.first_op + k], g.U, T, w * g.n)) {
+            if (!op_call(o, plan.ops[pd.first_op + k], g.U, T, w * g.n, pk)) {
                 *ok = false;
                 return;
             }
@@ -312,7 +329,9 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
     if (fold) o << "      }\n      cbar();  // every group is in registers: the renamed stores may land in any group\n      if (act) {\n";
     const std::vector<std::string> sa = mapped_addresses(o, g, g.store_map, "sb", tile_mask, sw);
     for (int e = 0; e < g.n; e += g.run) {
-        if (g.W == 2)
+        if (pk)
+            o << "      st_f2(tile + (" << sa[e] << "), v[" << e << "]);\n";
+        else if (g.W == 2)
             o << "      st_split<" << T << ">(tile + (" << sa[e] << "), v[" << e << "], v[" << g.n + e << "]);\n";
         else
             o << "      st_run<" << T << ", " << g.run << ">(tile + (" << sa[e] << "), v + " << e << ");\n";
@@ -321,7 +340,7 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
     o << "    }\n";
 }
 
-std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_bytes, int ctas, bool swz) {
+std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_bytes, int ctas, bool swz, bool packed) {
     const PassDesc& pd = plan.passes[pi];
     const char* T = type_name(precision);
     const Swizzle sw = Swizzle::for_elem(swz, elem_bytes);
@@ -358,7 +377,7 @@ std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_byt
       << "* __restrict__ data, long long member) {\n";
     bool ok = true;
     for (const BlockGen& g : gens) {
-        emit_block(o, g, plan, pd, T, sw, &ok);
+        emit_block(o, g, plan, pd, T, sw, packed && precision == LSG_R32, &ok);
         if (!ok) return "";
     }
     o << "    cbar();\n  }\n};\n";
@@ -388,6 +407,12 @@ int jit_mode() {
     return env[0] == '0' ? 0 : 1;
 }
 
+bool jit_packed(int precision) {
+    if (precision != LSG_R32) return false;
+    const char* env = getenv("LSG_FFMA2");
+    return env && env[0] == '1';
+}
+
 bool jit_wanted(int64_t bytes_per_run) {
     const int mode = jit_mode();
     if (mode != 2) return mode == 1;
@@ -399,9 +424,9 @@ bool jit_wanted(int64_t bytes_per_run) {
 namespace {
 
 // Pass i's body and kernel, or "" when the specializer does not take one of its blocks.
-std::string pass_kernel_source(const Plan& plan, size_t i, int precision, int ctas, bool swz) {
+std::string pass_kernel_source(const Plan& plan, size_t i, int precision, int ctas, bool swz, bool packed) {
     const char* T = type_name(precision);
-    const std::string body = pass_source(plan, i, precision, (int)lsg_elem_bytes(precision), ctas, swz);
+    const std::string body = pass_source(plan, i, precision, (int)lsg_elem_bytes(precision), ctas, swz, packed);
     if (body.empty()) return "";
     std::ostringstream o;
     o << body << "extern \"C\" __global__ void __launch_bounds__(" << kPipeThreadsHost << ", " << ctas
@@ -464,27 +489,89 @@ bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_byte
     return true;
 }
 
-std::string jit_source(const Plan& plan, int precision, int ctas, bool swz) {
+std::string jit_source(const Plan& plan, int precision, int ctas, bool swz, bool packed) {
     std::string src = kPrelude;
     for (size_t i = 0; i < plan.passes.size(); ++i) {
-        const std::string k = pass_kernel_source(plan, i, precision, ctas, swz);
+        const std::string k = pass_kernel_source(plan, i, precision, ctas, swz, packed);
         if (k.empty()) return "";  // a pass the specializer does not take: interpret them all
         src += k;
     }
     return src;
 }
 
-std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz) {
+namespace {
+
+// A loaded pass kernel: its function, resident CTAs per SM and local memory per thread (spills).
+struct Loaded {
+    void* fn = nullptr;
+    int per_sm = 1;
+    int local = 0;
+};
+
+// LSG_JIT_SPILL: local bytes per thread above which a pass is rebuilt for one CTA fewer per SM
+// (default 64; 0 or less: never).
+int jit_spill_bytes() {
+    const char* env = getenv("LSG_JIT_SPILL");
+    return env && env[0] ? atoi(env) : 64;
+}
+
+// Compile kernels[i] for every i in `which` (passes are independent translation units: compiled
+// in parallel, in chunks of about equal source length, NVRTC programs on concurrent host threads),
+// load the modules (appended to `modules`) and fill out[i]. False on any failure.
+bool compile_load(const std::vector<std::string>& kernels, const std::vector<size_t>& which, const Plan& plan,
+                  size_t eb, bool swz, std::vector<Loaded>& out, std::vector<void*>& modules) {
+    const Driver& drv = driver();
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nchunks = std::min<size_t>({which.size(), (size_t)hw, 16});
+    if (nchunks == 0) return true;
+    std::vector<std::string> units(nchunks, kPrelude);
+    std::vector<std::vector<size_t>> members(nchunks);
+    std::vector<size_t> load(nchunks, 0);
+    for (size_t i : which) {
+        const size_t c = std::min_element(load.begin(), load.end()) - load.begin();
+        units[c] += kernels[i];
+        members[c].push_back(i);
+        load[c] += kernels[i].size();
+    }
+    std::vector<std::vector<char>> cubins(nchunks);
+    std::vector<std::thread> workers;
+    for (size_t c = 1; c < nchunks; ++c) workers.emplace_back([&, c] { cubins[c] = compile_unit(units[c]); });
+    cubins[0] = compile_unit(units[0]);
+    for (std::thread& w : workers) w.join();
+    bool ok = true;
+    for (size_t c = 0; c < nchunks && ok; ++c) {
+        CUmodule mod;
+        ok = !cubins[c].empty() && drv.module_load(&mod, cubins[c].data()) == CUDA_SUCCESS;
+        if (ok) modules.push_back(mod);
+        for (size_t j = 0; j < members[c].size() && ok; ++j) {
+            const size_t i = members[c][j];
+            const std::string name = "lsg_pass_" + std::to_string(i);
+            CUfunction f;
+            const size_t smem = 2 * (eb << plan.passes[i].K) + (swz ? 1024 : 0);  // the two-tile ring, aligned
+            ok = drv.get_function(&f, mod, name.c_str()) == CUDA_SUCCESS &&
+                 drv.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) == CUDA_SUCCESS &&
+                 drv.occupancy(&out[i].per_sm, f, kPipeThreadsHost, smem) == CUDA_SUCCESS;
+            out[i].fn = f;
+            if (ok && drv.get_attribute && drv.get_attribute(&out[i].local, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, f) != CUDA_SUCCESS)
+                out[i].local = 0;
+        }
+    }
+    return ok;
+}
+
+}  // namespace
+
+std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz, bool packed) {
     const size_t np = plan.passes.size();
     if (np == 0) return nullptr;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
     // The source is a function of the plan (its descriptors are value-initialised, padding
-    // included), the precision, the CTAs per SM and the swizzle: the cache is keyed by their bytes,
+    // included), the precision, the CTAs per SM, the swizzle and the packing: the cache is keyed by their bytes,
     // so a program of a known shape (new data, same structure) skips source generation too.
     std::string key;
     {
-        const int head[4] = {dev, precision, ctas, swz ? 1 : 0};
+        const int head[6] = {dev, precision, ctas, swz ? 1 : 0, packed ? 1 : 0, jit_spill_bytes()};
         const size_t sizes[3] = {plan.passes.size(), plan.ops.size(), plan.blocks.size()};
         key.reserve(sizeof(head) + sizeof(sizes) + sizes[0] * sizeof(PassDesc) + sizes[1] * sizeof(TileOp) +
                     sizes[2] * sizeof(BlockDesc));
@@ -501,7 +588,7 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, 
     }
     std::vector<std::string> kernels(np);
     for (size_t i = 0; i < np; ++i) {
-        kernels[i] = pass_kernel_source(plan, i, precision, ctas, swz);
+        kernels[i] = pass_kernel_source(plan, i, precision, ctas, swz, packed);
         if (kernels[i].empty()) break;  // a pass the specializer does not take: interpret them all
     }
     std::lock_guard<std::mutex> lock(g_mu);
@@ -514,45 +601,31 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, 
     std::shared_ptr<JitPasses> out;
     const bool all = std::none_of(kernels.begin(), kernels.end(), [](const std::string& k) { return k.empty(); });
     if (all && rt.ok && drv.ok) {
-        // passes are independent translation units: compile them in parallel, in chunks of
-        // about equal source length (NVRTC programs are compiled concurrently on host threads)
-        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-        const size_t nchunks = std::min<size_t>({np, (size_t)hw, 16});
-        std::vector<std::string> units(nchunks, kPrelude);
-        std::vector<std::vector<size_t>> members(nchunks);
-        std::vector<size_t> load(nchunks, 0);
-        for (size_t i = 0; i < np; ++i) {
-            const size_t c = std::min_element(load.begin(), load.end()) - load.begin();
-            units[c] += kernels[i];
-            members[c].push_back(i);
-            load[c] += kernels[i].size();
-        }
-        std::vector<std::vector<char>> cubins(nchunks);
-        std::vector<std::thread> workers;
-        for (size_t c = 1; c < nchunks; ++c) workers.emplace_back([&, c] { cubins[c] = compile_unit(units[c]); });
-        cubins[0] = compile_unit(units[0]);
-        for (std::thread& w : workers) w.join();
         auto jp = std::make_shared<JitPasses>();
         jp->fns.resize(np);
         jp->per_sm.resize(np, 1);
         jp->swz = swz;
         const size_t eb = lsg_elem_bytes(precision);
-        bool ok = true;
-        for (size_t c = 0; c < nchunks && ok; ++c) {
-            CUmodule mod;
-            ok = !cubins[c].empty() && drv.module_load(&mod, cubins[c].data()) == CUDA_SUCCESS;
-            if (ok) jp->modules.push_back(mod);
-            for (size_t j = 0; j < members[c].size() && ok; ++j) {
-                const size_t i = members[c][j];
-                const std::string name = "lsg_pass_" + std::to_string(i);
-                CUfunction f;
-                const size_t smem = 2 * (eb << plan.passes[i].K) + (swz ? 1024 : 0);  // the two-tile ring, aligned
-                ok = drv.get_function(&f, mod, name.c_str()) == CUDA_SUCCESS &&
-                     drv.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) == CUDA_SUCCESS &&
-                     drv.occupancy(&jp->per_sm[i], f, kPipeThreadsHost, smem) == CUDA_SUCCESS;
-                jp->fns[i] = f;
-            }
+        std::vector<size_t> every(np);
+        for (size_t i = 0; i < np; ++i) every[i] = i;
+        std::vector<Loaded> got(np);
+        bool ok = compile_load(kernels, every, plan, eb, swz, got, jp->modules);
+        // A pass whose registers spill at `ctas` CTAs per SM (local memory beyond the threshold:
+        // with three CTAs' tiles in shared memory, spilled values overflow L1 to L2) is compiled
+        // again for one CTA fewer, with more registers per thread, and keeps the smaller spill.
+        const int spill = jit_spill_bytes();
+        std::vector<size_t> again;
+        for (size_t i = 0; ok && spill > 0 && ctas > 1 && i < np; ++i)
+            if (got[i].local > spill) again.push_back(i);
+        if (ok && !again.empty()) {
+            std::vector<std::string> fewer(np);
+            for (size_t i : again) fewer[i] = pass_kernel_source(plan, i, precision, ctas - 1, swz, packed);
+            std::vector<Loaded> alt(np);
+            if (compile_load(fewer, again, plan, eb, swz, alt, jp->modules))
+                for (size_t i : again)
+                    if (alt[i].local < got[i].local) got[i] = alt[i];
         }
+        for (size_t i = 0; ok && i < np; ++i) jp->fns[i] = got[i].fn, jp->per_sm[i] = got[i].per_sm;
         if (ok) out = jp;
     }
     g_cache[key] = out;  // a failure is remembered too: the interpreter runs those programs

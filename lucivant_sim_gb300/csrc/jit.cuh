@@ -32,9 +32,11 @@ struct JitPasses {
 // so of compilation is recovered within a few dozen runs).
 int jit_mode();
 bool jit_wanted(int64_t bytes_per_run);
+// Whether real32 group pairs run as packed 64-bit operands (fma.rn.f32x2; LSG_FFMA2=1).
+bool jit_packed(int precision);
 
 // The CUDA source of a planned gate program's specialized passes, or "" when a pass can't be.
-std::string jit_source(const Plan& plan, int precision, int ctas, bool swz);
+std::string jit_source(const Plan& plan, int precision, int ctas, bool swz, bool packed);
 
 // Compile `source` with NVRTC only (no device needed): LSG_OK, or an error with NVRTC's log.
 int jit_compile_check(const std::string& source);
@@ -49,7 +51,7 @@ bool jit_swizzle_fits(const Plan& plan, size_t elem_bytes, int64_t register_byte
 // interpreter then runs it. `ctas` is the launch bound's CTAs per SM. Passes compile in parallel
 // on host threads; modules are cached by plan (the descriptors the source is generated from) for
 // the life of the process, so a program of a known shape generates no source.
-std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz);
+std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, bool swz, bool packed);
 
 // Launch every pass on `stream` (events before each pass when `marks` is given).
 // `tiles_per_member[i]`: the tiles pass i visits in each of the `batch` members.

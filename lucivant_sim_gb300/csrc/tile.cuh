@@ -477,6 +477,144 @@ __device__ __forceinline__ void rb_scale(T* v, const T* m) {
     for (int e = 0; e < (1 << U); ++e) v[e] = cmul(f, v[e]);
 }
 
+// ------------------------------------------------------------------ packed group pairs (real32)
+//
+// A specialized pass whose block leaves tile bit 0 free handles two groups per thread (tile bit 0
+// clear and set). For real32 registers the pair's two values of element e can live in one 64-bit
+// register pair and every operator runs on both with one packed FP32 instruction (mul.rn.f32x2,
+// fma.rn.f32x2, sm_100 and later): lane 0 is the group with tile bit 0 clear. Each lane is
+// rounded exactly as the scalar mul / fma of the unpacked form, in the same order, so results
+// are identical bit for bit; the coefficient is broadcast to both lanes.
+struct F2 {
+    unsigned long long r;
+};
+__device__ __forceinline__ F2 f2_bcast(float c) {
+    F2 o;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(o.r) : "f"(c));
+    return o;
+}
+__device__ __forceinline__ F2 f2_mul(float c, F2 a) {
+    F2 o;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(f2_bcast(c).r), "l"(a.r));
+    return o;
+}
+__device__ __forceinline__ F2 f2_fma(float c, F2 a, F2 acc) {
+    F2 o;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(o.r) : "l"(f2_bcast(c).r), "l"(a.r), "l"(acc.r));
+    return o;
+}
+// the pair at p (8-byte aligned): p[0] to lane 0, p[1] to lane 1
+__device__ __forceinline__ F2 ld_f2(const float* p) {
+    F2 o;
+    o.r = *reinterpret_cast<const unsigned long long*>(p);
+    return o;
+}
+__device__ __forceinline__ void st_f2(float* p, F2 v) { *reinterpret_cast<unsigned long long*>(p) = v.r; }
+
+template <int U, int P>
+__device__ __forceinline__ void rp_dense1(F2* v, const float* m) {
+    constexpr int B = 1 << (U - 1 - P);
+    float mm[4];
+    ldv<float, 4>(m, mm);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & B) continue;
+        const F2 a0 = v[e], a1 = v[e | B];
+        v[e] = f2_fma(mm[1], a1, f2_mul(mm[0], a0));
+        v[e | B] = f2_fma(mm[3], a1, f2_mul(mm[2], a0));
+    }
+}
+
+template <int U, int P0, int P1>
+__device__ __forceinline__ void rp_dense2(F2* v, const float* m) {
+    constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+    float mm[16];
+    ldv<float, 16>(m, mm);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & (B0 | B1)) continue;
+        const F2 a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            F2 acc = f2_mul(mm[4 * r], a0);
+            acc = f2_fma(mm[4 * r + 1], a1, acc);
+            acc = f2_fma(mm[4 * r + 2], a2, acc);
+            acc = f2_fma(mm[4 * r + 3], a3, acc);
+            v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
+        }
+    }
+}
+
+template <int U, int P0, int P1>
+__device__ __forceinline__ void rp_tpd2(F2* v, const float* m) {
+    constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+    float mm[12];
+    ldv<float, 12>(m + 4, mm);
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & (B0 | B1)) continue;
+        const F2 a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+#pragma unroll
+        for (int r = 1; r < 4; ++r) {
+            F2 acc = f2_mul(mm[4 * r - 4], a0);
+            acc = f2_fma(mm[4 * r - 3], a1, acc);
+            acc = f2_fma(mm[4 * r - 2], a2, acc);
+            acc = f2_fma(mm[4 * r - 1], a3, acc);
+            v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
+        }
+    }
+}
+
+template <int U, int P>
+__device__ __forceinline__ void rp_perm1(F2* v, const float* m) {
+    constexpr int B = 1 << (U - 1 - P);
+    const float p0 = m[0], p1 = m[1];
+    const bool swap = m[2] != 0.0f;
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & B) continue;
+        const F2 a0 = v[e], a1 = v[e | B];
+        v[e] = f2_mul(p0, swap ? a1 : a0);
+        v[e | B] = f2_mul(p1, swap ? a0 : a1);
+    }
+}
+
+template <int U, int P0, int P1>
+__device__ __forceinline__ void rp_perm2(F2* v, const float* m) {
+    constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
+    const float p0 = m[0], p1 = m[1], p2 = m[2], p3 = m[3];
+    const int s0 = (int)m[4], s1 = (int)m[5], s2 = (int)m[6], s3 = (int)m[7];
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) {
+        if (e & (B0 | B1)) continue;
+        const F2 a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+        v[e] = f2_mul(p0, pick4(a0, a1, a2, a3, s0));
+        v[e | B1] = f2_mul(p1, pick4(a0, a1, a2, a3, s1));
+        v[e | B0] = f2_mul(p2, pick4(a0, a1, a2, a3, s2));
+        v[e | B0 | B1] = f2_mul(p3, pick4(a0, a1, a2, a3, s3));
+    }
+}
+
+template <int U>
+__device__ __forceinline__ void rp_diagb(F2* v, const float* m) {
+    if constexpr (((1 << U) * 4) % 16 == 0) {
+        float mm[1 << U];
+        ldv<float, (1 << U)>(m, mm);
+#pragma unroll
+        for (int e = 0; e < (1 << U); ++e) v[e] = f2_mul(mm[e], v[e]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < (1 << U); ++e) v[e] = f2_mul(m[e], v[e]);
+    }
+}
+
+template <int U>
+__device__ __forceinline__ void rp_scale(F2* v, const float* m) {
+    const float f = m[0];
+#pragma unroll
+    for (int e = 0; e < (1 << U); ++e) v[e] = f2_mul(f, v[e]);
+}
+
 // the branch matrix a member's uniform picks from a mixture channel, or nullptr for identity
 template <typename T>
 __device__ __forceinline__ const T* mixture_pick(const TileOp& op, const T* m, double u) {

@@ -55,6 +55,21 @@ def test_pauli_transfer_program(precision, n, monkeypatch):
     assert np.array_equal(got, want), f"max difference {np.max(np.abs(got - want))}"
 
 
+@pytest.mark.parametrize("variant", [{"LSG_FFMA2": "1"}, {"LSG_FFMA2": "0"}, {"LSG_JIT_SPILL": "0"}, {"LSG_JIT_SPILL": "1"}])
+def test_benchmark_shape_code_variants(variant, monkeypatch):
+    """The benchmark's circuit (12 qubits, 12 layers) as a real32 Pauli-transfer program: packed
+    group pairs (fma.rn.f32x2) or not, passes that spill rebuilt for fewer CTAs per SM or not —
+    every variant gives the interpreter's register bit for bit."""
+    for k, v in variant.items():
+        monkeypatch.setenv(k, v)
+    c = parse(wl.brickwork(12, 12, seed=12, measure=False))
+    ops = engine.ptm_oplist(c, wl.dm_noise_instances(2, seed=9))
+    start = np.random.default_rng(9).normal(size=(2, 1 << 24))
+    want = _run(24, _lib.R32, 2, ops, start, False, monkeypatch)
+    got = _run(24, _lib.R32, 2, ops, start, True, monkeypatch)
+    assert np.array_equal(got, want), f"max difference {np.max(np.abs(got - want))}"
+
+
 def _from_basis_pair(nbits, precision, batch, ops, index, jit, monkeypatch):
     monkeypatch.setenv("LSG_JIT", "1" if jit else "0")
     with _lib.Register(nbits, precision, batch) as a, _lib.Register(nbits, precision, batch) as b:

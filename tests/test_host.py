@@ -297,13 +297,35 @@ def test_specialized_pass_source_compiles():
     c = parse(wl.brickwork(7, 2, seed=3, measure=False))
     ptm = engine.ptm_oplist(c, wl.dm_noise_instances(2, seed=3))
     src = _lib.specialized_source(14, _lib.R32, 2, ptm, compile=True)
-    assert "rb_tpd2<float" in src and "ld_split<float>" in src and "lsg_pass_0" in src
+    unpacked = "rb_tpd2<float" in src and "ld_split<float>" in src
+    packed = "rp_tpd2<" in src and "ld_f2(" in src  # LSG_FFMA2=1
+    assert (unpacked or packed) and "lsg_pass_0" in src
     sv = engine.sv_oplist(parse(wl.brickwork(14, 2, seed=3, measure=False)))
     src = _lib.specialized_source(14, _lib.C64, 1, sv, compile=True)
     assert "lsg::Cx<float>" in src
     wide = _lib.OpList()
     wide.add(_lib.OP_MATRIX, [0, 1, 2, 3, 4], np.eye(32, dtype=complex))
     assert _lib.specialized_source(14, _lib.C64, 1, wide) == ""
+
+
+def test_packed_pair_source_compiles(monkeypatch):
+    """With LSG_FFMA2=1 real32 group pairs are generated as packed 64-bit operands (fma.rn.f32x2)
+    and still compile; the unpacked and packed sources load the same addresses."""
+    from lucivant_sim_gb300.qasm import parse
+
+    c = parse(wl.brickwork(7, 3, seed=4, measure=False))
+    ptm = engine.ptm_oplist(c, wl.dm_noise_instances(2, seed=5))
+    monkeypatch.setenv("LSG_FFMA2", "0")
+    plain = _lib.specialized_source(14, _lib.R32, 2, ptm)
+    monkeypatch.setenv("LSG_FFMA2", "1")
+    packed = _lib.specialized_source(14, _lib.R32, 2, ptm, compile=True)
+    assert "rp_tpd2<" in packed and "ld_f2(" in packed and "ld_split<" not in packed
+    assert "ld_split<float>" in plain and "rp_" not in plain
+    addr = re.compile(r"tile \+ \(([^)]*)\)")
+    assert sorted(addr.findall(plain)) == sorted(addr.findall(packed))
+    # complex registers are never packed
+    sv = engine.sv_oplist(parse(wl.brickwork(14, 2, seed=3, measure=False)))
+    assert "rp_" not in _lib.specialized_source(14, _lib.C64, 1, sv)
 
 
 def test_format_bits_many_matches_format_bits():
