@@ -410,7 +410,7 @@ int jit_mode() {
 bool jit_packed(int precision) {
     if (precision != LSG_R32) return false;
     const char* env = getenv("LSG_FFMA2");
-    return env && env[0] == '1';
+    return !(env && env[0] == '0');
 }
 
 bool jit_wanted(int64_t bytes_per_run) {

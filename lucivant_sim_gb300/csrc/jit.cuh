@@ -32,7 +32,7 @@ struct JitPasses {
 // so of compilation is recovered within a few dozen runs).
 int jit_mode();
 bool jit_wanted(int64_t bytes_per_run);
-// Whether real32 group pairs run as packed 64-bit operands (fma.rn.f32x2; LSG_FFMA2=1).
+// Whether real32 group pairs run as packed 64-bit operands (fma.rn.f32x2; LSG_FFMA2=0: never).
 bool jit_packed(int precision);
 
 // The CUDA source of a planned gate program's specialized passes, or "" when a pass can't be.

@@ -59,7 +59,7 @@ def test_pauli_transfer_program(precision, n, monkeypatch):
 def test_benchmark_shape_code_variants(variant, monkeypatch):
     """The benchmark's circuit (12 qubits, 12 layers) as a real32 Pauli-transfer program: packed
     group pairs (fma.rn.f32x2) or not, passes that spill rebuilt for fewer CTAs per SM or not —
-    every variant gives the interpreter's register bit for bit."""
+    every variant gives the interpreter's register bit for bit (defaults: packed, rebuilt)."""
     for k, v in variant.items():
         monkeypatch.setenv(k, v)
     c = parse(wl.brickwork(12, 12, seed=12, measure=False))

@@ -298,7 +298,7 @@ def test_specialized_pass_source_compiles():
     ptm = engine.ptm_oplist(c, wl.dm_noise_instances(2, seed=3))
     src = _lib.specialized_source(14, _lib.R32, 2, ptm, compile=True)
     unpacked = "rb_tpd2<float" in src and "ld_split<float>" in src
-    packed = "rp_tpd2<" in src and "ld_f2(" in src  # LSG_FFMA2=1
+    packed = "rp_tpd2<" in src and "ld_f2(" in src  # the default; unpacked with LSG_FFMA2=0
     assert (unpacked or packed) and "lsg_pass_0" in src
     sv = engine.sv_oplist(parse(wl.brickwork(14, 2, seed=3, measure=False)))
     src = _lib.specialized_source(14, _lib.C64, 1, sv, compile=True)
@@ -309,8 +309,8 @@ def test_specialized_pass_source_compiles():
 
 
 def test_packed_pair_source_compiles(monkeypatch):
-    """With LSG_FFMA2=1 real32 group pairs are generated as packed 64-bit operands (fma.rn.f32x2)
-    and still compile; the unpacked and packed sources load the same addresses."""
+    """Real32 group pairs are generated as packed 64-bit operands (fma.rn.f32x2), or unpacked with
+    LSG_FFMA2=0; both compile and load the same addresses."""
     from lucivant_sim_gb300.qasm import parse
 
     c = parse(wl.brickwork(7, 3, seed=4, measure=False))
