@@ -19,7 +19,7 @@ constexpr int kPipeThreadsHost = 288;
 struct JitPasses {
     std::vector<void*> fns;      // CUfunction per pass
     std::vector<int> per_sm;     // resident CTAs per SM of each pass at its shared memory
-    bool swz = false;            // tiles move by swizzled tensor copies (common.cuh tma_load_box)
+    bool swz = false;            // tiles move by swizzled tensor copies (common.cuh Tmap)
     std::vector<void*> modules;  // CUmodule per compiled unit
     JitPasses() = default;
     JitPasses(const JitPasses&) = delete;

@@ -428,3 +428,31 @@ def test_gate_errors_over_many_models_match_each_model():
         want = [None if m is None else m.gate_error(name, qubits) for m in models]
         got = lookup(name, qubits)
         assert all(a is b for a, b in zip(got, want)), (name, qubits)
+
+
+def test_cli_arguments_and_errors_without_a_device(tmp_path, capsys):
+    """The command-line front end: version, argument errors and program errors are reported
+    before any device work, with Orrery's exit codes and wording."""
+    from lucivant_sim_gb300 import cli
+
+    with pytest.raises(SystemExit) as stop:
+        cli.main(["--version"])
+    assert stop.value.code == 0 and capsys.readouterr().out.startswith("lucivant-sim 0.3.0")
+    bad = tmp_path / "bad.qasm"
+    bad.write_text("OPENQASM 3; qubit q; nope q;")
+    assert cli.main(["run", str(bad)]) == 2
+    assert "unknown gate 'nope'" in capsys.readouterr().err
+    assert cli.main(["state", str(tmp_path / "missing.qasm")]) == 2
+    assert capsys.readouterr().err.startswith("lucivant-sim: ")
+    with pytest.raises(SystemExit) as stop:
+        cli.main(["run", str(bad), "--param", "theta"])
+    assert "--param needs name=value" in str(stop.value.code)
+    with pytest.raises(SystemExit):
+        cli.main(["run", str(bad), "--method", "no_such_method"])
+    capsys.readouterr()
+    args = cli.build_parser().parse_args(["run", "x.qasm", "--two", "0.02"])
+    nm = cli.noise_of(args)
+    assert nm is not None and nm.gate_error("cx", (0, 1)) is not None and nm.gate_error("h", (0,)) is None
+    assert cli.noise_of(cli.build_parser().parse_args(["run", "x.qasm"])) is None
+    assert cli.parse_params(["a=0.5", " b =2"]) == {"a": 0.5, "b": 2.0}
+    assert cli.bar(0.5) == "█" * 16 and cli.bar(0.0) == ""
