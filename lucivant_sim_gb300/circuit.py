@@ -87,18 +87,25 @@ class Register:
     size: int
 
 
-_JSON_CACHE: dict[bytes, list[list[list[float]]]] = {}
+_JSON_CACHE: dict[bytes, tuple[list[list[list[float]]], str]] = {}
 
 
-def _matrix_entries(matrix: np.ndarray) -> list[list[list[float]]]:
+def _matrix_json(matrix: np.ndarray) -> tuple[list[list[list[float]]], str]:
+    """A matrix's canonical entries (rounded to 12 decimals, [re, im] pairs) and their compact
+    JSON text, cached by the matrix's bytes (every cx of a circuit shares one entry)."""
     key = np.ascontiguousarray(matrix).tobytes()
     hit = _JSON_CACHE.get(key)
     if hit is None:
         rounded = np.round(np.asarray(matrix, dtype=np.complex128), 12) + 0.0  # folds -0.0 into 0.0
-        hit = [[[float(v.real), float(v.imag)] for v in row] for row in rounded]
+        entries = [[[float(v.real), float(v.imag)] for v in row] for row in rounded]
+        hit = (entries, json.dumps(entries, separators=(",", ":")))
         if len(_JSON_CACHE) < 8192:
             _JSON_CACHE[key] = hit
     return hit
+
+
+def _matrix_entries(matrix: np.ndarray) -> list[list[list[float]]]:
+    return _matrix_json(matrix)[0]
 
 
 def _op_record(op: Any) -> object:
@@ -229,9 +236,25 @@ class Circuit:
             "ops": [_op_record(o) for o in self.operations],
         }
 
+    def canonical_text(self) -> str:
+        """``json.dumps(self.canonical(), separators=(",", ":"), sort_keys=True)``, assembled from
+        cached per-matrix texts: the records are lists (only the top level is a dict, written in
+        sorted key order), so joining the parts' compact texts gives the same characters."""
+        parts = []
+        for op in self.operations:
+            if op.kind == "gate":
+                qubits = ",".join(str(int(q)) for q in op.qubits)
+                parts.append(f'["g",[{qubits}],{_matrix_json(op.matrix)[1]}]')
+            else:
+                parts.append(json.dumps(_op_record(op), separators=(",", ":"), sort_keys=True))
+        cregs = json.dumps([[r.name, r.offset, r.size] for r in self.cregs], separators=(",", ":"))
+        return (
+            f'{{"clbits":{json.dumps(self.num_clbits)},"cregs":{cregs},"ops":[{",".join(parts)}],'
+            f'"qubits":{json.dumps(self.num_qubits)}}}'
+        )
+
     def digest(self) -> str:
-        text = json.dumps(self.canonical(), separators=(",", ":"), sort_keys=True).encode()
-        return "sha256:" + hashlib.sha256(text).hexdigest()
+        return "sha256:" + hashlib.sha256(self.canonical_text().encode()).hexdigest()
 
     def format_bits(self, bits: int) -> str:
         return format_bits(self, bits)

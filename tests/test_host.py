@@ -456,3 +456,22 @@ def test_cli_arguments_and_errors_without_a_device(tmp_path, capsys):
     assert cli.noise_of(cli.build_parser().parse_args(["run", "x.qasm"])) is None
     assert cli.parse_params(["a=0.5", " b =2"]) == {"a": 0.5, "b": 2.0}
     assert cli.bar(0.5) == "█" * 16 and cli.bar(0.0) == ""
+
+
+def test_canonical_text_is_the_sorted_compact_json_of_the_canonical_form():
+    """The digest's text, assembled from cached per-matrix texts, is character for character
+    ``json.dumps(canonical, separators=(",", ":"), sort_keys=True)`` (the form Orrery hashes)."""
+    import json
+
+    sources = [
+        wl.brickwork(12, 6, seed=7),
+        wl.brickwork(6, 2, seed=3, measure=False),
+        wl.midcircuit(8, 3, seed=5),
+        'OPENQASM 3; include "stdgates.inc"; qubit[3] q; bit[2] a; bit[1] b; h q[0]; barrier q; gphase(0.3); '
+        "a[0] = measure q[0]; if (a[0] == 1) { x q[1]; } else { z q[2]; } reset q[0]; b[0] = measure q[2];",
+        'OPENQASM 2.0; include "qelib1.inc"; qreg q[2]; creg c[2]; u3(0.1,0.2,0.3) q[0]; cx q[0],q[1]; measure q -> c;',
+        "OPENQASM 3; qubit[2] q; bit[2] c; U(0.5, -0.0, 1e-13) q[0]; c = measure q;",
+    ]
+    circuits = [ls.parse(s) for s in sources] + [wl.clifford_layers_circuit(16, 2, seed=3)]
+    for c in circuits:
+        assert c.canonical_text() == json.dumps(c.canonical(), separators=(",", ":"), sort_keys=True)
