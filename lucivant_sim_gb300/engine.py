@@ -46,10 +46,12 @@ def precision_code(precision: str | None) -> int:
 
 
 _OFFDIAG: dict[int, np.ndarray] = {}
+_CLASSIFIED: dict[bytes, tuple[int, np.ndarray]] = {}  # multi-qubit matrices (every cx shares one)
 
 
 def classify(m: np.ndarray) -> tuple[int, np.ndarray]:
-    """(kind, data) for a gate matrix: diagonal, phased permutation, or dense."""
+    """(kind, data) for a gate matrix: diagonal, phased permutation, or dense. The data of a
+    multi-qubit matrix is shared between calls with equal matrices: callers only read it."""
     m = np.asarray(m, dtype=np.complex128)
     d = m.shape[0]
     if d == 2:  # the common one-qubit case without array passes
@@ -59,6 +61,16 @@ def classify(m: np.ndarray) -> tuple[int, np.ndarray]:
         if a == 0 and e == 0 and b != 0 and c != 0:
             return OP_PERM, np.array([b, c, 1.0, 0.0], dtype=np.complex128)
         return OP_MATRIX, m
+    key = m.tobytes()
+    hit = _CLASSIFIED.get(key)
+    if hit is None:
+        hit = _classify_wide(m.copy(), d)
+        if len(_CLASSIFIED) < 4096:
+            _CLASSIFIED[key] = hit
+    return hit
+
+
+def _classify_wide(m: np.ndarray, d: int) -> tuple[int, np.ndarray]:
     nz = m != 0
     off = _OFFDIAG.get(d)
     if off is None:
