@@ -176,10 +176,11 @@ def format_bits(circuit: Any, bits: int) -> str:
     )
 
 
-def format_bits_many(circuit: Any, values: np.ndarray) -> list[str]:
-    """:func:`format_bits` of many packed outcomes (int64, fewer than 63 classical bits) at once:
-    the characters of every string are laid out in one byte array."""
-    values = np.asarray(values, dtype=np.int64)
+def format_bits_bytes(circuit: Any, values: np.ndarray) -> np.ndarray:
+    """:func:`format_bits` of many packed outcomes (int64, fewer than 63 classical bits) as one
+    fixed-width byte-string array (``S<width>``; ``S1`` of empty strings when there are no
+    characters): the characters of every string are laid out in one byte array."""
+    values = np.asarray(values, dtype=np.int64).reshape(-1)
     regs = list(reversed(circuit.cregs)) if circuit.cregs else [None]
     cols: list[np.ndarray] = []
     for i, reg in enumerate(regs):
@@ -189,13 +190,16 @@ def format_bits_many(circuit: Any, values: np.ndarray) -> list[str]:
         if size:
             shifts = np.arange(offset + size - 1, offset - 1, -1, dtype=np.int64)  # most significant first
             cols.append((((values[:, None] >> shifts) & 1) + ord("0")).astype(np.uint8))
-    if not cols or values.size == 0:
-        return ["" for _ in range(values.size)] if not cols else []
-    chars = np.ascontiguousarray(np.concatenate(cols, axis=1))
-    width = chars.shape[1]
+    width = sum(c.shape[1] for c in cols)
     if width == 0:
-        return ["" for _ in range(values.size)]
-    return [b.decode() for b in chars.view(f"S{width}").ravel()]
+        return np.zeros(values.size, dtype="S1")
+    chars = np.ascontiguousarray(np.concatenate(cols, axis=1))
+    return chars.view(f"S{width}").ravel()
+
+
+def format_bits_many(circuit: Any, values: np.ndarray) -> list[str]:
+    """:func:`format_bits` of many packed outcomes (int64, fewer than 63 classical bits) at once."""
+    return [b.decode() for b in format_bits_bytes(circuit, values)]
 
 
 @dataclass(frozen=True)

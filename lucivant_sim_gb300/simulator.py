@@ -26,7 +26,7 @@ import numpy as np
 from numpy.typing import NDArray
 
 from lucivant_sim_gb300 import _lib, engine
-from lucivant_sim_gb300.circuit import Circuit, final_measurements, format_bits, format_bits_many
+from lucivant_sim_gb300.circuit import Circuit, final_measurements, format_bits, format_bits_bytes
 from lucivant_sim_gb300.clifford import clifford_problem
 from lucivant_sim_gb300.engine import MAX_DENSITY_QUBITS, SimulationError, pauli_masks
 from lucivant_sim_gb300.qasm import load, parse
@@ -196,18 +196,22 @@ def sample_register(
 
 
 def count_bits(circuit: Any, bits: np.ndarray, clbits: list[int]) -> dict[str, int]:
-    """Pack per-pair outcome bits onto their classical bits and count (``simulator.py:279-284``)."""
+    """Pack per-pair outcome bits onto their classical bits and count (``simulator.py:279-284``);
+    the result is ordered by outcome string, as :class:`Result` keeps its counts."""
     shots = bits.shape[0]
     if circuit.num_clbits > 62:
         keys = [sum(int(bits[s, j]) << c for j, c in enumerate(clbits)) for s in range(shots)]
         values, counts = np.unique(np.array(keys, dtype=object), return_counts=True)
-    else:
-        packed = np.zeros(shots, dtype=np.int64)
-        for j, c in enumerate(clbits):
-            packed |= bits[:, j].astype(np.int64) << c
-        values, counts = np.unique(packed, return_counts=True)
-        return dict(zip(format_bits_many(circuit, values), counts.tolist(), strict=True))
-    return {format_bits(circuit, int(v)): int(n) for v, n in zip(values, counts, strict=True)}
+        return dict(sorted((format_bits(circuit, int(v)), int(n)) for v, n in zip(values, counts, strict=True)))
+    packed = np.zeros(shots, dtype=np.int64)
+    for j, c in enumerate(clbits):
+        packed |= bits[:, j].astype(np.int64) << c
+    values, counts = np.unique(packed, return_counts=True)
+    text = format_bits_bytes(circuit, values)
+    # ASCII byte order is str order; numeric order is already string order for contiguous
+    # registers (then the stable sort is a single pass)
+    order = np.argsort(text, kind="stable")
+    return dict(zip([b.decode() for b in text[order]], counts[order].tolist(), strict=True))
 
 
 def _evolved(circuit: Any, noise: Any, precision: int) -> tuple[_lib.Register, int]:
@@ -275,7 +279,7 @@ def run(
             counts, report = sample_register(reg, circuit, dm, shots, noise, rng)
     elapsed = round(time.perf_counter() - started, 6)
     return Result(
-        counts=dict(sorted(counts.items())),
+        counts=counts if chosen in ("statevector", "density_matrix") else dict(sorted(counts.items())),
         shots=shots,
         seed=seed,
         method=chosen,
