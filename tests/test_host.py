@@ -185,6 +185,15 @@ def test_count_bits_packs_like_orrery():
     from lucivant_sim_gb300.simulator import count_bits
 
     assert count_bits(c, bits, [1, 2]) == {"0 00": 1, "0 10": 1, "1 10": 2}
+    # ordered by outcome string, also where numeric order is not string order (registers
+    # declared out of clbit order)
+    c2 = ls.parse("OPENQASM 3; qubit[4] q; bit[2] a; bit[2] b; a[0] = measure q[0]; a[1] = measure q[1]; "
+                  "b[0] = measure q[2]; b[1] = measure q[3];")
+    rng = np.random.default_rng(3)
+    many = rng.integers(0, 2, (300, 4)).astype(np.uint8)
+    for clbits in ([0, 1, 2, 3], [3, 1, 0, 2]):
+        got = count_bits(c2, many, clbits)
+        assert list(got) == sorted(got) and sum(got.values()) == 300
 
 
 def test_pauli_masks():
