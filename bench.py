@@ -341,10 +341,10 @@ def e2e_upload_bytes(circuit, noises, precision: str) -> int:
     """Host-to-device bytes of one run_density_batch call: the operator table and data pool of
     each batch it evolves (two halves for an even batch)."""
     from lucivant_sim_gb300 import _lib, engine
+    from lucivant_sim_gb300.batch import halves
 
-    parts = [noises[: len(noises) // 2], noises[len(noises) // 2 :]] if len(noises) % 2 == 0 else [noises]
     total = 0
-    for part in parts:
+    for part in halves(noises):
         ops = engine.ptm_oplist(circuit, part) if engine.dm_form(circuit, part) == "ptm" else engine.dm_oplist(circuit, part)
         total += ops.size * 16 + len(ops) * _lib.OP_DTYPE.itemsize
     return total

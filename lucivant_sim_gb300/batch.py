@@ -69,6 +69,14 @@ class DensityBatch:
         self.reg.free()
 
 
+def halves(noises: list[Any], split: bool = True) -> list[list[Any]]:
+    """The batches :func:`run_density_batch` evolves: two equal halves of an even, non-empty
+    batch with ``split``, else the whole batch."""
+    if split and noises and len(noises) % 2 == 0:
+        return [noises[: len(noises) // 2], noises[len(noises) // 2 :]]
+    return [noises]
+
+
 def run_density_batch(
     circuit: Any, noises: list[Any], observables: list[str], precision: str | None = "c64", split: bool = True
 ):
@@ -80,20 +88,20 @@ def run_density_batch(
     device work. Every member's result is the same as in one whole batch (members evolve
     independently). A half that the library would not specialize while the whole batch would be
     (a run of the whole moves twice the bytes) is dropped for the whole batch."""
-    halves = [noises[: len(noises) // 2], noises[len(noises) // 2 :]] if split and len(noises) % 2 == 0 and noises else [noises]
+    parts = halves(noises, split)
     done: list[DensityBatch] = []
     try:
-        first = DensityBatch(circuit, halves[0], precision)
+        first = DensityBatch(circuit, parts[0], precision)
         done.append(first)
-        if len(halves) == 2 and not first.program.specialized:
+        if len(parts) == 2 and not first.program.specialized:
             nominal = first.program.bytes_per_run
             if not _lib.jit_wanted(nominal) and _lib.jit_wanted(2 * nominal):
                 done.pop().free()  # the whole batch would be specialized: run it as one
-                halves = [noises]
+                parts = [noises]
                 first = DensityBatch(circuit, noises, precision)
                 done.append(first)
         first.evolve()
-        for part in halves[1:]:
+        for part in parts[1:]:
             b = DensityBatch(circuit, part, precision)
             done.append(b)
             b.evolve()

@@ -484,3 +484,53 @@ def test_canonical_text_is_the_sorted_compact_json_of_the_canonical_form():
     circuits = [ls.parse(s) for s in sources] + [wl.clifford_layers_circuit(16, 2, seed=3)]
     for c in circuits:
         assert c.canonical_text() == json.dumps(c.canonical(), separators=(",", ":"), sort_keys=True)
+
+
+def test_density_batch_halves_decision(monkeypatch):
+    """run_density_batch's halves, with a stand-in for the device batch: an even batch runs as two
+    halves in member order unless a half would lose the specialization the whole batch gets."""
+    from lucivant_sim_gb300 import batch as batch_mod
+
+    made: list[list[int]] = []
+
+    class FakeProgram:
+        def __init__(self, n, specialized):
+            self.specialized = specialized
+            self.bytes_per_run = 100 * n
+
+    class FakeBatch:
+        specialize_from = 4  # members from which the stand-in policy specializes
+
+        def __init__(self, circuit, noises, precision):
+            made.append(list(noises))
+            self.members = list(noises)
+            self.program = FakeProgram(len(noises), len(noises) >= self.specialize_from)
+
+        def evolve(self):
+            pass
+
+        def probabilities(self):
+            return np.array([[m, m] for m in self.members], dtype=float)
+
+        def expectations(self, labels):
+            return np.array([self.members for _ in labels], dtype=float)
+
+        def free(self):
+            pass
+
+    monkeypatch.setattr(batch_mod, "DensityBatch", FakeBatch)
+    monkeypatch.setattr(_lib, "jit_wanted", lambda nbytes: nbytes >= 400)
+    assert batch_mod.halves([1, 2, 3]) == [[1, 2, 3]] and batch_mod.halves([]) == [[]]
+    assert batch_mod.halves([1, 2, 3, 4], split=False) == [[1, 2, 3, 4]]
+    for members, split, want in [
+        (list(range(8)), True, [[0, 1, 2, 3], [4, 5, 6, 7]]),  # halves stay specialized
+        (list(range(4)), True, [[0, 1], [0, 1, 2, 3]]),  # a half would not be: the whole batch
+        (list(range(2)), True, [[0], [1]]),  # neither would be: halves
+        (list(range(5)), True, [[0, 1, 2, 3, 4]]),  # odd: one batch
+        (list(range(8)), False, [[0, 1, 2, 3, 4, 5, 6, 7]]),
+    ]:
+        made.clear()
+        probs, exps = batch_mod.run_density_batch(None, members, ["Z", "ZZ"], split=split)
+        assert made == want
+        assert probs[:, 0].tolist() == members and exps.shape == (2, len(members))
+        assert exps[0].tolist() == members
