@@ -337,7 +337,7 @@ def config_block(args: argparse.Namespace) -> dict:
 # ------------------------------------------------------------------------------ GPU arm
 
 
-def e2e_upload_bytes(circuit, noises, precision: str) -> int:
+def e2e_upload_bytes(circuit, noises) -> int:
     """Host-to-device bytes of one run_density_batch call: the operator table and data pool of
     each batch it evolves (two halves for an even batch)."""
     from lucivant_sim_gb300 import _lib, engine
@@ -469,7 +469,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     from lucivant_sim_gb300 import engine
 
     # operator tables and data pools (one per half the call evolves), Pauli masks
-    h2d = int(e2e_upload_bytes(circuit, noises, args.precision) + 2 * 8 * len(labels))
+    h2d = int(e2e_upload_bytes(circuit, noises) + 2 * 8 * len(labels))
     d2h = int(probs_h.nbytes + exps_h.nbytes)
 
     if rank == 0:
