@@ -65,6 +65,7 @@ def classify(m: np.ndarray) -> tuple[int, np.ndarray]:
     hit = _CLASSIFIED.get(key)
     if hit is None:
         hit = _classify_wide(m.copy(), d)
+        hit[1].setflags(write=False)  # shared between callers
         if len(_CLASSIFIED) < 4096:
             _CLASSIFIED[key] = hit
     return hit
