@@ -534,3 +534,23 @@ def test_density_batch_halves_decision(monkeypatch):
         assert made == want
         assert probs[:, 0].tolist() == members and exps.shape == (2, len(members))
         assert exps[0].tolist() == members
+
+
+def test_public_header_is_plain_c(tmp_path):
+    """include/lsg.h compiles as C99 with warnings as errors (the boundary has no C++ or torch
+    types), and a C program links against the library's exported names."""
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    names = sorted(declared_functions())
+    src = tmp_path / "use.c"
+    body = "\n".join(f"    (void)&{n};" for n in names)
+    src.write_text(f'#include "lsg.h"\nint main(void) {{\n{body}\n    return 0;\n}}\n')
+    lib = Path(_lib.library()._name)
+    cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"), str(src), "-o",
+           str(tmp_path / "use"), "-L", str(lib.parent), "-l:" + lib.name]
+    done = subprocess.run(cmd, capture_output=True, text=True)
+    assert done.returncode == 0, done.stderr
