@@ -10,8 +10,9 @@ qubit most significant, Y as x = z = 1 — and the refusal messages follow
 from __future__ import annotations
 
 import itertools
+import operator
 from dataclasses import dataclass
-from functools import lru_cache
+from functools import cached_property, lru_cache
 from typing import Any
 
 import numpy as np
@@ -161,27 +162,103 @@ def all_gates(ops: Any) -> list[Any]:
     return found
 
 
-def clifford_problem(circuit: Any, noise: Any = None) -> str | None:
+class GateColumns:
+    """Per-gate fields of a long gate list as columns, each read once on first use with C-level
+    iteration (``map`` over ``attrgetter``): names, qubit tuples, arities, matrix identities
+    (gates that share a matrix object share its analysis) and name indices."""
+
+    def __init__(self, gates: list[Any]) -> None:
+        self.gates = gates
+        self.n = len(gates)
+
+    @cached_property
+    def names(self) -> list[str]:
+        return list(map(_NAME, self.gates))
+
+    @cached_property
+    def qubits(self) -> list[tuple[int, ...]]:
+        return list(map(_QUBITS, self.gates))
+
+    @cached_property
+    def arity(self) -> np.ndarray:
+        return np.fromiter(map(len, self.qubits), dtype=np.int64, count=self.n)
+
+    @cached_property
+    def matrix_ids(self) -> np.ndarray:
+        return np.fromiter(map(id, map(_MATRIX, self.gates)), dtype=np.int64, count=self.n)
+
+    @cached_property
+    def matrix_groups(self) -> tuple[np.ndarray, np.ndarray]:
+        """(index of each distinct matrix's first gate, per gate the index of its matrix)."""
+        _u, first, inv = np.unique(self.matrix_ids, return_index=True, return_inverse=True)
+        return first, inv
+
+    @cached_property
+    def name_ids(self) -> np.ndarray:
+        name_id = {name: i for i, name in enumerate(dict.fromkeys(self.names))}
+        return np.fromiter(map(name_id.__getitem__, self.names), dtype=np.int64, count=self.n)
+
+    @cached_property
+    def _flat(self) -> tuple[np.ndarray, np.ndarray]:
+        flat = np.fromiter(itertools.chain.from_iterable(self.qubits), dtype=np.int64, count=int(self.arity.sum()))
+        start = np.concatenate(([0], np.cumsum(self.arity)[:-1])).astype(np.int64)
+        return flat, start
+
+    def position(self, j: int) -> np.ndarray:
+        """Qubit j of every gate as int16 (0 where a gate has fewer than j + 1 qubits)."""
+        flat, start = self._flat
+        has = self.arity > j
+        at = np.where(has, start + j, 0)
+        vals = flat[at] if flat.size else np.zeros_like(at)
+        return np.where(has, vals, 0).astype(np.int16)
+
+
+_NAME = operator.attrgetter("name")
+_QUBITS = operator.attrgetter("qubits")
+_MATRIX = operator.attrgetter("matrix")
+
+
+def first_index(keys: list[Any]) -> dict[Any, int]:
+    """Each distinct key with the index of its first occurrence, in order of first occurrence."""
+    n = len(keys)
+    earliest = dict(zip(reversed(keys), range(n - 1, -1, -1)))  # the last write is the first index
+    return dict(sorted(earliest.items(), key=lambda kv: kv[1]))
+
+
+def clifford_problem(circuit: Any, noise: Any = None, gates: list[Any] | None = None,
+                     cols: GateColumns | None = None) -> str | None:
     """Why the stabilizer engine can't run ``circuit`` exactly, or None."""
     if circuit.num_qubits > MAX_STABILIZER_QUBITS:
         return f"it has {circuit.num_qubits} qubits; the stabilizer engine allows up to {MAX_STABILIZER_QUBITS}"
-    # circuits repeat their gate matrices and noise rules: check each distinct one once
-    by_arity = noise is not None and all(r.qubits is None for r in getattr(noise, "rules", []))
-    seen_matrix: set[int] = set()
-    seen_noise: set[tuple] = set()
-    for g in all_gates(circuit.operations):
-        if id(g.matrix) not in seen_matrix:
-            if clifford_map(g.matrix) is None:
-                return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
-            seen_matrix.add(id(g.matrix))
-        if noise:
-            key = (g.name, len(g.qubits)) if by_arity else (g.name, tuple(g.qubits))
-            if key in seen_noise:
-                continue
-            seen_noise.add(key)
-            ch = noise.gate_error(g.name, g.qubits)
+    # circuits repeat their gate matrices and noise rules: check each distinct one once, at its
+    # first gate; the problem reported is the one at the earliest gate (a gate's matrix before
+    # its noise), as a walk over the gates in order would find it
+    gates = all_gates(circuit.operations) if gates is None else gates
+    if not gates:
+        return None
+    cols = GateColumns(gates) if cols is None else cols
+    firsts = cols.matrix_groups[0]
+    bad_matrix = next((int(i) for i in np.sort(firsts) if clifford_map(gates[int(i)].matrix) is None), None)
+    bad_noise, bad_channel = None, None
+    if noise:
+        by_arity = all(r.qubits is None for r in getattr(noise, "rules", []))
+        if by_arity:
+            _k, kfirst = np.unique(cols.name_ids * 64 + cols.arity, return_index=True)
+            candidates = [int(i) for i in np.sort(kfirst)]
+        else:
+            candidates = list(first_index(list(zip(cols.names, cols.qubits))).values())
+        for i in candidates:
+            if bad_matrix is not None and i > bad_matrix:
+                break
+            ch = noise.gate_error(gates[i].name, gates[i].qubits)
             if ch is not None and pauli_noise(ch) is None:
-                return f"the {ch.name} noise after {g.name} isn't a Pauli channel"
+                bad_noise, bad_channel = i, ch
+                break
+    if bad_matrix is not None and (bad_noise is None or bad_matrix <= bad_noise):
+        g = gates[bad_matrix]
+        return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
+    if bad_noise is not None:
+        return f"the {bad_channel.name} noise after {gates[bad_noise].name} isn't a Pauli channel"
     return None
 
 

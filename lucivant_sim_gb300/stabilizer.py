@@ -16,7 +16,15 @@ import numpy as np
 
 from lucivant_sim_gb300 import _lib
 from lucivant_sim_gb300._lib import SimulationError, check, library, ptr
-from lucivant_sim_gb300.clifford import all_gates, clifford_map, clifford_problem, kind_of, pauli_noise
+from lucivant_sim_gb300.clifford import (
+    GateColumns,
+    all_gates,
+    clifford_map,
+    clifford_problem,
+    first_index,
+    kind_of,
+    pauli_noise,
+)
 
 CODES = {"id": 0, "h": 1, "s": 2, "sdg": 3, "x": 4, "y": 5, "z": 6, "cx": 7, "cz": 8}
 
@@ -129,28 +137,28 @@ class Encoder:
         self.noise_of[id(ch)] = (ch, idx)
         return idx
 
-    def encode(self, gates: list[Any], with_noise: bool) -> np.ndarray:
+    def encode(self, gates: list[Any], with_noise: bool, cols: GateColumns | None = None) -> np.ndarray:
         n = len(gates)
         out = np.zeros(n, dtype=CGATE)
-        # each distinct matrix and noise key once; per gate only attribute reads into NumPy arrays
-        ids = np.fromiter((id(g.matrix) for g in gates), dtype=np.int64, count=n)
-        _u, first, inv = np.unique(ids, return_index=True, return_inverse=True)
+        if n == 0:
+            return out
+        # each distinct matrix and noise key once; per gate only C-level attribute reads
+        # (map / attrgetter) into NumPy arrays
+        cols = GateColumns(gates) if cols is None else cols
+        first, inv = cols.matrix_groups
         codes = np.array([self.gate_code(gates[int(f)]) for f in first], dtype=np.int32).reshape(-1, 2)
         out["code"], out["nq"] = codes[inv, 0], codes[inv, 1]
-        qs = [g.qubits for g in gates]
-        out["a"] = np.fromiter((q[0] for q in qs), dtype=np.int16, count=n)
-        out["b"] = np.fromiter((q[1] if len(q) > 1 else 0 for q in qs), dtype=np.int16, count=n)
-        out["c"] = np.fromiter((q[2] if len(q) > 2 else 0 for q in qs), dtype=np.int16, count=n)
+        out["a"], out["b"], out["c"] = cols.position(0), cols.position(1), cols.position(2)
         if not with_noise:
             out["noise"] = -1
         elif self.by_arity:  # rules by gate name only: key (name, arity)
-            name_id: dict[str, int] = {}
-            nid = np.fromiter((name_id.setdefault(g.name, len(name_id)) for g in gates), dtype=np.int64, count=n)
-            _k, kfirst, kinv = np.unique(nid * 8 + out["nq"], return_index=True, return_inverse=True)
+            _k, kfirst, kinv = np.unique(cols.name_ids * 8 + out["nq"], return_index=True, return_inverse=True)
             idx = np.array([self.noise_code(gates[int(f)]) for f in kfirst], dtype=np.int16)
             out["noise"] = idx[kinv]
-        else:
-            out["noise"] = [self.noise_code(g) for g in gates]
+        else:  # (name, qubits) keys: each distinct one looked up once
+            keys = list(zip(cols.names, cols.qubits))
+            code_of = {k: self.noise_code(gates[i]) for k, i in first_index(keys).items()}
+            out["noise"] = np.fromiter(map(code_of.__getitem__, keys), dtype=np.int16, count=n)
         return out
 
     def table_bytes(self) -> np.ndarray:
@@ -267,16 +275,17 @@ def _has_gate_noise(gates: list[Any], noise: Any) -> bool:
 
 def run_counts(circuit: Any, shots: int, noise: Any, rng: np.random.Generator) -> dict[int, int]:
     """Counts keyed by the classical bits as an integer (bit c = classical bit c)."""
-    problem = clifford_problem(circuit, noise)
+    gates = all_gates(circuit.operations)
+    cols = GateColumns(gates)  # read once, shared by the Clifford check and the encoder
+    problem = clifford_problem(circuit, noise, gates, cols)
     if problem:
         raise SimulationError(f"the stabilizer method runs Clifford circuits only: {problem}")
     n = circuit.num_qubits
-    gates = all_gates(circuit.operations)
     if shots == 0 or circuit.num_clbits == 0:
         if n > 0 and not circuit.is_dynamic() and not _has_gate_noise(gates, noise):
             enc = Encoder(None)
             t = Tableau(n)
-            t.apply(enc.encode(gates, False), enc)
+            t.apply(enc.encode(gates, False, cols), enc)
             t.free()
         return {}
     if circuit.is_dynamic():
@@ -284,11 +293,12 @@ def run_counts(circuit: Any, shots: int, noise: Any, rng: np.random.Generator) -
 
         return stabilizer_shots.per_shot(circuit, shots, noise, rng)
     if _has_gate_noise(gates, noise):
-        return frames(circuit, shots, noise, rng, gates)
-    return sampled(circuit, shots, noise, rng, gates)
+        return frames(circuit, shots, noise, rng, gates, cols)
+    return sampled(circuit, shots, noise, rng, gates, cols)
 
 
-def frames(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gates: list[Any] | None = None) -> dict[int, int]:
+def frames(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gates: list[Any] | None = None,
+           cols: GateColumns | None = None) -> dict[int, int]:
     """Pauli frames for a static circuit with Pauli gate noise (``stabilizer.py:514-563``)."""
     lib = _lib_stab()
     n = circuit.num_qubits
@@ -298,7 +308,7 @@ def frames(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gates
         return {}
     measured = sorted({q for q, _ in pairs})
     enc = Encoder(noise)
-    cg = enc.encode(gates, True)
+    cg = enc.encode(gates, True, cols)
     tables = enc.table_bytes()
     tab = Tableau(n)
     try:
@@ -319,7 +329,8 @@ def frames(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gates
     return _count(bits)
 
 
-def sampled(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gates: list[Any] | None = None) -> dict[int, int]:
+def sampled(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gates: list[Any] | None = None,
+            cols: GateColumns | None = None) -> dict[int, int]:
     """Ideal static circuit: x0 plus random basis combinations (``stabilizer.py:597-619``)."""
     lib = _lib_stab()
     n = circuit.num_qubits
@@ -329,7 +340,7 @@ def sampled(circuit: Any, shots: int, noise: Any, rng: np.random.Generator, gate
         return {}
     measured = sorted({q for q, _ in pairs})
     enc = Encoder(None)
-    cg = enc.encode(gates, False)
+    cg = enc.encode(gates, False, cols)
     tab = Tableau(n)
     try:
         tab.apply(cg, enc)

@@ -554,3 +554,49 @@ def test_public_header_is_plain_c(tmp_path):
            str(tmp_path / "use"), "-L", str(lib.parent), "-l:" + lib.name]
     done = subprocess.run(cmd, capture_output=True, text=True)
     assert done.returncode == 0, done.stderr
+
+
+def _clifford_problem_walk(circuit, noise):
+    """The Clifford check as a plain walk over the gates in order (the first problem found)."""
+    from lucivant_sim_gb300.clifford import all_gates, clifford_map, pauli_noise
+
+    for g in all_gates(circuit.operations):
+        if clifford_map(g.matrix) is None:
+            return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
+        ch = noise.gate_error(g.name, g.qubits) if noise else None
+        if ch is not None and pauli_noise(ch) is None:
+            return f"the {ch.name} noise after {g.name} isn't a Pauli channel"
+    return None
+
+
+def test_clifford_check_and_encoder_columns():
+    """The columnar Clifford check reports the problem a walk over the gates finds first; the
+    encoder's columns give every gate's qubits."""
+    from lucivant_sim_gb300 import stabilizer as st
+    from lucivant_sim_gb300.clifford import GateColumns, clifford_problem
+    from lucivant_sim_gb300.noise import amplitude_damping, pauli_channel
+
+    head = 'OPENQASM 3; include "stdgates.inc"; qubit[4] q; bit[4] c; '
+    programs = [
+        head + "h q[0]; cx q[0], q[1]; s q[2]; c = measure q;",
+        head + "h q[0]; t q[1]; cx q[0], q[1]; rx(0.3) q[2];",
+        head + "h q[0]; x q[3]; t q[1];",
+        head + "x q[2]; ccx q[0], q[1], q[2]; h q[1];",
+    ]
+    models = [
+        None,
+        NoiseModel().add_gate_error(depolarizing(1e-3)),
+        NoiseModel().add_gate_error(amplitude_damping(0.1), gates="x"),
+        NoiseModel().add_gate_error(amplitude_damping(0.1), qubits=[1]).add_gate_error(pauli_channel({"Z": 0.1}), gates="h"),
+        NoiseModel().add_gate_error(amplitude_damping(0.2), gates="h", qubits=[0]),
+    ]
+    for src in programs:
+        c = ls.parse(src)
+        for nm in models:
+            assert clifford_problem(c, nm) == _clifford_problem_walk(c, nm), (src, nm)
+    c = ls.parse(head + "h q[0]; cx q[3], q[1]; ccx q[0], q[1], q[2]; s q[2];")
+    cols = GateColumns(st.all_gates(c.operations))
+    assert cols.position(0).tolist() == [0, 3, 0, 2]
+    assert cols.position(1).tolist() == [0, 1, 1, 0]
+    assert cols.position(2).tolist() == [0, 0, 2, 0]
+    assert cols.names == ["h", "cx", "ccx", "s"] and cols.arity.tolist() == [1, 2, 3, 1]
