@@ -508,8 +508,8 @@ struct Loaded {
     int local = 0;
 };
 
-// LSG_JIT_SPILL: local bytes per thread above which a pass is rebuilt for one CTA fewer per SM
-// (default 64; 0 or less: never).
+// LSG_JIT_SPILL: local bytes per thread above which a pass compiled for three CTAs per SM is
+// rebuilt for two (default 64; 0 or less: never).
 int jit_spill_bytes() {
     const char* env = getenv("LSG_JIT_SPILL");
     return env && env[0] ? atoi(env) : 64;
@@ -610,12 +610,14 @@ std::shared_ptr<JitPasses> jit_build(const Plan& plan, int precision, int ctas, 
         for (size_t i = 0; i < np; ++i) every[i] = i;
         std::vector<Loaded> got(np);
         bool ok = compile_load(kernels, every, plan, eb, swz, got, jp->modules);
-        // A pass whose registers spill at `ctas` CTAs per SM (local memory beyond the threshold:
+        // A pass whose registers spill at three CTAs per SM (local memory beyond the threshold:
         // with three CTAs' tiles in shared memory, spilled values overflow L1 to L2) is compiled
-        // again for one CTA fewer, with more registers per thread, and keeps the smaller spill.
+        // again for two, with more registers per thread, and keeps the smaller spill. Passes
+        // compiled for two CTAs or fewer are kept: one CTA per SM leaves too few warps to cover
+        // the memory latency of the lighter passes.
         const int spill = jit_spill_bytes();
         std::vector<size_t> again;
-        for (size_t i = 0; ok && spill > 0 && ctas > 1 && i < np; ++i)
+        for (size_t i = 0; ok && spill > 0 && ctas >= 3 && i < np; ++i)
             if (got[i].local > spill) again.push_back(i);
         if (ok && !again.empty()) {
             std::vector<std::string> fewer(np);
