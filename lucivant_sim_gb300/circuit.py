@@ -11,6 +11,7 @@ from __future__ import annotations
 import hashlib
 import json
 from dataclasses import dataclass, field
+from functools import cached_property
 from typing import Any, Literal
 
 import numpy as np
@@ -211,11 +212,21 @@ class Circuit:
     cregs: tuple[Register, ...] = ()
     inputs: dict[str, float] = field(default_factory=dict)
 
-    def is_dynamic(self) -> bool:
+    # Both scan every operation; the operations never change, so each is computed once per
+    # circuit (a 2048-qubit Clifford workload holds four million of them).
+    @cached_property
+    def _dynamic(self) -> bool:
         return is_dynamic(self)
 
+    @cached_property
+    def _final(self) -> tuple[tuple[int, int], ...]:
+        return tuple(final_measurements(self))
+
+    def is_dynamic(self) -> bool:
+        return self._dynamic
+
     def final_measurements(self) -> list[tuple[int, int]]:
-        return final_measurements(self)
+        return list(self._final)
 
     def count_ops(self) -> dict[str, int]:
         tally: dict[str, int] = {}
