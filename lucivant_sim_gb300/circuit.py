@@ -222,6 +222,15 @@ class Circuit:
     def _final(self) -> tuple[tuple[int, int], ...]:
         return tuple(final_measurements(self))
 
+    @cached_property
+    def gate_columns(self) -> Any:
+        """Every gate (branches included) and its fields as columns
+        (:class:`lucivant_sim_gb300.clifford.GateColumns`), read once per circuit and shared by the
+        Clifford check and the stabilizer encoder."""
+        from lucivant_sim_gb300.clifford import GateColumns, all_gates
+
+        return GateColumns(all_gates(self.operations))
+
     def is_dynamic(self) -> bool:
         return self._dynamic
 

@@ -218,6 +218,15 @@ _QUBITS = operator.attrgetter("qubits")
 _MATRIX = operator.attrgetter("matrix")
 
 
+def gates_and_columns(circuit: Any) -> tuple[list[Any], GateColumns]:
+    """A circuit's gates and their columns: the circuit's own cached ones when it keeps them,
+    else read here (circuits of other packages)."""
+    cols = getattr(circuit, "gate_columns", None)
+    if not isinstance(cols, GateColumns):
+        cols = GateColumns(all_gates(circuit.operations))
+    return cols.gates, cols
+
+
 def first_index(keys: list[Any]) -> dict[Any, int]:
     """Each distinct key with the index of its first occurrence, in order of first occurrence."""
     n = len(keys)
@@ -233,7 +242,8 @@ def clifford_problem(circuit: Any, noise: Any = None, gates: list[Any] | None = 
     # circuits repeat their gate matrices and noise rules: check each distinct one once, at its
     # first gate; the problem reported is the one at the earliest gate (a gate's matrix before
     # its noise), as a walk over the gates in order would find it
-    gates = all_gates(circuit.operations) if gates is None else gates
+    if gates is None:
+        gates, cols = gates_and_columns(circuit)
     if not gates:
         return None
     cols = GateColumns(gates) if cols is None else cols

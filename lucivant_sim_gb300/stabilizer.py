@@ -22,6 +22,7 @@ from lucivant_sim_gb300.clifford import (
     clifford_map,
     clifford_problem,
     first_index,
+    gates_and_columns,
     kind_of,
     pauli_noise,
 )
@@ -275,8 +276,7 @@ def _has_gate_noise(gates: list[Any], noise: Any) -> bool:
 
 def run_counts(circuit: Any, shots: int, noise: Any, rng: np.random.Generator) -> dict[int, int]:
     """Counts keyed by the classical bits as an integer (bit c = classical bit c)."""
-    gates = all_gates(circuit.operations)
-    cols = GateColumns(gates)  # read once, shared by the Clifford check and the encoder
+    gates, cols = gates_and_columns(circuit)  # read once, shared by the Clifford check and the encoder
     problem = clifford_problem(circuit, noise, gates, cols)
     if problem:
         raise SimulationError(f"the stabilizer method runs Clifford circuits only: {problem}")
