@@ -5,23 +5,24 @@ Workload (one step): 256 noise instances of a 12-qubit, 12-layer u3+cx brickwork
 U[0, 2π) from seed 7), each with thermal relaxation (T1 = 120, T2 = 90, t = 0.05) composed with a
 depolarising one-qubit error ~ U[1e-4, 5e-3] on every u3, depolarising two-qubit error
 ~ U[1e-3, 3e-2] on every cx, evolved as one 256-member register of density matrices in the
-Pauli-transfer form (24-bit registers of real32 coefficients for the complex64 request, 16 GiB),
-from |0><0| through passes compiled for the circuit at run time, then the exact probabilities and
-the 23 observables <Z_i>, <Z_i Z_i+1> of every instance. Inputs are larger than L2 (no flush
-needed).
+Pauli-transfer form from |0><0| through passes compiled for the circuit at run time, then the
+exact probabilities and the 23 observables <Z_i>, <Z_i Z_i+1> of every instance. The default
+precision is the reference's: complex128 requests run the Pauli-transfer register in real64
+(FP64 arithmetic, 32 GiB); ``--precision c64`` runs it in real32 (16 GiB). Both registers are
+larger than L2 (no flush needed).
 
-metric: statevector HBM GB/s — algorithmic HBM bytes of the step (2 x register bytes per fused
-pass, one register write to reset, the reduction reads) per second, whole job; the passes skip
-tiles the circuit has not reached yet, and the roofline counts the bytes they move. Beside it:
-the instances (circuits) per second, the end-to-end rate through the public batched call, and the
-same circuit as a plain complex128 single-instance run on the same GPU ("plain_c128"), with the
-complex64 path's error against it.
+metric: circuits/s — density-matrix instances evolved and reduced per second, whole job. Beside
+it: the HBM bytes the passes move per second, the roofline of the passes (FP64 arithmetic for
+the real64 register, which bounds it on this GPU; HBM for real32), the results of instances 0,
+1, 128 and 255 against Orrery's own (committed fixtures, made by running Orrery), the end-to-end
+rate through the public batched call (host inputs, host results), the complex64 batched run with
+its error, and the plain single-instance complex128 path on the same GPU.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Under torchrun each rank runs its own 256 instances on its own GPU (weak scaling, no data-path
 collective). ``--impl reference`` times the CPU port of Orrery's algorithm (the oracle) on the
-host cores instead, on rank 0 only.
+host cores instead, on rank 0 only, without loading the engine library.
 """
 
 from __future__ import annotations
@@ -29,7 +30,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -41,8 +41,9 @@ sys.path.insert(0, str(ROOT))
 
 QUBITS, LAYERS, SEED, INSTANCES = 12, 12, 7, 256
 FALLBACK_HBM_GBS = 6800.0
-CPU_SAMPLE_U3, CPU_SAMPLE_CX = 4, 2  # oracle ops timed for the CPU baseline (about 10-15 s)
-REF_SAMPLE_U3, REF_SAMPLE_CX = 2, 1  # per worker per step in the reference arm
+GOLDEN_MEMBERS = (0, 1, 128, 255)  # instances with Orrery-made fixtures (tests/golden/configs.*)
+CPU_SAMPLE_U3, CPU_SAMPLE_CX = 3, 2  # whole gate+channel operations timed for the CPU baseline
+REF_BUDGET_S = 120.0  # timed seconds of the reference arm, spread over its steps
 
 
 def parse_args() -> argparse.Namespace:
@@ -51,9 +52,12 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--precision", choices=("c64", "c128"), default="c64")
+    ap.add_argument("--precision", choices=("c128", "c64"), default="c128")
     ap.add_argument("--instances", type=int, default=INSTANCES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c64", action="store_true", help="skip the complex64 batched run beside the headline")
+    ap.add_argument("--ref-full", type=int, default=0, metavar="N",
+                    help="reference arm: evolve N whole instances (one per host process) instead of timed samples")
     ap.add_argument("--workload", choices=("dm-batch", "serve", "sv20", "traj18", "stab2048"), default="dm-batch",
                     help="dm-batch: the batched density-matrix step (default); serve: the served mix; sv20: "
                     "statevector 20q x 20 layers; traj18: trajectories 18q x 16 rounds x 4096 shots; stab2048: "
@@ -61,6 +65,17 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--jobs", type=int, default=400, help="serve: jobs in the served mix")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: offered arrivals per second")
     return ap.parse_args()
+
+
+def _plain(o):
+    """numpy scalars and arrays in a bench line as plain JSON values."""
+    import numpy as np
+
+    if isinstance(o, np.generic):
+        return o.item()
+    if isinstance(o, np.ndarray):
+        return o.tolist()
+    raise TypeError(f"Object of type {type(o).__name__} is not JSON serializable")
 
 
 def dist_info() -> tuple[int, int, int]:
@@ -155,50 +170,80 @@ def measured_peak() -> tuple[float, str]:
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(precision: str) -> float | None:
-    """DRAM bytes per launch of the tile pass, from the committed ncu summary (scaled there to a
-    full-size launch), or None."""
-    path = ROOT / "profiles" / f"tile_pass_dm12_{precision}.md"
-    if not path.exists():
-        return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", path.read_text())
-    return float(m.group(1)) if m else None
+def fp64_peak_tflops() -> float:
+    """FP64 rate of cuBLAS (torch float64 matmul, 4096^3, best of 5) on this GPU: the measured
+    denominator of the real64 passes' arithmetic roofline."""
+    import torch
+
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1000.0)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n**3 / best / 1e12
 
 
 def workload():
+    """The circuit (pure host code: no engine library) and the 23 Z observables."""
     from lucivant_sim_gb300 import qasm, workloads as wl
 
     circuit = qasm.parse(wl.brickwork(QUBITS, LAYERS, seed=SEED, measure=False))
     return circuit, wl.z_observables(QUBITS)
 
 
-def bytes_per_instance(circuit, noises, precision: str) -> tuple[int, int]:
-    """(algorithmic HBM bytes per instance, fused passes) for one evolution plus reductions."""
-    from lucivant_sim_gb300 import _lib, engine
+def load_golden() -> dict:
+    """Orrery's results for instances 0, 1, 128 and 255 of the benchmark (committed fixtures made
+    by running Orrery itself); empty when absent."""
+    import numpy as np
 
-    code = engine.precision_code(precision)
-    if engine.dm_form(circuit, noises[:1]) == "ptm":
-        code = engine.REAL_OF[code]
-        ops = engine.ptm_oplist(circuit, noises[:1])
-        reads = (1 << QUBITS) + 23  # the diagonal Paulis (probabilities), one coefficient per Z term
-    else:
-        ops = engine.dm_oplist(circuit, noises[:1])
-        reads = 24 << QUBITS  # the diagonal, read by probabilities and by each of the 23 Z terms
-    passes = _lib.plan_passes(2 * QUBITS, code, ops)
-    elt = _lib.ELEM_BYTES[code]
-    member = elt << (2 * QUBITS)
-    # 2 x member per pass, 1 x member to reset, and the reduction reads
-    return 2 * member * passes + member + reads * elt, passes
+    meta_path, arr_path = ROOT / "tests" / "golden" / "configs.json", ROOT / "tests" / "golden" / "configs.npz"
+    if not (meta_path.exists() and arr_path.exists()):
+        return {}
+    cases = json.loads(meta_path.read_text())["cases"]
+    out = {}
+    with np.load(arr_path) as data:
+        for m in GOLDEN_MEMBERS:
+            name = f"cfg2_inst{m}"
+            if name in cases and f"{name}_probs" in data.files:
+                out[m] = {"probs": data[f"{name}_probs"], "z": np.asarray(cases[name]["z"])}
+    return out
+
+
+def golden_errors(probs, exps, golden: dict) -> dict:
+    """Max-abs probability and <Z> errors and probability TVD against Orrery, per fixture member."""
+    import numpy as np
+
+    per = {}
+    for m, g in golden.items():
+        if m >= probs.shape[0]:
+            continue
+        per[str(m)] = {
+            "max_abs_probability": float(np.max(np.abs(probs[m] - g["probs"]))),
+            "probability_tvd": 0.5 * float(np.abs(probs[m] - g["probs"]).sum()),
+            "max_abs_z": float(np.max(np.abs(exps[:, m] - g["z"]))),
+        }
+    worst = {k: max(v[k] for v in per.values()) for k in ("max_abs_probability", "probability_tvd", "max_abs_z")} if per else {}
+    return {"members": per, "worst": worst, "against": "Orrery 0.3.0 run on the same instances (tests/golden/configs.*)"}
 
 
 # ------------------------------------------------------------------------------ CPU legs
 
 
-def _oracle_sample(args: tuple[int, int, int]) -> tuple[float, float]:
-    """Time the oracle on the first u3 and cx gate+channel operations of one instance; returns
-    the seconds per u3 operation and per cx operation."""
-    n_u3, n_cx, instance = args
-    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+def _oracle_ops(args: tuple[int, int, int]) -> tuple[float, int, int]:
+    """Evolve operations [start, start + count) (gate then its channel, circuit order, wrapping
+    around) of instance ``instance`` with the oracle on a full-size 12-qubit density matrix from
+    |0><0|; returns (seconds, operations done, operations per circuit). Host code only: the engine
+    library is never loaded here."""
+    instance, start, count = args
     import numpy as np
 
     from lucivant_sim_gb300 import workloads as wl
@@ -207,116 +252,142 @@ def _oracle_sample(args: tuple[int, int, int]) -> tuple[float, float]:
     circuit, _ = workload()
     noise = wl.dm_noise_instances(INSTANCES, seed=SEED)[instance % INSTANCES]
     n = QUBITS
+    gates = [op for op in circuit.operations if op.kind == "gate"]
     rho = np.zeros(1 << (2 * n), dtype=np.complex128)
     rho[0] = 1
-    gates = [op for op in circuit.operations if op.kind == "gate"]
-    u3 = [g for g in gates if len(g.qubits) == 1][:n_u3]
-    cx = [g for g in gates if len(g.qubits) == 2][:n_cx]
-    times = []
-    for group in (u3, cx):
-        t0 = time.perf_counter()
-        for op in group:
-            rho = dense.apply_bits(rho, 2 * n, op.matrix, [n + q for q in op.qubits])
-            rho = dense.apply_bits(rho, 2 * n, op.matrix.conj(), list(op.qubits))
-            ch = noise.gate_error(op.name, op.qubits)
-            if ch is not None:
-                rho = dense.dm_channel(rho, n, ch, op.qubits)
-        times.append((time.perf_counter() - t0) / max(len(group), 1))
-    return times[0], times[1]
+    t0 = time.perf_counter()
+    for j in range(count):
+        op = gates[(start + j) % len(gates)]
+        rho = dense.apply_bits(rho, 2 * n, op.matrix, [n + q for q in op.qubits])
+        rho = dense.apply_bits(rho, 2 * n, op.matrix.conj(), list(op.qubits))
+        ch = noise.gate_error(op.name, op.qubits)
+        if ch is not None:
+            rho = dense.dm_channel(rho, n, ch, op.qubits)
+    return time.perf_counter() - t0, count, len(gates)
 
 
-def _project(t_u3: float, t_cx: float, circuit) -> float:
-    gates = [op for op in circuit.operations if op.kind == "gate"]
-    n1 = sum(1 for g in gates if len(g.qubits) == 1)
-    return n1 * t_u3 + (len(gates) - n1) * t_cx
+def _oracle_instance(instance: int) -> tuple[float, float]:
+    """One whole instance with the oracle (gate, channel, then the probabilities); returns
+    (seconds, probability of |0...0>)."""
+    from lucivant_sim_gb300 import workloads as wl
+    from oracle import dense
+
+    circuit, _ = workload()
+    noise = wl.dm_noise_instances(INSTANCES, seed=SEED)[instance % INSTANCES]
+    t0 = time.perf_counter()
+    probs = dense.probabilities_array(circuit, noise)
+    return time.perf_counter() - t0, float(probs[0])
 
 
-def cpu_baseline(circuit, bytes_inst: int) -> dict:
-    """The oracle (a port of Orrery's algorithm) on one host thread, on a bounded sample."""
+def _mapped_libraries() -> list[str]:
+    """This repository's shared objects mapped into the process (Linux /proc/self/maps)."""
+    try:
+        text = Path("/proc/self/maps").read_text()
+    except OSError:
+        return []
+    return sorted({line.split()[-1] for line in text.splitlines() if line.endswith(".so") and str(ROOT) in line})
+
+
+def cpu_baseline() -> dict:
+    """The oracle (a port of Orrery's algorithm) on one host thread, on a bounded sample: the
+    first u3 and cx gate+channel operations of instance 0, projected to the whole circuit."""
     code = (
         "import sys, json; sys.path.insert(0, %r); import bench; "
-        "print(json.dumps(bench._oracle_sample((%d, %d, 0))))" % (str(ROOT), CPU_SAMPLE_U3, CPU_SAMPLE_CX)
+        "a = bench._oracle_ops((0, 0, %d)); b = bench._oracle_ops((0, 12, %d)); "
+        "print(json.dumps([a, b]))" % (str(ROOT), CPU_SAMPLE_U3, CPU_SAMPLE_CX)
     )
     env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
     t0 = time.perf_counter()
-    proc = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    proc = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
     wall = time.perf_counter() - t0
     if proc.returncode != 0:
-        return {"value": None, "unit": "GB/s", "error": proc.stderr.strip()[-300:]}
-    t_u3, t_cx = json.loads(proc.stdout.strip().splitlines()[-1])
-    per_circuit = _project(t_u3, t_cx, circuit)
+        return {"value": None, "unit": "circuits/s", "error": proc.stderr.strip()[-300:]}
+    (s1, k1, total), (s2, k2, _) = json.loads(proc.stdout.strip().splitlines()[-1])
+    circuit, _ = workload()
+    gates = [op for op in circuit.operations if op.kind == "gate"]
+    n1 = sum(1 for g in gates if len(g.qubits) == 1)
+    per_circuit = n1 * s1 / k1 + (len(gates) - n1) * s2 / k2
     return {
-        "value": bytes_inst / per_circuit / 1e9,
-        "unit": "GB/s",
+        "value": 1.0 / per_circuit,
+        "unit": "circuits/s",
         "cores": 1,
         "kind": "port",
-        "sample": f"oracle density-matrix evolution of instance 0: first {CPU_SAMPLE_U3} u3 and {CPU_SAMPLE_CX} cx "
-        f"gate+channel ops timed ({wall:.1f} s wall), projected to the full circuit "
-        f"({per_circuit:.1f} s per instance, {1 / per_circuit:.4f} circuits/s)",
-        "circuits_per_s": 1 / per_circuit,
+        "sample": f"oracle (port of Orrery's density-matrix algorithm), instance 0 at full size: {k1} u3 and {k2} cx "
+        f"gate+channel operations timed whole ({wall:.1f} s wall), projected to the circuit's {n1} u3 and "
+        f"{len(gates) - n1} cx: {per_circuit:.0f} s per instance",
     }
 
 
 def reference_arm(args: argparse.Namespace) -> None:
+    """The oracle port of Orrery's algorithm on every host core (one process per core, one thread
+    each), on the benchmark's workload. Each step, every process evolves whole gate+channel
+    operations of its own instance at full size; circuits counted = operations done / operations
+    per circuit (a projection from measured whole operations, labelled so). ``--ref-full N``
+    evolves N whole instances instead (no projection). The engine library is not loaded."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     import multiprocessing as mp
 
-    circuit, _ = workload()
-    from lucivant_sim_gb300 import workloads as wl
-
-    noises = wl.dm_noise_instances(INSTANCES, seed=SEED)
-    bytes_inst, _ = bytes_per_instance(circuit, noises, args.precision)
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
     os.environ["OPENBLAS_NUM_THREADS"] = "1"  # inherited by the spawned workers: one thread each
-    with ctx.Pool(cores) as pool:
-        jobs = [(REF_SAMPLE_U3, REF_SAMPLE_CX, i) for i in range(cores)]
-        for _ in range(args.warmup):
-            pool.map(_oracle_sample, jobs)
-        per_step, circuits = [], 0.0
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            res = pool.map(_oracle_sample, jobs)
-            dt = time.perf_counter() - t0
-            # each worker did a fraction of one circuit: fraction = sampled time / projected time
-            frac = sum((REF_SAMPLE_U3 * a + REF_SAMPLE_CX * b) / _project(a, b, circuit) for a, b in res)
-            circuits += frac
-            per_step.append(dt)
-    elapsed = sum(per_step)
-    cps = circuits / elapsed
-    value = cps * bytes_inst / 1e9
-    line = {
+    os.environ["OMP_NUM_THREADS"] = "1"
+    ctx = mp.get_context("spawn")
+    base = {
         "impl": "reference",
-        "metric": "statevector HBM GB/s",
-        "value": value,
-        "unit": "GB/s",
+        "metric": "circuits/s",
+        "unit": "circuits/s",
         "n_gpus": args.gpus,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": 1000 * elapsed / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "c128",
         "data": "synthetic",
         "config": config_block(args),
-        "circuits_per_s": cps,
-        "cpu_baseline": {
-            "value": value,
-            "unit": "GB/s",
-            "cores": cores,
-            "kind": "port",
-            "sample": f"each step: {cores} processes, each evolving the first {REF_SAMPLE_U3} u3 and {REF_SAMPLE_CX} cx "
-            "gate+channel ops of one instance with the oracle; circuits = sampled fraction of the full circuit",
-        },
-        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    if args.ref_full:
+        procs = min(cores, args.ref_full)
+        with ctx.Pool(procs) as pool:
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_instance, range(args.ref_full))
+            wall = time.perf_counter() - t0
+        value = args.ref_full / wall
+        line = dict(base, value=value, steps=1, warmup=0, ms_per_step=1000 * wall,
+                    instance_seconds=[r[0] for r in res],
+                    cpu_baseline={"value": value, "unit": "circuits/s", "cores": procs, "kind": "port",
+                                  "sample": f"{args.ref_full} whole instances on {procs} processes (no projection)"},
+                    e2e={"value": value, "unit": "circuits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    native_so_loaded=_mapped_libraries())  # fmt: skip
+        print(json.dumps(line, default=_plain), flush=True)
+        return
+    with ctx.Pool(cores) as pool:
+        warm = []
+        for w in range(max(args.warmup, 1)):  # one whole operation per process (the first u3, first cx)
+            warm += pool.map(_oracle_ops, [(i, 12 * (w % 2), 1) for i in range(cores)])
+        t_op = statistics.mean(s / max(k, 1) for s, k, _ in warm)
+        per_step = max(1, round(REF_BUDGET_S / max(args.steps, 1) / t_op))
+        step_s, circuits, cursor = [], 0.0, 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_ops, [(i, cursor, per_step) for i in range(cores)])
+            step_s.append(time.perf_counter() - t0)
+            circuits += sum(k / total for _, k, total in res)
+            cursor += per_step
+    elapsed = sum(step_s)
+    value = circuits / elapsed
+    line = dict(base, value=value, steps=args.steps, warmup=args.warmup, ms_per_step=1000 * elapsed / args.steps,
+                cpu_baseline={"value": value, "unit": "circuits/s", "cores": cores, "kind": "port",
+                              "sample": f"each step: {cores} processes (one thread each), each evolving {per_step} whole "
+                              "gate+channel operations of its own instance on a full-size 12-qubit density matrix with "
+                              "the oracle; circuits = operations done / 210 per circuit (a projection from measured "
+                              "whole operations)"},
+                e2e={"value": value, "unit": "circuits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                native_so_loaded=_mapped_libraries())  # fmt: skip
+    print(json.dumps(line, default=_plain), flush=True)
 
 
 def config_block(args: argparse.Namespace) -> dict:
+    elem = 8 if args.precision == "c128" else 4
     return {
         "workload": f"density_matrix {QUBITS}q x {LAYERS} brickwork layers, {args.instances} noise instances per GPU",
         "qubits": QUBITS,
@@ -326,10 +397,10 @@ def config_block(args: argparse.Namespace) -> dict:
         "noise": "thermal_relaxation(120, 90, 0.05) composed with depolarising U[1e-4,5e-3] on u3; "
         "depolarising U[1e-3,3e-2] on cx; readout 2e-2",
         "outputs": "probabilities (2^12) and 23 Z observables per instance",
-        # the workload's gates act on at most two qubits: the Pauli-transfer form, real32 for a
-        # complex64 request (real64 for complex128)
+        # the workload's gates act on at most two qubits: the Pauli-transfer form, real64 for a
+        # complex128 request (real32 for complex64)
         "form": "ptm",
-        "l2": f"register {((4 if args.precision == 'c64' else 8) * args.instances << 24) / 2**30:.0f} GiB > L2: no flush",
+        "l2": f"register {(elem * args.instances << 24) / 2**30:.0f} GiB > L2: no flush",
         "parallelism": f"replicas x{args.gpus} (independent instances per GPU)",
     }
 
@@ -350,6 +421,81 @@ def e2e_upload_bytes(circuit, noises) -> int:
     return total
 
 
+def timed_batch(batch, labels, steps: int, warmup: int, stream, local: int, dist) -> dict:
+    """Warm-up, then ``steps`` timed steps (evolve + expectations + probabilities) bracketed by a
+    barrier and device synchronisation, CUDA events on the register's stream, clocks sampled."""
+    import numpy as np
+    import torch
+
+    def step(timed: list | None = None) -> tuple:
+        if timed is None:
+            batch.evolve()
+        else:
+            timed.append(batch.evolve_timed())
+        return batch.expectations(labels), batch.probabilities()
+
+    for _ in range(warmup):
+        step()
+    batch.reg.sync()
+    dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    pass_ms: list = []
+    torch.cuda.synchronize()
+    t_start.record(stream)
+    for _ in range(steps):
+        exps, probs = step(pass_ms)
+    t_end.record(stream)
+    t_end.synchronize()
+    batch.reg.sync()
+    clock_info = clocks.stop()
+    dist.barrier()
+    elapsed = dist.max(t_start.elapsed_time(t_end) / 1000.0)
+    return {"elapsed": elapsed, "pass_ms": np.stack(pass_ms), "exps": exps, "probs": probs, "clocks": clock_info}
+
+
+def pass_rooflines(batch, pass_ms, real64: bool, fp64_peak: float | None) -> dict:
+    """Per pass and over the evolution: bytes moved and HBM rate (each pass against its own
+    bytes), FP arithmetic rate; the binding roofline of the dominant kernel."""
+    import numpy as np
+
+    info = batch.program.pass_info()
+    med = np.median(pass_ms.astype(np.float64), axis=0)  # ms per pass, median over the timed steps
+    elems = batch.batch << (2 * batch.n)
+    per_pass = []
+    for i, ms in enumerate(med.astype(np.float64).tolist()):
+        gbs = float(info["bytes"][i]) / (ms / 1000) / 1e9
+        tflops = float(info["flops_per_element"][i]) * elems / (ms / 1000) / 1e12
+        per_pass.append({"pass": i, "ms": round(float(ms), 4), "blocks": int(info["blocks"][i]),
+                         "bytes": int(info["bytes"][i]), "hbm_gbs": round(gbs, 1),
+                         "flops_per_element": float(info["flops_per_element"][i]), "tflops": round(tflops, 4)})  # fmt: skip
+    total_s = float(med.sum()) / 1000
+    moved = float(info["bytes"].sum())
+    flops = float(info["flops_per_element"].sum()) * elems
+    peak, peak_kind = measured_peak()
+    hbm = {"bound": "hbm", "achieved": moved / total_s / 1e9, "peak": peak, "unit": "GB/s",
+           "frac": moved / total_s / 1e9 / peak, "bytes_per_launch": moved / len(med),
+           "avg_launch_ms": 1000 * total_s / len(med), "launches": int(pass_ms.size),
+           "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s"}  # fmt: skip
+    arith = {"achieved": flops / total_s / 1e12, "unit": "TFLOP/s", "flops_per_evolution": flops}
+    if real64 and fp64_peak:
+        arith.update(bound="fp64", peak=fp64_peak, frac=flops / total_s / 1e12 / fp64_peak,
+                     peak_source="measured: cuBLAS FP64 matmul 4096^3 on this GPU, best of 5")  # fmt: skip
+    heaviest = max(per_pass, key=lambda p: p["ms"])
+    return {"hbm": hbm, "arith": arith, "per_pass": per_pass, "heaviest_pass": heaviest, "evolve_ms": 1000 * total_s}
+
+
+def _tune_summary(tune: dict | None) -> dict | None:
+    """The autotuner's choice for the bench line: options, whether cached, candidate times."""
+    if not tune:
+        return None
+    cands = [{**c["opts"], "ms": round(c["ms"], 3)} if "ms" in c else {**c["opts"], "error": c.get("error")}
+             for c in tune.get("candidates", [])]  # fmt: skip
+    return {"opts": tune.get("opts"), "cached": tune.get("cached"), "candidates_ms": cands}
+
+
 def gb300_arm(args: argparse.Namespace) -> None:
     rank, world, local = dist_info()
     dist = Dist(world)
@@ -363,80 +509,32 @@ def gb300_arm(args: argparse.Namespace) -> None:
     torch.cuda.set_device(local)
     circuit, labels = workload()
     noises = wl.dm_noise_instances(args.instances, seed=SEED + rank)
-    bytes_inst, passes = bytes_per_instance(circuit, noises, args.precision)
-    bytes_step = bytes_inst * args.instances
+    golden = load_golden() if rank == 0 else {}
+    real64 = args.precision == "c128"
+    fp64_peak = fp64_peak_tflops() if real64 and rank == 0 else None
 
-    batch = DensityBatch(circuit, noises, precision=args.precision)
-    assert batch.program.passes == passes
-    form, upload_bytes, reg_bytes = batch.form, batch.upload_bytes, batch.register_bytes
-    real = batch.reg.real
-    kernel = f"k_tile_pipe<{'float' if args.precision == 'c64' else 'double'}>" if real else \
-        f"k_tile_pipe<Cx<{'float' if args.precision == 'c64' else 'double'}>>"
+    batch = DensityBatch(circuit, noises, precision=args.precision, autotune=True)
+    passes, real = batch.program.passes, batch.reg.real
+    tune = batch.tune
+    kernel = f"k_tile_pipe<{'double' if real64 else 'float'}>" if real else \
+        f"k_tile_pipe<Cx<{'double' if real64 else 'float'}>>"
     specialized = batch.program.specialized
     if specialized:  # the passes run as kernels compiled for this circuit at run time
         kernel = f"lsg_pass_0..{passes - 1} (pipe_kernel specializations of {kernel})"
     stream = torch.cuda.ExternalStream(batch.reg.stream())
-
-    def step(timed: list | None = None) -> tuple:
-        if timed is None:
-            batch.evolve()
-        else:
-            timed.append(batch.evolve_timed())
-        return batch.expectations(labels), batch.probabilities()
-
-    for _ in range(args.warmup):
-        step()
-    batch.reg.sync()
-    dist.barrier()
-    clocks = Clocks(local)
-    clocks.start()
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    pass_ms: list = []
-    torch.cuda.synchronize()
-    t_start.record(stream)
-    for _ in range(args.steps):
-        exps, probs = step(pass_ms)
-    t_end.record(stream)
-    t_end.synchronize()
-    batch.reg.sync()
-    clock_info = clocks.stop()
-    dist.barrier()
-    elapsed = dist.max(t_start.elapsed_time(t_end) / 1000.0)
-    value = bytes_step * args.steps * world / elapsed / 1e9
+    run = timed_batch(batch, labels, args.steps, args.warmup, stream, local, dist)
+    elapsed = run["elapsed"]
     cps = args.instances * args.steps * world / elapsed
+    roof = pass_rooflines(batch, run["pass_ms"], real64, fp64_peak)
+    moved_step = batch.bytes_per_evolve
     # reset, passes, expectations, probabilities (the Pauli-transfer register reduces every member
     # in one launch each; the complex form sums rows in a second launch and runs one per member)
     launches_per_step = 1 + passes + (2 if real else 2 + args.instances)
+    accuracy = golden_errors(run["probs"], run["exps"], golden)
+    exps0, probs0 = run["exps"][:, :1].copy(), run["probs"][:1].copy()
+    batch.free()
 
-    all_pass = np.concatenate(pass_ms)
-    avg_launch_s = float(all_pass.mean()) / 1000.0
-    # bytes the passes actually move: a run from |0><0| skips tiles the circuit has not reached
-    # (still zero), so early passes move less than 2 x register bytes
-    nominal_launch_bytes = 2 * batch.register_bytes
-    moved_per_run = batch.bytes_per_evolve
-    launch_bytes = moved_per_run / passes
-    peak, peak_kind = measured_peak()
-    achieved = launch_bytes / avg_launch_s / 1e9
-    traffic = ncu_traffic(args.precision)
-    roofline = {
-        "kernel": kernel,
-        "bound": "hbm",
-        "achieved": achieved,
-        "peak": peak,
-        "unit": "GB/s",
-        "frac": achieved / peak,
-        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-        "traffic": traffic,
-        "bytes_per_launch": launch_bytes,
-        "nominal_bytes_per_launch": nominal_launch_bytes,
-        "skipped_zero_tile_bytes_frac": 1.0 - moved_per_run / (nominal_launch_bytes * passes),
-        "avg_launch_ms": avg_launch_s * 1000,
-        "launches": int(all_pass.size),
-        "share_of_step": float(all_pass.sum()) / 1000.0 / (elapsed / 1.0) if world == 1 else None,
-    }
-
-    # plain complex128 path on the same GPU: one instance at a time (instance 0)
+    # plain complex128 path on the same GPU: one instance at a time (instance 0), interpreted passes
     plain = DensityBatch(circuit, noises[:1], precision="c128")
     for _ in range(2):
         plain.evolve()
@@ -452,31 +550,61 @@ def gb300_arm(args: argparse.Namespace) -> None:
     plain.reg.sync()
     plain_s = (time.perf_counter() - t0) / reps
     plain.free()
-    tvd = 0.5 * float(np.abs(probs[0] - p_ref[0]).sum())
-    exp_err = float(np.max(np.abs(exps[:, 0] - e_ref[:, 0])))
+    plain_cps = world / plain_s
+
+    # the complex64 request beside it: real32 register, the same instances
+    c64 = None
+    if not args.no_c64 and real64:
+        b32 = DensityBatch(circuit, noises, precision="c64", autotune=True)
+        stream32 = torch.cuda.ExternalStream(b32.reg.stream())
+        r32 = timed_batch(b32, labels, args.steps, args.warmup, stream32, local, dist)
+        roof32 = pass_rooflines(b32, r32["pass_ms"], False, None)
+        cps32 = args.instances * args.steps * world / r32["elapsed"]
+        c64 = {
+            "circuits_per_s": cps32,
+            "ms_per_step": 1000 * r32["elapsed"] / args.steps,
+            "dtype": "f32",
+            "fused_passes": b32.program.passes,
+            "autotune": _tune_summary(b32.tune),
+            "speedup_vs_plain_c128": cps32 / plain_cps,
+            "speedup_vs_batched_f64": cps32 / cps,
+            "roofline": dict(roof32["hbm"], kernel=f"lsg_pass_0..{b32.program.passes - 1} (real32)",
+                             traffic=None, heaviest_pass=roof32["heaviest_pass"]),  # fmt: skip
+            "per_pass": roof32["per_pass"],
+            "accuracy_vs_orrery": golden_errors(r32["probs"], r32["exps"], golden),
+            "accuracy_vs_gpu_c128": {
+                "probability_tvd": 0.5 * float(np.abs(r32["probs"][0] - probs0[0]).sum()),
+                "max_expectation_error": float(np.max(np.abs(r32["exps"][:, 0] - exps0[:, 0]))),
+            },
+            "clocks": r32["clocks"],
+        }
+        b32.free()
 
     # end to end through the public batched API: host inputs in, host results out, every step
     e2e_steps = max(2, args.steps // 2)
-    batch.free()
     # one untimed call: the halves the call evolves are programs of their own shape (specialized
     # passes compiled once per process, like the whole batch's above)
-    run_density_batch(circuit, noises, labels, precision=args.precision)
+    run_density_batch(circuit, noises, labels, precision=args.precision, autotune=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        probs_h, exps_h = run_density_batch(circuit, noises, labels, precision=args.precision)
+        probs_h, exps_h = run_density_batch(circuit, noises, labels, precision=args.precision, autotune=True)
     e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
-    from lucivant_sim_gb300 import engine
-
     # operator tables and data pools (one per half the call evolves), Pauli masks
     h2d = int(e2e_upload_bytes(circuit, noises) + 2 * 8 * len(labels))
     d2h = int(probs_h.nbytes + exps_h.nbytes)
 
     if rank == 0:
+        if real64:
+            roofline = dict(roof["arith"], kernel=kernel, traffic=None, hbm=roof["hbm"],
+                            heaviest_pass=roof["heaviest_pass"])  # fmt: skip
+        else:
+            roofline = dict(roof["hbm"], kernel=kernel, traffic=None, arith=roof["arith"],
+                            heaviest_pass=roof["heaviest_pass"])  # fmt: skip
         line = {
-            "metric": "statevector HBM GB/s",
-            "value": value,
-            "unit": "GB/s",
+            "metric": "circuits/s",
+            "value": cps,
+            "unit": "circuits/s",
             "n_gpus": world,
             "steps": args.steps,
             "warmup": args.warmup,
@@ -484,33 +612,38 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": ("f32" if args.precision == "c64" else "f64") if real else args.precision,
+            "dtype": ("f64" if real64 else "f32") if real else args.precision,
             "data": "synthetic",
-            "config": dict(config_block(args), form=form),
-            "circuits_per_s": cps,
+            "config": dict(config_block(args), form=batch.form),
+            "hbm_gbs_moved": moved_step * args.steps * world / elapsed / 1e9,
             "fused_passes": passes,
             "specialized_passes": specialized,
+            "autotune": _tune_summary(tune),
+            "accuracy_vs_orrery": accuracy,
             "plain_c128": {
-                "circuits_per_s": world / plain_s,
+                "circuits_per_s": plain_cps,
                 "ms_per_circuit": 1000 * plain_s,
-                "speedup_of_batched": cps / (world / plain_s),
+                "speedup_of_batched": cps / plain_cps,
+                "what": "one instance (instance 0) per run, real64 Pauli-transfer register, interpreted passes",
+                "probability_max_abs_vs_batched": float(np.max(np.abs(p_ref[0] - probs0[0]))),
+                "expectation_max_abs_vs_batched": float(np.max(np.abs(e_ref[:, 0] - exps0[:, 0]))),
             },
-            "accuracy": {"probability_tvd_vs_c128": tvd, "max_expectation_error_vs_c128": exp_err},
             "roofline": roofline,
+            "per_pass": roof["per_pass"],
+            "c64_batched": c64,
             "e2e": {
-                "value": bytes_step * world / e2e_s / 1e9,
-                "unit": "GB/s",
+                "value": args.instances * world / e2e_s,
+                "unit": "circuits/s",
                 "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "circuits_per_s": args.instances * world / e2e_s,
                 "api": "lucivant_sim_gb300.batch.run_density_batch",
             },
             "gpu_launches": launches_per_step * args.steps,
-            "clocks": clock_info,
+            "clocks": run["clocks"],
         }
         if world == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(circuit, bytes_inst)
-        print(json.dumps(line), flush=True)
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line, default=_plain), flush=True)
     dist.close()
 
 
@@ -548,7 +681,8 @@ def serve_arm(args: argparse.Namespace) -> None:
     jobs = wl.served_mix(args.jobs, rate=args.rate, seed=5)
     warm = wl.served_mix(max(args.warmup, 3) * 8, rate=args.rate, seed=99)
     circuits = sum(_circuits(j) for j in jobs)
-    with serve.Server(precision=args.precision) as srv:
+    prec = "c64"  # the served path runs complex64 states
+    with serve.Server(precision=prec) as srv:
         serve.replay(warm, srv, realtime=False)
         clocks = Clocks(local)
         clocks.start()
@@ -590,12 +724,12 @@ def serve_arm(args: argparse.Namespace) -> None:
         "higher_is_better": True,
         "scaling": "replicas only",
         "vs_baseline": None,
-        "dtype": args.precision,
+        "dtype": prec,
         "data": "synthetic",
         "config": {
             "workload": f"served mix: {args.jobs} jobs ({circuits} circuits), widths 8..26, depths 10..100, "
             "30% 8-point HEA sweeps with 20-term Pauli sums, 20% noisy density matrices, 50% sampled (1000 shots)",
-            "precision": args.precision,
+            "precision": prec,
             "offered_rate_jobs_per_s": args.rate,
         },
         "latency_at_offered_rate": {"p50_s": offered["p50_s"], "p99_s": offered["p99_s"],
@@ -609,7 +743,7 @@ def serve_arm(args: argparse.Namespace) -> None:
                      "counts_identical_to_c128": f"{same_counts} of {sum(j['kind'] != 'expect' for j in sample)}"},  # fmt: skip
         "clocks": clock_info,
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_plain), flush=True)
 
 
 # ------------------------------------------------------------------------------ other configurations
@@ -620,7 +754,7 @@ def _line(metric: str, value: float, unit: str, workload: str, dtype: str, **ext
             "scaling": "replicas only", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
             "config": {"workload": workload}}  # fmt: skip
     line.update(extra)
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_plain), flush=True)
 
 
 def sv_arm(args: argparse.Namespace) -> None:

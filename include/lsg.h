@@ -129,6 +129,23 @@ int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float*
 int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run);
 /* Number of fused passes, and algorithmic HBM bytes of one run (2 x register bytes per pass). */
 int lsg_program_info(lsg_program p, int32_t* passes, int64_t* bytes_per_run);
+/* Per pass (cap >= the program's pass count; any output may be NULL): the HBM bytes one
+ * lsg_program_run_from_basis moves (2 x tile bytes per tile visited; all tiles before the first
+ * such run), the floating-point
+ * operations per register element its operators execute (multiply or add 1, fused multiply-add 2),
+ * and its register blocks. Host-side diagnostic for rooflines; no counterpart in the reference. */
+int lsg_program_pass_info(lsg_program p, int32_t cap, int64_t* bytes, double* flops_per_element, int32_t* blocks);
+/* Plan and launch choices of one program (0 in a field: the default for the element type, or
+ * its environment knob). tile_bits: register bits per tile (a tile at most 64 KB); low_bits:
+ * register bits every tile keeps contiguous (runs of at least 16 bytes); ctas: CTAs per SM the
+ * specialized passes are compiled for (1-4); max_ops: operators per pass (1-192). */
+typedef struct lsg_plan_opts {
+    int32_t tile_bits, low_bits, ctas, max_ops;
+} lsg_plan_opts;
+/* lsg_program_create with explicit plan choices (the autotuner's search space). No counterpart in
+ * the reference, whose kernel choices are fixed thresholds (engines.py:20-27). */
+int lsg_program_create_opts(lsg_state shape, const lsg_op* ops, int32_t nops, const double* pool,
+                            int64_t pool_entries, const lsg_plan_opts* opts, lsg_program* out);
 /* 1 when the program's passes run as kernels specialized for it at creation (NVRTC, LSG_JIT=1),
  * 0 when the generic pass kernel interprets its operator records, negative on error. */
 int lsg_program_specialized(lsg_program p);
@@ -174,6 +191,15 @@ int lsg_sample(lsg_state s, int dm_qubits, int64_t member, const int32_t* measur
                const int32_t* pair_has_err, const double* pair_p01, const double* pair_p10,
                const double* flip_uniforms, uint8_t* bits_out, uint8_t* near_out, int64_t* near_count);
 
+/* Replaces the readout branching of simulator.py:445-486 (outcome_probabilities): member 0's
+ * probabilities marginalised onto `measured` (m qubits, ascending), entries <= threshold left out,
+ * then final-measurement pair j (of npairs <= 30, in the circuit's order) reads measured position
+ * pair_pos[j] and reports a flipped bit with probability pair_p01[j] (true 0) or pair_p10[j]
+ * (true 1). out (host, 2^npairs doubles): out[e] = probability that pair j reported bit j of e for
+ * every j. The caller deposits the pair bits onto their classical bits. */
+int lsg_outcome_probabilities(lsg_state s, int dm_qubits, const int32_t* measured, int32_t m, int32_t npairs,
+                              const int32_t* pair_pos, const double* pair_p01, const double* pair_p10, double threshold,
+                              double* out);
 /* <P> for Pauli terms given by x/z masks (Y sets both; qubit q = bit q), for every member.
  * out[t * batch + b]. Statevector: sum_b conj(psi[b^x]) c(b) psi[b]; density register:
  * sum_s c(s) rho[s][s^x]. Replaces the per-term loops of expectation
@@ -318,9 +344,10 @@ int lsg_pcg_raw(const uint64_t* state, uint64_t index, uint64_t* out);
  * `out_device` (nterms x batch doubles, out[t * batch + b]). It calls no cudaMalloc/cudaFree: its
  * only working memory is one file-scope __device__ array of LSG_NOALLOC_SCRATCH_BYTES, which every
  * GPU that loads the library holds until the process exits. The masks and nterms x batch partial
- * sums must fit in it; larger requests fail with LSG_E_ARG. The first call on a device looks up
+ * sums must fit in it, and one call takes at most 65,535 members; larger requests fail with
+ * LSG_E_ARG, as do buffers that are not device memory of the current device. The first call on a device looks up
  * the array's device address on that device (call it once, with the device current, before any
- * latency-critical use). Every call shares the array, so calls that overlap on the GPU race:
+ * latency-critical use and before any stream capture). Every call shares the array, so calls that overlap on the GPU race:
  * serialise them (one stream, or wait between calls). The call waits for its own stream before
  * returning. `stream` is a cudaStream_t (NULL: the legacy default stream). */
 #define LSG_NOALLOC_SCRATCH_BYTES (1u << 20)

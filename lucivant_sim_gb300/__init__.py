@@ -33,6 +33,7 @@ from lucivant_sim_gb300.simulator import (
     density_matrix,
     expectation,
     outcome_probabilities,
+    precision_report,
     probabilities,
     probabilities_array,
     run,
@@ -61,6 +62,7 @@ __all__ = [
     "is_clifford",
     "load",
     "outcome_probabilities",
+    "precision_report",
     "parse",
     "pauli_channel",
     "phase_damping",

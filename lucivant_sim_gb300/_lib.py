@@ -65,6 +65,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_probabilities": (C.c_int, [_P, C.c_int, _I64, _PD]),
     "lsg_sample": (C.c_int, [_P, C.c_int, _I64, _PI32, _I32, _PD, _I64, _I32, _PI32, _PI32, _PD, _PD, _PD, _PU8, _PU8, _PI64]),
     "lsg_expect_pauli": (C.c_int, [_P, C.c_int, _PU64, _PU64, _I32, _PD]),
+    "lsg_outcome_probabilities": (C.c_int, [_P, C.c_int, _PI32, _I32, _I32, _PI32, _PD, _PD, _D, _PD]),
     "lsg_prob_one": (C.c_int, [_P, C.c_int, _I64, _PD]),
     "lsg_program_create": (C.c_int, [_P, _P, _I32, _PD, _I64, C.POINTER(_P)]),
     "lsg_program_run": (C.c_int, [_P, _P]),
@@ -76,6 +77,8 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_program_run_from_basis": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_float)]),
     "lsg_program_basis_info": (C.c_int, [_P, _PI64, _PI64]),
     "lsg_program_free": (C.c_int, [_P]),
+    "lsg_program_create_opts": (C.c_int, [_P, _P, _I32, _PD, _I64, _P, C.POINTER(_P)]),
+    "lsg_program_pass_info": (C.c_int, [_P, _I32, _PI64, _PD, _PI32]),
     "lsg_plan": (C.c_int, [C.c_int, C.c_int, _P, _I32, _PI32]),
     "lsg_program_source": (C.c_int, [C.c_int, C.c_int, _I64, _P, _I32, _PD, _I64, C.c_int, C.c_char_p, _I64, _PI64]),
     "lsg_state_sync": (C.c_int, [_P]),
@@ -289,6 +292,20 @@ class Register:
         check(self.lib.lsg_probabilities(self.handle, dm_qubits, member, ptr(out, C.c_double)))
         return out.reshape(self.batch, -1) if member < 0 else out
 
+    def outcome_probabilities(self, dm_qubits: int, measured: list[int], pair_pos: list[int],
+                              pair_err: list[tuple[float, float]], threshold: float) -> np.ndarray:  # fmt: skip
+        """Probabilities of every combination of reported pair bits (index bit j = pair j), with
+        each pair's readout flips applied on the device; member 0."""
+        meas = np.asarray(measured, dtype=np.int32)
+        pos = np.asarray(pair_pos, dtype=np.int32)
+        p01 = np.asarray([e[0] for e in pair_err], dtype=np.float64)
+        p10 = np.asarray([e[1] for e in pair_err], dtype=np.float64)
+        out = np.empty(1 << len(pos), dtype=np.float64)
+        check(self.lib.lsg_outcome_probabilities(self.handle, dm_qubits, ptr(meas, C.c_int32), len(meas), len(pos),
+                                                 ptr(pos, C.c_int32), ptr(p01, C.c_double), ptr(p10, C.c_double),
+                                                 float(threshold), ptr(out, C.c_double)))  # fmt: skip
+        return out
+
     def sample(
         self,
         dm_qubits: int,
@@ -351,17 +368,45 @@ class Register:
         return int(out.value)
 
 
+class _PlanOptsC(C.Structure):
+    _fields_ = [("tile_bits", C.c_int32), ("low_bits", C.c_int32), ("ctas", C.c_int32), ("max_ops", C.c_int32)]
+
+
+class PlanOpts:
+    """Plan and launch choices of a program (``lsg_plan_opts``; 0 keeps a field's default)."""
+
+    def __init__(self, tile_bits: int = 0, low_bits: int = 0, ctas: int = 0, max_ops: int = 0) -> None:
+        self.tile_bits, self.low_bits, self.ctas, self.max_ops = int(tile_bits), int(low_bits), int(ctas), int(max_ops)
+
+    def struct(self) -> _PlanOptsC:
+        return _PlanOptsC(self.tile_bits, self.low_bits, self.ctas, self.max_ops)
+
+    def as_dict(self) -> dict[str, int]:
+        return {"tile_bits": self.tile_bits, "low_bits": self.low_bits, "ctas": self.ctas, "max_ops": self.max_ops}
+
+    def __eq__(self, other: object) -> bool:
+        return isinstance(other, PlanOpts) and self.as_dict() == other.as_dict()
+
+    def __repr__(self) -> str:
+        return f"PlanOpts({', '.join(f'{k}={v}' for k, v in self.as_dict().items())})"
+
+
 class Program:
     """A planned, uploaded operator list for registers shaped like ``shape``: run it repeatedly
     without re-planning, re-uploading or synchronising."""
 
-    def __init__(self, shape: Register, ops: OpList) -> None:
+    def __init__(self, shape: Register, ops: OpList, opts: PlanOpts | None = None) -> None:
         self.lib = library()
         table, pool = ops.packed()
         handle = C.c_void_p()
-        check(self.lib.lsg_program_create(shape.handle, table.ctypes.data, len(table), ptr(pool, C.c_double),
-                                          pool.size // 2, C.byref(handle)))  # fmt: skip
+        if opts is None:
+            check(self.lib.lsg_program_create(shape.handle, table.ctypes.data, len(table), ptr(pool, C.c_double),
+                                              pool.size // 2, C.byref(handle)))  # fmt: skip
+        else:
+            check(self.lib.lsg_program_create_opts(shape.handle, table.ctypes.data, len(table), ptr(pool, C.c_double),
+                                                   pool.size // 2, C.byref(opts.struct()), C.byref(handle)))  # fmt: skip
         self.handle = handle
+        self.opts = opts
         passes, nbytes = C.c_int32(0), C.c_int64(0)
         check(self.lib.lsg_program_info(handle, C.byref(passes), C.byref(nbytes)))
         self.passes, self.bytes_per_run = int(passes.value), int(nbytes.value)
@@ -390,6 +435,18 @@ class Program:
         nbytes = C.c_int64(0)
         check(self.lib.lsg_program_basis_info(self.handle, C.byref(nbytes), None))
         return int(nbytes.value)
+
+    def pass_info(self) -> dict[str, np.ndarray]:
+        """Per pass: HBM bytes a run from a basis state moves (all tiles before the first such
+        run), floating-point operations per register element, register blocks."""
+        n = max(self.passes, 1)
+        tiles = np.zeros(n, dtype=np.int64)
+        flops = np.zeros(n, dtype=np.float64)
+        blocks = np.zeros(n, dtype=np.int32)
+        check(self.lib.lsg_program_pass_info(self.handle, n, ptr(tiles, C.c_int64), ptr(flops, C.c_double),
+                                             ptr(blocks, C.c_int32)))  # fmt: skip
+        k = self.passes
+        return {"bytes": tiles[:k], "flops_per_element": flops[:k], "blocks": blocks[:k]}
 
     def run_timed(self, reg: Register) -> np.ndarray:
         out = np.zeros(max(self.passes, 1), dtype=np.float32)

@@ -13,14 +13,15 @@ from typing import Any
 
 import numpy as np
 
-from lucivant_sim_gb300 import _lib, engine
+from lucivant_sim_gb300 import _lib, autotune as tuning, engine
 from lucivant_sim_gb300.engine import pauli_masks
 
 
 class DensityBatch:
     """``len(noises)`` noisy density-matrix instances of one static circuit."""
 
-    def __init__(self, circuit: Any, noises: list[Any], precision: str | None = "c64") -> None:
+    def __init__(self, circuit: Any, noises: list[Any], precision: str | None = "c64",
+                 autotune: bool | None = None) -> None:  # fmt: skip
         if circuit.is_dynamic():
             raise engine.SimulationError("a density matrix needs a circuit without mid-circuit measurement or conditions")
         self.circuit = circuit
@@ -34,7 +35,11 @@ class DensityBatch:
         else:
             self.reg = engine.new_density(self.n, prec, self.batch)
             self.ops = engine.dm_oplist(circuit, noises)
-        self.program = _lib.Program(self.reg, self.ops)
+        # plan choices searched on the device per program shape (autotune.py), when asked
+        if tuning.wanted(autotune):
+            self.program, self.tune = tuning.tuned_program(self.reg, self.ops)
+        else:
+            self.program, self.tune = _lib.Program(self.reg, self.ops), None
         self.upload_bytes = int(self.ops.size * 16 + len(self.ops) * _lib.OP_DTYPE.itemsize)
 
     @property
@@ -78,7 +83,8 @@ def halves(noises: list[Any], split: bool = True) -> list[list[Any]]:
 
 
 def run_density_batch(
-    circuit: Any, noises: list[Any], observables: list[str], precision: str | None = "c64", split: bool = True
+    circuit: Any, noises: list[Any], observables: list[str], precision: str | None = "c64", split: bool = True,
+    autotune: bool | None = None,
 ):
     """One call from host inputs to host results: probabilities (batch, 2^n) and expectations
     (terms, batch) of every noise instance.
@@ -91,18 +97,18 @@ def run_density_batch(
     parts = halves(noises, split)
     done: list[DensityBatch] = []
     try:
-        first = DensityBatch(circuit, parts[0], precision)
+        first = DensityBatch(circuit, parts[0], precision, autotune)
         done.append(first)
         if len(parts) == 2 and not first.program.specialized:
             nominal = first.program.bytes_per_run
             if not _lib.jit_wanted(nominal) and _lib.jit_wanted(2 * nominal):
                 done.pop().free()  # the whole batch would be specialized: run it as one
                 parts = [noises]
-                first = DensityBatch(circuit, noises, precision)
+                first = DensityBatch(circuit, noises, precision, autotune)
                 done.append(first)
         first.evolve()
         for part in parts[1:]:
-            b = DensityBatch(circuit, part, precision)
+            b = DensityBatch(circuit, part, precision, autotune)
             done.append(b)
             b.evolve()
         probs = [b.probabilities() for b in done]

@@ -297,6 +297,13 @@ static void form_blocks(Plan& plan, PassDesc& pd, int umax) {
 // (192 x 136 B + blocks stays under 40 KB, so two pipelined CTAs still share an SM).
 constexpr int kMaxPassOps = 192;
 
+// Plan and launch choices for the program being created on this thread (lsg_program_create_opts);
+// zero fields keep the defaults (and their environment knobs).
+struct PlanChoice {
+    int tile_bits = 0, low_bits = 0, ctas = 0, max_ops = 0;
+};
+static thread_local PlanChoice t_choice;
+
 // Starting tiles the planner tries per pass (LSG_PLAN_SEEDS; 1 = the plain greedy sweep). More
 // than about 64 found no better plan for brickwork circuits of 12-20 qubits.
 static int plan_seeds() {
@@ -320,7 +327,9 @@ Plan plan_ops(const lsg_op* ops, int nops, int nbits, int K, int L, const int* p
         return mask;
     };
     const char* ops_env = getenv("LSG_PASS_OPS");
-    const int max_ops = ops_env ? std::max(1, std::min(kMaxPassOps, atoi(ops_env))) : kMaxPassOps;
+    const int max_ops = t_choice.max_ops ? std::max(1, std::min(kMaxPassOps, t_choice.max_ops))
+                        : ops_env        ? std::max(1, std::min(kMaxPassOps, atoi(ops_env)))
+                                         : kMaxPassOps;
     // One pass by the greedy sweep from a starting tile: an operator joins when its bits fit and no
     // operator deferred earlier in the sweep shares a bit with it (program order where it matters).
     std::vector<uint64_t> masks(nops);
@@ -496,7 +505,8 @@ static int check_plan(const Plan& plan) {
 int tile_bits_for(int nbits, int precision) {
     const size_t eb = lsg_elem_bytes(precision);
     int K = eb == 16 ? 11 : eb == 8 ? 12 : 13;
-    if (const char* env = getenv("LSG_TILE_BITS")) K = atoi(env);
+    if (t_choice.tile_bits) K = t_choice.tile_bits;
+    else if (const char* env = getenv("LSG_TILE_BITS")) K = atoi(env);
     return std::max(0, std::min(K, nbits));
 }
 
@@ -506,7 +516,8 @@ int tile_bits_for(int nbits, int precision) {
 int low_bits_for(int nbits, int precision) {
     const size_t eb = lsg_elem_bytes(precision);
     int L = eb == 16 ? 5 : eb == 8 ? 6 : 7;
-    if (const char* env = getenv("LSG_LOW_BITS")) L = atoi(env);
+    if (t_choice.low_bits) L = t_choice.low_bits;
+    else if (const char* env = getenv("LSG_LOW_BITS")) L = atoi(env);
     return std::max(0, std::min(L, nbits));
 }
 
@@ -892,6 +903,7 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
 
 // Launch bound of specialized passes: CTAs per SM (the interpreter's pipe_ctas for the element).
 static int jit_ctas(int precision) {
+    if (t_choice.ctas) return std::max(1, std::min(4, t_choice.ctas));
     if (const char* env = getenv("LSG_JIT_CTAS")) return std::max(1, std::min(4, atoi(env)));
     return (precision == LSG_C128 || precision == LSG_R64) ? 1 : lsg_elem_bytes(precision) == 4 ? 3 : 2;
 }
@@ -1279,6 +1291,38 @@ int lsg_program_create(lsg_state shape, const lsg_op* ops, int32_t nops, const d
     return LSG_OK;
 }
 
+int lsg_program_create_opts(lsg_state shape, const lsg_op* ops, int32_t nops, const double* pool,
+                            int64_t pool_entries, const lsg_plan_opts* opts, lsg_program* out) {
+    clear_error();
+    if (!shape || !out) return fail(LSG_E_ARG, "null argument");
+    *out = nullptr;
+    PlanChoice c;
+    if (opts) {
+        const int eb_log = lsg_elem_bytes(shape->precision) == 16 ? 4 : lsg_elem_bytes(shape->precision) == 8 ? 3 : 2;
+        // a tile of at most 64 KB (two of them and the pass metadata fit shared memory); runs of at
+        // least 16 bytes (bulk copies); 1 to 4 CTAs per SM; 1 to 192 operators per pass
+        if (opts->tile_bits < 0 || (opts->tile_bits && opts->tile_bits + eb_log > 16))
+            return fail(LSG_E_ARG, "lsg_program_create_opts: tile of 2^%d elements exceeds 64 KB", opts->tile_bits);
+        if (opts->low_bits < 0 || (opts->low_bits && opts->low_bits + eb_log < 4))
+            return fail(LSG_E_ARG, "lsg_program_create_opts: runs of 2^%d elements are under 16 bytes", opts->low_bits);
+        if (opts->tile_bits && opts->low_bits && opts->low_bits > opts->tile_bits)
+            return fail(LSG_E_ARG, "lsg_program_create_opts: more low bits than tile bits");
+        if (opts->ctas < 0 || opts->ctas > 4) return fail(LSG_E_ARG, "lsg_program_create_opts: 1 to 4 CTAs per SM");
+        if (opts->max_ops < 0 || opts->max_ops > kMaxPassOps)
+            return fail(LSG_E_ARG, "lsg_program_create_opts: 1 to %d operators per pass", kMaxPassOps);
+        c = PlanChoice{opts->tile_bits, opts->low_bits, opts->ctas, opts->max_ops};
+    }
+    struct Restore {
+        PlanChoice saved = t_choice;
+        ~Restore() { t_choice = saved; }
+    } restore;
+    t_choice = c;
+    LSG_CHECK(program_create_jit(shape->nbits, shape->precision, shape->batch, ops, nops, pool, pool_entries, out,
+                                 shape->stream));
+    (*out)->dev.stream = nullptr;  // as lsg_program_create: the program may outlive the register
+    return LSG_OK;
+}
+
 int lsg_program_run(lsg_program p, lsg_state s) {
     clear_error();
     if (!p || !s) return fail(LSG_E_ARG, "null argument");
@@ -1323,6 +1367,50 @@ int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles
     for (const PassDesc& pd : p->basis_passes) tiles += (1ll << pd.nouter) * p->batch;
     if (tiles_per_run) *tiles_per_run = tiles;
     if (bytes_per_run) *bytes_per_run = 2 * tiles * ((int64_t)lsg_elem_bytes(p->precision) << p->K);
+    return LSG_OK;
+}
+
+// Floating-point operations per register element that one operator of a pass executes (a
+// multiply or add counts 1, a fused multiply-add 2), as the register-block functions and the
+// shared-memory operators compute them.
+static double op_flops_per_element(const lsg::TileOp& op, bool complex_elems) {
+    using namespace lsg;
+    const int c = op.tmpl;
+    const double mul = complex_elems ? 6.0 : 1.0;  // one (complex) product per element
+    if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) return complex_elems ? 14.0 : 3.0;
+    if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) return complex_elems ? 30.0 : 7.0;
+    if (c >= kT_TPD2 && c < kT_TPD2 + 16) return 5.25;
+    if ((c >= kT_PERM1 && c < kT_PERM1 + 4) || (c >= kT_PERM2 && c < kT_PERM2 + 16)) return mul;
+    if (c == kT_DIAGB || c == kT_SCALE || c == kT_DIAG) return mul;
+    if ((c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) || c == kT_DEPOL2) return 4.0;
+    if ((c >= kT_X1 && c < kT_X1 + 4) || (c >= kT_CX && c < kT_CX + 16) || (c >= kT_SWAP && c < kT_SWAP + 16)) return 0.0;
+    if ((c >= kT_MIX1 && c < kT_MIX1 + 4) || (c >= kT_MIX2 && c < kT_MIX2 + 16)) return complex_elems ? 30.0 : 7.0;
+    // the shared-memory path: a dense 2^k operator is 2^k (complex) multiply-adds per element
+    const double fma = complex_elems ? 8.0 : 2.0;
+    switch (op.kind) {
+        case LSG_OP_MATRIX: return fma * (double)(1 << op.k);
+        case LSG_OP_DEPOL: return 4.0;
+        default: return mul;
+    }
+}
+
+int lsg_program_pass_info(lsg_program p, int32_t cap, int64_t* bytes, double* flops_per_element, int32_t* blocks) {
+    clear_error();
+    if (!p) return fail(LSG_E_ARG, "null program");
+    const int32_t n = (int32_t)p->plan.passes.size();
+    if (cap < n) return fail(LSG_E_ARG, "lsg_program_pass_info: room for %d passes, the program has %d", cap, n);
+    const bool cx = !(p->precision == LSG_R64 || p->precision == LSG_R32);
+    for (int32_t i = 0; i < n; ++i) {
+        const lsg::PassDesc& pd = p->plan.passes[(size_t)i];
+        const lsg::PassDesc& visited = p->basis_passes.size() == (size_t)n ? p->basis_passes[(size_t)i] : pd;
+        if (bytes) bytes[i] = 2 * (1ll << visited.nouter) * p->batch * ((int64_t)lsg_elem_bytes(p->precision) << pd.K);
+        if (blocks) blocks[i] = pd.nblocks;
+        if (flops_per_element) {
+            double f = 0.0;
+            for (int k = 0; k < pd.nops; ++k) f += op_flops_per_element(p->plan.ops[(size_t)(pd.first_op + k)], cx);
+            flops_per_element[i] = f;
+        }
+    }
     return LSG_OK;
 }
 

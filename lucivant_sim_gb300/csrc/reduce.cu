@@ -16,6 +16,8 @@
 namespace lsg {
 
 constexpr int kThreads = 256;
+constexpr int64_t kMaxGridY = 65535;  // the largest grid y extent of a launch
+constexpr int kMaxOutcomePairs = 30;   // outcome space of lsg_outcome_probabilities: 2^30 doubles at most
 
 template <typename R>
 __device__ __forceinline__ double norm2(Cx<R> a) {
@@ -171,6 +173,39 @@ __global__ void k_search(const double* __restrict__ cum, int64_t n, const double
             }
             bits[s * npairs + j] = (uint8_t)bit;
         }
+    }
+}
+
+// Exact outcomes with readout error. Pair j of the final measurements reads measured position
+// pos[j]; the outcome space has one bit per pair (bit j = what pair j reported).
+struct PairPositions {
+    int pos[64];
+    int n;
+};
+
+// E[e(i)] = dist[i] (0 where dist[i] <= threshold: those indices are left out, as the reference
+// skips them), e(i) = the pair bits index i gives before any flip. E is zero elsewhere (the pair
+// bits of two pairs on one qubit agree).
+__global__ void k_pair_scatter(const double* __restrict__ dist, int64_t nd, PairPositions pp, double threshold,
+                               double* __restrict__ e_out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t e = 0;
+        for (int j = 0; j < pp.n; ++j) e |= (uint64_t)((i >> pp.pos[j]) & 1) << j;
+        const double v = dist[i];
+        e_out[e] = v > threshold ? v : 0.0;
+    }
+}
+
+// Pair j's readout error on the outcome space: a reported 0 becomes 1 with p01, a 1 becomes 0
+// with p10 (a column-stochastic 2x2 on bit j).
+__global__ void k_readout_flip(double* __restrict__ e, int64_t ne, int j, double p01, double p10) {
+    const uint64_t bit = 1ull << j;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (ne >> 1); t += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = (uint64_t)t & (bit - 1);
+        const uint64_t i0 = (((uint64_t)t >> j) << (j + 1)) | lo, i1 = i0 | bit;
+        const double a0 = e[i0], a1 = e[i1];
+        e[i0] = a0 * (1.0 - p01) + a1 * p10;
+        e[i1] = a0 * p01 + a1 * (1.0 - p10);
     }
 }
 
@@ -470,6 +505,68 @@ int lsg_sample(lsg_state s, int dm_qubits, int64_t member, const int32_t* measur
     return LSG_OK;
 }
 
+int lsg_outcome_probabilities(lsg_state s, int dm_qubits, const int32_t* measured, int32_t m, int32_t npairs,
+                              const int32_t* pair_pos, const double* pair_p01, const double* pair_p10, double threshold,
+                              double* out) {
+    clear_error();
+    if (!s || !measured || !out || m < 1 || npairs < 1 || !pair_pos || !pair_p01 || !pair_p10)
+        return fail(LSG_E_ARG, "lsg_outcome_probabilities: bad arguments");
+    if (npairs > kMaxOutcomePairs)
+        return fail(LSG_E_CAPACITY, "lsg_outcome_probabilities: %d measurement pairs; at most %d", npairs, kMaxOutcomePairs);
+    const int nq = dm_qubits ? dm_qubits : s->nbits;
+    if (m > nq || m > npairs) return fail(LSG_E_ARG, "lsg_outcome_probabilities: more measured qubits than pairs or qubits");
+    BitLists bl{};
+    uint64_t keepmask = 0;
+    for (int i = 0; i < m; ++i) {
+        if (measured[i] < 0 || measured[i] >= nq || (i && measured[i] <= measured[i - 1]))
+            return fail(LSG_E_ARG, "lsg_outcome_probabilities: measured qubits must be ascending and in range");
+        bl.keep[i] = measured[i];
+        keepmask |= 1ull << measured[i];
+    }
+    bl.nkeep = m;
+    for (int q = 0; q < nq; ++q)
+        if (!((keepmask >> q) & 1)) bl.drop[bl.ndrop++] = q;
+    PairPositions pp{};
+    pp.n = npairs;
+    uint64_t seen = 0;
+    for (int j = 0; j < npairs; ++j) {
+        if (pair_pos[j] < 0 || pair_pos[j] >= m) return fail(LSG_E_ARG, "lsg_outcome_probabilities: pair position out of range");
+        if (!(pair_p01[j] >= 0 && pair_p01[j] <= 1 && pair_p10[j] >= 0 && pair_p10[j] <= 1))
+            return fail(LSG_E_ARG, "lsg_outcome_probabilities: flip probabilities must lie in [0, 1]");
+        pp.pos[j] = pair_pos[j];
+        seen |= 1ull << pair_pos[j];
+    }
+    if (seen != (m >= 64 ? ~0ull : (1ull << m) - 1))
+        return fail(LSG_E_ARG, "lsg_outcome_probabilities: every measured qubit needs a pair");
+    const int64_t nfull = 1ll << nq, nd = 1ll << m, ne = 1ll << npairs;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off += (bytes + 255) & ~size_t(255);
+        return at;
+    };
+    const size_t o_p = take(nfull * 8), o_d = take(nd * 8), o_e = take(ne * 8);
+    LSG_CHECK(ensure(s->scratch, off));
+    char* base = (char*)s->scratch.ptr;
+    double* p = (double*)(base + o_p);
+    double* dist = (double*)(base + o_d);
+    double* e = (double*)(base + o_e);
+    int64_t got = 0;
+    LSG_CHECK(probs_device(s, dm_qubits, 0, p, &got));
+    if (m == nq) dist = p;
+    else if (bl.ndrop <= 6) k_marginal_thread<<<reduce_grid(nd), kThreads, 0, s->stream>>>(p, dist, bl);
+    else k_marginal_block<<<(unsigned)std::min<int64_t>(nd, 152 * 16), kThreads, 0, s->stream>>>(p, dist, bl);
+    LSG_CUDA(cudaMemsetAsync(e, 0, (size_t)ne * 8, s->stream));
+    k_pair_scatter<<<reduce_grid(nd), kThreads, 0, s->stream>>>(dist, nd, pp, threshold, e);
+    for (int j = 0; j < npairs; ++j)
+        if (pair_p01[j] != 0.0 || pair_p10[j] != 0.0)
+            k_readout_flip<<<reduce_grid(ne >> 1), kThreads, 0, s->stream>>>(e, ne, j, pair_p01[j], pair_p10[j]);
+    LSG_CUDA(cudaGetLastError());
+    LSG_CUDA(cudaMemcpyAsync(out, e, (size_t)ne * 8, cudaMemcpyDeviceToHost, s->stream));
+    LSG_CUDA(cudaStreamSynchronize(s->stream));
+    return LSG_OK;
+}
+
 int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const uint64_t* zmask, int32_t nterms,
                      double* out) {
     clear_error();
@@ -519,15 +616,20 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
     char* base = (char*)s->scratch.ptr;
     LSG_CUDA(cudaMemcpyAsync(base + o_x, xmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
     LSG_CUDA(cudaMemcpyAsync(base + o_z, zmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
-    const dim3 g2(grid, (unsigned)s->batch);
-    if (s->precision == LSG_C128)
-        k_expect<double><<<g2, kThreads, 0, s->stream>>>((const Cx<double>*)s->data, s->elems, dm_qubits,
-                                                        (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
-                                                        nterms, (double*)(base + o_part));
-    else
-        k_expect<float><<<g2, kThreads, 0, s->stream>>>((const Cx<float>*)s->data, s->elems, dm_qubits,
-                                                       (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
-                                                       nterms, (double*)(base + o_part));
+    // members go on grid y, at most 65,535 per launch: larger batches run in chunks of members
+    for (int64_t b0 = 0; b0 < s->batch; b0 += kMaxGridY) {
+        const int64_t nb = std::min<int64_t>(kMaxGridY, s->batch - b0);
+        const dim3 g2(grid, (unsigned)nb);
+        double* part = (double*)(base + o_part) + b0 * nterms * (int64_t)grid;
+        if (s->precision == LSG_C128)
+            k_expect<double><<<g2, kThreads, 0, s->stream>>>((const Cx<double>*)s->data + b0 * s->elems, s->elems,
+                                                            dm_qubits, (const uint64_t*)(base + o_x),
+                                                            (const uint64_t*)(base + o_z), nterms, part);
+        else
+            k_expect<float><<<g2, kThreads, 0, s->stream>>>((const Cx<float>*)s->data + b0 * s->elems, s->elems,
+                                                           dm_qubits, (const uint64_t*)(base + o_x),
+                                                           (const uint64_t*)(base + o_z), nterms, part);
+    }
     k_sum_rows<<<(unsigned)std::min<int64_t>(rows, 152 * 16), kThreads, 0, s->stream>>>((const double*)(base + o_part), grid,
                                                                                       rows, (double*)(base + o_out));
     LSG_CUDA(cudaGetLastError());
@@ -641,6 +743,9 @@ extern "C" int lsg_expect_pauli_noalloc(const void* amplitudes, int precision, i
     clear_error();
     if (!amplitudes || !out_device || nterms < 1 || !xmask || !zmask || batch < 1)
         return fail(LSG_E_ARG, "lsg_expect_pauli_noalloc: bad arguments");
+    if (batch > kMaxGridY)
+        return fail(LSG_E_ARG, "lsg_expect_pauli_noalloc: %lld members; one call takes at most %d",
+                    (long long)batch, (int)kMaxGridY);
     if (precision != LSG_C128 && precision != LSG_C64) return fail(LSG_E_ARG, "unknown precision %d", precision);
     if (nbits < 0 || nbits > kMaxBits) return fail(LSG_E_CAPACITY, "a register of %d bits exceeds the engine's %d", nbits, kMaxBits);
     if (dm_qubits && 2 * dm_qubits != nbits) return fail(LSG_E_STATE, "density register size mismatch");
@@ -660,6 +765,22 @@ extern "C" int lsg_expect_pauli_noalloc(const void* amplitudes, int precision, i
     const int64_t fit = (int64_t)(room / 8 / (size_t)rows);
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>({(int64_t)reduce_grid(count), fit,
                                                                              std::max<int64_t>(1, 4096 / batch)}));
+    // both buffers must be device memory of the current device: the scratch array used below is
+    // the current device's, and the kernels read and write the buffers from that device
+    int dev = 0;
+    LSG_CUDA(cudaGetDevice(&dev));
+    for (const void* ptr : {amplitudes, static_cast<const void*>(out_device)}) {
+        cudaPointerAttributes attr{};
+        if (cudaPointerGetAttributes(&attr, ptr) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(LSG_E_ARG, "lsg_expect_pauli_noalloc: %s is not a CUDA pointer",
+                        ptr == amplitudes ? "amplitudes" : "out_device");
+        }
+        const bool on_device = attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+        if (!on_device || attr.device != dev)
+            return fail(LSG_E_ARG, "lsg_expect_pauli_noalloc: %s is not device memory of the current device %d",
+                        ptr == amplitudes ? "amplitudes" : "out_device", dev);
+    }
     void* base = nullptr;
     LSG_CHECK(noalloc_scratch(&base));
     char* scratch = static_cast<char*>(base);

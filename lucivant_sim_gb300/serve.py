@@ -102,37 +102,64 @@ def sweep_oplist(circuits: list[Any]) -> _lib.OpList:
 
 
 class _RegisterPool:
-    """Registers kept for reuse by shape: allocation stays off the serving path."""
+    """Idle registers kept for reuse by shape: allocation stays off the serving path. Their
+    device bytes (``bytes``) stay allocated, so the server counts them against its budget and
+    frees idle registers when an admission needs the room."""
 
     def __init__(self) -> None:
         self.free: dict[tuple[int, int, int], list[_lib.Register]] = {}
+        self.bytes = 0
         self.lock = threading.Lock()
 
-    def take(self, nbits: int, precision: int, batch: int) -> _lib.Register:
+    def take(self, shape: tuple[int, int, int]) -> _lib.Register | None:
+        """An idle register of ``shape`` (nbits, precision, batch), or None."""
         with self.lock:
-            lst = self.free.get((nbits, precision, batch))
-            if lst:
-                return lst.pop()
-        return _lib.Register(nbits, precision, batch)
+            lst = self.free.get(shape)
+            if not lst:
+                return None
+            reg = lst.pop()
+            self.bytes -= register_bytes(*shape)
+            return reg
 
     def give(self, reg: _lib.Register) -> None:
         with self.lock:
             self.free.setdefault((reg.nbits, reg.precision, reg.batch), []).append(reg)
+            self.bytes += register_bytes(reg.nbits, reg.precision, reg.batch)
 
-    def clear(self) -> None:
+    def evict(self, nbytes: int) -> int:
+        """Free idle registers, largest first, until at least ``nbytes`` are released (or none are
+        left); returns the bytes released."""
         with self.lock:
-            for lst in self.free.values():
-                for r in lst:
-                    r.free()
-            self.free.clear()
+            regs = sorted((r for lst in self.free.values() for r in lst),
+                          key=lambda r: register_bytes(r.nbits, r.precision, r.batch), reverse=True)  # fmt: skip
+            released = 0
+            for r in regs:
+                if released >= nbytes:
+                    break
+                self.free[(r.nbits, r.precision, r.batch)].remove(r)
+                size = register_bytes(r.nbits, r.precision, r.batch)
+                r.free()
+                released += size
+                self.bytes -= size
+            self.free = {k: v for k, v in self.free.items() if v}
+            return released
+
+    def clear(self) -> int:
+        return self.evict(self.bytes + 1)
 
 
-def execute(prep: dict, precision: int, pool: _RegisterPool | None = None) -> dict:
-    """Device side of a prepared job (runs on a server worker thread, or alone)."""
+def register_bytes(nbits: int, precision: int, batch: int) -> int:
+    return (_lib.ELEM_BYTES[precision] << nbits) * batch
+
+
+def execute(prep: dict, precision: int, reg: _lib.Register | None = None) -> dict:
+    """Device side of a prepared job (runs on a server worker thread, or alone). ``reg``: a
+    register of the job's shape to run on (kept by the caller), else one is made and freed."""
     nbits, batch = prep["nbits"], prep["batch"]
-    if prep.get("real"):  # a density matrix in Pauli-transfer form
-        precision = engine.REAL_OF[precision]
-    reg = pool.take(nbits, precision, batch) if pool else _lib.Register(nbits, precision, batch)
+    precision = job_precision(prep, precision)
+    own = reg is None
+    if own:
+        reg = _lib.Register(nbits, precision, batch)
     try:
         table, flat = prep["ops"]  # |0...0> then the operators (tiles not reached yet are skipped)
         _lib.check(reg.lib.lsg_apply_from_basis(reg.handle, 0, table.ctypes.data, len(table),
@@ -146,15 +173,23 @@ def execute(prep: dict, precision: int, pool: _RegisterPool | None = None) -> di
                                          np.random.default_rng(prep["seed"]))  # fmt: skip
         return {"counts": counts, "near_boundary": report["near_boundary"]}
     finally:
-        if pool:
-            pool.give(reg)
-        else:
+        if own:
             reg.free()
 
 
+def job_precision(prep: dict, precision: int) -> int:
+    """The register precision of a job: density matrices in Pauli-transfer form are real."""
+    return engine.REAL_OF[precision] if prep.get("real") else precision
+
+
+def job_shape(prep: dict, precision: int) -> tuple[int, int, int]:
+    return prep["nbits"], job_precision(prep, precision), prep["batch"]
+
+
 def job_bytes(prep: dict, precision: int) -> int:
-    elt = _lib.ELEM_BYTES[engine.REAL_OF[precision] if prep.get("real") else precision]
-    return (elt << prep["nbits"]) * prep["batch"] * 2 + (64 << 20)  # register, reductions, program
+    """Device bytes a job holds while it runs: its register, as much again for reductions, and
+    room for the program."""
+    return 2 * register_bytes(*job_shape(prep, precision)) + (64 << 20)
 
 
 @dataclass(order=True)
@@ -200,8 +235,8 @@ class Server:
     def _prepared(self, pf: Any, fut: Future, t0: float) -> None:
         try:
             prep = pf.result()
-        except Exception as exc:  # noqa: BLE001 - handed to the client
-            fut.set_exception(exc)
+        except Exception as exc:  # noqa: BLE001 - handed to the client (a cancelled preparation too)
+            fut.set_exception(RuntimeError("server closed") if pf.cancelled() else exc)
             return
         prep["t0"] = t0
         need = job_bytes(prep, self.precision)
@@ -209,53 +244,81 @@ class Server:
             fut.set_exception(MemoryError(f"the job needs {need} bytes; the server admits at most {self.budget}"))
             return
         with self.cv:
+            if self.closed:
+                fut.set_exception(RuntimeError("server closed"))
+                return
             self.counter += 1
             heapq.heappush(self.waiting, _Waiting(self.counter, prep, fut, need))
             self.cv.notify()
 
     # -- device side ---------------------------------------------------------------------
-    def _admit(self) -> _Waiting | None:
+    # ``used`` counts the full need of every running job plus the idle pooled registers (they stay
+    # allocated). A job that reuses an idle register of its shape needs only the rest of its need.
+    def _admit(self) -> tuple[_Waiting, _lib.Register | None] | None:
         """The oldest waiting job that fits the free memory (oldest first; a smaller job may pass a
-        big one that does not fit yet)."""
-        for i, w in enumerate(sorted(self.waiting)):
-            if self.used + w.need <= self.budget:
+        big one that does not fit yet), freeing idle pooled registers when that makes it fit."""
+        for w in sorted(self.waiting):
+            shape = job_shape(w.prep, self.precision)
+            reg = self.pool.take(shape)
+            extra = w.need - (register_bytes(*shape) if reg is not None else 0)
+            if self.used + extra > self.budget and self.pool.bytes:
+                self.used -= self.pool.evict(self.used + extra - self.budget)
+            if self.used + extra <= self.budget:
                 self.waiting.remove(w)
                 heapq.heapify(self.waiting)
-                self.used += w.need
-                return w
+                self.used += extra
+                return w, reg
+            if reg is not None:  # not admitted: the register goes back to the pool
+                self.pool.give(reg)
         return None
 
     def _worker(self) -> None:
         _lib.ensure_device(self.device)
         while True:
             with self.cv:
-                w = None
+                picked = None
                 while not self.closed:
-                    w = self._admit() if self.waiting else None
-                    if w is not None:
+                    picked = self._admit() if self.waiting else None
+                    if picked is not None:
                         break
                     self.cv.wait(0.05)
-                if w is None:
+                if picked is None:
                     return
+            w, reg = picked
+            shape = job_shape(w.prep, self.precision)
             try:
-                res = execute(w.prep, self.precision, self.pool)
+                if reg is None:
+                    reg = _lib.Register(*shape)
+                res = execute(w.prep, self.precision, reg)
                 res["latency_s"] = time.perf_counter() - w.prep["t0"]
                 w.future.set_result(res)
             except Exception as exc:  # noqa: BLE001 - handed to the client
                 w.future.set_exception(exc)
             finally:
                 with self.cv:
-                    self.used -= w.need
+                    if reg is not None:  # the register stays allocated, idle in the pool
+                        self.pool.give(reg)
+                        self.used -= w.need - register_bytes(*shape)
+                    else:
+                        self.used -= w.need
                     self.cv.notify_all()
 
     def close(self) -> None:
+        """Stop the workers and free the device memory; jobs that have not run get a
+        ``RuntimeError('server closed')``."""
         with self.cv:
             self.closed = True
             self.cv.notify_all()
         for t in self.threads:
             t.join(timeout=60)
         self.prep.shutdown(wait=True, cancel_futures=True)
-        self.pool.clear()
+        with self.cv:
+            left, self.waiting = self.waiting, []
+        for w in left:
+            if not w.future.done():
+                w.future.set_exception(RuntimeError("server closed"))
+        with self.cv:
+            self.used -= self.pool.clear()
 
     def __enter__(self) -> Server:
         return self

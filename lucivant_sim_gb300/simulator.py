@@ -224,6 +224,47 @@ def _evolved(circuit: Any, noise: Any, precision: int) -> tuple[_lib.Register, i
     return reg, 0
 
 
+def precision_report(program: Any, noise: Any = None, observable: str | Mapping[str, float] | None = None,
+                     params: Mapping[str, float] | None = None) -> dict[str, Any]:  # fmt: skip
+    """How far the complex64 path's answers are from FP64 ones for a static circuit: the final
+    state evolved on the device in complex64 (real32 for a density matrix in Pauli-transfer form)
+    and again in complex128 (real64), compared.
+
+    Returns ``max_amplitude_error`` (max |a64 - a128| over the statevector's amplitudes or the
+    density matrix's entries; None for density matrices above 10 qubits, whose 4^n entries are not
+    downloaded), ``probability_tvd`` (total-variation distance of the exact probabilities) and
+    ``expectation_error`` (|<O>64 - <O>128| for ``observable``; without one, the largest error of
+    the single-qubit <Z_q>)."""
+    circuit = to_circuit(program, params)
+    _static(circuit, "a precision report")
+    n = circuit.num_qubits
+    if observable is None:
+        terms = {"".join("Z" if i == n - 1 - q else "I" for i in range(n)): 1.0 for q in range(n)}
+        per_term = True
+    else:
+        terms = {observable: 1.0} if isinstance(observable, str) else dict(observable)
+        per_term = False
+    masks = [pauli_masks(label) for label in terms]
+    weights = np.asarray(list(terms.values()))
+    out: dict[str, Any] = {"reference": "complex128 re-run on the device"}
+    states, probs, vals = [], [], []
+    for prec in (_lib.C64, _lib.C128):
+        reg, dm = _evolved(circuit, noise, prec)
+        with reg:
+            probs.append(reg.probabilities(dm))
+            v = reg.expect(dm, [m[0] for m in masks], [m[1] for m in masks])[:, 0] if masks else np.zeros(0)
+            vals.append(v if per_term else np.array([float(weights @ v)]))
+            if dm == 0:
+                states.append(reg.download()[0].astype(np.complex128))
+            elif n <= 10:
+                states.append(engine.density_download(reg))
+    out["max_amplitude_error"] = float(np.max(np.abs(states[0] - states[1]))) if len(states) == 2 else None
+    out["probability_tvd"] = 0.5 * float(np.abs(probs[0] - probs[1]).sum())
+    out["expectation_error"] = float(np.max(np.abs(vals[0] - vals[1]))) if vals[0].size else 0.0
+    out["form"] = "statevector" if not (noise is not None and noise.has_gate_errors()) else "density_matrix"
+    return out
+
+
 def run(
     program: Any,
     shots: int = 1024,
@@ -234,12 +275,15 @@ def run(
     params: Mapping[str, float] | None = None,
     precision: str | None = None,
     trajectory_mode: str | None = None,
+    report_precision: bool = False,
 ) -> Result:
     """Simulate ``program`` ``shots`` times; counts identical to Orrery's for the same seed.
 
     ``precision`` ("c128" default, or "c64") and ``trajectory_mode`` ("serial" default: Orrery's
     draw order; "batched": all shots at once, each with its own uniforms) are optional engine
-    knobs; defaults also come from ``LSG_PRECISION`` / ``LSG_TRAJ_MODE``."""
+    knobs; defaults also come from ``LSG_PRECISION`` / ``LSG_TRAJ_MODE``. ``report_precision``
+    (complex64 runs of static circuits; off by default, since it evolves the circuit again in
+    complex128): ``Result.report["precision"]`` holds :func:`precision_report`'s errors."""
     if not 0 <= shots <= MAX_SHOTS:
         raise ValueError(f"shots must be between 0 and {MAX_SHOTS:,}")
     circuit = to_circuit(program, params)
@@ -278,6 +322,8 @@ def run(
                 vector = reg.download()[0]
             counts, report = sample_register(reg, circuit, dm, shots, noise, rng)
     elapsed = round(time.perf_counter() - started, 6)
+    if report_precision and prec == _lib.C64 and chosen in ("statevector", "density_matrix"):
+        report = dict(report, precision=precision_report(circuit, noise))
     return Result(
         counts=counts if chosen in ("statevector", "density_matrix") else dict(sorted(counts.items())),
         shots=shots,
@@ -350,12 +396,33 @@ def outcome_probabilities(program: Any, noise: Any = None, params: Mapping[str, 
         return {}
     reg, dm = _evolved(circuit, noise, engine.precision_code(precision))
     measured = sorted({q for q, _ in pairs})
-    with reg:
-        probs = reg.probabilities(dm)
-    from lucivant_sim_gb300.readout import branch_outcomes
-
-    out = branch_outcomes(probs, circuit.num_qubits, measured, pairs, noise, threshold)
+    position = {q: i for i, q in enumerate(measured)}
+    errs = []
+    for q, _c in pairs:
+        err = noise.readout_error(q) if noise else None
+        errs.append((float(err.p01), float(err.p10)) if err is not None else (0.0, 0.0))
+    with reg:  # the marginal, the threshold and every pair's readout flips run on the device
+        space = reg.outcome_probabilities(dm, measured, [position[q] for q, _ in pairs], errs, threshold)
+    out = deposit_pairs(space, [c for _, c in pairs], circuit.num_clbits)
     return {format_bits(circuit, b): w for b, w in sorted(out.items()) if w > threshold}
+
+
+def deposit_pairs(space: NDArray[np.float64], clbits: list[int], num_clbits: int) -> dict[int, float]:
+    """Outcome probabilities keyed by classical bits from the pair-bit space (index bit j = the
+    bit pair j reported, written to classical bit ``clbits[j]``; pairs writing one classical bit
+    combine by OR, as the reference packs them); nonzero entries only."""
+    idx = np.flatnonzero(space)
+    if num_clbits > 62:
+        keys = [sum(((int(e) >> j) & 1) << c for j, c in enumerate(clbits)) for e in idx]
+    else:
+        packed = np.zeros(idx.size, dtype=np.int64)
+        for j, c in enumerate(clbits):
+            packed |= ((idx >> j) & 1).astype(np.int64) << c
+        keys = packed.tolist()
+    out: dict[int, float] = {}
+    for k, w in zip(keys, space[idx].tolist(), strict=True):
+        out[k] = out.get(k, 0.0) + w
+    return out
 
 
 def expectation(program: Any, observable: str | Mapping[str, float], noise: Any = None,
@@ -400,6 +467,7 @@ __all__ = [
     "density_matrix",
     "expectation",
     "outcome_probabilities",
+    "precision_report",
     "probabilities",
     "probabilities_array",
     "run",

@@ -501,7 +501,7 @@ def test_density_batch_halves_decision(monkeypatch):
     class FakeBatch:
         specialize_from = 4  # members from which the stand-in policy specializes
 
-        def __init__(self, circuit, noises, precision):
+        def __init__(self, circuit, noises, precision, autotune=None):
             made.append(list(noises))
             self.members = list(noises)
             self.program = FakeProgram(len(noises), len(noises) >= self.specialize_from)
@@ -600,3 +600,128 @@ def test_clifford_check_and_encoder_columns():
     assert cols.position(1).tolist() == [0, 1, 1, 0]
     assert cols.position(2).tolist() == [0, 0, 2, 0]
     assert cols.names == ["h", "cx", "ccx", "s"] and cols.arity.tolist() == [1, 2, 3, 1]
+
+
+class _StandInRegister:
+    """A register without a device: counts the bytes alive so a test can check a budget."""
+
+    live = 0
+    peak = 0
+    lock = __import__("threading").Lock()
+
+    def __init__(self, nbits: int, precision: int, batch: int = 1) -> None:
+        from lucivant_sim_gb300 import serve
+
+        self.nbits, self.precision, self.batch = nbits, precision, batch
+        self.size = serve.register_bytes(nbits, precision, batch)
+        with self.lock:
+            type(self).live += self.size
+            type(self).peak = max(type(self).peak, type(self).live)
+
+    def free(self) -> None:
+        with self.lock:
+            type(self).live -= self.size
+            self.size = 0
+
+
+def _stand_in_server(monkeypatch, budget: int, run_s: float = 0.0, workers: int = 3):
+    import time as _time
+
+    from lucivant_sim_gb300 import serve
+
+    _StandInRegister.live = _StandInRegister.peak = 0
+    monkeypatch.setattr(_lib, "ensure_device", lambda *a, **k: None)
+    monkeypatch.setattr(_lib, "mem_info", lambda: (1 << 40, 1 << 40))
+    monkeypatch.setattr(_lib, "Register", _StandInRegister)
+    seen: list[tuple[int, int]] = []
+
+    def fake_execute(prep, precision, reg=None):
+        seen.append((srv.used, _StandInRegister.live))
+        _time.sleep(run_s)
+        return {"values": np.zeros(prep["batch"])}
+
+    monkeypatch.setattr(serve, "execute", fake_execute)
+    srv = serve.Server(precision="c64", workers=workers, prep_workers=2, memory_bytes=budget)
+    return srv, seen
+
+
+def test_server_budget_covers_pooled_registers(monkeypatch):
+    """Idle registers kept for reuse stay allocated: across jobs of many shapes, the bytes alive
+    (running jobs' registers plus pooled ones) never exceed the server's budget, and the server's
+    own count covers them."""
+    from lucivant_sim_gb300 import serve
+
+    budget = 192 << 20  # the 64 MiB program room per job lets about two jobs in at once
+    srv, seen = _stand_in_server(monkeypatch, budget, run_s=0.01)
+    jobs = []
+    for i, (n, sweep) in enumerate([(14, 2), (15, 3), (16, 1), (14, 4), (17, 2), (15, 5), (16, 3), (18, 2)] * 2):
+        names = [f"p{k}" for k in range(2 * n)]
+        params = [dict(zip(names, np.random.default_rng(i + s).uniform(0, 6, 2 * n).tolist())) for s in range(sweep)]
+        jobs.append(dict(kind="expect", arrival=0.0, qasm=wl.hea_template(n, 1), params=params,
+                         observable={"Z" * n: 1.0}))  # fmt: skip
+    try:
+        out = serve.replay(jobs, srv, realtime=False)
+        assert len(out["results"]) == len(jobs)
+        assert _StandInRegister.peak <= budget
+        for used, live in seen:
+            assert used <= budget and live <= used
+        assert srv.used == srv.pool.bytes == _StandInRegister.live
+    finally:
+        srv.close()
+    assert _StandInRegister.live == 0 and srv.used == 0
+
+
+def test_server_close_resolves_every_future(monkeypatch):
+    """Closing the server with jobs still queued or in preparation resolves every future: run
+    jobs with their result, the rest with RuntimeError('server closed')."""
+    srv, _ = _stand_in_server(monkeypatch, 1 << 30, run_s=0.3, workers=1)
+    futures = [srv.submit(dict(kind="expect", qasm=wl.hea_template(4, 1), observable={"ZZZZ": 1.0},
+                               params=[{f"p{k}": 0.1 * k for k in range(8)}])) for _ in range(6)]  # fmt: skip
+    import concurrent.futures as cf
+
+    cf.wait(futures, timeout=120, return_when=cf.FIRST_COMPLETED)  # one job has run
+    srv.close()
+    for f in futures:
+        assert f.done()
+        exc = f.exception()
+        assert exc is None or (isinstance(exc, RuntimeError) and "server closed" in str(exc))
+    assert any(f.exception() is not None for f in futures)
+
+
+def test_outcome_pair_space_deposits_like_orrery():
+    """The device computes, per combination of reported pair bits, its probability (scatter of
+    the marginal onto the pair bits, then each pair's readout flips); depositing that space onto
+    classical bits gives the reference's branching result. Here the space is built on the host
+    from the oracle's probabilities, for pairs that share a qubit and pairs that share a bit."""
+    from lucivant_sim_gb300.circuit import final_measurements
+    from lucivant_sim_gb300.noise import ReadoutError
+    from lucivant_sim_gb300.simulator import deposit_pairs
+
+    src = """OPENQASM 3.0; include "stdgates.inc"; qubit[4] q; bit[5] c;
+    h q[0]; cx q[0], q[1]; ry(0.7) q[2]; cx q[2], q[3];
+    c[0] = measure q[0]; c[1] = measure q[1]; c[2] = measure q[1]; c[2] = measure q[3]; c[4] = measure q[2];"""
+    c = ls.parse(src)
+    noise = NoiseModel().add_readout_error(ReadoutError(0.04, 0.09), qubits=[1]).add_readout_error(
+        ReadoutError(0.2, 0.01), qubits=[3])
+    pairs = final_measurements(c)
+    measured = sorted({q for q, _ in pairs})
+    pos = {q: i for i, q in enumerate(measured)}
+    dist = dense.marginal(dense.probabilities_array(c, noise), c.num_qubits, measured)
+    space = np.zeros(1 << len(pairs))
+    for i, p in enumerate(dist):
+        if p > 1e-12:
+            space[sum(((i >> pos[q]) & 1) << j for j, (q, _) in enumerate(pairs))] = p
+    for j, (q, _) in enumerate(pairs):
+        err = noise.readout_error(q)
+        if err is None:
+            continue
+        b = 1 << j
+        for e in range(space.size):
+            if not e & b:
+                a0, a1 = space[e], space[e | b]
+                space[e], space[e | b] = a0 * (1 - err.p01) + a1 * err.p10, a0 * err.p01 + a1 * (1 - err.p10)
+    got = deposit_pairs(space, [cb for _, cb in pairs], c.num_clbits)
+    want = dense.outcome_probabilities(c, noise)
+    got = {ls.simulator.format_bits(c, k): v for k, v in got.items() if v > 1e-12}
+    assert got.keys() == want.keys()
+    assert all(abs(got[k] - v) < 1e-14 for k, v in want.items())

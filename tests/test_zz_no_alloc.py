@@ -20,6 +20,23 @@ from lucivant_sim_gb300 import _lib, engine, qasm, workloads as wl
 pytestmark = pytest.mark.gpu
 
 ATOL = 1e-12  # complex128 path: same tolerance as the other expectation tests
+ATOL_C64 = 1e-5  # complex64 amplitudes, FP64 accumulation
+
+
+def _numpy_expect(vec: np.ndarray, xs: list[int], zs: list[int]) -> np.ndarray:
+    """<v|P|v> per term, computed on the host from the amplitudes (independent of the library)."""
+    idx = np.arange(vec.size, dtype=np.uint64)
+    out = []
+    for x, z in zip(xs, zs, strict=True):
+        ny = bin(x & z).count("1") & 3
+        w = np.conj(vec[idx ^ np.uint64(x)]) * vec
+        masked, parity = idx & np.uint64(z), np.zeros_like(idx)
+        while masked.any():
+            parity ^= masked & np.uint64(1)
+            masked >>= np.uint64(1)
+        sign = 1.0 - 2.0 * parity.astype(np.float64)
+        out.append(float(np.real((1j**ny) * np.sum(w * sign))))
+    return np.array(out)
 
 
 def _noalloc(lib, amps, precision, nbits, batch, dm, xs, zs, out, stream):
@@ -56,6 +73,40 @@ def test_noalloc_matches_expect_pauli_twice_in_a_row():
             assert rc == 0, lib.lsg_last_error().decode()
             got = out.cpu().numpy().reshape(count, batch)
             assert np.max(np.abs(got - want)) < ATOL
+            for b in range(batch):  # and against a host computation from the same amplitudes
+                assert np.max(np.abs(got[:, b] - _numpy_expect(host[b].reshape(-1), xs, zs))) < ATOL
+
+
+def test_noalloc_complex64_matches_expect_pauli_and_refuses_bad_requests():
+    torch = pytest.importorskip("torch")
+    lib = _lib.library()
+    n, batch = 9, 2
+    circuit = qasm.parse(wl.hea(n, 2, seed=6))
+    with _lib.Register(n, _lib.C64, batch=batch) as reg:
+        reg.apply(engine.sv_oplist(circuit))
+        host = reg.download()  # complex128 on the host: the device holds complex64
+        amps = torch.from_numpy(host.reshape(-1).astype(np.complex64)).to("cuda")
+        stream = torch.cuda.current_stream().cuda_stream
+        xs, zs = _terms(n, 3, 10)
+        want = reg.expect(0, xs, zs)
+        out = torch.full((10 * batch,), float("nan"), dtype=torch.float64, device="cuda")
+        for _ in range(2):  # two calls in a row
+            rc = _noalloc(lib, amps.data_ptr(), _lib.C64, n, batch, 0, xs, zs, out.data_ptr(), stream)
+            assert rc == 0, lib.lsg_last_error().decode()
+            got = out.cpu().numpy().reshape(10, batch)
+            assert np.max(np.abs(got - want)) < ATOL_C64
+            exact = _numpy_expect(host[0].reshape(-1).astype(np.complex128), xs, zs)
+            assert np.max(np.abs(got[:, 0] - exact)) < ATOL_C64
+        # a host buffer is not device memory: refused before any launch
+        host_out = np.zeros(10 * batch)
+        rc = _noalloc(lib, amps.data_ptr(), _lib.C64, n, batch, 0, xs, zs, host_out.ctypes.data, stream)
+        assert rc == _lib.LSG_E_ARG and b"device memory" in lib.lsg_last_error()
+    # more members than one launch's grid takes: refused with a message, not a launch failure
+    members = 65_536
+    many = torch.zeros(members, dtype=torch.complex64, device="cuda")  # one amplitude per member
+    out = torch.zeros(members, dtype=torch.float64, device="cuda")
+    rc = _noalloc(lib, many.data_ptr(), _lib.C64, 0, members, 0, [0], [0], out.data_ptr(), stream)
+    assert rc == _lib.LSG_E_ARG and b"at most 65535" in lib.lsg_last_error()
 
 
 def test_noalloc_density_register_and_size_limit():
