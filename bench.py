@@ -56,6 +56,7 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--instances", type=int, default=INSTANCES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c64", action="store_true", help="skip the complex64 batched run beside the headline")
+    ap.add_argument("--no-autotune", action="store_true", help="default plan choices (no autotuner search)")
     ap.add_argument("--ref-full", type=int, default=0, metavar="N",
                     help="reference arm: evolve N whole instances (one per host process) instead of timed samples")
     ap.add_argument("--workload", choices=("dm-batch", "serve", "sv20", "traj18", "stab2048"), default="dm-batch",
@@ -513,7 +514,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     real64 = args.precision == "c128"
     fp64_peak = fp64_peak_tflops() if real64 and rank == 0 else None
 
-    batch = DensityBatch(circuit, noises, precision=args.precision, autotune=True)
+    batch = DensityBatch(circuit, noises, precision=args.precision, autotune=not args.no_autotune)
     passes, real = batch.program.passes, batch.reg.real
     tune = batch.tune
     kernel = f"k_tile_pipe<{'double' if real64 else 'float'}>" if real else \
@@ -555,7 +556,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     # the complex64 request beside it: real32 register, the same instances
     c64 = None
     if not args.no_c64 and real64:
-        b32 = DensityBatch(circuit, noises, precision="c64", autotune=True)
+        b32 = DensityBatch(circuit, noises, precision="c64", autotune=not args.no_autotune)
         stream32 = torch.cuda.ExternalStream(b32.reg.stream())
         r32 = timed_batch(b32, labels, args.steps, args.warmup, stream32, local, dist)
         roof32 = pass_rooflines(b32, r32["pass_ms"], False, None)
@@ -584,11 +585,12 @@ def gb300_arm(args: argparse.Namespace) -> None:
     e2e_steps = max(2, args.steps // 2)
     # one untimed call: the halves the call evolves are programs of their own shape (specialized
     # passes compiled once per process, like the whole batch's above)
-    run_density_batch(circuit, noises, labels, precision=args.precision, autotune=True)
+    run_density_batch(circuit, noises, labels, precision=args.precision, autotune=not args.no_autotune)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        probs_h, exps_h = run_density_batch(circuit, noises, labels, precision=args.precision, autotune=True)
+        probs_h, exps_h = run_density_batch(circuit, noises, labels, precision=args.precision,
+                                            autotune=not args.no_autotune)
     e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
     # operator tables and data pools (one per half the call evolves), Pauli masks
     h2d = int(e2e_upload_bytes(circuit, noises) + 2 * 8 * len(labels))

@@ -1,0 +1,115 @@
+"""Host-side pins against Orrery's results at the benchmarked sizes (``tests/golden/configs.*``,
+made by ``tests/golden/make_golden_configs.py`` running Orrery 0.3.0 itself).
+
+No device is used: these check that the benchmark builds the same noise models and circuits
+Orrery ran, that the host's Clifford conjugation tables (shared by the engine and the oracle)
+are Orrery's for every gate name, and that the oracle reproduces Orrery's per-shot trajectory
+draws on the 18-qubit, 16-round workload.
+"""
+
+from __future__ import annotations
+
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import lucivant_sim_gb300 as ls
+from lucivant_sim_gb300 import workloads as wl
+from lucivant_sim_gb300.clifford import clifford_map, kind_of
+from lucivant_sim_gb300.gates import GATES
+from lucivant_sim_gb300.noise import NoiseModel
+from oracle import dense, tableau
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def cfg() -> dict:
+    path = GOLDEN / "configs.json"
+    if not path.exists():
+        pytest.skip("benchmark-size fixtures not generated")
+    return json.loads(path.read_text())["cases"]
+
+
+@pytest.fixture(scope="module")
+def cfg_arrays() -> dict:
+    with np.load(GOLDEN / "configs.npz") as data:
+        return {k: data[k] for k in data.files}
+
+
+def test_benchmark_noise_models_are_the_ones_orrery_ran(cfg):
+    """The benchmark's 256 instances (seed 7) carry Orrery's noise models, digest for digest."""
+    noises = wl.dm_noise_instances(256, seed=7)
+    members = [int(k[len("cfg2_inst"):]) for k in cfg if k.startswith("cfg2_inst")]
+    assert members, "no batched-instance fixtures"
+    for m in members:
+        assert noises[m].digest() == cfg[f"cfg2_inst{m}"]["noise_digest"], m
+    assert wl.dm_noise().digest() == cfg["cfg2_plain"]["noise_digest"]
+    assert NoiseModel.uniform(single=1e-3, two=1e-2).digest() == cfg["cfg3_serial64"]["noise_digest"]
+    assert wl.stabilizer_noise(1e-3).digest() == cfg["cfg4_full"]["noise_digest"]
+
+
+def test_fixture_outputs_are_consistent(cfg, cfg_arrays):
+    """Each density-matrix fixture is a probability distribution whose <Z_i> agree with it."""
+    for name, case in cfg.items():
+        if not name.startswith("cfg2_") or name.endswith("expectation"):
+            continue
+        p = cfg_arrays[f"{name}_probs"]
+        assert p.shape == (4096,) and abs(p.sum() - 1) < 1e-12
+        idx = np.arange(4096)
+        z0 = float(np.sum(p * (1 - 2 * (idx & 1))))
+        assert abs(z0 - case["z"][0]) < 1e-12
+
+
+def test_clifford_tables_are_orreys_for_every_gate(cfg, cfg_arrays):
+    """The host's conjugation table and named kind of every gate Orrery knows, at Clifford
+    parameter values, equal Orrery's bit for bit (they drive the tableau kernels and the oracle)."""
+    maps = cfg["clifford_maps"]["maps"]
+    assert len(maps) >= 60
+    for key, info in maps.items():
+        m = np.asarray(GATES[info["name"]].build(*info["params"]), dtype=np.complex128)
+        cmap = clifford_map(m)
+        assert cmap is not None, key
+        assert np.array_equal(cmap.bits, cfg_arrays[f"cmap_bits::{key}"]), key
+        assert np.array_equal(cmap.sign, cfg_arrays[f"cmap_sign::{key}"]), key
+        assert kind_of(cmap) == info["kind"], key
+
+
+def test_oracle_tableau_matches_orrery_over_every_clifford_gate(cfg, cfg_arrays):
+    """A 6-qubit circuit over every Clifford gate name (twice, shuffled): the oracle's tableau is
+    Orrery's."""
+    c = ls.parse(clifford_program(cfg["clifford_maps"]["program"]))
+    t = tableau.reference_tableau(c)
+    assert np.array_equal(t.x, cfg_arrays["cliff6_x"])
+    assert np.array_equal(t.z, cfg_arrays["cliff6_z"])
+    assert np.array_equal(t.r, cfg_arrays["cliff6_r"])
+
+
+def clifford_program(applied: list) -> str:
+    """OpenQASM text of the fixture's gate list (parameters written exactly)."""
+    lines = ["OPENQASM 3.0;", 'include "stdgates.inc";', "qubit[6] q;"]
+    for name, params, qs in applied:
+        head = f"{name}({', '.join(repr(float(p)) for p in params)})" if params else name
+        lines.append(f"{head} " + ", ".join(f"q[{q}]" for q in qs) + ";")
+    return "\n".join(lines) + "\n"
+
+
+def test_oracle_serial_trajectories_follow_orreys_draws(cfg):
+    """The first 12 shots of the 18-qubit, 16-round mid-circuit workload (uniform noise 1e-3 /
+    1e-2, seed 7): the oracle's outcomes are Orrery's shot for shot."""
+    g = cfg["cfg3_serial64"]
+    c = ls.parse(wl.midcircuit(*g["qasm_args"]))
+    noise = NoiseModel.uniform(single=1e-3, two=1e-2)
+    rng = np.random.default_rng(g["seed"])
+    got = [dense.trajectory(c, noise, rng) for _ in range(12)]
+    assert got == g["shot_bits"][:12]
+
+
+def test_orrery_timings_recorded(cfg):
+    """The fixtures record how long Orrery took on this workload (the CPU reference)."""
+    for m in (0, 1, 128, 255):
+        assert cfg[f"cfg2_inst{m}"]["orrery_seconds"] > 0
+    assert math.isfinite(cfg["cfg4_full"]["orrery_run_seconds"])
