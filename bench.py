@@ -171,6 +171,18 @@ def measured_peak() -> tuple[float, str]:
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def ncu_traffic(tag: str) -> list[float] | None:
+    """DRAM bytes (read + write) per pass of a full-size launch, from the committed ncu summary
+    (an 8-instance capture scaled by the members), or None."""
+    path = ROOT / "profiles" / f"tile_pass_dm12_{tag}.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_pass:"):
+            return [float(x) for x in line.split(":", 1)[1].split(",")]
+    return None
+
+
 def fp64_peak_tflops() -> float:
     """FP64 rate of cuBLAS (torch float64 matmul, 4096^3, best of 5) on this GPU: the measured
     denominator of the real64 passes' arithmetic roofline."""
@@ -464,17 +476,18 @@ def pass_rooflines(batch, pass_ms, real64: bool, fp64_peak: float | None) -> dic
 
     info = batch.program.pass_info()
     med = np.median(pass_ms.astype(np.float64), axis=0)  # ms per pass, median over the timed steps
-    elems = batch.batch << (2 * batch.n)
+    elem_bytes = batch.register_bytes // (batch.batch << (2 * batch.n))
+    visited = info["bytes"] // (2 * elem_bytes)  # elements in the tiles each pass visits
     per_pass = []
     for i, ms in enumerate(med.astype(np.float64).tolist()):
         gbs = float(info["bytes"][i]) / (ms / 1000) / 1e9
-        tflops = float(info["flops_per_element"][i]) * elems / (ms / 1000) / 1e12
+        tflops = float(info["flops_per_element"][i]) * float(visited[i]) / (ms / 1000) / 1e12
         per_pass.append({"pass": i, "ms": round(float(ms), 4), "blocks": int(info["blocks"][i]),
                          "bytes": int(info["bytes"][i]), "hbm_gbs": round(gbs, 1),
                          "flops_per_element": float(info["flops_per_element"][i]), "tflops": round(tflops, 4)})  # fmt: skip
     total_s = float(med.sum()) / 1000
     moved = float(info["bytes"].sum())
-    flops = float(info["flops_per_element"].sum()) * elems
+    flops = float((info["flops_per_element"] * visited).sum())
     peak, peak_kind = measured_peak()
     hbm = {"bound": "hbm", "achieved": moved / total_s / 1e9, "peak": peak, "unit": "GB/s",
            "frac": moved / total_s / 1e9 / peak, "bytes_per_launch": moved / len(med),
@@ -570,7 +583,8 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "speedup_vs_plain_c128": cps32 / plain_cps,
             "speedup_vs_batched_f64": cps32 / cps,
             "roofline": dict(roof32["hbm"], kernel=f"lsg_pass_0..{b32.program.passes - 1} (real32)",
-                             traffic=None, heaviest_pass=roof32["heaviest_pass"]),  # fmt: skip
+                             traffic=(lambda t: sum(t) / len(t) if t else None)(ncu_traffic("c64")),
+                             heaviest_pass=roof32["heaviest_pass"]),  # fmt: skip
             "per_pass": roof32["per_pass"],
             "accuracy_vs_orrery": golden_errors(r32["probs"], r32["exps"], golden),
             "accuracy_vs_gpu_c128": {
@@ -597,12 +611,16 @@ def gb300_arm(args: argparse.Namespace) -> None:
     d2h = int(probs_h.nbytes + exps_h.nbytes)
 
     if rank == 0:
+        tr = ncu_traffic("f64" if real64 else "c64")
+        traffic = sum(tr) / len(tr) if tr else None  # mean DRAM bytes per full-size launch (ncu)
         if real64:
-            roofline = dict(roof["arith"], kernel=kernel, traffic=None, hbm=roof["hbm"],
+            roofline = dict(roof["arith"], kernel=kernel, traffic=traffic, hbm=roof["hbm"],
                             heaviest_pass=roof["heaviest_pass"])  # fmt: skip
         else:
-            roofline = dict(roof["hbm"], kernel=kernel, traffic=None, arith=roof["arith"],
+            roofline = dict(roof["hbm"], kernel=kernel, traffic=traffic, arith=roof["arith"],
                             heaviest_pass=roof["heaviest_pass"])  # fmt: skip
+        roofline["traffic_source"] = (f"profiles/tile_pass_dm12_{'f64' if real64 else 'c64'}.md: ncu DRAM read+write "
+                                      "of an 8-instance capture x 32, per launch, mean over the passes")
         line = {
             "metric": "circuits/s",
             "value": cps,

@@ -734,7 +734,13 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
             bool tp = true;
             for (int64_t b = 0; b < (t.stride ? batch : 1) && tp; ++b)
                 for (int c = 0; c < 4 && tp; ++c) tp = pool[2 * (t.data + b * t.stride + c)] == (c == 0 ? 1.0 : 0.0);
-            if (tp) t.tmpl = kT_TPD2 + (t.tmpl - kT_DENSE2);
+            if (!tp) continue;
+            t.tmpl = kT_TPD2 + (t.tmpl - kT_DENSE2);
+            int zmask = (1 << 12) - 1;  // rows 1-3: the coefficients that are zero for every member
+            for (int64_t b = 0; b < (t.stride ? batch : 1) && zmask; ++b)
+                for (int i = 0; i < 12; ++i)
+                    if (pool[2 * (t.data + b * t.stride + 4 + i)] != 0.0) zmask &= ~(1 << i);
+            t.zmask = zmask;
         }
     // permutations with unit phases shared by all members are register renames
     for (TileOp& t : p->plan.ops) {
@@ -1379,7 +1385,14 @@ static double op_flops_per_element(const lsg::TileOp& op, bool complex_elems) {
     const double mul = complex_elems ? 6.0 : 1.0;  // one (complex) product per element
     if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) return complex_elems ? 14.0 : 3.0;
     if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) return complex_elems ? 30.0 : 7.0;
-    if (c >= kT_TPD2 && c < kT_TPD2 + 16) return 5.25;
+    if (c >= kT_TPD2 && c < kT_TPD2 + 16) {  // rows 1-3: a product, then a multiply-add per further term
+        double f = 0.0;
+        for (int r = 0; r < 3; ++r) {
+            const int terms = 4 - __builtin_popcount((unsigned)(op.zmask >> (4 * r)) & 15u);
+            f += terms ? 1.0 + 2.0 * (terms - 1) : 0.0;
+        }
+        return f / 4.0;
+    }
     if ((c >= kT_PERM1 && c < kT_PERM1 + 4) || (c >= kT_PERM2 && c < kT_PERM2 + 16)) return mul;
     if (c == kT_DIAGB || c == kT_SCALE || c == kT_DIAG) return mul;
     if ((c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) || c == kT_DEPOL2) return 4.0;

@@ -118,10 +118,12 @@ bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int a
         if (packed && data_op) o << "rp_" << fn << "<" << U;
         else o << "rb_" << fn << "<" << (packed ? "lsg::F2" : T) << ", " << U;
     };
-    auto two = [&](const char* fn, int base, bool data_op = true) {
+    auto two = [&](const char* fn, int base, bool data_op = true, int extra = 0) {
         const int r = c - base;
         name(fn, data_op);
-        o << ", " << r / 4 << ", " << r % 4 << ">";
+        o << ", " << r / 4 << ", " << r % 4;
+        if (extra) o << ", " << extra;
+        o << ">";
     };
     auto one = [&](const char* fn, int base, bool data_op = true) {
         name(fn, data_op);
@@ -130,7 +132,7 @@ bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int a
     bool data = true;
     if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) one("dense1", kT_DENSE1);
     else if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) two("dense2", kT_DENSE2);
-    else if (c >= kT_TPD2 && c < kT_TPD2 + 16) two("tpd2", kT_TPD2);
+    else if (c >= kT_TPD2 && c < kT_TPD2 + 16) two("tpd2", kT_TPD2, true, t.zmask);  // zero terms left out
     else if (c >= kT_PERM1 && c < kT_PERM1 + 4) one("perm1", kT_PERM1);
     else if (c >= kT_PERM2 && c < kT_PERM2 + 16) two("perm2", kT_PERM2);
     else if (packed && ((c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) || c == kT_DEPOL2)) return false;  // complex only

@@ -54,7 +54,9 @@ struct TileOp {
     int count;      // mixture branches
     int tmpl;       // register-block code: kind and positions (see tile.cuh)
     int pos[8];     // positions of the operator's bits within its block (0 = block MSB)
-    int pad[2];
+    int zmask;      // trace-preserving 4x4 operators: coefficients zero for every member
+                    // (bit 4 * (row - 1) + column), left out by specialized passes
+    int pad;
 };
 
 // The descriptors are staged back to back in shared memory, followed by 16-byte operator records:

@@ -320,8 +320,12 @@ __device__ __forceinline__ void rb_dense2(T* v, const T* m) {
 }
 
 // A real 4x4 transfer matrix with first row (1,0,0,0) (trace preserving): output 0 keeps its
-// input, rows 1-3 are computed. 12 multiply-adds per 4 elements instead of 16.
-template <typename T, int U, int P0, int P1>
+// input, rows 1-3 are computed. 12 multiply-adds per 4 elements instead of 16. Z (specialized
+// passes) marks coefficients that are exactly zero for every member, bit 4 * (r - 1) + c for
+// row r, column c: their terms are left out. A zero term adds an exact zero to the row's sum, so
+// leaving it out gives the same values (a noisy one-qubit gate's X and Y rows have a zero first
+// column: 10 multiply-adds per 4 elements).
+template <typename T, int U, int P0, int P1, int Z = 0>
 __device__ __forceinline__ void rb_tpd2(T* v, const T* m) {
     if constexpr (!Elem<T>::complex) {
         constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
@@ -330,13 +334,17 @@ __device__ __forceinline__ void rb_tpd2(T* v, const T* m) {
 #pragma unroll
         for (int e = 0; e < (1 << U); ++e) {
             if (e & (B0 | B1)) continue;
-            const T a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+            const T a[4] = {v[e], v[e | B1], v[e | B0], v[e | B0 | B1]};
 #pragma unroll
             for (int r = 1; r < 4; ++r) {
-                T acc = cmul(mm[4 * r - 4], a0);
-                acc = cfma(mm[4 * r - 3], a1, acc);
-                acc = cfma(mm[4 * r - 2], a2, acc);
-                acc = cfma(mm[4 * r - 1], a3, acc);
+                T acc{};
+                bool first = true;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (Z & (1 << (4 * (r - 1) + c))) continue;
+                    acc = first ? cmul(mm[4 * r - 4 + c], a[c]) : cfma(mm[4 * r - 4 + c], a[c], acc);
+                    first = false;
+                }
                 v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
             }
         }
@@ -545,7 +553,7 @@ __device__ __forceinline__ void rp_dense2(F2* v, const float* m) {
     }
 }
 
-template <int U, int P0, int P1>
+template <int U, int P0, int P1, int Z = 0>
 __device__ __forceinline__ void rp_tpd2(F2* v, const float* m) {
     constexpr int B0 = 1 << (U - 1 - P0), B1 = 1 << (U - 1 - P1);
     float mm[12];
@@ -553,13 +561,17 @@ __device__ __forceinline__ void rp_tpd2(F2* v, const float* m) {
 #pragma unroll
     for (int e = 0; e < (1 << U); ++e) {
         if (e & (B0 | B1)) continue;
-        const F2 a0 = v[e], a1 = v[e | B1], a2 = v[e | B0], a3 = v[e | B0 | B1];
+        const F2 a[4] = {v[e], v[e | B1], v[e | B0], v[e | B0 | B1]};
 #pragma unroll
         for (int r = 1; r < 4; ++r) {
-            F2 acc = f2_mul(mm[4 * r - 4], a0);
-            acc = f2_fma(mm[4 * r - 3], a1, acc);
-            acc = f2_fma(mm[4 * r - 2], a2, acc);
-            acc = f2_fma(mm[4 * r - 1], a3, acc);
+            F2 acc = f2_bcast(0.0f);
+            bool first = true;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (Z & (1 << (4 * (r - 1) + c))) continue;
+                acc = first ? f2_mul(mm[4 * r - 4 + c], a[c]) : f2_fma(mm[4 * r - 4 + c], a[c], acc);
+                first = false;
+            }
             v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
         }
     }

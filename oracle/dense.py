@@ -274,6 +274,69 @@ def trajectory(circuit: Any, noise: Any, rng: np.random.Generator) -> int:
     return sum(b << i for i, b in enumerate(clbits))
 
 
+def exact_outcomes(circuit: Any, noise: Any = None) -> dict[int, float]:
+    """The exact distribution of the classical bits a trajectory run produces, for circuits with
+    mid-circuit measurement, conditions and resets: one density matrix per classical record,
+    summed over the shots' branches. The trajectory rules it averages are ``simulator.py:287-317``
+    with ``engines.py:159-205``: a gate's noise channel picked by Born weight averages to the
+    channel; a measurement splits a record by projection, its readout error mixes the recorded
+    bit; a reset (measure, then X on 1) is the channel {|0><0|, |0><1|}; a condition picks the
+    branch per record. Keys are the classical bits as an integer (bit c = classical bit c)."""
+    n = circuit.num_qubits
+    if n > 10:
+        raise OracleError("exact trajectory outcomes are for up to 10 qubits")
+    nb = 2 * n
+    rho0 = np.zeros(1 << nb, dtype=np.complex128)
+    rho0[0] = 1
+    records: dict[tuple[int, ...], C128] = {tuple([0] * circuit.num_clbits): rho0}
+    reset_kraus = (np.array([[1, 0], [0, 0]], dtype=np.complex128), np.array([[0, 1], [0, 0]], dtype=np.complex128))
+
+    def project(rho: C128, q: int, bit: int) -> C128:
+        proj = np.diag([1.0 - bit, float(bit)]).astype(np.complex128)
+        return apply_bits(apply_bits(rho, nb, proj, [n + q]), nb, proj, [q])
+
+    def walk(recs: dict[tuple[int, ...], C128], ops: Any) -> dict[tuple[int, ...], C128]:
+        for op in ops:
+            k = op.kind
+            if k == "gate":
+                ch = noise.gate_error(op.name, op.qubits) if noise else None
+                for key, rho in recs.items():
+                    rho = apply_bits(rho, nb, op.matrix, [n + q for q in op.qubits])
+                    rho = apply_bits(rho, nb, op.matrix.conj(), list(op.qubits))
+                    recs[key] = dm_channel(rho, n, ch, op.qubits) if ch is not None else rho
+            elif k == "measure":
+                err = noise.readout_error(op.qubit) if noise else None
+                p01, p10 = (float(err.p01), float(err.p10)) if err is not None else (0.0, 0.0)
+                out: dict[tuple[int, ...], C128] = {}
+                for key, rho in recs.items():
+                    for true in (0, 1):
+                        part = project(rho, op.qubit, true)
+                        flip = p10 if true else p01
+                        for seen, w in ((true, 1.0 - flip), (true ^ 1, flip)):
+                            if w == 0.0:
+                                continue
+                            bits = list(key)
+                            if op.clbit is not None:
+                                bits[op.clbit] = seen
+                            t = tuple(bits)
+                            out[t] = out[t] + w * part if t in out else w * part
+                recs = out
+            elif k == "reset":
+                for key, rho in recs.items():
+                    recs[key] = dm_kraus(rho, n, reset_kraus, (op.qubit,))
+            elif k == "if":
+                yes = {kk: v for kk, v in recs.items() if op.condition.holds(list(kk))}
+                no = {kk: v for kk, v in recs.items() if not op.condition.holds(list(kk))}
+                recs = walk(yes, op.then)
+                for kk, v in walk(no, op.otherwise).items():
+                    recs[kk] = recs[kk] + v if kk in recs else v
+        return recs
+
+    final = walk(records, circuit.operations)
+    d = 1 << n
+    return {sum(b << i for i, b in enumerate(key)): float(np.real(np.trace(rho.reshape(d, d)))) for key, rho in final.items()}
+
+
 # ----------------------------------------------------------------------------- run
 
 

@@ -62,7 +62,7 @@ def test_bad_plan_options_are_refused():
                     _lib.PlanOpts(max_ops=500), _lib.PlanOpts(tile_bits=6, low_bits=7)):  # fmt: skip
             with pytest.raises(ValueError):
                 _lib.Program(reg, ops, bad)
-        prog = _lib.Program(reg, ops, _lib.PlanOpts(tile_bits=7, max_ops=3))
+        prog = _lib.Program(reg, ops, _lib.PlanOpts(tile_bits=8, max_ops=3))
         try:
             assert prog.passes >= len(ops) // 3
         finally:

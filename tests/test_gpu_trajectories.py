@@ -56,19 +56,44 @@ def test_known_answers_reset_and_if():
     assert ls.run(c, shots=50, seed=1).counts == {"11": 50}
 
 
+def chi2_pvalue(counts: dict[int, int], exact: dict[int, float]) -> float:
+    """Pearson chi-square p-value of ``counts`` against the exact distribution: outcomes
+    expected at least 5 times are their own bins, the rest one pooled bin."""
+    from scipy.stats import chi2
+
+    shots = sum(counts.values())
+    stat, bins, pooled_o, pooled_e = 0.0, 0, 0, 0.0
+    for k in set(exact) | set(counts):
+        e, o = shots * exact.get(k, 0.0), counts.get(k, 0)
+        if e >= 5:
+            stat += (o - e) ** 2 / e
+            bins += 1
+        else:
+            pooled_o += o
+            pooled_e += e
+    if pooled_e > 0:
+        stat += (pooled_o - pooled_e) ** 2 / pooled_e
+        bins += 1
+    return float(chi2.sf(stat, max(bins - 1, 1)))
+
+
 @pytest.mark.parametrize("precision", [_lib.C128, _lib.C64])
-def test_batched_mode_agrees_with_serial(precision):
-    c = ls.parse(wl.midcircuit(10, 3, seed=5))
+@pytest.mark.parametrize("mode", ["batched", "serial"])
+def test_counts_follow_the_exact_outcome_distribution(precision, mode):
+    """8 qubits x 3 rounds of mid-circuit measurement, conditional X and reset with gate and
+    readout noise: the counts of 20,000 shots (6,000 serial) against the oracle's exact
+    distribution of the classical record (a density matrix per record), chi-square p > 1e-6."""
+    if mode == "serial" and precision == _lib.C64:
+        pytest.skip("serial mode is Orrery's complex128 draw order")
+    c = ls.parse(wl.midcircuit(8, 3, seed=5))
     noise = NoiseModel.uniform(single=1e-2, two=3e-2, readout=2e-2)
-    shots = 8000
-    serial, _ = trajectories.run_shots(c, shots, noise, np.random.default_rng(1), _lib.C128, "serial")
-    batched, _ = trajectories.run_shots(c, shots, noise, np.random.default_rng(2), precision, "batched")
-    assert sum(batched.values()) == shots
-    # each classical bit's marginal: two independent samples, sd about 0.008 each
-    for bit in range(c.num_clbits):
-        ps = sum(v for k, v in serial.items() if (k >> bit) & 1) / shots
-        pb = sum(v for k, v in batched.items() if (k >> bit) & 1) / shots
-        assert abs(ps - pb) < 0.04, (bit, ps, pb)
+    exact = dense.exact_outcomes(c, noise)
+    assert abs(sum(exact.values()) - 1) < 1e-12
+    shots = 20_000 if mode == "batched" else 6_000
+    counts, _ = trajectories.run_shots(c, shots, noise, np.random.default_rng(11), precision, mode)
+    assert sum(counts.values()) == shots
+    assert set(counts) <= {k for k, p in exact.items() if p > 0}
+    assert chi2_pvalue(counts, exact) > 1e-6
 
 
 def test_kraus_channel_statistics_against_density_matrix():

@@ -168,3 +168,38 @@ def test_known_endianness_of_registers():
     c = _parse("OPENQASM 3; qubit[3] q; bit[1] a; bit[2] b; x q[1]; a[0] = measure q[0]; b = measure q[1:2];")
     counts, method, _ = dense.run_counts(c, 50, 3)
     assert counts == {"01 0": 50}
+
+
+def test_exact_trajectory_outcomes_explain_orreys_counts(golden):
+    """The oracle's exact outcome distribution of a noisy mid-circuit program against Orrery's
+    300 recorded shots (chi-square over outcomes expected 5 times or more, pooled tail), and
+    against 2,000 shots of the oracle's own trajectories."""
+    from scipy.stats import chi2
+
+    g = golden["traj_mid8"]
+    c = qasm.parse(g["qasm"])
+    noise = NoiseModel.uniform(single=2e-2, two=5e-2, readout=3e-2)
+    exact = dense.exact_outcomes(c, noise)
+    assert abs(sum(exact.values()) - 1) < 1e-12
+
+    def pvalue(counts: dict[int, int]) -> float:
+        shots = sum(counts.values())
+        stat, bins, po, pe = 0.0, 0, 0, 0.0
+        for k in set(exact) | set(counts):
+            e, o = shots * exact.get(k, 0.0), counts.get(k, 0)
+            if e >= 5:
+                stat, bins = stat + (o - e) ** 2 / e, bins + 1
+            else:
+                po, pe = po + o, pe + e
+        if pe > 0:
+            stat, bins = stat + (po - pe) ** 2 / pe, bins + 1
+        return float(chi2.sf(stat, max(bins - 1, 1)))
+
+    orrery = {int(k.replace(" ", ""), 2): v for k, v in g["counts"].items()}
+    assert pvalue(orrery) > 1e-4
+    rng = np.random.default_rng(5)
+    own: dict[int, int] = {}
+    for _ in range(2000):
+        b = dense.trajectory(c, noise, rng)
+        own[b] = own.get(b, 0) + 1
+    assert pvalue(own) > 1e-4
