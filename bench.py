@@ -52,7 +52,8 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--precision", choices=("c128", "c64"), default="c128")
+    ap.add_argument("--precision", choices=("c128", "c64", "df64"), default="c128",
+                    help="c128: real64 Pauli-transfer register (FP64); c64: real32; df64: double-float pairs")
     ap.add_argument("--instances", type=int, default=INSTANCES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c64", action="store_true", help="skip the complex64 batched run beside the headline")
@@ -400,7 +401,7 @@ def reference_arm(args: argparse.Namespace) -> None:
 
 
 def config_block(args: argparse.Namespace) -> dict:
-    elem = 8 if args.precision == "c128" else 4
+    elem = 4 if args.precision == "c64" else 8
     return {
         "workload": f"density_matrix {QUBITS}q x {LAYERS} brickwork layers, {args.instances} noise instances per GPU",
         "qubits": QUBITS,
@@ -524,14 +525,14 @@ def gb300_arm(args: argparse.Namespace) -> None:
     circuit, labels = workload()
     noises = wl.dm_noise_instances(args.instances, seed=SEED + rank)
     golden = load_golden() if rank == 0 else {}
-    real64 = args.precision == "c128"
+    real64 = args.precision == "c128"  # the FP64 register: an FP64 roofline; df64 and c64: HBM
     fp64_peak = fp64_peak_tflops() if real64 and rank == 0 else None
 
     batch = DensityBatch(circuit, noises, precision=args.precision, autotune=not args.no_autotune)
     passes, real = batch.program.passes, batch.reg.real
     tune = batch.tune
-    kernel = f"k_tile_pipe<{'double' if real64 else 'float'}>" if real else \
-        f"k_tile_pipe<Cx<{'double' if real64 else 'float'}>>"
+    elem = {"c128": "double", "c64": "float", "df64": "lsg::DF"}[args.precision]
+    kernel = f"k_tile_pipe<{elem}>" if real else f"k_tile_pipe<Cx<{elem}>>"
     specialized = batch.program.specialized
     if specialized:  # the passes run as kernels compiled for this circuit at run time
         kernel = f"lsg_pass_0..{passes - 1} (pipe_kernel specializations of {kernel})"
@@ -566,34 +567,39 @@ def gb300_arm(args: argparse.Namespace) -> None:
     plain.free()
     plain_cps = world / plain_s
 
-    # the complex64 request beside it: real32 register, the same instances
-    c64 = None
-    if not args.no_c64 and real64:
-        b32 = DensityBatch(circuit, noises, precision="c64", autotune=not args.no_autotune)
-        stream32 = torch.cuda.ExternalStream(b32.reg.stream())
-        r32 = timed_batch(b32, labels, args.steps, args.warmup, stream32, local, dist)
-        roof32 = pass_rooflines(b32, r32["pass_ms"], False, None)
-        cps32 = args.instances * args.steps * world / r32["elapsed"]
-        c64 = {
-            "circuits_per_s": cps32,
-            "ms_per_step": 1000 * r32["elapsed"] / args.steps,
-            "dtype": "f32",
-            "fused_passes": b32.program.passes,
-            "autotune": _tune_summary(b32.tune),
-            "speedup_vs_plain_c128": cps32 / plain_cps,
-            "speedup_vs_batched_f64": cps32 / cps,
-            "roofline": dict(roof32["hbm"], kernel=f"lsg_pass_0..{b32.program.passes - 1} (real32)",
-                             traffic=(lambda t: sum(t) / len(t) if t else None)(ncu_traffic("c64")),
-                             heaviest_pass=roof32["heaviest_pass"]),  # fmt: skip
-            "per_pass": roof32["per_pass"],
-            "accuracy_vs_orrery": golden_errors(r32["probs"], r32["exps"], golden),
-            "accuracy_vs_gpu_c128": {
-                "probability_tvd": 0.5 * float(np.abs(r32["probs"][0] - probs0[0]).sum()),
-                "max_expectation_error": float(np.max(np.abs(r32["exps"][:, 0] - exps0[:, 0]))),
+    # the same instances in the other registers beside it: real32 (the complex64 request) and
+    # double-float pairs (FP64-level accuracy from FP32 arithmetic)
+    def beside(prec: str, dtype: str, what: str) -> dict:
+        bx = DensityBatch(circuit, noises, precision=prec, autotune=not args.no_autotune)
+        rx = timed_batch(bx, labels, args.steps, args.warmup, torch.cuda.ExternalStream(bx.reg.stream()), local, dist)
+        roofx = pass_rooflines(bx, rx["pass_ms"], False, None)
+        cpsx = args.instances * args.steps * world / rx["elapsed"]
+        out = {
+            "circuits_per_s": cpsx,
+            "ms_per_step": 1000 * rx["elapsed"] / args.steps,
+            "dtype": dtype,
+            "register": what,
+            "fused_passes": bx.program.passes,
+            "autotune": _tune_summary(bx.tune),
+            "speedup_vs_plain_c128": cpsx / plain_cps,
+            "speedup_vs_batched_headline": cpsx / cps,
+            "roofline": dict(roofx["hbm"], kernel=f"lsg_pass_0..{bx.program.passes - 1} ({what})",
+                             traffic=(lambda t: sum(t) / len(t) if t else None)(ncu_traffic(prec)),
+                             heaviest_pass=roofx["heaviest_pass"], arith=roofx["arith"]),  # fmt: skip
+            "per_pass": roofx["per_pass"],
+            "accuracy_vs_orrery": golden_errors(rx["probs"], rx["exps"], golden),
+            "accuracy_vs_gpu_headline": {
+                "probability_tvd": 0.5 * float(np.abs(rx["probs"][0] - probs0[0]).sum()),
+                "max_probability_error": float(np.max(np.abs(rx["probs"][0] - probs0[0]))),
+                "max_expectation_error": float(np.max(np.abs(rx["exps"][:, 0] - exps0[:, 0]))),
             },
-            "clocks": r32["clocks"],
+            "clocks": rx["clocks"],
         }
-        b32.free()
+        bx.free()
+        return out
+
+    c64 = beside("c64", "f32", "real32") if not args.no_c64 and real64 else None
+    df64 = beside("df64", "f32 pairs (double-float)", "double-float pairs") if not args.no_c64 and real64 else None
 
     # end to end through the public batched API: host inputs in, host results out, every step
     e2e_steps = max(2, args.steps // 2)
@@ -611,7 +617,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     d2h = int(probs_h.nbytes + exps_h.nbytes)
 
     if rank == 0:
-        tr = ncu_traffic("f64" if real64 else "c64")
+        tr = ncu_traffic({"c128": "f64"}.get(args.precision, args.precision))
         traffic = sum(tr) / len(tr) if tr else None  # mean DRAM bytes per full-size launch (ncu)
         if real64:
             roofline = dict(roof["arith"], kernel=kernel, traffic=traffic, hbm=roof["hbm"],
@@ -619,7 +625,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
         else:
             roofline = dict(roof["hbm"], kernel=kernel, traffic=traffic, arith=roof["arith"],
                             heaviest_pass=roof["heaviest_pass"])  # fmt: skip
-        roofline["traffic_source"] = (f"profiles/tile_pass_dm12_{'f64' if real64 else 'c64'}.md: ncu DRAM read+write "
+        roofline["traffic_source"] = (f"profiles/tile_pass_dm12_{({'c128': 'f64'}).get(args.precision, args.precision)}.md: ncu DRAM read+write "
                                       "of an 8-instance capture x 32, per launch, mean over the passes")
         line = {
             "metric": "circuits/s",
@@ -632,7 +638,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": ("f64" if real64 else "f32") if real else args.precision,
+            "dtype": {"c128": "f64", "c64": "f32", "df64": "f32 pairs (double-float)"}[args.precision],
             "data": "synthetic",
             "config": dict(config_block(args), form=batch.form),
             "hbm_gbs_moved": moved_step * args.steps * world / elapsed / 1e9,
@@ -651,6 +657,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "roofline": roofline,
             "per_pass": roof["per_pass"],
             "c64_batched": c64,
+            "df64_batched": df64,
             "e2e": {
                 "value": args.instances * world / e2e_s,
                 "unit": "circuits/s",

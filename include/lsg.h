@@ -41,6 +41,8 @@ extern "C" {
  * matrix they stand for. */
 #define LSG_R64 2 /* real FP64 coefficients */
 #define LSG_R32 3 /* real FP32 coefficients; reductions stay FP64 */
+#define LSG_RD 4  /* real coefficients as double-float pairs (hi + lo, two FP32 words, 8 bytes): about
+                           48 significant bits from FP32 arithmetic; reductions in FP64 */
 
 /* operator kinds for lsg_apply */
 #define LSG_OP_MATRIX 0 /* dense 2^k x 2^k complex matrix, row-major, on bits[0..k), k <= 5 */

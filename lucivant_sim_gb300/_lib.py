@@ -20,7 +20,8 @@ LIB_PATH = Path(__file__).resolve().parent / "liblsg.so"
 LSG_OK, LSG_E_ARG, LSG_E_CAPACITY, LSG_E_MEMORY, LSG_E_CUDA, LSG_E_TIMEOUT, LSG_E_STATE = 0, -1, -2, -3, -4, -5, -6
 C128, C64 = 0, 1
 R64, R32 = 2, 3  # real registers: density matrices in Pauli-transfer form
-ELEM_BYTES = {C128: 16, C64: 8, R64: 8, R32: 4}
+RD = 4  # real register of double-float pairs (two FP32 words per coefficient)
+ELEM_BYTES = {C128: 16, C64: 8, R64: 8, R32: 4, RD: 8}
 OP_MATRIX, OP_DIAG, OP_PERM, OP_DEPOL, OP_SCALE = 0, 1, 2, 3, 4
 MAX_OP_BITS = 8
 
@@ -268,7 +269,7 @@ class Register:
     @property
     def real(self) -> bool:
         """A Pauli-transfer (real) density register."""
-        return self.precision in (R64, R32)
+        return self.precision in (R64, R32, RD)
 
     def download(self) -> np.ndarray:
         """(batch, 2^nbits) complex128 amplitudes, or float64 coefficients of a real register."""

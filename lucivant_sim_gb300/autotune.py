@@ -6,9 +6,9 @@ per program shape instead. A shape is the register (bits, precision, batch membe
 structure of its operator list (kinds, bits, which operators carry per-member data), not the
 operators' values. For each candidate:
 
-* tile bits (the register bits a CTA holds in shared memory: one below, at and one above the
-  default 32 KB tile),
-* CTAs per SM the specialized passes are compiled for (the default and its neighbours among 1-3),
+* tile bits (the register bits a CTA holds in shared memory: the default 32 KB tile and the next
+  larger one; smaller tiles were slower on every workload measured),
+* CTAs per SM the specialized passes are compiled for (the default and one neighbour),
 
 the program is planned, compiled and run from the basis state on the register itself, timed with
 CUDA events per pass (once for programs of 200 ms or more, else the best of four runs); the fastest candidate is kept in memory for the process and in a JSON
@@ -32,7 +32,7 @@ import numpy as np
 from lucivant_sim_gb300 import _lib
 
 _DEFAULT_TILE = {16: 11, 8: 12, 4: 13}
-_DEFAULT_CTAS = {_lib.C128: 1, _lib.R64: 1, _lib.C64: 2, _lib.R32: 3}
+_DEFAULT_CTAS = {_lib.C128: 1, _lib.R64: 1, _lib.C64: 2, _lib.R32: 3, _lib.RD: 2}
 _lock = threading.Lock()
 _memory: dict[str, dict[str, Any]] = {}
 
@@ -58,8 +58,8 @@ def candidates(nbits: int, precision: int) -> list[_lib.PlanOpts]:
     k0 = min(_DEFAULT_TILE[eb], nbits)
     c0 = _DEFAULT_CTAS[precision]
     eb_log = {16: 4, 8: 3, 4: 2}[eb]
-    tiles = [k for k in (k0, k0 - 1, k0 + 1) if 5 <= k <= nbits and k + eb_log <= 16]
-    ctas = [c0] + [c for c in (1, 2, 3) if abs(c - c0) == 1]
+    tiles = [k for k in (k0, k0 + 1) if 5 <= k <= nbits and k + eb_log <= 16]
+    ctas = [c0, c0 + 1 if c0 == 1 else c0 - 1]
     out = []
     for k in tiles:
         for c in ctas:

@@ -18,7 +18,12 @@ from lucivant_sim_gb300.engine import pauli_masks
 
 
 class DensityBatch:
-    """``len(noises)`` noisy density-matrix instances of one static circuit."""
+    """``len(noises)`` noisy density-matrix instances of one static circuit.
+
+    ``precision``: "c128" (FP64), "c64" (complex64 request: real32 in Pauli-transfer form) or
+    "df64": the Pauli-transfer register in double-float pairs (two FP32 words per coefficient,
+    FP32 arithmetic with exact error terms, about 48 significant bits); it needs the
+    Pauli-transfer form (gates on at most two qubits)."""
 
     def __init__(self, circuit: Any, noises: list[Any], precision: str | None = "c64",
                  autotune: bool | None = None) -> None:  # fmt: skip
@@ -27,10 +32,13 @@ class DensityBatch:
         self.circuit = circuit
         self.n = circuit.num_qubits
         self.batch = len(noises)
-        prec = engine.precision_code(precision)
+        df64 = precision == "df64"
+        prec = _lib.C128 if df64 else engine.precision_code(precision)
         self.form = engine.dm_form(circuit, noises)
+        if df64 and self.form != "ptm":
+            raise ValueError("double-float registers hold the Pauli-transfer form (gates on at most two qubits)")
         if self.form == "ptm":  # Pauli-transfer form: real coefficients, real channel matrices
-            self.reg = engine.new_density(self.n, engine.REAL_OF[prec], self.batch)
+            self.reg = engine.new_density(self.n, _lib.RD if df64 else engine.REAL_OF[prec], self.batch)
             self.ops = engine.ptm_oplist(circuit, noises)
         else:
             self.reg = engine.new_density(self.n, prec, self.batch)

@@ -69,6 +69,11 @@ inline size_t lsg_elem_bytes(int precision) {
     return precision == LSG_C128 ? 16 : precision == LSG_R32 ? 4 : 8;
 }
 
+// Real (Pauli-transfer) register precisions.
+inline bool lsg_precision_real(int precision) {
+    return precision == LSG_R64 || precision == LSG_R32 || precision == LSG_RD;
+}
+
 struct lsg_state_s {
     int nbits = 0;
     int precision = LSG_C128;
@@ -80,7 +85,7 @@ struct lsg_state_s {
     lsg::Scratch scratch;  // reduction partials, CDFs, sampling buffers
     lsg::Scratch scratch2;
     size_t elem_bytes() const { return lsg_elem_bytes(precision); }
-    bool real() const { return precision == LSG_R64 || precision == LSG_R32; }
+    bool real() const { return lsg_precision_real(precision); }
     size_t member_bytes() const { return elem_bytes() * (size_t)elems; }
 };
 #else
@@ -130,6 +135,44 @@ __device__ __forceinline__ double cmul(double a, double b) { return a * b; }
 __device__ __forceinline__ float cfma(float a, float b, float acc) { return fmaf(a, b, acc); }
 __device__ __forceinline__ double cfma(double a, double b, double acc) { return fma(a, b, acc); }
 
+// Double-float elements (LSG_RD registers): a coefficient is the unevaluated sum hi + lo of two
+// FP32 words, |lo| <= ulp(hi) / 2: about 48 significant bits. Products and sums run on the FP32
+// units with their rounding errors carried exactly (the product's error by a fused multiply-add,
+// Dekker 1971; the sum's by Knuth's two-sum, TAOCP vol. 2, 4.2.2), a relative error of about
+// 2^-46 per step, where this GPU's FP64 units run at 1/64 of its FP32 rate. The round-to-nearest
+// intrinsics keep the compiler from contracting the error terms into other operations.
+struct DF {
+    float hi, lo;
+    __host__ __device__ DF() : hi(0.0f), lo(0.0f) {}
+    __host__ __device__ DF(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ explicit DF(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+    __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+
+// s + e as a normalised pair, for |s| >= |e| (fast two-sum)
+__device__ __forceinline__ DF df_norm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return DF(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ DF cmul(DF a, DF b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);  // the product's rounding error, exactly
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_norm(p, e);
+}
+// acc + a*b
+__device__ __forceinline__ DF cfma(DF a, DF b, DF acc) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const float s = __fadd_rn(acc.hi, p);  // two-sum of the high parts: s + t = acc.hi + p exactly
+    const float v = __fsub_rn(s, acc.hi);
+    const float t = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, v)), __fsub_rn(p, v));
+    return df_norm(s, __fadd_rn(t, __fadd_rn(e, acc.lo)));
+}
+
 template <typename T>
 struct Elem {  // complex elements
     using R = decltype(T::re);
@@ -145,6 +188,11 @@ struct Elem<double> {
     using R = double;
     static constexpr bool complex = false;
 };
+template <>
+struct Elem<DF> {  // FP32 arithmetic: the FP32 register budget and occupancy of 8-byte elements
+    using R = float;
+    static constexpr bool complex = false;
+};
 
 // real part (a real element is its own)
 template <typename R>
@@ -153,6 +201,7 @@ __host__ __device__ __forceinline__ R re_of(Cx<R> a) {
 }
 __host__ __device__ __forceinline__ float re_of(float a) { return a; }
 __host__ __device__ __forceinline__ double re_of(double a) { return a; }
+__host__ __device__ __forceinline__ float re_of(DF a) { return a.hi; }
 
 // Insert zero bits at the (ascending) positions in `pos` into x: spreads x over the other bits.
 __device__ __forceinline__ uint64_t spread(uint64_t x, const int* pos, int k) {

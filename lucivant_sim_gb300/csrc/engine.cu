@@ -525,7 +525,7 @@ static int validate_ops(int nbits, int precision, int64_t batch, const lsg_op* o
                         const double* pool, int64_t pool_entries) {
     if (nops < 0 || (nops > 0 && !ops) || pool_entries < 0 || (pool_entries > 0 && !pool))
         return fail(LSG_E_ARG, "bad operator list or pool");
-    const bool real = precision == LSG_R64 || precision == LSG_R32;
+    const bool real = lsg_precision_real(precision);
     if (real) {  // Pauli-transfer registers: real matrices only, channels already in transfer form
         for (int i = 0; i < nops; ++i)
             if (ops[i].kind == LSG_OP_DEPOL)
@@ -674,7 +674,7 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
 // fixed values hold zeros and pass p's operators (acting on tile bits only) keep them zero, so pass
 // p enumerates the free outer bits only and ORs the fixed values into every tile's base.
 static std::vector<PassDesc> basis_passes(const Plan& plan, int nbits, int precision, int64_t index) {
-    const bool real = precision == LSG_R64 || precision == LSG_R32;
+    const bool real = lsg_precision_real(precision);
     uint64_t fixed = nbits >= 64 ? ~0ull : ((1ull << nbits) - 1);
     uint64_t value = real ? 0 : (uint64_t)index;
     if (real) fixed &= ~((1ull << (nbits / 2)) - 1);  // z digits are free
@@ -728,7 +728,7 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
     }
     // real (Pauli-transfer) 4x4 operators whose first row is (1,0,0,0) for every member: trace
     // preserving; the kernel skips that row
-    if (precision == LSG_R64 || precision == LSG_R32)
+    if (lsg_precision_real(precision))
         for (TileOp& t : p->plan.ops) {
             if (t.kind != LSG_OP_MATRIX || t.k != 2 || t.tmpl < kT_DENSE2 || t.tmpl >= kT_DENSE2 + 16) continue;
             bool tp = true;
@@ -876,6 +876,9 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
         } else if (precision == LSG_R64) {
             double* d = reinterpret_cast<double*>(dst);
             for (int64_t i = 0; i < n; ++i) d[i] = src[2 * i];
+        } else if (precision == LSG_RD) {  // each coefficient split into hi + lo
+            DF* d = reinterpret_cast<DF*>(dst);
+            for (int64_t i = 0; i < n; ++i) d[i] = DF(src[2 * i]);
         } else {
             float* f = reinterpret_cast<float*>(dst);
             for (int64_t i = 0; i < n; ++i) f[i] = (float)src[2 * i];
@@ -911,6 +914,7 @@ int program_create_ex(int nbits, int precision, int64_t batch, const lsg_op* ops
 static int jit_ctas(int precision) {
     if (t_choice.ctas) return std::max(1, std::min(4, t_choice.ctas));
     if (const char* env = getenv("LSG_JIT_CTAS")) return std::max(1, std::min(4, atoi(env)));
+    // FP64 elements: one CTA (FP64-bound); double-float and complex64: two; real32: three
     return (precision == LSG_C128 || precision == LSG_R64) ? 1 : lsg_elem_bytes(precision) == 4 ? 3 : 2;
 }
 
@@ -961,6 +965,7 @@ static int program_launch(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, 
         case LSG_C128: return launch_passes<Cx<double>>(p, s, marks, ctx, from_basis);
         case LSG_C64: return launch_passes<Cx<float>>(p, s, marks, ctx, from_basis);
         case LSG_R64: return launch_passes<double>(p, s, marks, ctx, from_basis);
+        case LSG_RD: return launch_passes<DF>(p, s, marks, ctx, from_basis);
         default: return launch_passes<float>(p, s, marks, ctx, from_basis);
     }
 }
@@ -1049,7 +1054,7 @@ __global__ void k_basis_diag_ptm(R* state, int64_t elems, int64_t batch, int n, 
 template <typename R, typename C>
 __global__ void k_real_to_complex(const R* in, Cx<C>* out, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = Cx<C>((C)in[i], C(0));
+        out[i] = Cx<C>((C)(double)in[i], C(0));
 }
 
 __global__ void k_r32_to_r64(const float* in, double* out, int64_t n) {
@@ -1060,6 +1065,16 @@ __global__ void k_r32_to_r64(const float* in, double* out, int64_t n) {
 __global__ void k_r64_to_r32(const double* in, float* out, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (float)in[i];
+}
+
+__global__ void k_r64_to_rd(const double* in, DF* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = DF(in[i]);
+}
+
+__global__ void k_rd_to_r64(const DF* in, double* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
 }
 
 __global__ void k_c128_to_c64(const double2* in, float2* out, int64_t n) {
@@ -1090,6 +1105,8 @@ int set_basis_async(lsg_state_s* s, int64_t index) {
         k_basis_one<float><<<grid_for(s->batch), 256, 0, s->stream>>>((Cx<float>*)s->data, s->elems, s->batch, index);
     else if (s->precision == LSG_R64)
         k_basis_diag_ptm<double><<<grid_for(s->batch << n), 256, 0, s->stream>>>((double*)s->data, s->elems, s->batch, n, index);
+    else if (s->precision == LSG_RD)
+        k_basis_diag_ptm<DF><<<grid_for(s->batch << n), 256, 0, s->stream>>>((DF*)s->data, s->elems, s->batch, n, index);
     else
         k_basis_diag_ptm<float><<<grid_for(s->batch << n), 256, 0, s->stream>>>((float*)s->data, s->elems, s->batch, n, index);
     LSG_CUDA(cudaGetLastError());
@@ -1137,8 +1154,8 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
     *out = nullptr;
     if (nbits < 0) return fail(LSG_E_ARG, "lsg_state_create: negative bit count");
     if (nbits > kMaxBits) return fail(LSG_E_CAPACITY, "a register of %d bits exceeds the engine's %d", nbits, kMaxBits);
-    if (precision < LSG_C128 || precision > LSG_R32) return fail(LSG_E_ARG, "unknown precision %d", precision);
-    if ((precision == LSG_R64 || precision == LSG_R32) && (nbits & 1))
+    if (precision < LSG_C128 || precision > LSG_RD) return fail(LSG_E_ARG, "unknown precision %d", precision);
+    if ((lsg_precision_real(precision)) && (nbits & 1))
         return fail(LSG_E_ARG, "a Pauli-transfer register has an even number of bits (two per qubit)");
     if (batch < 1) return fail(LSG_E_ARG, "lsg_state_create: batch must be at least 1");
     auto* s = new lsg_state_s();
@@ -1198,6 +1215,8 @@ int lsg_state_upload(lsg_state s, const double* host, int64_t nbytes) {
         LSG_CUDA(cudaMemcpyAsync(s->scratch2.ptr, host, (size_t)nbytes, cudaMemcpyHostToDevice, s->stream));
         if (s->precision == LSG_R32)
             k_r64_to_r32<<<grid_for(n), 256, 0, s->stream>>>((const double*)s->scratch2.ptr, (float*)s->data, n);
+        else if (s->precision == LSG_RD)
+            k_r64_to_rd<<<grid_for(n), 256, 0, s->stream>>>((const double*)s->scratch2.ptr, (DF*)s->data, n);
         else
             k_c128_to_c64<<<grid_for(n), 256, 0, s->stream>>>((const double2*)s->scratch2.ptr, (float2*)s->data, n);
         LSG_CUDA(cudaGetLastError());
@@ -1218,6 +1237,8 @@ int lsg_state_download(lsg_state s, double* host, int64_t nbytes) {
         LSG_CHECK(ensure(s->scratch2, (size_t)nbytes));
         if (s->precision == LSG_R32)
             k_r32_to_r64<<<grid_for(n), 256, 0, s->stream>>>((const float*)s->data, (double*)s->scratch2.ptr, n);
+        else if (s->precision == LSG_RD)
+            k_rd_to_r64<<<grid_for(n), 256, 0, s->stream>>>((const DF*)s->data, (double*)s->scratch2.ptr, n);
         else
             k_c64_to_c128<<<grid_for(n), 256, 0, s->stream>>>((const float2*)s->data, (double2*)s->scratch2.ptr, n);
         LSG_CUDA(cudaGetLastError());
@@ -1271,7 +1292,11 @@ int lsg_state_to_complex(lsg_state src, int64_t member, lsg_state dst) {
     LSG_CUDA(cudaStreamSynchronize(src->stream));  // dst's stream reads what src's stream wrote
     const int64_t n = src->elems;
     const unsigned g = grid_for(n);
-    if (src->precision == LSG_R64 && dst->precision == LSG_C128)
+    if (src->precision == LSG_RD && dst->precision == LSG_C128)
+        k_real_to_complex<DF, double><<<g, 256, 0, dst->stream>>>((const DF*)src->data + member * n, (Cx<double>*)dst->data, n);
+    else if (src->precision == LSG_RD)
+        k_real_to_complex<DF, float><<<g, 256, 0, dst->stream>>>((const DF*)src->data + member * n, (Cx<float>*)dst->data, n);
+    else if (src->precision == LSG_R64 && dst->precision == LSG_C128)
         k_real_to_complex<double, double><<<g, 256, 0, dst->stream>>>((const double*)src->data + member * n, (Cx<double>*)dst->data, n);
     else if (src->precision == LSG_R64)
         k_real_to_complex<double, float><<<g, 256, 0, dst->stream>>>((const double*)src->data + member * n, (Cx<float>*)dst->data, n);
@@ -1412,7 +1437,7 @@ int lsg_program_pass_info(lsg_program p, int32_t cap, int64_t* bytes, double* fl
     if (!p) return fail(LSG_E_ARG, "null program");
     const int32_t n = (int32_t)p->plan.passes.size();
     if (cap < n) return fail(LSG_E_ARG, "lsg_program_pass_info: room for %d passes, the program has %d", cap, n);
-    const bool cx = !(p->precision == LSG_R64 || p->precision == LSG_R32);
+    const bool cx = !lsg_precision_real(p->precision);
     for (int32_t i = 0; i < n; ++i) {
         const lsg::PassDesc& pd = p->plan.passes[(size_t)i];
         const lsg::PassDesc& visited = p->basis_passes.size() == (size_t)n ? p->basis_passes[(size_t)i] : pd;

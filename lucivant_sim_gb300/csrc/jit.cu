@@ -104,6 +104,7 @@ const char* type_name(int precision) {
         case LSG_C128: return "lsg::Cx<double>";
         case LSG_C64: return "lsg::Cx<float>";
         case LSG_R64: return "double";
+        case LSG_RD: return "lsg::DF";
         default: return "float";
     }
 }

@@ -325,15 +325,17 @@ __global__ void k_expect_ptm(const R* __restrict__ r, int64_t elems, int n, cons
 static int launch_probs_ptm(lsg_state_s* s, int n, int64_t member0, int64_t members, double* dev_out) {
     const size_t smem = (size_t)8 << n;
     static std::mutex mu;
-    static bool done[2][64] = {};
+    static bool done[3][64] = {};
     int dev = 0;
     LSG_CUDA(cudaGetDevice(&dev));
-    const int which = s->precision == LSG_R64 ? 0 : 1;
+    const int which = s->precision == LSG_R64 ? 0 : s->precision == LSG_RD ? 2 : 1;
     if (smem > 48 * 1024) {
         std::lock_guard<std::mutex> lock(mu);
         if (dev >= 0 && dev < 64 && !done[which][dev]) {
             if (which == 0)
                 LSG_CUDA(cudaFuncSetAttribute(k_probs_ptm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 14));
+            else if (which == 2)
+                LSG_CUDA(cudaFuncSetAttribute(k_probs_ptm<DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 14));
             else
                 LSG_CUDA(cudaFuncSetAttribute(k_probs_ptm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 << 14));
             done[which][dev] = true;
@@ -341,6 +343,8 @@ static int launch_probs_ptm(lsg_state_s* s, int n, int64_t member0, int64_t memb
     }
     if (which == 0)
         k_probs_ptm<double><<<(unsigned)members, 512, smem, s->stream>>>((const double*)s->data, s->elems, n, member0, dev_out);
+    else if (which == 2)
+        k_probs_ptm<DF><<<(unsigned)members, 512, smem, s->stream>>>((const DF*)s->data, s->elems, n, member0, dev_out);
     else
         k_probs_ptm<float><<<(unsigned)members, 512, smem, s->stream>>>((const float*)s->data, s->elems, n, member0, dev_out);
     LSG_CUDA(cudaGetLastError());
@@ -588,6 +592,10 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
         if (s->precision == LSG_R64)
             k_expect_ptm<double><<<reduce_grid(rows), kThreads, 0, s->stream>>>(
                 (const double*)s->data, s->elems, dm_qubits, (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
+                nterms, s->batch, (double*)(base + o_out));
+        else if (s->precision == LSG_RD)
+            k_expect_ptm<DF><<<reduce_grid(rows), kThreads, 0, s->stream>>>(
+                (const DF*)s->data, s->elems, dm_qubits, (const uint64_t*)(base + o_x), (const uint64_t*)(base + o_z),
                 nterms, s->batch, (double*)(base + o_out));
         else
             k_expect_ptm<float><<<reduce_grid(rows), kThreads, 0, s->stream>>>(

@@ -267,6 +267,10 @@ __device__ __forceinline__ void ld16(const double* p, double* o) {
     const double2 w = __ldg(reinterpret_cast<const double2*>(p));
     o[0] = w.x, o[1] = w.y;
 }
+__device__ __forceinline__ void ld16(const DF* p, DF* o) {
+    const float4 w = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = DF(w.x, w.y), o[1] = DF(w.z, w.w);
+}
 __device__ __forceinline__ void ld16(const Cx<float>* p, Cx<float>* o) {
     const float4 w = __ldg(reinterpret_cast<const float4*>(p));
     o[0] = Cx<float>(w.x, w.y), o[1] = Cx<float>(w.z, w.w);

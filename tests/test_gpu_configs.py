@@ -2,8 +2,9 @@
 running Orrery 0.3.0 itself on the same seeded workloads).
 
 * 12-qubit, 12-layer noisy density matrices: the benchmark's 256-instance batch in the real64
-  Pauli-transfer register (instances 0, 1, 128, 255 to a max-abs error of 1e-12 on the 4096
-  probabilities and the 23 <Z> observables), the same batch in real32 (probability TVD <= 1e-6),
+  Pauli-transfer register and in double-float pairs (instances 0, 1, 128, 255 to a max-abs error of
+  1e-12 on the 4096 probabilities and the 23 <Z> observables), the same batch in real32
+  (probability TVD <= 1e-6),
   and Orrery's own noise reading through the public API in both register forms (1e-12).
 * 18 qubits x 16 rounds of mid-circuit measurement: 64 shots in Orrery's draw order give
   Orrery's counts and leave the generator where Orrery leaves it.
@@ -53,7 +54,7 @@ def _members(cfg) -> list[int]:
     return sorted(int(k[len("cfg2_inst"):]) for k in cfg if k.startswith("cfg2_inst"))
 
 
-@pytest.mark.parametrize("precision", ["c128", "c64"])
+@pytest.mark.parametrize("precision", ["c128", "df64", "c64"])
 def test_benchmark_batch_members_match_orrery(cfg, cfg_arrays, precision):
     """The benchmark's step itself: 256 instances in one register, every member evolved by the
     specialized passes, reduced on the device; the fixture members compared with Orrery's."""
@@ -70,7 +71,7 @@ def test_benchmark_batch_members_match_orrery(cfg, cfg_arrays, precision):
     for m in _members(cfg):
         want_p = cfg_arrays[f"cfg2_inst{m}_probs"]
         want_z = np.asarray(cfg[f"cfg2_inst{m}"]["z"])
-        if precision == "c128":
+        if precision in ("c128", "df64"):  # double-float pairs are held to the FP64 tolerance
             assert np.max(np.abs(probs[m] - want_p)) < ATOL_F64, m
             assert np.max(np.abs(exps[:, m] - want_z)) < ATOL_F64, m
         else:
