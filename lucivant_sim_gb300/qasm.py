@@ -722,6 +722,134 @@ class _Reader:
             self.user.add(gname.text)
 
 
+# ---------------------------------------------------------------------------- plain programs
+#
+# Most programs a server or a benchmark sends are plain: declarations, standard gates with number
+# or input arguments on indexed qubits, measurements. Those statements are read here by one regular
+# expression each, without the token stream; anything else (comments, gate definitions,
+# modifiers, expressions, broadcasting, ranges, conditions, resets, barriers, errors) sends the
+# whole program to the general reader. Both produce the same Circuit, operation for operation.
+
+_NUM = r"(?:\d[\d_]*\.?[\d_]*|\.\d[\d_]*)(?:[eE][+-]?\d+)?"
+_FAST_ARG = re.compile(rf"\s*(-?)\s*(?:({_NUM})|([A-Za-z_]\w*))\s*$")
+_FAST_GATE = re.compile(r"([A-Za-z_]\w*)\s*(?:\(([^()]*)\))?\s+(.+)", re.DOTALL)
+_FAST_QARG = re.compile(r"\s*([A-Za-z_]\w*)\s*\[\s*(\d+)\s*\]\s*$")
+_FAST_DECL = re.compile(r"(qubit|bit)\s*\[\s*(\d+)\s*\]\s*([A-Za-z_]\w*)$|(qreg|creg)\s+([A-Za-z_]\w*)\s*\[\s*(\d+)\s*\]$")
+_FAST_MEASURE = re.compile(r"([A-Za-z_]\w*)\s*(?:\[\s*(\d+)\s*\])?\s*=\s*measure\s+([A-Za-z_]\w*)\s*(?:\[\s*(\d+)\s*\])?$")
+_FAST_INPUT = re.compile(r"input\s+(?:float|angle)\s+([A-Za-z_]\w*)$")
+_FAST_HEADER = re.compile(r"OPENQASM\s+[23](?:\.\d+)?$")
+_FAST_INCLUDE = re.compile(r'include\s+"(?:stdgates\.inc|qelib1\.inc)"$')
+_FAST_WORDS = frozenset(("OPENQASM", "include", "qubit", "bit", "qreg", "creg", "input", "measure", "reset",
+                         "barrier", "if", "else", "gate", "gphase", "const", "box", "delay", "ctrl", "negctrl",
+                         "inv", "pow", "float", "angle", "int", "uint", "bool"))  # fmt: skip
+
+
+def _fast_parse(source: str, params: Mapping[str, float]) -> Circuit | None:
+    """The Circuit of a plain program, or None when the general reader must read it."""
+    # comments, blocks, modifiers, physical qubits, pragmas, strings other than two includes
+    if any(c in source for c in "/{}@$#'\\") or source.count('"') > 4:
+        return None
+    stmts = source.split(";")
+    if stmts[-1].strip():
+        return None
+    qregs: dict[str, Register] = {}
+    cregs: dict[str, Register] = {}
+    values: dict[str, float] = {}
+    used: dict[str, float] = {}
+    nq = nc = 0
+    ops: list[Any] = []
+    for k, raw in enumerate(stmts[:-1]):
+        st = raw.strip()
+        if not st:
+            return None  # empty statements: the general reader keeps its own rules
+        if k == 0 and st.startswith("OPENQASM"):
+            if not _FAST_HEADER.match(st):
+                return None
+            continue
+        if st.startswith("include"):
+            if not _FAST_INCLUDE.match(st):
+                return None
+            continue
+        m = _FAST_DECL.match(st)
+        if m:
+            quantum = (m.group(1) or m.group(4)) in ("qubit", "qreg")
+            name = m.group(3) or m.group(5)
+            size = int(m.group(2) or m.group(6))
+            if size < 1 or name in qregs or name in cregs or name in values or name in _FAST_WORDS:
+                return None
+            if quantum:
+                if nq + size > MAX_QUBITS:
+                    return None
+                qregs[name] = Register(name, nq, size)
+                nq += size
+            else:
+                cregs[name] = Register(name, nc, size)
+                nc += size
+            continue
+        m = _FAST_INPUT.match(st)
+        if m:
+            var = m.group(1)
+            if var in values or var in qregs or var in cregs or var not in params:
+                return None
+            values[var] = used[var] = float(params[var])
+            continue
+        if "measure" in st:
+            m = _FAST_MEASURE.match(st)
+            if not m or m.group(1) not in cregs or m.group(3) not in qregs:
+                return None
+            creg, qreg = cregs[m.group(1)], qregs[m.group(3)]
+            if (m.group(2) is None) != (m.group(4) is None):
+                return None
+            if m.group(2) is None:
+                if creg.size != qreg.size:
+                    return None
+                ops += [Measure(qreg.offset + i, creg.offset + i) for i in range(qreg.size)]
+            else:
+                ci, qi = int(m.group(2)), int(m.group(4))
+                if ci >= creg.size or qi >= qreg.size:
+                    return None
+                ops.append(Measure(qreg.offset + qi, creg.offset + ci))
+            continue
+        m = _FAST_GATE.match(st)
+        if not m:
+            return None
+        gname, argtext, qtext = m.group(1), m.group(2), m.group(3)
+        spec = GATES.get(gname)
+        if spec is None or gname in _FAST_WORDS or gname in qregs or gname in cregs:
+            return None
+        vals: list[float] = []
+        if argtext is not None and argtext.strip():
+            for a in argtext.split(","):
+                am = _FAST_ARG.match(a)
+                if not am:
+                    return None
+                if am.group(2) is not None:
+                    v = _number(am.group(2))
+                elif am.group(3) in values:
+                    v = values[am.group(3)]
+                else:
+                    return None  # constants and unknown names: the general reader
+                vals.append(-v if am.group(1) else v)
+        if len(vals) != spec.params:
+            return None
+        qs: list[int] = []
+        for q in qtext.split(","):
+            qm = _FAST_QARG.match(q)
+            if not qm or qm.group(1) not in qregs:
+                return None
+            reg, i = qregs[qm.group(1)], int(qm.group(2))
+            if i >= reg.size:
+                return None
+            qs.append(reg.offset + i)
+        if len(qs) != spec.qubits or len(set(qs)) != len(qs):
+            return None
+        pv = tuple(vals)
+        ops.append(Gate(canonical_name(gname), tuple(qs), gate_matrix(gname, pv), pv))
+    if set(params) - set(used):
+        return None
+    return Circuit(nq, nc, tuple(ops), tuple(qregs.values()), tuple(cregs.values()), dict(used))
+
+
 def parse(source: str, params: Mapping[str, float] | None = None, *, include_dir: str | Path | None = None) -> Circuit:
     """Read OpenQASM 2 or 3 source. ``params`` binds ``input`` values; ``include_dir`` allows
     includes of files inside that folder only."""
@@ -735,6 +863,10 @@ def parse(source: str, params: Mapping[str, float] | None = None, *, include_dir
                 raise QasmError(f"include {fname!r} is outside {root}")
             return path.read_text(encoding="utf-8")
 
+    if include_dir is None:
+        plain = _fast_parse(source, params or {})
+        if plain is not None:
+            return plain
     reader = _Reader(source, params or {}, include)
     ops = reader.program()
     s = reader.scope

@@ -725,3 +725,87 @@ def test_outcome_pair_space_deposits_like_orrery():
     got = {ls.simulator.format_bits(c, k): v for k, v in got.items() if v > 1e-12}
     assert got.keys() == want.keys()
     assert all(abs(got[k] - v) < 1e-14 for k, v in want.items())
+
+
+def _general_parse(src, params=None):
+    """The general reader alone (token stream, every rule), for comparison with the fast path."""
+    from lucivant_sim_gb300 import qasm
+
+    r = qasm._Reader(src, params or {}, None)
+    ops = r.program()
+    s = r.scope
+    extra = set(params or {}) - set(r.used)
+    if extra:
+        raise qasm.QasmError(f"the program has no input named {', '.join(sorted(extra))}")
+    return qasm.Circuit(s.nq, s.nc, tuple(ops), tuple(s.qregs.values()), tuple(s.cregs.values()), dict(r.used))
+
+
+def _same_circuit(a, b) -> None:
+    assert (a.num_qubits, a.num_clbits, a.qregs, a.cregs) == (b.num_qubits, b.num_clbits, b.qregs, b.cregs)
+    assert dict(getattr(a, "params", {}) or {}) == dict(getattr(b, "params", {}) or {})
+
+    def same_ops(xs, ys) -> None:
+        assert len(xs) == len(ys)
+        for x, y in zip(xs, ys, strict=True):
+            assert x.kind == y.kind
+            if x.kind == "gate":
+                assert (x.name, x.qubits, x.params) == (y.name, y.qubits, y.params)
+                assert x.matrix.tobytes() == y.matrix.tobytes()
+            elif x.kind == "if":
+                assert x.condition == y.condition
+                same_ops(x.then, y.then)
+                same_ops(x.otherwise, y.otherwise)
+            else:
+                assert x == y
+
+    same_ops(a.operations, b.operations)
+    assert a.digest() == b.digest()
+
+
+def test_plain_program_fast_path_reads_like_the_general_reader():
+    """Plain programs (declarations, standard gates with number or input arguments on indexed
+    qubits, measurements) are read without the token stream; the Circuit is the general reader's,
+    operation for operation, and everything else still goes through the general reader."""
+    from lucivant_sim_gb300 import qasm
+    from lucivant_sim_gb300.gates import GATES
+
+    rng = np.random.default_rng(8)
+    programs = [(wl.brickwork(9, 7, seed=2), None), (wl.brickwork(5, 3, seed=4, measure=False), None),
+                (wl.hea(6, 2, seed=3), None), (wl.clifford_layers(12, 3, seed=5), None)]  # fmt: skip
+    names = {n: GATES[n].params for n in ("u3", "rx", "ry", "rz", "cx", "cz", "swap", "h", "sx", "U", "CX", "p", "rzz", "crx", "ccx")}
+    for case in range(12):  # random plain programs: qreg/creg and qubit/bit spellings, inputs, measures
+        n = int(rng.integers(3, 9))
+        old = case % 2 == 0
+        lines = ["OPENQASM 2.0;" if old else "OPENQASM 3.0;", 'include "qelib1.inc";' if old else 'include "stdgates.inc";']
+        lines += [f"qreg q[{n}];", f"creg c[{n}];"] if old else [f"qubit[{n}] q;", f"bit[{n}] c;", "input float th;"]
+        for _ in range(25):
+            name = str(rng.choice(list(names)))
+            k = GATES[name].qubits
+            qs = ", ".join(f"q[{int(q)}]" for q in rng.permutation(n)[:k])
+            args = [repr(float(v)) for v in rng.uniform(-4, 4, size=names[name])]
+            if args and not old and rng.random() < 0.3:
+                args[0] = "-th" if rng.random() < 0.5 else "th"
+            lines.append(f"{name}({', '.join(args)}) {qs};" if args else f"{name} {qs};")
+        lines.append(f"c[{int(rng.integers(n))}] = measure q[{int(rng.integers(n))}];" if case % 3 else "c = measure q;")
+        programs.append(("\n".join(lines) + "\n", None if old else {"th": float(rng.uniform(-1, 1))}))
+    programs.append((wl.hea_template(5, 2), {f"p{k}": 0.25 * k - 1 for k in range(20)}))
+    for src, params in programs:
+        assert qasm._fast_parse(src, params or {}) is not None, src[:200]
+        _same_circuit(qasm.parse(src, params), _general_parse(src, params))
+    # not plain: the general reader (same Circuit, by construction)
+    for src in (wl.midcircuit(8, 1, seed=1), "OPENQASM 3; qubit[2] q; h q; // broadcast\n",
+                "OPENQASM 3; qubit[2] q; rx(pi/2) q[0]; cx q[0], q[1];", "OPENQASM 3; qubit[3] q; inv @ s q[1];"):  # fmt: skip
+        assert qasm._fast_parse(src, {}) is None
+        _same_circuit(qasm.parse(src), _general_parse(src))
+    # errors are the general reader's
+    bad = ["OPENQASM 3; qubit[2] q; cx q[0];", "OPENQASM 3; qubit[2] q; cx q[0], q[0];", "OPENQASM 3; qubit[2] q; h q[2];",
+           "OPENQASM 3; qubit[2] q; u3(1, 2) q[0];", "OPENQASM 3; qubit[2] q; foo q[0];",
+           "OPENQASM 3; input float a; qubit[1] q; rx(a) q[0];", "OPENQASM 3; qubit[0] q;"]  # fmt: skip
+    for src in bad:
+        with pytest.raises(qasm.QasmError) as fast_err:
+            qasm.parse(src)
+        with pytest.raises(qasm.QasmError) as general_err:
+            _general_parse(src)
+        assert str(fast_err.value) == str(general_err.value)
+    with pytest.raises(qasm.QasmError, match="no input named"):
+        qasm.parse("OPENQASM 3; qubit[1] q; h q[0];", {"zz": 1.0})
