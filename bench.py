@@ -765,6 +765,8 @@ def serve_arm(args: argparse.Namespace) -> None:
         "latency_at_70pct_of_throughput": {"rate_jobs_per_s": sustainable, "p50_s": steady["p50_s"],
                                            "p99_s": steady["p99_s"]},  # fmt: skip
         "latency_all_at_once": {"p50_s": burst["p50_s"], "p99_s": burst["p99_s"]},
+        "phases_at_offered_rate": offered["phases"],
+        "phases_at_70pct_of_throughput": steady["phases"],
         "plain_c128": {"circuits_per_s": plain_cps, "jobs_timed": len(sample), "speedup_of_served": cps / plain_cps},
         "accuracy": {"max_probability_tvd_vs_c128": tvd, "max_expectation_error_vs_c128": exp_err,
                      "counts_identical_to_c128": f"{same_counts} of {sum(j['kind'] != 'expect' for j in sample)}"},  # fmt: skip

@@ -239,6 +239,7 @@ class Server:
             fut.set_exception(RuntimeError("server closed") if pf.cancelled() else exc)
             return
         prep["t0"] = t0
+        prep["t_prepared"] = time.perf_counter()
         need = job_bytes(prep, self.precision)
         if need > self.budget:
             fut.set_exception(MemoryError(f"the job needs {need} bytes; the server admits at most {self.budget}"))
@@ -286,11 +287,18 @@ class Server:
                     return
             w, reg = picked
             shape = job_shape(w.prep, self.precision)
+            t_start = time.perf_counter()
             try:
                 if reg is None:
                     reg = _lib.Register(*shape)
                 res = execute(w.prep, self.precision, reg)
-                res["latency_s"] = time.perf_counter() - w.prep["t0"]
+                t_end = time.perf_counter()
+                res["latency_s"] = t_end - w.prep["t0"]
+                # where the latency went: host preparation (in the process pool, including its
+                # queue), waiting for a slot and memory, running (device work and host sampling)
+                res["prep_s"] = w.prep["t_prepared"] - w.prep["t0"]
+                res["wait_s"] = t_start - w.prep["t_prepared"]
+                res["run_s"] = t_end - t_start
                 w.future.set_result(res)
             except Exception as exc:  # noqa: BLE001 - handed to the client
                 w.future.set_exception(exc)
@@ -342,10 +350,13 @@ def replay(jobs: list[dict], server: Server, realtime: bool = True) -> dict:
     results = [f.result() for f in futures]
     elapsed = time.perf_counter() - start
     lat = np.array([r["latency_s"] for r in results])
+    parts = {k: np.array([r.get(k, np.nan) for r in results]) for k in ("prep_s", "wait_s", "run_s")}
     return {
         "results": results,
         "elapsed_s": elapsed,
         "circuits_per_s": len(jobs) / elapsed,
         "p50_s": float(np.percentile(lat, 50)),
         "p99_s": float(np.percentile(lat, 99)),
+        "phases": {k: {"p50_s": float(np.nanpercentile(v, 50)), "p99_s": float(np.nanpercentile(v, 99)),
+                       "mean_s": float(np.nanmean(v))} for k, v in parts.items()},  # fmt: skip
     }
