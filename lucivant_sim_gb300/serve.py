@@ -23,6 +23,7 @@ register, so a job's result alone and in the mix is identical (checked by ``test
 
 from __future__ import annotations
 
+import hashlib
 import heapq
 import multiprocessing as mp
 import os
@@ -71,7 +72,45 @@ def prepare(job: dict) -> dict:
                    weights=[float(job["observable"][lab]) for lab in labels])  # fmt: skip
     else:
         raise ValueError(f"unknown job kind {kind!r}")
+    if kind in ("sample", "density"):
+        out["key"] = structure_key(out)
     return out
+
+
+def structure_key(prep: dict) -> str:
+    """Jobs with equal keys can share one register: the same kind, register and operator
+    structure (kinds, bits, data sizes), whatever the operators' values."""
+    table, flat = prep["ops"]
+    h = hashlib.sha1()
+    h.update(f"{prep['kind']}:{prep['nbits']}:{prep.get('real', False)}:{flat.size}:".encode())
+    h.update(table.tobytes())
+    return h.hexdigest()
+
+
+def combined_ops(preps: list[dict]) -> tuple[np.ndarray, np.ndarray]:
+    """One operator table for jobs of one structure key, member b = job b: operators whose data
+    agree across the jobs keep one copy, the others carry one copy per member."""
+    table = preps[0]["ops"][0]
+    pools = np.stack([p["ops"][1].view(np.complex128) for p in preps])  # (members, entries)
+    starts = table["data"].astype(np.int64)
+    order = np.argsort(starts, kind="stable")
+    ends = np.empty_like(starts)
+    ends[order[:-1]] = starts[order[1:]]
+    ends[order[-1]] = pools.shape[1]
+    out = table.copy()
+    chunks, at = [], 0
+    for i in range(len(table)):
+        seg = pools[:, starts[i]:ends[i]]
+        if (seg == seg[0]).all():
+            chunks.append(seg[0])
+            out[i]["data"], out[i]["batch_stride"] = at, 0
+            at += seg.shape[1]
+        else:
+            chunks.append(seg.reshape(-1))
+            out[i]["data"], out[i]["batch_stride"] = at, seg.shape[1]
+            at += seg.size
+    flat = np.concatenate(chunks) if chunks else np.zeros(1, dtype=np.complex128)
+    return out, np.ascontiguousarray(flat.view(np.float64))
 
 
 def sweep_oplist(circuits: list[Any]) -> _lib.OpList:
@@ -177,6 +216,34 @@ def execute(prep: dict, precision: int, reg: _lib.Register | None = None) -> dic
             reg.free()
 
 
+def execute_group(preps: list[dict], precision: int, reg: _lib.Register | None = None) -> list[dict]:
+    """Jobs of one structure key on one register (member b = job b): one program, one launch per
+    pass for all of them, then each member sampled with its own seed and noise. Each member's
+    arithmetic is the same as alone (the same operators, per-member data), so each result is the
+    job's result alone."""
+    if len(preps) == 1:
+        return [execute(preps[0], precision, reg)]
+    first = preps[0]
+    code = job_precision(first, precision)
+    own = reg is None
+    if own:
+        reg = _lib.Register(first["nbits"], code, len(preps))
+    try:
+        table, flat = combined_ops(preps)
+        _lib.check(reg.lib.lsg_apply_from_basis(reg.handle, 0, table.ctypes.data, len(table),
+                                                _lib.ptr(flat, _lib.C.c_double), flat.size // 2))  # fmt: skip
+        out = []
+        for b, prep in enumerate(preps):
+            noise = NoiseModel.uniform(**prep["noise"]) if prep["noise"] else None
+            counts, report = sample_register(reg, prep["circuit"], prep["dm"], prep["shots"], noise,
+                                             np.random.default_rng(prep["seed"]), member=b)  # fmt: skip
+            out.append({"counts": counts, "near_boundary": report["near_boundary"], "batched_with": len(preps)})
+        return out
+    finally:
+        if own:
+            reg.free()
+
+
 def job_precision(prep: dict, precision: int) -> int:
     """The register precision of a job: density matrices in Pauli-transfer form are real."""
     return engine.REAL_OF[precision] if prep.get("real") else precision
@@ -184,6 +251,13 @@ def job_precision(prep: dict, precision: int) -> int:
 
 def job_shape(prep: dict, precision: int) -> tuple[int, int, int]:
     return prep["nbits"], job_precision(prep, precision), prep["batch"]
+
+
+def group_shape(group: list[Any], precision: int) -> tuple[int, int, int]:
+    """The register of a group of waiting jobs of one structure key: one member per job (a
+    sweep's members when alone)."""
+    nbits, code, batch = job_shape(group[0].prep, precision)
+    return nbits, code, batch if len(group) == 1 else len(group)
 
 
 def job_bytes(prep: dict, precision: int) -> int:
@@ -204,13 +278,14 @@ class Server:
     """Continuous-batching server: submit jobs, get futures."""
 
     def __init__(self, precision: str = "c64", workers: int = 8, prep_workers: int | None = None,
-                 memory_fraction: float = 0.6, memory_bytes: int | None = None) -> None:  # fmt: skip
+                 memory_fraction: float = 0.6, memory_bytes: int | None = None, group_max: int = 16) -> None:  # fmt: skip
         _lib.ensure_device()
         self.precision = engine.precision_code(precision)
         free, _total = _lib.mem_info()
         self.budget = int(memory_bytes if memory_bytes is not None else free * memory_fraction)
         self.used = 0
         self.slots = workers
+        self.group_max = max(1, int(group_max))  # jobs of one structure key run together, up to this many
         self.pool = _RegisterPool()
         self.cv = threading.Condition()
         self.waiting: list[_Waiting] = []
@@ -255,22 +330,33 @@ class Server:
     # -- device side ---------------------------------------------------------------------
     # ``used`` counts the full need of every running job plus the idle pooled registers (they stay
     # allocated). A job that reuses an idle register of its shape needs only the rest of its need.
-    def _admit(self) -> tuple[_Waiting, _lib.Register | None] | None:
+    def _admit(self) -> tuple[list[_Waiting], _lib.Register | None] | None:
         """The oldest waiting job that fits the free memory (oldest first; a smaller job may pass a
-        big one that does not fit yet), freeing idle pooled registers when that makes it fit."""
-        for w in sorted(self.waiting):
-            shape = job_shape(w.prep, self.precision)
-            reg = self.pool.take(shape)
-            extra = w.need - (register_bytes(*shape) if reg is not None else 0)
-            if self.used + extra > self.budget and self.pool.bytes:
-                self.used -= self.pool.evict(self.used + extra - self.budget)
-            if self.used + extra <= self.budget:
-                self.waiting.remove(w)
-                heapq.heapify(self.waiting)
-                self.used += extra
-                return w, reg
-            if reg is not None:  # not admitted: the register goes back to the pool
-                self.pool.give(reg)
+        big one that does not fit yet), with the other waiting jobs of its structure key (up to
+        ``group_max`` members, as many as fit), freeing idle pooled registers when that makes
+        them fit."""
+        queue = sorted(self.waiting)
+        for w in queue:
+            group = [w]
+            key = w.prep.get("key")
+            if key is not None:
+                group += [o for o in queue if o is not w and o.prep.get("key") == key][: self.group_max - 1]
+            while group:
+                shape = group_shape(group, self.precision)
+                need = sum(g.need for g in group)
+                reg = self.pool.take(shape)
+                extra = need - (register_bytes(*shape) if reg is not None else 0)
+                if self.used + extra > self.budget and self.pool.bytes:
+                    self.used -= self.pool.evict(self.used + extra - self.budget)
+                if self.used + extra <= self.budget:
+                    for g in group:
+                        self.waiting.remove(g)
+                    heapq.heapify(self.waiting)
+                    self.used += extra
+                    return group, reg
+                if reg is not None:  # not admitted: the register goes back to the pool
+                    self.pool.give(reg)
+                group.pop()  # fewer members, then try again
         return None
 
     def _worker(self) -> None:
@@ -285,30 +371,34 @@ class Server:
                     self.cv.wait(0.05)
                 if picked is None:
                     return
-            w, reg = picked
-            shape = job_shape(w.prep, self.precision)
+            group, reg = picked
+            shape = group_shape(group, self.precision)
+            need = sum(g.need for g in group)
             t_start = time.perf_counter()
             try:
                 if reg is None:
                     reg = _lib.Register(*shape)
-                res = execute(w.prep, self.precision, reg)
+                results = execute_group([g.prep for g in group], self.precision, reg)
                 t_end = time.perf_counter()
-                res["latency_s"] = t_end - w.prep["t0"]
-                # where the latency went: host preparation (in the process pool, including its
-                # queue), waiting for a slot and memory, running (device work and host sampling)
-                res["prep_s"] = w.prep["t_prepared"] - w.prep["t0"]
-                res["wait_s"] = t_start - w.prep["t_prepared"]
-                res["run_s"] = t_end - t_start
-                w.future.set_result(res)
+                for g, res in zip(group, results, strict=True):
+                    res["latency_s"] = t_end - g.prep["t0"]
+                    # where the latency went: host preparation (in the process pool, including its
+                    # queue), waiting for a slot and memory, running (device work, host sampling)
+                    res["prep_s"] = g.prep["t_prepared"] - g.prep["t0"]
+                    res["wait_s"] = t_start - g.prep["t_prepared"]
+                    res["run_s"] = t_end - t_start
+                    g.future.set_result(res)
             except Exception as exc:  # noqa: BLE001 - handed to the client
-                w.future.set_exception(exc)
+                for g in group:
+                    if not g.future.done():
+                        g.future.set_exception(exc)
             finally:
                 with self.cv:
                     if reg is not None:  # the register stays allocated, idle in the pool
                         self.pool.give(reg)
-                        self.used -= w.need - register_bytes(*shape)
+                        self.used -= need - register_bytes(*shape)
                     else:
-                        self.used -= w.need
+                        self.used -= need
                     self.cv.notify_all()
 
     def close(self) -> None:

@@ -58,3 +58,20 @@ def test_jobs_too_large_for_the_budget_are_refused():
         fut = srv.submit(dict(kind="sample", qasm=wl.brickwork(20, 2, seed=1), shots=10, seed=1))
         with pytest.raises(MemoryError, match="admits at most"):
             fut.result(timeout=120)
+
+
+def test_jobs_of_one_structure_run_together_with_the_results_they_get_alone():
+    """Sampled and noisy jobs of one width and depth (other angles, seeds) queued behind one
+    worker are grouped into one register; every grouped job's counts equal its counts alone."""
+    jobs = []
+    for s in range(6):
+        jobs.append(dict(kind="sample", arrival=0.0, qasm=wl.brickwork(9, 6, seed=100 + s), shots=700, seed=s, width=9))
+        jobs.append(dict(kind="density", arrival=0.0, qasm=wl.brickwork(5, 4, seed=200 + s), shots=700, seed=s, width=5))
+    jobs += [dict(j, id=i) for i, j in enumerate(wl.served_mix(6, seed=3, widths=(6, 10), depths=(4, 12), shots=300, sweep=3))]
+    alone = [serve.execute(serve.prepare(dict(j, id=i)), _lib.C64) for i, j in enumerate(jobs)]
+    with serve.Server(precision="c64", workers=1, prep_workers=2, group_max=8) as srv:
+        out = serve.replay(jobs, srv, realtime=False)
+    grouped = [r for r in out["results"] if r.get("batched_with", 1) > 1]
+    assert grouped, "no jobs were grouped"
+    for a, b in zip(alone, out["results"], strict=True):
+        assert _same(a, b)

@@ -809,3 +809,29 @@ def test_plain_program_fast_path_reads_like_the_general_reader():
         assert str(fast_err.value) == str(general_err.value)
     with pytest.raises(qasm.QasmError, match="no input named"):
         qasm.parse("OPENQASM 3; qubit[1] q; h q[0];", {"zz": 1.0})
+
+
+def test_jobs_of_one_structure_combine_into_one_table():
+    """Served jobs with the same operator structure (here brickwork circuits of one width and
+    depth, other angles and seeds) get one structure key, and their combined table gives each
+    member exactly its own job's operators: shared data once, differing data per member."""
+    from lucivant_sim_gb300 import serve
+
+    jobs = [dict(kind="sample", qasm=wl.brickwork(7, 5, seed=s), shots=100, seed=s) for s in (1, 2, 3)]
+    jobs.append(dict(kind="sample", qasm=wl.brickwork(7, 6, seed=4), shots=100, seed=4))
+    preps = [serve.prepare(j) for j in jobs]
+    assert preps[0]["key"] == preps[1]["key"] == preps[2]["key"] != preps[3]["key"]
+    table, flat = serve.combined_ops(preps[:3])
+    pool = flat.view(np.complex128)
+    shared = int((table["batch_stride"] == 0).sum())
+    assert 0 < shared < len(table)  # cx (and any equal gates) once, the u3 of each job per member
+    for b, prep in enumerate(preps[:3]):
+        t0, f0 = prep["ops"]
+        p0 = f0.view(np.complex128)
+        starts = t0["data"]
+        ends = np.append(starts[1:], p0.size)
+        for i in range(len(t0)):
+            size = ends[i] - starts[i]
+            at = table[i]["data"] + b * table[i]["batch_stride"]
+            assert np.array_equal(pool[at:at + size], p0[starts[i]:ends[i]])
+            assert (t0[i]["kind"], t0[i]["nbits"], tuple(t0[i]["bits"])) == (table[i]["kind"], table[i]["nbits"], tuple(table[i]["bits"]))
