@@ -282,3 +282,94 @@ class Circuit:
 
     def format_bits(self, bits: int) -> str:
         return format_bits(self, bits)
+
+
+class ColumnarCircuit:
+    """A static circuit held as arrays: gates, then measurements into classical bits.
+
+    Gate i is distinct gate ``kind[i]`` (a name, a matrix object shared by all its gates, its
+    parameters) on qubits ``qubits[i, :arity[i]]``. Built programmatically (a million-gate Clifford
+    workload), it gives the stabilizer engine its gate columns straight from the arrays, so no
+    per-gate object is made for a run; ``operations`` (and everything derived from it: digests,
+    op counts) materialises the ordinary operation list on first use, the same as a
+    :class:`Circuit` of those operations."""
+
+    def __init__(self, num_qubits: int, num_clbits: int, kind_names: list[str], kind_matrices: list[Any],
+                 kind: np.ndarray, qubits: np.ndarray, arity: np.ndarray, measures: list[tuple[int, int]],
+                 qregs: tuple[Register, ...] = (), cregs: tuple[Register, ...] = (),
+                 kind_params: list[tuple[float, ...]] | None = None) -> None:  # fmt: skip
+        self.num_qubits, self.num_clbits = num_qubits, num_clbits
+        self.kind_names, self.kind_matrices = list(kind_names), list(kind_matrices)
+        self.kind_params = list(kind_params) if kind_params is not None else [()] * len(self.kind_names)
+        self.kind = np.asarray(kind, dtype=np.int64)
+        self.qubits = np.asarray(qubits, dtype=np.int64)
+        self.arity = np.asarray(arity, dtype=np.int64)
+        self.measures = [(int(q), int(c)) for q, c in measures]
+        self.qregs, self.cregs = qregs, cregs
+        self.inputs: dict[str, float] = {}
+
+    def gate(self, i: int) -> Gate:
+        k, a = int(self.kind[i]), int(self.arity[i])
+        return Gate(self.kind_names[k], tuple(int(q) for q in self.qubits[i, :a]), self.kind_matrices[k],
+                    self.kind_params[k])  # fmt: skip
+
+    @cached_property
+    def operations(self) -> tuple[Any, ...]:
+        gates = [self.gate(i) for i in range(len(self.kind))]
+        return tuple(gates) + tuple(Measure(q, c) for q, c in self.measures)
+
+    @cached_property
+    def _plain(self) -> Circuit:
+        return Circuit(self.num_qubits, self.num_clbits, self.operations, self.qregs, self.cregs, {})
+
+    @cached_property
+    def gate_columns(self) -> Any:
+        from lucivant_sim_gb300.clifford import GateColumns
+
+        return GateColumns.from_arrays(_GateSequence(self), self.kind, self.kind_names, self.qubits, self.arity)
+
+    def is_dynamic(self) -> bool:
+        return False  # gates, then measurements only
+
+    def final_measurements(self) -> list[tuple[int, int]]:
+        last: dict[int, int] = {}
+        for q, c in self.measures:
+            last[c] = q
+        return [(q, c) for c, q in last.items()]
+
+    def count_ops(self) -> dict[str, int]:
+        return self._plain.count_ops()
+
+    def canonical(self) -> dict[str, object]:
+        return self._plain.canonical()
+
+    def canonical_text(self) -> str:
+        return self._plain.canonical_text()
+
+    def digest(self) -> str:
+        return self._plain.digest()
+
+    def format_bits(self, bits: int) -> str:
+        return format_bits(self, bits)
+
+
+class _GateSequence:
+    """The gates of a columnar circuit as a read-only sequence, each built on access."""
+
+    def __init__(self, circuit: ColumnarCircuit) -> None:
+        self.circuit = circuit
+
+    def __len__(self) -> int:
+        return len(self.circuit.kind)
+
+    def __getitem__(self, i: Any) -> Any:
+        if isinstance(i, slice):
+            return [self.circuit.gate(j) for j in range(*i.indices(len(self)))]
+        if i < 0:
+            i += len(self)
+        if not 0 <= i < len(self):
+            raise IndexError(i)
+        return self.circuit.gate(i)
+
+    def __iter__(self) -> Any:
+        return (self.circuit.gate(i) for i in range(len(self)))

@@ -165,18 +165,49 @@ def all_gates(ops: Any) -> list[Any]:
 class GateColumns:
     """Per-gate fields of a long gate list as columns, each read once on first use with C-level
     iteration (``map`` over ``attrgetter``): names, qubit tuples, arities, matrix identities
-    (gates that share a matrix object share its analysis) and name indices."""
+    (gates that share a matrix object share its analysis) and name indices. A columnar circuit
+    gives them from its arrays instead (:meth:`from_arrays`): no gate object is read."""
 
-    def __init__(self, gates: list[Any]) -> None:
+    def __init__(self, gates: Any) -> None:
         self.gates = gates
         self.n = len(gates)
 
+    @classmethod
+    def from_arrays(cls, gates: Any, kind: np.ndarray, kind_names: list[str], qubits: np.ndarray,
+                    arity: np.ndarray) -> GateColumns:  # fmt: skip
+        """Columns of gates given as arrays: ``kind[i]`` indexes the distinct gates (one matrix
+        object and one name each), ``qubits[i, :arity[i]]`` are gate i's qubits. ``gates`` is a
+        sequence that builds gate i on access (only the first gate of each kind is read)."""
+        self = cls(gates)
+        kind = np.asarray(kind, dtype=np.int64)
+        present = np.flatnonzero(np.bincount(kind, minlength=len(kind_names)))
+        rank = np.zeros(len(kind_names), dtype=np.int64)
+        rank[present] = np.arange(present.size)
+        first = np.array([int(np.argmax(kind == k)) for k in present], dtype=np.int64)
+        # names numbered in order of first appearance, as the per-gate reading numbers them
+        by_appearance = [kind_names[int(present[j])] for j in np.argsort(first, kind="stable")]
+        name_index = {name: i for i, name in enumerate(dict.fromkeys(by_appearance))}
+        kind_name_id = np.array([name_index.get(name, -1) for name in kind_names], dtype=np.int64)
+        self.__dict__.update(
+            arity=np.asarray(arity, dtype=np.int64),
+            matrix_ids=kind,
+            matrix_groups=(first, rank[kind]),
+            name_ids=kind_name_id[kind],
+        )
+        self._qmat = np.asarray(qubits, dtype=np.int64)
+        self._kind_names = kind_names
+        return self
+
     @cached_property
     def names(self) -> list[str]:
+        if hasattr(self, "_qmat"):
+            return [self._kind_names[k] for k in self.matrix_ids.tolist()]
         return list(map(_NAME, self.gates))
 
     @cached_property
     def qubits(self) -> list[tuple[int, ...]]:
+        if hasattr(self, "_qmat"):
+            return [tuple(row[:a]) for row, a in zip(self._qmat.tolist(), self.arity.tolist(), strict=True)]
         return list(map(_QUBITS, self.gates))
 
     @cached_property
@@ -194,6 +225,20 @@ class GateColumns:
         return first, inv
 
     @cached_property
+    def name_arity_groups(self) -> tuple[np.ndarray, np.ndarray]:
+        """Gates grouped by (name, arity), the key noise rules by gate name depend on: (index of
+        each group's first gate, per gate its group), groups in ascending key order."""
+        key = self.name_ids * 64 + self.arity
+        if hasattr(self, "_qmat"):  # from the distinct gates: key per kind, then per gate
+            first_k, inv_k = self.matrix_groups
+            kind_key = key[first_k]
+            uk, rank = np.unique(kind_key, return_inverse=True)
+            first = np.array([int(first_k[rank == r].min()) for r in range(uk.size)], dtype=np.int64)
+            return first, rank[inv_k]
+        _u, first, inv = np.unique(key, return_index=True, return_inverse=True)
+        return first, inv
+
+    @cached_property
     def name_ids(self) -> np.ndarray:
         name_id = {name: i for i, name in enumerate(dict.fromkeys(self.names))}
         return np.fromiter(map(name_id.__getitem__, self.names), dtype=np.int64, count=self.n)
@@ -206,6 +251,10 @@ class GateColumns:
 
     def position(self, j: int) -> np.ndarray:
         """Qubit j of every gate as int16 (0 where a gate has fewer than j + 1 qubits)."""
+        if hasattr(self, "_qmat"):
+            if j >= self._qmat.shape[1]:
+                return np.zeros(self.n, dtype=np.int16)
+            return np.where(self.arity > j, self._qmat[:, j], 0).astype(np.int16)
         flat, start = self._flat
         has = self.arity > j
         at = np.where(has, start + j, 0)
@@ -253,8 +302,7 @@ def clifford_problem(circuit: Any, noise: Any = None, gates: list[Any] | None = 
     if noise:
         by_arity = all(r.qubits is None for r in getattr(noise, "rules", []))
         if by_arity:
-            _k, kfirst = np.unique(cols.name_ids * 64 + cols.arity, return_index=True)
-            candidates = [int(i) for i in np.sort(kfirst)]
+            candidates = [int(i) for i in np.sort(cols.name_arity_groups[0])]
         else:
             candidates = list(first_index(list(zip(cols.names, cols.qubits))).values())
         for i in candidates:

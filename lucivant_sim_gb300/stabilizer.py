@@ -153,7 +153,7 @@ class Encoder:
         if not with_noise:
             out["noise"] = -1
         elif self.by_arity:  # rules by gate name only: key (name, arity)
-            _k, kfirst, kinv = np.unique(cols.name_ids * 8 + out["nq"], return_index=True, return_inverse=True)
+            kfirst, kinv = cols.name_arity_groups
             idx = np.array([self.noise_code(gates[int(f)]) for f in kfirst], dtype=np.int16)
             out["noise"] = idx[kinv]
         else:  # (name, qubits) keys: each distinct one looked up once
@@ -270,8 +270,15 @@ def _count(bits: np.ndarray) -> dict[int, int]:
     return {int.from_bytes(row.tobytes(), "little"): int(k) for row, k in zip(rows, cnt, strict=True)}
 
 
-def _has_gate_noise(gates: list[Any], noise: Any) -> bool:
-    return noise is not None and any(noise.gate_error(g.name, g.qubits) is not None for g in gates)
+def _has_gate_noise(gates: list[Any], noise: Any, cols: GateColumns | None = None) -> bool:
+    """Whether any gate draws a noise channel. With rules by gate name only, each distinct (name,
+    arity) is asked once, at its first gate."""
+    if noise is None:
+        return False
+    if cols is not None and all(r.qubits is None for r in getattr(noise, "rules", [])):
+        first = cols.name_arity_groups[0]
+        return any(noise.gate_error(gates[int(i)].name, gates[int(i)].qubits) is not None for i in first)
+    return any(noise.gate_error(g.name, g.qubits) is not None for g in gates)
 
 
 def run_counts(circuit: Any, shots: int, noise: Any, rng: np.random.Generator) -> dict[int, int]:
@@ -282,7 +289,7 @@ def run_counts(circuit: Any, shots: int, noise: Any, rng: np.random.Generator) -
         raise SimulationError(f"the stabilizer method runs Clifford circuits only: {problem}")
     n = circuit.num_qubits
     if shots == 0 or circuit.num_clbits == 0:
-        if n > 0 and not circuit.is_dynamic() and not _has_gate_noise(gates, noise):
+        if n > 0 and not circuit.is_dynamic() and not _has_gate_noise(gates, noise, cols):
             enc = Encoder(None)
             t = Tableau(n)
             t.apply(enc.encode(gates, False, cols), enc)
@@ -292,7 +299,7 @@ def run_counts(circuit: Any, shots: int, noise: Any, rng: np.random.Generator) -
         from lucivant_sim_gb300 import stabilizer_shots
 
         return stabilizer_shots.per_shot(circuit, shots, noise, rng)
-    if _has_gate_noise(gates, noise):
+    if _has_gate_noise(gates, noise, cols):
         return frames(circuit, shots, noise, rng, gates, cols)
     return sampled(circuit, shots, noise, rng, gates, cols)
 

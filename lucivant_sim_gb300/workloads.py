@@ -20,7 +20,7 @@ import math
 
 import numpy as np
 
-from lucivant_sim_gb300.circuit import Circuit, Gate, Measure, Register
+from lucivant_sim_gb300.circuit import ColumnarCircuit, Register
 from lucivant_sim_gb300.gates import GATES
 from lucivant_sim_gb300.noise import NoiseModel, ReadoutError, depolarizing, thermal_relaxation
 
@@ -95,18 +95,29 @@ def clifford_layers(n: int, layers: int, seed: int = 11) -> str:
     return "\n".join(lines) + "\n"
 
 
-def clifford_layers_circuit(n: int, layers: int, seed: int = 11) -> Circuit:
-    """The same circuit as :func:`clifford_layers` without writing and parsing its text."""
-    mats = {name: GATES[name].build() for name in (*_CLIFFORD_1Q, "cx", "cz")}
-    ops: list = []
+def clifford_layers_circuit(n: int, layers: int, seed: int = 11) -> ColumnarCircuit:
+    """The same circuit as :func:`clifford_layers` without writing and parsing its text, held as
+    arrays (a columnar circuit: its 4 million gates at 2048 qubits x 1000 layers need no per-gate
+    objects for a stabilizer run)."""
+    names = [*_CLIFFORD_1Q, "cx", "cz"]
+    mats = [GATES[name].build() for name in names]
+    cx, cz = len(_CLIFFORD_1Q), len(_CLIFFORD_1Q) + 1
+    kinds, rows, arity = [], [], []
     for picks, perm in _clifford_plan(n, layers, seed):
-        ops += [Gate(_CLIFFORD_1Q[int(g)], (q,), mats[_CLIFFORD_1Q[int(g)]]) for q, g in enumerate(picks)]
-        for i in range(0, n - 1, 2):
-            a, b = int(perm[i]), int(perm[i + 1])
-            ops.append(Gate("cx", (a, b), mats["cx"]))
-            ops.append(Gate("cz", (a, b), mats["cz"]))
-    ops += [Measure(q, q) for q in range(n)]
-    return Circuit(n, n, tuple(ops), (Register("q", 0, n),), (Register("c", 0, n),))
+        pairs = n // 2
+        a, b = perm[0 : 2 * pairs : 2], perm[1 : 2 * pairs : 2]
+        kinds += [picks.astype(np.int64), np.tile(np.array([cx, cz], dtype=np.int64), pairs)]
+        one = np.full((n, 3), -1, dtype=np.int64)
+        one[:, 0] = np.arange(n)
+        two = np.full((2 * pairs, 3), -1, dtype=np.int64)
+        two[:, 0], two[:, 1] = np.repeat(a, 2), np.repeat(b, 2)
+        rows += [one, two]
+        arity += [np.ones(n, dtype=np.int64), np.full(2 * pairs, 2, dtype=np.int64)]
+    kind = np.concatenate(kinds) if kinds else np.zeros(0, dtype=np.int64)
+    qubits = np.concatenate(rows) if rows else np.zeros((0, 3), dtype=np.int64)
+    ar = np.concatenate(arity) if arity else np.zeros(0, dtype=np.int64)
+    return ColumnarCircuit(n, n, names, mats, kind, qubits, ar, [(q, q) for q in range(n)],
+                           (Register("q", 0, n),), (Register("c", 0, n),))  # fmt: skip
 
 
 def hea(n: int, layers: int, seed: int, measure: bool = False) -> str:

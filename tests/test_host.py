@@ -835,3 +835,33 @@ def test_jobs_of_one_structure_combine_into_one_table():
             at = table[i]["data"] + b * table[i]["batch_stride"]
             assert np.array_equal(pool[at:at + size], p0[starts[i]:ends[i]])
             assert (t0[i]["kind"], t0[i]["nbits"], tuple(t0[i]["bits"])) == (table[i]["kind"], table[i]["nbits"], tuple(table[i]["bits"]))
+
+
+def test_columnar_clifford_circuit_is_the_parsed_circuit():
+    """The wide Clifford workload held as arrays is the circuit its OpenQASM text parses to
+    (digest, operations, final measurements), and its gate columns give the stabilizer encoder
+    and the Clifford check exactly what the parsed circuit's gate objects give."""
+    from lucivant_sim_gb300 import stabilizer as st
+    from lucivant_sim_gb300.clifford import clifford_problem, gates_and_columns
+
+    for n, layers, seed in ((16, 3, 3), (65, 7, 2)):
+        col = wl.clifford_layers_circuit(n, layers, seed=seed)
+        ref = ls.parse(wl.clifford_layers(n, layers, seed=seed))
+        assert col.digest() == ref.digest() and col.count_ops() == ref.count_ops()
+        assert col.final_measurements() == ref.final_measurements() and not col.is_dynamic()
+        g1, c1 = gates_and_columns(col)
+        g2, c2 = gates_and_columns(ref)
+        assert c1.names == c2.names and c1.qubits == c2.qubits and np.array_equal(c1.arity, c2.arity)
+        for j in range(3):
+            assert np.array_equal(c1.position(j), c2.position(j))
+        for a, b in zip(c1.name_arity_groups, c2.name_arity_groups, strict=True):
+            assert np.array_equal(a, b)
+        # the same gates share a matrix (each gate's group named by the group's first gate)
+        assert np.array_equal(c1.matrix_groups[0][c1.matrix_groups[1]], c2.matrix_groups[0][c2.matrix_groups[1]])
+        for noise in (wl.stabilizer_noise(1e-2), None):
+            assert clifford_problem(col, noise, g1, c1) == clifford_problem(ref, noise, g2, c2)
+            assert st._has_gate_noise(g1, noise, c1) == st._has_gate_noise(g2, noise, c2)
+            e1 = st.Encoder(noise).encode(g1, noise is not None, c1)
+            e2 = st.Encoder(noise).encode(g2, noise is not None, c2)
+            assert np.array_equal(e1, e2)
+        assert [g.qubits for g in g1[:5]] == [g.qubits for g in g2[:5]] and len(g1) == len(g2)
