@@ -66,6 +66,7 @@ def parse_args() -> argparse.Namespace:
                     "stabilizer 2048q x 1000 layers x 1000 shots")  # fmt: skip
     ap.add_argument("--jobs", type=int, default=400, help="serve: jobs in the served mix")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: offered arrivals per second")
+    ap.add_argument("--serve-workers", type=int, default=8, help="serve: device worker slots")
     return ap.parse_args()
 
 
@@ -122,7 +123,7 @@ class Clocks:
     QUERY = (
         "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-        "clocks_event_reasons.sw_power_cap"
+        "clocks_event_reasons.sw_power_cap,utilization.gpu"
     )
 
     def __init__(self, gpu: int) -> None:
@@ -142,7 +143,7 @@ class Clocks:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
-        sm, smax, reasons = [], [], set()
+        sm, smax, util, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
@@ -156,11 +157,17 @@ class Clocks:
             for name, val in zip(names, f[5:9], strict=True):
                 if val.lower().startswith("active"):
                     reasons.add(name)
+            if len(f) > 9:
+                try:
+                    util.append(float(f[9]))
+                except ValueError:
+                    pass
         return {
             "sm_mhz": statistics.median(sm) if sm else None,
             "sm_max_mhz": max(smax) if smax else None,
             "reasons": sorted(reasons),
             "samples": len(sm),
+            "gpu_util_median_pct": statistics.median(util) if util else None,
         }
 
 
@@ -709,7 +716,7 @@ def serve_arm(args: argparse.Namespace) -> None:
     warm = wl.served_mix(max(args.warmup, 3) * 8, rate=args.rate, seed=99)
     circuits = sum(_circuits(j) for j in jobs)
     prec = "c64"  # the served path runs complex64 states
-    with serve.Server(precision=prec) as srv:
+    with serve.Server(precision=prec, workers=args.serve_workers) as srv:
         serve.replay(warm, srv, realtime=False)
         clocks = Clocks(local)
         clocks.start()
@@ -758,6 +765,7 @@ def serve_arm(args: argparse.Namespace) -> None:
             "30% 8-point HEA sweeps with 20-term Pauli sums, 20% noisy density matrices, 50% sampled (1000 shots)",
             "precision": prec,
             "offered_rate_jobs_per_s": args.rate,
+            "worker_slots": args.serve_workers,
         },
         "latency_at_offered_rate": {"p50_s": offered["p50_s"], "p99_s": offered["p99_s"],
                                     "circuits_per_s": circuits / offered["elapsed_s"],

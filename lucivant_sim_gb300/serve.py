@@ -200,17 +200,21 @@ def execute(prep: dict, precision: int, reg: _lib.Register | None = None) -> dic
     if own:
         reg = _lib.Register(nbits, precision, batch)
     try:
+        t0 = time.perf_counter()
         table, flat = prep["ops"]  # |0...0> then the operators (tiles not reached yet are skipped)
         _lib.check(reg.lib.lsg_apply_from_basis(reg.handle, 0, table.ctypes.data, len(table),
                                                 _lib.ptr(flat, _lib.C.c_double), flat.size // 2))  # fmt: skip
+        t1 = time.perf_counter()  # planning, upload and the passes (the call waits for them)
         if prep["kind"] == "expect":
             vals = reg.expect(0, prep["xmask"], prep["zmask"])  # (terms, batch)
             w = np.asarray(prep["weights"])
-            return {"values": (w[:, None] * vals).sum(axis=0)}
+            return {"values": (w[:, None] * vals).sum(axis=0), "apply_s": t1 - t0,
+                    "reduce_s": time.perf_counter() - t1}  # fmt: skip
         noise = NoiseModel.uniform(**prep["noise"]) if prep["noise"] else None
         counts, report = sample_register(reg, prep["circuit"], prep["dm"], prep["shots"], noise,
                                          np.random.default_rng(prep["seed"]))  # fmt: skip
-        return {"counts": counts, "near_boundary": report["near_boundary"]}
+        return {"counts": counts, "near_boundary": report["near_boundary"], "apply_s": t1 - t0,
+                "reduce_s": time.perf_counter() - t1}  # fmt: skip
     finally:
         if own:
             reg.free()
@@ -440,7 +444,7 @@ def replay(jobs: list[dict], server: Server, realtime: bool = True) -> dict:
     results = [f.result() for f in futures]
     elapsed = time.perf_counter() - start
     lat = np.array([r["latency_s"] for r in results])
-    parts = {k: np.array([r.get(k, np.nan) for r in results]) for k in ("prep_s", "wait_s", "run_s")}
+    parts = {k: np.array([r.get(k, np.nan) for r in results]) for k in ("prep_s", "wait_s", "run_s", "apply_s", "reduce_s")}
     return {
         "results": results,
         "elapsed_s": elapsed,
