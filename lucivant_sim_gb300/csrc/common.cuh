@@ -173,6 +173,45 @@ __device__ __forceinline__ DF cfma(DF a, DF b, DF acc) {
     return df_norm(s, __fadd_rn(t, __fadd_rn(e, acc.lo)));
 }
 
+// One row of a double-float matrix-vector product: sum over the terms c not marked in `skip`
+// of m[c] * a[c]. The high products are summed with two-sums, their rounding errors, the
+// products' errors and the cross terms collected in one FP32 word, and the pair renormalised
+// once at the end: 4 FP32 instructions for the first term, 12 for each further one, 3 to finish.
+template <int N>
+__device__ __forceinline__ DF df_dot(const DF* m, const DF* a, unsigned skip) {
+    float s = 0.0f, t = 0.0f;
+    bool first = true;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+        if (skip & (1u << c)) continue;
+        const float p = __fmul_rn(m[c].hi, a[c].hi);
+        float e = __fmaf_rn(m[c].hi, a[c].hi, -p);
+        e = __fmaf_rn(m[c].hi, a[c].lo, e);
+        e = __fmaf_rn(m[c].lo, a[c].hi, e);
+        if (first) {
+            s = p;
+            t = e;
+            first = false;
+        } else {
+            const float u = __fadd_rn(s, p);
+            const float v = __fsub_rn(u, s);
+            const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(u, v)), __fsub_rn(p, v));
+            s = u;
+            t = __fadd_rn(t, __fadd_rn(err, e));
+        }
+    }
+    return df_norm(s, t);
+}
+
+template <typename T>
+struct IsDF {
+    static constexpr bool value = false;
+};
+template <>
+struct IsDF<DF> {
+    static constexpr bool value = true;
+};
+
 template <typename T>
 struct Elem {  // complex elements
     using R = decltype(T::re);

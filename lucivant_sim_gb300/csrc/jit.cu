@@ -247,8 +247,10 @@ BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int c
     g.U = b.u, g.n = 1 << b.u, g.groups = 1 << (pd.K - b.u);
     // Two groups per thread when tile bit 0 is not a block bit: the pair (tile bit 0 = 0, 1)
     // moves as one wider shared-memory access and every operator's coefficients, loaded once,
-    // serve both groups (the two calls read the same addresses).
-    g.W = (b.sorted[0] != 0 && g.groups >= 2 && 2 * g.n * elem_bytes / 4 <= state_reg_budget(ctas)) ? 2 : 1;
+    // serve both groups (the two calls read the same addresses). Only when there are at least as
+    // many pairs as compute threads: with fewer, half the threads would wait at the block's
+    // barrier (a 32 KB tile of 8-byte elements holds 256 groups of 16).
+    g.W = (b.sorted[0] != 0 && g.groups >= 2 * kComputeHost && 2 * g.n * elem_bytes / 4 <= state_reg_budget(ctas)) ? 2 : 1;
     if (sw.on && sw.unit == 0) g.W = 1;  // a pair must share a 16-byte unit: the swizzle moves whole units
     g.run = g.W == 2 ? 1 : std::min(std::max((int)b.vec, 1), std::max(1, 16 / elem_bytes));
     if (sw.on) g.run = std::min(g.run, 1 << sw.unit);

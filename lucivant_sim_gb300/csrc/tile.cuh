@@ -342,12 +342,16 @@ __device__ __forceinline__ void rb_tpd2(T* v, const T* m) {
 #pragma unroll
             for (int r = 1; r < 4; ++r) {
                 T acc{};
-                bool first = true;
+                if constexpr (IsDF<T>::value) {  // one renormalisation per row
+                    acc = df_dot<4>(mm + 4 * r - 4, a, (unsigned)(Z >> (4 * (r - 1))) & 15u);
+                } else {
+                    bool first = true;
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    if (Z & (1 << (4 * (r - 1) + c))) continue;
-                    acc = first ? cmul(mm[4 * r - 4 + c], a[c]) : cfma(mm[4 * r - 4 + c], a[c], acc);
-                    first = false;
+                    for (int c = 0; c < 4; ++c) {
+                        if (Z & (1 << (4 * (r - 1) + c))) continue;
+                        acc = first ? cmul(mm[4 * r - 4 + c], a[c]) : cfma(mm[4 * r - 4 + c], a[c], acc);
+                        first = false;
+                    }
                 }
                 v[e | ((r & 2) ? B0 : 0) | ((r & 1) ? B1 : 0)] = acc;
             }
