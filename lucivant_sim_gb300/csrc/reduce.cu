@@ -17,6 +17,7 @@ namespace lsg {
 
 constexpr int kThreads = 256;
 constexpr int64_t kMaxGridY = 65535;  // the largest grid y extent of a launch
+constexpr int64_t kExpectL2Bytes = 48ll << 20;  // a member group that stays resident in the 126 MiB L2
 constexpr int kMaxOutcomePairs = 30;   // outcome space of lsg_outcome_probabilities: 2^30 doubles at most
 
 template <typename R>
@@ -209,37 +210,59 @@ __global__ void k_readout_flip(double* __restrict__ e, int64_t ne, int j, double
     }
 }
 
-// <P> partial sums for every member (grid.y) and term: partials[(member * nterms + t) * gridDim.x + block]
+// Re(i^ny * conj(a[i ^ x]) * a[i]) * (-1)^|i & z|: one Pauli string's summand at index i, in R
+template <typename R>
+__device__ __forceinline__ R pauli_summand(const Cx<R>* __restrict__ s, uint64_t i, uint64_t x, uint64_t z, int ny) {
+    const Cx<R> va = s[i], vb = s[i ^ x];
+    const R wr = vb.re * va.re + vb.im * va.im;  // conj(b) * a
+    const R wi = vb.re * va.im - vb.im * va.re;
+    R term = ny == 0 ? wr : ny == 1 ? -wi : ny == 2 ? -wr : wi;
+    return (__popcll(i & z) & 1) ? -term : term;
+}
+
+// <P> partial sums for every member (grid.y) and term: partials[(member * nterms + t) * gridDim.x + block].
+// Statevectors: P is Hermitian, so the summands at i and i ^ x are equal; each pair is read once,
+// from the half of the indices with x's top bit clear, and counted twice (x = 0 sums every
+// index once). Summands are formed in the register's precision and added four at a time before
+// the FP64 accumulation. Density matrices (dm_n > 0): the summands are the diagonal-block
+// entries rho[i, i ^ x], in FP64.
 template <typename R>
 __global__ void k_expect(const Cx<R>* __restrict__ a, int64_t elems, int dm_n, const uint64_t* __restrict__ xm,
                          const uint64_t* __restrict__ zm, int nterms, double* __restrict__ partials) {
     const int64_t member = blockIdx.y;
     const Cx<R>* s = a + member * elems;
-    const int64_t count = dm_n ? (1ll << dm_n) : elems;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t first = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     for (int t = 0; t < nterms; ++t) {
         const uint64_t x = xm[t], z = zm[t];
         const int ny = __popcll(x & z) & 3;
         double acc = 0.0;
-        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
-            double wr, wi;
-            if (dm_n) {
+        if (dm_n) {
+            const int64_t count = 1ll << dm_n;
+            for (int64_t i = first; i < count; i += stride) {
                 const Cx<R> r = s[((uint64_t)i << dm_n) | ((uint64_t)i ^ x)];
-                wr = r.re;
-                wi = r.im;
-            } else {
-                const Cx<R> va = s[i], vb = s[(uint64_t)i ^ x];
-                wr = (double)vb.re * va.re + (double)vb.im * va.im;  // conj(b) * a
-                wi = (double)vb.re * va.im - (double)vb.im * va.re;
+                const double wr = r.re, wi = r.im;
+                double term = ny == 0 ? wr : ny == 1 ? -wi : ny == 2 ? -wr : wi;
+                if (__popcll((uint64_t)i & z) & 1) term = -term;
+                acc += term;
             }
-            double term;  // Re(i^ny * w)
-            switch (ny) {
-                case 0: term = wr; break;
-                case 1: term = -wi; break;
-                case 2: term = -wr; break;
-                default: term = wi; break;
+        } else {
+            const int h = x ? 63 - __clzll((long long)x) : 64;  // x's top bit (none for x = 0)
+            const uint64_t low = h < 64 ? (1ull << h) - 1 : ~0ull;
+            const int64_t count = x ? elems >> 1 : elems;
+            auto index = [&](int64_t j) -> uint64_t {  // the j-th index with bit h clear
+                return h < 64 ? ((((uint64_t)j & ~low) << 1) | ((uint64_t)j & low)) : (uint64_t)j;
+            };
+            int64_t j = first;
+            for (; j + 3 * stride < count; j += 4 * stride) {
+                R part = pauli_summand(s, index(j), x, z, ny);
+                part += pauli_summand(s, index(j + stride), x, z, ny);
+                part += pauli_summand(s, index(j + 2 * stride), x, z, ny);
+                part += pauli_summand(s, index(j + 3 * stride), x, z, ny);
+                acc += (double)part;
             }
-            if (__popcll((uint64_t)i & z) & 1) term = -term;
-            acc += term;
+            for (; j < count; j += stride) acc += (double)pauli_summand(s, index(j), x, z, ny);
+            if (x) acc *= 2.0;
         }
         double tot = block_sum(acc);
         if (threadIdx.x == 0) partials[(member * nterms + t) * gridDim.x + blockIdx.x] = tot;
@@ -610,7 +633,13 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
         return LSG_OK;
     }
     const int64_t count = dm_qubits ? (1ll << dm_qubits) : s->elems;
-    const unsigned grid = std::max(1u, std::min(reduce_grid(count), (unsigned)std::max<int64_t>(1, 4096 / s->batch)));
+    // Statevector members go through in groups small enough to stay in L2 while every term reads
+    // them (one group per launch); density-matrix diagonals are small and go all at once.
+    const int64_t member_bytes = s->elems * (s->precision == LSG_C128 ? 16 : 8);
+    const int64_t chunk = dm_qubits ? kMaxGridY
+                                    : std::min<int64_t>(kMaxGridY, std::max<int64_t>(1, kExpectL2Bytes / member_bytes));
+    const unsigned grid = std::max(1u, std::min(reduce_grid(count),
+                                                (unsigned)std::max<int64_t>(1, 4096 / std::min(chunk, s->batch))));
     size_t off = 0;
     auto take = [&](size_t bytes) {
         size_t at = off;
@@ -624,9 +653,9 @@ int lsg_expect_pauli(lsg_state s, int dm_qubits, const uint64_t* xmask, const ui
     char* base = (char*)s->scratch.ptr;
     LSG_CUDA(cudaMemcpyAsync(base + o_x, xmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
     LSG_CUDA(cudaMemcpyAsync(base + o_z, zmask, nterms * 8, cudaMemcpyHostToDevice, s->stream));
-    // members go on grid y, at most 65,535 per launch: larger batches run in chunks of members
-    for (int64_t b0 = 0; b0 < s->batch; b0 += kMaxGridY) {
-        const int64_t nb = std::min<int64_t>(kMaxGridY, s->batch - b0);
+    // members go on grid y, at most 65,535 (or one L2-sized group) per launch
+    for (int64_t b0 = 0; b0 < s->batch; b0 += chunk) {
+        const int64_t nb = std::min<int64_t>(chunk, s->batch - b0);
         const dim3 g2(grid, (unsigned)nb);
         double* part = (double*)(base + o_part) + b0 * nterms * (int64_t)grid;
         if (s->precision == LSG_C128)

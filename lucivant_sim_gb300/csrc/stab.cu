@@ -16,6 +16,8 @@
 //  * Ideal sampling (stabilizer.py:597-619): x0 plus combinations of the basis picked by the
 //    same stream's uint8 integers.
 #include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -291,6 +293,250 @@ __global__ void k_elim_xor(uint64_t* __restrict__ m, uint8_t* __restrict__ rhs, 
         for (int v = lane; v < W; v += 32) m[(int64_t)t * W + v] ^= m[(int64_t)p * W + v];
         if (lane == 0 && rhs) rhs[t] ^= rhs[p];
     }
+}
+
+// ---- support() in one launch: a thread-block cluster holds the n stabilizer rows in its CTAs'
+// shared memory (rows split evenly over the CTAs, a contiguous run of rows per warp) and walks
+// the columns with one cluster barrier each. Per column every warp offers its lowest eligible row
+// (atomicMin into its CTA's candidate slot), the cluster's minimum is read from every CTA's slot
+// over distributed shared memory, each warp loads the pivot row from the owning CTA into
+// registers and combines it into its own rows that have the bit. The X phase (pivots with the
+// phase rowsum, stabilizer.py:371-395) is followed by the Z phase on the rows no X pivot took
+// (plain GF(2) elimination with the signs as right-hand side, stabilizer.py:398-422).
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ int cluster_ctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return (int)r;
+}
+__device__ __forceinline__ int cluster_nctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return (int)r;
+}
+// the address of `p` (this CTA's shared memory) in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t dsmem_map(const void* p, int rank) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ uint64_t dsmem_u64(uint32_t a) {
+    uint64_t v;
+    asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ int dsmem_s32(uint32_t a) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ int dsmem_u8(uint32_t a) {
+    unsigned v;
+    asm volatile("ld.shared::cluster.u8 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return (int)v;
+}
+
+constexpr int kSupThreads = 1024;
+constexpr int kSupWarps = kSupThreads / 32;
+constexpr int kSupMaxCluster = 8;
+constexpr int kSupRowsPerCta = 256;
+
+struct SupArgs {
+    uint64_t* sx;  // n rows x W words, row-major: in, the stabilizer rows; out, reduced
+    uint64_t* sz;
+    uint8_t* sr;
+    uint8_t* used;  // out: rows taken as X pivots
+    int* pivots;    // out: the X pivot rows in column order
+    int* zcol;      // out: Z pivots, (column, row) in column order
+    int* zrow;
+    int* counts;    // out: [number of X pivots, number of Z pivots]
+    int n, W;
+};
+
+// shared memory of one CTA holding R rows of W words
+__host__ __device__ inline size_t sup_smem_bytes(int R, int W) { return (size_t)2 * R * (W | 1) * 8 + 16 + (size_t)3 * R; }
+
+template <int WPL>  // words of a row per lane: W <= 32 * WPL
+__global__ void __launch_bounds__(kSupThreads, 1) k_support_cluster(SupArgs A) {
+    extern __shared__ __align__(16) uint64_t sup_sm[];
+    const int C = cluster_nctarank(), rank = cluster_ctarank();
+    const int n = A.n, W = A.W, S = W | 1;  // odd row stride: the lanes' reads of one word of 32 rows spread over the banks
+    const int R = (n + C - 1) / C;
+    const int RW = (R + kSupWarps - 1) / kSupWarps;
+    uint64_t* lx = sup_sm;
+    uint64_t* lz = lx + (size_t)R * S;
+    int* lmin = (int*)(lz + (size_t)R * S);  // three rotating candidate slots
+    uint8_t* lr = (uint8_t*)(lmin + 4);
+    uint8_t* lu = lr + R;   // taken as an X pivot
+    uint8_t* lzu = lu + R;  // taken as a Z pivot
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r0 = rank * R;
+    const int nloc = max(0, min(R, n - r0));
+    for (int i = threadIdx.x; i < R * W; i += blockDim.x) {
+        const int t = i / W, v = i - t * W;
+        const bool in = t < nloc;
+        lx[t * S + v] = in ? A.sx[(int64_t)(r0 + t) * W + v] : 0;
+        lz[t * S + v] = in ? A.sz[(int64_t)(r0 + t) * W + v] : 0;
+    }
+    for (int t = threadIdx.x; t < R; t += blockDim.x) {
+        lr[t] = t < nloc ? A.sr[r0 + t] : 0;
+        lu[t] = 0;
+        lzu[t] = 0;
+    }
+    if (threadIdx.x < 3) lmin[threadIdx.x] = INT_MAX;
+    cluster_barrier();  // every CTA of the cluster running and initialised before the first remote read
+    const int w0 = warp * RW, w1 = min(w0 + RW, nloc);
+    const uint32_t slot_base = lane < C ? dsmem_map(lmin, lane) : 0u;
+    int np = 0, nz = 0, k = 0;
+    for (int phase = 0; phase < 2; ++phase) {
+        uint64_t* M = phase == 0 ? lx : lz;
+        for (int q = 0; q < n; ++q, ++k) {
+            const int qw = q >> 6, slot = k % 3;
+            const uint64_t qb = 1ull << (q & 63);
+            for (int base = w0; base < w1; base += 32) {  // this warp's lowest eligible row
+                const int t = base + lane;
+                const bool hit = t < w1 && (M[t * S + qw] & qb) && !lu[t] && (phase == 0 || !lzu[t]);
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (m) {
+                    if (lane == 0) atomicMin(&lmin[slot], r0 + base + __ffs(m) - 1);
+                    break;
+                }
+            }
+            cluster_barrier();
+            // the slot read two columns ago is free again: every CTA passed this barrier after reading it
+            if (threadIdx.x == 0) lmin[(k + 2) % 3] = INT_MAX;
+            const int p = __reduce_min_sync(0xffffffffu, lane < C ? dsmem_s32(slot_base + 4u * slot) : INT_MAX);
+            if (p == INT_MAX) continue;  // no pivot for this column (the same answer in every CTA)
+            const int owner = p / R, pl = p - owner * R;
+            if (owner == rank && pl >= w0 && pl < w1 && lane == 0) {
+                if (phase == 0) {
+                    lu[pl] = 1;
+                    A.pivots[np] = p;
+                } else {
+                    lzu[pl] = 1;
+                    A.zcol[nz] = q;
+                    A.zrow[nz] = p;
+                }
+            }
+            if (phase == 0) ++np; else ++nz;
+            uint64_t px[WPL], pz[WPL];
+            const uint32_t ax = dsmem_map(lx + (size_t)pl * S, owner), az = dsmem_map(lz + (size_t)pl * S, owner);
+#pragma unroll
+            for (int j = 0; j < WPL; ++j) {
+                const int v = lane + 32 * j;
+                px[j] = (phase == 0 && v < W) ? dsmem_u64(ax + 8u * v) : 0;
+                pz[j] = v < W ? dsmem_u64(az + 8u * v) : 0;
+            }
+            const int psign = dsmem_u8(dsmem_map(lr + pl, owner));
+            for (int base = w0; base < w1; base += 32) {
+                const int t = base + lane;
+                const bool hit = t < w1 && r0 + t != p && (M[t * S + qw] & qb) && (phase == 0 || !lu[t]);
+                unsigned m = __ballot_sync(0xffffffffu, hit);
+                while (m) {
+                    const int tt = base + __ffs(m) - 1;
+                    m &= m - 1;
+                    if (phase == 0) {
+                        int g = 0;
+#pragma unroll
+                        for (int j = 0; j < WPL; ++j) {
+                            const int v = lane + 32 * j;
+                            if (v < W) {
+                                const uint64_t x1 = px[j], z1 = pz[j], x2 = lx[tt * S + v], z2 = lz[tt * S + v];
+                                const uint64_t plus = (x1 & z1 & ~x2 & z2) | (x1 & ~z1 & x2 & z2) | (~x1 & z1 & x2 & ~z2);
+                                const uint64_t minus = (x1 & z1 & x2 & ~z2) | (x1 & ~z1 & ~x2 & z2) | (~x1 & z1 & x2 & z2);
+                                g += __popcll(plus) - __popcll(minus);
+                                lx[tt * S + v] = x2 ^ x1;
+                                lz[tt * S + v] = z2 ^ z1;
+                            }
+                        }
+                        g = __reduce_add_sync(0xffffffffu, g);
+                        if (lane == 0) {
+                            const int total = 2 * lr[tt] + 2 * psign + g;
+                            lr[tt] = (((total % 4) + 4) % 4) == 2 ? 1 : 0;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < WPL; ++j) {
+                            const int v = lane + 32 * j;
+                            if (v < W) lz[tt * S + v] ^= pz[j];
+                        }
+                        if (lane == 0) lr[tt] ^= (uint8_t)psign;
+                    }
+                }
+            }
+            __syncwarp();  // this warp's row and flag updates seen by all its lanes at the next column
+        }
+    }
+    cluster_barrier();  // no CTA leaves while another may still read its rows
+    for (int i = threadIdx.x; i < nloc * W; i += blockDim.x) {
+        const int t = i / W, v = i - t * W;
+        A.sx[(int64_t)(r0 + t) * W + v] = lx[t * S + v];
+        A.sz[(int64_t)(r0 + t) * W + v] = lz[t * S + v];
+    }
+    for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+        A.sr[r0 + t] = lr[t];
+        A.used[r0 + t] = lu[t];
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        A.counts[0] = np;
+        A.counts[1] = nz;
+    }
+}
+
+// cluster size for n rows, or 0 when this device cannot run the one-launch support
+static int support_cluster_size(int n, int W, size_t* smem) {
+    if (getenv("LSG_SUPPORT_STEPS")) return 0;  // diagnostics: the launch-per-column path
+    int C = 1;
+    while (C < kSupMaxCluster && (n + C - 1) / C > kSupRowsPerCta) C *= 2;
+    const int R = (n + C - 1) / C;
+    *smem = sup_smem_bytes(R, W);
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        (size_t)optin < *smem || W > 64)
+        return 0;
+    auto kern = W <= 32 ? k_support_cluster<1> : k_support_cluster<2>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kSupThreads);
+    cfg.dynamicSmemBytes = *smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    return C;
+}
+
+static cudaError_t launch_support_cluster(const SupArgs& A, int C, size_t smem, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kSupThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return A.W <= 32 ? cudaLaunchKernelEx(&cfg, k_support_cluster<1>, A) : cudaLaunchKernelEx(&cfg, k_support_cluster<2>, A);
 }
 
 // Pauli frames: one CTA per 32-shot word.
@@ -631,6 +877,76 @@ int lsg_tab_download(lsg_tab t, uint8_t* x, uint8_t* z, uint8_t* r) {
     return LSG_OK;
 }
 
+// support() with a launch per column and phase (the path for devices that cannot run the
+// one-launch cluster kernel): pivot kernels and rowsum/XOR kernels, the Z constraints compacted
+// on the host
+static int support_steps(int n, int W, uint64_t* sx, uint64_t* sz, uint8_t* sr, char* b, size_t o_used, size_t o_piv, size_t o_pivots, size_t o_np, size_t o_zm,
+                         size_t o_zb, size_t o_zp, size_t o_znp, size_t o_zused, cudaStream_t st,
+                         std::vector<uint8_t>& xfull, std::vector<int>& pivots, std::vector<uint64_t>& hsx) {
+    const size_t rowsb = (size_t)n * W * 8;
+    LSG_CUDA(cudaMemsetAsync(b + o_used, 0, n, st));
+    LSG_CUDA(cudaMemsetAsync(b + o_np, 0, 8, st));
+    const unsigned rg = (unsigned)std::max(1, std::min(152 * 4, (n * 32 + kS - 1) / kS));
+    for (int q = 0; q < n; ++q) {
+        k_elim_pivot<<<1, 1024, 0, st>>>(sx, n, W, q, (uint8_t*)(b + o_used), (int*)(b + o_piv), (int*)(b + o_pivots),
+                                        (int*)(b + o_np), 1);
+        k_sup_rowsum<<<rg, kS, 0, st>>>(sx, sz, sr, n, W, q, (const int*)(b + o_piv));
+    }
+    LSG_CUDA(cudaGetLastError());
+    // Z constraints of the unused rows, in row order (stabilizer.py:359-360, :398-422)
+    std::vector<uint8_t> used(n);
+    int npiv = 0;
+    LSG_CUDA(cudaMemcpyAsync(used.data(), b + o_used, n, cudaMemcpyDeviceToHost, st));
+    LSG_CUDA(cudaMemcpyAsync(&npiv, b + o_np, 4, cudaMemcpyDeviceToHost, st));
+    LSG_CUDA(cudaStreamSynchronize(st));
+    pivots.assign(npiv, 0);
+    if (npiv) LSG_CUDA(cudaMemcpy(pivots.data(), b + o_pivots, (size_t)npiv * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint64_t> hsz((size_t)n * W);
+    std::vector<uint8_t> hsr(n);
+    LSG_CUDA(cudaMemcpy(hsz.data(), sz, rowsb, cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(hsx.data(), sx, rowsb, cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(hsr.data(), sr, n, cudaMemcpyDeviceToHost));
+    std::vector<uint64_t> zm;
+    std::vector<uint8_t> zb;
+    for (int i = 0; i < n; ++i)
+        if (!used[i]) {
+            zm.insert(zm.end(), hsz.begin() + (size_t)i * W, hsz.begin() + (size_t)(i + 1) * W);
+            zb.push_back(hsr[i]);
+        }
+    const int zr = (int)zb.size();
+    if (zr == 0) return LSG_OK;
+    LSG_CUDA(cudaMemcpyAsync(b + o_zm, zm.data(), zm.size() * 8, cudaMemcpyHostToDevice, st));
+    LSG_CUDA(cudaMemcpyAsync(b + o_zb, zb.data(), zr, cudaMemcpyHostToDevice, st));
+    LSG_CUDA(cudaMemsetAsync(b + o_zused, 0, zr, st));
+    LSG_CUDA(cudaMemsetAsync(b + o_znp, 0, 8, st));
+    const unsigned zg = (unsigned)std::max(1, std::min(152 * 4, (zr * 32 + kS - 1) / kS));
+    for (int q = 0; q < n; ++q) {
+        k_elim_pivot<<<1, 1024, 0, st>>>((uint64_t*)(b + o_zm), zr, W, q, (uint8_t*)(b + o_zused), (int*)(b + o_piv),
+                                        (int*)(b + o_zp), (int*)(b + o_znp), 1);
+        k_elim_xor<<<zg, kS, 0, st>>>((uint64_t*)(b + o_zm), (uint8_t*)(b + o_zb), zr, W, q, (const int*)(b + o_piv));
+    }
+    LSG_CUDA(cudaGetLastError());
+    int nz = 0;
+    LSG_CUDA(cudaMemcpyAsync(&nz, b + o_znp, 4, cudaMemcpyDeviceToHost, st));
+    LSG_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> zp(nz);
+    std::vector<uint8_t> fb(zr);
+    std::vector<uint64_t> fm((size_t)zr * W);
+    if (nz) LSG_CUDA(cudaMemcpy(zp.data(), b + o_zp, (size_t)nz * 4, cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(fb.data(), b + o_zb, zr, cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(fm.data(), b + o_zm, (size_t)zr * W * 8, cudaMemcpyDeviceToHost));
+    // pivots are taken for ascending columns and the reduction is full, so the column of a
+    // pivot row is its lowest set bit: no earlier column survives in it
+    for (int j = 0; j < nz; ++j) {
+        const int p = zp[j];
+        int col = -1;
+        for (int v = 0; v < W && col < 0; ++v)
+            if (fm[(size_t)p * W + v]) col = 64 * v + __builtin_ctzll(fm[(size_t)p * W + v]);
+        if (col >= 0 && col < n) xfull[col] = fb[p];
+    }
+    return LSG_OK;
+}
+
 int lsg_tab_support(lsg_tab t, const int32_t* qubits, int32_t m, uint8_t* x0, uint8_t* basis, int32_t* rank) {
     clear_error();
     if (!t || !qubits || !x0 || m < 1 || !rank) return fail(LSG_E_ARG, "bad arguments");
@@ -655,6 +971,8 @@ int lsg_tab_support(lsg_tab t, const int32_t* qubits, int32_t m, uint8_t* x0, ui
     const size_t o_zp = off; off += al((size_t)n * 4);
     const size_t o_znp = off; off += al(8);
     const size_t o_zused = off; off += al(n);
+    const size_t o_zc = off; off += al((size_t)n * 4);
+    const size_t o_zrw = off; off += al((size_t)n * 4);
     LSG_CHECK(ensure(t->work2, off));
     char* b = (char*)t->work2.ptr;
     uint64_t* sx = (uint64_t*)(b + o_sx);
@@ -662,74 +980,52 @@ int lsg_tab_support(lsg_tab t, const int32_t* qubits, int32_t m, uint8_t* x0, ui
     uint8_t* sr = (uint8_t*)(b + o_sr);
     k_tab_rows<<<std::max(1, std::min(152 * 8, (n * W + kS - 1) / kS)), kS, 0, st>>>(t->x, t->z, t->r, n, t->words, W, sx,
                                                                                    sz, sr);
-    LSG_CUDA(cudaMemsetAsync(b + o_used, 0, n, st));
-    LSG_CUDA(cudaMemsetAsync(b + o_np, 0, 8, st));
-    const unsigned rg = (unsigned)std::max(1, std::min(152 * 4, (n * 32 + kS - 1) / kS));
-    for (int q = 0; q < n; ++q) {
-        k_elim_pivot<<<1, 1024, 0, st>>>(sx, n, W, q, (uint8_t*)(b + o_used), (int*)(b + o_piv), (int*)(b + o_pivots),
-                                        (int*)(b + o_np), 1);
-        k_sup_rowsum<<<rg, kS, 0, st>>>(sx, sz, sr, n, W, q, (const int*)(b + o_piv));
-    }
-    LSG_CUDA(cudaGetLastError());
-    // Z constraints of the unused rows, in row order (stabilizer.py:359-360, :398-422)
-    std::vector<uint8_t> used(n);
-    int npiv = 0;
-    LSG_CUDA(cudaMemcpyAsync(used.data(), b + o_used, n, cudaMemcpyDeviceToHost, st));
-    LSG_CUDA(cudaMemcpyAsync(&npiv, b + o_np, 4, cudaMemcpyDeviceToHost, st));
-    LSG_CUDA(cudaStreamSynchronize(st));
-    std::vector<int> pivots(npiv);
-    if (npiv) LSG_CUDA(cudaMemcpy(pivots.data(), b + o_pivots, (size_t)npiv * 4, cudaMemcpyDeviceToHost));
-    std::vector<uint64_t> hsz((size_t)n * W), hsx((size_t)n * W);
-    std::vector<uint8_t> hsr(n);
-    LSG_CUDA(cudaMemcpy(hsz.data(), sz, rowsb, cudaMemcpyDeviceToHost));
-    LSG_CUDA(cudaMemcpy(hsx.data(), sx, rowsb, cudaMemcpyDeviceToHost));
-    LSG_CUDA(cudaMemcpy(hsr.data(), sr, n, cudaMemcpyDeviceToHost));
-    std::vector<uint64_t> zm;
-    std::vector<uint8_t> zb;
-    for (int i = 0; i < n; ++i)
-        if (!used[i]) {
-            zm.insert(zm.end(), hsz.begin() + (size_t)i * W, hsz.begin() + (size_t)(i + 1) * W);
-            zb.push_back(hsr[i]);
-        }
-    const int zr = (int)zb.size();
     std::vector<uint8_t> xfull(n, 0);
-    if (zr > 0) {
-        LSG_CUDA(cudaMemcpyAsync(b + o_zm, zm.data(), zm.size() * 8, cudaMemcpyHostToDevice, st));
-        LSG_CUDA(cudaMemcpyAsync(b + o_zb, zb.data(), zr, cudaMemcpyHostToDevice, st));
-        LSG_CUDA(cudaMemsetAsync(b + o_zused, 0, zr, st));
-        LSG_CUDA(cudaMemsetAsync(b + o_znp, 0, 8, st));
-        const unsigned zg = (unsigned)std::max(1, std::min(152 * 4, (zr * 32 + kS - 1) / kS));
-        std::vector<int> zpiv_q;
-        for (int q = 0; q < n; ++q) {
-            k_elim_pivot<<<1, 1024, 0, st>>>((uint64_t*)(b + o_zm), zr, W, q, (uint8_t*)(b + o_zused), (int*)(b + o_piv),
-                                            (int*)(b + o_zp), (int*)(b + o_znp), 1);
-            k_elim_xor<<<zg, kS, 0, st>>>((uint64_t*)(b + o_zm), (uint8_t*)(b + o_zb), zr, W, q, (const int*)(b + o_piv));
-        }
-        LSG_CUDA(cudaGetLastError());
-        // which column each pivot belongs to: replay the pivot order on the host from the final
-        // matrix is not possible, so recover it from the pivot list (pivots are taken for
-        // ascending columns)
-        int nz = 0;
-        LSG_CUDA(cudaMemcpyAsync(&nz, b + o_znp, 4, cudaMemcpyDeviceToHost, st));
+    std::vector<int> pivots;
+    std::vector<uint64_t> hsx((size_t)n * W);
+    size_t smem = 0;
+    const int C = support_cluster_size(n, W, &smem);
+    if (C > 0) {
+        SupArgs A;
+        A.sx = sx;
+        A.sz = sz;
+        A.sr = sr;
+        A.used = (uint8_t*)(b + o_used);
+        A.pivots = (int*)(b + o_pivots);
+        A.zcol = (int*)(b + o_zc);
+        A.zrow = (int*)(b + o_zrw);
+        A.counts = (int*)(b + o_np);
+        A.n = n;
+        A.W = W;
+        LSG_CUDA(launch_support_cluster(A, C, smem, st));
+        int counts[2] = {0, 0};
+        LSG_CUDA(cudaMemcpyAsync(counts, A.counts, 8, cudaMemcpyDeviceToHost, st));
         LSG_CUDA(cudaStreamSynchronize(st));
-        std::vector<int> zp(nz);
-        std::vector<uint8_t> fb(zr);
-        std::vector<uint64_t> fm((size_t)zr * W);
-        if (nz) LSG_CUDA(cudaMemcpy(zp.data(), b + o_zp, (size_t)nz * 4, cudaMemcpyDeviceToHost));
-        LSG_CUDA(cudaMemcpy(fb.data(), b + o_zb, zr, cudaMemcpyDeviceToHost));
-        LSG_CUDA(cudaMemcpy(fm.data(), b + o_zm, (size_t)zr * W * 8, cudaMemcpyDeviceToHost));
-        // after full reduction each pivot row has exactly one pivot column: its lowest set bit
-        // among pivot columns is the column it was chosen for; columns were visited ascending,
-        // so pivot j belongs to the j-th column that received a pivot: the lowest set bit of the
-        // reduced row (every earlier pivot column was cleared from it)
-        for (int j = 0; j < nz; ++j) {
-            const int p = zp[j];
-            int col = -1;
-            for (int v = 0; v < W && col < 0; ++v)
-                if (fm[(size_t)p * W + v]) col = 64 * v + __builtin_ctzll(fm[(size_t)p * W + v]);
-            if (col >= 0 && col < n) xfull[col] = fb[p];
+        const int npiv = counts[0], nz = counts[1];
+        if (npiv < 0 || npiv > n || nz < 0 || nz > n) return fail(LSG_E_CUDA, "support: bad pivot counts %d, %d", npiv, nz);
+        pivots.resize(npiv);
+        std::vector<int> zc(nz), zrw(nz);
+        std::vector<uint8_t> hsr(n);
+        if (npiv) LSG_CUDA(cudaMemcpyAsync(pivots.data(), A.pivots, (size_t)npiv * 4, cudaMemcpyDeviceToHost, st));
+        if (nz) {
+            LSG_CUDA(cudaMemcpyAsync(zc.data(), A.zcol, (size_t)nz * 4, cudaMemcpyDeviceToHost, st));
+            LSG_CUDA(cudaMemcpyAsync(zrw.data(), A.zrow, (size_t)nz * 4, cudaMemcpyDeviceToHost, st));
         }
+        LSG_CUDA(cudaMemcpyAsync(hsr.data(), sr, n, cudaMemcpyDeviceToHost, st));
+        LSG_CUDA(cudaMemcpyAsync(hsx.data(), sx, rowsb, cudaMemcpyDeviceToHost, st));
+        LSG_CUDA(cudaStreamSynchronize(st));
+        // the solution of the Z constraints: each pivot column takes its reduced row's sign
+        for (int j = 0; j < nz; ++j) {
+            if (zc[j] < 0 || zc[j] >= n || zrw[j] < 0 || zrw[j] >= n) return fail(LSG_E_CUDA, "support: bad Z pivot %d", j);
+            xfull[zc[j]] = hsr[zrw[j]];
+        }
+        for (int j = 0; j < npiv; ++j)
+            if (pivots[j] < 0 || pivots[j] >= n) return fail(LSG_E_CUDA, "support: bad X pivot %d", j);
+    } else {
+        LSG_CHECK(support_steps(n, W, sx, sz, sr, b, o_used, o_piv, o_pivots, o_np, o_zm, o_zb, o_zp, o_znp, o_zused, st, xfull,
+                                pivots, hsx));
     }
+    const int npiv = (int)pivots.size();
     for (int i = 0; i < m; ++i) x0[i] = xfull[qubits[i]];
     // basis: X parts of the pivot rows restricted to `qubits` (stabilizer.py:361-365)
     bool identity = m == n;

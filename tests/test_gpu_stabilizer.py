@@ -59,6 +59,44 @@ def test_tableau_generic_gates_against_oracle(n, layers, seed):
     t.free()
 
 
+def _partial_clifford(n: int, layers: int, seed: int, frac: float):
+    """Random h/s/cx/cz layers on a random fraction of the qubits: the rest stay |0>, so both
+    the X pivots and the Z constraints of support() have work."""
+    rng = np.random.default_rng(seed)
+    active = rng.permutation(n)[: max(1, int(frac * n))]
+    lines = ["OPENQASM 3.0;", 'include "stdgates.inc";', f"qubit[{n}] q;"]
+    for _ in range(layers):
+        for q in active:
+            lines.append(f"{['h', 's', 'x', 'sdg'][rng.integers(4)]} q[{q}];")
+        perm = rng.permutation(active)
+        for i in range(0, len(perm) - 1, 2):
+            lines.append(f"{['cx', 'cz'][rng.integers(2)]} q[{perm[i]}], q[{perm[i + 1]}];")
+    return ls.parse("\n".join(lines))
+
+
+@pytest.mark.parametrize("n,frac", [(1, 1.0), (2, 0.5), (63, 0.7), (64, 1.0), (65, 0.3), (257, 0.6), (1000, 0.5), (2048, 0.8)])
+def test_support_one_launch_equals_launch_per_column(n, frac, monkeypatch):
+    """support() in one cluster launch (rows in distributed shared memory) against the path with a
+    launch per column, on full and partial qubit subsets; against the oracle up to 130 qubits."""
+    c = _partial_clifford(n, 4, seed=n, frac=frac)
+    rng = np.random.default_rng(n + 1)
+    subsets = [list(range(n)), sorted(rng.choice(n, size=max(1, n // 3), replace=False).tolist())]
+    t = _tab(c)
+    try:
+        got = [t.support(qs) for qs in subsets]
+        monkeypatch.setenv("LSG_SUPPORT_STEPS", "1")
+        want = [t.support(qs) for qs in subsets]
+    finally:
+        t.free()
+    for (x0, basis), (wx0, wbasis) in zip(got, want):
+        assert np.array_equal(x0, wx0) and np.array_equal(basis, wbasis)
+    if n <= 130:
+        ref = tableau.reference_tableau(c)
+        for qs, (x0, basis) in zip(subsets, got):
+            rx0, rbasis = ref.copy().support(qs)
+            assert np.array_equal(x0, rx0) and np.array_equal(basis, rbasis)
+
+
 def test_counts_golden(golden):
     g = golden["stab_frames64"]
     noise = NoiseModel()
