@@ -127,6 +127,19 @@ int lsg_program_run_timed(lsg_program p, lsg_state s, float* pass_ms);
  * of a real one), so tiles that differ there stay zero and are skipped. The result equals
  * set_basis + lsg_program_run. With pass_ms non-NULL, as lsg_program_run_timed. */
 int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float* pass_ms);
+/* lsg_program_run_from_basis of `count` (program, register) pairs — circuits of uneven widths and
+ * batches, one precision — as ONE sequence of launches: launch k carries pass k of every program
+ * that has one, each program's tiles taken by its own range of the launch's CTAs (the operator
+ * interpreter; a specialized program runs interpreted here, with the same results). index[i] is
+ * pair i's basis state (NULL: all 0). The launches go on register 0's stream after the earlier
+ * work of every register's stream, and later work on any of the registers goes after them; the
+ * call does not wait (lsg_state_sync on a register waits and reports device errors). A register
+ * may appear once. With step_ms non-NULL the call waits and step_ms gets each launch's device
+ * time (as many entries as the longest program has passes). Each register's result equals its
+ * lsg_program_run_from_basis alone. No counterpart in the reference, which runs one circuit per
+ * call (simulator.py:229-251). */
+int lsg_programs_run_ragged(int32_t count, const lsg_program* programs, const lsg_state* states, const int64_t* index,
+                            float* step_ms);
 /* HBM bytes (2 x tile bytes per tile visited) and tiles of one lsg_program_run_from_basis. */
 int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run);
 /* Number of fused passes, and algorithmic HBM bytes of one run (2 x register bytes per pass). */

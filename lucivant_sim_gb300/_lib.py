@@ -77,6 +77,7 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_apply_from_basis": (C.c_int, [_P, _I64, _P, _I32, _PD, _I64]),
     "lsg_program_run_from_basis": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_float)]),
     "lsg_program_basis_info": (C.c_int, [_P, _PI64, _PI64]),
+    "lsg_programs_run_ragged": (C.c_int, [_I32, C.POINTER(_P), C.POINTER(_P), _PI64, C.POINTER(C.c_float)]),
     "lsg_program_free": (C.c_int, [_P]),
     "lsg_program_create_opts": (C.c_int, [_P, _P, _I32, _PD, _I64, _P, C.POINTER(_P)]),
     "lsg_program_pass_info": (C.c_int, [_P, _I32, _PI64, _PD, _PI32]),
@@ -390,6 +391,30 @@ class PlanOpts:
 
     def __repr__(self) -> str:
         return f"PlanOpts({', '.join(f'{k}={v}' for k, v in self.as_dict().items())})"
+
+
+def run_ragged(pairs: list[tuple[Program, Register]], index: list[int] | None = None,
+               timed: bool = False, sync: bool = True) -> np.ndarray | None:
+    """Run every (program, register) pair from a basis state (``Program.run_from_basis``) as one
+    sequence of launches: launch k carries pass k of every program that has one, whatever the
+    registers' widths and batches (one precision). ``timed``: wait and return each launch's device
+    time in ms. ``sync``: wait for the registers and report device errors."""
+    if not pairs:
+        return None
+    lib = library()
+    n = len(pairs)
+    progs = (C.c_void_p * n)(*[p.handle for p, _ in pairs])
+    regs = (C.c_void_p * n)(*[r.handle for _, r in pairs])
+    idx = np.zeros(n, dtype=np.int64) if index is None else np.ascontiguousarray(index, dtype=np.int64)
+    if idx.shape != (n,):
+        raise ValueError("one basis index per pair")
+    steps = max(p.passes for p, _ in pairs)
+    out = np.zeros(max(steps, 1), dtype=np.float32) if timed else None
+    check(lib.lsg_programs_run_ragged(n, progs, regs, ptr(idx, C.c_int64), ptr(out, C.c_float) if timed else None))
+    if sync:
+        for _, r in pairs:
+            r.sync()
+    return out[:steps] if timed else None
 
 
 class Program:

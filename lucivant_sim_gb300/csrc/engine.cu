@@ -976,8 +976,9 @@ int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const 
 
 int set_basis_async(lsg_state_s* s, int64_t index);
 
-// Set every member to basis state `index`, then run the passes on the tiles that can be nonzero.
-static int program_run_basis(lsg_program_s* p, lsg_state_s* s, int64_t index, cudaEvent_t* marks) {
+// Set every member to basis state `index` and make the program's basis passes those of `index`
+// (on the register's stream).
+static int basis_prepare(lsg_program_s* p, lsg_state_s* s, int64_t index) {
     if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
         return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
                     p->nbits, p->precision, (long long)p->batch);
@@ -991,7 +992,109 @@ static int program_run_basis(lsg_program_s* p, lsg_state_s* s, int64_t index, cu
                                  cudaMemcpyHostToDevice, s->stream));
         p->basis_index = index;
     }
+    return LSG_OK;
+}
+
+// Set every member to basis state `index`, then run the passes on the tiles that can be nonzero.
+static int program_run_basis(lsg_program_s* p, lsg_state_s* s, int64_t index, cudaEvent_t* marks) {
+    LSG_CHECK(basis_prepare(p, s, index));
     return program_launch(p, s, marks, TrajCtx{}, true);
+}
+
+// Whether the pipelined interpreter takes this program's passes (bulk copies of its chunks, two
+// tiles and the operators in shared memory).
+template <typename T>
+static bool pipe_eligible(const lsg_program_s* p) {
+    const size_t tile_bytes = sizeof(T) << p->K;
+    const int L = p->plan.passes.empty() ? 0 : p->plan.passes[0].L;
+    return ((sizeof(T) << L) % 16) == 0 && getenv("LSG_NO_PIPELINE") == nullptr &&
+           2 * tile_bytes + (p->smem - tile_bytes) <= 200 * 1024;
+}
+
+// Ragged run: launch k carries pass k (from a basis state) of every job that has one. Each job
+// gets a range of the launch's CTAs in proportion to its tiles (at least one); the launch's
+// shared memory is the largest any of its jobs needs. `ms`, when given, receives each launch's
+// device time (events on `st`).
+template <typename T>
+static int launch_ragged(const std::vector<std::pair<lsg_program_s*, lsg_state_s*>>& jobs, cudaStream_t st,
+                         float* ms) {
+    size_t steps = 0;
+    for (const auto& j : jobs) steps = std::max(steps, j.first->plan.passes.size());
+    if (steps == 0) return LSG_OK;
+    int dev = 0, sms = 0;
+    LSG_CUDA(cudaGetDevice(&dev));
+    LSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int* status = device_status();
+    if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
+    auto kern = k_tile_pipe_ragged<T>;
+    LSG_CHECK(allow_smem(kern));
+    std::vector<RaggedJob> table;
+    std::vector<size_t> first(steps), count(steps), smem(steps);
+    std::vector<unsigned> grid(steps);
+    for (size_t k = 0; k < steps; ++k) {
+        first[k] = table.size();
+        int64_t sum = 0;
+        size_t need = 0;
+        for (const auto& j : jobs) {
+            const lsg_program_s* p = j.first;
+            if (p->plan.passes.size() <= k) continue;
+            const PassDesc& pd = p->basis_passes[k];
+            const size_t tile_bytes = sizeof(T) << p->K;
+            need = std::max(need, 2 * tile_bytes + (size_t)pd.nops * (sizeof(TileOp) + 16) +
+                                      (size_t)pd.nblocks * sizeof(BlockDesc));
+            sum += (1ll << pd.nouter) * p->batch;
+        }
+        int per_sm = 0;
+        LSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPipeThreads, need));
+        const double budget = (double)sms * std::max(per_sm, 1);
+        int cta = 0;
+        for (const auto& j : jobs) {
+            lsg_program_s* p = j.first;
+            lsg_state_s* s = j.second;
+            if (p->plan.passes.size() <= k) continue;
+            const PassDesc& pd = p->basis_passes[k];
+            RaggedJob r;
+            r.state = s->data;
+            r.member_elems = s->elems;
+            const PassDesc* plan_pd_dev = reinterpret_cast<const PassDesc*>(p->dev.ptr);
+            r.ops = reinterpret_cast<const TileOp*>(plan_pd_dev + p->plan.passes.size());
+            r.blocks = reinterpret_cast<const BlockDesc*>(r.ops + p->plan.ops.size());
+            r.pass = reinterpret_cast<const PassDesc*>(static_cast<unsigned char*>(p->dev.ptr) + p->basis_off) + k;
+            r.data = static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned;
+            r.tiles_per_member = 1ll << pd.nouter;
+            r.total_tiles = r.tiles_per_member * p->batch;
+            const int64_t want = (int64_t)std::llround(budget * (double)r.total_tiles / (double)sum);
+            r.ctas = (int)std::max<int64_t>(1, std::min<int64_t>(want, r.total_tiles));
+            r.cta0 = cta;
+            cta += r.ctas;
+            table.push_back(r);
+        }
+        count[k] = table.size() - first[k];
+        smem[k] = need;
+        grid[k] = (unsigned)cta;
+    }
+    RaggedJob* dtab = nullptr;
+    LSG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dtab), table.size() * sizeof(RaggedJob), st));
+    // pageable source: staged before the call returns
+    LSG_CUDA(cudaMemcpyAsync(dtab, table.data(), table.size() * sizeof(RaggedJob), cudaMemcpyHostToDevice, st));
+    std::vector<cudaEvent_t> marks;
+    if (ms) {
+        marks.resize(steps + 1);
+        for (auto& e : marks) LSG_CUDA(cudaEventCreate(&e));
+    }
+    for (size_t k = 0; k < steps; ++k) {
+        if (ms) LSG_CUDA(cudaEventRecord(marks[k], st));
+        kern<<<grid[k], kPipeThreads, smem[k], st>>>(dtab + first[k], (int)count[k], status);
+    }
+    if (ms) LSG_CUDA(cudaEventRecord(marks[steps], st));
+    LSG_CUDA(cudaGetLastError());
+    LSG_CUDA(cudaFreeAsync(dtab, st));
+    if (ms) {
+        LSG_CUDA(cudaEventSynchronize(marks[steps]));
+        for (size_t k = 0; k < steps; ++k) LSG_CUDA(cudaEventElapsedTime(&ms[k], marks[k], marks[k + 1]));
+        for (auto& e : marks) cudaEventDestroy(e);
+    }
+    return LSG_OK;
 }
 
 static int program_run(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks) {
@@ -1389,6 +1492,80 @@ int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float*
     LSG_CUDA(cudaEventSynchronize(p->events[need - 1]));
     for (size_t i = 0; i + 1 < need; ++i) LSG_CUDA(cudaEventElapsedTime(&pass_ms[i], p->events[i], p->events[i + 1]));
     return check_device_status(s->stream);
+}
+
+int lsg_programs_run_ragged(int32_t count, const lsg_program* programs, const lsg_state* states, const int64_t* index,
+                           float* step_ms) {
+    clear_error();
+    if (count < 1 || !programs || !states) return fail(LSG_E_ARG, "lsg_programs_run_ragged: bad arguments");
+    const int precision = states[0] ? states[0]->precision : -1;
+    for (int32_t i = 0; i < count; ++i) {
+        if (!programs[i] || !states[i]) return fail(LSG_E_ARG, "lsg_programs_run_ragged: null program or register %d", i);
+        if (states[i]->precision != precision)
+            return fail(LSG_E_ARG, "lsg_programs_run_ragged: register %d has another precision than register 0", i);
+        for (int32_t j = 0; j < i; ++j)
+            if (states[j] == states[i]) return fail(LSG_E_ARG, "lsg_programs_run_ragged: register %d appears twice", i);
+    }
+    cudaStream_t st = states[0]->stream;
+    std::vector<std::pair<lsg_program_s*, lsg_state_s*>> ragged;
+    std::vector<cudaEvent_t> events;
+    auto cleanup = [&]() {
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+    };
+    int rc = LSG_OK;
+    for (int32_t i = 0; i < count && rc == LSG_OK; ++i) {
+        lsg_program_s* p = programs[i];
+        lsg_state_s* s = states[i];
+        rc = basis_prepare(p, s, index ? index[i] : 0);
+        if (rc != LSG_OK) break;
+        bool eligible;
+        switch (precision) {
+            case LSG_C128: eligible = pipe_eligible<Cx<double>>(p); break;
+            case LSG_C64: eligible = pipe_eligible<Cx<float>>(p); break;
+            case LSG_R64: eligible = pipe_eligible<double>(p); break;
+            case LSG_RD: eligible = pipe_eligible<DF>(p); break;
+            default: eligible = pipe_eligible<float>(p); break;
+        }
+        if (!eligible) {  // this one runs alone on its own stream
+            rc = program_launch(p, s, nullptr, TrajCtx{}, true);
+            continue;
+        }
+        if (p->plan.passes.empty()) continue;
+        ragged.emplace_back(p, s);
+        if (s->stream != st) {  // the ragged launches go after this register's basis state
+            cudaEvent_t e;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                rc = fail(LSG_E_CUDA, "lsg_programs_run_ragged: cannot create an event");
+                break;
+            }
+            events.push_back(e);
+            if (cudaEventRecord(e, s->stream) != cudaSuccess || cudaStreamWaitEvent(st, e, 0) != cudaSuccess)
+                rc = fail(LSG_E_CUDA, "lsg_programs_run_ragged: cannot order the streams");
+        }
+    }
+    if (rc == LSG_OK && !ragged.empty()) {
+        switch (precision) {
+            case LSG_C128: rc = launch_ragged<Cx<double>>(ragged, st, step_ms); break;
+            case LSG_C64: rc = launch_ragged<Cx<float>>(ragged, st, step_ms); break;
+            case LSG_R64: rc = launch_ragged<double>(ragged, st, step_ms); break;
+            case LSG_RD: rc = launch_ragged<DF>(ragged, st, step_ms); break;
+            default: rc = launch_ragged<float>(ragged, st, step_ms); break;
+        }
+    }
+    if (rc == LSG_OK) {  // later work on every register goes after the ragged launches
+        cudaEvent_t done;
+        if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+            rc = fail(LSG_E_CUDA, "lsg_programs_run_ragged: cannot create an event");
+        } else {
+            events.push_back(done);
+            if (cudaEventRecord(done, st) != cudaSuccess) rc = fail(LSG_E_CUDA, "lsg_programs_run_ragged: event record");
+            for (const auto& j : ragged)
+                if (rc == LSG_OK && j.second->stream != st && cudaStreamWaitEvent(j.second->stream, done, 0) != cudaSuccess)
+                    rc = fail(LSG_E_CUDA, "lsg_programs_run_ragged: cannot order the streams");
+        }
+    }
+    cleanup();  // events already recorded are released when they complete
+    return rc;
 }
 
 int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run) {

@@ -954,11 +954,15 @@ constexpr int pipe_ctas() {
 template <typename T, bool Swz = false, typename F>
 __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_elems, const PassDesc& pd, T* buf0,
                                          T* buf1, uint64_t* full, uint64_t* empty, int64_t tiles_per_member,
-                                         int64_t total_tiles, int* status, F&& compute, const Tmap* tmap = nullptr) {
+                                         int64_t total_tiles, int* status, F&& compute, const Tmap* tmap = nullptr,
+                                         int64_t first = -1, int64_t stride = 0) {
     const int K = pd.K, L = pd.L;
     const int nchunks = 1 << (K - L);
     const uint32_t chunk_bytes = (uint32_t)(sizeof(T) << L);
-    const int64_t stride = gridDim.x;
+    if (first < 0) {  // this CTA's tiles: blockIdx.x, then every gridDim.x-th (or a CTA range's own share)
+        first = blockIdx.x;
+        stride = gridDim.x;
+    }
     // the pass's tensor map has this box shape (host jit_launch)
     const bool pair = chunk_bytes == 512u;
     const uint32_t box_bytes = pair ? 1024u : (chunk_bytes < 16384u ? chunk_bytes : 16384u);
@@ -1009,7 +1013,7 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
             __syncwarp();
         };
         int64_t it = 0;
-        for (int64_t t = blockIdx.x; t < total_tiles; t += stride, ++it) {
+        for (int64_t t = first; t < total_tiles; t += stride, ++it) {
             const int b = (int)(it & 1);
             T* buf = b ? buf1 : buf0;
             if (it >= 2) {  // buffer b still holds tile it-2: wait for its compute, store it
@@ -1042,14 +1046,14 @@ __device__ __forceinline__ void pipe_run(T* __restrict__ state, int64_t member_e
                 bulk_wait_all();
                 return;
             }
-            store(blockIdx.x + j * stride, b ? buf1 : buf0);
+            store(first + j * stride, b ? buf1 : buf0);
         }
         bulk_wait_all();
         return;
     }
     // ---------------- compute warps
     int64_t it = 0;
-    for (int64_t t = blockIdx.x; t < total_tiles; t += stride, ++it) {
+    for (int64_t t = first; t < total_tiles; t += stride, ++it) {
         const int b = (int)(it & 1);
         T* tile = b ? buf1 : buf0;
         const bool ok = mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), status);
@@ -1094,6 +1098,59 @@ __global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe(T* _
     __syncthreads();
     pipe_run<T>(state, member_elems, pd, buf0, buf1, full, empty, tiles_per_member, total_tiles, status,
                 [&](T* tile, int64_t member) { compute_tile<T>(tile, pd.K, pd, sblk, sops, recs, data, member, ctx); });
+}
+
+// One program's pass in a launch over several registers (circuits of uneven widths): the
+// program's device arrays, its register, and the range of the launch's CTAs that work on it.
+struct RaggedJob {
+    void* state;
+    int64_t member_elems;
+    const PassDesc* pass;
+    const TileOp* ops;
+    const BlockDesc* blocks;
+    const void* data;
+    int64_t tiles_per_member, total_tiles;
+    int cta0, ctas;  // CTAs cta0 .. cta0 + ctas - 1 of the launch take this job's tiles
+};
+
+// Pass k of every program of a ragged run in one launch: each CTA finds its job (jobs in CTA
+// order), stages that pass's operators and runs the pipelined loop over its share of the job's
+// tiles, exactly as k_tile_pipe does for one register.
+template <typename T>
+__global__ void __launch_bounds__(kPipeThreads, pipe_ctas<T>()) k_tile_pipe_ragged(const RaggedJob* __restrict__ jobs,
+                                                                      int njobs, int* status) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t full[2], empty[2];
+    __shared__ PassDesc pd;
+    __shared__ int job_s;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = njobs - 1;  // the last job whose first CTA is at or below this one
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].cta0 <= (int)blockIdx.x) lo = mid;
+            else hi = mid - 1;
+        }
+        job_s = lo;
+    }
+    __syncthreads();
+    const RaggedJob& J = jobs[job_s];
+    const PassDesc* pass_g = J.pass;
+    const size_t tile_bytes = sizeof(T) << pass_g->K;
+    T* buf0 = reinterpret_cast<T*>(smem_raw);
+    T* buf1 = reinterpret_cast<T*>(smem_raw + tile_bytes);
+    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + 2 * tile_bytes);
+    BlockDesc* sblk = reinterpret_cast<BlockDesc*>(sops + pass_g->nops);
+    OpRec* recs = reinterpret_cast<OpRec*>(sblk + pass_g->nblocks);
+    if (threadIdx.x == 0) pd = *pass_g;
+    stage_pass<T>(pass_g, J.ops, J.blocks, sops, sblk);
+    pipe_init(full, empty);
+    __syncthreads();
+    const T* data = static_cast<const T*>(J.data);
+    const TrajCtx ctx{};
+    pipe_run<T>(static_cast<T*>(J.state), J.member_elems, pd, buf0, buf1, full, empty, J.tiles_per_member,
+                J.total_tiles, status,
+                [&](T* tile, int64_t member) { compute_tile<T>(tile, pd.K, pd, sblk, sops, recs, data, member, ctx); },
+                nullptr, (int64_t)blockIdx.x - J.cta0, (int64_t)J.ctas);
 }
 
 // A pass specialized by the host: `Body::run(tile, data, member)` is generated straight-line code
