@@ -9,6 +9,7 @@
 // cp.async.bulk copies completing on an mbarrier, applies every operator of the pass in shared
 // memory, and writes the tile back with bulk stores: one HBM read and one write per pass.
 #include <algorithm>
+#include <complex>
 #include <cstring>
 #include <mutex>
 #include <set>
@@ -703,6 +704,72 @@ static std::vector<PassDesc> basis_passes(const Plan& plan, int nbits, int preci
     return out;
 }
 
+// ---- whole-block fusion (complex registers): a register block whose operators cost more than one
+// dense 2^u x 2^u product becomes that product, formed in FP64 on the host and rounded once.
+
+// The block operators a fused block may hold: unconditional unitary pieces (dense, permutation,
+// diagonal, scale) of complex registers.
+static bool block_fusable_op(const TileOp& t) {
+    if (t.pred != 0) return false;
+    const int c = t.tmpl;
+    return (c >= kT_DENSE1 && c < kT_DENSE2 + 16) || (c >= kT_PERM1 && c < kT_PERM2 + 16) || c == kT_SCALE ||
+           c == kT_DIAG || (c >= kT_X1 && c < kT_SWAP + 16);
+}
+
+// Per-element work of a block operator in complex multiply-add units (a dense 1-bit operator is
+// two per element), plus the interpreter's cost of taking one operator: about a quarter of the
+// work of a dense 1-bit operator for complex64 registers, whose passes are bound by instruction
+// issue, and little for complex128 ones, bound by FP64 arithmetic.
+static double block_op_cost(const TileOp& t, double overhead) {
+    const int c = t.tmpl;
+    double work = 1.0;  // phased permutation, diagonal, scale: one complex product
+    if (c >= kT_DENSE1 && c < kT_DENSE1 + 4) work = 2.0;
+    else if (c >= kT_DENSE2 && c < kT_DENSE2 + 16) work = 4.0;
+    else if ((c >= kT_X1 && c < kT_X1 + 4) || (c >= kT_CX && c < kT_CX + 16) || (c >= kT_SWAP && c < kT_SWAP + 16)) work = 0.25;
+    return work + overhead;
+}
+
+// One operator on a block's 2^U amplitudes (block order: position P is group bit U-1-P), by the
+// operator kind's own definition (lsg.h), in FP64.
+static void host_block_op(std::complex<double>* v, int U, const TileOp& t, const double* pool, int64_t member) {
+    const double* m = pool + 2 * (t.data + member * t.stride);
+    auto cx = [&](int i) { return std::complex<double>(m[2 * i], m[2 * i + 1]); };
+    const int D = 1 << U;
+    if (t.kind == LSG_OP_SCALE) {
+        for (int e = 0; e < D; ++e) v[e] *= cx(0);
+        return;
+    }
+    const int k = t.k, d = 1 << k;
+    uint32_t dep[5] = {0, 0, 0, 0, 0}, mask = 0;
+    for (int i = 0; i < k; ++i) {
+        dep[i] = 1u << (U - 1 - t.pos[i]);
+        mask |= dep[i];
+    }
+    auto at = [&](int e, int c) {
+        uint32_t a = (uint32_t)e;
+        for (int i = 0; i < k; ++i)
+            if ((c >> (k - 1 - i)) & 1) a |= dep[i];
+        return a;
+    };
+    std::complex<double> a[32], o[32];
+    for (int e = 0; e < D; ++e) {
+        if ((uint32_t)e & mask) continue;
+        for (int c = 0; c < d; ++c) a[c] = v[at(e, c)];
+        for (int r = 0; r < d; ++r) {
+            if (t.kind == LSG_OP_MATRIX) {
+                std::complex<double> acc = 0.0;
+                for (int c = 0; c < d; ++c) acc += cx(r * d + c) * a[c];
+                o[r] = acc;
+            } else if (t.kind == LSG_OP_PERM) {
+                o[r] = cx(r) * a[(int)m[2 * (d + r)] & (d - 1)];
+            } else {
+                o[r] = cx(r) * a[r];
+            }
+        }
+        for (int r = 0; r < d; ++r) v[at(e, r)] = o[r];
+    }
+}
+
 // Plan and lower `ops`; with `upload`, copy the program to the device (otherwise only the host
 // plan is made: no device call).
 static int program_build(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
@@ -775,10 +842,64 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
             ext.push_back(0.0);
         }
     };
+    const char* fuse_env = getenv("LSG_FUSE_BLOCKS");
+    const bool fuse = !lsg_precision_real(precision) && !(fuse_env && fuse_env[0] == '0');
     for (const PassDesc& pd : p->plan.passes)
         for (int bi = pd.first_block; bi < pd.first_block + pd.nblocks; ++bi) {
-            const BlockDesc& blk = p->plan.blocks[bi];
+            BlockDesc& blk = p->plan.blocks[bi];
             if (blk.generic) continue;
+            if (fuse && blk.u >= 2 && blk.nops > 1) {
+                const int U = blk.u, D = 1 << U;
+                const double overhead = precision == LSG_C64 ? 0.5 : 0.1;
+                bool ok = true;
+                bool per_member = false;
+                double cost = 0.0;
+                for (int o = blk.first; o < blk.first + blk.nops && ok; ++o) {
+                    const TileOp& t = p->plan.ops[pd.first_op + o];
+                    ok = block_fusable_op(t);
+                    per_member |= t.stride != 0;
+                    cost += block_op_cost(t, overhead);
+                }
+                // one dense block: D complex multiply-adds per element, its rows read per group
+                if (ok && cost > 1.1 * ((double)D + overhead + (double)D / 16.0)) {
+                    const int64_t members = per_member ? batch : 1;
+                    const int64_t len = (int64_t)D * D;
+                    pad_ext(0);
+                    const int64_t at = pool_entries + (int64_t)ext.size() / 2;
+                    std::vector<std::complex<double>> col(D);
+                    std::vector<double> mat((size_t)2 * len);
+                    for (int64_t b = 0; b < members; ++b) {
+                        for (int c = 0; c < D; ++c) {
+                            std::fill(col.begin(), col.end(), std::complex<double>(0.0, 0.0));
+                            col[c] = 1.0;
+                            for (int o = blk.first; o < blk.first + blk.nops; ++o) {
+                                const TileOp& t = p->plan.ops[pd.first_op + o];
+                                host_block_op(col.data(), U, t, pool, t.stride ? b : 0);
+                            }
+                            for (int r = 0; r < D; ++r) {
+                                mat[2 * ((size_t)r * D + c)] = col[r].real();
+                                mat[2 * ((size_t)r * D + c) + 1] = col[r].imag();
+                            }
+                        }
+                        ext.insert(ext.end(), mat.begin(), mat.end());
+                        ext.resize(ext.size() + 2 * (size_t)(round_up(len) - len), 0.0);
+                    }
+                    TileOp& f = p->plan.ops[pd.first_op + blk.first];
+                    f.kind = LSG_OP_MATRIX;
+                    f.k = U;
+                    for (int i = 0; i < 8; ++i) {
+                        f.lb[i] = i < U ? blk.bits[i] : 0;
+                        f.sorted[i] = i < U ? blk.sorted[i] : 0;
+                        f.pos[i] = i < U ? i : 0;
+                    }
+                    f.data = at;
+                    f.stride = members > 1 ? round_up(len) : 0;
+                    f.tmpl = kT_DENSEB;
+                    f.zmask = 0;
+                    blk.nops = 1;
+                    continue;
+                }
+            }
             for (int o = blk.first; o < blk.first + blk.nops; ++o) {
                 TileOp& t = p->plan.ops[pd.first_op + o];
                 const int64_t members = t.stride ? batch : 1;
@@ -1597,6 +1718,7 @@ static double op_flops_per_element(const lsg::TileOp& op, bool complex_elems) {
     }
     if ((c >= kT_PERM1 && c < kT_PERM1 + 4) || (c >= kT_PERM2 && c < kT_PERM2 + 16)) return mul;
     if (c == kT_DIAGB || c == kT_SCALE || c == kT_DIAG) return mul;
+    if (c == kT_DENSEB) return (complex_elems ? 8.0 : 2.0) * (double)(1 << op.k);
     if ((c >= kT_DEPOL1 && c < kT_DEPOL1 + 16) || c == kT_DEPOL2) return 4.0;
     if ((c >= kT_X1 && c < kT_X1 + 4) || (c >= kT_CX && c < kT_CX + 16) || (c >= kT_SWAP && c < kT_SWAP + 16)) return 0.0;
     if ((c >= kT_MIX1 && c < kT_MIX1 + 4) || (c >= kT_MIX2 && c < kT_MIX2 + 16)) return complex_elems ? 30.0 : 7.0;

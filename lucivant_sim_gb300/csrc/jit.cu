@@ -141,6 +141,7 @@ bool op_call(std::ostringstream& o, const TileOp& t, int U, const char* T, int a
     else if (c == kT_DEPOL2 && U == 4) o << "rb_depol2<" << T << ">";
     else if (c == kT_DIAGB) name("diagb", true), o << ">";
     else if (c == kT_SCALE) name("scale", true), o << ">";
+    else if (c == kT_DENSEB && !packed) name("denseb", true), o << ">";
     else if (c >= kT_X1 && c < kT_X1 + 4) one("x", kT_X1, false), data = false;
     else if (c >= kT_CX && c < kT_CX + 16) two("cx", kT_CX, false), data = false;
     else if (c >= kT_SWAP && c < kT_SWAP + 16) two("swap", kT_SWAP, false), data = false;

@@ -86,12 +86,13 @@ constexpr int kT_TPD2 = 59;     // + 4 * P0 + P1: real 4x4 transfer matrix whose
 constexpr int kT_X1 = 75;       // + P: unit-phase X (register swap)
 constexpr int kT_CX = 79;       // + 4 * Pcontrol + Ptarget: unit-phase CX (register swap)
 constexpr int kT_SWAP = 95;     // + 4 * P0 + P1
-constexpr int kT_CODES = 111;   // the kernel's codes are exactly 0 .. kT_CODES-1 (a dense switch)
+constexpr int kT_DENSEB = 111;  // a whole register block as one dense 2^u x 2^u complex matrix (block order)
+constexpr int kT_CODES = 112;   // the kernel's codes are exactly 0 .. kT_CODES-1 (a dense switch)
 // host-side markers, rewritten before upload: mixtures become dense codes per member in the kernel,
 // diagonals become kT_DIAGB
-constexpr int kT_MIX1 = 111;    // + P
-constexpr int kT_MIX2 = 115;    // + 4 * P0 + P1
-constexpr int kT_DIAG = 131;
+constexpr int kT_MIX1 = 112;    // + P
+constexpr int kT_MIX2 = 116;    // + 4 * P0 + P1
+constexpr int kT_DIAG = 132;
 constexpr int kT_GENERIC = -1;
 // The greedy fusion planner (csrc/engine.cu): lsg_op list -> passes of tile-local operators.
 // pred/draw/count (may be null) give trajectory operators their predicate bit, uniform offset and

@@ -389,6 +389,48 @@ __device__ __forceinline__ void rb_perm2(T* v, const T* m) {
     }
 }
 
+// A whole register block fused on the host into one dense 2^U x 2^U complex matrix (row-major,
+// rows and columns in block order): out[r] = sum_c m[r][c] v[c]. The host forms the product of
+// the block's operators in FP64 and rounds it once to the register precision.
+template <typename T, int U>
+__device__ __forceinline__ void rb_denseb(T* v, const T* m) {
+    constexpr int D = 1 << U;
+    T out[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+        T row[4];  // the row in 4-entry pieces: few registers beside the group and the outputs
+        ldv<T, 4>(m + r * D, row);
+        T acc = cmul(row[0], v[0]);
+#pragma unroll
+        for (int c = 1; c < D; ++c) {
+            if ((c & 3) == 0) ldv<T, 4>(m + r * D + c, row);
+            acc = cfma(row[c & 3], v[c], acc);
+        }
+        out[r] = acc;
+    }
+#pragma unroll
+    for (int e = 0; e < D; ++e) v[e] = out[e];
+}
+
+// The interpreter's form of rb_denseb: the group is in registers, each output row is stored to
+// the tile as soon as it is formed (the group's elements belong to this thread alone).
+template <typename T, int U>
+__device__ __forceinline__ void rb_denseb_store(T* tile, uint32_t base, const uint32_t* off, const T* v, const T* m) {
+    constexpr int D = 1 << U;
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+        T row[4];
+        ldv<T, 4>(m + r * D, row);
+        T acc = cmul(row[0], v[0]);
+#pragma unroll
+        for (int c = 1; c < D; ++c) {
+            if ((c & 3) == 0) ldv<T, 4>(m + r * D + c, row);
+            acc = cfma(row[c & 3], v[c], acc);
+        }
+        tile[base | off[r]] = acc;
+    }
+}
+
 // Unit-phase permutations are register renames: no arithmetic at all.
 template <typename T, int U, int P>
 __device__ __forceinline__ void rb_x(T* v) {
@@ -710,6 +752,7 @@ __device__ __forceinline__ void rb_apply(T* v, int code, const T* m) {
         LSG_R2(rb_swap, kT_SWAP)
         case kT_DIAGB: rb_diagb<T, U>(v, m); break;
         case kT_SCALE: rb_scale<T, U>(v, m); break;
+
         default: break;
     }
 }
@@ -812,12 +855,19 @@ __device__ void run_block(T* tile, int tbits, const BlockDesc& blk, const OpRec*
         off[e] = a;
     }
     const int groups = 1 << (tbits - U);
+    const bool dense = blk.nops == 1 && recs[blk.first].code == kT_DENSEB;
     for (int g = threadIdx.x; g < groups; g += kCompute) {
         uint32_t base = 0;
 #pragma unroll
         for (int i = 0; i <= U; ++i) base |= ((uint32_t)g << i) & blk.dep[i];
         T v[1 << U];
         load_group<T, U>(tile, base, off, blk.vec, v);
+        if constexpr (Elem<T>::complex) {
+            if (dense) {  // a fused block: each output row straight back to its place in the tile
+                rb_denseb_store<T, U>(tile, base, off, v, static_cast<const T*>(recs[blk.first].m));
+                continue;
+            }
+        }
         for (int o = 0; o < blk.nops; ++o) {
             const OpRec r = recs[blk.first + o];
             rb_apply<T, U>(v, r.code, static_cast<const T*>(r.m));
