@@ -140,6 +140,19 @@ int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float*
  * call (simulator.py:229-251). */
 int lsg_programs_run_ragged(int32_t count, const lsg_program* programs, const lsg_state* states, const int64_t* index,
                             float* step_ms);
+/* Circuit templates. lsg_program_set_data gives program p the operator data of `ops`/`pool` — the
+ * same circuit template with other parameters — without planning or allocating again: the
+ * operators must plan exactly as p's did (same passes, blocks, operator codes and data layout;
+ * otherwise LSG_E_STATE and p is unchanged). The copy is ordered on register s's stream, after
+ * its earlier work. lsg_program_graph_run is lsg_program_run_from_basis(p, s, index, NULL) as
+ * one CUDA graph launch: the first call for a (register, index) pair runs the program and
+ * captures basis state + passes into a graph that later calls replay; data set since stays in
+ * effect (the graph reads p's device data). Neither waits. No counterpart in the reference, which
+ * parses a template again for every set of `input` parameters (qasm.py:842-870) and evolves each
+ * circuit from scratch (simulator.py:229-251). */
+int lsg_program_set_data(lsg_program p, lsg_state s, const lsg_op* ops, int32_t nops, const double* pool,
+                         int64_t pool_entries);
+int lsg_program_graph_run(lsg_program p, lsg_state s, int64_t index);
 /* HBM bytes (2 x tile bytes per tile visited) and tiles of one lsg_program_run_from_basis. */
 int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run);
 /* Number of fused passes, and algorithmic HBM bytes of one run (2 x register bytes per pass). */

@@ -78,6 +78,8 @@ SIGNATURES: dict[str, tuple[Any, list[Any]]] = {
     "lsg_program_run_from_basis": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_float)]),
     "lsg_program_basis_info": (C.c_int, [_P, _PI64, _PI64]),
     "lsg_programs_run_ragged": (C.c_int, [_I32, C.POINTER(_P), C.POINTER(_P), _PI64, C.POINTER(C.c_float)]),
+    "lsg_program_set_data": (C.c_int, [_P, _P, _P, _I32, _PD, _I64]),
+    "lsg_program_graph_run": (C.c_int, [_P, _P, _I64]),
     "lsg_program_free": (C.c_int, [_P]),
     "lsg_program_create_opts": (C.c_int, [_P, _P, _I32, _PD, _I64, _P, C.POINTER(_P)]),
     "lsg_program_pass_info": (C.c_int, [_P, _I32, _PI64, _PD, _PI32]),
@@ -212,15 +214,30 @@ class OpList:
         return len(self.rows)
 
     def packed(self) -> tuple[np.ndarray, np.ndarray]:
-        ops = np.zeros(len(self.rows), dtype=OP_DTYPE)
-        for i, (kind, nb, bits, data, stride) in enumerate(self.rows):
-            ops[i]["kind"] = kind
-            ops[i]["nbits"] = nb
-            ops[i]["bits"][:nb] = bits
-            ops[i]["data"] = data
-            ops[i]["batch_stride"] = stride
+        """(operator table, float64 view of the pool), built column by column and kept until the
+        next ``add``."""
+        cached = getattr(self, "_packed", None)
+        if cached is not None and cached[0] == len(self.rows):
+            return cached[1]
+        n = len(self.rows)
+        ops = np.zeros(n, dtype=OP_DTYPE)
+        if n:
+            kinds, nbs, bitss, datas, strides = zip(*self.rows)
+            ops["kind"] = kinds
+            ops["nbits"] = nbs
+            ops["data"] = datas
+            ops["batch_stride"] = strides
+            bits = np.zeros((n, MAX_OP_BITS), dtype=np.int32)
+            widths = np.asarray(nbs)
+            for w in np.unique(widths):
+                rows = np.flatnonzero(widths == w)
+                if w:
+                    bits[rows, :w] = np.asarray([bitss[i] for i in rows], dtype=np.int32).reshape(len(rows), w)
+            ops["bits"] = bits
         pool = np.concatenate(self.chunks) if self.chunks else np.zeros(1, dtype=np.complex128)
-        return ops, np.ascontiguousarray(pool.view(np.float64))
+        out = ops, np.ascontiguousarray(pool.view(np.float64))
+        self._packed = (n, out)
+        return out
 
 
 class Register:
@@ -473,6 +490,19 @@ class Program:
                                              ptr(blocks, C.c_int32)))  # fmt: skip
         k = self.passes
         return {"bytes": tiles[:k], "flops_per_element": flops[:k], "blocks": blocks[:k]}
+
+    def set_data(self, reg: Register, ops: OpList) -> None:
+        """Take the operator data of ``ops`` (the same template with other parameters) without
+        planning or allocating again. :class:`EngineError` when ``ops`` plan differently (another
+        structure). Ordered after ``reg``'s earlier work."""
+        table, pool = ops.packed()
+        check(self.lib.lsg_program_set_data(self.handle, reg.handle, table.ctypes.data, len(table),
+                                            ptr(pool, C.c_double), pool.size // 2))  # fmt: skip
+
+    def graph_run(self, reg: Register, index: int = 0) -> None:
+        """``run_from_basis`` as one CUDA graph launch (captured on the first call for this
+        register and index). Does not wait."""
+        check(self.lib.lsg_program_graph_run(self.handle, reg.handle, index))
 
     def run_timed(self, reg: Register) -> np.ndarray:
         out = np.zeros(max(self.passes, 1), dtype=np.float32)

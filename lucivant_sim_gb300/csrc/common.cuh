@@ -84,6 +84,7 @@ struct lsg_state_s {
     lsg::Scratch program;  // uploaded pass programs
     lsg::Scratch scratch;  // reduction partials, CDFs, sampling buffers
     lsg::Scratch scratch2;
+    uint64_t uid = 0;  // distinct for every register made in this process (graphs are bound to one)
     size_t elem_bytes() const { return lsg_elem_bytes(precision); }
     bool real() const { return lsg_precision_real(precision); }
     size_t member_bytes() const { return elem_bytes() * (size_t)elems; }

@@ -9,6 +9,7 @@
 // cp.async.bulk copies completing on an mbarrier, applies every operator of the pass in shared
 // memory, and writes the tile back with bulk stores: one HBM read and one write per pass.
 #include <algorithm>
+#include <atomic>
 #include <complex>
 #include <cstring>
 #include <mutex>
@@ -576,6 +577,18 @@ struct lsg_program_s {
     std::vector<lsg::PassDesc> basis_passes;
     int64_t basis_index = -1;
     size_t basis_off = 0;
+    // the pool section (caller's pool, then relocated and fused data) in the register precision:
+    // kept by host-only builds, whose data a program of the same structure takes over
+    std::vector<unsigned char> pool_bytes;
+    lsg::PlanChoice choice;  // the plan choices it was made with
+    // the operator table and the plan before lowering: a template's new data is lowered onto this
+    // plan without planning again (lsg_program_set_data)
+    std::vector<lsg_op> src_ops;
+    lsg::Plan raw_plan;
+    // the template's CUDA graph: set basis state + every pass, captured for one register and index
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_uid = 0;
+    int64_t graph_index = -1;
 };
 
 namespace lsg {
@@ -774,16 +787,21 @@ static void host_block_op(std::complex<double>* v, int U, const TileOp& t, const
 // plan is made: no device call).
 static int program_build(int nbits, int precision, int64_t batch, const lsg_op* ops, int32_t nops, const double* pool,
                          int64_t pool_entries, const int* pred, const int* draw, const int* count, lsg_program_s** out,
-                         cudaStream_t stream, bool upload) {
+                         cudaStream_t stream, bool upload, const Plan* preplanned = nullptr) {
     auto* p = new lsg_program_s();
     p->nbits = nbits;
     p->precision = precision;
     p->batch = batch;
+    p->choice = t_choice;
     p->dev.stream = stream;
     p->K = tile_bits_for(nbits, precision);
     const int L = std::min(p->K, low_bits_for(nbits, precision));
     if (nops > 0) {
-        p->plan = plan_ops(ops, nops, nbits, p->K, L, pred, draw, count, block_bits_for(precision));
+        p->plan = preplanned ? *preplanned : plan_ops(ops, nops, nbits, p->K, L, pred, draw, count, block_bits_for(precision));
+        if (upload && !pred && !draw && !count) {
+            p->src_ops.assign(ops, ops + nops);
+            p->raw_plan = p->plan;
+        }
         if (p->plan.passes.empty()) {
             delete p;
             return fail(LSG_E_ARG, "an operator does not fit a tile of %d bits (%d kept low)", tile_bits_for(nbits, precision), L);
@@ -967,10 +985,6 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
         delete p;
         return fail(LSG_E_ARG, "a pass needs more than 220 KB of shared memory");
     }
-    if (!upload) {
-        *out = p;
-        return LSG_OK;
-    }
     const size_t head0 = p->plan.passes.size() * sizeof(PassDesc) + p->plan.ops.size() * sizeof(TileOp) +
                          p->plan.blocks.size() * sizeof(BlockDesc);
     p->basis_off = (head0 + 15) & ~size_t(15);
@@ -1008,6 +1022,11 @@ static int program_build(int nbits, int precision, int64_t batch, const lsg_op* 
     unsigned char* dst = blob.data() + p->head_aligned;
     put(pool, base_entries, dst);
     put(ext.data(), (int64_t)ext.size() / 2, dst + (size_t)base_entries * elt);
+    if (!upload) {
+        p->pool_bytes.assign(dst, dst + (size_t)pool_entries * elt);
+        *out = p;
+        return LSG_OK;
+    }
     int rc = ensure(p->dev, total);
     if (rc == LSG_OK) {
         // the host blob is released on return: the copy must have consumed it
@@ -1073,6 +1092,7 @@ static int program_create_jit(int nbits, int precision, int64_t batch, const lsg
 void program_destroy(lsg_program_s* p) {
     if (!p) return;
     for (cudaEvent_t e : p->events) cudaEventDestroy(e);
+    if (p->graph) cudaGraphExecDestroy(p->graph);
     release(p->dev);
     delete p;
 }
@@ -1097,6 +1117,19 @@ int program_run_ctx(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, const 
 
 int set_basis_async(lsg_state_s* s, int64_t index);
 
+// Make the program's device basis passes those of `index` (a complex register's fixed bits are the
+// index's bits; a real register's do not depend on it), on the register's stream.
+static int basis_passes_for(lsg_program_s* p, lsg_state_s* s, int64_t index) {
+    if (s->real() || index == p->basis_index) return LSG_OK;
+    p->basis_passes = basis_passes(p->plan, p->nbits, p->precision, index);
+    void* dst = static_cast<unsigned char*>(p->dev.ptr) + p->basis_off;
+    // pageable source: the copy is staged before the call returns
+    LSG_CUDA(cudaMemcpyAsync(dst, p->basis_passes.data(), p->basis_passes.size() * sizeof(PassDesc),
+                             cudaMemcpyHostToDevice, s->stream));
+    p->basis_index = index;
+    return LSG_OK;
+}
+
 // Set every member to basis state `index` and make the program's basis passes those of `index`
 // (on the register's stream).
 static int basis_prepare(lsg_program_s* p, lsg_state_s* s, int64_t index) {
@@ -1104,16 +1137,7 @@ static int basis_prepare(lsg_program_s* p, lsg_state_s* s, int64_t index) {
         return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
                     p->nbits, p->precision, (long long)p->batch);
     LSG_CHECK(set_basis_async(s, index));  // stream-ordered: no host wait before the passes
-    const bool real = s->real();
-    if (!real && index != p->basis_index) {  // the fixed values are the index's bits: re-upload
-        p->basis_passes = basis_passes(p->plan, p->nbits, p->precision, index);
-        void* dst = static_cast<unsigned char*>(p->dev.ptr) + p->basis_off;
-        // pageable source: the copy is staged before the call returns
-        LSG_CUDA(cudaMemcpyAsync(dst, p->basis_passes.data(), p->basis_passes.size() * sizeof(PassDesc),
-                                 cudaMemcpyHostToDevice, s->stream));
-        p->basis_index = index;
-    }
-    return LSG_OK;
+    return basis_passes_for(p, s, index);
 }
 
 // Set every member to basis state `index`, then run the passes on the tiles that can be nonzero.
@@ -1382,11 +1406,13 @@ int lsg_state_create(int nbits, int precision, int64_t batch, lsg_state* out) {
     if ((lsg_precision_real(precision)) && (nbits & 1))
         return fail(LSG_E_ARG, "a Pauli-transfer register has an even number of bits (two per qubit)");
     if (batch < 1) return fail(LSG_E_ARG, "lsg_state_create: batch must be at least 1");
+    static std::atomic<uint64_t> next_uid{0};
     auto* s = new lsg_state_s();
     s->nbits = nbits;
     s->precision = precision;
     s->batch = batch;
     s->elems = 1ll << nbits;
+    s->uid = ++next_uid;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete s;
@@ -1687,6 +1713,79 @@ int lsg_programs_run_ragged(int32_t count, const lsg_program* programs, const ls
     }
     cleanup();  // events already recorded are released when they complete
     return rc;
+}
+
+int lsg_program_set_data(lsg_program p, lsg_state s, const lsg_op* ops, int32_t nops, const double* pool,
+                         int64_t pool_entries) {
+    clear_error();
+    if (!p || !s) return fail(LSG_E_ARG, "null argument");
+    if (s->nbits != p->nbits || s->precision != p->precision || s->batch != p->batch)
+        return fail(LSG_E_STATE, "the program was built for a register of %d bits, precision %d, batch %lld",
+                    p->nbits, p->precision, (long long)p->batch);
+    LSG_CHECK(validate_ops(p->nbits, p->precision, p->batch, ops, nops, pool, pool_entries));
+    // the same operator table (kinds, bits, data offsets): the program's plan holds for it
+    if (p->src_ops.empty() || (size_t)nops != p->src_ops.size() ||
+        std::memcmp(ops, p->src_ops.data(), (size_t)nops * sizeof(lsg_op)) != 0)
+        return fail(LSG_E_STATE, "lsg_program_set_data: the operators plan differently from the program's (another "
+                                 "structure): build a new program");
+    lsg_program_s* q = nullptr;
+    const PlanChoice keep = t_choice;  // the plan choices the program was made with
+    t_choice = p->choice;
+    const int rc = program_build(p->nbits, p->precision, p->batch, ops, nops, pool, pool_entries, nullptr, nullptr,
+                                 nullptr, &q, nullptr, false, &p->raw_plan);
+    t_choice = keep;
+    LSG_CHECK(rc);
+    auto same_bytes = [](const auto& a, const auto& b) {
+        return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size() * sizeof(a[0])) == 0);
+    };
+    const bool same = q->K == p->K && same_bytes(q->plan.passes, p->plan.passes) && same_bytes(q->plan.ops, p->plan.ops) &&
+                      same_bytes(q->plan.blocks, p->plan.blocks) &&
+                      p->head_aligned + q->pool_bytes.size() <= p->dev.bytes;
+    if (!same) {
+        program_destroy(q);
+        return fail(LSG_E_STATE, "lsg_program_set_data: the operators plan differently from the program's (another "
+                                 "structure): build a new program");
+    }
+    // after the register's earlier work (a run may still read the old data); pageable source:
+    // staged before the call returns
+    const cudaError_t e = cudaMemcpyAsync(static_cast<unsigned char*>(p->dev.ptr) + p->head_aligned, q->pool_bytes.data(),
+                                          q->pool_bytes.size(), cudaMemcpyHostToDevice, s->stream);
+    program_destroy(q);
+    if (e != cudaSuccess) return fail(LSG_E_CUDA, "lsg_program_set_data: %s", cudaGetErrorString(e));
+    return LSG_OK;
+}
+
+int lsg_program_graph_run(lsg_program p, lsg_state s, int64_t index) {
+    clear_error();
+    if (!p || !s) return fail(LSG_E_ARG, "null argument");
+    if (!p->graph || p->graph_uid != s->uid || p->graph_index != index) {
+        if (p->graph) {
+            cudaGraphExecDestroy(p->graph);
+            p->graph = nullptr;
+        }
+        // everything that is not a stream operation happens before the capture: the basis passes
+        // for `index` (a host copy), the device status word, kernel attributes (a first run)
+        LSG_CHECK(program_run_basis(p, s, index, nullptr));
+        cudaGraph_t graph = nullptr;
+        LSG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = set_basis_async(s, index);
+        if (rc == LSG_OK) rc = program_launch(p, s, nullptr, TrajCtx{}, true);
+        const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+        if (rc == LSG_OK && e != cudaSuccess) rc = fail(LSG_E_CUDA, "capturing the program: %s", cudaGetErrorString(e));
+        if (rc == LSG_OK && cudaGraphInstantiate(&p->graph, graph, 0) != cudaSuccess) {
+            p->graph = nullptr;
+            rc = fail(LSG_E_CUDA, "instantiating the program's graph failed");
+        }
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (rc != LSG_OK) return rc;
+        p->graph_uid = s->uid;
+        p->graph_index = index;
+        return LSG_OK;  // this call's run was the plain one before the capture
+    }
+    LSG_CHECK(basis_passes_for(p, s, index));  // another index may have run in between
+    LSG_CUDA(cudaGraphLaunch(p->graph, s->stream));
+    return LSG_OK;
 }
 
 int lsg_program_basis_info(lsg_program p, int64_t* bytes_per_run, int64_t* tiles_per_run) {
