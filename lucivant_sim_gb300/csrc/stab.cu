@@ -17,6 +17,7 @@
 //    same stream's uint8 integers.
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -90,6 +91,9 @@ struct NTable {  // Pauli noise branches: normalised cumulative probabilities an
     int32_t k, nb;
     double cum[16];
     uint8_t label[16];  // per qubit i (first qubit bit 2(k-1-i)): x bit then z bit
+    // cum[i] <= u for a uniform u = m * 2^-53 (m = raw >> 11) exactly when m >= thr[i] =
+    // ceil(cum[i] * 2^53): the branch search in integers, with the same answers
+    uint64_t thr[16];
 };
 
 __device__ __forceinline__ uint32_t xor_reduce_block(uint32_t v) {
@@ -553,6 +557,8 @@ struct FrameArgs {
     const u128* word_mult;
     const u128* word_plus;
     u128 s0;  // generator state at the start of the run (no uint32 buffered)
+    const uint4* masks;  // the noise masks of k_noise_masks, or null: drawn here, per gate
+    int64_t nnoisy;
     // outputs
     uint32_t* fx;  // n x words (the final X parts of the frames)
     int words;
@@ -595,15 +601,25 @@ __global__ void k_frames(FrameArgs A) {
             const GateRec g = A.gates[i];
             frame_gate(X, Z, g, A.tables);
             if (g.noise < 0) continue;
+            if (A.masks) {
+                const uint4 mk = A.masks[(int64_t)w * A.nnoisy + g.nk];
+                X[g.a] ^= mk.x;
+                Z[g.a] ^= mk.y;
+                if (mk.z | mk.w) {  // only two-qubit noise sets them
+                    X[g.b] ^= mk.z;
+                    Z[g.b] ^= mk.w;
+                }
+                continue;
+            }
             const NTable& nt = A.noise[g.noise];
             // this word's shots draw uniforms number shot0 .. shot0+31 of the gate's block
             u128 st = wm * A.gate_states[g.nk] + wp;
             uint32_t mx[2] = {0, 0}, mz[2] = {0, 0};
             for (int j = 0; j < valid; ++j) {
                 st = st * mult + A.inc;
-                const double u = pcg_double(pcg_output(st));
+                const uint64_t um = pcg_output(st) >> 11;  // the uniform is um * 2^-53
                 int pick = 0;  // searchsorted(cumulative, u, side='right'), clamped
-                while (pick < nt.nb && nt.cum[pick] <= u) ++pick;
+                while (pick < nt.nb && nt.thr[pick] <= um) ++pick;
                 if (pick > nt.nb - 1) pick = nt.nb - 1;
                 const uint8_t lab = nt.label[pick];
                 for (int qi = 0; qi < nt.k; ++qi) {
@@ -692,6 +708,38 @@ __global__ void k_words_to_pairs(const uint64_t* __restrict__ outw, int W, int s
 __global__ void k_gate_states(u128 s0, u128 inc, uint64_t base, uint64_t stride, int64_t count, u128* out) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
         out[k] = pcg_advance(s0, inc, base + (uint64_t)k * stride);
+}
+
+// The Pauli-noise masks of every noisy gate for every 32-shot word, over all SMs: a warp per
+// (gate, word), lane j drawing shot 32w + j's uniform (the gate's block state advanced by
+// 32w + j + 1: word jump, then lane jump) and choosing its branch; ballots give the word's X and Z
+// masks of the gate's (up to two) qubits. masks[w * nnoisy + nk] = {x0, z0, x1, z1}.
+__global__ void k_noise_masks(const u128* __restrict__ gate_states, const int16_t* __restrict__ gate_table,
+                              const NTable* __restrict__ noise, int64_t nnoisy, int words, int shots,
+                              const u128* __restrict__ word_mult, const u128* __restrict__ word_plus,
+                              const u128* __restrict__ lane_mult, const u128* __restrict__ lane_plus, uint4* masks) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const u128 lm = lane_mult[lane], lp = lane_plus[lane];
+    for (int64_t t = (((int64_t)blockIdx.x * blockDim.x) + threadIdx.x) >> 5; t < nnoisy * words; t += nwarps) {
+        const int w = (int)(t / nnoisy);
+        const int64_t nk = t - (int64_t)w * nnoisy;
+        const NTable& nt = noise[gate_table[nk]];
+        const u128 st = lm * (word_mult[w] * gate_states[nk] + word_plus[w]) + lp;
+        const uint64_t m = pcg_output(st) >> 11;
+        int pick = 0;  // searchsorted(cumulative, u, side='right'), clamped
+        while (pick < nt.nb && nt.thr[pick] <= m) ++pick;
+        if (pick > nt.nb - 1) pick = nt.nb - 1;
+        const bool live = 32 * w + lane < shots;
+        const unsigned lab = live ? nt.label[pick] : 0u;
+        const int sh = 2 * (nt.k - 1);  // the first qubit's bits
+        uint4 out;
+        out.x = __ballot_sync(0xffffffffu, (lab >> (sh + 1)) & 1);
+        out.y = __ballot_sync(0xffffffffu, (lab >> sh) & 1);
+        out.z = nt.k == 2 ? __ballot_sync(0xffffffffu, (lab >> 1) & 1) : 0u;
+        out.w = nt.k == 2 ? __ballot_sync(0xffffffffu, lab & 1) : 0u;
+        if (lane == 0) masks[t] = out;
+    }
 }
 
 // ASAP moments of a gate list: a gate's moment is one past the latest moment among its qubits
@@ -1100,6 +1148,9 @@ int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t*
         for (int j = 0; j < 16; ++j) {
             nt[i].cum[j] = s.cumulative[j];
             nt[i].label[j] = s.label[j];
+            const double c = s.cumulative[j];
+            // exact: scaling by 2^53 and ceil are exact in FP64; c >= 1 is never <= a uniform
+            nt[i].thr[j] = !(c > 0.0) ? 0ull : c >= 1.0 ? (1ull << 53) : (uint64_t)std::ceil(std::ldexp(c, 53));
         }
     }
     std::vector<int64_t> order, starts;
@@ -1121,8 +1172,17 @@ int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t*
         if (pair_err[j] >= 0) ++nerr;
     if (raw_used) *raw_used = (int64_t)(base_flip + (uint64_t)nerr * shots);
     const int words = (int)((shots + 31) / 32);
-    std::vector<u128> wmul(words), wplus(words);
+    std::vector<u128> wmul(words), wplus(words), lmul(32), lplus(32);
     for (int w = 0; w < words; ++w) pcg_jump(inc, (uint64_t)32 * w, &wmul[w], &wplus[w]);
+    for (int j = 0; j < 32; ++j) pcg_jump(inc, (uint64_t)j + 1, &lmul[j], &lplus[j]);
+    // the noise masks of all noisy gates and words drawn up front over every SM, when they fit a
+    // quarter of the free device memory (else the frame kernel draws them per gate)
+    std::vector<int16_t> gate_table((size_t)std::max<int64_t>(nk, 1), 0);
+    for (int64_t i = 0; i < ngates; ++i)
+        if (recs[i].noise >= 0) gate_table[(size_t)recs[i].nk] = recs[i].noise;
+    const size_t mask_bytes = (size_t)nk * (size_t)words * sizeof(uint4);
+    size_t free_mem = 0, total_mem = 0;
+    const bool premask = nk > 0 && cudaMemGetInfo(&free_mem, &total_mem) == cudaSuccess && mask_bytes <= free_mem / 4;
     cudaStream_t st = nullptr;
     LSG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
@@ -1142,6 +1202,10 @@ int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t*
     const size_t o_p1 = off; off += al((size_t)npairs * 8);
     const size_t o_x0 = off; off += al((size_t)npairs);
     const size_t o_out = off; off += al((size_t)shots * nclbits);
+    const size_t o_lm = off; off += al(32 * 16);
+    const size_t o_lp = off; off += al(32 * 16);
+    const size_t o_gt = off; off += al(gate_table.size() * sizeof(int16_t));
+    const size_t o_mk = off; off += premask ? al(mask_bytes) : 0;
     Scratch work;
     int rc = ensure(work, off);
     if (rc != LSG_OK) {
@@ -1170,6 +1234,9 @@ int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t*
     H2D(o_p0, p01, (size_t)npairs * 8);
     H2D(o_p1, p10, (size_t)npairs * 8);
     H2D(o_x0, pair_x0, (size_t)npairs);
+    H2D(o_lm, lmul.data(), 32 * 16);
+    H2D(o_lp, lplus.data(), 32 * 16);
+    if (premask) H2D(o_gt, gate_table.data(), gate_table.size() * sizeof(int16_t));
     if (ce == cudaSuccess) ce = cudaMemsetAsync(b + o_out, 0, (size_t)shots * nclbits, st);
     if (ce == cudaSuccess && nk)
         k_gate_states<<<std::max<int64_t>(1, std::min<int64_t>((nk + kS - 1) / kS, 152 * 64)), kS, 0, st>>>(
@@ -1189,6 +1256,16 @@ int lsg_frames_run(int n, const lsg_cgate* gates, int64_t ngates, const uint8_t*
     A.s0 = s0;
     A.fx = (uint32_t*)(b + o_fx);
     A.words = words;
+    A.masks = premask ? (const uint4*)(b + o_mk) : nullptr;
+    A.nnoisy = nk;
+    if (ce == cudaSuccess && premask) {
+        const int64_t warps = nk * (int64_t)words;
+        k_noise_masks<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((warps * 32 + kS - 1) / kS, 152 * 32)), kS, 0, st>>>(
+            (const u128*)(b + o_s), (const int16_t*)(b + o_gt), (const NTable*)(b + o_n), nk, words, (int)shots,
+            (const u128*)(b + o_wm), (const u128*)(b + o_wp), (const u128*)(b + o_lm), (const u128*)(b + o_lp),
+            (uint4*)(b + o_mk));
+        ce = cudaGetLastError();
+    }
     if (ce == cudaSuccess) {
         k_frames<<<words, kS, (size_t)2 * n * 4, st>>>(A);
         ce = cudaGetLastError();
