@@ -226,7 +226,10 @@ struct Swizzle {
 // (applied to the load addresses, last rename first) and stores (in program order).
 struct BlockGen {
     const BlockDesc* b = nullptr;
-    int U = 0, n = 0, groups = 0, W = 1, run = 1;
+    int U = 0, n = 0, groups = 0, W = 1, run = 1, elem_bytes = 4;
+    // the bits of the group loop index a warp's lanes drive (5, ascending): chosen so that the
+    // block's shared-memory accesses of one warp need the fewest wavefronts
+    int lane_bits[5] = {0, 1, 2, 3, 4};
     std::vector<uint32_t> off;
     uint32_t vec_bits = 0;  // tile bits inside one shared-memory access (renames must keep them)
     std::vector<Rename> load_map, store_map;
@@ -246,6 +249,7 @@ BlockGen block_gen(const BlockDesc& b, const PassDesc& pd, int elem_bytes, int c
     BlockGen g;
     g.b = &b;
     g.U = b.u, g.n = 1 << b.u, g.groups = 1 << (pd.K - b.u);
+    g.elem_bytes = elem_bytes;
     // Two groups per thread when tile bit 0 is not a block bit: the pair (tile bit 0 = 0, 1)
     // moves as one wider shared-memory access and every operator's coefficients, loaded once,
     // serve both groups (the two calls read the same addresses). Only when there are at least as
@@ -299,6 +303,145 @@ std::vector<std::string> mapped_addresses(std::ostringstream& o, const BlockGen&
     return addr;
 }
 
+// The group loop index with its low five bits (the lane) moved to the positions in `lane` and
+// the other bits, in order, to the remaining positions below `m` bits: a bijection of [0, 2^m).
+uint32_t lane_permute(uint32_t g, const int* lane, int m) {
+    uint32_t out = 0, lanes = 0;
+    for (int i = 0; i < 5; ++i) {
+        out |= ((g >> i) & 1u) << lane[i];
+        lanes |= 1u << lane[i];
+    }
+    int src = 5;
+    for (int t = 0; t < m; ++t)
+        if (!((lanes >> t) & 1u)) out |= ((g >> src++) & 1u) << t;
+    return out;
+}
+
+// Element addresses of one group (base = the group's first element) under a folded rename map
+// and the swizzle, as mapped_addresses emits them.
+void group_addresses(const BlockGen& g, uint32_t base, const std::vector<Rename>& map, uint32_t tile_mask,
+                     const Swizzle& sw, std::vector<uint32_t>& out) {
+    out.resize(g.n);
+    if (map.empty() && !sw.on) {
+        for (int e = 0; e < g.n; ++e) out[e] = base + g.off[e];
+        return;
+    }
+    uint32_t block_bits = 0;
+    for (int i = 0; i < g.U; ++i) block_bits |= 1u << g.b->bits[i];
+    uint32_t may = tile_mask & ~block_bits & ~(g.W == 2 ? 1u : 0u) & ~g.vec_bits;
+    uint32_t var = base, zero = 0;
+    for (const Rename& r : map) {
+        var = r.apply(var);
+        may = r.may(may);
+        zero = r.apply(zero);
+    }
+    if (sw.on) {
+        var = sw.apply(var);
+        may = sw.may(may);
+    }
+    for (int e = 0; e < g.n; ++e) {
+        uint32_t c = g.off[e];
+        for (const Rename& r : map) c = r.apply(c);
+        c = sw.apply(c ^ zero);
+        out[e] = (c & may) ? (var ^ c) : (var + c);
+    }
+}
+
+// Shared-memory wavefronts of one warp's accesses (lane i at byte address addr[i], `bytes` wide):
+// phases of 128 / bytes lanes; in each, the most distinct 4-byte words any bank must serve.
+int warp_wavefronts(const uint32_t* addr, int bytes) {
+    const int per = std::max(1, 128 / std::max(bytes, 4));
+    int total = 0;
+    for (int p0 = 0; p0 < 32; p0 += per) {
+        uint32_t words[32][8];
+        int count[32] = {0};
+        int worst = 1;
+        for (int l = p0; l < p0 + per && l < 32; ++l)
+            for (int w = 0; w < std::max(bytes, 4) / 4; ++w) {
+                const uint32_t word = addr[l] / 4 + (uint32_t)w;
+                const int bank = (int)(word & 31u);
+                bool seen = false;
+                for (int k = 0; k < count[bank] && !seen; ++k) seen = words[bank][k] == word;
+                if (!seen && count[bank] < 8) {
+                    words[bank][count[bank]++] = word;
+                    worst = std::max(worst, count[bank]);
+                }
+            }
+        total += worst;
+    }
+    return total;
+}
+
+// Wavefronts of one warp's loads and stores of a block (the first warp of the loop, lanes driving
+// the index bits in `lane`).
+int block_wavefronts(const BlockGen& g, const int* lane, int m, uint32_t tile_mask, const Swizzle& sw) {
+    const int bytes = (g.W == 2 ? 2 : g.run) * g.elem_bytes;
+    std::vector<uint32_t> ld[32], st[32];
+    for (int l = 0; l < 32; ++l) {
+        const uint32_t G = lane_permute((uint32_t)l, lane, m) << (g.W == 2 ? 1 : 0);
+        uint32_t base = 0;
+        for (int i = 0; i <= g.U; ++i) base |= (G << i) & g.b->dep[i];
+        group_addresses(g, base, g.load_map, tile_mask, sw, ld[l]);
+        group_addresses(g, base, g.store_map, tile_mask, sw, st[l]);
+    }
+    int total = 0;
+    uint32_t a[32];
+    for (int e = 0; e < g.n; e += g.run) {
+        for (int l = 0; l < 32; ++l) a[l] = ld[l][e] * (uint32_t)g.elem_bytes;
+        total += warp_wavefronts(a, bytes);
+        for (int l = 0; l < 32; ++l) a[l] = st[l][e] * (uint32_t)g.elem_bytes;
+        total += warp_wavefronts(a, bytes);
+    }
+    return total;
+}
+
+// Pick the five index bits the lanes drive (a 5-subset of the loop index's bits, ascending) with
+// the fewest wavefronts; the lowest five when nothing is better.
+void choose_lane_bits(BlockGen& g, uint32_t tile_mask, const Swizzle& sw) {
+    int m = 0;
+    while ((1 << m) < g.groups / g.W) ++m;
+    if (m <= 5) return;
+    int best[5] = {0, 1, 2, 3, 4};
+    int best_cost = block_wavefronts(g, best, m, tile_mask, sw);
+    int c[5];
+    for (c[0] = 0; c[0] < m; ++c[0])
+        for (c[1] = c[0] + 1; c[1] < m; ++c[1])
+            for (c[2] = c[1] + 1; c[2] < m; ++c[2])
+                for (c[3] = c[2] + 1; c[3] < m; ++c[3])
+                    for (c[4] = c[3] + 1; c[4] < m; ++c[4]) {
+                        const int cost = block_wavefronts(g, c, m, tile_mask, sw);
+                        if (cost < best_cost) {
+                            best_cost = cost;
+                            std::copy(c, c + 5, best);
+                        }
+                    }
+    std::copy(best, best + 5, g.lane_bits);
+}
+
+// The generated expression of lane_permute(g) (constant positions; runs of bits move together).
+std::string lane_permute_expr(const BlockGen& g, int m) {
+    int target[32];
+    uint32_t lanes = 0;
+    for (int i = 0; i < 5; ++i) {
+        target[i] = g.lane_bits[i];
+        lanes |= 1u << g.lane_bits[i];
+    }
+    int src = 5;
+    for (int t = 0; t < m; ++t)
+        if (!((lanes >> t) & 1u)) target[src++] = t;
+    std::ostringstream e;
+    bool first = true;
+    for (int j = 0; j < m;) {
+        int k = j + 1;
+        while (k < m && target[k] == target[k - 1] + 1) ++k;
+        const uint32_t mask = (1u << (k - j)) - 1u;
+        e << (first ? "" : " | ") << "(((uint32_t(g) >> " << j << ") & " << mask << "u) << " << target[j] << ")";
+        first = false;
+        j = k;
+    }
+    return e.str();
+}
+
 void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, const PassDesc& pd, const char* T,
                 const Swizzle& sw, bool packed, bool* ok) {
     const BlockDesc& b = *g.b;
@@ -309,7 +452,14 @@ void emit_block(std::ostringstream& o, const BlockGen& g, const Plan& plan, cons
         o << "    cbar();\n    {\n      const int g = threadIdx.x;\n      const bool act = g < " << g.groups / g.W << ";\n";
     else
         o << "    cbar();\n    for (int g = threadIdx.x; g < " << g.groups / g.W << "; g += kCompute) {\n";
-    o << "      const uint32_t G = uint32_t(g)" << (g.W == 2 ? " << 1" : "") << ";\n";
+    int m = 0;
+    while ((1 << m) < g.groups / g.W) ++m;
+    const bool moved = m > 5 && !(g.lane_bits[0] == 0 && g.lane_bits[1] == 1 && g.lane_bits[2] == 2 &&
+                                  g.lane_bits[3] == 3 && g.lane_bits[4] == 4);
+    if (moved)
+        o << "      const uint32_t G = (" << lane_permute_expr(g, m) << ")" << (g.W == 2 ? " << 1" : "") << ";\n";
+    else
+        o << "      const uint32_t G = uint32_t(g)" << (g.W == 2 ? " << 1" : "") << ";\n";
     o << "      const uint32_t base =";
     for (int i = 0; i <= g.U; ++i) o << (i ? " |" : "") << " ((G << " << i << ") & " << b.dep[i] << "u)";
     if (pk) o << ";\n      lsg::F2 v[" << g.n << "];\n";
@@ -378,6 +528,13 @@ std::string pass_source(const Plan& plan, size_t pi, int precision, int elem_byt
         gens.push_back(g);
     }
     gens.insert(gens.end(), held.begin(), held.end());
+    {
+        const char* env = getenv("LSG_LANE_BITS");  // 0: lanes drive the lowest index bits (diagnostics)
+        if (!(env && env[0] == '0')) {
+            const uint32_t tile_mask = pd.K >= 32 ? ~0u : ((1u << pd.K) - 1u);
+            for (BlockGen& g : gens) choose_lane_bits(g, tile_mask, sw);
+        }
+    }
     std::ostringstream o;
     o << "struct Body" << pi << " {\n  static __device__ __forceinline__ void run(" << T << "* tile, const " << T
       << "* __restrict__ data, long long member) {\n";
