@@ -337,6 +337,39 @@ def test_packed_pair_source_compiles(monkeypatch):
     assert "rp_" not in _lib.specialized_source(14, _lib.C64, 1, sv)
 
 
+def test_fused_blocks_and_lane_bits_in_specialized_source(monkeypatch):
+    """Whole-block fusion gives complex programs dense block operators (rb_denseb), never real
+    ones; the lane-bit choice moves group-index bits in some real32 blocks; both compile."""
+    from lucivant_sim_gb300.qasm import parse
+
+    sv = engine.sv_oplist(parse(wl.brickwork(14, 12, seed=5, measure=False)))
+    fused = _lib.specialized_source(14, _lib.C64, 1, sv, compile=True)
+    assert "rb_denseb<lsg::Cx<float>" in fused
+    monkeypatch.setenv("LSG_FUSE_BLOCKS", "0")
+    assert "rb_denseb" not in _lib.specialized_source(14, _lib.C64, 1, sv)
+    monkeypatch.delenv("LSG_FUSE_BLOCKS")
+    c = parse(wl.brickwork(12, 12, seed=7, measure=False))
+    ptm = engine.ptm_oplist(c, wl.dm_noise_instances(2, seed=7))
+    chosen = _lib.specialized_source(24, _lib.R32, 2, ptm, compile=True)
+    assert "rb_denseb" not in chosen
+    moved = re.compile(r"const uint32_t G = \(+uint32_t\(g\) >>")
+    assert moved.search(chosen)
+    monkeypatch.setenv("LSG_LANE_BITS", "0")
+    plain = _lib.specialized_source(24, _lib.R32, 2, ptm)
+    assert not moved.search(plain)
+    # the same arithmetic: only the group enumeration differs
+    calls = re.compile(r"r[bp]_\w+<[^>]*>\([^;]*;")
+    assert calls.findall(plain) == calls.findall(chosen)
+
+
+def test_new_entry_points_refuse_bad_arguments_before_any_device_call():
+    lib = _lib.library()
+    assert lib.lsg_programs_run_ragged(0, None, None, None, None) == _lib.LSG_E_ARG
+    assert lib.lsg_program_set_data(None, None, None, 0, None, 0) == _lib.LSG_E_ARG
+    assert lib.lsg_program_graph_run(None, None, 0) == _lib.LSG_E_ARG
+    assert b"null" in lib.lsg_last_error() or b"bad" in lib.lsg_last_error()
+
+
 def test_format_bits_many_matches_format_bits():
     from lucivant_sim_gb300.circuit import format_bits, format_bits_many
 
