@@ -26,7 +26,7 @@ import numpy as np
 from numpy.typing import NDArray
 
 from lucivant_sim_gb300 import _lib, engine
-from lucivant_sim_gb300.circuit import Circuit, final_measurements, format_bits, format_bits_bytes
+from lucivant_sim_gb300.circuit import Circuit, ColumnarCircuit, final_measurements, format_bits, format_bits_bytes
 from lucivant_sim_gb300.clifford import clifford_problem
 from lucivant_sim_gb300.engine import MAX_DENSITY_QUBITS, SimulationError, pauli_masks
 from lucivant_sim_gb300.qasm import load, parse
@@ -59,7 +59,8 @@ def to_circuit(program: Any, params: Mapping[str, float] | None = None) -> Any:
         return load(Path(program), params)
     if isinstance(program, str):
         return parse(program, params)
-    if hasattr(program, "operations") and hasattr(program, "num_qubits"):
+    # a columnar circuit builds its operation objects only when asked: never just to recognise it
+    if isinstance(program, (Circuit, ColumnarCircuit)) or (hasattr(program, "operations") and hasattr(program, "num_qubits")):
         if params:
             raise ValueError("params apply to OpenQASM source, not to an already-built Circuit")
         return program
