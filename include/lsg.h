@@ -134,7 +134,7 @@ int lsg_program_run_from_basis(lsg_program p, lsg_state s, int64_t index, float*
  * pair i's basis state (NULL: all 0). The launches go on register 0's stream after the earlier
  * work of every register's stream, and later work on any of the registers goes after them; the
  * call does not wait (lsg_state_sync on a register waits and reports device errors). A register
- * may appear once. With step_ms non-NULL the call waits and step_ms gets each launch's device
+ * may appear once; a program more than once only with the same basis index. With step_ms non-NULL the call waits and step_ms gets each launch's device
  * time (as many entries as the longest program has passes). Each register's result equals its
  * lsg_program_run_from_basis alone. No counterpart in the reference, which runs one circuit per
  * call (simulator.py:229-251). */

@@ -1650,8 +1650,12 @@ int lsg_programs_run_ragged(int32_t count, const lsg_program* programs, const ls
         if (!programs[i] || !states[i]) return fail(LSG_E_ARG, "lsg_programs_run_ragged: null program or register %d", i);
         if (states[i]->precision != precision)
             return fail(LSG_E_ARG, "lsg_programs_run_ragged: register %d has another precision than register 0", i);
-        for (int32_t j = 0; j < i; ++j)
+        for (int32_t j = 0; j < i; ++j) {
             if (states[j] == states[i]) return fail(LSG_E_ARG, "lsg_programs_run_ragged: register %d appears twice", i);
+            // one program's basis passes live in its device memory: shared only by equal indices
+            if (programs[j] == programs[i] && !states[i]->real() && (index ? index[i] != index[j] : false))
+                return fail(LSG_E_ARG, "lsg_programs_run_ragged: program %d appears again with another basis index", i);
+        }
     }
     cudaStream_t st = states[0]->stream;
     std::vector<std::pair<lsg_program_s*, lsg_state_s*>> ragged;

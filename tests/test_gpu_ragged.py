@@ -96,6 +96,11 @@ def test_ragged_refuses_mixed_precisions_and_repeated_registers():
                 _lib.run_ragged([(pa, a), (pb, b)])
             with pytest.raises(ValueError, match="appears twice"):
                 _lib.run_ragged([(pa, a), (pa, a)])
+            with _lib.Register(4, _lib.C64) as a2:
+                with pytest.raises(ValueError, match="another basis index"):
+                    _lib.run_ragged([(pa, a), (pa, a2)], index=[0, 3])
+                _lib.run_ragged([(pa, a), (pa, a2)], index=[2, 2])  # one program, two registers
+                assert np.array_equal(a.download(), a2.download())
         finally:
             pa.free()
             pb.free()
