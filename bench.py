@@ -66,7 +66,7 @@ def parse_args() -> argparse.Namespace:
                     "stabilizer 2048q x 1000 layers x 1000 shots")  # fmt: skip
     ap.add_argument("--jobs", type=int, default=400, help="serve: jobs in the served mix")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: offered arrivals per second")
-    ap.add_argument("--serve-workers", type=int, default=8, help="serve: device worker slots")
+    ap.add_argument("--serve-workers", type=int, default=16, help="serve: device worker slots")
     return ap.parse_args()
 
 

@@ -281,7 +281,7 @@ class _Waiting:
 class Server:
     """Continuous-batching server: submit jobs, get futures."""
 
-    def __init__(self, precision: str = "c64", workers: int = 8, prep_workers: int | None = None,
+    def __init__(self, precision: str = "c64", workers: int = 16, prep_workers: int | None = None,
                  memory_fraction: float = 0.6, memory_bytes: int | None = None, group_max: int = 16) -> None:  # fmt: skip
         _lib.ensure_device()
         self.precision = engine.precision_code(precision)
