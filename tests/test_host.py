@@ -870,6 +870,21 @@ def test_jobs_of_one_structure_combine_into_one_table():
             assert (t0[i]["kind"], t0[i]["nbits"], tuple(t0[i]["bits"])) == (table[i]["kind"], table[i]["nbits"], tuple(table[i]["bits"]))
 
 
+def test_run_takes_a_columnar_circuit_without_building_its_operations(monkeypatch):
+    """ls.run recognises a columnar circuit as a circuit without asking for its operation objects
+    (4.1 M of them at the 2048-qubit config), and the stabilizer choice reads its columns."""
+    from lucivant_sim_gb300 import circuit as circ, simulator
+
+    col = wl.clifford_layers_circuit(64, 5, seed=1)
+
+    def refuse(self):
+        raise AssertionError("operations built")
+
+    monkeypatch.setattr(circ.ColumnarCircuit, "operations", property(refuse))
+    assert simulator.to_circuit(col) is col
+    assert simulator.choose_method(col, wl.stabilizer_noise(1e-3), "automatic") == "stabilizer"
+
+
 def test_columnar_clifford_circuit_is_the_parsed_circuit():
     """The wide Clifford workload held as arrays is the circuit its OpenQASM text parses to
     (digest, operations, final measurements), and its gate columns give the stabilizer encoder
