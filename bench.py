@@ -574,6 +574,27 @@ def gb300_arm(args: argparse.Namespace) -> None:
     plain.free()
     plain_cps = world / plain_s
 
+    # and in Orrery's own form: the complex128 vectorised density matrix (superoperators on 2n bits)
+    os.environ["LSG_DM_FORM"] = "superop"
+    try:
+        sup = DensityBatch(circuit, noises[:1], precision="c128")
+    finally:
+        del os.environ["LSG_DM_FORM"]
+    for _ in range(2):
+        sup.evolve()
+        sup.expectations(labels)
+        p_sup = sup.probabilities()
+    sup.reg.sync()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sup.evolve()
+        e_sup = sup.expectations(labels)
+        p_sup = sup.probabilities()
+    sup.reg.sync()
+    sup_s = (time.perf_counter() - t0) / reps
+    sup_form = sup.form
+    sup.free()
+
     # the same instances in the other registers beside it: real32 (the complex64 request) and
     # double-float pairs (FP64-level accuracy from FP32 arithmetic)
     def beside(prec: str, dtype: str, what: str) -> dict:
@@ -589,6 +610,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
             "fused_passes": bx.program.passes,
             "autotune": _tune_summary(bx.tune),
             "speedup_vs_plain_c128": cpsx / plain_cps,
+            "speedup_vs_plain_c128_superop": cpsx * sup_s / world,
             "speedup_vs_batched_headline": cpsx / cps,
             "roofline": dict(roofx["hbm"], kernel=f"lsg_pass_0..{bx.program.passes - 1} ({what})",
                              traffic=(lambda t: sum(t) / len(t) if t else None)(ncu_traffic(prec)),
@@ -660,6 +682,15 @@ def gb300_arm(args: argparse.Namespace) -> None:
                 "what": "one instance (instance 0) per run, real64 Pauli-transfer register, interpreted passes",
                 "probability_max_abs_vs_batched": float(np.max(np.abs(p_ref[0] - probs0[0]))),
                 "expectation_max_abs_vs_batched": float(np.max(np.abs(e_ref[:, 0] - exps0[:, 0]))),
+            },
+            "plain_c128_superop": {
+                "circuits_per_s": world / sup_s,
+                "ms_per_circuit": 1000 * sup_s,
+                "speedup_of_batched": cps * sup_s / world,
+                "what": f"one instance (instance 0) per run, complex128 vectorised density matrix ({sup_form}: "
+                        "Orrery's form), interpreted passes",
+                "probability_max_abs_vs_batched": float(np.max(np.abs(p_sup[0] - probs0[0]))),
+                "expectation_max_abs_vs_batched": float(np.max(np.abs(e_sup[:, 0] - exps0[:, 0]))),
             },
             "roofline": roofline,
             "per_pass": roof["per_pass"],
