@@ -15,7 +15,7 @@ from typing import Any
 import numpy as np
 
 from lucivant_sim_gb300 import _lib
-from lucivant_sim_gb300._lib import SimulationError, check, library, ptr
+from lucivant_sim_gb300._lib import SimulationError, check, library
 from lucivant_sim_gb300.clifford import (
     GateColumns,
     all_gates,
