@@ -322,6 +322,14 @@ int lsg_tab_download(lsg_tab t, uint8_t* x, uint8_t* z, uint8_t* r);
 /* Tableau.support (stabilizer.py:333-365): x0 (m bytes) and the basis (rank x m bytes, may be
  * NULL) of the outcomes on `qubits`. */
 int lsg_tab_support(lsg_tab t, const int32_t* qubits, int32_t m, uint8_t* x0, uint8_t* basis, int32_t* rank);
+/* Gate records of a circuit held as arrays (host only, no device): gate i is of kind kind[i] (one
+ * distinct gate each; kind_code / kind_nq / kind_noise per kind, as the encoder gives them for
+ * that kind's gates) on qubits[3i .. 3i + arity[i]) (arity 1..3; the other slots are written 0).
+ * The per-gate loop of the encoder behind Tableau gates and _frames (stabilizer.py:224-264,
+ * :514-594) for the columnar form of a wide circuit. */
+int lsg_cgates_from_kinds(int64_t n, const int64_t* kind, int32_t nkinds, const int16_t* kind_code,
+                          const int16_t* kind_nq, const int16_t* kind_noise, const int64_t* qubits, const int64_t* arity,
+                          lsg_cgate* out);
 /* _frames (stabilizer.py:514-563) plus _count's readout flips (:622-643): the noisy static
  * circuit's Pauli frames over `shots`, drawing from the PCG64 generator state `rng_state`
  * (state hi, state lo, inc hi, inc lo; no uint32 buffered) in Orrery's order: the frame bits, one

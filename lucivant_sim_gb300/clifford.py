@@ -196,6 +196,7 @@ class GateColumns:
         )
         self._qmat = np.asarray(qubits, dtype=np.int64)
         self._kind_names = kind_names
+        self._kind_name_id = kind_name_id
         return self
 
     @cached_property
@@ -228,13 +229,13 @@ class GateColumns:
     def name_arity_groups(self) -> tuple[np.ndarray, np.ndarray]:
         """Gates grouped by (name, arity), the key noise rules by gate name depend on: (index of
         each group's first gate, per gate its group), groups in ascending key order."""
-        key = self.name_ids * 64 + self.arity
         if hasattr(self, "_qmat"):  # from the distinct gates: key per kind, then per gate
             first_k, inv_k = self.matrix_groups
-            kind_key = key[first_k]
+            kind_key = self._kind_name_id[self.matrix_ids[first_k]] * 64 + self.arity[first_k]
             uk, rank = np.unique(kind_key, return_inverse=True)
             first = np.array([int(first_k[rank == r].min()) for r in range(uk.size)], dtype=np.int64)
             return first, rank[inv_k]
+        key = self.name_ids * 64 + self.arity
         _u, first, inv = np.unique(key, return_index=True, return_inverse=True)
         return first, inv
 

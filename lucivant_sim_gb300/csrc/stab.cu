@@ -834,6 +834,38 @@ int lsg_pcg_raw(const uint64_t* state, uint64_t index, uint64_t* out) {
     return LSG_OK;
 }
 
+int lsg_cgates_from_kinds(int64_t n, const int64_t* kind, int32_t nkinds, const int16_t* kind_code,
+                          const int16_t* kind_nq, const int16_t* kind_noise, const int64_t* qubits, const int64_t* arity,
+                          lsg_cgate* out) {
+    clear_error();
+    if (n < 0 || nkinds < 0 ||
+        (n > 0 && (!kind || !kind_code || !kind_nq || !kind_noise || !qubits || !arity || !out)))
+        return fail(LSG_E_ARG, "lsg_cgates_from_kinds: bad arguments");
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t k = kind[i], a = arity[i];
+        if (k < 0 || k >= nkinds || a < 1 || a > 3)
+            return fail(LSG_E_ARG, "lsg_cgates_from_kinds: gate %lld has kind %lld and %lld qubits", (long long)i,
+                        (long long)k, (long long)a);
+        int16_t q[3] = {0, 0, 0};
+        for (int64_t j = 0; j < a; ++j) {
+            const int64_t v = qubits[3 * i + j];
+            if (v < 0 || v > 32767)
+                return fail(LSG_E_ARG, "lsg_cgates_from_kinds: gate %lld names qubit %lld", (long long)i, (long long)v);
+            q[j] = (int16_t)v;
+        }
+        lsg_cgate g;
+        g.code = kind_code[k];
+        g.noise = kind_noise[k];
+        g.a = q[0];
+        g.b = q[1];
+        g.c = q[2];
+        g.nq = kind_nq[k];
+        g.pad = 0;
+        out[i] = g;
+    }
+    return LSG_OK;
+}
+
 int lsg_tab_create(int n, lsg_tab* out) {
     clear_error();
     if (!out) return fail(LSG_E_ARG, "null output");

@@ -48,6 +48,8 @@ _SIGS = {
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                   C.POINTER(C.c_int64)]),
     "lsg_pcg_raw": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "lsg_cgates_from_kinds": (C.c_int, [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]),
 }  # fmt: skip
 
 
@@ -148,6 +150,28 @@ class Encoder:
         cols = GateColumns(gates) if cols is None else cols
         first, inv = cols.matrix_groups
         codes = np.array([self.gate_code(gates[int(f)]) for f in first], dtype=np.int32).reshape(-1, 2)
+        qmat = getattr(cols, "_qmat", None)
+        if qmat is not None and (not with_noise or self.by_arity):
+            # a columnar circuit: per kind (its distinct gates) the code, width and noise code, the
+            # records filled by the library (same lookups in the same order as below)
+            kind = np.ascontiguousarray(cols.matrix_ids, dtype=np.int64)
+            nkinds = int(kind.max()) + 1
+            group_kind = kind[first]
+            kcode = np.zeros(nkinds, dtype=np.int16)
+            knq = np.zeros(nkinds, dtype=np.int16)
+            knoise = np.full(nkinds, -1, dtype=np.int16)
+            kcode[group_kind], knq[group_kind] = codes[:, 0], codes[:, 1]
+            if with_noise:
+                kfirst, kinv = cols.name_arity_groups
+                idx = np.array([self.noise_code(gates[int(f)]) for f in kfirst], dtype=np.int16)
+                knoise[group_kind] = idx[kinv[first]]
+            q = np.ascontiguousarray(qmat, dtype=np.int64)
+            if q.ndim != 2 or q.shape[1] < 3:
+                q = np.ascontiguousarray(np.pad(q.reshape(n, -1), ((0, 0), (0, 3 - q.reshape(n, -1).shape[1]))))
+            arity = np.ascontiguousarray(cols.arity, dtype=np.int64)
+            check(_lib_stab().lsg_cgates_from_kinds(n, _p(kind), nkinds, _p(kcode), _p(knq), _p(knoise), _p(q),
+                                                    _p(arity), _p(out)))  # fmt: skip
+            return out
         out["code"], out["nq"] = codes[inv, 0], codes[inv, 1]
         out["a"], out["b"], out["c"] = cols.position(0), cols.position(1), cols.position(2)
         if not with_noise:

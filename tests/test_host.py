@@ -870,6 +870,31 @@ def test_jobs_of_one_structure_combine_into_one_table():
             assert (t0[i]["kind"], t0[i]["nbits"], tuple(t0[i]["bits"])) == (table[i]["kind"], table[i]["nbits"], tuple(table[i]["bits"]))
 
 
+def test_cgates_from_kinds_fills_and_refuses():
+    """The library's gate-record filler for columnar circuits: per-kind fields, qubits of the
+    used slots, zeros elsewhere; bad kinds, widths and qubits refused (host only)."""
+    from lucivant_sim_gb300 import stabilizer as st
+
+    lib = st._lib_stab()
+    kind = np.array([1, 0, 1], dtype=np.int64)
+    code = np.array([5, 7], dtype=np.int16)
+    nq = np.array([1, 2], dtype=np.int16)
+    noise = np.array([-1, 3], dtype=np.int16)
+    q = np.array([[4, -1, -1], [2, 9, -1], [0, -1, -1]], dtype=np.int64)
+    ar = np.array([1, 2, 1], dtype=np.int64)
+    out = np.zeros(3, dtype=st.CGATE)
+    assert lib.lsg_cgates_from_kinds(3, kind.ctypes.data, 2, code.ctypes.data, nq.ctypes.data, noise.ctypes.data,
+                                     q.ctypes.data, ar.ctypes.data, out.ctypes.data) == 0  # fmt: skip
+    assert out["code"].tolist() == [7, 5, 7] and out["nq"].tolist() == [2, 1, 2] and out["noise"].tolist() == [3, -1, 3]
+    assert out["a"].tolist() == [4, 2, 0] and out["b"].tolist() == [0, 9, 0] and out["c"].tolist() == [0, 0, 0]
+    for bad_kind, bad_ar, bad_q in ((2, 1, 4), (0, 4, 4), (0, 1, -3)):
+        k2, a2, q2 = kind.copy(), ar.copy(), q.copy()
+        k2[0], a2[0], q2[0, 0] = bad_kind, bad_ar, bad_q
+        rc = lib.lsg_cgates_from_kinds(3, k2.ctypes.data, 2, code.ctypes.data, nq.ctypes.data, noise.ctypes.data,
+                                       q2.ctypes.data, a2.ctypes.data, out.ctypes.data)  # fmt: skip
+        assert rc == _lib.LSG_E_ARG
+
+
 def test_run_takes_a_columnar_circuit_without_building_its_operations(monkeypatch):
     """ls.run recognises a columnar circuit as a circuit without asking for its operation objects
     (4.1 M of them at the 2048-qubit config), and the stabilizer choice reads its columns."""
