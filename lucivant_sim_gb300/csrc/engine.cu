@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "jit.cuh"
+#include "kernels.cuh"
 #include "program.cuh"
 #include "tile.cuh"
 
@@ -646,7 +647,7 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
     }
     if (pipe) {
         // each pass gets the shared memory its own operators need: short passes fit more CTAs per SM
-        auto kern = k_tile_pipe<T>;
+        const void* kern = PassKernels<T>::pipe();
         LSG_CHECK(allow_smem(kern));
         size_t last_smem = 0;
         int64_t grid = 1;
@@ -660,19 +661,19 @@ static int launch_passes(lsg_program_s* p, lsg_state_s* s, cudaEvent_t* marks, c
             }
             grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1)));
             if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
-            kern<<<(unsigned)grid, kPipeThreads, smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
-                                                                    tpm[i], total, status, ctx);
+            PassKernels<T>::launch_pipe((unsigned)grid, smem, s->stream, state, s->elems, pd_dev + i, ops_dev, blk_dev,
+                                        pool_dev, tpm[i], total, status, ctx);
         }
     } else {
-        auto kern = k_tile_pass<T>;
+        const void* kern = PassKernels<T>::pass();
         LSG_CHECK(allow_smem(kern));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, p->smem);
         for (size_t i = 0; i < p->plan.passes.size(); ++i) {
             const int64_t total = tpm[i] * s->batch;
             const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)sms * std::max(per_sm, 1) * 4));
             if (marks) LSG_CUDA(cudaEventRecord(marks[i], s->stream));
-            kern<<<(unsigned)grid, 256, p->smem, s->stream>>>(state, s->elems, pd_dev + i, ops_dev, blk_dev, pool_dev,
-                                                              tpm[i], total, status, ctx);
+            PassKernels<T>::launch_pass((unsigned)grid, p->smem, s->stream, state, s->elems, pd_dev + i, ops_dev, blk_dev,
+                                        pool_dev, tpm[i], total, status, ctx);
         }
     }
     if (marks) LSG_CUDA(cudaEventRecord(marks[p->plan.passes.size()], s->stream));
@@ -1171,7 +1172,7 @@ static int launch_ragged(const std::vector<std::pair<lsg_program_s*, lsg_state_s
     LSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int* status = device_status();
     if (!status) return fail(LSG_E_CUDA, "cannot allocate the device status word");
-    auto kern = k_tile_pipe_ragged<T>;
+    const void* kern = PassKernels<T>::ragged();
     LSG_CHECK(allow_smem(kern));
     std::vector<RaggedJob> table;
     std::vector<size_t> first(steps), count(steps), smem(steps);
@@ -1229,7 +1230,7 @@ static int launch_ragged(const std::vector<std::pair<lsg_program_s*, lsg_state_s
     }
     for (size_t k = 0; k < steps; ++k) {
         if (ms) LSG_CUDA(cudaEventRecord(marks[k], st));
-        kern<<<grid[k], kPipeThreads, smem[k], st>>>(dtab + first[k], (int)count[k], status);
+        PassKernels<T>::launch_ragged(grid[k], smem[k], st, dtab + first[k], (int)count[k], status);
     }
     if (ms) LSG_CUDA(cudaEventRecord(marks[steps], st));
     LSG_CUDA(cudaGetLastError());
