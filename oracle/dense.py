@@ -342,7 +342,7 @@ def exact_outcomes(circuit: Any, noise: Any = None) -> dict[int, float]:
 
 def choose(circuit: Any, noise: Any, method: str) -> str:
     """Method choice (``simulator.py:157-193``) for the four native methods."""
-    from lucivant_sim_gb300.clifford import clifford_problem
+    from oracle.clifford import clifford_problem
 
     gate_noise = noise is not None and noise.has_gate_errors()
     dynamic = circuit.is_dynamic()
@@ -432,10 +432,15 @@ def pauli_masks(label: str) -> tuple[int, int]:
     return xm, zm
 
 
+_PAULI = {
+    "X": np.array([[0, 1], [1, 0]], dtype=np.complex128),
+    "Y": np.array([[0, -1j], [1j, 0]], dtype=np.complex128),
+    "Z": np.array([[1, 0], [0, -1]], dtype=np.complex128),
+}
+
+
 def expectation(circuit: Any, observable: Any, noise: Any = None) -> float:
     """Σ w ⟨P⟩ (``simulator.py:489-527``): ket copy with Paulis applied, or Pauli-left trace."""
-    from lucivant_sim_gb300.gates import PAULIS
-
     terms = {observable: 1.0} if isinstance(observable, str) else dict(observable)
     n = circuit.num_qubits
     total = 0.0
@@ -446,7 +451,7 @@ def expectation(circuit: Any, observable: Any, noise: Any = None) -> float:
             probe = rho
             for q, letter in enumerate(reversed(label.upper())):
                 if letter != "I":
-                    probe = apply_bits(probe, 2 * n, PAULIS[letter], [n + q])
+                    probe = apply_bits(probe, 2 * n, _PAULI[letter], [n + q])
             total += w * float(np.trace(probe.reshape(d, d)).real)
         return total
     ket = evolve_sv(circuit)
@@ -454,6 +459,6 @@ def expectation(circuit: Any, observable: Any, noise: Any = None) -> float:
         probe = ket.copy()
         for q, letter in enumerate(reversed(label.upper())):
             if letter != "I":
-                probe = apply_bits(probe, n, PAULIS[letter], [q])
+                probe = apply_bits(probe, n, _PAULI[letter], [q])
         total += w * float(np.vdot(ket, probe).real)
     return total

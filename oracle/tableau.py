@@ -12,7 +12,8 @@ from typing import Any
 import numpy as np
 from numpy.typing import NDArray
 
-from lucivant_sim_gb300.clifford import clifford_map, clifford_problem, kind_of, pauli_noise
+from oracle.clifford import clifford_problem, kind_of, pauli_noise
+from oracle.clifford import conjugation_table as clifford_map
 
 U8 = NDArray[np.uint8]
 

@@ -2,8 +2,8 @@
 made by ``tests/golden/make_golden_configs.py`` running Orrery 0.3.0 itself).
 
 No device is used: these check that the benchmark builds the same noise models and circuits
-Orrery ran, that the host's Clifford conjugation tables (shared by the engine and the oracle)
-are Orrery's for every gate name, and that the oracle reproduces Orrery's per-shot trajectory
+Orrery ran, that the host's Clifford conjugation tables (the engine's) and the oracle's own
+restatement of them are Orrery's for every gate name, and that the oracle reproduces Orrery's per-shot trajectory
 draws on the 18-qubit, 16-round workload.
 """
 
@@ -21,6 +21,7 @@ from lucivant_sim_gb300 import workloads as wl
 from lucivant_sim_gb300.clifford import clifford_map, kind_of
 from lucivant_sim_gb300.gates import GATES
 from lucivant_sim_gb300.noise import NoiseModel
+from oracle import clifford as oracle_clifford
 from oracle import dense, tableau
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
@@ -76,6 +77,19 @@ def test_clifford_tables_are_orreys_for_every_gate(cfg, cfg_arrays):
         assert np.array_equal(cmap.bits, cfg_arrays[f"cmap_bits::{key}"]), key
         assert np.array_equal(cmap.sign, cfg_arrays[f"cmap_sign::{key}"]), key
         assert kind_of(cmap) == info["kind"], key
+
+
+def test_oracle_clifford_tables_are_orreys_for_every_gate(cfg, cfg_arrays):
+    """The oracle derives its tables on its own (the image Pauli read off the matrix, not
+    projected on the Pauli basis); they too equal Orrery's, kind included."""
+    maps = cfg["clifford_maps"]["maps"]
+    for key, info in maps.items():
+        m = np.asarray(GATES[info["name"]].build(*info["params"]), dtype=np.complex128)
+        table = oracle_clifford.conjugation_table(m)
+        assert table is not None, key
+        assert np.array_equal(table.bits, cfg_arrays[f"cmap_bits::{key}"]), key
+        assert np.array_equal(table.sign, cfg_arrays[f"cmap_sign::{key}"]), key
+        assert oracle_clifford.kind_of(table) == info["kind"], key
 
 
 def test_oracle_tableau_matches_orrery_over_every_clifford_gate(cfg, cfg_arrays):

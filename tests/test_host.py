@@ -590,16 +590,54 @@ def test_public_header_is_plain_c(tmp_path):
 
 
 def _clifford_problem_walk(circuit, noise):
-    """The Clifford check as a plain walk over the gates in order (the first problem found)."""
-    from lucivant_sim_gb300.clifford import all_gates, clifford_map, pauli_noise
+    """The Clifford check as a plain walk over the gates in order (the first problem found), by
+    the oracle's own tables."""
+    from oracle.clifford import clifford_problem
 
-    for g in all_gates(circuit.operations):
-        if clifford_map(g.matrix) is None:
-            return f"{g.name} on qubits {list(g.qubits)} isn't a Clifford gate"
-        ch = noise.gate_error(g.name, g.qubits) if noise else None
-        if ch is not None and pauli_noise(ch) is None:
-            return f"the {ch.name} noise after {g.name} isn't a Pauli channel"
-    return None
+    return clifford_problem(circuit, noise)
+
+
+def test_oracle_pauli_tables_and_branches_equal_the_engines():
+    """The oracle's Clifford tables and Pauli branches (derived its own way) equal the host's for
+    products of random Clifford gates on one to three qubits, refuse the same non-Clifford gates,
+    and give the same branches and cumulative probabilities for Pauli channels."""
+    from lucivant_sim_gb300.clifford import clifford_map, kind_of, pauli_noise
+    from lucivant_sim_gb300.gates import GATES
+    from lucivant_sim_gb300.noise import amplitude_damping, pauli_channel
+    from oracle import clifford as oc
+
+    rng = np.random.default_rng(5)
+    names = [n for n in ("h", "s", "sdg", "x", "y", "z", "sx", "cx", "cz", "swap", "iswap", "ecr") if n in GATES]
+    for trial in range(60):
+        k = 1 + trial % 3
+        u = np.eye(1 << k, dtype=np.complex128)
+        for _ in range(5):
+            name = names[int(rng.integers(len(names)))]
+            spec = GATES[name]
+            if spec.qubits > k:
+                continue
+            qs = [int(q) for q in rng.permutation(k)[: spec.qubits]]
+            m = np.asarray(spec.build(), dtype=np.complex128)
+            # embed on qubits qs (first qubit most significant) by permuting a kron with identity
+            full = np.kron(m, np.eye(1 << (k - spec.qubits)))
+            order = qs + [q for q in range(k) if q not in qs]
+            t = full.reshape([2] * (2 * k))
+            inv = np.argsort(order)
+            t = t.transpose(list(inv) + [k + i for i in inv])
+            u = t.reshape(1 << k, 1 << k) @ u
+        mine, theirs = oc.conjugation_table(u), clifford_map(u)
+        assert mine is not None and theirs is not None
+        assert np.array_equal(mine.bits, theirs.bits) and np.array_equal(mine.sign, theirs.sign)
+        assert oc.kind_of(mine) == kind_of(theirs)
+    for name, params in (("t", ()), ("rx", (0.3,)), ("ccx", ()), ("u3", (0.1, 0.2, 0.3))):
+        m = np.asarray(GATES[name].build(*params), dtype=np.complex128)
+        assert oc.conjugation_table(m) is None and clifford_map(m) is None, name
+    for ch in (depolarizing(1e-3), depolarizing(0.02, 2), pauli_channel({"X": 0.1, "Z": 0.05}),
+               pauli_channel({"XY": 0.2, "ZI": 0.1})):
+        a, b = oc.pauli_noise(ch), pauli_noise(ch)
+        assert a is not None and b is not None
+        assert a.branches == b.branches and np.array_equal(a.cumulative, b.cumulative)
+    assert oc.pauli_noise(amplitude_damping(0.1)) is None and pauli_noise(amplitude_damping(0.1)) is None
 
 
 def test_clifford_check_and_encoder_columns():
