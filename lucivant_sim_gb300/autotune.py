@@ -42,10 +42,30 @@ def cache_path() -> Path:
     return Path(env) if env else Path.home() / ".cache" / "lucivant_sim_gb300" / "tune.json"
 
 
+_identity: str | None = None
+
+
+def engine_identity() -> str:
+    """The build and device a timing belongs to: the engine library's contents, its ABI version
+    and the device's memory size. A choice timed with another build or on another GPU model is
+    searched again rather than reused."""
+    global _identity
+    if _identity is None:
+        h = hashlib.sha256()
+        try:
+            h.update(_lib.LIB_PATH.read_bytes())
+        except OSError:
+            pass
+        h.update(f"{_lib.library().lsg_version()}:{_lib.mem_info()[1]}".encode())
+        _identity = h.hexdigest()[:16]
+    return _identity
+
+
 def shape_key(reg: _lib.Register, ops: _lib.OpList) -> str:
-    """The program shape a choice is kept for: register and operator structure, not values."""
+    """The program shape a choice is kept for: register and operator structure, not values, on
+    this engine build and device (``engine_identity``)."""
     h = hashlib.sha256()
-    h.update(f"{reg.nbits}:{reg.precision}:{reg.batch}:".encode())
+    h.update(f"{engine_identity()}:{reg.nbits}:{reg.precision}:{reg.batch}:".encode())
     for kind, nb, bits, _at, stride in ops.rows:
         h.update(f"{kind},{nb},{bits},{int(stride > 0)};".encode())
     return h.hexdigest()[:32]
@@ -80,7 +100,7 @@ def _save(key: str, entry: dict[str, Any]) -> None:
         path.parent.mkdir(parents=True, exist_ok=True)
         data = _load()
         data[key] = entry
-        tmp = path.with_suffix(".tmp")
+        tmp = path.with_suffix(f".{os.getpid()}.tmp")  # concurrent processes never share one
         tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
         tmp.replace(path)
     except OSError:
@@ -102,7 +122,11 @@ def tuned_program(reg: _lib.Register, ops: _lib.OpList, search: bool = True) -> 
                 _memory[key] = entry
     if entry is not None:
         opts = _lib.PlanOpts(**entry["opts"])
-        return _lib.Program(reg, ops, opts), dict(entry, cached=True)
+        try:
+            return _lib.Program(reg, ops, opts), dict(entry, cached=True)
+        except (ValueError, _lib.EngineError):  # a choice this build no longer plans: search again
+            with _lock:
+                _memory.pop(key, None)
     if not search:
         return _lib.Program(reg, ops), {"opts": None, "cached": False, "searched": False}
     timings: list[dict[str, Any]] = []

@@ -976,3 +976,53 @@ def test_columnar_clifford_circuit_is_the_parsed_circuit():
             e2 = st.Encoder(noise).encode(g2, noise is not None, c2)
             assert np.array_equal(e1, e2)
         assert [g.qubits for g in g1[:5]] == [g.qubits for g in g2[:5]] and len(g1) == len(g2)
+
+
+def test_autotuner_cache_is_per_build_and_survives_a_choice_that_no_longer_plans(tmp_path, monkeypatch):
+    """With a stand-in program (no device): the fastest candidate is kept in the file; an entry
+    whose choice a later build refuses is searched again instead of failing the run; another
+    build or device keys its choices apart."""
+    from types import SimpleNamespace
+
+    from lucivant_sim_gb300 import autotune
+
+    monkeypatch.setenv("LSG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_identity", "build-a")
+    monkeypatch.setattr(autotune, "_memory", {})
+    reg = SimpleNamespace(nbits=24, precision=_lib.R64, batch=4)
+    ops = SimpleNamespace(rows=[(0, 2, (0, 12), 0, 0), (2, 4, (0, 1, 12, 13), 16, 0)])
+
+    class FakeProgram:
+        refuse: set = set()
+
+        def __init__(self, reg, ops, opts=None):
+            key = None if opts is None else (opts.tile_bits, opts.ctas)
+            if key in FakeProgram.refuse:
+                raise ValueError("the plan does not fit")
+            self.key, self.passes, self.specialized = key, 3, True
+
+        def run_from_basis(self, reg, index, timed=False):
+            # larger tiles and fewer CTAs are faster here
+            return np.array([10.0 - self.key[0] * 0.5 + self.key[1] * 0.1])
+
+        def free(self):
+            pass
+
+    monkeypatch.setattr(_lib, "Program", FakeProgram)
+    prog, info = autotune.tuned_program(reg, ops)
+    assert not info["cached"] and len(info["candidates"]) == 4
+    best = prog.key
+    cands = [(c.tile_bits, c.ctas) for c in autotune.candidates(24, _lib.R64)]
+    assert best == (max(k for k, _ in cands), min(c for _, c in cands))
+    key_a = autotune.shape_key(reg, ops)
+    assert list(__import__("json").loads((tmp_path / "tune.json").read_text())) == [key_a]
+    autotune._memory.clear()  # a later process finds it in the file
+    prog, info = autotune.tuned_program(reg, ops)
+    assert info["cached"] and prog.key == best
+    autotune._memory.clear()
+    FakeProgram.refuse = {best}  # a later build refuses the kept choice: searched again
+    prog, info = autotune.tuned_program(reg, ops)
+    assert not info["cached"] and prog.key != best and prog.key is not None
+    monkeypatch.setattr(autotune, "_identity", "build-b")
+    assert autotune.shape_key(reg, ops) != key_a
+    assert not list(tmp_path.glob("*.tmp"))
