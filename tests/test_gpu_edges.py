@@ -68,3 +68,34 @@ def test_parameters_and_thresholded_probabilities():
     assert ls.probabilities(src, params={"t": 0.0}) == {"00": pytest.approx(1.0, abs=1e-12)}
     with pytest.raises(Exception):
         ls.statevector(src)  # the input is unbound
+
+
+def test_expectations_of_more_members_than_one_launch_takes():
+    """70,000 members (above the 65,535 a launch's grid y holds): lsg_expect_pauli splits them
+    into launches and every member's expectations equal a host computation from its amplitudes,
+    for a complex128 statevector register and a real Pauli-transfer register."""
+    from lucivant_sim_gb300 import _lib
+
+    members, n = 70_000, 3
+    rng = np.random.default_rng(11)
+    vec = rng.normal(size=(members, 1 << n)) + 1j * rng.normal(size=(members, 1 << n))
+    vec /= np.linalg.norm(vec, axis=1, keepdims=True)
+    xs, zs = [0, 1, 3, 5, 6], [1, 0, 3, 4, 6]
+    idx = np.arange(1 << n)
+    want = np.empty((len(xs), members))
+    for t, (x, z) in enumerate(zip(xs, zs, strict=True)):
+        sign = 1.0 - 2.0 * (np.array([bin(i & z).count("1") for i in idx]) & 1)
+        phase = 1j ** (bin(x & z).count("1") & 3)
+        want[t] = np.real(phase * np.sum(np.conj(vec[:, idx ^ x]) * vec * sign, axis=1))
+    with _lib.Register(n, _lib.C128, batch=members) as reg:
+        reg.upload(vec)
+        got = reg.expect(0, xs, zs)
+    assert got.shape == (len(xs), members)
+    assert np.max(np.abs(got - want)) < 1e-12
+    # Pauli-transfer members: each expectation is the coefficient at the term's digits
+    coef = rng.uniform(-1, 1, size=(members, 1 << (2 * n)))
+    digits = [(x << n) | z for x, z in zip(xs, zs, strict=True)]
+    with _lib.Register(2 * n, _lib.R64, batch=members) as reg:
+        reg.upload(coef)
+        got = reg.expect(n, xs, zs)
+    assert np.array_equal(got, coef[:, digits].T)
