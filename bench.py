@@ -235,17 +235,23 @@ def load_golden() -> dict:
         for m in GOLDEN_MEMBERS:
             name = f"cfg2_inst{m}"
             if name in cases and f"{name}_probs" in data.files:
-                out[m] = {"probs": data[f"{name}_probs"], "z": np.asarray(cases[name]["z"])}
+                out[m] = {"probs": data[f"{name}_probs"], "z": np.asarray(cases[name]["z"]),
+                          "noise_digest": cases[name].get("noise_digest")}
     return out
 
 
-def golden_errors(probs, exps, golden: dict) -> dict:
-    """Max-abs probability and <Z> errors and probability TVD against Orrery, per fixture member."""
+def golden_errors(probs, exps, golden: dict, noises: list) -> dict:
+    """Max-abs probability and <Z> errors and probability TVD against Orrery, per fixture member
+    whose noise model is the one Orrery ran (same digest): another instance count draws other
+    noise parameters, and those members are listed as not comparable."""
     import numpy as np
 
-    per = {}
+    per, other = {}, []
     for m, g in golden.items():
         if m >= probs.shape[0]:
+            continue
+        if g.get("noise_digest") != noises[m].digest():
+            other.append(m)
             continue
         per[str(m)] = {
             "max_abs_probability": float(np.max(np.abs(probs[m] - g["probs"]))),
@@ -253,7 +259,11 @@ def golden_errors(probs, exps, golden: dict) -> dict:
             "max_abs_z": float(np.max(np.abs(exps[:, m] - g["z"]))),
         }
     worst = {k: max(v[k] for v in per.values()) for k in ("max_abs_probability", "probability_tvd", "max_abs_z")} if per else {}
-    return {"members": per, "worst": worst, "against": "Orrery 0.3.0 run on the same instances (tests/golden/configs.*)"}
+    out = {"members": per, "worst": worst, "against": "Orrery 0.3.0 run on the same instances (tests/golden/configs.*)"}
+    if other:
+        out["not_comparable"] = {"members": other, "why": "other noise parameters than Orrery's run (the instance "
+                                 "count changes the seeded draws)"}
+    return out
 
 
 # ------------------------------------------------------------------------------ CPU legs
@@ -552,7 +562,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
     # reset, passes, expectations, probabilities (the Pauli-transfer register reduces every member
     # in one launch each; the complex form sums rows in a second launch and runs one per member)
     launches_per_step = 1 + passes + (2 if real else 2 + args.instances)
-    accuracy = golden_errors(run["probs"], run["exps"], golden)
+    accuracy = golden_errors(run["probs"], run["exps"], golden, noises)
     exps0, probs0 = run["exps"][:, :1].copy(), run["probs"][:1].copy()
     batch.free()
 
@@ -616,7 +626,7 @@ def gb300_arm(args: argparse.Namespace) -> None:
                              traffic=(lambda t: sum(t) / len(t) if t else None)(ncu_traffic(prec)),
                              heaviest_pass=roofx["heaviest_pass"], arith=roofx["arith"]),  # fmt: skip
             "per_pass": roofx["per_pass"],
-            "accuracy_vs_orrery": golden_errors(rx["probs"], rx["exps"], golden),
+            "accuracy_vs_orrery": golden_errors(rx["probs"], rx["exps"], golden, noises),
             "accuracy_vs_gpu_headline": {
                 "probability_tvd": 0.5 * float(np.abs(rx["probs"][0] - probs0[0]).sum()),
                 "max_probability_error": float(np.max(np.abs(rx["probs"][0] - probs0[0]))),
