@@ -451,6 +451,11 @@ def replay(jobs: list[dict], server: Server, realtime: bool = True) -> dict:
         "circuits_per_s": len(jobs) / elapsed,
         "p50_s": float(np.percentile(lat, 50)),
         "p99_s": float(np.percentile(lat, 99)),
-        "phases": {k: {"p50_s": float(np.nanpercentile(v, 50)), "p99_s": float(np.nanpercentile(v, 99)),
-                       "mean_s": float(np.nanmean(v))} for k, v in parts.items()},  # fmt: skip
+        "phases": {k: _phase_summary(v) for k, v in parts.items() if np.isfinite(v).any()},
     }
+
+
+def _phase_summary(v: np.ndarray) -> dict[str, float]:
+    """p50, p99 and mean of one phase's times over the jobs that report it."""
+    v = v[np.isfinite(v)]
+    return {"p50_s": float(np.percentile(v, 50)), "p99_s": float(np.percentile(v, 99)), "mean_s": float(v.mean())}
