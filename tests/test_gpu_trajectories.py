@@ -103,3 +103,34 @@ def test_kraus_channel_statistics_against_density_matrix():
     exact = dense.outcome_probabilities(ls.parse(src), noise)
     got = ls.run(src, shots=20000, seed=3, noise=noise, method="trajectories", trajectory_mode="batched").counts
     assert tvd_counts(got, {k: int(round(v * 1e6)) for k, v in exact.items()}) < 0.02
+
+
+def test_batched_mode_at_benchmark_size_agrees_with_serial():
+    """The benchmark's trajectory workload at full size (18 qubits, 16 rounds of mid-circuit
+    measurement, conditional X and reset, depolarising 1e-3 / 1e-2): 8192 batched complex64 shots
+    and 2048 serial complex128 shots (Orrery's draw order, identical to Orrery's shots for the
+    same seed) are samples of one distribution over the 256 classical records: two-sample
+    chi-square p > 1e-6 (records expected fewer than 5 times in either sample pooled)."""
+    from scipy.stats import chi2
+
+    c = ls.parse(wl.midcircuit(18, 16, seed=7))
+    noise = NoiseModel.uniform(single=1e-3, two=1e-2)
+    a, _ = trajectories.run_shots(c, 8192, noise, np.random.default_rng(3), _lib.C64, "batched")
+    b, _ = trajectories.run_shots(c, 2048, noise, np.random.default_rng(4), _lib.C128, "serial")
+    na, nb = sum(a.values()), sum(b.values())
+    assert (na, nb) == (8192, 2048)
+    stat, bins, pool = 0.0, 0, [0, 0, 0.0, 0.0]
+    for k in set(a) | set(b):
+        oa, ob = a.get(k, 0), b.get(k, 0)
+        share = (oa + ob) / (na + nb)
+        ea, eb = na * share, nb * share
+        if min(ea, eb) >= 5:
+            stat += (oa - ea) ** 2 / ea + (ob - eb) ** 2 / eb
+            bins += 1
+        else:
+            pool = [pool[0] + oa, pool[1] + ob, pool[2] + ea, pool[3] + eb]
+    if pool[2] > 0 and pool[3] > 0:
+        stat += (pool[0] - pool[2]) ** 2 / pool[2] + (pool[1] - pool[3]) ** 2 / pool[3]
+        bins += 1
+    assert bins >= 8
+    assert float(chi2.sf(stat, bins - 1)) > 1e-6
