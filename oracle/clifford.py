@@ -7,9 +7,9 @@ What it restates (``src/lucivant_sim/stabilizer.py``):
   convention as the reference: a Pauli's bits (x0, z0, x1, z1, ...) read as a binary number, first
   qubit most significant, Y = (1, 1); the matrix is rounded to 12 decimals first and a gate is
   refused (None) when an image is not ±1 times one Pauli to 1e-8.
-* ``kind_of``: the standard gates the reference gives named rules (``:121-145``).
+* ``kind_of``: the standard gates the reference gives named rules (``:122-147``).
 * ``pauli_noise``: a mixture channel as cumulative branch probabilities and Pauli bits
-  (``:148-187``), with the reference's arithmetic (cumulative sum, then divided by the total).
+  (``:150-184``), with the reference's arithmetic (cumulative sum, then divided by the total).
 * ``clifford_problem``: the reference's walk over the gates in order (``:446-467``).
 
 The derivation differs from the reference's (and from the product's): instead of projecting
@@ -28,8 +28,8 @@ from typing import Any
 import numpy as np
 from numpy.typing import NDArray
 
-MAX_QUBITS = 2048  # stabilizer.py:34
-MAX_GATE_QUBITS = 3  # stabilizer.py:35
+MAX_QUBITS = 2048  # stabilizer.py:37
+MAX_GATE_QUBITS = 3  # stabilizer.py:39
 _TOL = 1e-8
 
 
@@ -105,7 +105,8 @@ def _table_of(raw: bytes, k: int) -> Table | None:
 
 
 def conjugation_table(matrix: NDArray[np.complex128]) -> Table | None:
-    """The conjugation table of a gate matrix, or None when it is not Clifford (or too wide)."""
+    """The conjugation table of a gate matrix, or None when it is not Clifford (or too wide)
+    (``stabilizer.py:83-118``)."""
     k = matrix.shape[0].bit_length() - 1
     if not 0 < k <= MAX_GATE_QUBITS:
         return None
@@ -138,12 +139,14 @@ _KINDS = _standard()
 
 
 def kind_of(table: Table) -> str | None:
-    """The standard gate a table is (h, s, sdg, x, y, z, id, cx, cz), or None."""
+    """The standard gate a table is (h, s, sdg, x, y, z, id, cx, cz), or None
+    (``stabilizer.py:122-147``)."""
     return _KINDS.get((table.k, table.bits.tobytes(), table.sign.tobytes()))
 
 
 def pauli_label(matrix: NDArray[np.complex128]) -> list[tuple[int, int]] | None:
-    """(x, z) bits per qubit of a Pauli-string matrix up to a unit phase (first qubit first)."""
+    """(x, z) bits per qubit of a Pauli-string matrix up to a unit phase (first qubit first)
+    (``stabilizer.py:150-158``)."""
     k = matrix.shape[0].bit_length() - 1
     found = _as_pauli(np.asarray(matrix, dtype=np.complex128), k)
     if found is None or abs(abs(found[2]) - 1) > _TOL:
@@ -159,7 +162,8 @@ class PauliNoise:
 
 
 def pauli_noise(channel: Any) -> PauliNoise | None:
-    """Branches of a mixture channel whose operators are all Pauli strings, else None."""
+    """Branches of a mixture channel whose operators are all Pauli strings, else None
+    (``stabilizer.py:169-184``)."""
     if channel.mixture is None:
         return None
     probs, branches = [], []
@@ -173,7 +177,7 @@ def pauli_noise(channel: Any) -> PauliNoise | None:
 
 
 def gates(ops: Any) -> list[Any]:
-    """Every gate of an operation list, if/else branches included, in order."""
+    """Every gate of an operation list, if/else branches included, in order (``stabilizer.py:446-454``)."""
     out: list[Any] = []
     for op in ops:
         if op.kind == "gate":
@@ -184,7 +188,8 @@ def gates(ops: Any) -> list[Any]:
 
 
 def clifford_problem(circuit: Any, noise: Any = None) -> str | None:
-    """Why the stabilizer engine cannot run ``circuit`` exactly, or None (one gate at a time)."""
+    """Why the stabilizer engine cannot run ``circuit`` exactly, or None, one gate at a time
+    (``stabilizer.py:457-467``)."""
     if circuit.num_qubits > MAX_QUBITS:
         return f"it has {circuit.num_qubits} qubits; the stabilizer engine allows up to {MAX_QUBITS}"
     seen: dict[int, bool] = {}
