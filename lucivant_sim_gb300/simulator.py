@@ -149,11 +149,16 @@ def choose_method(circuit: Any, noise: Any, method: str = "automatic") -> str:
         if problem:
             raise SimulationError(f"the stabilizer method runs Clifford circuits only: {problem}")
         return method
-    if method == "statevector_aer":
-        raise SimulationError("this method needs Qiskit Aer: pip install lucivant-sim[accel]")
     if method == "stabilizer_stim":
-        raise SimulationError("this method needs Stim: pip install lucivant-sim[accel]")
-    if method == "statevector" and (gate_noise or dynamic):
+        if noise is not None and not noise.is_empty():
+            raise SimulationError("stabilizer_stim runs ideal circuits; use 'stabilizer' for Pauli noise")
+        if any(op.kind == "if" for op in circuit.operations):
+            raise SimulationError("stabilizer_stim runs circuits without classical conditions; use 'stabilizer'")
+        problem = clifford_problem(circuit, None)
+        if problem:
+            raise SimulationError(f"the stabilizer methods run Clifford circuits only: {problem}")
+        return method
+    if method in ("statevector", "statevector_aer") and (gate_noise or dynamic):
         raise SimulationError(
             "the statevector method runs ideal circuits without mid-circuit measurement; "
             "use 'density_matrix' or 'trajectories'"
@@ -163,6 +168,23 @@ def choose_method(circuit: Any, noise: Any, method: str = "automatic") -> str:
     if method == "density_matrix" and circuit.num_qubits > MAX_DENSITY_QUBITS:
         raise SimulationError(f"the density-matrix method handles up to {MAX_DENSITY_QUBITS} qubits")
     return method
+
+
+# Orrery's accelerator methods and the package each runs on (``accel.py:45-51``)
+_ACCELERATORS = {"statevector_aer": ("qiskit_aer", "Qiskit Aer"), "stabilizer_stim": ("stim", "Stim")}
+
+
+def refuse_accelerator(method: str) -> None:
+    """Orrery runs ``statevector_aer`` and ``stabilizer_stim`` on another package once the method
+    is chosen and the seed checked (``simulator.py:339-357``); this engine has no path to them.
+    Without the package the refusal is Orrery's own message; with it, the method is refused by
+    name."""
+    module, extra = _ACCELERATORS[method]
+    try:
+        __import__(module)
+    except ImportError as exc:
+        raise SimulationError(f"this method needs {extra}: pip install lucivant-sim[accel]") from exc
+    raise SimulationError(f"the GB300 engine does not drive {extra}; use '{method.split('_')[0]}'")
 
 
 def sample_register(
@@ -292,6 +314,8 @@ def run(
     seed = secrets.randbelow(2**63) if seed is None else int(seed)
     if seed < 0:
         raise ValueError("seed must not be negative")
+    if chosen in _ACCELERATORS:
+        refuse_accelerator(chosen)
     rng = np.random.default_rng(seed)
     prec = engine.precision_code(precision)
     started = time.perf_counter()

@@ -127,3 +127,35 @@ def test_orrery_timings_recorded(cfg):
     for m in (0, 1, 128, 255):
         assert cfg[f"cfg2_inst{m}"]["orrery_seconds"] > 0
     assert math.isfinite(cfg["cfg4_full"]["orrery_run_seconds"])
+
+
+def test_method_choice_is_orreys_for_every_method_name():
+    """``choose_method`` against Orrery's own answers (``tests/golden/methods.json``, made by
+    running Orrery): every method name, including the accelerator names and an unknown one, over
+    Clifford circuits below and at the stabilizer threshold, with a non-Clifford gate, a
+    three-qubit gate, mid-circuit measurement and reset, circuits at and above the
+    density-matrix limits, and noise models with no rules, Pauli channels, readout only and a
+    non-Pauli channel: the same method, or the same exception class and message."""
+    import sys
+
+    from lucivant_sim_gb300 import noise as ns
+    from lucivant_sim_gb300 import simulator
+
+    sys.path.insert(0, str(GOLDEN))
+    try:
+        from make_golden_methods import noise_model
+    finally:
+        sys.path.remove(str(GOLDEN))
+    data = json.loads((GOLDEN / "methods.json").read_text())
+    circuits = {name: ls.parse(src) for name, src in data["programs"].items()}
+    assert len(data["cases"]) >= 500
+    for case in data["cases"]:
+        nm = noise_model(case["noise"], ns)
+        where = (case["program"], case["noise"], case["method"])
+        try:
+            got = {"method": simulator.choose_method(circuits[case["program"]], nm, case["method"])}
+        except Exception as exc:  # noqa: BLE001 - compared with Orrery's record
+            got = {"error": type(exc).__name__, "message": str(exc)}
+        want = {k: case[k] for k in ("method", "error", "message") if k in case and k != "method" or
+                (k == "method" and "error" not in case and k in case)}
+        assert got == want, where

@@ -1026,3 +1026,22 @@ def test_autotuner_cache_is_per_build_and_survives_a_choice_that_no_longer_plans
     monkeypatch.setattr(autotune, "_identity", "build-b")
     assert autotune.shape_key(reg, ops) != key_a
     assert not list(tmp_path.glob("*.tmp"))
+
+
+def test_accelerator_methods_are_refused_as_orrery_refuses_them():
+    """Orrery's opt-in accelerator methods: the method-choice checks come first (a noisy circuit
+    gets the statevector misfit message), then the seed check, then the missing package's
+    message; no device call is made on the way."""
+    bell = 'OPENQASM 3; include "stdgates.inc"; qubit[2] q; bit[2] c; h q[0]; cx q[0], q[1]; c = measure q;'
+    for method, extra, module in (("statevector_aer", "Qiskit Aer", "qiskit_aer"), ("stabilizer_stim", "Stim", "stim")):
+        try:
+            __import__(module)
+        except ImportError:
+            with pytest.raises(ls.SimulationError, match=f"this method needs {extra}: pip install lucivant-sim\\[accel\\]"):
+                ls.run(bell, shots=10, seed=1, method=method)
+        with pytest.raises(ValueError, match="seed must not be negative"):
+            ls.run(bell, shots=10, seed=-1, method=method)
+    with pytest.raises(ls.SimulationError, match="runs ideal circuits without mid-circuit measurement"):
+        ls.run(bell, shots=10, seed=1, method="statevector_aer", noise=NoiseModel.uniform(single=0.01))
+    with pytest.raises(ls.SimulationError, match="stabilizer_stim runs ideal circuits"):
+        ls.run(bell, shots=10, seed=1, method="stabilizer_stim", noise=NoiseModel.uniform(single=0.01))
