@@ -159,3 +159,36 @@ def test_method_choice_is_orreys_for_every_method_name():
         want = {k: case[k] for k in ("method", "error", "message") if k in case and k != "method" or
                 (k == "method" and "error" not in case and k in case)}
         assert got == want, where
+
+
+def test_qasm_reader_is_orreys_on_valid_and_malformed_programs():
+    """The OpenQASM reader against Orrery's own reader (``tests/golden/qasm.json``, made by running
+    Orrery): for programs covering the language (OpenQASM 2 and 3 declarations, every statement
+    kind, gate definitions, modifiers, inputs, physical qubits, ranges, conditions, expressions,
+    comments) the same circuit — digest, sizes, registers, inputs and operation kinds; for
+    malformed programs reaching each of Orrery's error messages the same exception class, message,
+    line and column."""
+    from lucivant_sim_gb300 import qasm
+
+    kind_names = {"gate": "Gate", "measure": "Measure", "reset": "Reset", "barrier": "Barrier",
+                  "if": "IfElse", "gphase": "GlobalPhase"}  # fmt: skip
+    data = json.loads((GOLDEN / "qasm.json").read_text())
+    assert len(data["programs"]) >= 80
+    for rec in data["programs"]:
+        try:
+            c = qasm.parse(rec["source"], rec["params"])
+        except Exception as exc:  # noqa: BLE001 - compared with Orrery's record
+            got = {"error": {"class": type(exc).__name__, "message": str(exc), "line": getattr(exc, "line", None),
+                             "column": getattr(exc, "column", None)}}  # fmt: skip
+        else:
+            got = {"circuit": {
+                "digest": c.digest(),
+                "num_qubits": c.num_qubits,
+                "num_clbits": c.num_clbits,
+                "qregs": [[r.name, r.offset, r.size] for r in c.qregs],
+                "cregs": [[r.name, r.offset, r.size] for r in c.cregs],
+                "inputs": dict(c.inputs),
+                "kinds": [kind_names[op.kind] for op in c.operations],
+            }}  # fmt: skip
+        want = {k: rec[k] for k in ("circuit", "error") if k in rec}
+        assert got == want, rec["name"]
