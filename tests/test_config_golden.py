@@ -192,3 +192,56 @@ def test_qasm_reader_is_orreys_on_valid_and_malformed_programs():
             }}  # fmt: skip
         want = {k: rec[k] for k in ("circuit", "error") if k in rec}
         assert got == want, rec["name"]
+
+
+def test_noise_models_are_orreys():
+    """Noise models against Orrery's own (``tests/golden/noise.*``, made by running Orrery): every
+    channel factory over several parameters gives the same Kraus operators and mixture branches
+    (to 1e-15) and description; the factories refuse the same parameters with the same messages;
+    models with overlapping rules resolve every (gate, qubits) query to the same channel, give the
+    same readout errors, descriptions and digests; calibrations read into the same models."""
+    import sys
+
+    from lucivant_sim_gb300 import noise as ns
+
+    sys.path.insert(0, str(GOLDEN))
+    try:
+        from make_golden_noise import build_channel, build_model
+    finally:
+        sys.path.remove(str(GOLDEN))
+    data = json.loads((GOLDEN / "noise.json").read_text())
+    with np.load(GOLDEN / "noise.npz") as arrays:
+        for i, rec in enumerate(data["channels"]):
+            ch = build_channel(ns, rec["recipe"])
+            where = rec["recipe"]
+            assert [ch.name, ch.num_qubits, ch.describe()] == [rec["name"], rec["num_qubits"], rec["describe"]], where
+            assert bool(getattr(ch, "analytic_depolarizing", False)) == rec["analytic_depolarizing"], where
+            kraus = np.stack([np.asarray(k, dtype=np.complex128) for k in ch.kraus])
+            assert kraus.shape == arrays[f"ch{i}::kraus"].shape, where
+            assert np.max(np.abs(kraus - arrays[f"ch{i}::kraus"])) <= 1e-15, where
+            if rec["mixture"] is None:
+                assert ch.mixture is None, where
+            else:
+                assert [float(p) for p, _m in ch.mixture] == rec["mixture"], where
+                mats = np.stack([np.asarray(m, dtype=np.complex128) for _p, m in ch.mixture])
+                assert np.array_equal(mats, arrays[f"ch{i}::mixture"]), where
+    for rec in data["bad_channels"]:
+        with pytest.raises(Exception) as info:
+            build_channel(ns, rec["recipe"])
+        assert {"class": type(info.value).__name__, "message": str(info.value)} == rec["error"], rec["recipe"]
+    with pytest.raises(ValueError) as info:
+        build_model(ns, [["gate", ["depolarizing", [0.1, 2]], None, [0]]])
+    assert str(info.value) == data["bad_attach"]["message"]
+    for name, rec in data["models"].items():
+        m = build_model(ns, rec["steps"])
+        assert m.describe() == rec["describe"] and m.digest() == rec["digest"], name
+        assert (m.has_gate_errors(), m.is_empty()) == (rec["has_gate_errors"], rec["is_empty"]), name
+        for (gate, qubits), want in zip(data["queries"], rec["gate_error"], strict=True):
+            ch = m.gate_error(gate, tuple(qubits))
+            assert (None if ch is None else ch.describe()) == want, (name, gate, qubits)
+        for q, want in enumerate(rec["readout_error"]):
+            e = m.readout_error(q)
+            assert (None if e is None else [e.p01, e.p10]) == want, (name, q)
+    for rec in data["calibrations"]:
+        m = ns.NoiseModel.from_calibration(rec["calibration"])
+        assert (m.describe(), m.digest(), m.source) == (rec["describe"], rec["digest"], rec["source"])
