@@ -245,3 +245,41 @@ def test_noise_models_are_orreys():
     for rec in data["calibrations"]:
         m = ns.NoiseModel.from_calibration(rec["calibration"])
         assert (m.describe(), m.digest(), m.source) == (rec["describe"], rec["digest"], rec["source"])
+
+
+def test_gates_results_and_command_line_are_orreys(monkeypatch):
+    """Orrery's public surface that needs no simulation (``tests/golden/api.*``, made by running
+    Orrery): every gate's matrix at seeded parameters (to 1e-15), arity and canonical name; matrix
+    powers; the ``Result`` record of synthetic results (fingerprint, counts digest, dictionary form,
+    frequencies, most frequent outcome); and the command line's help, version and argument errors
+    (output and exit code, at a fixed terminal width)."""
+    import contextlib
+    import io
+
+    from lucivant_sim_gb300 import cli, gates
+    from lucivant_sim_gb300.simulator import Result
+
+    data = json.loads((GOLDEN / "api.json").read_text())
+    with np.load(GOLDEN / "api.npz") as arrays:
+        assert sorted(gates.GATES) == [g["name"] for g in data["gates"]]
+        for g in data["gates"]:
+            m = np.asarray(gates.gate_matrix(g["name"], tuple(g["params"])), dtype=np.complex128)
+            assert np.max(np.abs(m - arrays[f"gate::{g['name']}"])) <= 1e-15, g["name"]
+            assert gates.GATES[g["name"]].qubits == g["qubits"] and gates.canonical_name(g["name"]) == g["canonical"]
+        for i, p in enumerate(data["powers"]):
+            u = gates.gate_matrix(p["name"], tuple([0.7] * gates.GATES[p["name"]].params))
+            assert np.max(np.abs(gates.matrix_power(u, p["k"]) - arrays[f"power::{i}"])) <= 1e-14, p
+    for rec in data["results"]:
+        r = Result(**rec["fields"])
+        assert (r.fingerprint, r.counts_digest, r.frequencies(), r.most_frequent()) == (
+            rec["fingerprint"], rec["counts_digest"], rec["frequencies"], rec["most_frequent"])
+        assert json.loads(json.dumps(r.to_dict())) == rec["to_dict"]
+    monkeypatch.setenv("COLUMNS", data["columns"])
+    for rec in data["cli"]:
+        out, err = io.StringIO(), io.StringIO()
+        with contextlib.redirect_stdout(out), contextlib.redirect_stderr(err):
+            try:
+                code = cli.main(rec["argv"])
+            except SystemExit as exc:
+                code = exc.code
+        assert (code, out.getvalue(), err.getvalue()) == (rec["code"], rec["stdout"], rec["stderr"]), rec["argv"]
