@@ -7,7 +7,8 @@ Run from the repository root, in a checkout where Orrery's sources are readable:
     python tests/golden/make_golden_qasm.py /path/to/lucivant-sim/src
 
 It writes ``tests/golden/qasm.json``: per program the source, the ``input`` values given, and
-Orrery's answer: the circuit (digest, qubit and bit counts, registers, inputs, operation kinds),
+Orrery's answer: the circuit (digest, qubit and bit counts, registers, inputs, operation kinds,
+whether it is dynamic, its final measurements, operation counts, bit-string formatting),
 or the exception's class, message, line and column. The tests never need Orrery.
 """
 
@@ -146,6 +147,10 @@ def main(ref_src: str) -> None:
                 "cregs": [[r.name, r.offset, r.size] for r in c.cregs],
                 "inputs": dict(c.inputs),
                 "kinds": [type(op).__name__ for op in c.operations],
+                "is_dynamic": c.is_dynamic(),
+                "final_measurements": [list(p) for p in c.final_measurements()],
+                "count_ops": c.count_ops(),
+                "format_bits": [c.format_bits(b) for b in (0, 1, 5, (1 << c.num_clbits) - 1)] if c.num_clbits else [],
             }
         except Exception as exc:  # noqa: BLE001 - the class, message and position are the record
             rec["error"] = {"class": type(exc).__name__, "message": str(exc), "line": getattr(exc, "line", None),

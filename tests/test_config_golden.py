@@ -165,7 +165,8 @@ def test_qasm_reader_is_orreys_on_valid_and_malformed_programs():
     """The OpenQASM reader against Orrery's own reader (``tests/golden/qasm.json``, made by running
     Orrery): for programs covering the language (OpenQASM 2 and 3 declarations, every statement
     kind, gate definitions, modifiers, inputs, physical qubits, ranges, conditions, expressions,
-    comments) the same circuit — digest, sizes, registers, inputs and operation kinds; for
+    comments) the same circuit — digest, sizes, registers, inputs, operation kinds, whether it is
+    dynamic, final measurements, operation counts and bit-string formatting; for
     malformed programs reaching each of Orrery's error messages the same exception class, message,
     line and column."""
     from lucivant_sim_gb300 import qasm
@@ -189,6 +190,10 @@ def test_qasm_reader_is_orreys_on_valid_and_malformed_programs():
                 "cregs": [[r.name, r.offset, r.size] for r in c.cregs],
                 "inputs": dict(c.inputs),
                 "kinds": [kind_names[op.kind] for op in c.operations],
+                "is_dynamic": c.is_dynamic(),
+                "final_measurements": [list(p) for p in c.final_measurements()],
+                "count_ops": c.count_ops(),
+                "format_bits": [c.format_bits(b) for b in (0, 1, 5, (1 << c.num_clbits) - 1)] if c.num_clbits else [],
             }}  # fmt: skip
         want = {k: rec[k] for k in ("circuit", "error") if k in rec}
         assert got == want, rec["name"]
