@@ -288,3 +288,48 @@ def test_gates_results_and_command_line_are_orreys(monkeypatch):
             except SystemExit as exc:
                 code = exc.code
         assert (code, out.getvalue(), err.getvalue()) == (rec["code"], rec["stdout"], rec["stderr"]), rec["argv"]
+
+
+def _sim_cases():
+    import sys
+
+    from lucivant_sim_gb300 import noise as ns
+
+    sys.path.insert(0, str(GOLDEN))
+    try:
+        from make_golden_noise import build_model
+    finally:
+        sys.path.remove(str(GOLDEN))
+    data = json.loads((GOLDEN / "sim.json").read_text())
+    arrays = dict(np.load(GOLDEN / "sim.npz"))
+    for case in data["cases"]:
+        steps = data["noises"][case["noise"]]
+        yield case, (None if steps is None else build_model(ns, steps)), arrays
+
+
+def test_oracle_matches_orreys_public_functions_on_random_programs():
+    """The oracle against Orrery's public functions on seeded random programs over every gate name
+    and several measurement layouts (``tests/golden/sim.*``, made by running Orrery): identical
+    counts for the same seed, probabilities and outcome probabilities (readout included),
+    expectations and final states within 1e-12."""
+    for case, nm, arrays in _sim_cases():
+        c = ls.parse(case["qasm"])
+        counts, method, _ = dense.run_counts(c, 3000, case["seed"], nm)
+        assert (method, counts) == (case["method"], case["counts"]), case["name"]
+        probs = dense.probabilities_array(c, nm)
+        n = c.num_qubits
+        want = case["probabilities"]
+        got = {format(i, f"0{n}b"): float(p) for i, p in enumerate(probs) if p > 1e-12}
+        assert set(got) == set(want), case["name"]
+        assert max(abs(got[k] - want[k]) for k in want) < 1e-12, case["name"]
+        if case["outcome_probabilities"]:
+            op = dense.outcome_probabilities(c, nm)
+            assert set(op) == set(case["outcome_probabilities"]), case["name"]
+            assert max(abs(op[k] - v) for k, v in case["outcome_probabilities"].items()) < 1e-12, case["name"]
+        for obs, value in zip(case["observables"], case["expectations"], strict=True):
+            assert abs(dense.expectation(c, obs, nm) - value) < 1e-12, (case["name"], obs)
+        if f"{case['name']}::statevector" in arrays:
+            assert np.max(np.abs(dense.evolve_sv(c) - arrays[f"{case['name']}::statevector"])) < 1e-12
+        else:
+            rho = dense.evolve_dm(c, nm).reshape(1 << n, 1 << n)
+            assert np.max(np.abs(rho - arrays[f"{case['name']}::density_matrix"])) < 1e-12
