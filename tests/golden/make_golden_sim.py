@@ -12,7 +12,9 @@ the tests never need Orrery.
 
 The programs draw gates from every one- and two-qubit gate name, several three-qubit ones and
 modifiers, and measure into two classical registers in layouts Orrery allows: a qubit measured
-into two bits, a bit written twice (the later measurement wins), bits left unmeasured.
+into two bits, a bit written twice (the later measurement wins), bits left unmeasured. Run-only
+cases add programs with mid-circuit measurement, conditions and reset (Orrery's trajectories) and
+random Clifford layers over every Clifford gate name at 12 to 16 qubits (its stabilizer engine).
 """
 
 from __future__ import annotations
@@ -93,6 +95,60 @@ CASES = [
     ("dm3_all_mixed", 3, 15, 10, "all", "mixed", 20),
 ]
 
+CLIFFORD_ONE = ["h", "s", "sdg", "x", "y", "z", "sx", "sxdg", "id"]
+CLIFFORD_TWO = ["cx", "cy", "cz", "swap", "iswap", "ecr", "dcx"]
+
+
+def dynamic_program(n: int, rounds: int, seed: int) -> str:
+    """Rounds of random one- and two-qubit gates, a mid-circuit measurement, a condition on it
+    (a gate, or an if/else block) and a reset; all qubits measured at the end."""
+    rng = np.random.default_rng(seed)
+    lines = ["OPENQASM 3.0;", 'include "stdgates.inc";', f"qubit[{n}] q;", f"bit[{n}] c;", "bit[2] m;"]
+    for r in range(rounds):
+        for q in range(n):
+            ps = ", ".join(repr(float(v)) for v in rng.uniform(-3.2, 3.2, size=3))
+            lines.append(f"u3({ps}) q[{q}];")
+        a = int(rng.integers(n - 1))
+        lines.append(f"cx q[{a}], q[{a + 1}];")
+        mq = int(rng.integers(n))
+        lines.append(f"m[{r % 2}] = measure q[{mq}];")
+        t = (mq + 1) % n
+        if r % 2:
+            lines.append(f"if (m[{r % 2}] == 1) {{ x q[{t}]; h q[{(t + 1) % n}]; }} else {{ ry(0.7) q[{t}]; }}")
+        else:
+            lines.append(f"if (m == {int(rng.integers(4))}) z q[{t}];")
+        lines.append(f"reset q[{int(rng.integers(n))}];")
+    lines.append("c = measure q;")
+    return "\n".join(lines) + "\n"
+
+
+def clifford_program(n: int, layers: int, seed: int) -> str:
+    """Random Clifford layers on ``n`` qubits (every Clifford gate name), measured into one register
+    in a permuted order, a few qubits left unmeasured."""
+    rng = np.random.default_rng(seed)
+    lines = ["OPENQASM 3.0;", 'include "stdgates.inc";', f"qubit[{n}] q;", f"bit[{n - 2}] c;"]
+    for _ in range(layers):
+        for q in range(n):
+            lines.append(f"{CLIFFORD_ONE[rng.integers(len(CLIFFORD_ONE))]} q[{q}];")
+        order = [int(v) for v in rng.permutation(n)]
+        for i in range(0, n - 1, 2):
+            lines.append(f"{CLIFFORD_TWO[rng.integers(len(CLIFFORD_TWO))]} q[{order[i]}], q[{order[i + 1]}];")
+    for i, q in enumerate(int(v) for v in rng.permutation(n)[: n - 2]):
+        lines.append(f"c[{i}] = measure q[{q}];")
+    return "\n".join(lines) + "\n"
+
+
+# run-only cases (Orrery's expectations and probabilities refuse dynamic circuits):
+# (name, program kind, qubits, size, program seed, noise, run seed, shots)
+RUN_CASES = [
+    ("traj5_ideal", "dynamic", 5, 3, 31, "none", 41, 400),
+    ("traj6_uniform", "dynamic", 6, 3, 32, "uniform", 42, 300),
+    ("traj4_mixed", "dynamic", 4, 4, 33, "mixed", 43, 300),
+    ("stab14_ideal", "clifford", 14, 6, 34, "none", 44, 500),
+    ("stab16_uniform", "clifford", 16, 5, 35, "uniform", 45, 500),
+    ("stab12_readout", "clifford", 12, 8, 36, "readout_only", 46, 500),
+]
+
 OBSERVABLES = [lambda n: "Z" * n, lambda n: {"X" + "I" * (n - 1): 0.5, "I" * (n - 2) + "YZ": -1.25, "Z" * n: 0.75}]
 
 
@@ -121,9 +177,18 @@ def main(ref_src: str) -> None:
         else:
             arrays[f"{name}::density_matrix"] = ls.density_matrix(src, nm)
         cases.append(rec)
+    run_cases = []
+    for name, kind, n, size, pseed, noise_name, seed, shots in RUN_CASES:
+        src = dynamic_program(n, size, pseed) if kind == "dynamic" else clifford_program(n, size, pseed)
+        steps = NOISES[noise_name]
+        nm = None if steps is None else build_model(ns, steps)
+        r = ls.run(src, shots=shots, seed=seed, noise=nm)
+        run_cases.append({"name": name, "qasm": src, "noise": noise_name, "seed": seed, "shots": shots,
+                          "method": r.method, "counts": r.counts, "circuit_digest": r.circuit_digest,
+                          "fingerprint_noise": r.noise_digest, "fingerprint": r.fingerprint})  # fmt: skip
     np.savez_compressed(HERE / "sim.npz", **arrays)
-    (HERE / "sim.json").write_text(json.dumps({"reference_version": ls.__version__, "noises": NOISES, "cases": cases},
-                                              indent=1, sort_keys=True))  # fmt: skip
+    (HERE / "sim.json").write_text(json.dumps({"reference_version": ls.__version__, "noises": NOISES, "cases": cases,
+                                               "run_cases": run_cases}, indent=1, sort_keys=True))  # fmt: skip
     print("wrote", HERE / "sim.json", HERE / "sim.npz", len(cases), "cases")
 
 

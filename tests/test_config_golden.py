@@ -333,3 +333,26 @@ def test_oracle_matches_orreys_public_functions_on_random_programs():
         else:
             rho = dense.evolve_dm(c, nm).reshape(1 << n, 1 << n)
             assert np.max(np.abs(rho - arrays[f"{case['name']}::density_matrix"])) < 1e-12
+
+
+def test_oracle_matches_orreys_runs_of_dynamic_and_clifford_programs():
+    """The oracle against Orrery's ``run`` on seeded random programs with mid-circuit measurement,
+    conditions and reset (trajectories, Orrery's draw order) and on random Clifford layers over
+    every Clifford gate name at 12 to 16 qubits (the stabilizer engine): the same method and
+    identical counts for the same seed."""
+    import sys
+
+    from lucivant_sim_gb300 import noise as ns
+
+    sys.path.insert(0, str(GOLDEN))
+    try:
+        from make_golden_noise import build_model
+    finally:
+        sys.path.remove(str(GOLDEN))
+    data = json.loads((GOLDEN / "sim.json").read_text())
+    assert len(data["run_cases"]) >= 6
+    for case in data["run_cases"]:
+        steps = data["noises"][case["noise"]]
+        nm = None if steps is None else build_model(ns, steps)
+        counts, method, _ = dense.run_counts(ls.parse(case["qasm"]), case["shots"], case["seed"], nm)
+        assert (method, counts) == (case["method"], case["counts"]), case["name"]

@@ -2,7 +2,9 @@
 gate name, several measurement layouts and noise models (``tests/golden/sim.*``, made by running
 Orrery): the same method and counts for the same seed (unless a shot lies on a CDF boundary),
 probabilities, outcome probabilities (readout included), expectations and final states within
-1e-12, all through the engine's complex128 path."""
+1e-12, all through the engine's complex128 path; and for programs with mid-circuit measurement,
+conditions and reset (trajectories) and random Clifford layers (the stabilizer engine), the same
+method and counts."""
 
 from __future__ import annotations
 
@@ -62,3 +64,23 @@ def test_public_functions_match_orrery(index):
         assert np.max(np.abs(ls.statevector(src) - arrays[f"{name}::statevector"])) < TOL
     else:
         assert np.max(np.abs(ls.density_matrix(src, noise) - arrays[f"{name}::density_matrix"])) < TOL
+
+
+RUN_CASES = json.loads((GOLDEN / "sim.json").read_text())["run_cases"]
+
+
+@pytest.mark.parametrize("index", range(len(RUN_CASES)), ids=[c["name"] for c in RUN_CASES])
+def test_runs_of_dynamic_and_clifford_programs_match_orrery(index):
+    case = RUN_CASES[index]
+    sys.path.insert(0, str(GOLDEN))
+    try:
+        from make_golden_noise import build_model
+    finally:
+        sys.path.remove(str(GOLDEN))
+    steps = json.loads((GOLDEN / "sim.json").read_text())["noises"][case["noise"]]
+    noise = None if steps is None else build_model(ns, steps)
+    r = ls.run(case["qasm"], shots=case["shots"], seed=case["seed"], noise=noise)
+    assert r.method == case["method"]
+    assert r.circuit_digest == case["circuit_digest"] and r.noise_digest == case["fingerprint_noise"]
+    near = r.report.get("near_threshold", 0) + r.report.get("near_boundary", 0)
+    assert r.counts == case["counts"] or near > 0
