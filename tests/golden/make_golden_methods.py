@@ -6,7 +6,7 @@ Run from the repository root, in a checkout where Orrery's sources are readable:
     python tests/golden/make_golden_methods.py /path/to/lucivant-sim/src
 
 It writes ``tests/golden/methods.json``: per case the OpenQASM text, the noise model's name (built
-the same way on both sides by ``noise_model``), the requested method and Orrery's answer (the
+the same way on both sides by ``recipes.noise_model``), the requested method and Orrery's answer (the
 chosen method, or the exception's class name and message). The tests never need Orrery.
 """
 
@@ -18,6 +18,9 @@ from pathlib import Path
 
 sys.dont_write_bytecode = True
 HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+from recipes import noise_model  # noqa: E402
 
 METHODS = ("automatic", "statevector", "density_matrix", "trajectories", "stabilizer", "statevector_aer",
            "stabilizer_stim", "no_such_method")  # fmt: skip
@@ -50,24 +53,6 @@ PROGRAMS = {
 }
 
 NOISES = ("none", "empty", "pauli", "readout_only", "damping_on_h", "depolarizing_on_cx")
-
-
-def noise_model(name: str, ns) -> object:
-    """The named noise model, built with the NoiseModel class and channel factories of ``ns``
-    (Orrery's module or the engine's, which take the same calls)."""
-    if name == "none":
-        return None
-    if name == "empty":
-        return ns.NoiseModel()
-    if name == "pauli":
-        return ns.NoiseModel.uniform(single=1e-3, two=1e-2, readout=2e-2)
-    if name == "readout_only":
-        return ns.NoiseModel.uniform(readout=3e-2)
-    if name == "damping_on_h":
-        return ns.NoiseModel().add_gate_error(ns.amplitude_damping(0.1), gates="h")
-    if name == "depolarizing_on_cx":
-        return ns.NoiseModel().add_gate_error(ns.depolarizing(0.02, 2), gates="cx")
-    raise KeyError(name)
 
 
 def main(ref_src: str) -> None:

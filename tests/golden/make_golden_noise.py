@@ -8,8 +8,8 @@ Run from the repository root, in a checkout where Orrery's sources are readable:
     python tests/golden/make_golden_noise.py /path/to/lucivant-sim/src
 
 It writes ``tests/golden/noise.json`` and ``tests/golden/noise.npz``. The recipes are data
-(``CHANNELS``, ``MODELS``, ``CALIBRATIONS``) applied to either module by ``build_channel`` and
-``build_model``, so the tests build the same objects with the engine's module.
+(``CHANNELS``, ``MODELS``, ``CALIBRATIONS``) applied to either module by ``recipes.build_channel``
+and ``recipes.build_model``, so the tests build the same objects with the engine's module.
 """
 
 from __future__ import annotations
@@ -22,6 +22,9 @@ import numpy as np
 
 sys.dont_write_bytecode = True
 HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+from recipes import build_channel, build_model  # noqa: E402
 
 # (factory, args) — each is called as getattr(module, factory)(*args)
 CHANNELS = [
@@ -84,28 +87,6 @@ CALIBRATIONS = [
     {"calibration": {"device": "wrapped", "readout_error": 0.05, "qubits": [{"qubit": 1, "single_qubit_error": 0.002}]}},
     {},
 ]  # fmt: skip
-
-
-def build_channel(ns, recipe):
-    name, args = recipe
-    return getattr(ns, name)(*args)
-
-
-def build_model(ns, steps):
-    model = ns.NoiseModel()
-    for step in steps:
-        if step[0] == "uniform":
-            fresh = ns.NoiseModel.uniform(single=step[1], two=step[2], readout=step[3])
-            model.rules.extend(fresh.rules)
-            model.readout.update(fresh.readout)
-            model.source = fresh.source
-        elif step[0] == "gate":
-            model.add_gate_error(build_channel(ns, step[1]), gates=step[2], qubits=step[3])
-        else:
-            value = step[1]
-            err = ns.ReadoutError(*value) if isinstance(value, list) else value
-            model.add_readout_error(err, qubits=step[2])
-    return model
 
 
 def channel_record(ch, arrays: dict, key: str) -> dict:

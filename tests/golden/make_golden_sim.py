@@ -157,7 +157,7 @@ def main(ref_src: str) -> None:
     sys.path.insert(0, str(HERE))
     import lucivant_sim as ls
     from lucivant_sim import noise as ns
-    from make_golden_noise import build_model
+    from recipes import build_model
 
     arrays: dict[str, np.ndarray] = {}
     cases = []

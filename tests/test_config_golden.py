@@ -143,7 +143,7 @@ def test_method_choice_is_orreys_for_every_method_name():
 
     sys.path.insert(0, str(GOLDEN))
     try:
-        from make_golden_methods import noise_model
+        from recipes import noise_model
     finally:
         sys.path.remove(str(GOLDEN))
     data = json.loads((GOLDEN / "methods.json").read_text())
@@ -211,7 +211,7 @@ def test_noise_models_are_orreys():
 
     sys.path.insert(0, str(GOLDEN))
     try:
-        from make_golden_noise import build_channel, build_model
+        from recipes import build_channel, build_model
     finally:
         sys.path.remove(str(GOLDEN))
     data = json.loads((GOLDEN / "noise.json").read_text())
@@ -297,7 +297,7 @@ def _sim_cases():
 
     sys.path.insert(0, str(GOLDEN))
     try:
-        from make_golden_noise import build_model
+        from recipes import build_model
     finally:
         sys.path.remove(str(GOLDEN))
     data = json.loads((GOLDEN / "sim.json").read_text())
@@ -346,7 +346,7 @@ def test_oracle_matches_orreys_runs_of_dynamic_and_clifford_programs():
 
     sys.path.insert(0, str(GOLDEN))
     try:
-        from make_golden_noise import build_model
+        from recipes import build_model
     finally:
         sys.path.remove(str(GOLDEN))
     data = json.loads((GOLDEN / "sim.json").read_text())

@@ -27,7 +27,7 @@ TOL = 1e-12
 def _cases():
     sys.path.insert(0, str(GOLDEN))
     try:
-        from make_golden_noise import build_model
+        from recipes import build_model
     finally:
         sys.path.remove(str(GOLDEN))
     data = json.loads((GOLDEN / "sim.json").read_text())
@@ -74,7 +74,7 @@ def test_runs_of_dynamic_and_clifford_programs_match_orrery(index):
     case = RUN_CASES[index]
     sys.path.insert(0, str(GOLDEN))
     try:
-        from make_golden_noise import build_model
+        from recipes import build_model
     finally:
         sys.path.remove(str(GOLDEN))
     steps = json.loads((GOLDEN / "sim.json").read_text())["noises"][case["noise"]]
